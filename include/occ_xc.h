@@ -1,0 +1,141 @@
+/*
+ * occ_xc.h -- C ABI of the GB300 exchange-correlation (XC) build.
+ *
+ * A drop-in for the XC part of OCC's Kohn-Sham method: the molecule, its
+ * AOBasis and a density matrix go in; E_xc and the V_xc matrix come out.
+ * Plain C types only (no C++ or CUDA types), so any host language can bind
+ * it (see INTEGRATION.md for the C++ and Python bindings).
+ *
+ * Conventions (those of OCC):
+ *   - coordinates in Bohr;
+ *   - shell coefficients as OCC's gto::Shell holds them after
+ *     Shell::incorporate_shell_norm (occ_xc_normalize_shell does that step);
+ *   - AO order: shells in the given order, Cartesian CCA order within a
+ *     Cartesian shell, m = -l..l within a pure shell;
+ *   - matrices nbf x nbf, column-major (Eigen's default), D = OCC's mo.D
+ *     (C_occ C_occ^T for a restricted wavefunction; the build uses 2 D);
+ *   - V receives V_xc = -K of DFT::compute_JK, and *exc E_xc.
+ * Every entry point returns OCC_XC_OK (0) or a negative status; the message
+ * is available from occ_xc_last_error().  No C++ exception crosses the ABI.
+ * Calls on one context are serialised internally; different contexts may be
+ * used from different threads.
+ */
+#ifndef OCC_XC_H
+#define OCC_XC_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  OCC_XC_OK = 0,
+  OCC_XC_ERR_ARG = -1,      /* invalid argument */
+  OCC_XC_ERR_CUDA = -2,     /* CUDA runtime error */
+  OCC_XC_ERR_METHOD = -3,   /* unknown or unsupported functional */
+  OCC_XC_ERR_NOMEM = -4,    /* device memory / admission budget exhausted */
+  OCC_XC_ERR_TIMEOUT = -5,  /* a bounded device wait gave up */
+  OCC_XC_ERR_BUSY = -6,     /* request queue full */
+  OCC_XC_ERR_INTERNAL = -7,
+};
+
+enum {
+  OCC_XC_FP64 = 0,  /* plain path: every operation in FP64 */
+  OCC_XC_MIXED = 1, /* contractions in 3xTF32 on tcgen05 tensor cores with FP32
+                       accumulation; functionals, cross-block sums and the final
+                       symmetrisation in FP64 */
+};
+
+typedef struct occ_xc_context occ_xc_context;
+typedef struct occ_xc_molecule occ_xc_molecule;
+
+/* Mirrors occ::numint::GridSettings (include/occ/numint/grid_settings.h:81-95). */
+typedef struct {
+  int max_angular_points;             /* 302 */
+  int min_angular_points;             /* 110 */
+  int radial_points;                  /* 50 (not used by the LMG radial grid) */
+  double radial_precision;            /* 1e-12 */
+  int reduced_first_row_element_grid; /* 1 */
+  int treutler_alrichs_adjustment;    /* 1 */
+  int pruning_scheme;                 /* 1 = NWChem, 0 = none */
+} occ_xc_grid_settings;
+
+/* Build knobs: DFT::set_xc_screening_threshold (include/occ/dft/dft.h:590),
+ * the density threshold (dft.h:760) and the Morton leaf sizes
+ * (include/occ/numint/spatial_grid_hierarchy.h:26-30). */
+typedef struct {
+  double xc_screening_threshold; /* 1e-10 */
+  double density_threshold;      /* 1e-10 */
+  int leaf_target;               /* 128 */
+  int leaf_min;                  /* 32 */
+  int leaf_max;                  /* 256 */
+} occ_xc_build_settings;
+
+typedef struct {
+  int nbf, natoms, nshells, deriv;
+  long npoints, nleaves;
+  double flops_per_build;    /* 4 * sum_b n_b * m_b^2 (useful contraction FLOPs) */
+  double device_bytes;       /* resident device memory held by the molecule */
+  double workspace_bytes;    /* per-build workspace (FP64 path) */
+} occ_xc_molecule_info;
+
+void occ_xc_default_grid_settings(occ_xc_grid_settings *out);
+void occ_xc_default_build_settings(occ_xc_build_settings *out);
+
+/* Replaces Shell::incorporate_shell_norm (src/gto/shell.cpp:180-186):
+ * scales coefs[nprim] in place. */
+int occ_xc_normalize_shell(int l, int nprim, const double *exps, double *coefs);
+
+/* Replaces MolecularGrid(basis, settings).get_molecular_grid_points()
+ * (src/numint/molecular_grid.cpp:11-140): host-only, needs no device.
+ * Call with points == NULL to get *npoints; then with buffers of that size:
+ * points[3*npoints] (x,y,z per point, Bohr), weights[npoints]. */
+int occ_xc_molecular_grid(int natoms, const int *atomic_numbers, const double *xyz_bohr,
+                          int nshells, const int *shell_l, const int *shell_atom,
+                          const int *shell_nprim, const double *exponents,
+                          const double *coefficients, int pure, const occ_xc_grid_settings *grid,
+                          long *npoints, double *points, double *weights);
+
+/* Context: one CUDA device, one stream.  Replaces nothing in OCC (OCC has
+ * no device state). */
+int occ_xc_context_create(int device, occ_xc_context **out);
+void occ_xc_context_destroy(occ_xc_context *ctx);
+const char *occ_xc_last_error(const occ_xc_context *ctx);
+
+/* Replaces DFT::DFT(method, basis, grid_settings) (include/occ/dft/dft.h:39,
+ * src/dft/dft.cpp:19-35) for the XC part: builds the molecular grid
+ * (MolecularGrid, src/numint/molecular_grid.cpp:11-256), the Morton leaves
+ * and screening lists, and keeps them resident on the device.
+ * method: OCC method name ("lda", "svwn5", "pbe", "blyp", "b3lyp", ...).
+ * grid/build settings may be NULL for OCC's defaults. */
+int occ_xc_molecule_create(occ_xc_context *ctx, int natoms, const int *atomic_numbers,
+                           const double *xyz_bohr, int nshells, const int *shell_l,
+                           const int *shell_atom, const int *shell_nprim,
+                           const double *exponents, const double *coefficients, int pure,
+                           const char *method, const occ_xc_grid_settings *grid,
+                           const occ_xc_build_settings *build, occ_xc_molecule **out);
+void occ_xc_molecule_destroy(occ_xc_molecule *mol);
+int occ_xc_molecule_info_get(const occ_xc_molecule *mol, occ_xc_molecule_info *out);
+
+/* Copies the molecular grid out in OCC's layout (atom blocks in atom order,
+ * MolecularGridPoints, src/numint/molecular_grid_points.cpp:15-50):
+ * points[3*npoints] (x,y,z per point), weights[npoints]. */
+int occ_xc_molecule_grid(const occ_xc_molecule *mol, double *points, double *weights);
+
+/* Replaces DFT::compute_vxc(mo) for a restricted wavefunction
+ * (include/occ/dft/dft.h:395-429) together with
+ * DFT::exchange_correlation_energy() (dft.h:83).  Host buffers; blocking.
+ * nelec_out (may be NULL) receives the integrated density. */
+int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D,
+                       int precision, double *V, double *exc, double *nelec_out);
+
+/* Same build on device buffers, asynchronous on `stream` (a cudaStream_t, or
+ * NULL for the context's stream).  d_exc2 receives {E_xc, integrated density}. */
+int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
+                              int precision, double *d_V, double *d_exc2, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCC_XC_H */

@@ -1,0 +1,21 @@
+"""GB300-native exchange-correlation build for OCC's Kohn-Sham method.
+
+Python mirror of the reference's XC call surface (occpy's Molecule, AOBasis,
+DFT; src/python/dft_bindings.cpp:79-118), implemented over the C ABI in
+include/occ_xc.h.  Every compute call runs the CUDA library; there is no CPU
+path.
+"""
+from .xc import (  # noqa: F401
+    FP64,
+    MIXED,
+    AOBasis,
+    Atom,
+    BuildSettings,
+    DFT,
+    GridSettings,
+    Molecule,
+    Shell,
+    XCError,
+    library,
+    library_path,
+)

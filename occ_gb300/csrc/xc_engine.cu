@@ -1,0 +1,553 @@
+// Engine and C ABI of the GB300 XC build (include/occ_xc.h).
+//
+// occ_xc_molecule_create does OCC's set-up (grid, leaves, screening) once on
+// the host and uploads the result; occ_xc_compute_vxc runs the per-iteration
+// build on the device.  All device memory of a molecule is allocated at
+// creation so that a build allocates nothing.
+#include <algorithm>
+#include <cctype>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/occ_xc.h"
+#include "host/gto_eval.h"
+#include "host/xc_host.hpp"
+#include "xc_device.cuh"
+#include "xc_engine.hpp"
+
+namespace occx {
+
+void fill_sph_table(double *out) {
+  for (int l = 0; l <= kMaxL; l++) {
+    const std::vector<double> &T = spherical_transform(l);
+    std::copy(T.begin(), T.end(), out + sph_offset(l));
+  }
+}
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess)
+    throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// OCC method names -> functional components (share/methods/dft_methods.json,
+// src/dft/dft_method.cpp:14-37, 161-227).  Component scale factors are not
+// applied, as in OCC's DensityFunctional::evaluate.
+FuncSet parse_method(const std::string &method_in) {
+  std::string method;
+  for (char c : method_in)
+    method.push_back(static_cast<char>(std::tolower(static_cast<unsigned char>(c))));
+  std::istringstream ss(method);
+  std::string tok;
+  FuncSet fs{};
+  auto add = [&](int id) {
+    if (fs.n >= kMaxFuncs)
+      throw MethodError("too many functional components");
+    fs.id[fs.n] = id;
+    fs.coef[fs.n] = 1.0;
+    fs.n++;
+  };
+  while (ss >> tok) {
+    if (!tok.empty() && tok[0] == 'u')
+      throw MethodError("unrestricted (spin-polarised) XC is not supported: " + tok);
+    if (tok == "lda" || tok == "svwn" || tok == "lsda") {
+      add(kLdaX);
+      add(kLdaCVwn3);
+    } else if (tok == "svwn5") {
+      add(kLdaX);
+      add(kLdaCVwn);
+    } else if (tok == "pbe" || tok == "pbepbe" || tok == "pbe0" || tok == "pbe1pbe") {
+      add(kGgaXPbe);
+      add(kGgaCPbe);
+    } else if (tok == "blyp") {
+      add(kGgaXB88);
+      add(kGgaCLyp);
+    } else if (tok == "bpbe") {
+      add(kGgaXB88);
+      add(kGgaCPbe);
+    } else if (tok == "b3lyp") {
+      add(kHybB3lyp);
+    } else if (tok == "b3lyp5") {
+      add(kHybB3lyp5);
+    } else if (tok == "lda_x" || tok == "xc_lda_x") {
+      add(kLdaX);
+    } else if (tok == "lda_c_vwn" || tok == "xc_lda_c_vwn") {
+      add(kLdaCVwn);
+    } else if (tok == "lda_c_vwn_rpa" || tok == "xc_lda_c_vwn_rpa") {
+      add(kLdaCVwnRpa);
+    } else if (tok == "lda_c_vwn_3" || tok == "xc_lda_c_vwn_3") {
+      add(kLdaCVwn3);
+    } else if (tok == "gga_x_pbe" || tok == "xc_gga_x_pbe") {
+      add(kGgaXPbe);
+    } else if (tok == "gga_c_pbe" || tok == "xc_gga_c_pbe") {
+      add(kGgaCPbe);
+    } else if (tok == "gga_x_b88" || tok == "xc_gga_x_b88") {
+      add(kGgaXB88);
+    } else if (tok == "gga_c_lyp" || tok == "xc_gga_c_lyp") {
+      add(kGgaCLyp);
+    } else {
+      throw MethodError("unknown or unsupported functional: " + tok);
+    }
+  }
+  if (fs.n == 0)
+    throw MethodError("empty method string");
+  return fs;
+}
+
+template <typename T> static T *dev_upload(const std::vector<T> &h, size_t &bytes) {
+  T *d = nullptr;
+  size_t n = std::max<size_t>(h.size(), 1);
+  cuda_check(cudaMalloc(&d, n * sizeof(T)), "cudaMalloc");
+  if (!h.empty())
+    cuda_check(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice),
+               "cudaMemcpy H2D");
+  bytes += n * sizeof(T);
+  return d;
+}
+
+Molecule::~Molecule() {
+  for (void *p : allocations)
+    cudaFree(p);
+}
+
+void *Molecule::alloc(size_t bytes) {
+  void *p = nullptr;
+  cuda_check(cudaMalloc(&p, std::max<size_t>(bytes, 16)), "cudaMalloc");
+  allocations.push_back(p);
+  device_bytes += static_cast<double>(bytes);
+  return p;
+}
+
+static size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+void Molecule::build_plan() {
+  morton_leaves(grid, bs, plan);
+  screen_leaves(basis, bs, plan);
+  const int ncomp = deriv ? 4 : 1;
+  leaves.clear();
+  leaf_sh.clear();
+  leaf_ao.clear();
+  slabs.clear();
+  tiles.clear();
+  ws_elems = 0;
+  flops = 0.0;
+  for (long b = 0; b < plan.nleaves(); b++) {
+    const int m = plan.leaf_nbf[b];
+    if (m == 0)
+      continue; // no significant shell: the leaf contributes nothing (dft.h:321-322)
+    DevLeaf L{};
+    L.off = static_cast<int>(plan.leaf_off[b]);
+    L.cnt = static_cast<int>(plan.leaf_cnt[b]);
+    L.sh_begin = static_cast<int>(leaf_sh.size());
+    L.ao_begin = static_cast<int>(leaf_ao.size());
+    for (long k = plan.leaf_sh_ptr[b]; k < plan.leaf_sh_ptr[b + 1]; k++) {
+      int s = plan.leaf_sh[k];
+      leaf_sh.push_back(s);
+      for (int f = 0; f < basis.shell_size(s); f++)
+        leaf_ao.push_back(basis.first_bf[s] + f);
+    }
+    L.sh_end = static_cast<int>(leaf_sh.size());
+    L.nbf = m;
+    L.mpad = static_cast<int>(round_up(m, kAoTile));
+    L.npad = static_cast<int>(round_up(L.cnt, kPtTile));
+    L.ws_off = static_cast<long long>(ws_elems);
+    ws_elems += static_cast<size_t>(ncomp) * L.mpad * L.npad;
+    const int li = static_cast<int>(leaves.size());
+    for (int p0 = 0; p0 < L.npad; p0 += kPtTile)
+      slabs.push_back({li, p0});
+    for (int i0 = 0; i0 < L.mpad; i0 += kAoTile)
+      for (int j0 = 0; j0 < L.mpad; j0 += kAoTile)
+        tiles.push_back({li, i0, j0, 0});
+    flops += 4.0 * L.cnt * static_cast<double>(m) * m;
+    leaves.push_back(L);
+  }
+}
+
+void Molecule::upload() {
+  size_t bytes = 0;
+  std::vector<DevShell> sh(basis.shells.size());
+  std::vector<double2> prims;
+  for (size_t s = 0; s < basis.shells.size(); s++) {
+    const Shell &S = basis.shells[s];
+    DevShell &d = sh[s];
+    for (int k = 0; k < 3; k++)
+      d.A[k] = S.origin[k];
+    d.fac = common_fac(S.l, basis.pure);
+    d.l = S.l;
+    d.nprim = static_cast<int>(S.exps.size());
+    d.prim_off = static_cast<int>(prims.size());
+    d.nfunc = basis.shell_size(static_cast<int>(s));
+    for (size_t k = 0; k < S.exps.size(); k++)
+      prims.push_back(make_double2(S.exps[k], S.coefs[k]));
+  }
+  std::vector<Pt4> pts(plan.npts);
+  for (long i = 0; i < plan.npts; i++)
+    pts[i] = make_pt4(plan.pts4[4 * i], plan.pts4[4 * i + 1], plan.pts4[4 * i + 2],
+                          plan.pts4[4 * i + 3]);
+  d_pts = dev_upload(pts, bytes);
+  allocations.push_back(d_pts);
+  d_shells = dev_upload(sh, bytes);
+  allocations.push_back(d_shells);
+  d_prims = dev_upload(prims, bytes);
+  allocations.push_back(d_prims);
+  d_leaves = dev_upload(leaves, bytes);
+  allocations.push_back(d_leaves);
+  d_leaf_sh = dev_upload(leaf_sh, bytes);
+  allocations.push_back(d_leaf_sh);
+  d_leaf_ao = dev_upload(leaf_ao, bytes);
+  allocations.push_back(d_leaf_ao);
+  d_slabs = dev_upload(slabs, bytes);
+  allocations.push_back(d_slabs);
+  d_tiles = dev_upload(tiles, bytes);
+  allocations.push_back(d_tiles);
+  device_bytes += static_cast<double>(bytes);
+
+  const size_t N = static_cast<size_t>(std::max<long>(plan.npts, 1));
+  const size_t nl = std::max<size_t>(leaves.size(), 1);
+  d_ws = static_cast<double *>(alloc(ws_elems * sizeof(double)));
+  d_rho = static_cast<double *>(alloc(4 * N * sizeof(double)));
+  d_coef = static_cast<double *>(alloc(4 * N * sizeof(double)));
+  d_epart = static_cast<double *>(alloc(2 * nl * sizeof(double)));
+  d_out2 = static_cast<double *>(alloc(2 * sizeof(double)));
+  const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
+  d_D = static_cast<double *>(alloc(std::max<size_t>(nbf2, 1) * sizeof(double)));
+  d_V = static_cast<double *>(alloc(std::max<size_t>(nbf2, 1) * sizeof(double)));
+  cuda_check(cudaMemset(d_rho, 0, 4 * N * sizeof(double)), "cudaMemset");
+}
+
+MolDev Molecule::dev() const {
+  MolDev m;
+  m.pts = d_pts;
+  m.shells = d_shells;
+  m.prims = d_prims;
+  m.leaves = d_leaves;
+  m.leaf_sh = d_leaf_sh;
+  m.leaf_ao = d_leaf_ao;
+  m.nleaves = static_cast<int>(leaves.size());
+  m.npts = static_cast<int>(plan.npts);
+  m.nbf = basis.nbf;
+  m.pure = basis.pure ? 1 : 0;
+  return m;
+}
+
+// One restricted XC build on device buffers (the FP64 sequence).
+void Molecule::build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st) {
+  const MolDev m = dev();
+  const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
+  cuda_check(cudaMemsetAsync(dV, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
+  launch_colloc_f64(m, deriv, d_ws, st);
+  launch_rho_f64(m, deriv, dD, d_ws, d_slabs, static_cast<int>(slabs.size()), d_rho, st);
+  launch_func(m, deriv, fs, bs.density_threshold, d_rho, d_coef, d_epart, st);
+  launch_vxc_f64(m, deriv, d_ws, d_coef, d_tiles, static_cast<int>(tiles.size()), dV, st);
+  launch_reduce(d_epart, m.nleaves, dout2, st);
+  cuda_check(cudaGetLastError(), "kernel launch");
+}
+
+void Molecule::build(int precision, const double *dD, double *dV, double *dout2,
+                     cudaStream_t st) {
+  if (precision == OCC_XC_MIXED)
+    build_mixed(dD, dV, dout2, st);
+  else
+    build_fp64(dD, dV, dout2, st);
+}
+
+std::once_flag g_sph_once;
+
+Context::Context(int dev) : device(dev) {
+  cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+  cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  std::call_once(g_sph_once, [] { upload_sph_table(); });
+  upload_sph_table();
+}
+Context::~Context() {
+  if (stream)
+    cudaStreamDestroy(stream);
+}
+
+} // namespace occx
+
+using namespace occx;
+
+struct occ_xc_context {
+  std::unique_ptr<Context> impl;
+  std::string err;
+  std::mutex mu;
+};
+struct occ_xc_molecule {
+  std::unique_ptr<Molecule> impl;
+  occ_xc_context *ctx;
+};
+
+namespace {
+Basis make_basis(int natoms, const double *xyz, int nshells, const int *shell_l,
+                 const int *shell_atom, const int *shell_nprim, const double *exponents,
+                 const double *coefficients, int pure) {
+  Basis basis;
+  basis.pure = pure != 0;
+  size_t off = 0;
+  for (int s = 0; s < nshells; s++) {
+    if (shell_l[s] < 0 || shell_l[s] > kMaxL)
+      throw ArgError("shell angular momentum must be in 0..4");
+    if (shell_atom[s] < 0 || shell_atom[s] >= natoms || shell_nprim[s] <= 0)
+      throw ArgError("bad shell atom index or primitive count");
+    Shell sh;
+    sh.l = shell_l[s];
+    sh.atom = shell_atom[s];
+    for (int k = 0; k < 3; k++)
+      sh.origin[k] = xyz[3 * sh.atom + k];
+    sh.exps.assign(exponents + off, exponents + off + shell_nprim[s]);
+    sh.coefs.assign(coefficients + off, coefficients + off + shell_nprim[s]);
+    off += shell_nprim[s];
+    basis.shells.push_back(sh);
+  }
+  basis.finalise();
+  return basis;
+}
+
+GridSettings grid_settings_from(const occ_xc_grid_settings *grid) {
+  GridSettings gs;
+  if (grid) {
+    gs.max_angular_points = grid->max_angular_points;
+    gs.min_angular_points = grid->min_angular_points;
+    gs.radial_points = grid->radial_points;
+    gs.radial_precision = grid->radial_precision;
+    gs.reduced_first_row_element_grid = grid->reduced_first_row_element_grid != 0;
+    gs.treutler_alrichs_adjustment = grid->treutler_alrichs_adjustment != 0;
+    gs.pruning_scheme = grid->pruning_scheme;
+  }
+  return gs;
+}
+
+template <typename F> int guarded(occ_xc_context *ctx, F &&f) {
+  try {
+    f();
+    return OCC_XC_OK;
+  } catch (const MethodError &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_METHOD;
+  } catch (const CudaError &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_CUDA;
+  } catch (const ArgError &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_ARG;
+  } catch (const std::bad_alloc &) {
+    if (ctx)
+      ctx->err = "host allocation failed";
+    return OCC_XC_ERR_NOMEM;
+  } catch (const std::exception &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_INTERNAL;
+  }
+}
+} // namespace
+
+extern "C" {
+
+void occ_xc_default_grid_settings(occ_xc_grid_settings *o) {
+  GridSettings g;
+  o->max_angular_points = g.max_angular_points;
+  o->min_angular_points = g.min_angular_points;
+  o->radial_points = g.radial_points;
+  o->radial_precision = g.radial_precision;
+  o->reduced_first_row_element_grid = g.reduced_first_row_element_grid;
+  o->treutler_alrichs_adjustment = g.treutler_alrichs_adjustment;
+  o->pruning_scheme = g.pruning_scheme;
+}
+
+void occ_xc_default_build_settings(occ_xc_build_settings *o) {
+  BuildSettings b;
+  o->xc_screening_threshold = b.xc_screening_threshold;
+  o->density_threshold = b.density_threshold;
+  o->leaf_target = static_cast<int>(b.leaf_target);
+  o->leaf_min = static_cast<int>(b.leaf_min);
+  o->leaf_max = static_cast<int>(b.leaf_max);
+}
+
+int occ_xc_normalize_shell(int l, int nprim, const double *exps, double *coefs) {
+  if (l < 0 || l > kMaxL || nprim <= 0 || !exps || !coefs)
+    return OCC_XC_ERR_ARG;
+  normalize_shell(l, nprim, exps, coefs);
+  return OCC_XC_OK;
+}
+
+int occ_xc_molecular_grid(int natoms, const int *Z, const double *xyz, int nshells,
+                          const int *shell_l, const int *shell_atom, const int *shell_nprim,
+                          const double *exponents, const double *coefficients, int pure,
+                          const occ_xc_grid_settings *grid, long *npoints, double *points,
+                          double *weights) {
+  if (natoms <= 0 || nshells <= 0 || !Z || !xyz || !shell_l || !shell_atom || !shell_nprim ||
+      !exponents || !coefficients || !npoints)
+    return OCC_XC_ERR_ARG;
+  try {
+    Basis basis = make_basis(natoms, xyz, nshells, shell_l, shell_atom, shell_nprim, exponents,
+                             coefficients, pure);
+    GridSettings gs = grid_settings_from(grid);
+    MolecularGrid mg = build_molecular_grid(std::vector<int>(Z, Z + natoms),
+                                            std::vector<double>(xyz, xyz + 3 * natoms), basis, gs,
+                                            0);
+    if (points && weights) {
+      if (*npoints < mg.npts())
+        return OCC_XC_ERR_ARG;
+      std::memcpy(points, mg.xyz.data(), mg.xyz.size() * sizeof(double));
+      std::memcpy(weights, mg.w.data(), mg.w.size() * sizeof(double));
+    }
+    *npoints = mg.npts();
+    return OCC_XC_OK;
+  } catch (const std::exception &e) {
+    std::fprintf(stderr, "occ_xc_molecular_grid: %s\n", e.what());
+    return OCC_XC_ERR_ARG;
+  }
+}
+
+int occ_xc_context_create(int device, occ_xc_context **out) {
+  if (!out)
+    return OCC_XC_ERR_ARG;
+  *out = nullptr;
+  auto ctx = std::make_unique<occ_xc_context>();
+  int rc = guarded(ctx.get(), [&] { ctx->impl = std::make_unique<Context>(device); });
+  if (rc != OCC_XC_OK) {
+    std::fprintf(stderr, "occ_xc_context_create: %s\n", ctx->err.c_str());
+    return rc;
+  }
+  *out = ctx.release();
+  return OCC_XC_OK;
+}
+
+void occ_xc_context_destroy(occ_xc_context *ctx) { delete ctx; }
+
+const char *occ_xc_last_error(const occ_xc_context *ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+int occ_xc_molecule_create(occ_xc_context *ctx, int natoms, const int *Z, const double *xyz,
+                           int nshells, const int *shell_l, const int *shell_atom,
+                           const int *shell_nprim, const double *exponents,
+                           const double *coefficients, int pure, const char *method,
+                           const occ_xc_grid_settings *grid, const occ_xc_build_settings *build,
+                           occ_xc_molecule **out) {
+  if (!ctx || !out)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *out = nullptr;
+  auto mol = std::make_unique<occ_xc_molecule>();
+  mol->ctx = ctx;
+  int rc = guarded(ctx, [&] {
+    if (natoms <= 0 || nshells <= 0 || !Z || !xyz || !shell_l || !shell_atom || !shell_nprim ||
+        !exponents || !coefficients || !method)
+      throw ArgError("occ_xc_molecule_create: missing or empty input");
+    cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
+    auto M = std::make_unique<Molecule>();
+    M->ctx = ctx->impl.get();
+    M->fs = parse_method(method);
+    M->deriv = 0;
+    for (int i = 0; i < M->fs.n; i++)
+      M->deriv = std::max(M->deriv, func_is_gga(M->fs.id[i]) ? 1 : 0);
+    M->Z.assign(Z, Z + natoms);
+    M->xyz.assign(xyz, xyz + 3 * natoms);
+    M->basis = make_basis(natoms, xyz, nshells, shell_l, shell_atom, shell_nprim, exponents,
+                          coefficients, pure);
+    M->gs = grid_settings_from(grid);
+    if (build) {
+      M->bs.xc_screening_threshold = build->xc_screening_threshold;
+      M->bs.density_threshold = build->density_threshold;
+      M->bs.leaf_target = build->leaf_target;
+      M->bs.leaf_min = build->leaf_min;
+      M->bs.leaf_max = build->leaf_max;
+      if (M->bs.leaf_max > 256 || M->bs.leaf_target <= 0 || M->bs.leaf_min <= 0 ||
+          M->bs.leaf_target > M->bs.leaf_max || 2 * M->bs.leaf_min > M->bs.leaf_max)
+        throw ArgError("leaf sizes must satisfy 0 < target <= max <= 256, 2 min <= max");
+    }
+    M->grid = build_molecular_grid(M->Z, M->xyz, M->basis, M->gs, 0);
+    M->build_plan();
+    M->upload();
+    M->prepare_mixed();
+    mol->impl = std::move(M);
+  });
+  if (rc == OCC_XC_OK)
+    *out = mol.release();
+  return rc;
+}
+
+void occ_xc_molecule_destroy(occ_xc_molecule *mol) {
+  if (!mol)
+    return;
+  if (mol->ctx)
+    cudaSetDevice(mol->ctx->impl->device);
+  delete mol;
+}
+
+int occ_xc_molecule_info_get(const occ_xc_molecule *mol, occ_xc_molecule_info *o) {
+  if (!mol || !o)
+    return OCC_XC_ERR_ARG;
+  const Molecule &M = *mol->impl;
+  o->nbf = M.basis.nbf;
+  o->natoms = static_cast<int>(M.Z.size());
+  o->nshells = static_cast<int>(M.basis.shells.size());
+  o->deriv = M.deriv;
+  o->npoints = M.plan.npts;
+  o->nleaves = static_cast<long>(M.leaves.size());
+  o->flops_per_build = M.flops;
+  o->device_bytes = M.device_bytes;
+  o->workspace_bytes = static_cast<double>(M.ws_elems) * sizeof(double);
+  return OCC_XC_OK;
+}
+
+int occ_xc_molecule_grid(const occ_xc_molecule *mol, double *points, double *weights) {
+  if (!mol || !points || !weights)
+    return OCC_XC_ERR_ARG;
+  const Molecule &M = *mol->impl;
+  std::memcpy(points, M.grid.xyz.data(), M.grid.xyz.size() * sizeof(double));
+  std::memcpy(weights, M.grid.w.data(), M.grid.w.size() * sizeof(double));
+  return OCC_XC_OK;
+}
+
+int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
+                              int precision, double *d_V, double *d_exc2, void *stream) {
+  if (!ctx || !mol || !d_D || !d_V || !d_exc2)
+    return OCC_XC_ERR_ARG;
+  if (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return guarded(ctx, [&] {
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
+    mol->impl->build(precision, d_D, d_V, d_exc2, st);
+  });
+}
+
+int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D,
+                       int precision, double *V, double *exc, double *nelec_out) {
+  if (!ctx || !mol || !D || !V || !exc)
+    return OCC_XC_ERR_ARG;
+  if (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return guarded(ctx, [&] {
+    Molecule &M = *mol->impl;
+    cudaStream_t st = ctx->impl->stream;
+    const size_t nbf2 = static_cast<size_t>(M.basis.nbf) * M.basis.nbf;
+    cuda_check(cudaMemcpyAsync(M.d_D, D, nbf2 * sizeof(double), cudaMemcpyHostToDevice, st),
+               "cudaMemcpyAsync H2D");
+    M.build(precision, M.d_D, M.d_V, M.d_out2, st);
+    double out2[2];
+    cuda_check(cudaMemcpyAsync(V, M.d_V, nbf2 * sizeof(double), cudaMemcpyDeviceToHost, st),
+               "cudaMemcpyAsync D2H");
+    cuda_check(cudaMemcpyAsync(out2, M.d_out2, sizeof(out2), cudaMemcpyDeviceToHost, st),
+               "cudaMemcpyAsync D2H");
+    cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    *exc = out2[0];
+    if (nelec_out)
+      *nelec_out = out2[1];
+  });
+}
+
+} // extern "C"

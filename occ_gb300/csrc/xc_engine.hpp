@@ -1,0 +1,77 @@
+// Engine internals shared by the C ABI and the precision-specific build paths.
+#pragma once
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "host/xc_host.hpp"
+#include "xc_device.cuh"
+
+namespace occx {
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct MethodError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct ArgError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+void cuda_check(cudaError_t e, const char *what);
+FuncSet parse_method(const std::string &method);
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  explicit Context(int dev);
+  ~Context();
+};
+
+struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)
+
+struct Molecule {
+  Context *ctx = nullptr;
+  // host model
+  std::vector<int> Z;
+  std::vector<double> xyz;
+  Basis basis;
+  GridSettings gs;
+  BuildSettings bs;
+  FuncSet fs{};
+  int deriv = 0;
+  MolecularGrid grid;
+  Plan plan;
+  // device plan
+  std::vector<DevLeaf> leaves;
+  std::vector<int> leaf_sh, leaf_ao;
+  std::vector<SlabItem> slabs;
+  std::vector<TileItem> tiles;
+  size_t ws_elems = 0;
+  double flops = 0.0;
+  double device_bytes = 0.0;
+  std::vector<void *> allocations;
+  Pt4 *d_pts = nullptr;
+  DevShell *d_shells = nullptr;
+  double2 *d_prims = nullptr;
+  DevLeaf *d_leaves = nullptr;
+  int *d_leaf_sh = nullptr, *d_leaf_ao = nullptr;
+  SlabItem *d_slabs = nullptr;
+  TileItem *d_tiles = nullptr;
+  double *d_ws = nullptr, *d_rho = nullptr, *d_coef = nullptr, *d_epart = nullptr;
+  double *d_out2 = nullptr, *d_D = nullptr, *d_V = nullptr;
+  MixedState *mixed = nullptr;
+
+  ~Molecule();
+  void *alloc(size_t bytes);
+  void build_plan();
+  void upload();
+  void prepare_mixed();
+  MolDev dev() const;
+  void build(int precision, const double *dD, double *dV, double *dout2, cudaStream_t st);
+  void build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st);
+  void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
+};
+
+} // namespace occx

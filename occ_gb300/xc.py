@@ -1,0 +1,316 @@
+"""ctypes binding of include/occ_xc.h and the OCC-shaped host classes.
+
+Molecule        occ::core::Molecule (positions in Angstrom, atoms() in Bohr;
+                src/core/molecule.cpp:115-121)
+AOBasis.load    occ::gto::AOBasis::load (src/gto/shell.cpp:499-571): JSON
+                basis, general contractions split, Shell::incorporate_shell_norm
+DFT             occ::dft::DFT for the XC part: DFT(method, basis, grid),
+                compute_vxc(D) (include/occ/dft/dft.h:395-429),
+                exchange_correlation_energy() (dft.h:83)
+"""
+import ctypes as C
+import json
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+FP64 = 0
+MIXED = 1
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+ANGSTROM_TO_BOHR = 1.0 / 0.52917721067  # include/occ/core/units.h:7-8
+
+
+class XCError(RuntimeError):
+    pass
+
+
+def library_path():
+    return os.path.join(_HERE, "lib", "libocc_xc.so")
+
+
+class _GridSettings(C.Structure):
+    _fields_ = [("max_angular_points", C.c_int), ("min_angular_points", C.c_int),
+                ("radial_points", C.c_int), ("radial_precision", C.c_double),
+                ("reduced_first_row_element_grid", C.c_int),
+                ("treutler_alrichs_adjustment", C.c_int), ("pruning_scheme", C.c_int)]
+
+
+class _BuildSettings(C.Structure):
+    _fields_ = [("xc_screening_threshold", C.c_double), ("density_threshold", C.c_double),
+                ("leaf_target", C.c_int), ("leaf_min", C.c_int), ("leaf_max", C.c_int)]
+
+
+class _MolInfo(C.Structure):
+    _fields_ = [("nbf", C.c_int), ("natoms", C.c_int), ("nshells", C.c_int), ("deriv", C.c_int),
+                ("npoints", C.c_long), ("nleaves", C.c_long), ("flops_per_build", C.c_double),
+                ("device_bytes", C.c_double), ("workspace_bytes", C.c_double)]
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def library():
+    """Load the in-tree CUDA library; fail loudly if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise XCError(f"{path} is missing: build it with `python -m occ_gb300.build`")
+    lib = C.CDLL(path)
+    lib.occ_xc_last_error.restype = C.c_char_p
+    lib.occ_xc_last_error.argtypes = [C.c_void_p]
+    lib.occ_xc_context_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+    lib.occ_xc_context_destroy.argtypes = [C.c_void_p]
+    lib.occ_xc_normalize_shell.argtypes = [C.c_int, C.c_int, _dp, _dp]
+    lib.occ_xc_default_grid_settings.argtypes = [C.POINTER(_GridSettings)]
+    lib.occ_xc_default_build_settings.argtypes = [C.POINTER(_BuildSettings)]
+    lib.occ_xc_molecule_create.argtypes = [
+        C.c_void_p, C.c_int, _ip, _dp, C.c_int, _ip, _ip, _ip, _dp, _dp, C.c_int, C.c_char_p,
+        C.POINTER(_GridSettings), C.POINTER(_BuildSettings), C.POINTER(C.c_void_p)]
+    lib.occ_xc_molecule_destroy.argtypes = [C.c_void_p]
+    lib.occ_xc_molecule_info_get.argtypes = [C.c_void_p, C.POINTER(_MolInfo)]
+    lib.occ_xc_molecule_grid.argtypes = [C.c_void_p, _dp, _dp]
+    lib.occ_xc_compute_vxc.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp, _dp, _dp]
+    lib.occ_xc_compute_vxc_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                              C.c_void_p, C.c_void_p, C.c_void_p]
+    _LIB = lib
+    return lib
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+@dataclass
+class Atom:
+    atomic_number: int
+    x: float  # Bohr
+    y: float
+    z: float
+
+
+class Molecule:
+    def __init__(self, atomic_numbers, positions_angstrom):
+        self.atomic_numbers = np.asarray(atomic_numbers, dtype=np.int32)
+        pos = np.asarray(positions_angstrom, dtype=np.float64)
+        if pos.shape == (3, len(self.atomic_numbers)) and pos.shape != (3, 3):
+            pos = pos.T
+        self.positions = pos.reshape(-1, 3)  # Angstrom, one row per atom
+
+    def atoms(self):
+        b = self.positions * ANGSTROM_TO_BOHR
+        return [Atom(int(z), *map(float, r)) for z, r in zip(self.atomic_numbers, b)]
+
+    def __len__(self):
+        return len(self.atomic_numbers)
+
+
+@dataclass
+class Shell:
+    l: int
+    atom: int
+    origin: np.ndarray  # Bohr
+    exponents: np.ndarray
+    coefficients: np.ndarray  # normalised (incorporate_shell_norm applied)
+
+    def size(self, pure):
+        return 2 * self.l + 1 if pure else (self.l + 1) * (self.l + 2) // 2
+
+
+def _canonical_basis_name(name):
+    return name.lower().replace("*", "_st_")
+
+
+class AOBasis:
+    def __init__(self, atoms, shells, name=""):
+        self._atoms = atoms
+        self.shells = shells
+        self.name = name
+        self.pure = False  # OCC's AOBasis is Cartesian until set_pure(true)
+
+    @staticmethod
+    def load(atoms, name, path=None):
+        fname = os.path.join(path or os.path.join(_HERE, "data", "basis"),
+                             _canonical_basis_name(name) + ".json")
+        if not os.path.exists(fname):
+            raise XCError(f"basis set file not found: {fname}")
+        with open(fname) as f:
+            elements = json.load(f)["elements"]
+        lib = library()
+        shells = []
+        for a, atom in enumerate(atoms):
+            key = str(atom.atomic_number)
+            if key not in elements:
+                raise XCError(f"element {atom.atomic_number} not found in basis {name}")
+            for s in elements[key]["electron_shells"]:
+                exps = np.array([float(x) for x in s["exponents"]], dtype=np.float64)
+                for i, coefs in enumerate(s["coefficients"]):
+                    l = s["angular_momentum"][i % len(s["angular_momentum"])]
+                    c = np.array([float(x) for x in coefs], dtype=np.float64)
+                    rc = lib.occ_xc_normalize_shell(l, len(exps), _ptr(exps), _ptr(c))
+                    if rc != 0:
+                        raise XCError(f"cannot normalise shell l={l}")
+                    shells.append(Shell(l, a, np.array([atom.x, atom.y, atom.z]), exps.copy(), c))
+        return AOBasis(atoms, shells, name)
+
+    def set_pure(self, pure=True):
+        self.pure = bool(pure)
+
+    def atoms(self):
+        return self._atoms
+
+    def nbf(self):
+        return sum(s.size(self.pure) for s in self.shells)
+
+    def nsh(self):
+        return len(self.shells)
+
+    def first_bf(self):
+        out, n = [], 0
+        for s in self.shells:
+            out.append(n)
+            n += s.size(self.pure)
+        return out
+
+    def arrays(self):
+        """Flat arrays in the C ABI's layout."""
+        l = np.array([s.l for s in self.shells], dtype=np.int32)
+        atom = np.array([s.atom for s in self.shells], dtype=np.int32)
+        nprim = np.array([len(s.exponents) for s in self.shells], dtype=np.int32)
+        exps = np.concatenate([s.exponents for s in self.shells]).astype(np.float64)
+        coefs = np.concatenate([s.coefficients for s in self.shells]).astype(np.float64)
+        return l, atom, nprim, exps, coefs
+
+
+@dataclass
+class GridSettings:
+    """occ::numint::GridSettings defaults (grid_settings.h:81-95)."""
+    max_angular_points: int = 302
+    min_angular_points: int = 110
+    radial_points: int = 50
+    radial_precision: float = 1e-12
+    reduced_first_row_element_grid: bool = True
+    treutler_alrichs_adjustment: bool = True
+    pruning_scheme: int = 1
+
+    def _c(self):
+        return _GridSettings(self.max_angular_points, self.min_angular_points, self.radial_points,
+                             self.radial_precision, int(self.reduced_first_row_element_grid),
+                             int(self.treutler_alrichs_adjustment), self.pruning_scheme)
+
+
+@dataclass
+class BuildSettings:
+    xc_screening_threshold: float = 1e-10
+    density_threshold: float = 1e-10
+    leaf_target: int = 128
+    leaf_min: int = 32
+    leaf_max: int = 256
+
+    def _c(self):
+        return _BuildSettings(self.xc_screening_threshold, self.density_threshold,
+                              self.leaf_target, self.leaf_min, self.leaf_max)
+
+
+class _Context:
+    def __init__(self, device=0):
+        lib = library()
+        h = C.c_void_p()
+        rc = lib.occ_xc_context_create(device, C.byref(h))
+        if rc != 0:
+            raise XCError(f"occ_xc_context_create failed ({rc})")
+        self.h = h
+        self.lib = lib
+
+    def error(self):
+        return self.lib.occ_xc_last_error(self.h).decode()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.occ_xc_context_destroy(self.h)
+            self.h = None
+
+
+_CONTEXTS = {}
+
+
+def _context(device):
+    if device not in _CONTEXTS:
+        _CONTEXTS[device] = _Context(device)
+    return _CONTEXTS[device]
+
+
+class DFT:
+    """The XC part of occ::dft::DFT on one GB300."""
+
+    def __init__(self, method, basis, grid_settings=None, build_settings=None, device=0):
+        self.method = method
+        self.basis = basis
+        self.ctx = _context(device)
+        lib = self.ctx.lib
+        atoms = basis.atoms()
+        Z = np.array([a.atomic_number for a in atoms], dtype=np.int32)
+        xyz = np.array([[a.x, a.y, a.z] for a in atoms], dtype=np.float64).ravel()
+        l, atom, nprim, exps, coefs = basis.arrays()
+        gs = (grid_settings or GridSettings())._c()
+        bs = (build_settings or BuildSettings())._c()
+        h = C.c_void_p()
+        rc = lib.occ_xc_molecule_create(self.ctx.h, len(Z), _ptr(Z, _ip), _ptr(xyz), len(l),
+                                        _ptr(l, _ip), _ptr(atom, _ip), _ptr(nprim, _ip),
+                                        _ptr(exps), _ptr(coefs), int(basis.pure),
+                                        method.encode(), C.byref(gs), C.byref(bs), C.byref(h))
+        if rc != 0:
+            raise XCError(f"occ_xc_molecule_create failed ({rc}): {self.ctx.error()}")
+        self.h = h
+        self._exc = 0.0
+        self._nelec = 0.0
+        self._keep = (Z, xyz, l, atom, nprim, exps, coefs)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.occ_xc_molecule_destroy(self.h)
+            self.h = None
+
+    def info(self):
+        i = _MolInfo()
+        self.ctx.lib.occ_xc_molecule_info_get(self.h, C.byref(i))
+        return {f: getattr(i, f) for f, _ in _MolInfo._fields_}
+
+    def nbf(self):
+        return self.basis.nbf()
+
+    def grid(self):
+        """(points[N,3] Bohr, weights[N]) in OCC's atom-block layout."""
+        n = self.info()["npoints"]
+        pts = np.zeros((n, 3))
+        w = np.zeros(n)
+        self.ctx.lib.occ_xc_molecule_grid(self.h, _ptr(pts), _ptr(w))
+        return pts, w
+
+    def compute_vxc(self, D, precision=FP64):
+        """V_xc for mo.D (nbf x nbf); E_xc via exchange_correlation_energy()."""
+        nbf = self.nbf()
+        Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if Dm.shape != (nbf, nbf):
+            raise XCError(f"density matrix must be {nbf}x{nbf}")
+        V = np.zeros((nbf, nbf), order="F")
+        exc = C.c_double()
+        nel = C.c_double()
+        rc = self.ctx.lib.occ_xc_compute_vxc(self.ctx.h, self.h, _ptr(Dm), int(precision),
+                                             _ptr(V), C.byref(exc), C.byref(nel))
+        if rc != 0:
+            raise XCError(f"occ_xc_compute_vxc failed ({rc}): {self.ctx.error()}")
+        self._exc = exc.value
+        self._nelec = nel.value
+        return V
+
+    def exchange_correlation_energy(self):
+        return self._exc
+
+    def integrated_density(self):
+        return self._nelec

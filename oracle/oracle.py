@@ -1,0 +1,136 @@
+"""Python access to the CPU oracle (oracle/xc_oracle.cpp) -- TEST
+INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the CPU
+baseline leg of bench.py, never by the product.
+
+The oracle restates OCC's restricted XC build on the CPU in FP64
+(include/occ/dft/dft.h:192-388).  Its collocation is pinned against the
+reference's gau2grid and its PBE exchange against tests/dft_tests.cpp:71-111;
+the remaining functionals are restated from their papers (Libxc is not
+available here).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lp = C.POINTER(C.c_long)
+_lib = None
+
+# Libxc ids of the components of OCC's method names (share/methods/dft_methods.json)
+METHODS = {
+    "lda": [1, 30], "svwn": [1, 30], "lsda": [1, 30], "svwn5": [1, 7],
+    "pbe": [101, 130], "blyp": [106, 131], "bpbe": [106, 130],
+    "b3lyp": [402], "b3lyp5": [475],
+}
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.oracle_functional.argtypes = [C.c_int, C.c_long, _dp, _dp, _dp, _dp, _dp]
+        L.oracle_collocation.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_long, _dp,
+                                         C.c_int, _dp]
+        L.oracle_decay_cutoff.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, C.c_int,
+                                          C.c_double, _dp]
+        L.oracle_morton_leaves.argtypes = [C.c_long, _dp, C.c_long, C.c_long, C.c_long, _lp, _lp,
+                                           _lp, _dp, _dp]
+        L.oracle_morton_leaves.restype = C.c_long
+        L.oracle_xc_build.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, C.c_int, C.c_long,
+                                      _dp, _dp, _dp, C.c_int, _ip, _dp, C.c_double, C.c_double,
+                                      C.c_long, C.c_long, C.c_long, C.c_int, C.c_long, _dp, _dp,
+                                      _dp]
+        _lib = L
+    return _lib
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def functional(fid, rho, sigma=None):
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    n = len(rho)
+    sig = np.ascontiguousarray(sigma if sigma is not None else np.zeros(n), dtype=np.float64)
+    exc, vrho, vsig = np.zeros(n), np.zeros(n), np.zeros(n)
+    rc = lib().oracle_functional(fid, n, _p(rho), _p(sig), _p(exc), _p(vrho), _p(vsig))
+    if rc != 0:
+        raise ValueError(f"unknown functional {fid}")
+    return exc, vrho, vsig
+
+
+def collocation(l, pure, exps, coefs, origin, xyz, deriv=1):
+    exps = np.ascontiguousarray(exps, dtype=np.float64)
+    coefs = np.ascontiguousarray(coefs, dtype=np.float64)
+    origin = np.ascontiguousarray(origin, dtype=np.float64)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    nf = 2 * l + 1 if pure else (l + 1) * (l + 2) // 2
+    out = np.zeros((4 if deriv else 1, nf, len(xyz)))
+    lib().oracle_collocation(l, int(pure), len(exps), _p(exps), _p(coefs), _p(origin), len(xyz),
+                             _p(xyz), int(deriv), _p(out))
+    return out
+
+
+def _basis_arrays(basis):
+    l, atom, nprim, exps, coefs = basis.arrays()
+    off = np.zeros(len(l), dtype=np.int32)
+    off[1:] = np.cumsum(nprim)[:-1]
+    origin = np.array([s.origin for s in basis.shells], dtype=np.float64).ravel()
+    return l, nprim, off, exps, coefs, origin
+
+
+def decay_cutoff(basis, threshold=1e-10):
+    l, nprim, off, exps, coefs, origin = _basis_arrays(basis)
+    ext = np.zeros(len(l))
+    lib().oracle_decay_cutoff(len(l), _p(l, _ip), _p(nprim, _ip), _p(off, _ip), _p(exps),
+                              _p(coefs), _p(origin), int(basis.pure), threshold, _p(ext))
+    return ext
+
+
+def morton_leaves(points, target=128, min_leaf=32, max_leaf=256):
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    n = len(pts)
+    perm = np.zeros(n, dtype=np.int64)
+    off = np.zeros(n + 1, dtype=np.int64)
+    cnt = np.zeros(n + 1, dtype=np.int64)
+    cen = np.zeros(3 * (n + 1))
+    rad = np.zeros(n + 1)
+    nl = lib().oracle_morton_leaves(n, _p(pts), target, min_leaf, max_leaf, _p(perm, _lp),
+                                    _p(off, _lp), _p(cnt, _lp), _p(cen), _p(rad))
+    return perm, off[:nl], cnt[:nl], cen[:3 * nl].reshape(-1, 3), rad[:nl]
+
+
+def xc_build(basis, points, weights, D, method, screen=1e-10, density_threshold=1e-10,
+             leaf=(128, 32, 256), nthreads=0, leaf_subset=0, func_ids=None):
+    """E_xc, V_xc (nbf x nbf) and the integrated density for mo.D = D."""
+    l, nprim, off, exps, coefs, origin = _basis_arrays(basis)
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    nbf = basis.nbf()
+    Df = np.asfortranarray(D, dtype=np.float64)
+    ids = np.array(func_ids if func_ids is not None else METHODS[method.lower()], dtype=np.int32)
+    coef = np.ones(len(ids))
+    V = np.zeros((nbf, nbf), order="F")
+    exc = C.c_double()
+    nel = C.c_double()
+    rc = lib().oracle_xc_build(len(l), _p(l, _ip), _p(nprim, _ip), _p(off, _ip), _p(exps),
+                               _p(coefs), _p(origin), int(basis.pure), len(w), _p(pts), _p(w),
+                               Df.ctypes.data_as(_dp), len(ids), _p(ids, _ip), _p(coef), screen,
+                               density_threshold, leaf[0], leaf[1], leaf[2], nthreads,
+                               leaf_subset, V.ctypes.data_as(_dp), C.byref(exc), C.byref(nel))
+    if rc != 0:
+        raise RuntimeError(f"oracle_xc_build failed ({rc})")
+    return exc.value, V, nel.value

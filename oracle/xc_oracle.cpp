@@ -1,0 +1,547 @@
+// CPU oracle for the restricted Kohn-Sham XC build -- TEST INFRASTRUCTURE
+// ONLY (see xc_oracle.h).  Every step cites the reference code it restates.
+#include "xc_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <utility>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const double kPi = 3.14159265358979323846;
+
+// src/gto/gto.cpp:7-16
+double common_fac(int l, bool pure) {
+  if (l == 0)
+    return 0.282094791773878143;
+  if (l == 1)
+    return 0.488602511902919921;
+  return pure ? std::sqrt((2 * l + 1) / (4 * kPi)) : 1.0;
+}
+
+double factorial(int n) {
+  double r = 1;
+  for (int i = 2; i <= n; i++)
+    r *= i;
+  return r;
+}
+double binom(int n, int k) {
+  if (k < 0 || k > n)
+    return 0.0;
+  return factorial(n) / (factorial(k) * factorial(n - k));
+}
+
+int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+// Position of x^a y^b z^(l-a-b) in CCA order (xx, xy, xz, yy, yz, zz, ...).
+int cart_index(int l, int a, int b) {
+  int idx = 0;
+  for (int aa = l; aa > a; aa--)
+    idx += l - aa + 1;
+  return idx + (l - a - b);
+}
+
+// Real solid harmonics in CCA order m = -l..l as combinations of Cartesian
+// monomials (Helgaker, Jorgensen, Olsen, Molecular Electronic-Structure
+// Theory, eqs. 6.4.47-6.4.50).  This is the convention gau2grid's
+// GG_SPHERICAL_CCA transform follows (src/3rdparty/gau2grid).
+std::vector<double> spherical_transform(int l) {
+  int nc = ncart(l), ns = 2 * l + 1;
+  std::vector<double> T(ns * nc, 0.0);
+  for (int m = -l; m <= l; m++) {
+    int am = std::abs(m);
+    double N = 1.0 / (std::pow(2.0, am) * factorial(l)) *
+               std::sqrt(2.0 * factorial(l + am) * factorial(l - am) / (m == 0 ? 2.0 : 1.0));
+    int v2_lo = (m < 0) ? 1 : 0;
+    int v2_hi = (m < 0) ? 2 * ((am - 1) / 2) + 1 : 2 * (am / 2);
+    for (int t = 0; t <= (l - am) / 2; t++)
+      for (int u = 0; u <= t; u++)
+        for (int v2 = v2_lo; v2 <= v2_hi; v2 += 2) {
+          int sgn_exp = t + (v2 - v2_lo) / 2;
+          double C = ((sgn_exp % 2) ? -1.0 : 1.0) * std::pow(0.25, t) * binom(l, t) *
+                     binom(l - t, am + t) * binom(t, u) * binom(am, v2);
+          int ex = 2 * t + am - 2 * u - v2;
+          int ey = 2 * u + v2;
+          int ez = l - 2 * t - am;
+          if (ex < 0 || ey < 0 || ez < 0)
+            continue;
+          T[(m + l) * nc + cart_index(l, ex, ey)] += N * C;
+        }
+  }
+  return T;
+}
+
+inline double ipow(double x, int n) {
+  double r = 1.0;
+  for (int i = 0; i < n; i++)
+    r *= x;
+  return r;
+}
+
+// Collocation of one shell at points; out[comp][func][p], comp 0 = value,
+// 1..3 = d/dx, d/dy, d/dz.  Restates what src/gto/gto.cpp:212-287 obtains from
+// gau2grid (contracted Cartesian Gaussians, CCA order, optional spherical
+// transform) including the common_fac scaling.
+void collocate(int l, bool pure, int nprim, const double *exps, const double *coefs,
+               const double *A, long n, const double *xyz, long stride, int deriv,
+               double *out, long out_stride) {
+  const int nc = ncart(l);
+  const int nf = pure ? 2 * l + 1 : nc;
+  std::vector<double> T;
+  if (pure)
+    T = spherical_transform(l);
+  const double fac = common_fac(l, pure);
+  std::vector<double> cart(4 * nc);
+  for (long p = 0; p < n; p++) {
+    double x = xyz[3 * p] - A[0], y = xyz[3 * p + 1] - A[1], z = xyz[3 * p + 2] - A[2];
+    double r2 = x * x + y * y + z * z;
+    double R = 0.0, dR = 0.0;
+    for (int k = 0; k < nprim; k++) {
+      double e = coefs[k] * std::exp(-exps[k] * r2);
+      R += e;
+      dR += -2.0 * exps[k] * e;
+    }
+    for (int a = l; a >= 0; a--)
+      for (int b = l - a; b >= 0; b--) {
+        int c = l - a - b;
+        int i = cart_index(l, a, b);
+        double mono = ipow(x, a) * ipow(y, b) * ipow(z, c);
+        cart[i] = mono * R;
+        if (deriv) {
+          double gx = (a > 0 ? a * ipow(x, a - 1) * ipow(y, b) * ipow(z, c) : 0.0);
+          double gy = (b > 0 ? b * ipow(x, a) * ipow(y, b - 1) * ipow(z, c) : 0.0);
+          double gz = (c > 0 ? c * ipow(x, a) * ipow(y, b) * ipow(z, c - 1) : 0.0);
+          cart[nc + i] = gx * R + mono * x * dR;
+          cart[2 * nc + i] = gy * R + mono * y * dR;
+          cart[3 * nc + i] = gz * R + mono * z * dR;
+        }
+      }
+    int ncomp = deriv ? 4 : 1;
+    for (int q = 0; q < ncomp; q++)
+      for (int f = 0; f < nf; f++) {
+        double v;
+        if (pure) {
+          v = 0.0;
+          for (int i = 0; i < nc; i++)
+            v += T[f * nc + i] * cart[q * nc + i];
+        } else {
+          v = cart[q * nc + f];
+        }
+        out[(q * nf + f) * out_stride + p] = v * fac;
+      }
+  }
+}
+
+struct Basis {
+  int nsh;
+  const int *l, *nprim, *off;
+  const double *exps, *coefs, *origin;
+  bool pure;
+  std::vector<int> first_bf;
+  int nbf;
+  int size(int s) const { return pure ? 2 * l[s] + 1 : ncart(l[s]); }
+};
+
+// src/gto/gto.cpp:18-67: first radius (0.5 .. 30 Bohr in 0.1 steps, along
+// +x from the shell centre) where max |phi| drops below the threshold.
+void decay_cutoff(const Basis &bs, double threshold, double *ext) {
+  const double max_radius = 30.0, increment = 0.1, min_radius = 0.5;
+  const int npts = static_cast<int>((max_radius - min_radius) / increment) + 1;
+  const double step = (max_radius - min_radius) / (npts - 1); // Eigen LinSpaced
+  std::vector<double> xyz(3 * npts);
+  for (int s = 0; s < bs.nsh; s++) {
+    const double *A = bs.origin + 3 * s;
+    for (int i = 0; i < npts; i++) {
+      double xi = (i == npts - 1) ? max_radius : min_radius + i * step;
+      xyz[3 * i] = xi + A[0];
+      xyz[3 * i + 1] = 0.0 + A[1];
+      xyz[3 * i + 2] = 0.0 + A[2];
+    }
+    int nf = bs.size(s);
+    std::vector<double> vals(nf * npts);
+    collocate(bs.l[s], bs.pure, bs.nprim[s], bs.exps + bs.off[s], bs.coefs + bs.off[s], A,
+              npts, xyz.data(), 3, 0, vals.data(), npts);
+    for (int i = 0; i < npts; i++) {
+      ext[s] = i * increment + min_radius;
+      double v = 0.0;
+      for (int f = 0; f < nf; f++)
+        v = std::max(v, std::fabs(vals[f * npts + i]));
+      if (v < threshold)
+        break;
+    }
+  }
+}
+
+// src/numint/spatial_grid_hierarchy.cpp:7-31 (bit dilation, 21 bits/axis)
+inline uint64_t dilate3(uint64_t x) {
+  x &= 0x1fffff;
+  x = (x | (x << 32)) & 0x1f00000000ffffULL;
+  x = (x | (x << 16)) & 0x1f0000ff0000ffULL;
+  x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
+  x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
+  x = (x | (x << 2)) & 0x1249249249249249ULL;
+  return x;
+}
+
+struct Leaf {
+  long off, cnt;
+  double c[3], r;
+};
+
+// src/numint/spatial_grid_hierarchy.cpp:40-147
+std::vector<Leaf> morton_leaves(long n, const double *pts, long target, long min_leaf,
+                                long max_leaf, std::vector<long> &perm) {
+  std::vector<Leaf> leaves;
+  perm.assign(n, 0);
+  if (n == 0)
+    return leaves;
+  double lo[3], hi[3], ext[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = hi[d] = pts[d];
+  }
+  for (long i = 0; i < n; i++)
+    for (int d = 0; d < 3; d++) {
+      lo[d] = std::min(lo[d], pts[3 * i + d]);
+      hi[d] = std::max(hi[d], pts[3 * i + d]);
+    }
+  for (int d = 0; d < 3; d++) {
+    ext[d] = hi[d] - lo[d];
+    if (ext[d] < 1e-10)
+      ext[d] = 1.0;
+  }
+  const uint64_t scale = (1ULL << 21) - 1;
+  std::vector<std::pair<uint64_t, long>> codes(n);
+  for (long i = 0; i < n; i++) {
+    uint64_t q[3];
+    for (int d = 0; d < 3; d++) {
+      double u = (pts[3 * i + d] - lo[d]) / ext[d];
+      u = std::min(std::max(u, 0.0), 1.0);
+      q[d] = static_cast<uint64_t>(u * scale);
+    }
+    codes[i] = {dilate3(q[0]) | (dilate3(q[1]) << 1) | (dilate3(q[2]) << 2), i};
+  }
+  std::sort(codes.begin(), codes.end());
+  for (long i = 0; i < n; i++)
+    perm[i] = codes[i].second;
+  long off = 0;
+  while (off < n) {
+    long rem = n - off, cnt;
+    if (rem <= max_leaf)
+      cnt = rem;
+    else if (rem < 2 * min_leaf)
+      cnt = rem / 2;
+    else
+      cnt = std::min(target, rem);
+    Leaf lf;
+    lf.off = off;
+    lf.cnt = cnt;
+    double c[3] = {0, 0, 0};
+    for (long i = off; i < off + cnt; i++)
+      for (int d = 0; d < 3; d++)
+        c[d] += pts[3 * perm[i] + d];
+    for (int d = 0; d < 3; d++)
+      lf.c[d] = c[d] / cnt;
+    double r = 0.0;
+    for (long i = off; i < off + cnt; i++) {
+      double dx = pts[3 * perm[i]] - lf.c[0], dy = pts[3 * perm[i] + 1] - lf.c[1],
+             dz = pts[3 * perm[i] + 2] - lf.c[2];
+      r = std::max(r, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    lf.r = r;
+    leaves.push_back(lf);
+    off += cnt;
+  }
+  return leaves;
+}
+
+} // namespace
+
+extern "C" int oracle_collocation(int l, int pure, int nprim, const double *exps,
+                                  const double *coefs, const double *origin, long n,
+                                  const double *xyz, int deriv, double *out) {
+  collocate(l, pure != 0, nprim, exps, coefs, origin, n, xyz, 3, deriv, out, n);
+  return 0;
+}
+
+extern "C" void oracle_decay_cutoff(int nsh, const int *sh_l, const int *sh_nprim,
+                                    const int *sh_off, const double *exps,
+                                    const double *coefs, const double *sh_origin, int pure,
+                                    double threshold, double *extents) {
+  Basis bs{nsh, sh_l, sh_nprim, sh_off, exps, coefs, sh_origin, pure != 0, {}, 0};
+  decay_cutoff(bs, threshold, extents);
+}
+
+extern "C" long oracle_morton_leaves(long n, const double *points, long target,
+                                     long min_leaf, long max_leaf, long *perm,
+                                     long *leaf_off, long *leaf_cnt, double *centres,
+                                     double *radii) {
+  std::vector<double> xyz(3 * n);
+  for (long i = 0; i < n; i++)
+    for (int d = 0; d < 3; d++)
+      xyz[3 * i + d] = points[3 * i + d];
+  std::vector<long> p;
+  auto leaves = morton_leaves(n, xyz.data(), target, min_leaf, max_leaf, p);
+  if (perm)
+    std::memcpy(perm, p.data(), sizeof(long) * n);
+  for (size_t i = 0; i < leaves.size(); i++) {
+    if (leaf_off)
+      leaf_off[i] = leaves[i].off;
+    if (leaf_cnt)
+      leaf_cnt[i] = leaves[i].cnt;
+    if (centres)
+      for (int d = 0; d < 3; d++)
+        centres[3 * i + d] = leaves[i].c[d];
+    if (radii)
+      radii[i] = leaves[i].r;
+  }
+  return static_cast<long>(leaves.size());
+}
+
+// include/occ/dft/dft.h:192-388 (screened path), src/dft/dft_kernels.cpp:9-70,
+// src/gto/density.cpp:8-43, src/dft/xc_potential_matrix.cpp:9-41.
+extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
+                               const int *sh_off, const double *exps, const double *coefs,
+                               const double *sh_origin, int pure, long npts,
+                               const double *points, const double *weights, const double *D,
+                               int nfunc, const int *func_ids, const double *func_coefs,
+                               double screen_threshold, double density_threshold,
+                               long leaf_target, long leaf_min, long leaf_max, int nthreads,
+                               long leaf_subset, double *V, double *exc_out,
+                               double *nelec_out) {
+  Basis bs{nsh, sh_l, sh_nprim, sh_off, exps, coefs, sh_origin, pure != 0, {}, 0};
+  bs.first_bf.resize(nsh);
+  int nbf = 0;
+  for (int s = 0; s < nsh; s++) {
+    bs.first_bf[s] = nbf;
+    nbf += bs.size(s);
+  }
+  bs.nbf = nbf;
+  int deriv = 0;
+  for (int f = 0; f < nfunc; f++) {
+    if (oracle_functional_is_gga(func_ids[f]) < 0)
+      return -1;
+    deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
+  }
+  std::vector<double> ext(nsh);
+  decay_cutoff(bs, screen_threshold, ext.data());
+  std::vector<long> perm;
+  auto leaves = morton_leaves(npts, points, leaf_target, leaf_min, leaf_max, perm);
+  long nleaves = static_cast<long>(leaves.size());
+  if (leaf_subset > 0 && leaf_subset < nleaves)
+    nleaves = leaf_subset;
+
+  // D2 = 2 D (dft.h:205)
+  std::vector<double> D2(static_cast<size_t>(nbf) * nbf);
+  for (size_t i = 0; i < D2.size(); i++)
+    D2[i] = 2.0 * D[i];
+
+#ifdef _OPENMP
+  int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  int nt = 1;
+  (void)nthreads;
+#endif
+  std::vector<std::vector<double>> Vloc(nt);
+  std::vector<double> eloc(nt, 0.0), nloc(nt, 0.0);
+
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    std::vector<double> &K = Vloc[tid];
+    K.assign(static_cast<size_t>(nbf) * nbf, 0.0);
+    std::vector<double> xyz, w, phi, Dloc, Dphi, rho, sigma, exc, vrho, vsig, e1, v1, s1, Y,
+        Kb;
+    std::vector<int> sig, loc0;
+#pragma omp for schedule(dynamic, 4)
+    for (long li = 0; li < nleaves; li++) {
+      const Leaf &lf = leaves[li];
+      const long n = lf.cnt;
+      if (n == 0)
+        continue;
+      sig.clear();
+      for (int s = 0; s < nsh; s++) {
+        const double *A = sh_origin + 3 * s;
+        double dx = A[0] - lf.c[0], dy = A[1] - lf.c[1], dz = A[2] - lf.c[2];
+        double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (dist - ext[s] < lf.r)
+          sig.push_back(s);
+      }
+      if (sig.empty())
+        continue;
+      loc0.assign(sig.size(), 0);
+      int m = 0;
+      for (size_t k = 0; k < sig.size(); k++) {
+        loc0[k] = m;
+        m += bs.size(sig[k]);
+      }
+      xyz.resize(3 * n);
+      w.resize(n);
+      for (long i = 0; i < n; i++) {
+        long o = perm[lf.off + i];
+        for (int d = 0; d < 3; d++)
+          xyz[3 * i + d] = points[3 * o + d];
+        w[i] = weights[o];
+      }
+      // gather D_local (dft.h:340-348)
+      Dloc.assign(static_cast<size_t>(m) * m, 0.0);
+      for (size_t a = 0; a < sig.size(); a++)
+        for (size_t b = 0; b < sig.size(); b++) {
+          int la = bs.size(sig[a]), lb = bs.size(sig[b]);
+          for (int j = 0; j < lb; j++)
+            for (int i = 0; i < la; i++)
+              Dloc[(loc0[b] + j) * static_cast<size_t>(m) + loc0[a] + i] =
+                  D2[(bs.first_bf[sig[b]] + j) * static_cast<size_t>(nbf) + bs.first_bf[sig[a]] + i];
+        }
+      // collocation: phi[comp][m][n]
+      const int ncomp = deriv ? 4 : 1;
+      phi.assign(static_cast<size_t>(ncomp) * m * n, 0.0);
+      {
+        std::vector<double> tmp;
+        for (size_t k = 0; k < sig.size(); k++) {
+          int s = sig[k], nf = bs.size(s);
+          tmp.assign(static_cast<size_t>(ncomp) * nf * n, 0.0);
+          collocate(sh_l[s], bs.pure, sh_nprim[s], exps + sh_off[s], coefs + sh_off[s],
+                    sh_origin + 3 * s, n, xyz.data(), 3, deriv, tmp.data(), n);
+          for (int q = 0; q < ncomp; q++)
+            for (int f = 0; f < nf; f++)
+              std::memcpy(&phi[(static_cast<size_t>(q) * m + loc0[k] + f) * n],
+                          &tmp[(static_cast<size_t>(q) * nf + f) * n], sizeof(double) * n);
+        }
+      }
+      // density (src/gto/density.cpp:33-43): Dphi = phi * D, rho = rowsum(phi o Dphi)
+      Dphi.assign(static_cast<size_t>(m) * n, 0.0);
+      for (int j = 0; j < m; j++) {
+        double *out = &Dphi[static_cast<size_t>(j) * n];
+        for (int k = 0; k < m; k++) {
+          double d = Dloc[static_cast<size_t>(j) * m + k];
+          if (d == 0.0)
+            continue;
+          const double *ph = &phi[static_cast<size_t>(k) * n];
+          for (long p = 0; p < n; p++)
+            out[p] += ph[p] * d;
+        }
+      }
+      rho.assign(4 * n, 0.0);
+      for (int j = 0; j < m; j++) {
+        const double *dp = &Dphi[static_cast<size_t>(j) * n];
+        const double *ph = &phi[static_cast<size_t>(j) * n];
+        for (long p = 0; p < n; p++)
+          rho[p] += ph[p] * dp[p];
+        if (deriv)
+          for (int q = 1; q < 4; q++) {
+            const double *g = &phi[(static_cast<size_t>(q) * m + j) * n];
+            for (long p = 0; p < n; p++)
+              rho[q * n + p] += 2.0 * g[p] * dp[p];
+          }
+      }
+      // totals and block skip (src/dft/dft_kernels.cpp:27-40)
+      double maxrho = -1e300;
+      for (long p = 0; p < n; p++) {
+        nloc[tid] += rho[p] * w[p];
+        maxrho = std::max(maxrho, rho[p]);
+      }
+      if (maxrho < density_threshold)
+        continue;
+      // functional (src/dft/functional.cpp:18-65, summed over components)
+      sigma.assign(n, 0.0);
+      if (deriv)
+        for (long p = 0; p < n; p++)
+          sigma[p] = rho[n + p] * rho[n + p] + rho[2 * n + p] * rho[2 * n + p] +
+                     rho[3 * n + p] * rho[3 * n + p];
+      exc.assign(n, 0.0);
+      vrho.assign(n, 0.0);
+      vsig.assign(n, 0.0);
+      e1.resize(n);
+      v1.resize(n);
+      s1.resize(n);
+      for (int f = 0; f < nfunc; f++) {
+        std::fill(s1.begin(), s1.end(), 0.0);
+        oracle_functional(func_ids[f], n, rho.data(), sigma.data(), e1.data(), v1.data(),
+                          s1.data());
+        double c = func_coefs ? func_coefs[f] : 1.0;
+        for (long p = 0; p < n; p++) {
+          exc[p] += c * e1[p];
+          vrho[p] += c * v1[p];
+          vsig[p] += c * s1[p];
+        }
+      }
+      // weight_by (include/occ/dft/functional.h:460-470)
+      for (long p = 0; p < n; p++) {
+        exc[p] *= w[p];
+        vrho[p] *= w[p];
+        vsig[p] *= w[p];
+      }
+      for (long p = 0; p < n; p++)
+        eloc[tid] += rho[p] * exc[p];
+      // V block (src/dft/xc_potential_matrix.cpp:9-41)
+      Y.assign(static_cast<size_t>(m) * n, 0.0);
+      for (int j = 0; j < m; j++) {
+        const double *ph = &phi[static_cast<size_t>(j) * n];
+        double *y = &Y[static_cast<size_t>(j) * n];
+        if (!deriv) {
+          for (long p = 0; p < n; p++)
+            y[p] = ph[p] * vrho[p];
+        } else {
+          const double *gx = &phi[(static_cast<size_t>(1) * m + j) * n];
+          const double *gy = &phi[(static_cast<size_t>(2) * m + j) * n];
+          const double *gz = &phi[(static_cast<size_t>(3) * m + j) * n];
+          for (long p = 0; p < n; p++)
+            y[p] = 0.5 * ph[p] * vrho[p] + 2.0 * gx[p] * (rho[n + p] * vsig[p]) +
+                   2.0 * gy[p] * (rho[2 * n + p] * vsig[p]) +
+                   2.0 * gz[p] * (rho[3 * n + p] * vsig[p]);
+        }
+      }
+      Kb.assign(static_cast<size_t>(m) * m, 0.0);
+      for (int j = 0; j < m; j++)
+        for (int i = 0; i < m; i++) {
+          const double *a = &phi[static_cast<size_t>(i) * n];
+          const double *b = &Y[static_cast<size_t>(j) * n];
+          double acc = 0.0;
+          for (long p = 0; p < n; p++)
+            acc += a[p] * b[p];
+          Kb[static_cast<size_t>(j) * m + i] = acc;
+        }
+      if (deriv) { // V = K + K^T
+        for (int j = 0; j < m; j++)
+          for (int i = 0; i < j; i++) {
+            double s = Kb[static_cast<size_t>(j) * m + i] + Kb[static_cast<size_t>(i) * m + j];
+            Kb[static_cast<size_t>(j) * m + i] = s;
+            Kb[static_cast<size_t>(i) * m + j] = s;
+          }
+        for (int i = 0; i < m; i++)
+          Kb[static_cast<size_t>(i) * m + i] *= 2.0;
+      }
+      // scatter (dft.h:361-369)
+      for (size_t a = 0; a < sig.size(); a++)
+        for (size_t b = 0; b < sig.size(); b++) {
+          int la = bs.size(sig[a]), lb = bs.size(sig[b]);
+          for (int j = 0; j < lb; j++)
+            for (int i = 0; i < la; i++)
+              K[(bs.first_bf[sig[b]] + j) * static_cast<size_t>(nbf) + bs.first_bf[sig[a]] + i] +=
+                  Kb[(loc0[b] + j) * static_cast<size_t>(m) + loc0[a] + i];
+        }
+    }
+  }
+  // reduction (dft.h:374-380)
+  std::memset(V, 0, sizeof(double) * nbf * nbf);
+  double E = 0.0, Ne = 0.0;
+  for (int t = 0; t < nt; t++) {
+    for (size_t i = 0; i < static_cast<size_t>(nbf) * nbf; i++)
+      V[i] += Vloc[t][i];
+    E += eloc[t];
+    Ne += nloc[t];
+  }
+  *exc_out = E;
+  if (nelec_out)
+    *nelec_out = Ne;
+  return 0;
+}

@@ -1,0 +1,79 @@
+// CPU oracle for the Kohn-Sham XC build -- TEST INFRASTRUCTURE ONLY.
+//
+// A plain FP64 restatement of OCC's restricted XC build
+// (include/occ/dft/dft.h:192-388, compute_K_dft<deriv, Restricted>), used by
+// the test suite, the smoke check and bench.py's CPU baseline as the checker.
+// Nothing in the product links, loads or calls this library.
+//
+// Parity pins: the collocation is checked against the reference's own
+// gau2grid (compiled under oracle/_ref on the development machine) and the
+// PBE exchange known-answer test of tests/dft_tests.cpp:71-111.  The other
+// functionals (Slater, VWN, B88, LYP, PBE correlation) are restated from the
+// published papers because Libxc 6.2.2 (the reference's functional library,
+// fetched at configure time) is not available; their derivatives are checked
+// against finite differences of the energy density.
+#pragma once
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Functional identifiers use Libxc's public numbers.
+enum {
+  ORC_LDA_X = 1,
+  ORC_LDA_C_VWN = 7,
+  ORC_LDA_C_VWN_RPA = 8,
+  ORC_LDA_C_VWN_3 = 30,
+  ORC_GGA_X_PBE = 101,
+  ORC_GGA_X_B88 = 106,
+  ORC_GGA_C_PBE = 130,
+  ORC_GGA_C_LYP = 131,
+  ORC_HYB_GGA_XC_B3LYP = 402,
+  ORC_HYB_GGA_XC_B3LYP5 = 475,
+};
+
+// Evaluate one functional on n points (unpolarised).  exc is energy per
+// particle, vrho = d(rho*exc)/drho, vsigma = d(rho*exc)/dsigma (GGA only;
+// may be null for LDA).  Returns 0, or -1 for an unknown id.
+int oracle_functional(int id, long n, const double *rho, const double *sigma,
+                      double *exc, double *vrho, double *vsigma);
+int oracle_functional_is_gga(int id);
+
+// Collocation of one shell (values and, if deriv, gradients) at n points
+// (xyz interleaved).  Output layout: [ncomp][nfunc][n].
+int oracle_collocation(int l, int pure, int nprim, const double *exps,
+                       const double *coefs, const double *origin, long n,
+                       const double *xyz, int deriv, double *out);
+
+// Shell decay radii (src/gto/gto.cpp:18-67).
+void oracle_decay_cutoff(int nsh, const int *sh_l, const int *sh_nprim,
+                         const int *sh_off, const double *exps,
+                         const double *coefs, const double *sh_origin, int pure,
+                         double threshold, double *extents);
+
+// Morton sort + leaves (src/numint/spatial_grid_hierarchy.cpp:35-147).
+// perm: sorted -> original index (n); leaves: (offset, count) pairs, returns
+// the number of leaves; centres (3 per leaf) and radii may be null.
+long oracle_morton_leaves(long n, const double *points, long target,
+                          long min_leaf, long max_leaf, long *perm,
+                          long *leaf_off, long *leaf_cnt, double *centres,
+                          double *radii);
+
+// The whole restricted XC build.  D is OCC's mo.D (nbf x nbf, column-major);
+// V (nbf x nbf) receives V_xc = -K of compute_JK.  func ids/coefs give the
+// components summed as in src/dft/dft_kernels.cpp:55-58 (coefficients are
+// Libxc-internal mixture weights, not OCC's never-applied scale factors).
+// leaf_subset > 0 restricts the build to the first leaf_subset leaves (used
+// only to time a bounded CPU sample).  Returns 0 on success.
+int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
+                    const int *sh_off, const double *exps, const double *coefs,
+                    const double *sh_origin, int pure, long npts,
+                    const double *points, const double *weights,
+                    const double *D, int nfunc, const int *func_ids,
+                    const double *func_coefs, double screen_threshold,
+                    double density_threshold, long leaf_target, long leaf_min,
+                    long leaf_max, int nthreads, long leaf_subset, double *V,
+                    double *exc_out, double *nelec_out);
+
+#ifdef __cplusplus
+}
+#endif
