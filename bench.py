@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 XC build.
+
+Workload (one "step" = one XC build: D in -> V_xc, E_xc out, grid, weights
+and screening already resident): a 32-water cluster (centres uniform in a
+seeded 10 Angstrom cube, O-O >= 2.6 Angstrom, random orientations),
+def2-SVP (768 pure AOs), PBE, OCC's default grid, mo.D = C C^T with 160
+occupied columns of a seeded random orthonormal matrix.  Synthetic inputs
+with the benchmark configuration's shapes (no dataset is involved).
+
+value    builds/s of the headline precision with D, V on the device
+e2e      builds/s through the public C ABI call (occ_xc_compute_vxc) with
+         host buffers, H2D of D and D2H of V and E_xc inside the timed region
+Both precisions (plain FP64 and mixed) are timed back to back on the same
+GPU and their E_xc difference is reported.
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/) on the host cores instead; the reference itself (OCC) cannot be
+built here (its dependencies are fetched over the network at configure time).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "water32_def2svp_pbe"
+METRIC = "XC builds/s & p50/p99 ms, mixed vs FP64 on same GPU at |dE_xc|<=1e-6 Ha"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_workload(seed=0):
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(32, box=10.0, seed=seed)
+    basis = wl.basis_for(mol, "def2-svp")
+    D = wl.random_density(basis.nbf(), 160, seed=seed)
+    return mol, basis, D
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def device_timing(dft, D, precision, steps, warmup, torch):
+    """Builds with D, V, E_xc resident on the device; CUDA events on the
+    launching stream.  Returns (total_ms, per_step_ms, exc)."""
+    lib = dft.ctx.lib
+    nbf = D.shape[0]
+    dD = torch.tensor(np.asfortranarray(D).ravel(order="F"), device="cuda", dtype=torch.float64)
+    dV = torch.zeros(nbf * nbf, device="cuda", dtype=torch.float64)
+    dE = torch.zeros(2, device="cuda", dtype=torch.float64)
+    torch.cuda.synchronize()
+    # a dedicated stream: the library's kernels and the timing events share it
+    stream = torch.cuda.Stream()
+    assert stream.cuda_stream != 0
+
+    def one():
+        rc = lib.occ_xc_compute_vxc_device(dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), precision,
+                                           C.c_void_p(dV.data_ptr()), C.c_void_p(dE.data_ptr()),
+                                           C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(dft.ctx.error())
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for i in range(steps):
+        one()
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+    return ev[0].elapsed_time(ev[-1]), per, float(dE[0].item()), dV
+
+
+def e2e_timing(dft, D, precision, steps, warmup):
+    for _ in range(warmup):
+        dft.compute_vxc(D, precision)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dft.compute_vxc(D, precision)
+    return (time.perf_counter() - t0) * 1e3
+
+
+def kernel_profile(dft, D, precision, nbuilds, torch):
+    lib = dft.ctx.lib
+    lib.occ_xc_profile_enable.argtypes = [C.c_void_p, C.c_int]
+    lib.occ_xc_profile_reset.argtypes = [C.c_void_p]
+    lib.occ_xc_profile_count.argtypes = [C.c_void_p]
+    lib.occ_xc_profile_entry.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_char_p),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_long)]
+    lib.occ_xc_profile_reset(dft.ctx.h)
+    lib.occ_xc_profile_enable(dft.ctx.h, 1)
+    for _ in range(nbuilds):
+        dft.compute_vxc(D, precision)
+    n = lib.occ_xc_profile_count(dft.ctx.h)
+    out = {}
+    for i in range(n):
+        name, ms, cnt = C.c_char_p(), C.c_double(), C.c_long()
+        lib.occ_xc_profile_entry(dft.ctx.h, i, C.byref(name), C.byref(ms), C.byref(cnt))
+        out[name.value.decode()] = (ms.value, cnt.value)
+    lib.occ_xc_profile_enable(dft.ctx.h, 0)
+    lib.occ_xc_profile_reset(dft.ctx.h)
+    return out
+
+
+def leaf_stats(dft):
+    info = dft.info()
+    lib = dft.ctx.lib
+    n = info["nleaves"]
+    cnt = np.zeros(n, dtype=np.int32)
+    m = np.zeros(n, dtype=np.int32)
+    lib.occ_xc_molecule_leaves.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.occ_xc_molecule_leaves(dft.h, cnt.ctypes.data, m.ctypes.data)
+    return cnt, m
+
+
+def cpu_baseline(basis, P, W, D, target_s=15.0):
+    """Oracle (CPU restatement of the reference algorithm) on every host core,
+    on a strided sample of leaves; scaled to builds/s by the sampled share of
+    the contraction FLOPs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    cores = os.cpu_count() or 1
+    L = oracle.lib()
+    L.oracle_last_flops.restype = C.c_double
+    L.oracle_total_flops.restype = C.c_double
+    stride = 64
+    t0 = time.perf_counter()
+    oracle.xc_build(basis, P, W, D, "pbe", nthreads=cores, leaf_stride=stride)
+    dt = time.perf_counter() - t0
+    f_sample = L.oracle_last_flops()
+    f_all = L.oracle_total_flops()
+    # grow the sample to about target_s of work
+    stride2 = max(1, int(stride * dt / target_s)) if dt > 0 else stride
+    if stride2 < stride:
+        t0 = time.perf_counter()
+        oracle.xc_build(basis, P, W, D, "pbe", nthreads=cores, leaf_stride=stride2)
+        dt = time.perf_counter() - t0
+        f_sample = L.oracle_last_flops()
+        stride = stride2
+    builds_per_s = (f_sample / f_all) / dt
+    return {"value": builds_per_s, "unit": "builds/s", "cores": cores, "kind": "port",
+            "sample": f"every {stride}th Morton leaf ({100 * f_sample / f_all:.1f}% of the "
+                      f"contraction FLOPs) of the same build, {dt:.1f} s wall on {cores} threads, "
+                      f"scaled by the FLOP share"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    _, basis, D = make_workload()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import host_grid
+    P, W = host_grid(basis)
+    vals = []
+    for _ in range(max(1, args.warmup // 3)):
+        cpu_baseline(basis, P, W, D, target_s=5.0)
+    cb = None
+    for _ in range(args.steps if args.steps <= 3 else 3):
+        cb = cpu_baseline(basis, P, W, D, target_s=10.0)
+        vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "builds/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": len(vals), "warmup": args.warmup,
+            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "note": "CPU restatement of the reference algorithm "
+                       "(oracle/); OCC itself cannot be built offline"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "builds/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+
+    import occ_gb300 as og
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    mol, basis, D = make_workload(seed=0)
+    dft = og.DFT("pbe", basis, device=local)
+    info = dft.info()
+    lib = dft.ctx.lib
+    lib.occ_xc_launch_count.restype = C.c_long
+    lib.occ_xc_launch_count.argtypes = [C.c_void_p]
+
+    have_mixed = True
+    try:
+        dft.compute_vxc(D, og.MIXED)
+    except og.XCError:
+        have_mixed = False
+    head = og.MIXED if (have_mixed and args.precision != "fp64") else og.FP64
+
+    results = {}
+    precisions = [og.FP64] + ([og.MIXED] if have_mixed else [])
+    clocks = None
+    for prec in precisions:
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = lib.occ_xc_launch_count(dft.ctx.h)
+        with ClockSampler(local) as cs:
+            total_ms, per, exc, _ = device_timing(dft, D, prec, args.steps, args.warmup, torch)
+        launches = lib.occ_xc_launch_count(dft.ctx.h) - l0
+        if world > 1:
+            t = torch.tensor([total_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total_ms = float(t.item())
+        results[prec] = dict(total_ms=total_ms, per=per, exc=exc,
+                             launches=launches * args.steps // (args.steps + args.warmup))
+        if prec == head:
+            clocks = cs.summary()
+    e2e_ms = e2e_timing(dft, D, head, args.steps, max(1, args.warmup))
+    prof = kernel_profile(dft, D, head, 3, torch)
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    r = results[head]
+    ms_per = r["total_ms"] / args.steps
+    value = world * args.steps / (r["total_ms"] / 1e3)
+    nbf = info["nbf"]
+    # dominant kernel and its roofline
+    tot = sum(v[0] for v in prof.values())
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_n) = dom
+    dom_avg_ms = dom_ms / dom_n
+    flops_half = info["flops_per_build"] / 2  # one of the two contractions
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    if "f64" in dom_name or head == og.FP64:
+        achieved = flops_half / (dom_avg_ms / 1e3) / 1e12
+        roof = {"bound": "fp64", "achieved": achieved, "peak": None, "unit": "TFLOP/s",
+                "frac": None, "traffic": None, "kernel": dom_name,
+                "note": "FP64 DFMA pipe; MEASURED_PEAKS.json has no FP64 figure"}
+    else:
+        peak = peaks.get("bf16_tflops", 1900.0)
+        achieved = 3 * 2 * flops_half / (dom_avg_ms / 1e3) / 1e12  # 3 TF32 products, bf16-equivalent
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "kernel": dom_name}
+    roof["kernel_share"] = dom_ms / tot if tot else None
+    roof["kernels_ms_per_build"] = {k: v[0] / v[1] for k, v in prof.items()}
+
+    out = {
+        "metric": METRIC,
+        "value": value, "unit": "builds/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == og.FP64 else "tf32x3+f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "natoms": len(mol), "nbf": nbf,
+                   "npoints": info["npoints"], "nleaves": info["nleaves"],
+                   "flops_per_build": info["flops_per_build"], "precision": "fp64" if head == og.FP64 else "mixed",
+                   "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2: per-build workspace "
+                         f"{info['workspace_bytes'] / 1e9:.1f} GB > 129 MB"},
+        "p50_ms": float(np.percentile(r["per"], 50)), "p99_ms": float(np.percentile(r["per"], 99)),
+        "fp64": {"builds_per_s": args.steps / (results[og.FP64]["total_ms"] / 1e3),
+                 "p50_ms": float(np.percentile(results[og.FP64]["per"], 50)),
+                 "p99_ms": float(np.percentile(results[og.FP64]["per"], 99)),
+                 "exc": results[og.FP64]["exc"]},
+        "e2e": {"value": world * args.steps / (e2e_ms / 1e3), "unit": "builds/s",
+                "h2d_bytes_per_step": nbf * nbf * 8, "d2h_bytes_per_step": nbf * nbf * 8 + 16},
+        "gpu_launches": int(r["launches"]),
+        "roofline": roof,
+        "clocks": clocks,
+    }
+    if og.MIXED in results:
+        m = results[og.MIXED]
+        out["mixed"] = {"builds_per_s": args.steps / (m["total_ms"] / 1e3),
+                        "p50_ms": float(np.percentile(m["per"], 50)),
+                        "p99_ms": float(np.percentile(m["per"], 99)), "exc": m["exc"],
+                        "dE_xc_vs_fp64": m["exc"] - results[og.FP64]["exc"]}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        P, W = dft.grid()
+        out["cpu_baseline"] = cpu_baseline(basis, P, W, D)
+    print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

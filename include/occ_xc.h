@@ -135,6 +135,24 @@ int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *
 int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
                               int precision, double *d_V, double *d_exc2, void *stream);
 
+/* Per-leaf view of the build plan (for tests and tooling): for each leaf
+ * that has at least one significant shell, in Morton order, its point count
+ * and its significant-AO count m_b.  Arrays sized nleaves (molecule info). */
+int occ_xc_molecule_leaves(const occ_xc_molecule *mol, int *npoints, int *nbf_local);
+
+/* Device-side kernel timing, the analogue of OCC's timing categories
+ * (include/occ/core/timings.h:11-141, e.g. dft_xc): when enabled, every kernel
+ * a build launches is bracketed by CUDA events on its stream.
+ * occ_xc_profile_count synchronises and returns the number of kernel names;
+ * occ_xc_profile_entry reads one (name valid until the next reset). */
+int occ_xc_profile_enable(occ_xc_context *ctx, int on);
+int occ_xc_profile_reset(occ_xc_context *ctx);
+int occ_xc_profile_count(occ_xc_context *ctx);
+int occ_xc_profile_entry(occ_xc_context *ctx, int i, const char **name, double *total_ms,
+                         long *launches);
+/* Number of kernels the library has launched on this context so far. */
+long occ_xc_launch_count(const occ_xc_context *ctx);
+
 #ifdef __cplusplus
 }
 #endif

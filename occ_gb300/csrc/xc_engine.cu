@@ -239,12 +239,19 @@ MolDev Molecule::dev() const {
 void Molecule::build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st) {
   const MolDev m = dev();
   const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
+  Context &c = *ctx;
   cuda_check(cudaMemsetAsync(dV, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
-  launch_colloc_f64(m, deriv, d_ws, st);
-  launch_rho_f64(m, deriv, dD, d_ws, d_slabs, static_cast<int>(slabs.size()), d_rho, st);
-  launch_func(m, deriv, fs, bs.density_threshold, d_rho, d_coef, d_epart, st);
-  launch_vxc_f64(m, deriv, d_ws, d_coef, d_tiles, static_cast<int>(tiles.size()), dV, st);
-  launch_reduce(d_epart, m.nleaves, dout2, st);
+  c.launch("colloc_f64", st, [&] { launch_colloc_f64(m, deriv, d_ws, st); });
+  c.launch("rho_f64", st, [&] {
+    launch_rho_f64(m, deriv, dD, d_ws, d_slabs, static_cast<int>(slabs.size()), d_rho, st);
+  });
+  c.launch("func", st, [&] {
+    launch_func(m, deriv, fs, bs.density_threshold, d_rho, d_coef, d_epart, st);
+  });
+  c.launch("vxc_f64", st, [&] {
+    launch_vxc_f64(m, deriv, d_ws, d_coef, d_tiles, static_cast<int>(tiles.size()), dV, st);
+  });
+  c.launch("reduce", st, [&] { launch_reduce(d_epart, m.nleaves, dout2, st); });
   cuda_check(cudaGetLastError(), "kernel launch");
 }
 
@@ -256,12 +263,60 @@ void Molecule::build(int precision, const double *dD, double *dV, double *dout2,
     build_fp64(dD, dV, dout2, st);
 }
 
-std::once_flag g_sph_once;
+cudaEvent_t KernelProfiler::get() {
+  if (pool.empty()) {
+    cudaEvent_t e;
+    cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    return e;
+  }
+  cudaEvent_t e = pool.back();
+  pool.pop_back();
+  return e;
+}
+
+void KernelProfiler::begin(const char *name, cudaStream_t st) {
+  Rec r{name, get(), get()};
+  cuda_check(cudaEventRecord(r.a, st), "cudaEventRecord");
+  pending.push_back(r);
+}
+
+void KernelProfiler::end(cudaStream_t st) {
+  cuda_check(cudaEventRecord(pending.back().b, st), "cudaEventRecord");
+}
+
+void KernelProfiler::collect() {
+  for (Rec &r : pending) {
+    cuda_check(cudaEventSynchronize(r.b), "cudaEventSynchronize");
+    float ms = 0.f;
+    cuda_check(cudaEventElapsedTime(&ms, r.a, r.b), "cudaEventElapsedTime");
+    Total *t = nullptr;
+    for (Total &x : totals)
+      if (x.name == r.name)
+        t = &x;
+    if (!t) {
+      totals.push_back(Total{r.name, 0.0, 0});
+      t = &totals.back();
+    }
+    t->ms += ms;
+    t->launches++;
+    pool.push_back(r.a);
+    pool.push_back(r.b);
+  }
+  pending.clear();
+}
+
+KernelProfiler::~KernelProfiler() {
+  for (Rec &r : pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : pool)
+    cudaEventDestroy(e);
+}
 
 Context::Context(int dev) : device(dev) {
   cuda_check(cudaSetDevice(dev), "cudaSetDevice");
   cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
-  std::call_once(g_sph_once, [] { upload_sph_table(); });
   upload_sph_table();
 }
 Context::~Context() {
@@ -549,5 +604,62 @@ int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *
       *nelec_out = out2[1];
   });
 }
+
+} // extern "C"
+
+extern "C" {
+
+int occ_xc_molecule_leaves(const occ_xc_molecule *mol, int *npoints, int *nbf_local) {
+  if (!mol || !npoints || !nbf_local)
+    return OCC_XC_ERR_ARG;
+  const Molecule &M = *mol->impl;
+  for (size_t i = 0; i < M.leaves.size(); i++) {
+    npoints[i] = M.leaves[i].cnt;
+    nbf_local[i] = M.leaves[i].nbf;
+  }
+  return OCC_XC_OK;
+}
+
+int occ_xc_profile_enable(occ_xc_context *ctx, int on) {
+  if (!ctx)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->impl->prof.on = on != 0;
+  return OCC_XC_OK;
+}
+
+int occ_xc_profile_reset(occ_xc_context *ctx) {
+  if (!ctx)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return guarded(ctx, [&] {
+    ctx->impl->prof.collect();
+    ctx->impl->prof.totals.clear();
+  });
+}
+
+int occ_xc_profile_count(occ_xc_context *ctx) {
+  if (!ctx)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int rc = guarded(ctx, [&] { ctx->impl->prof.collect(); });
+  return rc == OCC_XC_OK ? static_cast<int>(ctx->impl->prof.totals.size()) : rc;
+}
+
+int occ_xc_profile_entry(occ_xc_context *ctx, int i, const char **name, double *total_ms,
+                         long *launches) {
+  if (!ctx || !name || !total_ms || !launches)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  auto &t = ctx->impl->prof.totals;
+  if (i < 0 || i >= static_cast<int>(t.size()))
+    return OCC_XC_ERR_ARG;
+  *name = t[i].name.c_str();
+  *total_ms = t[i].ms;
+  *launches = t[i].launches;
+  return OCC_XC_OK;
+}
+
+long occ_xc_launch_count(const occ_xc_context *ctx) { return ctx ? ctx->impl->launches : -1; }
 
 } // extern "C"

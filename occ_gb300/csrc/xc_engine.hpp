@@ -22,11 +22,46 @@ struct ArgError : std::runtime_error {
 void cuda_check(cudaError_t e, const char *what);
 FuncSet parse_method(const std::string &method);
 
+// Per-kernel device timing with CUDA events on the launching stream, the
+// device analogue of OCC's timing categories (include/occ/core/timings.h).
+// Off by default; when on, every kernel launch of a build is bracketed.
+struct KernelProfiler {
+  struct Rec {
+    const char *name;
+    cudaEvent_t a, b;
+  };
+  struct Total {
+    std::string name;
+    double ms = 0.0;
+    long launches = 0;
+  };
+  bool on = false;
+  std::vector<Rec> pending;
+  std::vector<cudaEvent_t> pool;
+  std::vector<Total> totals;
+  cudaEvent_t get();
+  void begin(const char *name, cudaStream_t st);
+  void end(cudaStream_t st);
+  void collect();
+  ~KernelProfiler();
+};
+
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
+  KernelProfiler prof;
+  long launches = 0; // kernels launched by the library on this context
   explicit Context(int dev);
   ~Context();
+  // bracket one kernel launch (profiling) and count it
+  template <typename F> void launch(const char *name, cudaStream_t st, F &&f) {
+    if (prof.on)
+      prof.begin(name, st);
+    f();
+    if (prof.on)
+      prof.end(st);
+    launches++;
+  }
 };
 
 struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)

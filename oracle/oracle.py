@@ -114,7 +114,7 @@ def morton_leaves(points, target=128, min_leaf=32, max_leaf=256):
 
 
 def xc_build(basis, points, weights, D, method, screen=1e-10, density_threshold=1e-10,
-             leaf=(128, 32, 256), nthreads=0, leaf_subset=0, func_ids=None):
+             leaf=(128, 32, 256), nthreads=0, leaf_stride=1, func_ids=None):
     """E_xc, V_xc (nbf x nbf) and the integrated density for mo.D = D."""
     l, nprim, off, exps, coefs, origin = _basis_arrays(basis)
     pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
@@ -130,7 +130,7 @@ def xc_build(basis, points, weights, D, method, screen=1e-10, density_threshold=
                                _p(coefs), _p(origin), int(basis.pure), len(w), _p(pts), _p(w),
                                Df.ctypes.data_as(_dp), len(ids), _p(ids, _ip), _p(coef), screen,
                                density_threshold, leaf[0], leaf[1], leaf[2], nthreads,
-                               leaf_subset, V.ctypes.data_as(_dp), C.byref(exc), C.byref(nel))
+                               leaf_stride, V.ctypes.data_as(_dp), C.byref(exc), C.byref(nel))
     if rc != 0:
         raise RuntimeError(f"oracle_xc_build failed ({rc})")
     return exc.value, V, nel.value

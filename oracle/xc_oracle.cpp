@@ -259,7 +259,13 @@ std::vector<Leaf> morton_leaves(long n, const double *pts, long target, long min
   return leaves;
 }
 
+double g_last_flops = 0.0;  // 4 sum n_b m_b^2 over the leaves the last build processed
+double g_total_flops = 0.0; // the same over all leaves of the last build
+
 } // namespace
+
+extern "C" double oracle_last_flops() { return g_last_flops; }
+extern "C" double oracle_total_flops() { return g_total_flops; }
 
 extern "C" int oracle_collocation(int l, int pure, int nprim, const double *exps,
                                   const double *coefs, const double *origin, long n,
@@ -311,7 +317,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
                                int nfunc, const int *func_ids, const double *func_coefs,
                                double screen_threshold, double density_threshold,
                                long leaf_target, long leaf_min, long leaf_max, int nthreads,
-                               long leaf_subset, double *V, double *exc_out,
+                               long leaf_stride, double *V, double *exc_out,
                                double *nelec_out) {
   Basis bs{nsh, sh_l, sh_nprim, sh_off, exps, coefs, sh_origin, pure != 0, {}, 0};
   bs.first_bf.resize(nsh);
@@ -332,8 +338,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
   std::vector<long> perm;
   auto leaves = morton_leaves(npts, points, leaf_target, leaf_min, leaf_max, perm);
   long nleaves = static_cast<long>(leaves.size());
-  if (leaf_subset > 0 && leaf_subset < nleaves)
-    nleaves = leaf_subset;
+  const long stride = leaf_stride > 1 ? leaf_stride : 1;
 
   // D2 = 2 D (dft.h:205)
   std::vector<double> D2(static_cast<size_t>(nbf) * nbf);
@@ -347,7 +352,18 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
   (void)nthreads;
 #endif
   std::vector<std::vector<double>> Vloc(nt);
-  std::vector<double> eloc(nt, 0.0), nloc(nt, 0.0);
+  std::vector<double> eloc(nt, 0.0), nloc(nt, 0.0), floc(nt, 0.0);
+  g_total_flops = 0.0;
+  for (const Leaf &lf : leaves) {
+    double m = 0.0;
+    for (int s = 0; s < nsh; s++) {
+      const double *A = sh_origin + 3 * s;
+      double dx = A[0] - lf.c[0], dy = A[1] - lf.c[1], dz = A[2] - lf.c[2];
+      if (std::sqrt(dx * dx + dy * dy + dz * dz) - ext[s] < lf.r)
+        m += bs.size(s);
+    }
+    g_total_flops += 4.0 * lf.cnt * m * m;
+  }
 
 #pragma omp parallel num_threads(nt)
   {
@@ -363,6 +379,8 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
     std::vector<int> sig, loc0;
 #pragma omp for schedule(dynamic, 4)
     for (long li = 0; li < nleaves; li++) {
+      if (li % stride != 0)
+        continue;
       const Leaf &lf = leaves[li];
       const long n = lf.cnt;
       if (n == 0)
@@ -383,6 +401,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
         loc0[k] = m;
         m += bs.size(sig[k]);
       }
+      floc[tid] += 4.0 * n * static_cast<double>(m) * m;
       xyz.resize(3 * n);
       w.resize(n);
       for (long i = 0; i < n; i++) {
@@ -534,6 +553,9 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
   // reduction (dft.h:374-380)
   std::memset(V, 0, sizeof(double) * nbf * nbf);
   double E = 0.0, Ne = 0.0;
+  g_last_flops = 0.0;
+  for (int t = 0; t < nt; t++)
+    g_last_flops += floc[t];
   for (int t = 0; t < nt; t++) {
     for (size_t i = 0; i < static_cast<size_t>(nbf) * nbf; i++)
       V[i] += Vloc[t][i];

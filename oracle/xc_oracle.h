@@ -62,8 +62,8 @@ long oracle_morton_leaves(long n, const double *points, long target,
 // V (nbf x nbf) receives V_xc = -K of compute_JK.  func ids/coefs give the
 // components summed as in src/dft/dft_kernels.cpp:55-58 (coefficients are
 // Libxc-internal mixture weights, not OCC's never-applied scale factors).
-// leaf_subset > 0 restricts the build to the first leaf_subset leaves (used
-// only to time a bounded CPU sample).  Returns 0 on success.
+// leaf_stride > 1 restricts the build to every leaf_stride-th leaf (used only
+// to time a bounded CPU sample).  Returns 0 on success.
 int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
                     const int *sh_off, const double *exps, const double *coefs,
                     const double *sh_origin, int pure, long npts,
@@ -71,7 +71,7 @@ int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
                     const double *D, int nfunc, const int *func_ids,
                     const double *func_coefs, double screen_threshold,
                     double density_threshold, long leaf_target, long leaf_min,
-                    long leaf_max, int nthreads, long leaf_subset, double *V,
+                    long leaf_max, int nthreads, long leaf_stride, double *V,
                     double *exc_out, double *nelec_out);
 
 #ifdef __cplusplus
