@@ -135,6 +135,22 @@ int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *
 int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
                               int precision, double *d_V, double *d_exc2, void *stream);
 
+/* The FP64 build of occ_xc_compute_vxc_device for callers that cannot
+ * allocate device memory -- code inside a host application that owns all of
+ * the GPU's memory through its own pool, or code that must never block in the
+ * allocator.  It has no counterpart in the reference (OCC allocates freely on
+ * the host).  It calls no cudaMalloc, cudaFree or other allocating routine:
+ * its scratch is one static device array of 64 MiB that every GPU loading
+ * the library holds until the process exits.  A molecule whose scratch would
+ * exceed 64 MiB (roughly a water molecule in a split-valence basis with a GGA)
+ * is rejected with OCC_XC_ERR_ARG and a message.  The first call on a device
+ * looks up the array's device address (make it before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race on it, so
+ * serialise them.  d_D, d_V and d_exc2 are as for occ_xc_compute_vxc_device;
+ * the molecule is created beforehand with occ_xc_molecule_create. */
+int occ_xc_compute_vxc_noalloc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
+                               double *d_V, double *d_exc2, void *stream);
+
 /* Per-leaf view of the build plan (for tests and tooling): for each leaf
  * that has at least one significant shell, in Morton order, its point count
  * and its significant-AO count m_b.  Arrays sized nleaves (molecule info). */

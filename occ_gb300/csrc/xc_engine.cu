@@ -328,16 +328,6 @@ Context::~Context() {
 
 using namespace occx;
 
-struct occ_xc_context {
-  std::unique_ptr<Context> impl;
-  std::string err;
-  std::mutex mu;
-};
-struct occ_xc_molecule {
-  std::unique_ptr<Molecule> impl;
-  occ_xc_context *ctx;
-};
-
 namespace {
 Basis make_basis(int natoms, const double *xyz, int nshells, const int *shell_l,
                  const int *shell_atom, const int *shell_nprim, const double *exponents,

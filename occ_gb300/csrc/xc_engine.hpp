@@ -1,5 +1,7 @@
 // Engine internals shared by the C ABI and the precision-specific build paths.
 #pragma once
+#include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -110,3 +112,14 @@ struct Molecule {
 };
 
 } // namespace occx
+
+// The opaque handles of include/occ_xc.h.
+struct occ_xc_context {
+  std::unique_ptr<occx::Context> impl;
+  std::string err;
+  std::mutex mu;
+};
+struct occ_xc_molecule {
+  std::unique_ptr<occx::Molecule> impl;
+  occ_xc_context *ctx;
+};
