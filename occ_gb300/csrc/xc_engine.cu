@@ -113,6 +113,7 @@ template <typename T> static T *dev_upload(const std::vector<T> &h, size_t &byte
 Molecule::~Molecule() {
   for (void *p : allocations)
     cudaFree(p);
+  free_mixed(mixed);
 }
 
 void *Molecule::alloc(size_t bytes) {
@@ -318,6 +319,7 @@ Context::Context(int dev) : device(dev) {
   cuda_check(cudaSetDevice(dev), "cudaSetDevice");
   cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   upload_sph_table();
+  upload_sph_table_mixed();
 }
 Context::~Context() {
   if (stream)
@@ -384,6 +386,10 @@ template <typename F> int guarded(occ_xc_context *ctx, F &&f) {
     if (ctx)
       ctx->err = e.what();
     return OCC_XC_ERR_ARG;
+  } catch (const TimeoutError &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_TIMEOUT;
   } catch (const std::bad_alloc &) {
     if (ctx)
       ctx->err = "host allocation failed";
@@ -493,6 +499,7 @@ int occ_xc_molecule_create(occ_xc_context *ctx, int natoms, const int *Z, const 
     cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
     auto M = std::make_unique<Molecule>();
     M->ctx = ctx->impl.get();
+    M->device = ctx->impl->device;
     M->fs = parse_method(method);
     M->deriv = 0;
     for (int i = 0; i < M->fs.n; i++)
@@ -526,8 +533,10 @@ int occ_xc_molecule_create(occ_xc_context *ctx, int natoms, const int *Z, const 
 void occ_xc_molecule_destroy(occ_xc_molecule *mol) {
   if (!mol)
     return;
-  if (mol->ctx)
-    cudaSetDevice(mol->ctx->impl->device);
+  // the molecule may outlive its context (e.g. at process exit): use its own
+  // device ordinal, never the context
+  if (mol->impl)
+    cudaSetDevice(mol->impl->device);
   delete mol;
 }
 
@@ -589,6 +598,8 @@ int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *
     cuda_check(cudaMemcpyAsync(out2, M.d_out2, sizeof(out2), cudaMemcpyDeviceToHost, st),
                "cudaMemcpyAsync D2H");
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (precision == OCC_XC_MIXED && mixed_error_flag(M, st))
+      throw TimeoutError("a bounded wait of the tensor-core pipeline gave up");
     *exc = out2[0];
     if (nelec_out)
       *nelec_out = out2[1];

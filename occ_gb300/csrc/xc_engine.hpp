@@ -20,9 +20,18 @@ struct MethodError : std::runtime_error {
 struct ArgError : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
+struct TimeoutError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
 
 void cuda_check(cudaError_t e, const char *what);
 FuncSet parse_method(const std::string &method);
+void upload_sph_table_mixed();
+struct MixedState;
+void free_mixed(MixedState *S);
+struct Molecule;
+// 1 if a bounded wait in the mixed-precision kernels gave up (synchronises st)
+int mixed_error_flag(Molecule &M, cudaStream_t st);
 
 // Per-kernel device timing with CUDA events on the launching stream, the
 // device analogue of OCC's timing categories (include/occ/core/timings.h).
@@ -70,6 +79,7 @@ struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)
 
 struct Molecule {
   Context *ctx = nullptr;
+  int device = 0;
   // host model
   std::vector<int> Z;
   std::vector<double> xyz;

@@ -22,7 +22,6 @@
 namespace occx {
 
 __constant__ double c_sph[kSphTableSize];
-__constant__ float c_sphf[kSphTableSize];
 
 // One shell at one point: values (and gradients) of its nfunc AOs, scaled.
 template <int L, bool DERIV, typename T>
@@ -401,15 +400,12 @@ __global__ void __launch_bounds__(256) k_reduce(const double *__restrict__ epart
   }
 }
 
+void fill_sph_table(double *out);
+
 void upload_sph_table() {
   double h[kSphTableSize];
-  float hf[kSphTableSize];
-  extern void fill_sph_table(double *);
   fill_sph_table(h);
-  for (int i = 0; i < kSphTableSize; i++)
-    hf[i] = static_cast<float>(h[i]);
   cudaMemcpyToSymbol(c_sph, h, sizeof(h));
-  cudaMemcpyToSymbol(c_sphf, hf, sizeof(hf));
 }
 
 void launch_colloc_f64(const MolDev &m, int deriv, double *ws, cudaStream_t st) {

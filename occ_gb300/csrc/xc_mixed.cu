@@ -1,14 +1,970 @@
-// Mixed-precision (tcgen05 3xTF32) XC build path.
+// Mixed-precision XC build on the tcgen05 tensor cores.
+//
+// Both contractions run as TF32 MMAs with FP32 accumulators in tensor memory
+// (TMEM).  The TMEM accumulation truncates (rounds toward zero) at every MMA,
+// which biases long sums of same-signed terms; the density contraction is
+// therefore done on an exact grid (see k_rho_mixed) so that its result is
+// unbiased, while the potential contraction uses 3xTF32.  Collocation runs in
+// FP32 with FP64 displacements and compensated exponents/coefficients; the
+// functional, the per-leaf energy partials, the cross-block accumulation of
+// V_xc (FP64 atomics) and the final sums are FP64.
+//
+// Work unit: a "block" = up to 128 points of one Morton leaf (a 256-point
+// leaf is two blocks sharing the leaf's significant-AO list).  Per block:
+//   k_colloc_f32   phi, grad phi (FP32) -> ws32[block][comp][mp][128], and a
+//                  power-of-two bound of each point's |phi| row
+//   k_rho_mixed    X = phi D2 (M = 128 points, N <= 128 AOs per pass, K = m in
+//                  segments of <= 512), epilogue rho = rowsum(phi o X),
+//                  grad rho = 2 rowsum(grad phi o X)   (src/gto/density.cpp:33-43)
+//   k_func         FP64 functional per leaf (shared with the FP64 path)
+//   k_vxc_mixed    K = phi^T Y (M = 128 AOs, N <= 256, K = 128 points),
+//                  Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi,
+//                  V += K + K^T with FP64 atomics   (src/dft/xc_potential_matrix.cpp:19-41)
+//   k_reduce       fixed-order FP64 sum of the per-leaf partials
+#include <cstring>
+#include <type_traits>
+
+#include "../../include/occ_xc.h"
+#include "host/gto_eval.h"
+#include "umma.cuh"
 #include "xc_engine.hpp"
 
 namespace occx {
 
-struct MixedState {};
+// Solid-harmonic transform for the FP32 collocation, factored per row f as
+// T[f][k] = n_f t[f][k] with t small integers (exact in FP32) and the row
+// scale n_f kept as a (hi, lo) float pair: rounding a factor such as sqrt(3)
+// to one float would scale every AO of that kind the same way, a bias that
+// does not average out over the grid.
+constexpr int kSphRows = (kMaxL + 1) * (kMaxL + 1); // sum over l of 2l + 1
+__constant__ float c_spht[kSphTableSize];
+__constant__ float2 c_sphn[kSphRows];
 
-void Molecule::prepare_mixed() {}
+void fill_sph_table(double *out);
 
-void Molecule::build_mixed(const double *, double *, double *, cudaStream_t) {
-  throw ArgError("mixed-precision path is not available in this build");
+void upload_sph_table_mixed() {
+  double h[kSphTableSize];
+  float t[kSphTableSize];
+  float2 n[kSphRows];
+  fill_sph_table(h);
+  int row = 0;
+  for (int l = 0; l <= kMaxL; l++) {
+    const int nc = ncart_of(l);
+    for (int f = 0; f < 2 * l + 1; f++, row++) {
+      const double *T = h + sph_offset(l) + f * nc;
+      double mn = 1e300;
+      for (int k = 0; k < nc; k++)
+        if (T[k] != 0.0)
+          mn = std::min(mn, std::fabs(T[k]));
+      int q = 1;
+      for (; q <= 16; q++) {
+        bool ok = true;
+        for (int k = 0; k < nc; k++) {
+          const double r = T[k] / (mn / q);
+          ok = ok && std::fabs(r - std::nearbyint(r)) < 1e-9;
+        }
+        if (ok)
+          break;
+      }
+      if (q > 16)
+        throw std::runtime_error("solid-harmonic row does not factor into integers");
+      const double scale = mn / q;
+      for (int k = 0; k < nc; k++)
+        t[sph_offset(l) + f * nc + k] = static_cast<float>(std::nearbyint(T[k] / scale));
+      const float hi = static_cast<float>(scale);
+      n[row] = make_float2(hi, static_cast<float>(scale - hi));
+    }
+  }
+  cuda_check(cudaMemcpyToSymbol(c_spht, t, sizeof(t)), "cudaMemcpyToSymbol");
+  cuda_check(cudaMemcpyToSymbol(c_sphn, n, sizeof(n)), "cudaMemcpyToSymbol");
 }
 
+namespace {
+
+constexpr int kBlockPts = 128;  // points per block (M of the density GEMM)
+constexpr int kKc = 32;         // K chunk: one 128-byte swizzle row of TF32
+constexpr int kMaxN = 256;      // N per pass of the 3xTF32 GEMM
+constexpr int kExactN = 128;    // N per pass of the exact-grid GEMM
+constexpr int kExactKSeg = 512; // K per exact accumulation (keeps integer sums < 2^24)
+constexpr uint32_t kStageBytes = 96 * 1024;
+// 3xTF32 stage: A hi/lo (128 x 32) and B hi/lo (up to 256 x 32)
+constexpr uint32_t kOffAhi = 0, kOffAlo = 16 * 1024, kOffBhi = 32 * 1024, kOffBlo = 64 * 1024;
+// exact-grid stage: A slices 1..3 (128 x 32) and B slices 1..3 (up to 128 x 32)
+constexpr uint32_t kOffA1 = 0, kOffA2 = 16 * 1024, kOffA3 = 32 * 1024;
+constexpr uint32_t kOffB1 = 48 * 1024, kOffB2 = 64 * 1024, kOffB3 = 80 * 1024;
+constexpr uint32_t kWaitIter = 1u << 24; // bounded mbarrier waits
+constexpr int kErrTimeout = 1;
+
+struct MBlock {
+  int leaf;         // index into leaves
+  int p0;           // first point of the block within the leaf
+  int cnt;          // points in the block (<= 128)
+  int mp;           // significant AOs of the leaf, padded to 32
+  long long ws_off; // float offset of the block's [4][mp][128] planes
+};
+struct VItem {
+  int block, i0; // block and first AO row (multiple of 128) of the K tile
+};
+
+// Shared state of a CTA's two-stage shared-memory pipeline.
+struct Pipe {
+  uint8_t *stage[2];
+  uint64_t *bar; // 2 mbarriers, one per stage
+  uint32_t uses[2];
+  uint32_t tmem;
+  uint32_t ncols;
+  bool ok;
+};
+
+__device__ __forceinline__ void pipe_wait_stage(Pipe &P, int s, int *err) {
+  if (P.uses[s] > 0 && P.ok) {
+    if (!umma::mbar_wait(&P.bar[s], (P.uses[s] - 1) & 1u, kWaitIter)) {
+      P.ok = false;
+      atomicExch(err, kErrTimeout);
+    }
+  }
+}
+
+__device__ __forceinline__ void pipe_drain(Pipe &P, int *err) {
+  for (int s = 0; s < 2; s++)
+    pipe_wait_stage(P, s, err);
+}
+
+// Barriers and TMEM (warp 0 allocates ncols columns, a power of two >= 32).
+__device__ __forceinline__ void pipe_init(Pipe &P, uint8_t *smem, uint64_t *bars,
+                                          uint32_t *tmem_slot, uint32_t ncols) {
+  P.stage[0] = smem;
+  P.stage[1] = smem + kStageBytes;
+  P.bar = bars;
+  P.uses[0] = P.uses[1] = 0;
+  P.ok = true;
+  P.ncols = ncols;
+  if (threadIdx.x == 0) {
+    umma::mbar_init(&bars[0], 1);
+    umma::mbar_init(&bars[1], 1);
+    umma::fence_proxy_async();
+  }
+  if (threadIdx.x < 32)
+    umma::tmem_alloc(tmem_slot, ncols);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  P.tmem = *tmem_slot;
+}
+
+__device__ __forceinline__ void pipe_finish(Pipe &P) {
+  umma::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32)
+    umma::tmem_dealloc(P.tmem, P.ncols);
+}
+
+// 3xTF32 MMAs of one K chunk into TMEM columns [tmem, tmem + N).
+__device__ __forceinline__ void issue_tf32x3(const Pipe &P, int s, int N, bool first) {
+  const uint32_t base = umma::smem_u32(P.stage[s]);
+  const uint32_t idesc = umma::idesc_tf32(128, N);
+  umma::fence_after_sync();
+#pragma unroll
+  for (int kk = 0; kk < kKc / 8; kk++) {
+    const uint32_t o = kk * 32;
+    const uint64_t ahi = umma::desc_kmajor_sw128(base + kOffAhi + o);
+    const uint64_t alo = umma::desc_kmajor_sw128(base + kOffAlo + o);
+    const uint64_t bhi = umma::desc_kmajor_sw128(base + kOffBhi + o);
+    const uint64_t blo = umma::desc_kmajor_sw128(base + kOffBlo + o);
+    umma::mma_tf32(P.tmem, alo, bhi, idesc, (first && kk == 0) ? 0u : 1u);
+    umma::mma_tf32(P.tmem, ahi, blo, idesc, 1u);
+    umma::mma_tf32(P.tmem, ahi, bhi, idesc, 1u);
+  }
+}
+
+// Exact-grid MMAs of one K chunk: acc0 += A1 B1 (exact), acc1 += A1 B2 +
+// A2 B1 (exact), acc2 += A2 B2 + A1 B3 + A3 B1 + A2 B3 + A3 B2 (tail, at most
+// 2^-15 of the result, so its truncation is negligible), at TMEM columns
+// tmem, tmem + 128, tmem + 256.  Only A3 B3 (about 2^-32 of the row bounds)
+// is dropped.
+__device__ __forceinline__ void issue_exact(const Pipe &P, int s, int N, bool first) {
+  const uint32_t base = umma::smem_u32(P.stage[s]);
+  const uint32_t idesc = umma::idesc_tf32(128, N);
+  const uint32_t d0 = P.tmem, d1 = P.tmem + kExactN, d2 = P.tmem + 2 * kExactN;
+  umma::fence_after_sync();
+#pragma unroll
+  for (int kk = 0; kk < kKc / 8; kk++) {
+    const uint32_t o = kk * 32;
+    const uint64_t a1 = umma::desc_kmajor_sw128(base + kOffA1 + o);
+    const uint64_t a2 = umma::desc_kmajor_sw128(base + kOffA2 + o);
+    const uint64_t a3 = umma::desc_kmajor_sw128(base + kOffA3 + o);
+    const uint64_t b1 = umma::desc_kmajor_sw128(base + kOffB1 + o);
+    const uint64_t b2 = umma::desc_kmajor_sw128(base + kOffB2 + o);
+    const uint64_t b3 = umma::desc_kmajor_sw128(base + kOffB3 + o);
+    const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+    umma::mma_tf32(d0, a1, b1, idesc, acc);
+    umma::mma_tf32(d1, a1, b2, idesc, acc);
+    umma::mma_tf32(d1, a2, b1, idesc, 1u);
+    umma::mma_tf32(d2, a2, b3, idesc, acc);
+    umma::mma_tf32(d2, a3, b2, idesc, 1u);
+    umma::mma_tf32(d2, a2, b2, idesc, 1u);
+    umma::mma_tf32(d2, a1, b3, idesc, 1u);
+    umma::mma_tf32(d2, a3, b1, idesc, 1u);
+  }
+}
+
+// One GEMM pass over nchunks K chunks: producers fill a stage (all threads),
+// thread 0 issues the MMAs and commits them to the stage's barrier.
+template <bool EXACT, class FA, class FB>
+__device__ __forceinline__ void gemm_pass(Pipe &P, int N, int nchunks, FA &&fa, FB &&fb,
+                                          int *err) {
+  for (int c = 0; c < nchunks; c++) {
+    const int s = c & 1;
+    pipe_wait_stage(P, s, err);
+    if (P.ok) {
+      fa(c, P.stage[s]);
+      fb(c, P.stage[s]);
+    }
+    umma::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0 && P.ok) {
+      if (EXACT)
+        issue_exact(P, s, N, c == 0);
+      else
+        issue_tf32x3(P, s, N, c == 0);
+      umma::commit(&P.bar[s]);
+    }
+    P.uses[s]++;
+  }
+  pipe_drain(P, err);
+  umma::fence_after_sync();
+}
+
+// Store 4 consecutive FP32 values as TF32 hi/lo into row r, 16-byte chunk c.
+__device__ __forceinline__ void store4(uint8_t *hi_tile, uint8_t *lo_tile, int r, int c, float a,
+                                       float b, float cc, float d) {
+  uint32_t h0, l0, h1, l1, h2, l2, h3, l3;
+  umma::split_tf32(a, h0, l0);
+  umma::split_tf32(b, h1, l1);
+  umma::split_tf32(cc, h2, l2);
+  umma::split_tf32(d, h3, l3);
+  const uint32_t off = umma::sw128_offset(r, c);
+  *reinterpret_cast<uint4 *>(hi_tile + off) = make_uint4(h0, h1, h2, h3);
+  *reinterpret_cast<uint4 *>(lo_tile + off) = make_uint4(l0, l1, l2, l3);
+}
+
+// x = a1 + a2 + a3 relative to a power-of-two row bound s >= |row|:
+// a1 on the grid s 2^-7 and a2 on the grid s 2^-15 (each at most 8
+// significant bits, so products of slices of two rows are exact and their
+// sums are exact integers on a common grid while below 2^24 units), a3 the
+// TF32-rounded tail (|a3| <= s 2^-16).
+// `tail` (optional) is a correction below the float precision of x (the
+// FP64 residual of a value rounded to float) folded into a3.
+__device__ __forceinline__ void slice3(float x, float s, float inv_s, uint32_t &a1, uint32_t &a2,
+                                       uint32_t &a3, float tail = 0.f) {
+  const float q = x * inv_s;
+  const float i1 = rintf(q * 128.f);
+  const float r1 = q - i1 * (1.f / 128.f);
+  const float i2 = rintf(r1 * 32768.f);
+  const float r2 = r1 - i2 * (1.f / 32768.f);
+  a1 = __float_as_uint(i1 * (1.f / 128.f) * s);
+  a2 = __float_as_uint(i2 * (1.f / 32768.f) * s);
+  uint32_t t;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(fmaf(r2, s, tail)));
+  a3 = t;
+}
+
+__device__ __forceinline__ void store4_exact(uint8_t *t1, uint8_t *t2, uint8_t *t3, int r, int c,
+                                             const float (&v)[4], float s, float inv_s,
+                                             const float (&tail)[4] = {0.f, 0.f, 0.f, 0.f}) {
+  uint32_t a1[4], a2[4], a3[4];
+#pragma unroll
+  for (int e = 0; e < 4; e++)
+    slice3(v[e], s, inv_s, a1[e], a2[e], a3[e], tail[e]);
+  const uint32_t off = umma::sw128_offset(r, c);
+  *reinterpret_cast<uint4 *>(t1 + off) = make_uint4(a1[0], a1[1], a1[2], a1[3]);
+  *reinterpret_cast<uint4 *>(t2 + off) = make_uint4(a2[0], a2[1], a2[2], a2[3]);
+  *reinterpret_cast<uint4 *>(t3 + off) = make_uint4(a3[0], a3[1], a3[2], a3[3]);
+}
+
+// Power of two >= |v| (1 for zero rows).
+__device__ __forceinline__ float pow2_bound(float v) {
+  if (!(v > 0.f))
+    return 1.f;
+  int e;
+  frexpf(v, &e); // v = f 2^e, 0.5 <= f < 1
+  return ldexpf(1.f, e);
+}
+
+// One step of a compensated dot product (Ogita, Rump, Oishi, SIAM J. Sci.
+// Comput. 26, 1955 (2005), Dot2): the product's rounding error from an FMA
+// and the sum's from TwoSum go to the running correction c.  The _rn
+// intrinsics are never contracted into FMAs, which would break the
+// error-free transformations.
+__device__ __forceinline__ void dot2_step(float a, float b, float &s, float &c) {
+  const float p = __fmul_rn(a, b);
+  const float pe = fmaf(a, b, -p);
+  const float t = __fadd_rn(s, p);
+  const float bp = __fsub_rn(t, s);
+  const float se = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(se, pe));
+}
+
+// s + e = a + b exactly (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// e^(-t) for t >= 0 in FP32 without a systematic error: Cody-Waite argument
+// reduction (W.J. Cody, W. Waite, Software Manual for the Elementary
+// Functions, 1980), -t = n ln2 + r with |r| <= ln2/2 and ln2 split into a
+// 15-bit head (n * head is exact) and a tail, then the degree-8 Taylor
+// polynomial of e^r (truncation below 2e-10, of either sign with r) and an
+// exact scaling by 2^n.  Measured on GB300, the library expf has a one-sided
+// mean relative error of about +6e-9, which summed over a grid biases the
+// density; this routine's rounding errors are unbiased.
+__device__ __forceinline__ float exp_neg(float t) {
+  const float x = -t;
+  const float n = rintf(x * 1.44269504088896341f);
+  float r = fmaf(-n, 0.693145751953125f, x);  // exact (Sterbenz)
+  r = fmaf(-n, 1.42860682030941723e-06f, r);  // ln2 - head
+  float p = 2.48015873015873016e-05f;         // 1/8!
+  p = fmaf(p, r, 1.98412698412698413e-04f);   // 1/7!
+  p = fmaf(p, r, 1.38888888888888889e-03f);   // 1/6!
+  p = fmaf(p, r, 8.33333333333333333e-03f);   // 1/5!
+  p = fmaf(p, r, 4.16666666666666667e-02f);   // 1/4!
+  p = fmaf(p, r, 1.66666666666666667e-01f);   // 1/3!
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  return n < -126.f ? 0.f : ldexpf(p, static_cast<int>(n));
+}
+
+// ---------------------------------------------------------------------------
+// FP32 collocation of one block: ws32[comp][mp][128]
+template <int L>
+__device__ __forceinline__ float colloc_shell_f32(const DevShell &sh, bool pure, float x, float y,
+                                                  float z, float R, float dR, bool valid,
+                                                  float *out, size_t plane) {
+  // common_fac is folded into the contraction coefficients (prim32)
+  constexpr int NC = ncart_of(L);
+  constexpr int NF = 2 * L + 1 > NC ? 2 * L + 1 : NC;
+  float cv[NC], cx[NC], cy[NC], cz[NC];
+  cart_eval_l<L, float>(x, y, z, R, dR, cv, cx, cy, cz);
+  float v[NF], gx[NF], gy[NF], gz[NF];
+  if (!pure || L == 0) {
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      v[c] = cv[c];
+      gx[c] = cx[c];
+      gy[c] = cy[c];
+      gz[c] = cz[c];
+    }
+  } else {
+    const float *Tm = c_spht + sph_offset(L);
+    const float2 *Nm = c_sphn + L * L;
+#pragma unroll
+    for (int f = 0; f < 2 * L + 1; f++) {
+      float a = 0.f, b = 0.f, c = 0.f, d = 0.f;
+#pragma unroll
+      for (int k = 0; k < NC; k++) {
+        const float t = Tm[f * NC + k];
+        a = fmaf(t, cv[k], a);
+        b = fmaf(t, cx[k], b);
+        c = fmaf(t, cy[k], c);
+        d = fmaf(t, cz[k], d);
+      }
+      const float2 n = Nm[f];
+      v[f] = fmaf(n.x, a, n.y * a);
+      gx[f] = fmaf(n.x, b, n.y * b);
+      gy[f] = fmaf(n.x, c, n.y * c);
+      gz[f] = fmaf(n.x, d, n.y * d);
+    }
+  }
+  float vmax = 0.f;
+  for (int f = 0; f < sh.nfunc; f++) {
+    const size_t o = static_cast<size_t>(f) * kBlockPts;
+    const float val = valid ? v[f] : 0.f;
+    vmax = fmaxf(vmax, fabsf(val));
+    out[o] = val;
+    out[plane + o] = valid ? gx[f] : 0.f;
+    out[2 * plane + o] = valid ? gy[f] : 0.f;
+    out[3 * plane + o] = valid ? gz[f] : 0.f;
+  }
+  return vmax;
+}
+
+// Exponents and coefficients as (hi, lo) float pairs: rounding alpha or c to
+// one float would bias every point a primitive touches the same way, an error
+// that does not average out over the grid.
+__global__ void __launch_bounds__(128) k_colloc_f32(MolDev m, const MBlock *__restrict__ blocks,
+                                                    const float4 *__restrict__ prim32,
+                                                    float *__restrict__ ws,
+                                                    float *__restrict__ rowscale) {
+  const MBlock B = blocks[blockIdx.x];
+  const DevLeaf L = m.leaves[B.leaf];
+  const int p = threadIdx.x;
+  const bool valid = p < B.cnt;
+  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+  float *base = ws + B.ws_off;
+  const Pt4 P = valid ? m.pts[L.off + B.p0 + p] : make_pt4(0.0, 0.0, 0.0, 0.0);
+  float vmax = 0.f;
+  int loc = 0;
+  for (int k = L.sh_begin; k < L.sh_end; k++) {
+    const DevShell sh = m.shells[m.leaf_sh[k]];
+    // Displacement in FP64, then as (hi, lo) floats; r^2 and alpha r^2 as
+    // double-float pairs.  All points of a radial shell of an atom's grid lie
+    // at the same distance from that atom, so a rounding of r^2 or alpha r^2
+    // would be shared by every point of the shell and would not average out.
+    const double dx = P.x - sh.A[0], dy = P.y - sh.A[1], dz = P.z - sh.A[2];
+    const float x = static_cast<float>(dx), y = static_cast<float>(dy), z = static_cast<float>(dz);
+    const float xl = static_cast<float>(dx - x), yl = static_cast<float>(dy - y),
+                zl = static_cast<float>(dz - z);
+    float r2h, r2l;
+    {
+      const float p1 = __fmul_rn(x, x), p2 = __fmul_rn(y, y), p3 = __fmul_rn(z, z);
+      const float q = (fmaf(x, x, -p1) + fmaf(y, y, -p2) + fmaf(z, z, -p3)) +
+                      2.f * (x * xl + y * yl + z * zl);
+      float s12, e12, e3;
+      two_sum(p1, p2, s12, e12);
+      two_sum(s12, p3, r2h, e3);
+      r2l = (e12 + e3) + q;
+    }
+    float R = 0.f, dR = 0.f;
+    for (int q = 0; q < sh.nprim; q++) {
+      const float4 pc = prim32[sh.prim_off + q]; // alpha hi, alpha lo, c hi, c lo
+      const float th = __fmul_rn(pc.x, r2h);
+      const float tl = fmaf(pc.x, r2h, -th) + fmaf(pc.x, r2l, pc.y * r2h);
+      const float e0 = exp_neg(th);
+      const float ex = fmaf(-e0, tl, e0); // e^(-th - tl) to first order in tl
+      const float e = fmaf(pc.z, ex, pc.w * ex);
+      R += e;
+      dR = fmaf(-2.f * pc.x, e, fmaf(-2.f * pc.y, e, dR));
+    }
+    float *out = base + static_cast<size_t>(loc) * kBlockPts + p;
+    float v;
+    switch (sh.l) {
+    case 0: v = colloc_shell_f32<0>(sh, m.pure, x, y, z, R, dR, valid, out, plane); break;
+    case 1: v = colloc_shell_f32<1>(sh, m.pure, x, y, z, R, dR, valid, out, plane); break;
+    case 2: v = colloc_shell_f32<2>(sh, m.pure, x, y, z, R, dR, valid, out, plane); break;
+    case 3: v = colloc_shell_f32<3>(sh, m.pure, x, y, z, R, dR, valid, out, plane); break;
+    default: v = colloc_shell_f32<4>(sh, m.pure, x, y, z, R, dR, valid, out, plane); break;
+    }
+    vmax = fmaxf(vmax, v);
+    loc += sh.nfunc;
+  }
+  for (int f = loc; f < B.mp; f++) {
+    const size_t o = static_cast<size_t>(f) * kBlockPts + p;
+    base[o] = 0.f;
+    base[plane + o] = 0.f;
+    base[2 * plane + o] = 0.f;
+    base[3 * plane + o] = 0.f;
+  }
+  rowscale[static_cast<size_t>(blockIdx.x) * kBlockPts + p] = pow2_bound(vmax);
+}
+
+constexpr uint32_t kSmemMain = 2 * kStageBytes;
+
+struct alignas(16) SmemTail {
+  uint64_t bars[2];
+  uint32_t tmem_slot;
+  uint32_t pad;
+  float coef[4][kBlockPts];
+  float red[2][4][kBlockPts];
+  float bscale[kExactN];
+};
+constexpr uint32_t kSmemTotal = kSmemMain + sizeof(SmemTail) + 1024;
+
+__device__ __forceinline__ uint8_t *aligned_smem(uint8_t *raw) {
+  const uint32_t a = umma::smem_u32(raw);
+  return raw + ((1024u - (a & 1023u)) & 1023u);
+}
+
+// rho, grad rho of one block.  X = phi D2 is computed on the exact grid:
+// row scales s_p (phi rows, from the collocation) and t_j (D2 columns,
+// computed here), slices a1, a2, a3 / b1, b2, b3 (slice3), three TMEM
+// accumulators; a K segment holds at most 512 AOs so that the integer sums
+// of the exact levels stay below 2^24.  The epilogue forms X = acc0 + acc1 +
+// acc2 per segment and accumulates rowsum(phi o X) with compensated sums.
+template <bool DERIV>
+__global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__restrict__ blocks,
+                                                      const float *__restrict__ ws,
+                                                      const float *__restrict__ rowscale,
+                                                      const double *__restrict__ D,
+                                                      double *__restrict__ rho, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = aligned_smem(smem_raw);
+  SmemTail *tail = reinterpret_cast<SmemTail *>(smem + kSmemMain);
+  const MBlock B = blocks[blockIdx.x];
+  const DevLeaf L = m.leaves[B.leaf];
+  const int *g = m.leaf_ao + L.ao_begin;
+  const float *phi = ws + B.ws_off;
+  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+  const size_t nbf = static_cast<size_t>(m.nbf);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int quad = warp & 3, half = warp >> 2;
+  // A producer rows: point t & 127; its scale
+  const float sA = rowscale[static_cast<size_t>(blockIdx.x) * kBlockPts + (t & 127)];
+  const float isA = 1.f / sA;
+
+  Pipe P;
+  pipe_init(P, smem, tail->bars, &tail->tmem_slot, 512);
+  float acc[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
+  const int p = quad * 32 + lane; // this thread's point in the epilogue
+  for (int n0 = 0; n0 < B.mp; n0 += kExactN) {
+    const int N = min(kExactN, B.mp - n0);
+    // B row scales for this pass: bound of |2 D[k][j]| over the block's AOs k
+    if (t < N) {
+      const int lj = n0 + t;
+      float mx = 0.f;
+      if (lj < L.nbf) {
+        const size_t gj = static_cast<size_t>(g[lj]);
+        for (int lk = 0; lk < L.nbf; lk++)
+          mx = fmaxf(mx, fabsf(static_cast<float>(2.0 * D[static_cast<size_t>(g[lk]) * nbf + gj])));
+      }
+      tail->bscale[t] = pow2_bound(mx);
+    }
+    __syncthreads();
+    const float sB = (t < N) ? tail->bscale[t] : 1.f;
+    const float isB = 1.f / sB;
+    auto fa = [&](int c, uint8_t *st) {
+      const int r = t & 127, kh = t >> 7;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int k = c * kKc + kh * 16 + q * 4;
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++)
+          v[e] = phi[static_cast<size_t>(k + e) * kBlockPts + r];
+        store4_exact(st + kOffA1, st + kOffA2, st + kOffA3, r, kh * 4 + q, v, sA, isA);
+      }
+    };
+    for (int k0 = 0; k0 < B.mp; k0 += kExactKSeg) {
+      const int nk = min(kExactKSeg, B.mp - k0) / kKc;
+      auto fa_seg = [&](int c, uint8_t *st) { fa(k0 / kKc + c, st); };
+      auto fb = [&](int c, uint8_t *st) {
+        const int j = t;
+        if (j >= N)
+          return;
+        const int lj = n0 + j;
+        const bool jv = lj < L.nbf;
+        const size_t gj = jv ? static_cast<size_t>(g[lj]) : 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          float v[4], lo[4];
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            const int lk = k0 + c * kKc + q * 4 + e;
+            const double d =
+                (jv && lk < L.nbf) ? 2.0 * D[static_cast<size_t>(g[lk]) * nbf + gj] : 0.0;
+            v[e] = static_cast<float>(d);
+            lo[e] = static_cast<float>(d - static_cast<double>(v[e]));
+          }
+          store4_exact(st + kOffB1, st + kOffB2, st + kOffB3, j, q, v, sB, isB, lo);
+        }
+      };
+      gemm_pass<true>(P, N, nk, fa_seg, fb, err);
+      // epilogue of this segment: X = acc0 + acc1 + acc2 on this warp's
+      // 32 points and half of the pass's columns
+      const int cols = N / 2;
+      const uint32_t lanebase = P.tmem + (static_cast<uint32_t>(quad * 32) << 16);
+      for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
+        uint32_t r0[16], r1[16], r2[16];
+        umma::tmem_ld16(lanebase + c0, r0);
+        umma::tmem_ld16(lanebase + kExactN + c0, r1);
+        umma::tmem_ld16(lanebase + 2 * kExactN + c0, r2);
+        umma::tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          const float x = __fadd_rn(__uint_as_float(r0[i]),
+                                    __fadd_rn(__uint_as_float(r1[i]), __uint_as_float(r2[i])));
+          const size_t o = static_cast<size_t>(n0 + c0 + i) * kBlockPts + p;
+          dot2_step(phi[o], x, acc[0], cmp[0]);
+          if (DERIV) {
+            dot2_step(phi[plane + o], x, acc[1], cmp[1]);
+            dot2_step(phi[2 * plane + o], x, acc[2], cmp[2]);
+            dot2_step(phi[3 * plane + o], x, acc[3], cmp[3]);
+          }
+        }
+      }
+      umma::fence_before_sync();
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+    tail->red[half][c][p] = acc[c] + cmp[c];
+  __syncthreads();
+  if (t < kBlockPts && t < B.cnt) {
+    const size_t idx = static_cast<size_t>(L.off) + B.p0 + t;
+    const size_t Np = static_cast<size_t>(m.npts);
+    rho[idx] = static_cast<double>(tail->red[0][0][t]) + static_cast<double>(tail->red[1][0][t]);
+    if (DERIV)
+      for (int c = 1; c < 4; c++)
+        rho[c * Np + idx] = 2.0 * (static_cast<double>(tail->red[0][c][t]) +
+                                   static_cast<double>(tail->red[1][c][t]));
+  }
+  pipe_finish(P);
+}
+
+// K = phi^T Y for one 128-row AO tile of one block; V += K + K^T (FP64).
+template <bool DERIV>
+__global__ void __launch_bounds__(256, 1) k_vxc_mixed(MolDev m, const MBlock *__restrict__ blocks,
+                                                      const VItem *__restrict__ items,
+                                                      const float *__restrict__ ws,
+                                                      const double *__restrict__ coef,
+                                                      double *__restrict__ V, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = aligned_smem(smem_raw);
+  SmemTail *tail = reinterpret_cast<SmemTail *>(smem + kSmemMain);
+  const VItem it = items[blockIdx.x];
+  const MBlock B = blocks[it.block];
+  const DevLeaf L = m.leaves[B.leaf];
+  const int *g = m.leaf_ao + L.ao_begin;
+  const float *phi = ws + B.ws_off;
+  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+  const size_t nbf = static_cast<size_t>(m.nbf);
+  const size_t Np = static_cast<size_t>(m.npts);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int quad = warp & 3, half = warp >> 2;
+  // the block's functional coefficients (0 beyond its points)
+  for (int q = t; q < 4 * kBlockPts; q += blockDim.x) {
+    const int c = q / kBlockPts, pp = q % kBlockPts;
+    float v = 0.f;
+    if (pp < B.cnt && (DERIV || c == 0))
+      v = static_cast<float>(coef[c * Np + L.off + B.p0 + pp]);
+    tail->coef[c][pp] = v;
+  }
+  Pipe P;
+  pipe_init(P, smem, tail->bars, &tail->tmem_slot, kMaxN);
+  const int rows = min(128, B.mp - it.i0);
+  for (int n0 = 0; n0 < B.mp; n0 += kMaxN) {
+    const int N = min(kMaxN, B.mp - n0);
+    auto fa = [&](int c, uint8_t *st) {
+      const int r = t & 127, kh = t >> 7;
+      const bool rv = r < rows;
+      const float *src = phi + static_cast<size_t>(it.i0 + (rv ? r : 0)) * kBlockPts + c * kKc +
+                         kh * 16;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        float4 v = rv ? *reinterpret_cast<const float4 *>(src + 4 * q) : make_float4(0, 0, 0, 0);
+        store4(st + kOffAhi, st + kOffAlo, r, kh * 4 + q, v.x, v.y, v.z, v.w);
+      }
+    };
+    auto fb = [&](int c, uint8_t *st) {
+      const int j = t;
+      if (j >= N)
+        return;
+      const size_t row = static_cast<size_t>(n0 + j) * kBlockPts + c * kKc;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int pp = c * kKc + q * 4;
+        float4 a = *reinterpret_cast<const float4 *>(phi + row + 4 * q);
+        float y[4] = {a.x * tail->coef[0][pp], a.y * tail->coef[0][pp + 1],
+                      a.z * tail->coef[0][pp + 2], a.w * tail->coef[0][pp + 3]};
+        if (DERIV) {
+#pragma unroll
+          for (int d = 1; d < 4; d++) {
+            float4 gd = *reinterpret_cast<const float4 *>(phi + d * plane + row + 4 * q);
+            y[0] = fmaf(gd.x, tail->coef[d][pp], y[0]);
+            y[1] = fmaf(gd.y, tail->coef[d][pp + 1], y[1]);
+            y[2] = fmaf(gd.z, tail->coef[d][pp + 2], y[2]);
+            y[3] = fmaf(gd.w, tail->coef[d][pp + 3], y[3]);
+          }
+        }
+        store4(st + kOffBhi, st + kOffBlo, j, q, y[0], y[1], y[2], y[3]);
+      }
+    };
+    gemm_pass<false>(P, N, kBlockPts / kKc, fa, fb, err);
+    // epilogue: rows = AOs it.i0 + quad*32 + lane, this warp's half of N
+    const int li = it.i0 + quad * 32 + lane;
+    const bool iv = li < L.nbf;
+    const size_t gi = iv ? static_cast<size_t>(g[li]) : 0;
+    const int cols = N / 2;
+    for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
+      uint32_t r[16];
+      umma::tmem_ld16(P.tmem + (static_cast<uint32_t>(quad * 32) << 16) + c0, r);
+      umma::tmem_wait_ld();
+      if (iv) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          const int lj = n0 + c0 + i;
+          if (lj < L.nbf) {
+            const size_t gj = static_cast<size_t>(g[lj]);
+            const double k = static_cast<double>(__uint_as_float(r[i]));
+            atomicAdd(&V[gj * nbf + gi], k);
+            atomicAdd(&V[gi * nbf + gj], k);
+          }
+        }
+      }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+  }
+  pipe_finish(P);
+}
+
+// Self-test: C[128][N] = A[128][K] B[N][K]^T with the 3xTF32 pipeline
+// (exact = 0) or the exact-grid pipeline (exact = 1, N <= 128, K <= 512).
+__global__ void __launch_bounds__(256, 1) k_selftest_gemm(const float *__restrict__ A,
+                                                          const float *__restrict__ Bm,
+                                                          float *__restrict__ Cm, int N, int K,
+                                                          int exact, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = aligned_smem(smem_raw);
+  SmemTail *tail = reinterpret_cast<SmemTail *>(smem + kSmemMain);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int quad = warp & 3, half = warp >> 2;
+  Pipe P;
+  pipe_init(P, smem, tail->bars, &tail->tmem_slot, exact ? 512 : kMaxN);
+  const int row = quad * 32 + lane;
+  const int cols = N / 2;
+  if (!exact) {
+    auto fa = [&](int c, uint8_t *st) {
+      const int r = t & 127, kh = t >> 7;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const float *s = A + static_cast<size_t>(r) * K + c * kKc + kh * 16 + 4 * q;
+        store4(st + kOffAhi, st + kOffAlo, r, kh * 4 + q, s[0], s[1], s[2], s[3]);
+      }
+    };
+    auto fb = [&](int c, uint8_t *st) {
+      if (t >= N)
+        return;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const float *s = Bm + static_cast<size_t>(t) * K + c * kKc + 4 * q;
+        store4(st + kOffBhi, st + kOffBlo, t, q, s[0], s[1], s[2], s[3]);
+      }
+    };
+    gemm_pass<false>(P, N, K / kKc, fa, fb, err);
+    for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
+      uint32_t r[16];
+      umma::tmem_ld16(P.tmem + (static_cast<uint32_t>(quad * 32) << 16) + c0, r);
+      umma::tmem_wait_ld();
+#pragma unroll
+      for (int i = 0; i < 16; i++)
+        Cm[static_cast<size_t>(row) * N + c0 + i] = __uint_as_float(r[i]);
+    }
+  } else {
+    // row bounds of A (row t & 127) and B (row t < N)
+    float ma = 0.f, mb = 0.f;
+    for (int k = 0; k < K; k++) {
+      ma = fmaxf(ma, fabsf(A[static_cast<size_t>(t & 127) * K + k]));
+      if (t < N)
+        mb = fmaxf(mb, fabsf(Bm[static_cast<size_t>(t) * K + k]));
+    }
+    const float sA = pow2_bound(ma), isA = 1.f / sA, sB = pow2_bound(mb), isB = 1.f / sB;
+    auto fa = [&](int c, uint8_t *st) {
+      const int r = t & 127, kh = t >> 7;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const float *s = A + static_cast<size_t>(r) * K + c * kKc + kh * 16 + 4 * q;
+        const float v[4] = {s[0], s[1], s[2], s[3]};
+        store4_exact(st + kOffA1, st + kOffA2, st + kOffA3, r, kh * 4 + q, v, sA, isA);
+      }
+    };
+    auto fb = [&](int c, uint8_t *st) {
+      if (t >= N)
+        return;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const float *s = Bm + static_cast<size_t>(t) * K + c * kKc + 4 * q;
+        const float v[4] = {s[0], s[1], s[2], s[3]};
+        store4_exact(st + kOffB1, st + kOffB2, st + kOffB3, t, q, v, sB, isB);
+      }
+    };
+    gemm_pass<true>(P, N, K / kKc, fa, fb, err);
+    const uint32_t lanebase = P.tmem + (static_cast<uint32_t>(quad * 32) << 16);
+    for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
+      uint32_t r0[16], r1[16], r2[16];
+      umma::tmem_ld16(lanebase + c0, r0);
+      umma::tmem_ld16(lanebase + kExactN + c0, r1);
+      umma::tmem_ld16(lanebase + 2 * kExactN + c0, r2);
+      umma::tmem_wait_ld();
+#pragma unroll
+      for (int i = 0; i < 16; i++)
+        Cm[static_cast<size_t>(row) * N + c0 + i] =
+            __fadd_rn(__uint_as_float(r0[i]),
+                      __fadd_rn(__uint_as_float(r1[i]), __uint_as_float(r2[i])));
+    }
+  }
+  pipe_finish(P);
+}
+
+size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+void set_smem_attributes() {
+  cuda_check(cudaFuncSetAttribute(k_rho_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemTotal), "cudaFuncSetAttribute");
+  cuda_check(cudaFuncSetAttribute(k_rho_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemTotal), "cudaFuncSetAttribute");
+  cuda_check(cudaFuncSetAttribute(k_vxc_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemTotal), "cudaFuncSetAttribute");
+  cuda_check(cudaFuncSetAttribute(k_vxc_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemTotal), "cudaFuncSetAttribute");
+  cuda_check(cudaFuncSetAttribute(k_selftest_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemTotal), "cudaFuncSetAttribute");
+}
+
+} // namespace
+
+struct MixedState {
+  std::vector<MBlock> blocks;
+  std::vector<VItem> items;
+  std::vector<float4> prim32;
+  size_t ws_floats = 0;
+  MBlock *d_blocks = nullptr;
+  VItem *d_items = nullptr;
+  float4 *d_prim32 = nullptr;
+  float *d_ws = nullptr;
+  float *d_rowscale = nullptr;
+  int *d_err = nullptr;
+};
+
+void Molecule::prepare_mixed() {
+  MixedState *S = new MixedState();
+  mixed = S;
+  for (size_t li = 0; li < leaves.size(); li++) {
+    const DevLeaf &L = leaves[li];
+    const int mp = static_cast<int>(round_up(L.nbf, kKc));
+    for (int p0 = 0; p0 < L.cnt; p0 += kBlockPts) {
+      MBlock B;
+      B.leaf = static_cast<int>(li);
+      B.p0 = p0;
+      B.cnt = std::min(kBlockPts, L.cnt - p0);
+      B.mp = mp;
+      B.ws_off = static_cast<long long>(S->ws_floats);
+      S->ws_floats += static_cast<size_t>(4) * mp * kBlockPts;
+      const int bi = static_cast<int>(S->blocks.size());
+      for (int i0 = 0; i0 < mp; i0 += 128)
+        S->items.push_back({bi, i0});
+      S->blocks.push_back(B);
+    }
+  }
+  // primitives as (alpha hi, alpha lo, c hi, c lo) float pairs, with OCC's
+  // common_fac folded into c in FP64
+  for (const Shell &sh : basis.shells) {
+    const double fac = common_fac(sh.l, basis.pure);
+    for (size_t k = 0; k < sh.exps.size(); k++) {
+      const double c = sh.coefs[k] * fac;
+      const float ah = static_cast<float>(sh.exps[k]);
+      const float ch = static_cast<float>(c);
+      S->prim32.push_back(make_float4(ah, static_cast<float>(sh.exps[k] - ah), ch,
+                                      static_cast<float>(c - ch)));
+    }
+  }
+  auto up = [&](auto &vec, auto *&dptr) {
+    using T = typename std::remove_reference<decltype(vec)>::type::value_type;
+    dptr = static_cast<T *>(alloc(std::max<size_t>(vec.size(), 1) * sizeof(T)));
+    if (!vec.empty())
+      cuda_check(cudaMemcpy(dptr, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice),
+                 "cudaMemcpy H2D");
+  };
+  up(S->blocks, S->d_blocks);
+  up(S->items, S->d_items);
+  up(S->prim32, S->d_prim32);
+  S->d_ws = static_cast<float *>(alloc(std::max<size_t>(S->ws_floats, 1) * sizeof(float)));
+  S->d_rowscale = static_cast<float *>(
+      alloc(std::max<size_t>(S->blocks.size(), 1) * kBlockPts * sizeof(float)));
+  S->d_err = static_cast<int *>(alloc(sizeof(int)));
+  cuda_check(cudaMemset(S->d_err, 0, sizeof(int)), "cudaMemset");
+  set_smem_attributes();
+}
+
+void Molecule::build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st) {
+  MixedState &S = *mixed;
+  const MolDev m = dev();
+  Context &c = *ctx;
+  const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
+  const int nb = static_cast<int>(S.blocks.size());
+  const int ni = static_cast<int>(S.items.size());
+  cuda_check(cudaMemsetAsync(dV, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
+  if (nb > 0) {
+    c.launch("colloc_f32", st, [&] {
+      k_colloc_f32<<<nb, kBlockPts, 0, st>>>(m, S.d_blocks, S.d_prim32, S.d_ws, S.d_rowscale);
+    });
+    c.launch("rho_mixed", st, [&] {
+      if (deriv)
+        k_rho_mixed<true><<<nb, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_ws, S.d_rowscale, dD,
+                                                       d_rho, S.d_err);
+      else
+        k_rho_mixed<false><<<nb, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_ws, S.d_rowscale, dD,
+                                                        d_rho, S.d_err);
+    });
+  }
+  c.launch("func", st, [&] {
+    launch_func(m, deriv, fs, bs.density_threshold, d_rho, d_coef, d_epart, st);
+  });
+  if (ni > 0) {
+    c.launch("vxc_mixed", st, [&] {
+      if (deriv)
+        k_vxc_mixed<true><<<ni, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_items, S.d_ws, d_coef,
+                                                       dV, S.d_err);
+      else
+        k_vxc_mixed<false><<<ni, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_items, S.d_ws, d_coef,
+                                                        dV, S.d_err);
+    });
+  }
+  c.launch("reduce", st, [&] { launch_reduce(d_epart, m.nleaves, dout2, st); });
+  cuda_check(cudaGetLastError(), "kernel launch");
+}
+
+int mixed_error_flag(Molecule &M, cudaStream_t st) {
+  if (!M.mixed)
+    return 0;
+  int h = 0;
+  cuda_check(cudaMemcpyAsync(&h, M.mixed->d_err, sizeof(int), cudaMemcpyDeviceToHost, st),
+             "cudaMemcpyAsync D2H");
+  cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  return h;
+}
+
+void free_mixed(MixedState *S) { delete S; }
+
 } // namespace occx
+
+using namespace occx;
+
+// C = A B^T for A[128][K], B[N][K] (row-major FP32, host buffers): one tile of
+// the mixed path's tcgen05 pipeline, for testing it in isolation.  exact = 0:
+// 3xTF32, N a multiple of 32 up to 256, K a multiple of 32.  exact = 1: the
+// exact-grid split, N a multiple of 32 up to 128, K a multiple of 32 up to 512.
+extern "C" int occ_xc_selftest_tf32_gemm(occ_xc_context *ctx, int exact, int N, int K,
+                                         const float *A, const float *Bm, float *Cm) {
+  const int nmax = exact ? kExactN : kMaxN;
+  if (!ctx || !A || !Bm || !Cm || N <= 0 || N > nmax || N % 32 || K <= 0 || K % kKc ||
+      (exact && K > kExactKSeg))
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  float *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  int *dErr = nullptr;
+  int rc = OCC_XC_OK;
+  try {
+    cudaStream_t st = ctx->impl->stream;
+    set_smem_attributes();
+    cuda_check(cudaMalloc(&dA, sizeof(float) * 128 * K), "cudaMalloc");
+    cuda_check(cudaMalloc(&dB, sizeof(float) * N * K), "cudaMalloc");
+    cuda_check(cudaMalloc(&dC, sizeof(float) * 128 * N), "cudaMalloc");
+    cuda_check(cudaMalloc(&dErr, sizeof(int)), "cudaMalloc");
+    cuda_check(cudaMemcpy(dA, A, sizeof(float) * 128 * K, cudaMemcpyHostToDevice), "H2D");
+    cuda_check(cudaMemcpy(dB, Bm, sizeof(float) * N * K, cudaMemcpyHostToDevice), "H2D");
+    cuda_check(cudaMemset(dErr, 0, sizeof(int)), "memset");
+    k_selftest_gemm<<<1, 256, kSmemTotal, st>>>(dA, dB, dC, N, K, exact, dErr);
+    cuda_check(cudaGetLastError(), "launch");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    int herr = 0;
+    cuda_check(cudaMemcpy(&herr, dErr, sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(Cm, dC, sizeof(float) * 128 * N, cudaMemcpyDeviceToHost), "D2H");
+    if (herr) {
+      ctx->err = "tcgen05 pipeline wait timed out";
+      rc = OCC_XC_ERR_TIMEOUT;
+    }
+  } catch (const std::exception &e) {
+    ctx->err = e.what();
+    rc = OCC_XC_ERR_CUDA;
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  cudaFree(dErr);
+  return rc;
+}

@@ -230,12 +230,9 @@ class _Context:
     def error(self):
         return self.lib.occ_xc_last_error(self.h).decode()
 
-    def __del__(self):
-        if getattr(self, "h", None):
-            self.lib.occ_xc_context_destroy(self.h)
-            self.h = None
 
-
+# One context per device for the life of the process (never destroyed from
+# Python: molecules may be finalised after it at interpreter exit).
 _CONTEXTS = {}
 
 

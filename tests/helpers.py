@@ -41,3 +41,4 @@ def water_case(basis_name="6-31g", nocc=5, seed=0, pure=True):
     b = wl.basis_for(mol, basis_name, pure)
     D = wl.random_density(b.nbf(), nocc, seed)
     return mol, b, D
+TOL_V_MIXED = 1e-5  # max |dV_xc| of the mixed path against FP64

@@ -7,7 +7,7 @@ import pytest
 import occ_gb300 as og
 import oracle
 from occ_gb300 import workloads as wl
-from helpers import TOL_E_FP64, TOL_E_MIXED, TOL_V_FP64, water_case
+from helpers import TOL_E_FP64, TOL_E_MIXED, TOL_V_FP64, TOL_V_MIXED, water_case
 
 pytestmark = pytest.mark.gpu
 
@@ -75,6 +75,29 @@ def test_screening_off_matches_dense_limit():
     d2 = og.DFT("pbe", b, build_settings=og.BuildSettings(xc_screening_threshold=1e-14))
     d2.compute_vxc(D)
     assert abs(d1.exchange_correlation_energy() - d2.exchange_correlation_energy()) < 1e-8
+
+
+@pytest.mark.parametrize("method", ["lda", "pbe", "blyp", "b3lyp"])
+@pytest.mark.parametrize("basis_name", ["6-31g", "def2-svp"])
+def test_water_mixed(method, basis_name):
+    mol, b, D = water_case(basis_name)
+    dft, V, V_ref, e_ref, n_ref = _run(method, b, D, precision=og.MIXED)
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= TOL_E_MIXED
+    assert np.max(np.abs(V - V_ref)) <= TOL_V_MIXED
+    assert abs(dft.integrated_density() - n_ref) <= 1e-6
+
+
+def test_water_hexamer_svp_mixed_vs_fp64():
+    mol = wl.water_cluster(6, box=6.0, seed=5)
+    b = wl.basis_for(mol, "def2-svp")
+    D = wl.random_density(b.nbf(), 30, seed=5)
+    dft = og.DFT("pbe", b)
+    V64 = dft.compute_vxc(D, og.FP64)
+    e64 = dft.exchange_correlation_energy()
+    Vm = dft.compute_vxc(D, og.MIXED)
+    em = dft.exchange_correlation_energy()
+    assert abs(em - e64) <= TOL_E_MIXED
+    assert np.max(np.abs(Vm - V64)) <= TOL_V_MIXED
 
 
 def test_repeat_builds_identical_energy():
