@@ -256,6 +256,7 @@ def main():
     import torch.distributed as dist
 
     import occ_gb300 as og
+    from occ_gb300.replicas import aggregate_rate
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -288,11 +289,8 @@ def main():
         with ClockSampler(local) as cs:
             total_ms, per, exc, _ = device_timing(dft, D, prec, args.steps, args.warmup, torch)
         launches = lib.occ_xc_launch_count(dft.ctx.h) - l0
-        if world > 1:
-            t = torch.tensor([total_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total_ms = float(t.item())
-        results[prec] = dict(total_ms=total_ms, per=per, exc=exc,
+        rate, secs, _ = aggregate_rate(args.steps, total_ms / 1e3, dist if world > 1 else None)
+        results[prec] = dict(total_ms=secs * 1e3, rate=rate, per=per, exc=exc,
                              launches=launches * args.steps // (args.steps + args.warmup))
         if prec == head:
             clocks = cs.summary()
@@ -305,7 +303,7 @@ def main():
         return
     r = results[head]
     ms_per = r["total_ms"] / args.steps
-    value = world * args.steps / (r["total_ms"] / 1e3)
+    value = r["rate"]
     nbf = info["nbf"]
     # dominant kernel and its roofline
     tot = sum(v[0] for v in prof.values())

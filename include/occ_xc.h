@@ -97,6 +97,12 @@ int occ_xc_molecular_grid(int natoms, const int *atomic_numbers, const double *x
                           const double *coefficients, int pure, const occ_xc_grid_settings *grid,
                           long *npoints, double *points, double *weights);
 
+/* Replaces occ::numint::grid::lebedev(n) (include/occ/numint/lebedev.h,
+ * src/numint/lebedev.cpp:5388-5503) for n in {6, 14, 26, 38, 50, 74, 86, 110,
+ * 146, 170, 194, 230, 266, 302}: xyzw[4*n] receives x, y, z, weight per point
+ * (weights sum to one).  Host-only.  Returns n, or 0 for an unsupported n. */
+int occ_xc_lebedev(int n, double *xyzw);
+
 /* Context: one CUDA device, one stream.  Replaces nothing in OCC (OCC has
  * no device state). */
 int occ_xc_context_create(int device, occ_xc_context **out);

@@ -460,6 +460,17 @@ int occ_xc_molecular_grid(int natoms, const int *Z, const double *xyz, int nshel
   }
 }
 
+int occ_xc_lebedev(int n, double *xyzw) {
+  if (!xyzw)
+    return 0;
+  std::vector<double> v;
+  const int got = lebedev_rule(n, v);
+  if (got != n)
+    return 0;
+  std::memcpy(xyzw, v.data(), v.size() * sizeof(double));
+  return n;
+}
+
 int occ_xc_context_create(int device, occ_xc_context **out) {
   if (!out)
     return OCC_XC_ERR_ARG;
