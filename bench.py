@@ -45,14 +45,20 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--waters", type=int, default=32,
+                    help="cluster size (32 is the benchmark; smaller only for profiling)")
     return ap.parse_args()
 
 
-def make_workload(seed=0):
+def make_workload(seed=0, waters=32):
+    """n rigid waters in a cube of side 10 (32/n)^(-1/3) Angstrom (the same
+    density as the 32-water benchmark), def2-SVP, 5 occupied orbitals per
+    water."""
     from occ_gb300 import workloads as wl
-    mol = wl.water_cluster(32, box=10.0, seed=seed)
+    box = 10.0 * (waters / 32.0) ** (1.0 / 3.0)
+    mol = wl.water_cluster(waters, box=box, seed=seed)
     basis = wl.basis_for(mol, "def2-svp")
-    D = wl.random_density(basis.nbf(), 160, seed=seed)
+    D = wl.random_density(basis.nbf(), 5 * waters, seed=seed)
     return mol, basis, D
 
 
@@ -222,7 +228,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    _, basis, D = make_workload()
+    _, basis, D = make_workload(waters=args.waters)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import host_grid
     P, W = host_grid(basis)
@@ -264,7 +270,7 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl")
-    mol, basis, D = make_workload(seed=0)
+    mol, basis, D = make_workload(seed=0, waters=args.waters)
     dft = og.DFT("pbe", basis, device=local)
     info = dft.info()
     lib = dft.ctx.lib

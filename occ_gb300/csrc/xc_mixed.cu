@@ -335,7 +335,19 @@ __device__ __forceinline__ float exp_neg(float t) {
   p = fmaf(p, r, 0.5f);
   p = fmaf(p, r, 1.0f);
   p = fmaf(p, r, 1.0f);
-  return n < -126.f ? 0.f : ldexpf(p, static_cast<int>(n));
+  // exact scaling by 2^n, -126 <= n <= 0, through the exponent field
+  return n < -126.f ? 0.f : p * __int_as_float((static_cast<int>(n) + 127) << 23);
+}
+
+// Difference of two double-float numbers (ah + al) - (bh + bl) as a
+// double-float (hi, lo), from FP32 operations only (TwoSum on the heads).
+__device__ __forceinline__ void df_sub(float ah, float al, float bh, float bl, float &h,
+                                       float &l) {
+  float s, e;
+  two_sum(ah, -bh, s, e);
+  e = __fadd_rn(e, __fsub_rn(al, bl));
+  h = __fadd_rn(s, e);
+  l = __fsub_rn(e, __fsub_rn(h, s));
 }
 
 // ---------------------------------------------------------------------------
@@ -380,14 +392,18 @@ __device__ __forceinline__ float colloc_shell_f32(const DevShell &sh, bool pure,
     }
   }
   float vmax = 0.f;
-  for (int f = 0; f < sh.nfunc; f++) {
-    const size_t o = static_cast<size_t>(f) * kBlockPts;
-    const float val = valid ? v[f] : 0.f;
-    vmax = fmaxf(vmax, fabsf(val));
-    out[o] = val;
-    out[plane + o] = valid ? gx[f] : 0.f;
-    out[2 * plane + o] = valid ? gy[f] : 0.f;
-    out[3 * plane + o] = valid ? gz[f] : 0.f;
+  const int nf = pure ? 2 * L + 1 : NC;
+#pragma unroll
+  for (int f = 0; f < NF; f++) { // compile-time bound keeps v[] in registers
+    if (f < nf) {
+      const size_t o = static_cast<size_t>(f) * kBlockPts;
+      const float val = valid ? v[f] : 0.f;
+      vmax = fmaxf(vmax, fabsf(val));
+      out[o] = val;
+      out[plane + o] = valid ? gx[f] : 0.f;
+      out[2 * plane + o] = valid ? gy[f] : 0.f;
+      out[3 * plane + o] = valid ? gz[f] : 0.f;
+    }
   }
   return vmax;
 }
@@ -395,8 +411,9 @@ __device__ __forceinline__ float colloc_shell_f32(const DevShell &sh, bool pure,
 // Exponents and coefficients as (hi, lo) float pairs: rounding alpha or c to
 // one float would bias every point a primitive touches the same way, an error
 // that does not average out over the grid.
-__global__ void __launch_bounds__(128) k_colloc_f32(MolDev m, const MBlock *__restrict__ blocks,
+__global__ void __launch_bounds__(128, 4) k_colloc_f32(MolDev m, const MBlock *__restrict__ blocks,
                                                     const float4 *__restrict__ prim32,
+                                                    const float4 *__restrict__ shA,
                                                     float *__restrict__ ws,
                                                     float *__restrict__ rowscale) {
   const MBlock B = blocks[blockIdx.x];
@@ -406,18 +423,25 @@ __global__ void __launch_bounds__(128) k_colloc_f32(MolDev m, const MBlock *__re
   const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
   float *base = ws + B.ws_off;
   const Pt4 P = valid ? m.pts[L.off + B.p0 + p] : make_pt4(0.0, 0.0, 0.0, 0.0);
+  // the point as double-float coordinates (once per point)
+  const float pxh = static_cast<float>(P.x), pyh = static_cast<float>(P.y),
+              pzh = static_cast<float>(P.z);
+  const float pxl = static_cast<float>(P.x - pxh), pyl = static_cast<float>(P.y - pyh),
+              pzl = static_cast<float>(P.z - pzh);
   float vmax = 0.f;
   int loc = 0;
   for (int k = L.sh_begin; k < L.sh_end; k++) {
-    const DevShell sh = m.shells[m.leaf_sh[k]];
-    // Displacement in FP64, then as (hi, lo) floats; r^2 and alpha r^2 as
+    const int si = m.leaf_sh[k];
+    const DevShell sh = m.shells[si];
+    // Displacement as a double-float (hi, lo) pair; r^2 and alpha r^2 as
     // double-float pairs.  All points of a radial shell of an atom's grid lie
     // at the same distance from that atom, so a rounding of r^2 or alpha r^2
     // would be shared by every point of the shell and would not average out.
-    const double dx = P.x - sh.A[0], dy = P.y - sh.A[1], dz = P.z - sh.A[2];
-    const float x = static_cast<float>(dx), y = static_cast<float>(dy), z = static_cast<float>(dz);
-    const float xl = static_cast<float>(dx - x), yl = static_cast<float>(dy - y),
-                zl = static_cast<float>(dz - z);
+    const float4 ah = shA[2 * si], al = shA[2 * si + 1]; // centre (hi xyz, lo xyz)
+    float x, y, z, xl, yl, zl;
+    df_sub(pxh, pxl, ah.x, al.x, x, xl);
+    df_sub(pyh, pyl, ah.y, al.y, y, yl);
+    df_sub(pzh, pzl, ah.z, al.z, z, zl);
     float r2h, r2l;
     {
       const float p1 = __fmul_rn(x, x), p2 = __fmul_rn(y, y), p3 = __fmul_rn(z, z);
@@ -463,13 +487,16 @@ __global__ void __launch_bounds__(128) k_colloc_f32(MolDev m, const MBlock *__re
 
 constexpr uint32_t kSmemMain = 2 * kStageBytes;
 
+constexpr int kMaxMapSmem = 1024; // block AO maps up to this size live in shared memory
+
 struct alignas(16) SmemTail {
   uint64_t bars[2];
   uint32_t tmem_slot;
   uint32_t pad;
   float coef[4][kBlockPts];
   float red[2][4][kBlockPts];
-  float bscale[kExactN];
+  int gmap[kMaxMapSmem];
+  float bscale[kExactN]; // exact-split scales of the current pass's B rows
 };
 constexpr uint32_t kSmemTotal = kSmemMain + sizeof(SmemTail) + 1024;
 
@@ -478,9 +505,47 @@ __device__ __forceinline__ uint8_t *aligned_smem(uint8_t *raw) {
   return raw + ((1024u - (a & 1023u)) & 1023u);
 }
 
+// Per build: D2 = 2 D as (hi, lo) float pairs and, per column j, a power of
+// two bounding |D2[k][j]| over all k (the column scale of the exact split).
+__global__ void __launch_bounds__(256) k_prep_density(const double *__restrict__ D, int nbf,
+                                                      float2 *__restrict__ dhl,
+                                                      float *__restrict__ colb) {
+  __shared__ float red[256];
+  const int j = blockIdx.x;
+  float mx = 0.f;
+  for (int k = threadIdx.x; k < nbf; k += 256) {
+    const size_t o = static_cast<size_t>(j) * nbf + k;
+    const double d = 2.0 * D[o];
+    const float hi = static_cast<float>(d);
+    dhl[o] = make_float2(hi, static_cast<float>(d - static_cast<double>(hi)));
+    mx = fmaxf(mx, fabsf(hi));
+  }
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    colb[j] = pow2_bound(red[0]);
+}
+
+// V holds only its upper triangle (row <= column) after the mixed build;
+// copy it to the lower one (the final FP64 symmetrisation).
+__global__ void __launch_bounds__(256) k_mirror_upper(double *__restrict__ V, int nbf) {
+  const size_t n = static_cast<size_t>(nbf);
+  for (size_t q = static_cast<size_t>(blockIdx.x) * 256 + threadIdx.x; q < n * n;
+       q += static_cast<size_t>(gridDim.x) * 256) {
+    const size_t c = q / n, r = q % n; // element (r, c), column-major
+    if (r > c)
+      V[q] = V[r * n + c];
+  }
+}
+
 // rho, grad rho of one block.  X = phi D2 is computed on the exact grid:
-// row scales s_p (phi rows, from the collocation) and t_j (D2 columns,
-// computed here), slices a1, a2, a3 / b1, b2, b3 (slice3), three TMEM
+// row scales s_p (phi rows, from the collocation) and t_j (D2 columns, from
+// k_prep_density), slices a1, a2, a3 / b1, b2, b3 (slice3), three TMEM
 // accumulators; a K segment holds at most 512 AOs so that the integer sums
 // of the exact levels stay below 2^24.  The epilogue forms X = acc0 + acc1 +
 // acc2 per segment and accumulates rowsum(phi o X) with compensated sums.
@@ -488,7 +553,8 @@ template <bool DERIV>
 __global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__restrict__ blocks,
                                                       const float *__restrict__ ws,
                                                       const float *__restrict__ rowscale,
-                                                      const double *__restrict__ D,
+                                                      const float2 *__restrict__ dhl,
+                                                      const float *__restrict__ colb,
                                                       double *__restrict__ rho, int *err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
@@ -504,6 +570,12 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__
   // A producer rows: point t & 127; its scale
   const float sA = rowscale[static_cast<size_t>(blockIdx.x) * kBlockPts + (t & 127)];
   const float isA = 1.f / sA;
+  // the block's AO map in shared memory (gathers then need no dependent load)
+  const bool gsh = L.nbf <= kMaxMapSmem;
+  if (gsh)
+    for (int q = t; q < L.nbf; q += blockDim.x)
+      tail->gmap[q] = g[q];
+  const int *gm = gsh ? tail->gmap : g;
 
   Pipe P;
   pipe_init(P, smem, tail->bars, &tail->tmem_slot, 512);
@@ -511,20 +583,9 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__
   const int p = quad * 32 + lane; // this thread's point in the epilogue
   for (int n0 = 0; n0 < B.mp; n0 += kExactN) {
     const int N = min(kExactN, B.mp - n0);
-    // B row scales for this pass: bound of |2 D[k][j]| over the block's AOs k
-    if (t < N) {
-      const int lj = n0 + t;
-      float mx = 0.f;
-      if (lj < L.nbf) {
-        const size_t gj = static_cast<size_t>(g[lj]);
-        for (int lk = 0; lk < L.nbf; lk++)
-          mx = fmaxf(mx, fabsf(static_cast<float>(2.0 * D[static_cast<size_t>(g[lk]) * nbf + gj])));
-      }
-      tail->bscale[t] = pow2_bound(mx);
-    }
+    if (t < N)
+      tail->bscale[t] = (n0 + t < L.nbf) ? colb[gm[n0 + t]] : 1.f;
     __syncthreads();
-    const float sB = (t < N) ? tail->bscale[t] : 1.f;
-    const float isB = 1.f / sB;
     auto fa = [&](int c, uint8_t *st) {
       const int r = t & 127, kh = t >> 7;
 #pragma unroll
@@ -540,23 +601,23 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__
     for (int k0 = 0; k0 < B.mp; k0 += kExactKSeg) {
       const int nk = min(kExactKSeg, B.mp - k0) / kKc;
       auto fa_seg = [&](int c, uint8_t *st) { fa(k0 / kKc + c, st); };
+      // all threads: (row j, 16-byte chunk q) pairs of the N x 32 B tile
       auto fb = [&](int c, uint8_t *st) {
-        const int j = t;
-        if (j >= N)
-          return;
-        const int lj = n0 + j;
-        const bool jv = lj < L.nbf;
-        const size_t gj = jv ? static_cast<size_t>(g[lj]) : 0;
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
+        for (int idx = t; idx < N * 8; idx += 256) {
+          const int j = idx >> 3, q = idx & 7;
+          const int lj = n0 + j;
+          const bool jv = lj < L.nbf;
+          const size_t gj = jv ? static_cast<size_t>(gm[lj]) : 0;
+          const float sB = tail->bscale[j], isB = 1.f / sB;
           float v[4], lo[4];
 #pragma unroll
           for (int e = 0; e < 4; e++) {
             const int lk = k0 + c * kKc + q * 4 + e;
-            const double d =
-                (jv && lk < L.nbf) ? 2.0 * D[static_cast<size_t>(g[lk]) * nbf + gj] : 0.0;
-            v[e] = static_cast<float>(d);
-            lo[e] = static_cast<float>(d - static_cast<double>(v[e]));
+            const float2 d = (jv && lk < L.nbf)
+                                 ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
+                                 : make_float2(0.f, 0.f);
+            v[e] = d.x;
+            lo[e] = d.y;
           }
           store4_exact(st + kOffB1, st + kOffB2, st + kOffB3, j, q, v, sB, isB, lo);
         }
@@ -649,13 +710,11 @@ __global__ void __launch_bounds__(256, 1) k_vxc_mixed(MolDev m, const MBlock *__
         store4(st + kOffAhi, st + kOffAlo, r, kh * 4 + q, v.x, v.y, v.z, v.w);
       }
     };
+    // all threads: (row j, 16-byte chunk q) pairs of the N x 32 B tile
     auto fb = [&](int c, uint8_t *st) {
-      const int j = t;
-      if (j >= N)
-        return;
-      const size_t row = static_cast<size_t>(n0 + j) * kBlockPts + c * kKc;
-#pragma unroll
-      for (int q = 0; q < 8; q++) {
+      for (int idx = t; idx < N * 8; idx += 256) {
+        const int j = idx >> 3, q = idx & 7;
+        const size_t row = static_cast<size_t>(n0 + j) * kBlockPts + c * kKc;
         const int pp = c * kKc + q * 4;
         float4 a = *reinterpret_cast<const float4 *>(phi + row + 4 * q);
         float y[4] = {a.x * tail->coef[0][pp], a.y * tail->coef[0][pp + 1],
@@ -674,26 +733,51 @@ __global__ void __launch_bounds__(256, 1) k_vxc_mixed(MolDev m, const MBlock *__
       }
     };
     gemm_pass<false>(P, N, kBlockPts / kKc, fa, fb, err);
-    // epilogue: rows = AOs it.i0 + quad*32 + lane, this warp's half of N
+    // epilogue: rows = AOs it.i0 + quad*32 + lane, this warp's half of N.
+    // V receives its upper triangle only (the AO map is ascending, so local
+    // order is global order); k_mirror_upper completes it.
     const int li = it.i0 + quad * 32 + lane;
     const bool iv = li < L.nbf;
     const size_t gi = iv ? static_cast<size_t>(g[li]) : 0;
     const int cols = N / 2;
+    const bool whole = (B.mp <= 128); // K of the block fits one tile: symmetrise here
+    float *kt = reinterpret_cast<float *>(P.stage[0]); // [128][129] after the GEMM
     for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
       uint32_t r[16];
       umma::tmem_ld16(P.tmem + (static_cast<uint32_t>(quad * 32) << 16) + c0, r);
       umma::tmem_wait_ld();
-      if (iv) {
+      if (whole) {
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+          kt[(quad * 32 + lane) * 129 + c0 + i] = __uint_as_float(r[i]);
+      } else if (iv) {
 #pragma unroll
         for (int i = 0; i < 16; i++) {
           const int lj = n0 + c0 + i;
           if (lj < L.nbf) {
             const size_t gj = static_cast<size_t>(g[lj]);
             const double k = static_cast<double>(__uint_as_float(r[i]));
-            atomicAdd(&V[gj * nbf + gi], k);
-            atomicAdd(&V[gi * nbf + gj], k);
+            if (gi < gj)
+              atomicAdd(&V[gj * nbf + gi], k);
+            else if (gj < gi)
+              atomicAdd(&V[gi * nbf + gj], k);
+            else
+              atomicAdd(&V[gi * nbf + gi], 2.0 * k);
           }
         }
+      }
+    }
+    if (whole) {
+      __syncthreads();
+      // one atomic per unordered pair: V[a][b] += K[a][b] + K[b][a], a <= b
+      const int mm = L.nbf;
+      for (int idx = t; idx < mm * mm; idx += blockDim.x) {
+        const int a = idx / mm, b = idx - a * mm;
+        if (a > b)
+          continue;
+        const double k = static_cast<double>(kt[a * 129 + b]) +
+                         static_cast<double>(kt[b * 129 + a]);
+        atomicAdd(&V[static_cast<size_t>(g[b]) * nbf + g[a]], k);
       }
     }
     umma::fence_before_sync();
@@ -815,8 +899,11 @@ struct MixedState {
   MBlock *d_blocks = nullptr;
   VItem *d_items = nullptr;
   float4 *d_prim32 = nullptr;
+  float4 *d_shA = nullptr; // shell centres as (hi xyz, lo xyz) float pairs
   float *d_ws = nullptr;
   float *d_rowscale = nullptr;
+  float2 *d_dhl = nullptr; // D2 as (hi, lo) floats, per build
+  float *d_colb = nullptr; // column bounds of D2, per build
   int *d_err = nullptr;
 };
 
@@ -840,6 +927,22 @@ void Molecule::prepare_mixed() {
       S->blocks.push_back(B);
     }
   }
+  // Interleave the V_xc work items: consecutive CTAs (which run at the same
+  // time) then come from distant parts of the Morton order and so update
+  // different V_xc elements, instead of contending for the same ones.
+  {
+    const size_t n = S->items.size(), lanes = 152;
+    std::vector<VItem> il;
+    il.reserve(n);
+    const size_t stride = (n + lanes - 1) / lanes;
+    for (size_t r = 0; r < stride; r++)
+      for (size_t q = 0; q < lanes; q++) {
+        const size_t i = q * stride + r;
+        if (i < n)
+          il.push_back(S->items[i]);
+      }
+    S->items.swap(il);
+  }
   // primitives as (alpha hi, alpha lo, c hi, c lo) float pairs, with OCC's
   // common_fac folded into c in FP64
   for (const Shell &sh : basis.shells) {
@@ -859,12 +962,26 @@ void Molecule::prepare_mixed() {
       cuda_check(cudaMemcpy(dptr, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice),
                  "cudaMemcpy H2D");
   };
+  std::vector<float4> shA;
+  for (const Shell &sh : basis.shells) {
+    float h[3], l[3];
+    for (int d = 0; d < 3; d++) {
+      h[d] = static_cast<float>(sh.origin[d]);
+      l[d] = static_cast<float>(sh.origin[d] - h[d]);
+    }
+    shA.push_back(make_float4(h[0], h[1], h[2], 0.f));
+    shA.push_back(make_float4(l[0], l[1], l[2], 0.f));
+  }
   up(S->blocks, S->d_blocks);
   up(S->items, S->d_items);
   up(S->prim32, S->d_prim32);
+  up(shA, S->d_shA);
   S->d_ws = static_cast<float *>(alloc(std::max<size_t>(S->ws_floats, 1) * sizeof(float)));
   S->d_rowscale = static_cast<float *>(
       alloc(std::max<size_t>(S->blocks.size(), 1) * kBlockPts * sizeof(float)));
+  const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
+  S->d_dhl = static_cast<float2 *>(alloc(std::max<size_t>(nbf2, 1) * sizeof(float2)));
+  S->d_colb = static_cast<float *>(alloc(std::max<int>(basis.nbf, 1) * sizeof(float)));
   S->d_err = static_cast<int *>(alloc(sizeof(int)));
   cuda_check(cudaMemset(S->d_err, 0, sizeof(int)), "cudaMemset");
   set_smem_attributes();
@@ -878,17 +995,21 @@ void Molecule::build_mixed(const double *dD, double *dV, double *dout2, cudaStre
   const int nb = static_cast<int>(S.blocks.size());
   const int ni = static_cast<int>(S.items.size());
   cuda_check(cudaMemsetAsync(dV, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
+  c.launch("prep_density", st, [&] {
+    k_prep_density<<<basis.nbf, 256, 0, st>>>(dD, basis.nbf, S.d_dhl, S.d_colb);
+  });
   if (nb > 0) {
     c.launch("colloc_f32", st, [&] {
-      k_colloc_f32<<<nb, kBlockPts, 0, st>>>(m, S.d_blocks, S.d_prim32, S.d_ws, S.d_rowscale);
+      k_colloc_f32<<<nb, kBlockPts, 0, st>>>(m, S.d_blocks, S.d_prim32, S.d_shA, S.d_ws,
+                                             S.d_rowscale);
     });
     c.launch("rho_mixed", st, [&] {
       if (deriv)
-        k_rho_mixed<true><<<nb, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_ws, S.d_rowscale, dD,
-                                                       d_rho, S.d_err);
+        k_rho_mixed<true><<<nb, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_ws, S.d_rowscale,
+                                                       S.d_dhl, S.d_colb, d_rho, S.d_err);
       else
-        k_rho_mixed<false><<<nb, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_ws, S.d_rowscale, dD,
-                                                        d_rho, S.d_err);
+        k_rho_mixed<false><<<nb, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_ws, S.d_rowscale,
+                                                        S.d_dhl, S.d_colb, d_rho, S.d_err);
     });
   }
   c.launch("func", st, [&] {
@@ -904,6 +1025,11 @@ void Molecule::build_mixed(const double *dD, double *dV, double *dout2, cudaStre
                                                         dV, S.d_err);
     });
   }
+  c.launch("mirror", st, [&] {
+    const size_t n2 = static_cast<size_t>(basis.nbf) * basis.nbf;
+    const int grid = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 4096));
+    k_mirror_upper<<<grid, 256, 0, st>>>(dV, basis.nbf);
+  });
   c.launch("reduce", st, [&] { launch_reduce(d_epart, m.nleaves, dout2, st); });
   cuda_check(cudaGetLastError(), "kernel launch");
 }
