@@ -141,6 +141,56 @@ int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *
 int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
                               int precision, double *d_V, double *d_exc2, void *stream);
 
+/* ---- batches: many molecules' XC builds in one launch sequence -------------
+ * OCC builds one molecule at a time (a TBB loop over one grid); a batch runs
+ * the blocks of all its molecules through the same kernel launches (the
+ * tensor-core kernels persistent over one queue of blocks from every
+ * molecule; LDA and GGA molecules go in one sequence each).  A molecule
+ * appears at most once in a batch.  The batch owns one D, V and
+ * {E_xc, integrated density} device buffer per molecule (same conventions as
+ * occ_xc_compute_vxc_device); write D into them and read V / E_xc back. */
+typedef struct occ_xc_batch occ_xc_batch;
+int occ_xc_batch_create(occ_xc_context *ctx, int nmol, occ_xc_molecule *const *mols,
+                        occ_xc_batch **out);
+void occ_xc_batch_destroy(occ_xc_batch *batch);
+int occ_xc_batch_buffers(occ_xc_batch *batch, int i, double **d_D, double **d_V,
+                         double **d_exc2);
+/* Asynchronous on stream (NULL: the context's stream).  OCC_XC_MIXED: one
+ * launch sequence for the whole batch; OCC_XC_FP64: the molecules' FP64 builds
+ * one after the other. */
+int occ_xc_batch_compute(occ_xc_context *ctx, occ_xc_batch *batch, int precision, void *stream);
+/* Synchronises stream; OCC_XC_ERR_TIMEOUT if a bounded device wait gave up. */
+int occ_xc_batch_check(occ_xc_context *ctx, occ_xc_batch *batch, void *stream);
+/* Host-buffer form: D[i], V[i] are nbf_i x nbf_i host matrices, exc[i] (and
+ * nelec[i] if not NULL) receive E_xc and the integrated density; blocking. */
+int occ_xc_batch_compute_host(occ_xc_context *ctx, occ_xc_batch *batch, int precision,
+                              const double *const *D, double *const *V, double *exc,
+                              double *nelec);
+/* Blocking copies between host memory and molecule i's batch-owned buffers
+ * (D: nbf_i x nbf_i in; V: nbf_i x nbf_i and exc2 = {E_xc, density} out). */
+int occ_xc_batch_set_density(occ_xc_context *ctx, occ_xc_batch *batch, int i, const double *D);
+int occ_xc_batch_get_result(occ_xc_context *ctx, occ_xc_batch *batch, int i, double *V,
+                            double *exc2);
+
+/* ---- CUDA graphs ----------------------------------------------------------
+ * Capture niter consecutive builds of one molecule (build k reads d_D[k] and
+ * writes d_V[k], d_exc2[k]; e.g. the XC builds of the iterations of an SCF
+ * whose densities are known) or one build of a batch into one CUDA graph;
+ * launching the graph replays them with no host work per kernel. */
+typedef struct occ_xc_graph occ_xc_graph;
+int occ_xc_graph_capture(occ_xc_context *ctx, occ_xc_molecule *mol, int precision, int niter,
+                         const double *const *d_D, double *const *d_V, double *const *d_exc2,
+                         occ_xc_graph **out);
+int occ_xc_batch_graph_capture(occ_xc_context *ctx, occ_xc_batch *batch, int precision,
+                               occ_xc_graph **out);
+/* stream NULL: the stream of the context the graph was captured on. */
+int occ_xc_graph_launch(occ_xc_graph *graph, void *stream);
+void occ_xc_graph_destroy(occ_xc_graph *graph);
+
+/* CTAs of the persistent tensor-core kernels (0 = one per SM, the default);
+ * fewer leave SMs free for concurrent builds on other streams. */
+int occ_xc_set_persistent_ctas(occ_xc_context *ctx, int ctas);
+
 /* The FP64 build of occ_xc_compute_vxc_device for callers that cannot
  * allocate device memory -- code inside a host application that owns all of
  * the GPU's memory through its own pool, or code that must never block in the

@@ -10,12 +10,16 @@ from .xc import (  # noqa: F401
     MIXED,
     AOBasis,
     Atom,
+    Batch,
     BuildSettings,
     DFT,
+    Graph,
     GridSettings,
     Molecule,
     Shell,
     XCError,
+    capture_scf_graph,
     library,
     library_path,
+    set_persistent_ctas,
 )

@@ -62,6 +62,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   KernelProfiler prof;
   long launches = 0; // kernels launched by the library on this context
+  int max_ctas = 0;  // CTAs of the persistent tensor-core kernels (0: one per SM)
   explicit Context(int dev);
   ~Context();
   // bracket one kernel launch (profiling) and count it

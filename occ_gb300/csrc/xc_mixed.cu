@@ -21,6 +21,7 @@
 //                  Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi,
 //                  V += K + K^T with FP64 atomics   (src/dft/xc_potential_matrix.cpp:19-41)
 //   k_reduce       fixed-order FP64 sum of the per-leaf partials
+#include <algorithm>
 #include <cstring>
 #include <type_traits>
 
@@ -96,15 +97,54 @@ constexpr uint32_t kWaitIter = 1u << 24; // bounded mbarrier waits
 constexpr int kErrTimeout = 1;
 
 struct MBlock {
-  int leaf;         // index into leaves
+  int mol;          // molecule (row of the MixTab table)
+  int leaf;         // index into that molecule's leaves
   int p0;           // first point of the block within the leaf
   int cnt;          // points in the block (<= 128)
   int mp;           // significant AOs of the leaf, padded to 32
-  long long ws_off; // float offset of the block's [4][mp][128] planes
+  int lblock;       // index of the block within its molecule (row scales)
+  long long ws_off; // float offset of the block's [4][mp][128] planes in the molecule's ws
 };
 struct VItem {
-  int block, i0; // block and first AO row (multiple of 128) of the K tile
+  int block, i0; // block (index into the launch's block list) and first AO row of the tile
 };
+struct LeafItem {
+  int mol, leaf;
+};
+
+// Everything the mixed kernels need of one molecule; a launch covers a table
+// of these (one molecule for a single build, many for a batched build).
+struct MixTab {
+  MolDev m;
+  FuncSet fs;
+  double dens_thr;
+  const float4 *prim32; // primitives (alpha hi, alpha lo, c hi, c lo)
+  const float4 *shA;    // shell centres (hi xyz, lo xyz)
+  float *ws;            // AO values [block][4][mp][128]
+  float *rowscale;      // power-of-two bound of each block row of phi
+  float2 *dhl;          // D2 as (hi, lo) floats
+  float *colb;          // column bounds of D2
+  double *rho, *coef, *epart;
+  const double *D;      // this build's density (mo.D)
+  double *V;            // V_xc (upper triangle, then mirrored)
+  double *out2;         // {E_xc, integrated density}
+};
+
+// Per-launch replacement of a one-molecule table's D / V / out2 (so that a
+// single build can read and write caller-owned buffers without a table update).
+struct Override {
+  const double *D;
+  double *V, *out2;
+};
+__device__ __forceinline__ const double *t_D(const MixTab &T, const Override &o) {
+  return o.D ? o.D : T.D;
+}
+__device__ __forceinline__ double *t_V(const MixTab &T, const Override &o) {
+  return o.V ? o.V : T.V;
+}
+__device__ __forceinline__ double *t_out(const MixTab &T, const Override &o) {
+  return o.out2 ? o.out2 : T.out2;
+}
 
 // Shared state of a CTA's two-stage shared-memory pipeline.
 struct Pipe {
@@ -411,12 +451,14 @@ __device__ __forceinline__ float colloc_shell_f32(const DevShell &sh, bool pure,
 // Exponents and coefficients as (hi, lo) float pairs: rounding alpha or c to
 // one float would bias every point a primitive touches the same way, an error
 // that does not average out over the grid.
-__global__ void __launch_bounds__(128, 4) k_colloc_f32(MolDev m, const MBlock *__restrict__ blocks,
-                                                    const float4 *__restrict__ prim32,
-                                                    const float4 *__restrict__ shA,
-                                                    float *__restrict__ ws,
-                                                    float *__restrict__ rowscale) {
+__global__ void __launch_bounds__(128, 4) k_colloc_f32(const MixTab *__restrict__ tabs,
+                                                    const MBlock *__restrict__ blocks) {
   const MBlock B = blocks[blockIdx.x];
+  const MixTab &T = tabs[B.mol];
+  const MolDev m = T.m;
+  const float4 *__restrict__ prim32 = T.prim32;
+  const float4 *__restrict__ shA = T.shA;
+  float *__restrict__ ws = T.ws;
   const DevLeaf L = m.leaves[B.leaf];
   const int p = threadIdx.x;
   const bool valid = p < B.cnt;
@@ -482,7 +524,7 @@ __global__ void __launch_bounds__(128, 4) k_colloc_f32(MolDev m, const MBlock *_
     base[2 * plane + o] = 0.f;
     base[3 * plane + o] = 0.f;
   }
-  rowscale[static_cast<size_t>(blockIdx.x) * kBlockPts + p] = pow2_bound(vmax);
+  T.rowscale[static_cast<size_t>(B.lblock) * kBlockPts + p] = pow2_bound(vmax);
 }
 
 constexpr uint32_t kSmemMain = 2 * kStageBytes;
@@ -492,7 +534,7 @@ constexpr int kMaxMapSmem = 1024; // block AO maps up to this size live in share
 struct alignas(16) SmemTail {
   uint64_t bars[2];
   uint32_t tmem_slot;
-  uint32_t pad;
+  int next; // work item fetched from the queue, broadcast to the CTA
   float coef[4][kBlockPts];
   float red[2][4][kBlockPts];
   int gmap[kMaxMapSmem];
@@ -507,14 +549,25 @@ __device__ __forceinline__ uint8_t *aligned_smem(uint8_t *raw) {
 
 // Per build: D2 = 2 D as (hi, lo) float pairs and, per column j, a power of
 // two bounding |D2[k][j]| over all k (the column scale of the exact split).
-__global__ void __launch_bounds__(256) k_prep_density(const double *__restrict__ D, int nbf,
-                                                      float2 *__restrict__ dhl,
-                                                      float *__restrict__ colb) {
+// Grid: (max nbf, molecules).
+__global__ void __launch_bounds__(256) k_prep_density(const MixTab *__restrict__ tabs,
+                                                      Override ov, int *queue) {
   __shared__ float red[256];
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 2)
+    queue[threadIdx.x] = 0; // work queues of k_rho_mixed and k_vxc_mixed
+  const MixTab &T = tabs[blockIdx.y];
+  const int nbf = T.m.nbf;
   const int j = blockIdx.x;
+  if (j >= nbf)
+    return;
+  const double *__restrict__ D = t_D(T, ov);
+  double *__restrict__ V = t_V(T, ov);
+  float2 *__restrict__ dhl = T.dhl;
+  float *__restrict__ colb = T.colb;
   float mx = 0.f;
   for (int k = threadIdx.x; k < nbf; k += 256) {
     const size_t o = static_cast<size_t>(j) * nbf + k;
+    V[o] = 0.0; // V_xc is accumulated with atomics later in the build
     const double d = 2.0 * D[o];
     const float hi = static_cast<float>(d);
     dhl[o] = make_float2(hi, static_cast<float>(d - static_cast<double>(hi)));
@@ -532,9 +585,12 @@ __global__ void __launch_bounds__(256) k_prep_density(const double *__restrict__
 }
 
 // V holds only its upper triangle (row <= column) after the mixed build;
-// copy it to the lower one (the final FP64 symmetrisation).
-__global__ void __launch_bounds__(256) k_mirror_upper(double *__restrict__ V, int nbf) {
-  const size_t n = static_cast<size_t>(nbf);
+// copy it to the lower one (the final FP64 symmetrisation).  Grid: (x, molecules).
+__global__ void __launch_bounds__(256) k_mirror_upper(const MixTab *__restrict__ tabs,
+                                                      Override ov) {
+  const MixTab &T = tabs[blockIdx.y];
+  double *__restrict__ V = t_V(T, ov);
+  const size_t n = static_cast<size_t>(T.m.nbf);
   for (size_t q = static_cast<size_t>(blockIdx.x) * 256 + threadIdx.x; q < n * n;
        q += static_cast<size_t>(gridDim.x) * 256) {
     const size_t c = q / n, r = q % n; // element (r, c), column-major
@@ -549,26 +605,39 @@ __global__ void __launch_bounds__(256) k_mirror_upper(double *__restrict__ V, in
 // accumulators; a K segment holds at most 512 AOs so that the integer sums
 // of the exact levels stay below 2^24.  The epilogue forms X = acc0 + acc1 +
 // acc2 per segment and accumulates rowsum(phi o X) with compensated sums.
+// Persistent (TMEM and barriers set up once per CTA): each CTA takes the next
+// block of `order` (most expensive first) from a global counter.
 template <bool DERIV>
-__global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__restrict__ blocks,
-                                                      const float *__restrict__ ws,
-                                                      const float *__restrict__ rowscale,
-                                                      const float2 *__restrict__ dhl,
-                                                      const float *__restrict__ colb,
-                                                      double *__restrict__ rho, int *err) {
+__global__ void __launch_bounds__(256, 1) k_rho_mixed(const MixTab *__restrict__ tabs,
+                                                      const MBlock *__restrict__ blocks,
+                                                      const int *__restrict__ order, int nblocks,
+                                                      int *queue, int *err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
   SmemTail *tail = reinterpret_cast<SmemTail *>(smem + kSmemMain);
-  const MBlock B = blocks[blockIdx.x];
-  const DevLeaf L = m.leaves[B.leaf];
-  const int *g = m.leaf_ao + L.ao_begin;
-  const float *phi = ws + B.ws_off;
-  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
-  const size_t nbf = static_cast<size_t>(m.nbf);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int quad = warp & 3, half = warp >> 2;
+  Pipe P;
+  pipe_init(P, smem, tail->bars, &tail->tmem_slot, 512);
+  for (;;) {
+  if (t == 0)
+    tail->next = atomicAdd(&queue[0], 1);
+  __syncthreads();
+  const int qi = tail->next;
+  if (qi >= nblocks)
+    break;
+  const MBlock B = blocks[order[qi]];
+  const MixTab &T = tabs[B.mol];
+  const MolDev &m = T.m;
+  const DevLeaf L = m.leaves[B.leaf];
+  const int *g = m.leaf_ao + L.ao_begin;
+  const float *phi = T.ws + B.ws_off;
+  const float2 *__restrict__ dhl = T.dhl;
+  const float *__restrict__ colb = T.colb;
+  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+  const size_t nbf = static_cast<size_t>(m.nbf);
   // A producer rows: point t & 127; its scale
-  const float sA = rowscale[static_cast<size_t>(blockIdx.x) * kBlockPts + (t & 127)];
+  const float sA = T.rowscale[static_cast<size_t>(B.lblock) * kBlockPts + (t & 127)];
   const float isA = 1.f / sA;
   // the block's AO map in shared memory (gathers then need no dependent load)
   const bool gsh = L.nbf <= kMaxMapSmem;
@@ -576,9 +645,7 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__
     for (int q = t; q < L.nbf; q += blockDim.x)
       tail->gmap[q] = g[q];
   const int *gm = gsh ? tail->gmap : g;
-
-  Pipe P;
-  pipe_init(P, smem, tail->bars, &tail->tmem_slot, 512);
+  __syncthreads();
   float acc[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
   const int p = quad * 32 + lane; // this thread's point in the epilogue
   for (int n0 = 0; n0 < B.mp; n0 += kExactN) {
@@ -655,6 +722,7 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__
     tail->red[half][c][p] = acc[c] + cmp[c];
   __syncthreads();
   if (t < kBlockPts && t < B.cnt) {
+    double *rho = T.rho;
     const size_t idx = static_cast<size_t>(L.off) + B.p0 + t;
     const size_t Np = static_cast<size_t>(m.npts);
     rho[idx] = static_cast<double>(tail->red[0][0][t]) + static_cast<double>(tail->red[1][0][t]);
@@ -663,29 +731,44 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(MolDev m, const MBlock *__
         rho[c * Np + idx] = 2.0 * (static_cast<double>(tail->red[0][c][t]) +
                                    static_cast<double>(tail->red[1][c][t]));
   }
+  __syncthreads(); // tail->red and gmap are reused by the next block
+  } // blocks
   pipe_finish(P);
 }
 
 // K = phi^T Y for one 128-row AO tile of one block; V += K + K^T (FP64).
+// Persistent over the item list (most expensive first), like k_rho_mixed.
 template <bool DERIV>
-__global__ void __launch_bounds__(256, 1) k_vxc_mixed(MolDev m, const MBlock *__restrict__ blocks,
-                                                      const VItem *__restrict__ items,
-                                                      const float *__restrict__ ws,
-                                                      const double *__restrict__ coef,
-                                                      double *__restrict__ V, int *err) {
+__global__ void __launch_bounds__(256, 1) k_vxc_mixed(const MixTab *__restrict__ tabs,
+                                                      const MBlock *__restrict__ blocks,
+                                                      const VItem *__restrict__ items, int nitems,
+                                                      Override ov, int *queue, int *err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
   SmemTail *tail = reinterpret_cast<SmemTail *>(smem + kSmemMain);
-  const VItem it = items[blockIdx.x];
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int quad = warp & 3, half = warp >> 2;
+  Pipe P;
+  pipe_init(P, smem, tail->bars, &tail->tmem_slot, kMaxN);
+  for (;;) {
+  if (t == 0)
+    tail->next = atomicAdd(&queue[1], 1);
+  __syncthreads();
+  const int ii = tail->next;
+  if (ii >= nitems)
+    break;
+  const VItem it = items[ii];
   const MBlock B = blocks[it.block];
+  const MixTab &T = tabs[B.mol];
+  const MolDev &m = T.m;
   const DevLeaf L = m.leaves[B.leaf];
   const int *g = m.leaf_ao + L.ao_begin;
-  const float *phi = ws + B.ws_off;
+  const float *phi = T.ws + B.ws_off;
+  const double *__restrict__ coef = T.coef;
+  double *__restrict__ V = t_V(T, ov);
   const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
   const size_t nbf = static_cast<size_t>(m.nbf);
   const size_t Np = static_cast<size_t>(m.npts);
-  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int quad = warp & 3, half = warp >> 2;
   // the block's functional coefficients (0 beyond its points)
   for (int q = t; q < 4 * kBlockPts; q += blockDim.x) {
     const int c = q / kBlockPts, pp = q % kBlockPts;
@@ -694,8 +777,7 @@ __global__ void __launch_bounds__(256, 1) k_vxc_mixed(MolDev m, const MBlock *__
       v = static_cast<float>(coef[c * Np + L.off + B.p0 + pp]);
     tail->coef[c][pp] = v;
   }
-  Pipe P;
-  pipe_init(P, smem, tail->bars, &tail->tmem_slot, kMaxN);
+  __syncthreads();
   const int rows = min(128, B.mp - it.i0);
   for (int n0 = 0; n0 < B.mp; n0 += kMaxN) {
     const int N = min(kMaxN, B.mp - n0);
@@ -783,7 +865,100 @@ __global__ void __launch_bounds__(256, 1) k_vxc_mixed(MolDev m, const MBlock *__
     umma::fence_before_sync();
     __syncthreads();
   }
+  } // items
   pipe_finish(P);
+}
+
+// Functional per leaf (one CTA per leaf item), the batched counterpart of the
+// FP64 path's k_func: block skip, FP64 functional, weights, coefficients and
+// the per-leaf energy / electron-count partials.
+__device__ __forceinline__ double bsum256(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < 8; i++)
+    s += sh[i];
+  __syncthreads();
+  return s;
+}
+__device__ __forceinline__ double bmax256(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = sh[0];
+  for (int i = 1; i < 8; i++)
+    s = fmax(s, sh[i]);
+  __syncthreads();
+  return s;
+}
+
+template <bool DERIV>
+__global__ void __launch_bounds__(256) k_func_b(const MixTab *__restrict__ tabs,
+                                                const LeafItem *__restrict__ litems) {
+  __shared__ double sh[8];
+  const LeafItem li = litems[blockIdx.x];
+  const MixTab &T = tabs[li.mol];
+  const DevLeaf L = T.m.leaves[li.leaf];
+  const int p = threadIdx.x;
+  const bool valid = p < L.cnt;
+  const size_t idx = static_cast<size_t>(L.off) + p;
+  const size_t N = static_cast<size_t>(T.m.npts);
+  const double *__restrict__ rho = T.rho;
+  const double r = valid ? rho[idx] : 0.0;
+  const double w = valid ? T.m.pts[idx].w : 0.0;
+  const double mx = bmax256(valid ? r : -1e300, sh);
+  const double nel = bsum256(w * r, sh);
+  double gx = 0, gy = 0, gz = 0, sigma = 0;
+  if (DERIV && valid) {
+    gx = rho[N + idx];
+    gy = rho[2 * N + idx];
+    gz = rho[3 * N + idx];
+    sigma = gx * gx + gy * gy + gz * gz;
+  }
+  double e = 0, vr = 0, vs = 0;
+  if (valid && !(mx < T.dens_thr))
+    eval_xc(T.fs, r, sigma, e, vr, vs);
+  if (valid) {
+    double *__restrict__ coef = T.coef;
+    coef[idx] = 0.5 * w * vr;
+    if (DERIV) {
+      const double f = 2.0 * w * vs;
+      coef[N + idx] = f * gx;
+      coef[2 * N + idx] = f * gy;
+      coef[3 * N + idx] = f * gz;
+    }
+  }
+  const double esum = bsum256(w * e, sh);
+  if (threadIdx.x == 0) {
+    T.epart[2 * li.leaf] = esum;
+    T.epart[2 * li.leaf + 1] = nel;
+  }
+}
+
+// Fixed-order FP64 sums of the per-leaf partials, one CTA per molecule.
+__global__ void __launch_bounds__(256) k_reduce_b(const MixTab *__restrict__ tabs, Override ov) {
+  __shared__ double sh[8];
+  const MixTab &T = tabs[blockIdx.x];
+  const int n = T.m.nleaves;
+  double e = 0.0, ne = 0.0;
+  for (int i = threadIdx.x; i < n; i += 256) {
+    e += T.epart[2 * i];
+    ne += T.epart[2 * i + 1];
+  }
+  e = bsum256(e, sh);
+  ne = bsum256(ne, sh);
+  if (threadIdx.x == 0) {
+    double *o = t_out(T, ov);
+    o[0] = e;
+    o[1] = ne;
+  }
 }
 
 // Self-test: C[128][N] = A[128][K] B[N][K]^T with the 3xTF32 pipeline
@@ -891,13 +1066,32 @@ void set_smem_attributes() {
 
 } // namespace
 
-struct MixedState {
+// Work lists and molecule table of one launch sequence: a single molecule,
+// or a batch whose blocks, items and leaves all go into the same launches.
+struct LaunchPlan {
   std::vector<MBlock> blocks;
   std::vector<VItem> items;
-  std::vector<float4> prim32;
-  size_t ws_floats = 0;
+  std::vector<LeafItem> litems;
+  std::vector<MixTab> tabs;
+  std::vector<int> order; // k_rho_mixed's block order
   MBlock *d_blocks = nullptr;
+  int *d_order = nullptr;
+  int *d_queue = nullptr; // the two work-queue counters
   VItem *d_items = nullptr;
+  LeafItem *d_litems = nullptr;
+  MixTab *d_tabs = nullptr;
+  int maxnbf = 0, deriv = 0;
+  std::vector<void *> owned;
+  ~LaunchPlan() {
+    for (void *p : owned)
+      cudaFree(p);
+  }
+};
+
+// Per-molecule resident state of the mixed path.
+struct MixedState {
+  std::vector<MBlock> blocks; // this molecule's blocks (mol = 0)
+  size_t ws_floats = 0;
   float4 *d_prim32 = nullptr;
   float4 *d_shA = nullptr; // shell centres as (hi xyz, lo xyz) float pairs
   float *d_ws = nullptr;
@@ -905,65 +1099,166 @@ struct MixedState {
   float2 *d_dhl = nullptr; // D2 as (hi, lo) floats, per build
   float *d_colb = nullptr; // column bounds of D2, per build
   int *d_err = nullptr;
+  MixTab tab{};            // host copy; D / V / out2 point at the molecule's buffers
+  LaunchPlan single;       // the one-molecule plan
 };
+
+namespace {
+
+template <typename T> T *plan_upload(LaunchPlan &P, const std::vector<T> &v) {
+  T *d = nullptr;
+  cuda_check(cudaMalloc(&d, std::max<size_t>(v.size(), 1) * sizeof(T)), "cudaMalloc");
+  P.owned.push_back(d);
+  if (!v.empty())
+    cuda_check(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice),
+               "cudaMemcpy H2D");
+  return d;
+}
+
+// Concatenate the molecules' work lists.  Items are interleaved so that CTAs
+// running at the same time come from distant parts of the Morton order (and of
+// the batch) and update different V_xc elements.
+void make_plan(LaunchPlan &P, const std::vector<Molecule *> &mols, const std::vector<MixTab> &tabs) {
+  P.tabs = tabs;
+  P.deriv = mols.empty() ? 0 : mols[0]->deriv;
+  std::vector<VItem> items;
+  for (size_t mi = 0; mi < mols.size(); mi++) {
+    Molecule &M = *mols[mi];
+    if (M.deriv != P.deriv)
+      throw ArgError("a launch plan holds molecules of one functional family (LDA or GGA)");
+    P.maxnbf = std::max(P.maxnbf, M.basis.nbf);
+    const int base = static_cast<int>(P.blocks.size());
+    for (const MBlock &b0 : M.mixed->blocks) {
+      MBlock b = b0;
+      b.mol = static_cast<int>(mi);
+      const int bi = static_cast<int>(P.blocks.size());
+      for (int i0 = 0; i0 < b.mp; i0 += 128)
+        items.push_back({bi, i0});
+      P.blocks.push_back(b);
+    }
+    (void)base;
+    for (size_t l = 0; l < M.leaves.size(); l++)
+      P.litems.push_back({static_cast<int>(mi), static_cast<int>(l)});
+  }
+  // interleave (CTAs running together then work on distant parts of the
+  // Morton order and touch different V elements), then order by decreasing
+  // cost so that the dynamic queue ends with small items (greedy balance)
+  const size_t n = items.size(), lanes = 152, stride = (n + lanes - 1) / lanes;
+  for (size_t r = 0; r < stride; r++)
+    for (size_t q = 0; q < lanes; q++)
+      if (q * stride + r < n)
+        P.items.push_back(items[q * stride + r]);
+  auto vcost = [&](const VItem &v) {
+    const MBlock &b = P.blocks[v.block];
+    return static_cast<long>(std::min(128, b.mp - v.i0)) * b.mp;
+  };
+  std::stable_sort(P.items.begin(), P.items.end(),
+                   [&](const VItem &a, const VItem &b) { return vcost(a) > vcost(b); });
+  const size_t nb = P.blocks.size(), bstride = (nb + lanes - 1) / lanes;
+  for (size_t r = 0; r < bstride; r++)
+    for (size_t q = 0; q < lanes; q++)
+      if (q * bstride + r < nb)
+        P.order.push_back(static_cast<int>(q * bstride + r));
+  std::stable_sort(P.order.begin(), P.order.end(),
+                   [&](int a, int b) { return P.blocks[a].mp > P.blocks[b].mp; });
+  P.d_blocks = plan_upload(P, P.blocks);
+  P.d_order = plan_upload(P, P.order);
+  P.d_queue = plan_upload(P, std::vector<int>(2, 0));
+  P.d_items = plan_upload(P, P.items);
+  P.d_litems = plan_upload(P, P.litems);
+  P.d_tabs = plan_upload(P, P.tabs);
+}
+
+int num_sms(int device) {
+  int n = 0;
+  cuda_check(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device), "attribute");
+  return n;
+}
+
+// The mixed launch sequence of a plan (7 kernels whatever the molecule count).
+void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st, int max_ctas) {
+  const int nmol = static_cast<int>(P.tabs.size());
+  const int nb = static_cast<int>(P.blocks.size());
+  const int ni = static_cast<int>(P.items.size());
+  const int nl = static_cast<int>(P.litems.size());
+  if (nmol == 0)
+    return;
+  const int ctas = max_ctas > 0 ? max_ctas : num_sms(c.device);
+  c.launch("prep_density", st, [&] {
+    k_prep_density<<<dim3(P.maxnbf, nmol), 256, 0, st>>>(P.d_tabs, ov, P.d_queue);
+  });
+  if (nb > 0) {
+    c.launch("colloc_f32", st, [&] { k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks); });
+    c.launch("rho_mixed", st, [&] {
+      const int g = std::min(nb, ctas);
+      if (P.deriv)
+        k_rho_mixed<true><<<g, 256, kSmemTotal, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
+                                                      P.d_queue, err);
+      else
+        k_rho_mixed<false><<<g, 256, kSmemTotal, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
+                                                       P.d_queue, err);
+    });
+  }
+  if (nl > 0)
+    c.launch("func", st, [&] {
+      if (P.deriv)
+        k_func_b<true><<<nl, 256, 0, st>>>(P.d_tabs, P.d_litems);
+      else
+        k_func_b<false><<<nl, 256, 0, st>>>(P.d_tabs, P.d_litems);
+    });
+  if (ni > 0)
+    c.launch("vxc_mixed", st, [&] {
+      const int g = std::min(ni, ctas);
+      if (P.deriv)
+        k_vxc_mixed<true><<<g, 256, kSmemTotal, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov,
+                                                      P.d_queue, err);
+      else
+        k_vxc_mixed<false><<<g, 256, kSmemTotal, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov,
+                                                       P.d_queue, err);
+    });
+  c.launch("mirror", st, [&] {
+    const size_t n2 = static_cast<size_t>(P.maxnbf) * P.maxnbf;
+    const int gx = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
+    k_mirror_upper<<<dim3(gx, nmol), 256, 0, st>>>(P.d_tabs, ov);
+  });
+  c.launch("reduce", st, [&] { k_reduce_b<<<nmol, 256, 0, st>>>(P.d_tabs, ov); });
+  cuda_check(cudaGetLastError(), "kernel launch");
+}
+
+} // namespace
 
 void Molecule::prepare_mixed() {
   MixedState *S = new MixedState();
   mixed = S;
+  int lblock = 0;
   for (size_t li = 0; li < leaves.size(); li++) {
     const DevLeaf &L = leaves[li];
     const int mp = static_cast<int>(round_up(L.nbf, kKc));
     for (int p0 = 0; p0 < L.cnt; p0 += kBlockPts) {
       MBlock B;
+      B.mol = 0;
       B.leaf = static_cast<int>(li);
       B.p0 = p0;
       B.cnt = std::min(kBlockPts, L.cnt - p0);
       B.mp = mp;
+      B.lblock = lblock++;
       B.ws_off = static_cast<long long>(S->ws_floats);
       S->ws_floats += static_cast<size_t>(4) * mp * kBlockPts;
-      const int bi = static_cast<int>(S->blocks.size());
-      for (int i0 = 0; i0 < mp; i0 += 128)
-        S->items.push_back({bi, i0});
       S->blocks.push_back(B);
     }
   }
-  // Interleave the V_xc work items: consecutive CTAs (which run at the same
-  // time) then come from distant parts of the Morton order and so update
-  // different V_xc elements, instead of contending for the same ones.
-  {
-    const size_t n = S->items.size(), lanes = 152;
-    std::vector<VItem> il;
-    il.reserve(n);
-    const size_t stride = (n + lanes - 1) / lanes;
-    for (size_t r = 0; r < stride; r++)
-      for (size_t q = 0; q < lanes; q++) {
-        const size_t i = q * stride + r;
-        if (i < n)
-          il.push_back(S->items[i]);
-      }
-    S->items.swap(il);
-  }
   // primitives as (alpha hi, alpha lo, c hi, c lo) float pairs, with OCC's
   // common_fac folded into c in FP64
+  std::vector<float4> prim32, shA;
   for (const Shell &sh : basis.shells) {
     const double fac = common_fac(sh.l, basis.pure);
     for (size_t k = 0; k < sh.exps.size(); k++) {
       const double c = sh.coefs[k] * fac;
       const float ah = static_cast<float>(sh.exps[k]);
       const float ch = static_cast<float>(c);
-      S->prim32.push_back(make_float4(ah, static_cast<float>(sh.exps[k] - ah), ch,
-                                      static_cast<float>(c - ch)));
+      prim32.push_back(make_float4(ah, static_cast<float>(sh.exps[k] - ah), ch,
+                                   static_cast<float>(c - ch)));
     }
-  }
-  auto up = [&](auto &vec, auto *&dptr) {
-    using T = typename std::remove_reference<decltype(vec)>::type::value_type;
-    dptr = static_cast<T *>(alloc(std::max<size_t>(vec.size(), 1) * sizeof(T)));
-    if (!vec.empty())
-      cuda_check(cudaMemcpy(dptr, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice),
-                 "cudaMemcpy H2D");
-  };
-  std::vector<float4> shA;
-  for (const Shell &sh : basis.shells) {
     float h[3], l[3];
     for (int d = 0; d < 3; d++) {
       h[d] = static_cast<float>(sh.origin[d]);
@@ -972,9 +1267,14 @@ void Molecule::prepare_mixed() {
     shA.push_back(make_float4(h[0], h[1], h[2], 0.f));
     shA.push_back(make_float4(l[0], l[1], l[2], 0.f));
   }
-  up(S->blocks, S->d_blocks);
-  up(S->items, S->d_items);
-  up(S->prim32, S->d_prim32);
+  auto up = [&](auto &vec, auto *&dptr) {
+    using T = typename std::remove_reference<decltype(vec)>::type::value_type;
+    dptr = static_cast<T *>(alloc(std::max<size_t>(vec.size(), 1) * sizeof(T)));
+    if (!vec.empty())
+      cuda_check(cudaMemcpy(dptr, vec.data(), vec.size() * sizeof(T), cudaMemcpyHostToDevice),
+                 "cudaMemcpy H2D");
+  };
+  up(prim32, S->d_prim32);
   up(shA, S->d_shA);
   S->d_ws = static_cast<float *>(alloc(std::max<size_t>(S->ws_floats, 1) * sizeof(float)));
   S->d_rowscale = static_cast<float *>(
@@ -984,54 +1284,28 @@ void Molecule::prepare_mixed() {
   S->d_colb = static_cast<float *>(alloc(std::max<int>(basis.nbf, 1) * sizeof(float)));
   S->d_err = static_cast<int *>(alloc(sizeof(int)));
   cuda_check(cudaMemset(S->d_err, 0, sizeof(int)), "cudaMemset");
+  MixTab &T = S->tab;
+  T.m = dev();
+  T.fs = fs;
+  T.dens_thr = bs.density_threshold;
+  T.prim32 = S->d_prim32;
+  T.shA = S->d_shA;
+  T.ws = S->d_ws;
+  T.rowscale = S->d_rowscale;
+  T.dhl = S->d_dhl;
+  T.colb = S->d_colb;
+  T.rho = d_rho;
+  T.coef = d_coef;
+  T.epart = d_epart;
+  T.D = d_D;
+  T.V = d_V;
+  T.out2 = d_out2;
+  make_plan(S->single, {this}, {T});
   set_smem_attributes();
 }
 
 void Molecule::build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st) {
-  MixedState &S = *mixed;
-  const MolDev m = dev();
-  Context &c = *ctx;
-  const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
-  const int nb = static_cast<int>(S.blocks.size());
-  const int ni = static_cast<int>(S.items.size());
-  cuda_check(cudaMemsetAsync(dV, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
-  c.launch("prep_density", st, [&] {
-    k_prep_density<<<basis.nbf, 256, 0, st>>>(dD, basis.nbf, S.d_dhl, S.d_colb);
-  });
-  if (nb > 0) {
-    c.launch("colloc_f32", st, [&] {
-      k_colloc_f32<<<nb, kBlockPts, 0, st>>>(m, S.d_blocks, S.d_prim32, S.d_shA, S.d_ws,
-                                             S.d_rowscale);
-    });
-    c.launch("rho_mixed", st, [&] {
-      if (deriv)
-        k_rho_mixed<true><<<nb, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_ws, S.d_rowscale,
-                                                       S.d_dhl, S.d_colb, d_rho, S.d_err);
-      else
-        k_rho_mixed<false><<<nb, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_ws, S.d_rowscale,
-                                                        S.d_dhl, S.d_colb, d_rho, S.d_err);
-    });
-  }
-  c.launch("func", st, [&] {
-    launch_func(m, deriv, fs, bs.density_threshold, d_rho, d_coef, d_epart, st);
-  });
-  if (ni > 0) {
-    c.launch("vxc_mixed", st, [&] {
-      if (deriv)
-        k_vxc_mixed<true><<<ni, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_items, S.d_ws, d_coef,
-                                                       dV, S.d_err);
-      else
-        k_vxc_mixed<false><<<ni, 256, kSmemTotal, st>>>(m, S.d_blocks, S.d_items, S.d_ws, d_coef,
-                                                        dV, S.d_err);
-    });
-  }
-  c.launch("mirror", st, [&] {
-    const size_t n2 = static_cast<size_t>(basis.nbf) * basis.nbf;
-    const int grid = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 4096));
-    k_mirror_upper<<<grid, 256, 0, st>>>(dV, basis.nbf);
-  });
-  c.launch("reduce", st, [&] { launch_reduce(d_epart, m.nleaves, dout2, st); });
-  cuda_check(cudaGetLastError(), "kernel launch");
+  run_plan(mixed->single, *ctx, Override{dD, dV, dout2}, mixed->d_err, st, ctx->max_ctas);
 }
 
 int mixed_error_flag(Molecule &M, cudaStream_t st) {
@@ -1045,6 +1319,82 @@ int mixed_error_flag(Molecule &M, cudaStream_t st) {
 }
 
 void free_mixed(MixedState *S) { delete S; }
+
+// ---- batches ---------------------------------------------------------------
+struct Batch {
+  std::vector<Molecule *> mols;
+  std::vector<double *> dD, dV, dE; // batch-owned buffers, one set per molecule
+  LaunchPlan plan[2];               // LDA molecules, GGA molecules
+  int *d_err = nullptr;
+  Context *ctx = nullptr;
+  ~Batch() {
+    for (double *p : dD)
+      cudaFree(p);
+    for (double *p : dV)
+      cudaFree(p);
+    for (double *p : dE)
+      cudaFree(p);
+    cudaFree(d_err);
+  }
+};
+
+Batch *batch_create(Context *ctx, const std::vector<Molecule *> &mols) {
+  auto B = std::make_unique<Batch>();
+  B->ctx = ctx;
+  B->mols = mols;
+  std::vector<MixTab> tabs[2];
+  std::vector<Molecule *> group[2];
+  for (size_t i = 0; i < mols.size(); i++) {
+    for (size_t j = 0; j < i; j++)
+      if (mols[j] == mols[i])
+        throw ArgError("a molecule may appear only once in a batch (its workspace is shared)");
+    const size_t n2 = static_cast<size_t>(mols[i]->basis.nbf) * mols[i]->basis.nbf;
+    double *d = nullptr, *v = nullptr, *e = nullptr;
+    cuda_check(cudaMalloc(&d, std::max<size_t>(n2, 1) * sizeof(double)), "cudaMalloc");
+    B->dD.push_back(d);
+    cuda_check(cudaMalloc(&v, std::max<size_t>(n2, 1) * sizeof(double)), "cudaMalloc");
+    B->dV.push_back(v);
+    cuda_check(cudaMalloc(&e, 2 * sizeof(double)), "cudaMalloc");
+    B->dE.push_back(e);
+    MixTab T = mols[i]->mixed->tab;
+    T.D = d;
+    T.V = v;
+    T.out2 = e;
+    const int g = mols[i]->deriv ? 1 : 0;
+    tabs[g].push_back(T);
+    group[g].push_back(mols[i]);
+  }
+  cuda_check(cudaMalloc(&B->d_err, sizeof(int)), "cudaMalloc");
+  cuda_check(cudaMemset(B->d_err, 0, sizeof(int)), "cudaMemset");
+  for (int g = 0; g < 2; g++)
+    if (!group[g].empty())
+      make_plan(B->plan[g], group[g], tabs[g]);
+  return B.release();
+}
+
+void batch_build(Batch &B, int precision, cudaStream_t st) {
+  if (precision == OCC_XC_MIXED) {
+    for (LaunchPlan &P : B.plan)
+      run_plan(P, *B.ctx, Override{nullptr, nullptr, nullptr}, B.d_err, st, B.ctx->max_ctas);
+  } else {
+    for (size_t i = 0; i < B.mols.size(); i++)
+      B.mols[i]->build_fp64(B.dD[i], B.dV[i], B.dE[i], st);
+  }
+}
+
+void batch_destroy(Batch *B) { delete B; }
+void batch_buffers(Batch &B, int i, double **d, double **v, double **e) {
+  *d = B.dD.at(i);
+  *v = B.dV.at(i);
+  *e = B.dE.at(i);
+}
+int batch_size(const Batch &B) { return static_cast<int>(B.mols.size()); }
+int batch_error_flag(Batch &B, cudaStream_t st) {
+  int h = 0;
+  cuda_check(cudaMemcpyAsync(&h, B.d_err, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+  cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  return h;
+}
 
 } // namespace occx
 
@@ -1093,4 +1443,252 @@ extern "C" int occ_xc_selftest_tf32_gemm(occ_xc_context *ctx, int exact, int N, 
   cudaFree(dC);
   cudaFree(dErr);
   return rc;
+}
+
+// ---- batches and CUDA graphs (C ABI) ----------------------------------------
+struct occ_xc_batch {
+  occx::Batch *impl;
+  occ_xc_context *ctx;
+};
+struct occ_xc_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int device = 0;
+  cudaStream_t stream = nullptr; // the context's stream: where a NULL-stream launch goes
+};
+
+namespace {
+template <typename F> int api_guard(occ_xc_context *ctx, F &&f) {
+  try {
+    f();
+    return OCC_XC_OK;
+  } catch (const MethodError &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_METHOD;
+  } catch (const ArgError &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_ARG;
+  } catch (const TimeoutError &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_TIMEOUT;
+  } catch (const CudaError &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_CUDA;
+  } catch (const std::exception &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_INTERNAL;
+  }
+}
+
+// Capture what `body` launches on a private stream into an instantiated graph.
+template <typename F> occ_xc_graph *capture(Context &c, F &&body) {
+  auto G = std::make_unique<occ_xc_graph>();
+  G->device = c.device;
+  G->stream = c.stream;
+  cudaStream_t st;
+  cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+  const bool prof = c.prof.on;
+  c.prof.on = false; // no profiling events inside a graph
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    try {
+      body(st);
+    } catch (...) {
+      cudaGraph_t g;
+      cudaStreamEndCapture(st, &g);
+      if (g)
+        cudaGraphDestroy(g);
+      cudaStreamDestroy(st);
+      c.prof.on = prof;
+      throw;
+    }
+    e = cudaStreamEndCapture(st, &G->graph);
+  }
+  c.prof.on = prof;
+  cudaStreamDestroy(st);
+  cuda_check(e, "stream capture");
+  cuda_check(cudaGraphInstantiate(&G->exec, G->graph, 0), "cudaGraphInstantiate");
+  return G.release();
+}
+} // namespace
+
+extern "C" {
+
+int occ_xc_batch_create(occ_xc_context *ctx, int nmol, occ_xc_molecule *const *mols,
+                        occ_xc_batch **out) {
+  if (!ctx || !out || nmol <= 0 || !mols)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *out = nullptr;
+  return api_guard(ctx, [&] {
+    std::vector<Molecule *> ms;
+    for (int i = 0; i < nmol; i++) {
+      if (!mols[i] || mols[i]->ctx != ctx)
+        throw ArgError("every molecule of a batch must belong to the batch's context");
+      ms.push_back(mols[i]->impl.get());
+    }
+    cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
+    auto b = std::make_unique<occ_xc_batch>();
+    b->ctx = ctx;
+    b->impl = batch_create(ctx->impl.get(), ms);
+    *out = b.release();
+  });
+}
+
+void occ_xc_batch_destroy(occ_xc_batch *b) {
+  if (!b)
+    return;
+  batch_destroy(b->impl);
+  delete b;
+}
+
+int occ_xc_batch_buffers(occ_xc_batch *b, int i, double **d_D, double **d_V, double **d_exc2) {
+  if (!b || !d_D || !d_V || !d_exc2 || i < 0 || i >= batch_size(*b->impl))
+    return OCC_XC_ERR_ARG;
+  batch_buffers(*b->impl, i, d_D, d_V, d_exc2);
+  return OCC_XC_OK;
+}
+
+int occ_xc_batch_compute(occ_xc_context *ctx, occ_xc_batch *b, int precision, void *stream) {
+  if (!ctx || !b || (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED))
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return api_guard(ctx, [&] {
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
+    batch_build(*b->impl, precision, st);
+  });
+}
+
+int occ_xc_batch_check(occ_xc_context *ctx, occ_xc_batch *b, void *stream) {
+  if (!ctx || !b)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return api_guard(ctx, [&] {
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
+    if (batch_error_flag(*b->impl, st))
+      throw TimeoutError("a bounded wait of the tensor-core pipeline gave up");
+  });
+}
+
+int occ_xc_graph_capture(occ_xc_context *ctx, occ_xc_molecule *mol, int precision, int niter,
+                         const double *const *d_D, double *const *d_V,
+                         double *const *d_exc2, occ_xc_graph **out) {
+  if (!ctx || !mol || !out || niter <= 0 || !d_D || !d_V || !d_exc2 ||
+      (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED))
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *out = nullptr;
+  return api_guard(ctx, [&] {
+    cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
+    *out = capture(*ctx->impl, [&](cudaStream_t st) {
+      for (int k = 0; k < niter; k++)
+        mol->impl->build(precision, d_D[k], d_V[k], d_exc2[k], st);
+    });
+  });
+}
+
+int occ_xc_batch_graph_capture(occ_xc_context *ctx, occ_xc_batch *b, int precision,
+                               occ_xc_graph **out) {
+  if (!ctx || !b || !out || (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED))
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *out = nullptr;
+  return api_guard(ctx, [&] {
+    cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
+    *out = capture(*ctx->impl, [&](cudaStream_t st) { batch_build(*b->impl, precision, st); });
+  });
+}
+
+int occ_xc_graph_launch(occ_xc_graph *g, void *stream) {
+  if (!g || !g->exec)
+    return OCC_XC_ERR_ARG;
+  cudaError_t e = cudaGraphLaunch(g->exec, stream ? static_cast<cudaStream_t>(stream) : g->stream);
+  return e == cudaSuccess ? OCC_XC_OK : OCC_XC_ERR_CUDA;
+}
+
+void occ_xc_graph_destroy(occ_xc_graph *g) {
+  if (!g)
+    return;
+  cudaSetDevice(g->device);
+  if (g->exec)
+    cudaGraphExecDestroy(g->exec);
+  if (g->graph)
+    cudaGraphDestroy(g->graph);
+  delete g;
+}
+
+int occ_xc_set_persistent_ctas(occ_xc_context *ctx, int ctas) {
+  if (!ctx || ctas < 0)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->impl->max_ctas = ctas;
+  return OCC_XC_OK;
+}
+
+} // extern "C"
+
+extern "C" int occ_xc_batch_compute_host(occ_xc_context *ctx, occ_xc_batch *b, int precision,
+                                         const double *const *D, double *const *V, double *exc,
+                                         double *nelec) {
+  if (!ctx || !b || !D || !V || !exc || (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED))
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return api_guard(ctx, [&] {
+    Batch &B = *b->impl;
+    cudaStream_t st = ctx->impl->stream;
+    for (size_t i = 0; i < B.mols.size(); i++) {
+      const size_t n2 = static_cast<size_t>(B.mols[i]->basis.nbf) * B.mols[i]->basis.nbf;
+      cuda_check(cudaMemcpyAsync(B.dD[i], D[i], n2 * sizeof(double), cudaMemcpyHostToDevice, st),
+                 "H2D");
+    }
+    batch_build(B, precision, st);
+    std::vector<double> e2(2 * B.mols.size());
+    for (size_t i = 0; i < B.mols.size(); i++) {
+      const size_t n2 = static_cast<size_t>(B.mols[i]->basis.nbf) * B.mols[i]->basis.nbf;
+      cuda_check(cudaMemcpyAsync(V[i], B.dV[i], n2 * sizeof(double), cudaMemcpyDeviceToHost, st),
+                 "D2H");
+      cuda_check(cudaMemcpyAsync(&e2[2 * i], B.dE[i], 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                 st), "D2H");
+    }
+    cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (precision == OCC_XC_MIXED && batch_error_flag(B, st))
+      throw TimeoutError("a bounded wait of the tensor-core pipeline gave up");
+    for (size_t i = 0; i < B.mols.size(); i++) {
+      exc[i] = e2[2 * i];
+      if (nelec)
+        nelec[i] = e2[2 * i + 1];
+    }
+  });
+}
+
+extern "C" int occ_xc_batch_set_density(occ_xc_context *ctx, occ_xc_batch *b, int i,
+                                        const double *D) {
+  if (!ctx || !b || !D || i < 0 || i >= batch_size(*b->impl))
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return api_guard(ctx, [&] {
+    Batch &B = *b->impl;
+    const size_t n2 = static_cast<size_t>(B.mols[i]->basis.nbf) * B.mols[i]->basis.nbf;
+    cudaStream_t st = ctx->impl->stream;
+    cuda_check(cudaMemcpyAsync(B.dD[i], D, n2 * sizeof(double), cudaMemcpyHostToDevice, st),
+               "H2D");
+    cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  });
+}
+
+extern "C" int occ_xc_batch_get_result(occ_xc_context *ctx, occ_xc_batch *b, int i, double *V,
+                                       double *exc2) {
+  if (!ctx || !b || !V || !exc2 || i < 0 || i >= batch_size(*b->impl))
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return api_guard(ctx, [&] {
+    Batch &B = *b->impl;
+    const size_t n2 = static_cast<size_t>(B.mols[i]->basis.nbf) * B.mols[i]->basis.nbf;
+    cudaStream_t st = ctx->impl->stream;
+    cuda_check(cudaMemcpyAsync(V, B.dV[i], n2 * sizeof(double), cudaMemcpyDeviceToHost, st),
+               "D2H");
+    cuda_check(cudaMemcpyAsync(exc2, B.dE[i], 2 * sizeof(double), cudaMemcpyDeviceToHost, st),
+               "D2H");
+    cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  });
 }

@@ -78,6 +78,21 @@ def library():
     lib.occ_xc_compute_vxc.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp, _dp, _dp]
     lib.occ_xc_compute_vxc_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                               C.c_void_p, C.c_void_p, C.c_void_p]
+    _vp = C.c_void_p
+    _pp = C.POINTER(C.c_void_p)
+    lib.occ_xc_batch_create.argtypes = [_vp, C.c_int, _pp, _pp]
+    lib.occ_xc_batch_destroy.argtypes = [_vp]
+    lib.occ_xc_batch_buffers.argtypes = [_vp, C.c_int, _pp, _pp, _pp]
+    lib.occ_xc_batch_compute.argtypes = [_vp, _vp, C.c_int, _vp]
+    lib.occ_xc_batch_check.argtypes = [_vp, _vp, _vp]
+    lib.occ_xc_batch_compute_host.argtypes = [_vp, _vp, C.c_int, _pp, _pp, _dp, _dp]
+    lib.occ_xc_graph_capture.argtypes = [_vp, _vp, C.c_int, C.c_int, _pp, _pp, _pp, _pp]
+    lib.occ_xc_batch_graph_capture.argtypes = [_vp, _vp, C.c_int, _pp]
+    lib.occ_xc_graph_launch.argtypes = [_vp, _vp]
+    lib.occ_xc_graph_destroy.argtypes = [_vp]
+    lib.occ_xc_set_persistent_ctas.argtypes = [_vp, C.c_int]
+    lib.occ_xc_batch_set_density.argtypes = [_vp, _vp, C.c_int, _dp]
+    lib.occ_xc_batch_get_result.argtypes = [_vp, _vp, C.c_int, _dp, _dp]
     _LIB = lib
     return lib
 
@@ -311,3 +326,137 @@ class DFT:
 
     def integrated_density(self):
         return self._nelec
+
+
+class Batch:
+    """Several molecules built together: one persistent launch sequence per
+    precision, the molecules' leaves interleaved over the SMs."""
+
+    def __init__(self, dfts):
+        if not dfts:
+            raise XCError("a batch needs at least one molecule")
+        self.dfts = list(dfts)
+        self.ctx = self.dfts[0].ctx
+        if any(d.ctx is not self.ctx for d in self.dfts):
+            raise XCError("every molecule of a batch must be on the same device")
+        hs = (C.c_void_p * len(self.dfts))(*[d.h.value for d in self.dfts])
+        h = C.c_void_p()
+        rc = self.ctx.lib.occ_xc_batch_create(self.ctx.h, len(self.dfts), hs, C.byref(h))
+        if rc != 0:
+            raise XCError(f"occ_xc_batch_create failed ({rc}): {self.ctx.error()}")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.occ_xc_batch_destroy(self.h)
+            self.h = None
+
+    def __len__(self):
+        return len(self.dfts)
+
+    def device_buffers(self, i):
+        """(D, V, exc2) device addresses of molecule i's batch-owned buffers."""
+        d, v, e = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        rc = self.ctx.lib.occ_xc_batch_buffers(self.h, i, C.byref(d), C.byref(v), C.byref(e))
+        if rc != 0:
+            raise XCError(f"occ_xc_batch_buffers failed ({rc})")
+        return d.value, v.value, e.value
+
+    def compute_vxc(self, Ds, precision=FP64):
+        """V_xc for every molecule; returns (Vs, E_xc array, integrated densities)."""
+        if len(Ds) != len(self.dfts):
+            raise XCError(f"expected {len(self.dfts)} density matrices")
+        Dm, Vs = [], []
+        for D, dft in zip(Ds, self.dfts):
+            n = dft.nbf()
+            a = np.asfortranarray(np.asarray(D, dtype=np.float64))
+            if a.shape != (n, n):
+                raise XCError(f"density matrix must be {n}x{n}")
+            Dm.append(a)
+            Vs.append(np.zeros((n, n), order="F"))
+        k = len(Dm)
+        dp = (C.c_void_p * k)(*[a.ctypes.data for a in Dm])
+        vp = (C.c_void_p * k)(*[a.ctypes.data for a in Vs])
+        exc = np.zeros(k)
+        nel = np.zeros(k)
+        rc = self.ctx.lib.occ_xc_batch_compute_host(self.ctx.h, self.h, int(precision), dp, vp,
+                                                    _ptr(exc), _ptr(nel))
+        if rc != 0:
+            raise XCError(f"occ_xc_batch_compute_host failed ({rc}): {self.ctx.error()}")
+        return Vs, exc, nel
+
+    def set_density(self, i, D):
+        n = self.dfts[i].nbf()
+        a = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if a.shape != (n, n):
+            raise XCError(f"density matrix must be {n}x{n}")
+        rc = self.ctx.lib.occ_xc_batch_set_density(self.ctx.h, self.h, i, _ptr(a))
+        if rc != 0:
+            raise XCError(f"occ_xc_batch_set_density failed ({rc}): {self.ctx.error()}")
+
+    def result(self, i):
+        """(V, E_xc, integrated density) of molecule i from the batch buffers."""
+        n = self.dfts[i].nbf()
+        V = np.zeros((n, n), order="F")
+        e2 = np.zeros(2)
+        rc = self.ctx.lib.occ_xc_batch_get_result(self.ctx.h, self.h, i, _ptr(V), _ptr(e2))
+        if rc != 0:
+            raise XCError(f"occ_xc_batch_get_result failed ({rc}): {self.ctx.error()}")
+        return V, e2[0], e2[1]
+
+    def capture_graph(self, precision=MIXED):
+        """One build of the whole batch as a CUDA graph over its own buffers."""
+        g = C.c_void_p()
+        rc = self.ctx.lib.occ_xc_batch_graph_capture(self.ctx.h, self.h, int(precision),
+                                                     C.byref(g))
+        if rc != 0:
+            raise XCError(f"occ_xc_batch_graph_capture failed ({rc}): {self.ctx.error()}")
+        return Graph(self.ctx, g, keep=self)
+
+    def check(self, stream=None):
+        rc = self.ctx.lib.occ_xc_batch_check(self.ctx.h, self.h, stream)
+        if rc != 0:
+            raise XCError(f"occ_xc_batch_check failed ({rc}): {self.ctx.error()}")
+
+
+class Graph:
+    """An instantiated CUDA graph of XC builds; launch() replays it."""
+
+    def __init__(self, ctx, h, keep=None):
+        self.ctx = ctx
+        self.h = h
+        self._keep = keep
+
+    def launch(self, stream=None):
+        rc = self.ctx.lib.occ_xc_graph_launch(self.h, stream)
+        if rc != 0:
+            raise XCError(f"occ_xc_graph_launch failed ({rc})")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.occ_xc_graph_destroy(self.h)
+            self.h = None
+
+
+def capture_scf_graph(dft, precision, d_D, d_V, d_exc2):
+    """Capture len(d_D) consecutive builds of one molecule (build k reads the
+    device matrix at address d_D[k], writes d_V[k] and the two doubles at
+    d_exc2[k]) as one CUDA graph."""
+    k = len(d_D)
+    if not (k == len(d_V) == len(d_exc2)) or k == 0:
+        raise XCError("d_D, d_V and d_exc2 need one address per iteration")
+    arr = lambda xs: (C.c_void_p * k)(*[int(x) for x in xs])  # noqa: E731
+    g = C.c_void_p()
+    rc = dft.ctx.lib.occ_xc_graph_capture(dft.ctx.h, dft.h, int(precision), k, arr(d_D),
+                                          arr(d_V), arr(d_exc2), C.byref(g))
+    if rc != 0:
+        raise XCError(f"occ_xc_graph_capture failed ({rc}): {dft.ctx.error()}")
+    return Graph(dft.ctx, g, keep=dft)
+
+
+def set_persistent_ctas(ctas, device=0):
+    """CTAs of the persistent tensor-core kernels (0: one per SM)."""
+    ctx = _context(device)
+    rc = ctx.lib.occ_xc_set_persistent_ctas(ctx.h, int(ctas))
+    if rc != 0:
+        raise XCError(f"occ_xc_set_persistent_ctas failed ({rc})")
