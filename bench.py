@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--waters", type=int, default=32,
                     help="cluster size (32 is the benchmark; smaller only for profiling)")
+    ap.add_argument("--ctas", type=int, default=0,
+                    help="CTAs of the persistent tensor-core kernels (0: one per SM)")
     return ap.parse_args()
 
 
@@ -272,6 +274,7 @@ def main():
         dist.init_process_group("nccl")
     mol, basis, D = make_workload(seed=0, waters=args.waters)
     dft = og.DFT("pbe", basis, device=local)
+    og.set_persistent_ctas(args.ctas, device=local)
     info = dft.info()
     lib = dft.ctx.lib
     lib.occ_xc_launch_count.restype = C.c_long

@@ -187,6 +187,70 @@ int occ_xc_batch_graph_capture(occ_xc_context *ctx, occ_xc_batch *batch, int pre
 int occ_xc_graph_launch(occ_xc_graph *graph, void *stream);
 void occ_xc_graph_destroy(occ_xc_graph *graph);
 
+/* ---- serving loop ----------------------------------------------------------
+ * Builds of many molecules through one GPU (OCC itself has no server; this
+ * is the xc_submit / xc_poll layer in front of compute_vxc).  A client opens
+ * a session per molecule -- the grid and screening are built on the calling
+ * thread, no device memory yet -- then submits one density per SCF
+ * iteration and collects V_xc / E_xc by ticket.  A worker thread owns the
+ * GPU: each tick it takes the oldest pending build of up to max_batch
+ * sessions (one per session, so a session's builds run in submission order)
+ * and runs them through one launch sequence.  A session's device state is
+ * materialised when it is admitted, which happens only while the admitted
+ * sessions' device bytes (an upper bound computed at open) fit the budget;
+ * a session that could never fit is refused at open with OCC_XC_ERR_NOMEM.
+ * Closing a session frees its device state after its pending builds.  All
+ * calls are thread-safe; errors are described by occ_xc_server_last_error()
+ * of the calling thread. */
+typedef struct occ_xc_server occ_xc_server;
+typedef struct {
+  double hbm_budget_bytes; /* 150e9 */
+  int queue_capacity;      /* pending builds before submit returns BUSY (4096) */
+  int max_batch;           /* builds per tick (64) */
+  int precision;           /* OCC_XC_MIXED */
+} occ_xc_server_settings;
+typedef struct {
+  long completed, failed, pending, ticks;
+  long sessions_admitted, sessions_waiting;
+  double mean_batch;            /* builds per tick */
+  double p50_ms, p99_ms, max_ms; /* submit -> result ready, completed builds */
+  double admitted_bytes, peak_admitted_bytes;
+} occ_xc_server_stats;
+void occ_xc_default_server_settings(occ_xc_server_settings *out);
+const char *occ_xc_server_last_error(void);
+int occ_xc_server_create(int device, const occ_xc_server_settings *settings,
+                         occ_xc_server **out);
+/* Stops the worker (a running tick finishes) and frees everything; builds
+ * not yet run are dropped. */
+void occ_xc_server_destroy(occ_xc_server *server);
+/* Arguments as occ_xc_molecule_create. */
+int occ_xc_server_open(occ_xc_server *server, int natoms, const int *atomic_numbers,
+                       const double *xyz_bohr, int nshells, const int *shell_l,
+                       const int *shell_atom, const int *shell_nprim, const double *exponents,
+                       const double *coefficients, int pure, const char *method,
+                       const occ_xc_grid_settings *grid, const occ_xc_build_settings *build,
+                       uint64_t *session);
+/* D: nbf x nbf host matrix (copied before the call returns).  OCC_XC_ERR_BUSY
+ * when queue_capacity builds are pending. */
+int occ_xc_server_submit(occ_xc_server *server, uint64_t session, const double *D,
+                         uint64_t *ticket);
+/* *done = 0: not finished.  *done = 1: V (nbf x nbf, may be NULL) and exc2 =
+ * {E_xc, integrated density} (may be NULL) are written, the ticket is
+ * released and the build's status is returned. */
+int occ_xc_server_poll(occ_xc_server *server, uint64_t ticket, double *V, double *exc2,
+                       int *done);
+/* Blocks up to timeout_s; OCC_XC_ERR_TIMEOUT (ticket kept) if not finished. */
+int occ_xc_server_wait(occ_xc_server *server, uint64_t ticket, double timeout_s, double *V,
+                       double *exc2);
+int occ_xc_server_close(occ_xc_server *server, uint64_t session);
+/* paused != 0: no new ticks start (submissions still queue). */
+int occ_xc_server_pause(occ_xc_server *server, int paused);
+/* device_bytes = bytes held now (0 until admitted); workspace_bytes = the
+ * admission charge. */
+int occ_xc_server_session_info(occ_xc_server *server, uint64_t session,
+                               occ_xc_molecule_info *out, int *admitted);
+int occ_xc_server_stats_get(occ_xc_server *server, occ_xc_server_stats *out);
+
 /* CTAs of the persistent tensor-core kernels (0 = one per SM, the default);
  * fewer leave SMs free for concurrent builds on other streams. */
 int occ_xc_set_persistent_ctas(occ_xc_context *ctx, int ctas);

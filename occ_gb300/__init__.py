@@ -16,6 +16,7 @@ from .xc import (  # noqa: F401
     Graph,
     GridSettings,
     Molecule,
+    Server,
     Shell,
     XCError,
     capture_scf_graph,

@@ -326,11 +326,7 @@ Context::~Context() {
     cudaStreamDestroy(stream);
 }
 
-} // namespace occx
 
-using namespace occx;
-
-namespace {
 Basis make_basis(int natoms, const double *xyz, int nshells, const int *shell_l,
                  const int *shell_atom, const int *shell_nprim, const double *exponents,
                  const double *coefficients, int pure) {
@@ -370,6 +366,95 @@ GridSettings grid_settings_from(const occ_xc_grid_settings *grid) {
   return gs;
 }
 
+
+std::unique_ptr<Molecule> molecule_host(Context *ctx, const MoleculeArgs &a) {
+  if (a.natoms <= 0 || a.nshells <= 0 || !a.Z || !a.xyz || !a.shell_l || !a.shell_atom ||
+      !a.shell_nprim || !a.exponents || !a.coefficients || !a.method)
+    throw ArgError("molecule: missing or empty input");
+  auto M = std::make_unique<Molecule>();
+  M->ctx = ctx;
+  M->device = ctx->device;
+  M->fs = parse_method(a.method);
+  M->deriv = 0;
+  for (int i = 0; i < M->fs.n; i++)
+    M->deriv = std::max(M->deriv, func_is_gga(M->fs.id[i]) ? 1 : 0);
+  M->Z.assign(a.Z, a.Z + a.natoms);
+  M->xyz.assign(a.xyz, a.xyz + 3 * a.natoms);
+  M->basis = make_basis(a.natoms, a.xyz, a.nshells, a.shell_l, a.shell_atom,
+                                a.shell_nprim, a.exponents, a.coefficients, a.pure);
+  M->gs = grid_settings_from(a.grid);
+  if (a.build) {
+    M->bs.xc_screening_threshold = a.build->xc_screening_threshold;
+    M->bs.density_threshold = a.build->density_threshold;
+    M->bs.leaf_target = a.build->leaf_target;
+    M->bs.leaf_min = a.build->leaf_min;
+    M->bs.leaf_max = a.build->leaf_max;
+    if (M->bs.leaf_max > 256 || M->bs.leaf_target <= 0 || M->bs.leaf_min <= 0 ||
+        M->bs.leaf_target > M->bs.leaf_max || 2 * M->bs.leaf_min > M->bs.leaf_max)
+      throw ArgError("leaf sizes must satisfy 0 < target <= max <= 256, 2 min <= max");
+  }
+  M->grid = build_molecular_grid(M->Z, M->xyz, M->basis, M->gs, 0);
+  M->build_plan();
+  return M;
+}
+
+void Molecule::materialise() {
+  upload();
+  prepare_mixed();
+}
+
+void Molecule::release_device() {
+  for (void *p : allocations)
+    cudaFree(p);
+  allocations.clear();
+  free_mixed(mixed);
+  mixed = nullptr;
+  device_bytes = 0.0;
+  d_pts = nullptr;
+  d_shells = nullptr;
+  d_prims = nullptr;
+  d_leaves = nullptr;
+  d_leaf_sh = d_leaf_ao = nullptr;
+  d_slabs = nullptr;
+  d_tiles = nullptr;
+  d_ws = d_rho = d_coef = d_epart = d_out2 = d_D = d_V = nullptr;
+}
+
+// Device bytes that materialise() will allocate (an upper bound: every array
+// rounded up to 256 bytes, plus the mixed path's launch lists).
+double Molecule::estimate_device_bytes() const {
+  auto r = [](double b) { return std::ceil(std::max(b, 16.0) / 256.0) * 256.0; };
+  const double N = static_cast<double>(std::max<long>(plan.npts, 1));
+  const double nl = static_cast<double>(std::max<size_t>(leaves.size(), 1));
+  const double nbf2 = static_cast<double>(basis.nbf) * basis.nbf;
+  double nprim = 0;
+  for (const Shell &sh : basis.shells)
+    nprim += static_cast<double>(sh.exps.size());
+  const double nsh = static_cast<double>(basis.shells.size());
+  double b = r(N * sizeof(Pt4)) + r(nsh * sizeof(DevShell)) + r(nprim * sizeof(double2)) +
+             r(nl * sizeof(DevLeaf)) + r(leaf_sh.size() * 4.0) + r(leaf_ao.size() * 4.0) +
+             r(slabs.size() * sizeof(SlabItem)) + r(tiles.size() * sizeof(TileItem));
+  b += r(ws_elems * 8.0) + 2 * r(4 * N * 8.0) + r(2 * nl * 8.0) + r(16.0) + 2 * r(nbf2 * 8.0);
+  // mixed path: per-block FP32 AO planes, row scales, D2 hi/lo, column bounds
+  double blocks = 0, wsf = 0, items = 0;
+  for (const DevLeaf &L : leaves) {
+    const double mp = std::ceil(L.nbf / 32.0) * 32.0;
+    const double nb = std::ceil(L.cnt / 128.0);
+    blocks += nb;
+    wsf += nb * 4.0 * mp * 128.0;
+    items += nb * std::ceil(mp / 128.0);
+  }
+  b += r(nprim * 16.0) + r(2 * nsh * 16.0) + r(wsf * 4.0) + r(blocks * 128 * 4.0) +
+       r(nbf2 * 8.0) + r(basis.nbf * 4.0) + r(16.0);
+  b += r(blocks * 32.0) + r(blocks * 4.0) + r(items * 8.0) + r(nl * 8.0) + r(4096.0) + r(16.0);
+  return b;
+}
+
+} // namespace occx
+
+using namespace occx;
+
+namespace {
 template <typename F> int guarded(occ_xc_context *ctx, F &&f) {
   try {
     f();
@@ -504,36 +589,11 @@ int occ_xc_molecule_create(occ_xc_context *ctx, int natoms, const int *Z, const 
   auto mol = std::make_unique<occ_xc_molecule>();
   mol->ctx = ctx;
   int rc = guarded(ctx, [&] {
-    if (natoms <= 0 || nshells <= 0 || !Z || !xyz || !shell_l || !shell_atom || !shell_nprim ||
-        !exponents || !coefficients || !method)
-      throw ArgError("occ_xc_molecule_create: missing or empty input");
+    MoleculeArgs a{natoms, Z, xyz, nshells, shell_l, shell_atom, shell_nprim, exponents,
+                   coefficients, pure, method, grid, build};
     cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
-    auto M = std::make_unique<Molecule>();
-    M->ctx = ctx->impl.get();
-    M->device = ctx->impl->device;
-    M->fs = parse_method(method);
-    M->deriv = 0;
-    for (int i = 0; i < M->fs.n; i++)
-      M->deriv = std::max(M->deriv, func_is_gga(M->fs.id[i]) ? 1 : 0);
-    M->Z.assign(Z, Z + natoms);
-    M->xyz.assign(xyz, xyz + 3 * natoms);
-    M->basis = make_basis(natoms, xyz, nshells, shell_l, shell_atom, shell_nprim, exponents,
-                          coefficients, pure);
-    M->gs = grid_settings_from(grid);
-    if (build) {
-      M->bs.xc_screening_threshold = build->xc_screening_threshold;
-      M->bs.density_threshold = build->density_threshold;
-      M->bs.leaf_target = build->leaf_target;
-      M->bs.leaf_min = build->leaf_min;
-      M->bs.leaf_max = build->leaf_max;
-      if (M->bs.leaf_max > 256 || M->bs.leaf_target <= 0 || M->bs.leaf_min <= 0 ||
-          M->bs.leaf_target > M->bs.leaf_max || 2 * M->bs.leaf_min > M->bs.leaf_max)
-        throw ArgError("leaf sizes must satisfy 0 < target <= max <= 256, 2 min <= max");
-    }
-    M->grid = build_molecular_grid(M->Z, M->xyz, M->basis, M->gs, 0);
-    M->build_plan();
-    M->upload();
-    M->prepare_mixed();
+    auto M = molecule_host(ctx->impl.get(), a);
+    M->materialise();
     mol->impl = std::move(M);
   });
   if (rc == OCC_XC_OK)

@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/occ_xc.h"
 #include "host/xc_host.hpp"
 #include "xc_device.cuh"
 
@@ -78,6 +79,20 @@ struct Context {
 
 struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)
 
+// The molecule arguments of occ_xc_molecule_create.
+struct MoleculeArgs {
+  int natoms;
+  const int *Z;
+  const double *xyz;
+  int nshells;
+  const int *shell_l, *shell_atom, *shell_nprim;
+  const double *exponents, *coefficients;
+  int pure;
+  const char *method;
+  const occ_xc_grid_settings *grid;
+  const occ_xc_build_settings *build;
+};
+
 struct Molecule {
   Context *ctx = nullptr;
   int device = 0;
@@ -116,11 +131,34 @@ struct Molecule {
   void build_plan();
   void upload();
   void prepare_mixed();
+  void materialise(); // upload() + prepare_mixed(): all device state
+  void release_device(); // frees all device state (back to the host-only molecule)
+  double estimate_device_bytes() const;
   MolDev dev() const;
   void build(int precision, const double *dD, double *dV, double *dout2, cudaStream_t st);
   void build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st);
   void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
 };
+
+// Host part of a molecule: basis, molecular grid, Morton leaves and screening
+// (no device memory); materialise() uploads it.
+std::unique_ptr<Molecule> molecule_host(Context *ctx, const MoleculeArgs &a);
+
+// Staging for launch lists built per call (the server's batched builds):
+// one device region and one pinned host region, grown on demand.
+struct ListArena {
+  void *d = nullptr, *h = nullptr;
+  size_t cap = 0;
+  void reserve(size_t bytes);
+  ~ListArena();
+};
+// One mixed-precision build of each molecule in `mols` (each at most once)
+// through shared launches, reading and writing the molecules' own D, V and
+// {E_xc, density} buffers.  Lists go through `arena`; *d_err is the
+// bounded-wait flag.  Asynchronous on st; the arena may be reused once st has
+// passed this call.
+void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListArena &arena,
+                       int *d_err, cudaStream_t st);
 
 } // namespace occx
 

@@ -1118,7 +1118,8 @@ template <typename T> T *plan_upload(LaunchPlan &P, const std::vector<T> &v) {
 // Concatenate the molecules' work lists.  Items are interleaved so that CTAs
 // running at the same time come from distant parts of the Morton order (and of
 // the batch) and update different V_xc elements.
-void make_plan(LaunchPlan &P, const std::vector<Molecule *> &mols, const std::vector<MixTab> &tabs) {
+void make_plan_lists(LaunchPlan &P, const std::vector<Molecule *> &mols,
+                     const std::vector<MixTab> &tabs) {
   P.tabs = tabs;
   P.deriv = mols.empty() ? 0 : mols[0]->deriv;
   std::vector<VItem> items;
@@ -1161,6 +1162,12 @@ void make_plan(LaunchPlan &P, const std::vector<Molecule *> &mols, const std::ve
         P.order.push_back(static_cast<int>(q * bstride + r));
   std::stable_sort(P.order.begin(), P.order.end(),
                    [&](int a, int b) { return P.blocks[a].mp > P.blocks[b].mp; });
+}
+
+// Lists in their own device allocations (a plan that lives with its molecule
+// or batch).
+void make_plan(LaunchPlan &P, const std::vector<Molecule *> &mols, const std::vector<MixTab> &tabs) {
+  make_plan_lists(P, mols, tabs);
   P.d_blocks = plan_upload(P, P.blocks);
   P.d_order = plan_upload(P, P.order);
   P.d_queue = plan_upload(P, std::vector<int>(2, 0));
@@ -1319,6 +1326,94 @@ int mixed_error_flag(Molecule &M, cudaStream_t st) {
 }
 
 void free_mixed(MixedState *S) { delete S; }
+
+void ListArena::reserve(size_t bytes) {
+  if (bytes <= cap)
+    return;
+  const size_t n = std::max(bytes, 2 * cap);
+  if (d)
+    cudaFree(d);
+  if (h)
+    cudaFreeHost(h);
+  d = h = nullptr;
+  cap = 0;
+  cuda_check(cudaMalloc(&d, n), "cudaMalloc");
+  cuda_check(cudaMallocHost(&h, n), "cudaMallocHost");
+  cap = n;
+}
+ListArena::~ListArena() {
+  if (d)
+    cudaFree(d);
+  if (h)
+    cudaFreeHost(h);
+}
+
+void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListArena &arena,
+                       int *d_err, cudaStream_t st) {
+  LaunchPlan P[2];
+  std::vector<Molecule *> group[2];
+  std::vector<MixTab> tabs[2];
+  for (size_t i = 0; i < mols.size(); i++) {
+    for (size_t j = 0; j < i; j++)
+      if (mols[j] == mols[i])
+        throw ArgError("a molecule may appear only once in a group build");
+    const int g = mols[i]->deriv ? 1 : 0;
+    group[g].push_back(mols[i]);
+    tabs[g].push_back(mols[i]->mixed->tab);
+  }
+  // pack both plans' lists into the arena: one pinned staging area, one copy
+  size_t off = 0;
+  auto place = [&](size_t bytes) {
+    const size_t o = off;
+    off = round_up(off + std::max<size_t>(bytes, 16), 256);
+    return o;
+  };
+  struct Slot {
+    size_t tabs, blocks, order, queue, items, litems;
+  } slot[2]{};
+  for (int g = 0; g < 2; g++) {
+    if (group[g].empty())
+      continue;
+    make_plan_lists(P[g], group[g], tabs[g]);
+    slot[g].tabs = place(P[g].tabs.size() * sizeof(MixTab));
+    slot[g].blocks = place(P[g].blocks.size() * sizeof(MBlock));
+    slot[g].order = place(P[g].order.size() * sizeof(int));
+    slot[g].queue = place(2 * sizeof(int));
+    slot[g].items = place(P[g].items.size() * sizeof(VItem));
+    slot[g].litems = place(P[g].litems.size() * sizeof(LeafItem));
+  }
+  if (off == 0)
+    return;
+  arena.reserve(off);
+  char *h = static_cast<char *>(arena.h);
+  char *d = static_cast<char *>(arena.d);
+  auto put = [&](size_t o, const void *src, size_t bytes) {
+    if (bytes)
+      std::memcpy(h + o, src, bytes);
+  };
+  for (int g = 0; g < 2; g++) {
+    if (group[g].empty())
+      continue;
+    LaunchPlan &L = P[g];
+    const int zero[2] = {0, 0};
+    put(slot[g].tabs, L.tabs.data(), L.tabs.size() * sizeof(MixTab));
+    put(slot[g].blocks, L.blocks.data(), L.blocks.size() * sizeof(MBlock));
+    put(slot[g].order, L.order.data(), L.order.size() * sizeof(int));
+    put(slot[g].queue, zero, sizeof(zero));
+    put(slot[g].items, L.items.data(), L.items.size() * sizeof(VItem));
+    put(slot[g].litems, L.litems.data(), L.litems.size() * sizeof(LeafItem));
+    L.d_tabs = reinterpret_cast<MixTab *>(d + slot[g].tabs);
+    L.d_blocks = reinterpret_cast<MBlock *>(d + slot[g].blocks);
+    L.d_order = reinterpret_cast<int *>(d + slot[g].order);
+    L.d_queue = reinterpret_cast<int *>(d + slot[g].queue);
+    L.d_items = reinterpret_cast<VItem *>(d + slot[g].items);
+    L.d_litems = reinterpret_cast<LeafItem *>(d + slot[g].litems);
+  }
+  cuda_check(cudaMemcpyAsync(d, h, off, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync H2D");
+  for (int g = 0; g < 2; g++)
+    if (!group[g].empty())
+      run_plan(P[g], c, Override{nullptr, nullptr, nullptr}, d_err, st, c.max_ctas);
+}
 
 // ---- batches ---------------------------------------------------------------
 struct Batch {

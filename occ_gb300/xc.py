@@ -24,7 +24,14 @@ ANGSTROM_TO_BOHR = 1.0 / 0.52917721067  # include/occ/core/units.h:7-8
 
 
 class XCError(RuntimeError):
-    pass
+    """A failed library call; `code` is the OCC_XC_ERR_* status (or None)."""
+
+    def __init__(self, message, code=None):
+        super().__init__(message)
+        self.code = code
+
+
+ERR_ARG, ERR_CUDA, ERR_METHOD, ERR_NOMEM, ERR_TIMEOUT, ERR_BUSY = -1, -2, -3, -4, -5, -6
 
 
 def library_path():
@@ -51,6 +58,19 @@ class _MolInfo(C.Structure):
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
+
+
+class _ServerSettings(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("queue_capacity", C.c_int),
+                ("max_batch", C.c_int), ("precision", C.c_int)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_long), ("failed", C.c_long), ("pending", C.c_long),
+                ("ticks", C.c_long), ("sessions_admitted", C.c_long),
+                ("sessions_waiting", C.c_long), ("mean_batch", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
+                ("admitted_bytes", C.c_double), ("peak_admitted_bytes", C.c_double)]
 
 
 def library():
@@ -91,6 +111,23 @@ def library():
     lib.occ_xc_graph_launch.argtypes = [_vp, _vp]
     lib.occ_xc_graph_destroy.argtypes = [_vp]
     lib.occ_xc_set_persistent_ctas.argtypes = [_vp, C.c_int]
+    _u64 = C.c_uint64
+    lib.occ_xc_default_server_settings.argtypes = [C.POINTER(_ServerSettings)]
+    lib.occ_xc_server_last_error.restype = C.c_char_p
+    lib.occ_xc_server_last_error.argtypes = []
+    lib.occ_xc_server_create.argtypes = [C.c_int, C.POINTER(_ServerSettings), _pp]
+    lib.occ_xc_server_destroy.argtypes = [_vp]
+    lib.occ_xc_server_open.argtypes = [
+        _vp, C.c_int, _ip, _dp, C.c_int, _ip, _ip, _ip, _dp, _dp, C.c_int, C.c_char_p,
+        C.POINTER(_GridSettings), C.POINTER(_BuildSettings), C.POINTER(_u64)]
+    lib.occ_xc_server_submit.argtypes = [_vp, _u64, _dp, C.POINTER(_u64)]
+    lib.occ_xc_server_poll.argtypes = [_vp, _u64, _dp, _dp, C.POINTER(C.c_int)]
+    lib.occ_xc_server_wait.argtypes = [_vp, _u64, C.c_double, _dp, _dp]
+    lib.occ_xc_server_close.argtypes = [_vp, _u64]
+    lib.occ_xc_server_pause.argtypes = [_vp, C.c_int]
+    lib.occ_xc_server_session_info.argtypes = [_vp, _u64, C.POINTER(_MolInfo),
+                                               C.POINTER(C.c_int)]
+    lib.occ_xc_server_stats_get.argtypes = [_vp, C.POINTER(_ServerStats)]
     lib.occ_xc_batch_set_density.argtypes = [_vp, _vp, C.c_int, _dp]
     lib.occ_xc_batch_get_result.argtypes = [_vp, _vp, C.c_int, _dp, _dp]
     _LIB = lib
@@ -257,6 +294,21 @@ def _context(device):
     return _CONTEXTS[device]
 
 
+def _molecule_args(method, basis, grid_settings=None, build_settings=None):
+    """The molecule arguments of occ_xc_molecule_create / occ_xc_server_open,
+    and the arrays they point into (kept alive by the caller)."""
+    atoms = basis.atoms()
+    Z = np.array([a.atomic_number for a in atoms], dtype=np.int32)
+    xyz = np.array([[a.x, a.y, a.z] for a in atoms], dtype=np.float64).ravel()
+    l, atom, nprim, exps, coefs = basis.arrays()
+    gs = (grid_settings or GridSettings())._c()
+    bs = (build_settings or BuildSettings())._c()
+    args = (len(Z), _ptr(Z, _ip), _ptr(xyz), len(l), _ptr(l, _ip), _ptr(atom, _ip),
+            _ptr(nprim, _ip), _ptr(exps), _ptr(coefs), int(basis.pure), method.encode(),
+            C.byref(gs), C.byref(bs))
+    return args, (Z, xyz, l, atom, nprim, exps, coefs, gs, bs)
+
+
 class DFT:
     """The XC part of occ::dft::DFT on one GB300."""
 
@@ -265,23 +317,14 @@ class DFT:
         self.basis = basis
         self.ctx = _context(device)
         lib = self.ctx.lib
-        atoms = basis.atoms()
-        Z = np.array([a.atomic_number for a in atoms], dtype=np.int32)
-        xyz = np.array([[a.x, a.y, a.z] for a in atoms], dtype=np.float64).ravel()
-        l, atom, nprim, exps, coefs = basis.arrays()
-        gs = (grid_settings or GridSettings())._c()
-        bs = (build_settings or BuildSettings())._c()
+        args, self._keep = _molecule_args(method, basis, grid_settings, build_settings)
         h = C.c_void_p()
-        rc = lib.occ_xc_molecule_create(self.ctx.h, len(Z), _ptr(Z, _ip), _ptr(xyz), len(l),
-                                        _ptr(l, _ip), _ptr(atom, _ip), _ptr(nprim, _ip),
-                                        _ptr(exps), _ptr(coefs), int(basis.pure),
-                                        method.encode(), C.byref(gs), C.byref(bs), C.byref(h))
+        rc = lib.occ_xc_molecule_create(self.ctx.h, *args, C.byref(h))
         if rc != 0:
             raise XCError(f"occ_xc_molecule_create failed ({rc}): {self.ctx.error()}")
         self.h = h
         self._exc = 0.0
         self._nelec = 0.0
-        self._keep = (Z, xyz, l, atom, nprim, exps, coefs)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -460,3 +503,92 @@ def set_persistent_ctas(ctas, device=0):
     rc = ctx.lib.occ_xc_set_persistent_ctas(ctx.h, int(ctas))
     if rc != 0:
         raise XCError(f"occ_xc_set_persistent_ctas failed ({rc})")
+
+
+class Server:
+    """Serving loop over one GPU: sessions (one per molecule), submitted
+    densities, results by ticket; continuous batching and admission against
+    a device-memory budget (occ_xc_server_* in include/occ_xc.h)."""
+
+    def __init__(self, device=0, hbm_budget_bytes=150e9, queue_capacity=4096, max_batch=64,
+                 precision=MIXED):
+        self.lib = library()
+        cfg = _ServerSettings(float(hbm_budget_bytes), int(queue_capacity), int(max_batch),
+                              int(precision))
+        h = C.c_void_p()
+        rc = self.lib.occ_xc_server_create(device, C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise XCError(f"occ_xc_server_create failed ({rc}): {self._err()}")
+        self.h = h
+        self._nbf = {}
+
+    def _err(self):
+        return self.lib.occ_xc_server_last_error().decode()
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise XCError(f"{what} failed ({rc}): {self._err()}", rc)
+
+    def open(self, method, basis, grid_settings=None, build_settings=None):
+        args, keep = _molecule_args(method, basis, grid_settings, build_settings)
+        sid = C.c_uint64()
+        self._check(self.lib.occ_xc_server_open(self.h, *args, C.byref(sid)), "open")
+        self._nbf[sid.value] = basis.nbf()
+        del keep
+        return sid.value
+
+    def submit(self, session, D):
+        n = self._nbf[session]
+        a = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if a.shape != (n, n):
+            raise XCError(f"density matrix must be {n}x{n}")
+        t = C.c_uint64()
+        self._check(self.lib.occ_xc_server_submit(self.h, session, _ptr(a), C.byref(t)),
+                    "submit")
+        return t.value, n
+
+    def poll(self, ticket):
+        """None while running, else (V, E_xc, integrated density)."""
+        tid, n = ticket
+        V = np.zeros((n, n), order="F")
+        e2 = np.zeros(2)
+        done = C.c_int(0)
+        self._check(self.lib.occ_xc_server_poll(self.h, tid, _ptr(V), _ptr(e2), C.byref(done)),
+                    "poll")
+        return (V, e2[0], e2[1]) if done.value else None
+
+    def wait(self, ticket, timeout=120.0):
+        tid, n = ticket
+        V = np.zeros((n, n), order="F")
+        e2 = np.zeros(2)
+        self._check(self.lib.occ_xc_server_wait(self.h, tid, float(timeout), _ptr(V), _ptr(e2)),
+                    "wait")
+        return V, e2[0], e2[1]
+
+    def close(self, session):
+        self._check(self.lib.occ_xc_server_close(self.h, session), "close")
+
+    def pause(self, paused=True):
+        self._check(self.lib.occ_xc_server_pause(self.h, int(bool(paused))), "pause")
+
+    def session_info(self, session):
+        i = _MolInfo()
+        adm = C.c_int(0)
+        self._check(self.lib.occ_xc_server_session_info(self.h, session, C.byref(i),
+                                                        C.byref(adm)), "session_info")
+        d = {f: getattr(i, f) for f, _ in _MolInfo._fields_}
+        d["admitted"] = bool(adm.value)
+        return d
+
+    def stats(self):
+        st = _ServerStats()
+        self._check(self.lib.occ_xc_server_stats_get(self.h, C.byref(st)), "stats")
+        return {f: getattr(st, f) for f, _ in _ServerStats._fields_}
+
+    def shutdown(self):
+        if getattr(self, "h", None):
+            self.lib.occ_xc_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.shutdown()
