@@ -350,7 +350,8 @@ def main():
                    "flops_per_build": info["flops_per_build"], "precision": "fp64" if head == og.FP64 else "mixed",
                    "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2: per-build workspace "
-                         f"{info['workspace_bytes'] / 1e9:.1f} GB > 129 MB"},
+                         f"{(info['mixed_workspace_bytes'] if head == og.MIXED else info['workspace_bytes']) / 1e9:.1f}"
+                         " GB > 129 MB"},
         "p50_ms": float(np.percentile(r["per"], 50)), "p99_ms": float(np.percentile(r["per"], 99)),
         "fp64": {"builds_per_s": args.steps / (results[og.FP64]["total_ms"] / 1e3),
                  "p50_ms": float(np.percentile(results[og.FP64]["per"], 50)),

@@ -76,8 +76,11 @@ typedef struct {
   int nbf, natoms, nshells, deriv;
   long npoints, nleaves;
   double flops_per_build;    /* 4 * sum_b n_b * m_b^2 (useful contraction FLOPs) */
-  double device_bytes;       /* resident device memory held by the molecule */
-  double workspace_bytes;    /* per-build workspace (FP64 path) */
+  double device_bytes;          /* device memory held now (resident state and the
+                                   private workspaces allocated so far) */
+  double workspace_bytes;       /* per-build workspace of the FP64 path */
+  double mixed_workspace_bytes; /* per-build workspace of the mixed path */
+  double resident_bytes;        /* resident state alone (upper bound, no workspace) */
 } occ_xc_molecule_info;
 
 void occ_xc_default_grid_settings(occ_xc_grid_settings *out);
@@ -152,6 +155,14 @@ int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const d
 typedef struct occ_xc_batch occ_xc_batch;
 int occ_xc_batch_create(occ_xc_context *ctx, int nmol, occ_xc_molecule *const *mols,
                         occ_xc_batch **out);
+/* The batch keeps one shared per-build workspace.  Its molecules are split, in
+ * order, into sub-batches whose mixed-path workspaces sum to at most
+ * workspace_cap_bytes (a molecule above the cap forms its own); sub-batches
+ * run one after the other through the same workspace, so a batch of any size
+ * fits the device.  occ_xc_batch_create uses half of the free device memory
+ * as the cap (workspace_cap_bytes <= 0 does the same). */
+int occ_xc_batch_create_capped(occ_xc_context *ctx, int nmol, occ_xc_molecule *const *mols,
+                               double workspace_cap_bytes, occ_xc_batch **out);
 void occ_xc_batch_destroy(occ_xc_batch *batch);
 int occ_xc_batch_buffers(occ_xc_batch *batch, int i, double **d_D, double **d_V,
                          double **d_exc2);
@@ -245,8 +256,9 @@ int occ_xc_server_wait(occ_xc_server *server, uint64_t ticket, double timeout_s,
 int occ_xc_server_close(occ_xc_server *server, uint64_t session);
 /* paused != 0: no new ticks start (submissions still queue). */
 int occ_xc_server_pause(occ_xc_server *server, int paused);
-/* device_bytes = bytes held now (0 until admitted); workspace_bytes = the
- * admission charge. */
+/* Molecule figures of the session; device_bytes = bytes held now (0 until
+ * admitted).  Sessions hold only their resident state: per-build workspaces
+ * come from one server-owned workspace sized for each tick. */
 int occ_xc_server_session_info(occ_xc_server *server, uint64_t session,
                                occ_xc_molecule_info *out, int *admitted);
 int occ_xc_server_stats_get(occ_xc_server *server, occ_xc_server_stats *out);

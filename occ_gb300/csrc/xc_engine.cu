@@ -210,7 +210,6 @@ void Molecule::upload() {
 
   const size_t N = static_cast<size_t>(std::max<long>(plan.npts, 1));
   const size_t nl = std::max<size_t>(leaves.size(), 1);
-  d_ws = static_cast<double *>(alloc(ws_elems * sizeof(double)));
   d_rho = static_cast<double *>(alloc(4 * N * sizeof(double)));
   d_coef = static_cast<double *>(alloc(4 * N * sizeof(double)));
   d_epart = static_cast<double *>(alloc(2 * nl * sizeof(double)));
@@ -237,20 +236,37 @@ MolDev Molecule::dev() const {
 }
 
 // One restricted XC build on device buffers (the FP64 sequence).
-void Molecule::build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st) {
+void Molecule::ensure_fp64_ws() {
+  if (!d_ws)
+    d_ws = static_cast<double *>(alloc(std::max<size_t>(ws_elems, 1) * sizeof(double)));
+}
+
+void Molecule::prepare(int precision) {
+  if (precision == OCC_XC_MIXED)
+    ensure_mixed_ws();
+  else
+    ensure_fp64_ws();
+}
+
+void Molecule::build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st,
+                          double *ws) {
+  if (!ws) {
+    ensure_fp64_ws();
+    ws = d_ws;
+  }
   const MolDev m = dev();
   const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
   Context &c = *ctx;
   cuda_check(cudaMemsetAsync(dV, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
-  c.launch("colloc_f64", st, [&] { launch_colloc_f64(m, deriv, d_ws, st); });
+  c.launch("colloc_f64", st, [&] { launch_colloc_f64(m, deriv, ws, st); });
   c.launch("rho_f64", st, [&] {
-    launch_rho_f64(m, deriv, dD, d_ws, d_slabs, static_cast<int>(slabs.size()), d_rho, st);
+    launch_rho_f64(m, deriv, dD, ws, d_slabs, static_cast<int>(slabs.size()), d_rho, st);
   });
   c.launch("func", st, [&] {
     launch_func(m, deriv, fs, bs.density_threshold, d_rho, d_coef, d_epart, st);
   });
   c.launch("vxc_f64", st, [&] {
-    launch_vxc_f64(m, deriv, d_ws, d_coef, d_tiles, static_cast<int>(tiles.size()), dV, st);
+    launch_vxc_f64(m, deriv, ws, d_coef, d_tiles, static_cast<int>(tiles.size()), dV, st);
   });
   c.launch("reduce", st, [&] { launch_reduce(d_epart, m.nleaves, dout2, st); });
   cuda_check(cudaGetLastError(), "kernel launch");
@@ -420,9 +436,10 @@ void Molecule::release_device() {
   d_ws = d_rho = d_coef = d_epart = d_out2 = d_D = d_V = nullptr;
 }
 
-// Device bytes that materialise() will allocate (an upper bound: every array
-// rounded up to 256 bytes, plus the mixed path's launch lists).
-double Molecule::estimate_device_bytes() const {
+// Device bytes that materialise() allocates -- the resident state, without the
+// per-build workspaces (an upper bound: every array rounded up to 256 bytes,
+// plus the mixed path's launch lists).
+double Molecule::estimate_resident_bytes() const {
   auto r = [](double b) { return std::ceil(std::max(b, 16.0) / 256.0) * 256.0; };
   const double N = static_cast<double>(std::max<long>(plan.npts, 1));
   const double nl = static_cast<double>(std::max<size_t>(leaves.size(), 1));
@@ -434,20 +451,20 @@ double Molecule::estimate_device_bytes() const {
   double b = r(N * sizeof(Pt4)) + r(nsh * sizeof(DevShell)) + r(nprim * sizeof(double2)) +
              r(nl * sizeof(DevLeaf)) + r(leaf_sh.size() * 4.0) + r(leaf_ao.size() * 4.0) +
              r(slabs.size() * sizeof(SlabItem)) + r(tiles.size() * sizeof(TileItem));
-  b += r(ws_elems * 8.0) + 2 * r(4 * N * 8.0) + r(2 * nl * 8.0) + r(16.0) + 2 * r(nbf2 * 8.0);
-  // mixed path: per-block FP32 AO planes, row scales, D2 hi/lo, column bounds
-  double blocks = 0, wsf = 0, items = 0;
+  b += 2 * r(4 * N * 8.0) + r(2 * nl * 8.0) + r(16.0) + 2 * r(nbf2 * 8.0);
+  double blocks = 0, items = 0;
   for (const DevLeaf &L : leaves) {
-    const double mp = std::ceil(L.nbf / 32.0) * 32.0;
     const double nb = std::ceil(L.cnt / 128.0);
     blocks += nb;
-    wsf += nb * 4.0 * mp * 128.0;
-    items += nb * std::ceil(mp / 128.0);
+    items += nb * std::ceil(std::ceil(L.nbf / 32.0) * 32.0 / 128.0);
   }
-  b += r(nprim * 16.0) + r(2 * nsh * 16.0) + r(wsf * 4.0) + r(blocks * 128 * 4.0) +
-       r(nbf2 * 8.0) + r(basis.nbf * 4.0) + r(16.0);
+  b += r(nprim * 16.0) + r(2 * nsh * 16.0) + r(16.0);
   b += r(blocks * 32.0) + r(blocks * 4.0) + r(items * 8.0) + r(nl * 8.0) + r(4096.0) + r(16.0);
   return b;
+}
+
+size_t Molecule::fp64_workspace_bytes() const {
+  return std::max<size_t>(ws_elems, 1) * sizeof(double);
 }
 
 } // namespace occx
@@ -623,7 +640,9 @@ int occ_xc_molecule_info_get(const occ_xc_molecule *mol, occ_xc_molecule_info *o
   o->nleaves = static_cast<long>(M.leaves.size());
   o->flops_per_build = M.flops;
   o->device_bytes = M.device_bytes;
-  o->workspace_bytes = static_cast<double>(M.ws_elems) * sizeof(double);
+  o->workspace_bytes = static_cast<double>(M.fp64_workspace_bytes());
+  o->mixed_workspace_bytes = M.mixed ? static_cast<double>(M.mixed_workspace_bytes()) : 0.0;
+  o->resident_bytes = M.estimate_resident_bytes();
   return OCC_XC_OK;
 }
 

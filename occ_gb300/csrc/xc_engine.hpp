@@ -131,12 +131,22 @@ struct Molecule {
   void build_plan();
   void upload();
   void prepare_mixed();
-  void materialise(); // upload() + prepare_mixed(): all device state
+  void materialise();    // upload() + prepare_mixed(): the resident device state
   void release_device(); // frees all device state (back to the host-only molecule)
-  double estimate_device_bytes() const;
+  double estimate_resident_bytes() const; // what materialise() allocates (upper bound)
+  // Per-build workspaces.  A molecule built on its own allocates a private
+  // one per precision on first use; batches and the server lend it a region
+  // of a shared one instead.
+  size_t fp64_workspace_bytes() const;
+  size_t mixed_workspace_bytes() const;
+  void ensure_fp64_ws();
+  void ensure_mixed_ws();
+  void prepare(int precision); // the private workspace of `precision` (before a capture)
   MolDev dev() const;
   void build(int precision, const double *dD, double *dV, double *dout2, cudaStream_t st);
-  void build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st);
+  // ws: an FP64 workspace of fp64_workspace_bytes() (nullptr: the private one)
+  void build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st,
+                  double *ws = nullptr);
   void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
 };
 
@@ -154,11 +164,14 @@ struct ListArena {
 };
 // One mixed-precision build of each molecule in `mols` (each at most once)
 // through shared launches, reading and writing the molecules' own D, V and
-// {E_xc, density} buffers.  Lists go through `arena`; *d_err is the
+// {E_xc, density} buffers, with their workspaces laid out one after the
+// other from d_ws.  Lists go through `arena`; *d_err is the
 // bounded-wait flag.  Asynchronous on st; the arena may be reused once st has
 // passed this call.
 void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListArena &arena,
-                       int *d_err, cudaStream_t st);
+                       char *d_ws, int *d_err, cudaStream_t st);
+// Bytes of the shared workspace mixed_build_group needs for `mols` (d_ws).
+size_t group_workspace_bytes(const std::vector<Molecule *> &mols);
 
 } // namespace occx
 

@@ -1088,20 +1088,58 @@ struct LaunchPlan {
   }
 };
 
-// Per-molecule resident state of the mixed path.
+// Per-molecule resident state of the mixed path.  The per-build workspace
+// (AO planes, row scales, D2 hi/lo, column bounds) is bound separately: a
+// private one for builds of the molecule alone, or a region of a batch's or
+// the server's shared workspace.
 struct MixedState {
   std::vector<MBlock> blocks; // this molecule's blocks (mol = 0)
   size_t ws_floats = 0;
   float4 *d_prim32 = nullptr;
   float4 *d_shA = nullptr; // shell centres as (hi xyz, lo xyz) float pairs
-  float *d_ws = nullptr;
-  float *d_rowscale = nullptr;
-  float2 *d_dhl = nullptr; // D2 as (hi, lo) floats, per build
-  float *d_colb = nullptr; // column bounds of D2, per build
   int *d_err = nullptr;
-  MixTab tab{};            // host copy; D / V / out2 point at the molecule's buffers
-  LaunchPlan single;       // the one-molecule plan
+  MixTab tab{};            // resident fields; workspace fields null
+  char *d_private = nullptr;           // private workspace, allocated on first use
+  std::unique_ptr<LaunchPlan> single;  // the one-molecule plan over it
 };
+
+// Layout of one molecule's mixed workspace (offsets from its base, 256-byte
+// aligned).
+struct WsLayout {
+  size_t ws, rowscale, dhl, colb, total;
+};
+WsLayout ws_layout(const Molecule &M) {
+  WsLayout L{};
+  size_t off = 0;
+  auto put = [&](size_t bytes) {
+    const size_t o = off;
+    off = (off + std::max<size_t>(bytes, 16) + 255) / 256 * 256;
+    return o;
+  };
+  const size_t nbf = static_cast<size_t>(M.basis.nbf);
+  size_t ws_floats = 0, nblocks = 0; // as prepare_mixed lays the blocks out
+  for (const DevLeaf &Lf : M.leaves) {
+    const size_t nb = (Lf.cnt + kBlockPts - 1) / kBlockPts;
+    const size_t mp = (Lf.nbf + kKc - 1) / kKc * kKc;
+    nblocks += nb;
+    ws_floats += nb * 4 * mp * kBlockPts;
+  }
+  L.ws = put(ws_floats * sizeof(float));
+  L.rowscale = put(nblocks * kBlockPts * sizeof(float));
+  L.dhl = put(nbf * nbf * sizeof(float2));
+  L.colb = put(nbf * sizeof(float));
+  L.total = off;
+  return L;
+}
+MixTab bind_ws(const Molecule &M, char *base) {
+  const WsLayout L = ws_layout(M);
+  MixTab T = M.mixed->tab;
+  T.ws = reinterpret_cast<float *>(base + L.ws);
+  T.rowscale = reinterpret_cast<float *>(base + L.rowscale);
+  T.dhl = reinterpret_cast<float2 *>(base + L.dhl);
+  T.colb = reinterpret_cast<float *>(base + L.colb);
+  return T;
+}
 
 namespace {
 
@@ -1283,12 +1321,6 @@ void Molecule::prepare_mixed() {
   };
   up(prim32, S->d_prim32);
   up(shA, S->d_shA);
-  S->d_ws = static_cast<float *>(alloc(std::max<size_t>(S->ws_floats, 1) * sizeof(float)));
-  S->d_rowscale = static_cast<float *>(
-      alloc(std::max<size_t>(S->blocks.size(), 1) * kBlockPts * sizeof(float)));
-  const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
-  S->d_dhl = static_cast<float2 *>(alloc(std::max<size_t>(nbf2, 1) * sizeof(float2)));
-  S->d_colb = static_cast<float *>(alloc(std::max<int>(basis.nbf, 1) * sizeof(float)));
   S->d_err = static_cast<int *>(alloc(sizeof(int)));
   cuda_check(cudaMemset(S->d_err, 0, sizeof(int)), "cudaMemset");
   MixTab &T = S->tab;
@@ -1297,22 +1329,34 @@ void Molecule::prepare_mixed() {
   T.dens_thr = bs.density_threshold;
   T.prim32 = S->d_prim32;
   T.shA = S->d_shA;
-  T.ws = S->d_ws;
-  T.rowscale = S->d_rowscale;
-  T.dhl = S->d_dhl;
-  T.colb = S->d_colb;
+  T.ws = nullptr;
+  T.rowscale = nullptr;
+  T.dhl = nullptr;
+  T.colb = nullptr;
   T.rho = d_rho;
   T.coef = d_coef;
   T.epart = d_epart;
   T.D = d_D;
   T.V = d_V;
   T.out2 = d_out2;
-  make_plan(S->single, {this}, {T});
   set_smem_attributes();
 }
 
+size_t Molecule::mixed_workspace_bytes() const { return ws_layout(*this).total; }
+
+void Molecule::ensure_mixed_ws() {
+  MixedState *S = mixed;
+  if (S->d_private)
+    return;
+  S->d_private = static_cast<char *>(alloc(ws_layout(*this).total));
+  auto P = std::make_unique<LaunchPlan>();
+  make_plan(*P, {this}, {bind_ws(*this, S->d_private)});
+  S->single = std::move(P);
+}
+
 void Molecule::build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st) {
-  run_plan(mixed->single, *ctx, Override{dD, dV, dout2}, mixed->d_err, st, ctx->max_ctas);
+  ensure_mixed_ws();
+  run_plan(*mixed->single, *ctx, Override{dD, dV, dout2}, mixed->d_err, st, ctx->max_ctas);
 }
 
 int mixed_error_flag(Molecule &M, cudaStream_t st) {
@@ -1349,17 +1393,19 @@ ListArena::~ListArena() {
 }
 
 void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListArena &arena,
-                       int *d_err, cudaStream_t st) {
+                       char *d_ws, int *d_err, cudaStream_t st) {
   LaunchPlan P[2];
   std::vector<Molecule *> group[2];
   std::vector<MixTab> tabs[2];
+  size_t wsoff = 0;
   for (size_t i = 0; i < mols.size(); i++) {
     for (size_t j = 0; j < i; j++)
       if (mols[j] == mols[i])
         throw ArgError("a molecule may appear only once in a group build");
     const int g = mols[i]->deriv ? 1 : 0;
     group[g].push_back(mols[i]);
-    tabs[g].push_back(mols[i]->mixed->tab);
+    tabs[g].push_back(bind_ws(*mols[i], d_ws + wsoff));
+    wsoff += mols[i]->mixed_workspace_bytes();
   }
   // pack both plans' lists into the arena: one pinned staging area, one copy
   size_t off = 0;
@@ -1415,11 +1461,29 @@ void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListAren
       run_plan(P[g], c, Override{nullptr, nullptr, nullptr}, d_err, st, c.max_ctas);
 }
 
+size_t group_workspace_bytes(const std::vector<Molecule *> &mols) {
+  size_t b = 0;
+  for (const Molecule *M : mols)
+    b += M->mixed_workspace_bytes();
+  return b;
+}
+
 // ---- batches ---------------------------------------------------------------
+// A batch owns one D, V and {E_xc, density} buffer per molecule and one
+// shared mixed workspace.  Its molecules are split, in order, into
+// sub-batches whose workspaces fit the cap; each sub-batch is one launch
+// sequence per functional family (LDA, GGA) and the sub-batches run one
+// after the other over the same workspace.
+struct SubBatch {
+  LaunchPlan plan[2];
+};
 struct Batch {
   std::vector<Molecule *> mols;
-  std::vector<double *> dD, dV, dE; // batch-owned buffers, one set per molecule
-  LaunchPlan plan[2];               // LDA molecules, GGA molecules
+  std::vector<double *> dD, dV, dE;
+  std::vector<std::unique_ptr<SubBatch>> subs;
+  char *d_ws = nullptr;      // mixed workspace of the largest sub-batch
+  size_t ws_bytes = 0;
+  double *d_ws64 = nullptr;  // FP64 workspace (molecules built one at a time), on first use
   int *d_err = nullptr;
   Context *ctx = nullptr;
   ~Batch() {
@@ -1429,51 +1493,95 @@ struct Batch {
       cudaFree(p);
     for (double *p : dE)
       cudaFree(p);
+    cudaFree(d_ws);
+    cudaFree(d_ws64);
     cudaFree(d_err);
   }
 };
 
-Batch *batch_create(Context *ctx, const std::vector<Molecule *> &mols) {
+Batch *batch_create(Context *ctx, const std::vector<Molecule *> &mols, double ws_cap) {
   auto B = std::make_unique<Batch>();
   B->ctx = ctx;
   B->mols = mols;
-  std::vector<MixTab> tabs[2];
-  std::vector<Molecule *> group[2];
-  for (size_t i = 0; i < mols.size(); i++) {
+  for (size_t i = 0; i < mols.size(); i++)
     for (size_t j = 0; j < i; j++)
       if (mols[j] == mols[i])
-        throw ArgError("a molecule may appear only once in a batch (its workspace is shared)");
-    const size_t n2 = static_cast<size_t>(mols[i]->basis.nbf) * mols[i]->basis.nbf;
+        throw ArgError("a molecule may appear only once in a batch (its buffers are shared)");
+  if (ws_cap <= 0) {
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    ws_cap = 0.5 * static_cast<double>(fr);
+  }
+  for (Molecule *M : mols) {
+    const size_t n2 = std::max<size_t>(static_cast<size_t>(M->basis.nbf) * M->basis.nbf, 1);
     double *d = nullptr, *v = nullptr, *e = nullptr;
-    cuda_check(cudaMalloc(&d, std::max<size_t>(n2, 1) * sizeof(double)), "cudaMalloc");
+    cuda_check(cudaMalloc(&d, n2 * sizeof(double)), "cudaMalloc");
     B->dD.push_back(d);
-    cuda_check(cudaMalloc(&v, std::max<size_t>(n2, 1) * sizeof(double)), "cudaMalloc");
+    cuda_check(cudaMalloc(&v, n2 * sizeof(double)), "cudaMalloc");
     B->dV.push_back(v);
     cuda_check(cudaMalloc(&e, 2 * sizeof(double)), "cudaMalloc");
     B->dE.push_back(e);
-    MixTab T = mols[i]->mixed->tab;
-    T.D = d;
-    T.V = v;
-    T.out2 = e;
-    const int g = mols[i]->deriv ? 1 : 0;
-    tabs[g].push_back(T);
-    group[g].push_back(mols[i]);
+  }
+  // partition in order under the cap (a molecule above the cap goes alone)
+  std::vector<std::vector<size_t>> parts;
+  size_t cur = 0;
+  for (size_t i = 0; i < mols.size(); i++) {
+    const size_t w = mols[i]->mixed_workspace_bytes();
+    if (parts.empty() || (cur + w > ws_cap && !parts.back().empty())) {
+      parts.emplace_back();
+      cur = 0;
+    }
+    parts.back().push_back(i);
+    cur += w;
+    B->ws_bytes = std::max(B->ws_bytes, cur);
+  }
+  cuda_check(cudaMalloc(&B->d_ws, std::max<size_t>(B->ws_bytes, 256)), "cudaMalloc");
+  for (const auto &part : parts) {
+    auto sb = std::make_unique<SubBatch>();
+    std::vector<Molecule *> group[2];
+    std::vector<MixTab> tabs[2];
+    size_t off = 0;
+    for (size_t i : part) {
+      Molecule *M = mols[i];
+      MixTab T = bind_ws(*M, B->d_ws + off);
+      off += M->mixed_workspace_bytes();
+      T.D = B->dD[i];
+      T.V = B->dV[i];
+      T.out2 = B->dE[i];
+      const int g = M->deriv ? 1 : 0;
+      group[g].push_back(M);
+      tabs[g].push_back(T);
+    }
+    for (int g = 0; g < 2; g++)
+      if (!group[g].empty())
+        make_plan(sb->plan[g], group[g], tabs[g]);
+    B->subs.push_back(std::move(sb));
   }
   cuda_check(cudaMalloc(&B->d_err, sizeof(int)), "cudaMalloc");
   cuda_check(cudaMemset(B->d_err, 0, sizeof(int)), "cudaMemset");
-  for (int g = 0; g < 2; g++)
-    if (!group[g].empty())
-      make_plan(B->plan[g], group[g], tabs[g]);
   return B.release();
+}
+
+// Workspaces a build of `precision` needs (allocated outside any capture).
+void batch_prepare(Batch &B, int precision) {
+  if (precision == OCC_XC_FP64 && !B.d_ws64) {
+    size_t w = 1;
+    for (Molecule *M : B.mols)
+      w = std::max(w, M->fp64_workspace_bytes());
+    cuda_check(cudaMalloc(&B.d_ws64, w), "cudaMalloc");
+  }
 }
 
 void batch_build(Batch &B, int precision, cudaStream_t st) {
   if (precision == OCC_XC_MIXED) {
-    for (LaunchPlan &P : B.plan)
-      run_plan(P, *B.ctx, Override{nullptr, nullptr, nullptr}, B.d_err, st, B.ctx->max_ctas);
+    for (auto &sb : B.subs)
+      for (LaunchPlan &P : sb->plan)
+        run_plan(P, *B.ctx, Override{nullptr, nullptr, nullptr}, B.d_err, st, B.ctx->max_ctas);
   } else {
+    if (!B.d_ws64)
+      throw ArgError("FP64 batch workspace missing (batch_prepare not called)");
     for (size_t i = 0; i < B.mols.size(); i++)
-      B.mols[i]->build_fp64(B.dD[i], B.dV[i], B.dE[i], st);
+      B.mols[i]->build_fp64(B.dD[i], B.dV[i], B.dE[i], st, B.d_ws64);
   }
 }
 
@@ -1609,8 +1717,8 @@ template <typename F> occ_xc_graph *capture(Context &c, F &&body) {
 
 extern "C" {
 
-int occ_xc_batch_create(occ_xc_context *ctx, int nmol, occ_xc_molecule *const *mols,
-                        occ_xc_batch **out) {
+int occ_xc_batch_create_capped(occ_xc_context *ctx, int nmol, occ_xc_molecule *const *mols,
+                               double workspace_cap_bytes, occ_xc_batch **out) {
   if (!ctx || !out || nmol <= 0 || !mols)
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
@@ -1625,9 +1733,14 @@ int occ_xc_batch_create(occ_xc_context *ctx, int nmol, occ_xc_molecule *const *m
     cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
     auto b = std::make_unique<occ_xc_batch>();
     b->ctx = ctx;
-    b->impl = batch_create(ctx->impl.get(), ms);
+    b->impl = batch_create(ctx->impl.get(), ms, workspace_cap_bytes);
     *out = b.release();
   });
+}
+
+int occ_xc_batch_create(occ_xc_context *ctx, int nmol, occ_xc_molecule *const *mols,
+                        occ_xc_batch **out) {
+  return occ_xc_batch_create_capped(ctx, nmol, mols, 0.0, out);
 }
 
 void occ_xc_batch_destroy(occ_xc_batch *b) {
@@ -1650,6 +1763,7 @@ int occ_xc_batch_compute(occ_xc_context *ctx, occ_xc_batch *b, int precision, vo
   std::lock_guard<std::mutex> lock(ctx->mu);
   return api_guard(ctx, [&] {
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
+    batch_prepare(*b->impl, precision);
     batch_build(*b->impl, precision, st);
   });
 }
@@ -1675,6 +1789,7 @@ int occ_xc_graph_capture(occ_xc_context *ctx, occ_xc_molecule *mol, int precisio
   *out = nullptr;
   return api_guard(ctx, [&] {
     cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
+    mol->impl->prepare(precision); // workspaces are allocated outside the capture
     *out = capture(*ctx->impl, [&](cudaStream_t st) {
       for (int k = 0; k < niter; k++)
         mol->impl->build(precision, d_D[k], d_V[k], d_exc2[k], st);
@@ -1690,6 +1805,7 @@ int occ_xc_batch_graph_capture(occ_xc_context *ctx, occ_xc_batch *b, int precisi
   *out = nullptr;
   return api_guard(ctx, [&] {
     cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
+    batch_prepare(*b->impl, precision);
     *out = capture(*ctx->impl, [&](cudaStream_t st) { batch_build(*b->impl, precision, st); });
   });
 }
@@ -1736,6 +1852,7 @@ extern "C" int occ_xc_batch_compute_host(occ_xc_context *ctx, occ_xc_batch *b, i
       cuda_check(cudaMemcpyAsync(B.dD[i], D[i], n2 * sizeof(double), cudaMemcpyHostToDevice, st),
                  "H2D");
     }
+    batch_prepare(B, precision);
     batch_build(B, precision, st);
     std::vector<double> e2(2 * B.mols.size());
     for (size_t i = 0; i < B.mols.size(); i++) {

@@ -39,7 +39,8 @@ thread_local std::string t_server_error;
 struct Session {
   uint64_t id = 0;
   std::unique_ptr<Molecule> mol;
-  double charge = 0.0; // admission charge: upper bound of the device bytes
+  double charge = 0.0; // admission charge: upper bound of the resident device bytes
+  size_t ws = 0;       // per-build workspace at the server's precision
   bool admitted = false;
   bool closing = false;
   long queued = 0; // builds submitted and not yet run
@@ -82,6 +83,8 @@ struct Server {
   long ticks = 0, tick_builds = 0, completed = 0, failed = 0;
   std::string fatal;
   ListArena arena;
+  char *d_ws = nullptr; // shared per-build workspace, sized for the tick
+  size_t ws_cap = 0;
   int *d_err = nullptr;
   double *h_stage = nullptr; // pinned staging for D in / V out
   size_t stage_cap = 0;      // doubles
@@ -108,6 +111,8 @@ struct Server {
       cudaFreeHost(h_stage);
     if (d_err)
       cudaFree(d_err);
+    if (d_ws)
+      cudaFree(d_ws);
   }
 
   void stage(size_t doubles) {
@@ -125,7 +130,7 @@ struct Server {
   // Pick this tick's builds; sessions to admit are charged here and
   // materialised by the caller outside the lock.
   void select(std::vector<Job *> &tick, std::vector<Session *> &admit,
-              std::vector<std::unique_ptr<Session>> &retire) {
+              std::vector<std::unique_ptr<Session>> &retire, size_t &tick_ws) {
     for (auto it = sessions.begin(); it != sessions.end();) {
       Session &S = *it->second;
       if (S.closing && S.queued == 0) {
@@ -140,6 +145,7 @@ struct Server {
     if (paused)
       return;
     std::vector<uint64_t> taken;
+    tick_ws = 0;
     for (auto &kv : jobs) {
       Job &J = *kv.second;
       if (J.status != 1 || static_cast<int>(tick.size()) >= cfg.max_batch)
@@ -148,16 +154,36 @@ struct Server {
         continue; // one build per session per tick, in submission order
       taken.push_back(J.session);
       Session &S = *sessions.at(J.session);
+      // the tick's workspace: the sum over its molecules (one launch
+      // sequence) or the largest one (FP64 builds one after the other)
+      const size_t ws_after =
+          cfg.precision == OCC_XC_MIXED ? tick_ws + S.ws : std::max(tick_ws, S.ws);
+      const double resident_after = admitted_bytes + (S.admitted ? 0.0 : S.charge);
+      if (resident_after + static_cast<double>(ws_after) > cfg.hbm_budget_bytes)
+        continue; // waits for memory; a smaller session may go first
       if (!S.admitted) {
-        if (admitted_bytes + S.charge > cfg.hbm_budget_bytes)
-          continue; // waits for memory; a smaller session may go first
         S.admitted = true;
         admitted_bytes += S.charge;
-        peak_bytes = std::max(peak_bytes, admitted_bytes);
         admit.push_back(&S);
       }
+      tick_ws = ws_after;
       tick.push_back(&J);
     }
+  }
+
+  // Shared workspace of at least `need` bytes within the budget.
+  void workspace(size_t need) {
+    const bool over = admitted_bytes + static_cast<double>(ws_cap) > cfg.hbm_budget_bytes;
+    if (need <= ws_cap && !over)
+      return;
+    if (d_ws)
+      cudaFree(d_ws);
+    d_ws = nullptr;
+    ws_cap = 0;
+    cuda_check(cudaMalloc(&d_ws, std::max<size_t>(need, 256)), "cudaMalloc");
+    ws_cap = need;
+    std::lock_guard<std::mutex> lk(mu);
+    peak_bytes = std::max(peak_bytes, admitted_bytes + static_cast<double>(ws_cap));
   }
 
   void run() {
@@ -170,12 +196,13 @@ struct Server {
       std::vector<Job *> tick;
       std::vector<Session *> admit;
       std::vector<std::unique_ptr<Session>> retire;
+      size_t tick_ws = 0;
       {
         std::unique_lock<std::mutex> lk(mu);
         cv_work.wait(lk, [&] { return stop || work_ready(); });
         if (stop)
           return;
-        select(tick, admit, retire);
+        select(tick, admit, retire, tick_ws);
       }
       retire.clear(); // device memory freed outside the lock
       if (tick.empty()) {
@@ -185,7 +212,7 @@ struct Server {
         cv_work.wait_for(lk, std::chrono::milliseconds(50));
         continue;
       }
-      execute(tick, admit);
+      execute(tick, admit, tick_ws);
     }
   }
 
@@ -219,7 +246,7 @@ struct Server {
     cv_work.notify_all();
   }
 
-  void execute(std::vector<Job *> &tick, std::vector<Session *> &admit) {
+  void execute(std::vector<Job *> &tick, std::vector<Session *> &admit, size_t tick_ws) {
     // materialise newly admitted sessions; one that does not get its memory
     // (the budget is an accounting limit, the device may hold less) is
     // returned to the waiting state and its build fails with NOMEM
@@ -256,6 +283,14 @@ struct Server {
     }
     cudaStream_t st = ctx->stream;
     try {
+      if (!failed_sessions.empty()) {
+        tick_ws = 0;
+        for (Molecule *M : mols)
+          tick_ws = cfg.precision == OCC_XC_MIXED
+                        ? tick_ws + M->mixed_workspace_bytes()
+                        : std::max(tick_ws, M->fp64_workspace_bytes());
+      }
+      workspace(tick_ws);
       size_t total = 0;
       for (Molecule *M : mols)
         total += 2 * static_cast<size_t>(M->basis.nbf) * M->basis.nbf + 2;
@@ -272,10 +307,10 @@ struct Server {
         off += 2 * n2 + 2;
       }
       if (cfg.precision == OCC_XC_MIXED) {
-        mixed_build_group(*ctx, mols, arena, d_err, st);
+        mixed_build_group(*ctx, mols, arena, d_ws, d_err, st);
       } else {
         for (Molecule *M : mols)
-          M->build_fp64(M->d_D, M->d_V, M->d_out2, st);
+          M->build_fp64(M->d_D, M->d_V, M->d_out2, st, reinterpret_cast<double *>(d_ws));
       }
       for (size_t i = 0; i < mols.size(); i++) {
         Molecule &M = *mols[i];
@@ -398,9 +433,12 @@ int occ_xc_server_open(occ_xc_server *srv, int natoms, const int *Z, const doubl
                    coefficients, pure, method, grid, build};
     auto sess = std::make_unique<Session>();
     sess->mol = molecule_host(S.ctx.get(), a); // host work on the caller's thread
-    sess->charge = sess->mol->estimate_device_bytes();
-    if (sess->charge > S.cfg.hbm_budget_bytes) {
-      t_server_error = "molecule needs " + std::to_string(sess->charge / 1e9) +
+    sess->charge = sess->mol->estimate_resident_bytes();
+    sess->ws = S.cfg.precision == OCC_XC_MIXED ? sess->mol->mixed_workspace_bytes()
+                                               : sess->mol->fp64_workspace_bytes();
+    if (sess->charge + static_cast<double>(sess->ws) > S.cfg.hbm_budget_bytes) {
+      t_server_error = "molecule needs " +
+                       std::to_string((sess->charge + static_cast<double>(sess->ws)) / 1e9) +
                        " GB of device memory, more than the server's budget";
       return static_cast<int>(OCC_XC_ERR_NOMEM);
     }
@@ -568,7 +606,9 @@ int occ_xc_server_session_info(occ_xc_server *srv, uint64_t session, occ_xc_mole
   out->nleaves = static_cast<long>(M.leaves.size());
   out->flops_per_build = M.flops;
   out->device_bytes = it->second->admitted ? M.device_bytes : 0.0;
-  out->workspace_bytes = it->second->charge;
+  out->workspace_bytes = static_cast<double>(M.fp64_workspace_bytes());
+  out->mixed_workspace_bytes = static_cast<double>(M.mixed_workspace_bytes());
+  out->resident_bytes = it->second->charge;
   if (admitted)
     *admitted = it->second->admitted ? 1 : 0;
   return OCC_XC_OK;
@@ -593,7 +633,7 @@ int occ_xc_server_stats_get(occ_xc_server *srv, occ_xc_server_stats *o) {
     (kv.second->admitted ? adm : wait)++;
   o->sessions_admitted = adm;
   o->sessions_waiting = wait;
-  o->admitted_bytes = S.admitted_bytes;
+  o->admitted_bytes = S.admitted_bytes + static_cast<double>(S.ws_cap);
   o->peak_admitted_bytes = S.peak_bytes;
   return OCC_XC_OK;
 }

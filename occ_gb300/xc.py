@@ -53,7 +53,8 @@ class _BuildSettings(C.Structure):
 class _MolInfo(C.Structure):
     _fields_ = [("nbf", C.c_int), ("natoms", C.c_int), ("nshells", C.c_int), ("deriv", C.c_int),
                 ("npoints", C.c_long), ("nleaves", C.c_long), ("flops_per_build", C.c_double),
-                ("device_bytes", C.c_double), ("workspace_bytes", C.c_double)]
+                ("device_bytes", C.c_double), ("workspace_bytes", C.c_double),
+                ("mixed_workspace_bytes", C.c_double), ("resident_bytes", C.c_double)]
 
 
 _dp = C.POINTER(C.c_double)
@@ -101,6 +102,7 @@ def library():
     _vp = C.c_void_p
     _pp = C.POINTER(C.c_void_p)
     lib.occ_xc_batch_create.argtypes = [_vp, C.c_int, _pp, _pp]
+    lib.occ_xc_batch_create_capped.argtypes = [_vp, C.c_int, _pp, C.c_double, _pp]
     lib.occ_xc_batch_destroy.argtypes = [_vp]
     lib.occ_xc_batch_buffers.argtypes = [_vp, C.c_int, _pp, _pp, _pp]
     lib.occ_xc_batch_compute.argtypes = [_vp, _vp, C.c_int, _vp]
@@ -375,7 +377,7 @@ class Batch:
     """Several molecules built together: one persistent launch sequence per
     precision, the molecules' leaves interleaved over the SMs."""
 
-    def __init__(self, dfts):
+    def __init__(self, dfts, workspace_cap_bytes=0.0):
         if not dfts:
             raise XCError("a batch needs at least one molecule")
         self.dfts = list(dfts)
@@ -384,7 +386,8 @@ class Batch:
             raise XCError("every molecule of a batch must be on the same device")
         hs = (C.c_void_p * len(self.dfts))(*[d.h.value for d in self.dfts])
         h = C.c_void_p()
-        rc = self.ctx.lib.occ_xc_batch_create(self.ctx.h, len(self.dfts), hs, C.byref(h))
+        rc = self.ctx.lib.occ_xc_batch_create_capped(self.ctx.h, len(self.dfts), hs,
+                                                     float(workspace_cap_bytes), C.byref(h))
         if rc != 0:
             raise XCError(f"occ_xc_batch_create failed ({rc}): {self.ctx.error()}")
         self.h = h

@@ -51,6 +51,20 @@ def test_batch_matches_direct_builds(cases, precision):
         assert np.max(np.abs(Vs[i] - V)) <= TOL_SAME_V, i
 
 
+def test_workspace_cap_splits_into_sub_batches(cases):
+    """A cap below every molecule's workspace: each molecule its own
+    sub-batch, same results."""
+    direct = []
+    for dft, D, _, _ in cases:
+        V = dft.compute_vxc(D, og.MIXED)
+        direct.append((V, dft.exchange_correlation_energy()))
+    batch = og.Batch([c[0] for c in cases], workspace_cap_bytes=1.0)
+    Vs, exc, _ = batch.compute_vxc([c[1] for c in cases], og.MIXED)
+    for i, (V, e) in enumerate(direct):
+        assert abs(exc[i] - e) <= TOL_SAME_E
+        assert np.max(np.abs(Vs[i] - V)) <= TOL_SAME_V
+
+
 def test_mixed_batch_against_oracle(cases):
     batch = og.Batch([c[0] for c in cases])
     Vs, exc, _ = batch.compute_vxc([c[1] for c in cases], og.MIXED)

@@ -81,13 +81,21 @@ def test_iterations_of_a_session_run_in_order(specs):
         srv.shutdown()
 
 
-def test_admission_waits_for_memory(specs):
-    method, b, nocc = specs[4]
+def _sizes(method, b):
     probe = og.Server()
-    sid = probe.open(method, b)
-    charge = probe.session_info(sid)["workspace_bytes"]
-    probe.shutdown()
-    srv = og.Server(hbm_budget_bytes=1.5 * charge)  # room for one of the two
+    try:
+        info = probe.session_info(probe.open(method, b))
+    finally:
+        probe.shutdown()
+    return info["resident_bytes"], info["mixed_workspace_bytes"]
+
+
+def test_admission_waits_for_memory(specs):
+    """Room for one session's resident state plus a tick's workspace, not two."""
+    method, b, nocc = specs[4]
+    r, w = _sizes(method, b)
+    budget = 1.5 * r + w
+    srv = og.Server(hbm_budget_bytes=budget)
     try:
         a = srv.open(method, b)
         c = srv.open(method, b)
@@ -101,11 +109,33 @@ def test_admission_waits_for_memory(specs):
         st = srv.stats()
         assert st["sessions_admitted"] == 1 and st["sessions_waiting"] == 1
         info = srv.session_info(a)
-        assert info["admitted"] and 0 < info["device_bytes"] <= info["workspace_bytes"]
+        assert info["admitted"] and 0 < info["device_bytes"] <= info["resident_bytes"]
         srv.close(a)
         Vc, ec, _ = srv.wait(tc, timeout=120.0)
         assert abs(ec - ea) <= TOL_SAME and np.max(np.abs(Vc - Va)) <= TOL_SAME
-        assert srv.stats()["peak_admitted_bytes"] <= 1.5 * charge
+        assert srv.stats()["peak_admitted_bytes"] <= budget
+    finally:
+        srv.shutdown()
+
+
+def test_tick_workspace_bounds_the_batch(specs):
+    """Both sessions resident, but one tick's workspace holds only one build."""
+    method, b, nocc = specs[4]
+    r, w = _sizes(method, b)
+    budget = 2.2 * r + 1.5 * w
+    srv = og.Server(hbm_budget_bytes=budget)
+    try:
+        srv.pause(True)
+        a = srv.open(method, b)
+        c = srv.open(method, b)
+        D = wl.random_density(b.nbf(), nocc, seed=8)
+        ta, tc = srv.submit(a, D), srv.submit(c, D)
+        srv.pause(False)
+        (Va, ea, _), (Vc, ec, _) = srv.wait(ta), srv.wait(tc)
+        st = srv.stats()
+        assert st["ticks"] == 2 and st["sessions_admitted"] == 2
+        assert st["peak_admitted_bytes"] <= budget
+        assert abs(ec - ea) <= TOL_SAME and np.max(np.abs(Vc - Va)) <= TOL_SAME
     finally:
         srv.shutdown()
 
