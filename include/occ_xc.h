@@ -263,6 +263,35 @@ int occ_xc_server_session_info(occ_xc_server *server, uint64_t session,
                                occ_xc_molecule_info *out, int *admitted);
 int occ_xc_server_stats_get(occ_xc_server *server, occ_xc_server_stats *out);
 
+/* ---- build settings and autotuning ----------------------------------------
+ * Replaces DFT::set_xc_screening_threshold (include/occ/dft/dft.h:590) and
+ * the leaf sizes of SpatialGridHierarchy (spatial_grid_hierarchy.h:26-30):
+ * new leaves and screening for the molecule, grid kept.  The molecule's
+ * device buffers are reallocated: graphs captured on it become invalid. */
+int occ_xc_molecule_set_build_settings(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                       const occ_xc_build_settings *build);
+
+typedef struct {
+  int leaf_target, leaf_min, leaf_max; /* chosen Morton leaf sizes */
+  int vxc_tile_n;                      /* N of the mixed path's V_xc tile */
+  int persistent_ctas;                 /* 0 = one per SM */
+  double ms_per_build;                 /* measured at the choice */
+  double default_ms_per_build;         /* measured at OCC's leaf sizes */
+  double max_dexc;                     /* largest |E_xc - E_xc(default)| accepted */
+  int candidates;                      /* builds configurations timed */
+  int from_cache;                      /* 1: taken from OCC_XC_TUNE_CACHE, nothing timed */
+} occ_xc_tune_result;
+/* Times builds of the molecule with density D (host, nbf x nbf) at several
+ * leaf sizes {64, 128, 256, 512}, V_xc tiles {128, 256} and CTA counts, keeps
+ * candidates whose E_xc is within tol_exc of the default-settings build, and
+ * (apply != 0) leaves the molecule set up with the fastest.  The choice is
+ * appended to the file named by the environment variable OCC_XC_TUNE_CACHE
+ * (when set) and read back from it on later calls.  Invalidates graphs
+ * captured on the molecule. */
+int occ_xc_molecule_autotune(occ_xc_context *ctx, occ_xc_molecule *mol, int precision,
+                             const double *D, double tol_exc, int apply,
+                             occ_xc_tune_result *out);
+
 /* CTAs of the persistent tensor-core kernels (0 = one per SM, the default);
  * fewer leave SMs free for concurrent builds on other streams. */
 int occ_xc_set_persistent_ctas(occ_xc_context *ctx, int ctas);

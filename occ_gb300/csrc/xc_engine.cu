@@ -383,6 +383,14 @@ GridSettings grid_settings_from(const occ_xc_grid_settings *grid) {
 }
 
 
+void check_build_settings(const BuildSettings &b) {
+  if (b.leaf_max > 1024 || b.leaf_target <= 0 || b.leaf_min <= 0 || b.leaf_target > b.leaf_max ||
+      2 * b.leaf_min > b.leaf_max)
+    throw ArgError("leaf sizes must satisfy 0 < target <= max <= 1024, 2 min <= max");
+  if (!(b.xc_screening_threshold >= 0.0) || !(b.density_threshold >= 0.0))
+    throw ArgError("thresholds must be non-negative");
+}
+
 std::unique_ptr<Molecule> molecule_host(Context *ctx, const MoleculeArgs &a) {
   if (a.natoms <= 0 || a.nshells <= 0 || !a.Z || !a.xyz || !a.shell_l || !a.shell_atom ||
       !a.shell_nprim || !a.exponents || !a.coefficients || !a.method)
@@ -405,13 +413,22 @@ std::unique_ptr<Molecule> molecule_host(Context *ctx, const MoleculeArgs &a) {
     M->bs.leaf_target = a.build->leaf_target;
     M->bs.leaf_min = a.build->leaf_min;
     M->bs.leaf_max = a.build->leaf_max;
-    if (M->bs.leaf_max > 256 || M->bs.leaf_target <= 0 || M->bs.leaf_min <= 0 ||
-        M->bs.leaf_target > M->bs.leaf_max || 2 * M->bs.leaf_min > M->bs.leaf_max)
-      throw ArgError("leaf sizes must satisfy 0 < target <= max <= 256, 2 min <= max");
+    check_build_settings(M->bs);
   }
   M->grid = build_molecular_grid(M->Z, M->xyz, M->basis, M->gs, 0);
   M->build_plan();
   return M;
+}
+
+void replan(Molecule &M, const BuildSettings &b) {
+  check_build_settings(b);
+  const bool had = !M.allocations.empty();
+  if (had)
+    M.release_device();
+  M.bs = b;
+  M.build_plan();
+  if (had)
+    M.materialise();
 }
 
 void Molecule::materialise() {

@@ -104,6 +104,8 @@ struct Molecule {
   BuildSettings bs;
   FuncSet fs{};
   int deriv = 0;
+  int vxc_n = 256; // tuning: N of the mixed path's V_xc tile
+  int ctas = 0;    // tuning: CTAs of its persistent kernels (0: the context's setting)
   MolecularGrid grid;
   Plan plan;
   // device plan
@@ -153,6 +155,10 @@ struct Molecule {
 // Host part of a molecule: basis, molecular grid, Morton leaves and screening
 // (no device memory); materialise() uploads it.
 std::unique_ptr<Molecule> molecule_host(Context *ctx, const MoleculeArgs &a);
+void check_build_settings(const BuildSettings &b);
+// New leaves and screening under `b` (the grid is kept); device state is
+// rebuilt if the molecule had any.
+void replan(Molecule &M, const BuildSettings &b);
 
 // Staging for launch lists built per call (the server's batched builds):
 // one device region and one pinned host region, grown on demand.

@@ -18,6 +18,7 @@
 //   k_reduce      fixed-order sum of the per-leaf partials (dft.h:374-380)
 #include "host/gto_eval.h"
 #include "xc_device.cuh"
+#include "xc_leaf_func.cuh"
 
 namespace occx {
 
@@ -249,20 +250,6 @@ __device__ __forceinline__ double block_sum_256(double v, double *sh) {
   return s;
 }
 
-__device__ __forceinline__ double block_max_256(double v, double *sh) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
-    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0)
-    sh[w] = v;
-  __syncthreads();
-  double s = sh[0];
-  for (int i = 1; i < (blockDim.x >> 5); i++)
-    s = fmax(s, sh[i]);
-  __syncthreads();
-  return s;
-}
 
 // One CTA per leaf (<= 256 points).
 template <bool DERIV>
@@ -271,40 +258,8 @@ __global__ void __launch_bounds__(256) k_func(MolDev m, FuncSet fs, double thr,
                                               double *__restrict__ coef,
                                               double *__restrict__ epart) {
   __shared__ double sh[8];
-  const DevLeaf L = m.leaves[blockIdx.x];
-  const int p = threadIdx.x;
-  const bool valid = p < L.cnt;
-  const size_t idx = static_cast<size_t>(L.off) + p;
-  const size_t N = static_cast<size_t>(m.npts);
-  const double r = valid ? rho[idx] : 0.0;
-  const double w = valid ? m.pts[idx].w : 0.0;
-  const double mx = block_max_256(valid ? r : -1e300, sh);
-  const double nel = block_sum_256(w * r, sh);
-  double gx = 0, gy = 0, gz = 0, sigma = 0;
-  if (DERIV && valid) {
-    gx = rho[N + idx];
-    gy = rho[2 * N + idx];
-    gz = rho[3 * N + idx];
-    sigma = gx * gx + gy * gy + gz * gz;
-  }
-  double e = 0, vr = 0, vs = 0;
-  const bool skip = mx < thr;
-  if (valid && !skip)
-    eval_xc(fs, r, sigma, e, vr, vs);
-  if (valid) {
-    coef[idx] = 0.5 * w * vr;
-    if (DERIV) {
-      const double f = 2.0 * w * vs;
-      coef[N + idx] = f * gx;
-      coef[2 * N + idx] = f * gy;
-      coef[3 * N + idx] = f * gz;
-    }
-  }
-  const double esum = block_sum_256(w * e, sh);
-  if (threadIdx.x == 0) {
-    epart[2 * blockIdx.x] = esum;
-    epart[2 * blockIdx.x + 1] = nel;
-  }
+  leaf_functional<DERIV>(m.leaves[blockIdx.x], m.pts, static_cast<size_t>(m.npts), fs, thr, rho,
+                         coef, epart + 2 * blockIdx.x, sh);
 }
 
 // K = phi_I^T Y_J for one 64x64 AO tile of one leaf; V += K + K^T.

@@ -1,0 +1,86 @@
+// The functional stage of one Morton leaf, shared by the FP64 and the mixed
+// paths: include/occ/dft/dft.h:339-352 with src/dft/dft_kernels.cpp:27-70.
+// One CTA of 256 threads per leaf; a leaf may hold any number of points
+// (threads stride over them).  The leaf is skipped when max rho < thr
+// (dft_kernels.cpp:37-40); coefficients are those of the V_xc contraction
+// (src/dft/xc_potential_matrix.cpp:19-41): coef0 = 0.5 w vrho and, for a GGA,
+// coef1..3 = 2 w vsigma grad rho.  epart2 receives {sum w e_xc rho, sum w rho}.
+#pragma once
+#include "functionals.cuh"
+#include "xc_device.cuh"
+
+namespace occx {
+
+__device__ __forceinline__ double leaf_sum256(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < 8; i++)
+    s += sh[i];
+  __syncthreads();
+  return s;
+}
+
+__device__ __forceinline__ double leaf_max256(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = sh[0];
+  for (int i = 1; i < 8; i++)
+    s = fmax(s, sh[i]);
+  __syncthreads();
+  return s;
+}
+
+template <bool DERIV>
+__device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__restrict__ pts,
+                                                size_t N, const FuncSet &fs, double thr,
+                                                const double *__restrict__ rho,
+                                                double *__restrict__ coef, double *epart2,
+                                                double *sh) {
+  double mx = -1e300;
+  for (int p = threadIdx.x; p < L.cnt; p += 256)
+    mx = fmax(mx, rho[static_cast<size_t>(L.off) + p]);
+  mx = leaf_max256(mx, sh);
+  const bool skip = mx < thr;
+  double nel = 0.0, ew = 0.0;
+  for (int p = threadIdx.x; p < L.cnt; p += 256) {
+    const size_t idx = static_cast<size_t>(L.off) + p;
+    const double r = rho[idx];
+    const double w = pts[idx].w;
+    nel += w * r;
+    double gx = 0, gy = 0, gz = 0, sigma = 0;
+    if (DERIV) {
+      gx = rho[N + idx];
+      gy = rho[2 * N + idx];
+      gz = rho[3 * N + idx];
+      sigma = gx * gx + gy * gy + gz * gz;
+    }
+    double e = 0, vr = 0, vs = 0;
+    if (!skip)
+      eval_xc(fs, r, sigma, e, vr, vs);
+    coef[idx] = 0.5 * w * vr;
+    if (DERIV) {
+      const double f = 2.0 * w * vs;
+      coef[N + idx] = f * gx;
+      coef[2 * N + idx] = f * gy;
+      coef[3 * N + idx] = f * gz;
+    }
+    ew += w * e;
+  }
+  nel = leaf_sum256(nel, sh);
+  ew = leaf_sum256(ew, sh);
+  if (threadIdx.x == 0) {
+    epart2[0] = ew;
+    epart2[1] = nel;
+  }
+}
+
+} // namespace occx

@@ -28,6 +28,7 @@
 #include "../../include/occ_xc.h"
 #include "host/gto_eval.h"
 #include "umma.cuh"
+#include "xc_leaf_func.cuh"
 #include "xc_engine.hpp"
 
 namespace occx {
@@ -128,6 +129,7 @@ struct MixTab {
   const double *D;      // this build's density (mo.D)
   double *V;            // V_xc (upper triangle, then mirrored)
   double *out2;         // {E_xc, integrated density}
+  int vxc_n;            // N of the V_xc tile (64, 128 or 256)
 };
 
 // Per-launch replacement of a one-molecule table's D / V / out2 (so that a
@@ -779,8 +781,9 @@ __global__ void __launch_bounds__(256, 1) k_vxc_mixed(const MixTab *__restrict__
   }
   __syncthreads();
   const int rows = min(128, B.mp - it.i0);
-  for (int n0 = 0; n0 < B.mp; n0 += kMaxN) {
-    const int N = min(kMaxN, B.mp - n0);
+  const int NT = T.vxc_n; // tile N (a multiple of 32, at most kMaxN)
+  for (int n0 = 0; n0 < B.mp; n0 += NT) {
+    const int N = min(NT, B.mp - n0);
     auto fa = [&](int c, uint8_t *st) {
       const int r = t & 127, kh = t >> 7;
       const bool rv = r < rows;
@@ -885,19 +888,6 @@ __device__ __forceinline__ double bsum256(double v, double *sh) {
   __syncthreads();
   return s;
 }
-__device__ __forceinline__ double bmax256(double v, double *sh) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
-    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  if ((threadIdx.x & 31) == 0)
-    sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double s = sh[0];
-  for (int i = 1; i < 8; i++)
-    s = fmax(s, sh[i]);
-  __syncthreads();
-  return s;
-}
 
 template <bool DERIV>
 __global__ void __launch_bounds__(256) k_func_b(const MixTab *__restrict__ tabs,
@@ -905,41 +895,8 @@ __global__ void __launch_bounds__(256) k_func_b(const MixTab *__restrict__ tabs,
   __shared__ double sh[8];
   const LeafItem li = litems[blockIdx.x];
   const MixTab &T = tabs[li.mol];
-  const DevLeaf L = T.m.leaves[li.leaf];
-  const int p = threadIdx.x;
-  const bool valid = p < L.cnt;
-  const size_t idx = static_cast<size_t>(L.off) + p;
-  const size_t N = static_cast<size_t>(T.m.npts);
-  const double *__restrict__ rho = T.rho;
-  const double r = valid ? rho[idx] : 0.0;
-  const double w = valid ? T.m.pts[idx].w : 0.0;
-  const double mx = bmax256(valid ? r : -1e300, sh);
-  const double nel = bsum256(w * r, sh);
-  double gx = 0, gy = 0, gz = 0, sigma = 0;
-  if (DERIV && valid) {
-    gx = rho[N + idx];
-    gy = rho[2 * N + idx];
-    gz = rho[3 * N + idx];
-    sigma = gx * gx + gy * gy + gz * gz;
-  }
-  double e = 0, vr = 0, vs = 0;
-  if (valid && !(mx < T.dens_thr))
-    eval_xc(T.fs, r, sigma, e, vr, vs);
-  if (valid) {
-    double *__restrict__ coef = T.coef;
-    coef[idx] = 0.5 * w * vr;
-    if (DERIV) {
-      const double f = 2.0 * w * vs;
-      coef[N + idx] = f * gx;
-      coef[2 * N + idx] = f * gy;
-      coef[3 * N + idx] = f * gz;
-    }
-  }
-  const double esum = bsum256(w * e, sh);
-  if (threadIdx.x == 0) {
-    T.epart[2 * li.leaf] = esum;
-    T.epart[2 * li.leaf + 1] = nel;
-  }
+  leaf_functional<DERIV>(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts), T.fs,
+                         T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
 }
 
 // Fixed-order FP64 sums of the per-leaf partials, one CTA per molecule.
@@ -1339,6 +1296,7 @@ void Molecule::prepare_mixed() {
   T.D = d_D;
   T.V = d_V;
   T.out2 = d_out2;
+  T.vxc_n = vxc_n;
   set_smem_attributes();
 }
 
@@ -1356,7 +1314,8 @@ void Molecule::ensure_mixed_ws() {
 
 void Molecule::build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st) {
   ensure_mixed_ws();
-  run_plan(*mixed->single, *ctx, Override{dD, dV, dout2}, mixed->d_err, st, ctx->max_ctas);
+  run_plan(*mixed->single, *ctx, Override{dD, dV, dout2}, mixed->d_err, st,
+           ctas > 0 ? ctas : ctx->max_ctas);
 }
 
 int mixed_error_flag(Molecule &M, cudaStream_t st) {

@@ -61,6 +61,13 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
 
+class _TuneResult(C.Structure):
+    _fields_ = [("leaf_target", C.c_int), ("leaf_min", C.c_int), ("leaf_max", C.c_int),
+                ("vxc_tile_n", C.c_int), ("persistent_ctas", C.c_int),
+                ("ms_per_build", C.c_double), ("default_ms_per_build", C.c_double),
+                ("max_dexc", C.c_double), ("candidates", C.c_int), ("from_cache", C.c_int)]
+
+
 class _ServerSettings(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("queue_capacity", C.c_int),
                 ("max_batch", C.c_int), ("precision", C.c_int)]
@@ -130,6 +137,9 @@ def library():
     lib.occ_xc_server_session_info.argtypes = [_vp, _u64, C.POINTER(_MolInfo),
                                                C.POINTER(C.c_int)]
     lib.occ_xc_server_stats_get.argtypes = [_vp, C.POINTER(_ServerStats)]
+    lib.occ_xc_molecule_set_build_settings.argtypes = [_vp, _vp, C.POINTER(_BuildSettings)]
+    lib.occ_xc_molecule_autotune.argtypes = [_vp, _vp, C.c_int, _dp, C.c_double, C.c_int,
+                                             C.POINTER(_TuneResult)]
     lib.occ_xc_batch_set_density.argtypes = [_vp, _vp, C.c_int, _dp]
     lib.occ_xc_batch_get_result.argtypes = [_vp, _vp, C.c_int, _dp, _dp]
     _LIB = lib
@@ -365,6 +375,28 @@ class DFT:
         self._exc = exc.value
         self._nelec = nel.value
         return V
+
+    def set_build_settings(self, build_settings):
+        """New leaves and screening (DFT::set_xc_screening_threshold and the
+        Morton leaf sizes); the grid is kept."""
+        bs = build_settings._c()
+        rc = self.ctx.lib.occ_xc_molecule_set_build_settings(self.ctx.h, self.h, C.byref(bs))
+        if rc != 0:
+            raise XCError(f"occ_xc_molecule_set_build_settings failed ({rc}): "
+                          f"{self.ctx.error()}", rc)
+
+    def autotune(self, D, precision=MIXED, tol_exc=1e-7, apply=True):
+        """Time builds at several leaf sizes / tiles and keep the fastest
+        (see occ_xc_molecule_autotune); returns the choice and timings."""
+        Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if Dm.shape != (self.nbf(), self.nbf()):
+            raise XCError(f"density matrix must be {self.nbf()}x{self.nbf()}")
+        r = _TuneResult()
+        rc = self.ctx.lib.occ_xc_molecule_autotune(self.ctx.h, self.h, int(precision), _ptr(Dm),
+                                                   float(tol_exc), int(bool(apply)), C.byref(r))
+        if rc != 0:
+            raise XCError(f"occ_xc_molecule_autotune failed ({rc}): {self.ctx.error()}", rc)
+        return {f: getattr(r, f) for f, _ in _TuneResult._fields_}
 
     def exchange_correlation_energy(self):
         return self._exc
