@@ -49,7 +49,37 @@ def parse():
                     help="cluster size (32 is the benchmark; smaller only for profiling)")
     ap.add_argument("--ctas", type=int, default=0,
                     help="CTAs of the persistent tensor-core kernels (0: one per SM)")
+    ap.add_argument("--workload", default="water32",
+                    choices=["water32", "alkane", "clusters", "stream"],
+                    help="water32: the headline build (default); alkane: C30H62 def2-TZVP "
+                         "B3LYP, 15 iterations as one CUDA graph; clusters: 512 clusters "
+                         "as one batch; stream: served Poisson request stream")
+    ap.add_argument("--clusters", type=int, default=512)
+    ap.add_argument("--requests", type=int, default=32)
+    ap.add_argument("--rate", type=float, default=10.0, help="stream arrivals per second")
     return ap.parse_args()
+
+
+def run_workload(args):
+    """The non-headline workloads (occ_gb300/bench_workloads.py), one JSON line."""
+    import torch
+    from occ_gb300 import bench_workloads as bw
+    torch.cuda.set_device(0)
+    with ClockSampler(0) as cs:
+        if args.workload == "alkane":
+            r = bw.alkane_graph(torch, steps=args.steps, warmup=args.warmup)
+        elif args.workload == "clusters":
+            r = bw.clusters_batch(torch, steps=args.steps, warmup=args.warmup,
+                                  nclusters=args.clusters)
+        else:
+            r = bw.stream(nreq=args.requests, rate=args.rate)
+    m = r["mixed"]
+    line = {"metric": METRIC, "value": m["builds_per_s"], "unit": "builds/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3+f64", "data": "synthetic",
+            "config": {"workload": r.pop("workload")}, "clocks": cs.summary()}
+    line.update(r)
+    print(json.dumps(line))
 
 
 def make_workload(seed=0, waters=32):
@@ -259,6 +289,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "water32":
+        run_workload(args)
         return
     import torch
     import torch.distributed as dist

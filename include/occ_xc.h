@@ -291,6 +291,10 @@ typedef struct {
 int occ_xc_molecule_autotune(occ_xc_context *ctx, occ_xc_molecule *mol, int precision,
                              const double *D, double tol_exc, int apply,
                              occ_xc_tune_result *out);
+/* Sets a molecule up with a tuning result (leaf sizes, tile, CTAs) found for
+ * a similar one, e.g. one molecule per size class of a batch. */
+int occ_xc_molecule_apply_tuning(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                 const occ_xc_tune_result *tuning);
 
 /* CTAs of the persistent tensor-core kernels (0 = one per SM, the default);
  * fewer leave SMs free for concurrent builds on other streams. */

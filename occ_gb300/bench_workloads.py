@@ -1,0 +1,209 @@
+"""Benchmark harness for the workloads beside the 32-water headline build.
+
+alkane_graph    n-C30H62, def2-TZVP, B3LYP (local part), 15 SCF-iteration
+                densities captured as one CUDA graph per precision; graph
+                replays timed with CUDA events; E_xc of every iteration,
+                mixed against FP64.
+clusters        512 water clusters, n uniform in {1..24}, box 3.1 n^(1/3)
+                Angstrom, def2-SVP, PBE, built as one batch (one launch
+                sequence per sub-batch); leaf size and tile from the
+                autotuner, tuned on one molecule per size and applied to the
+                rest; builds/s and grid points/s, mixed against FP64.
+stream          Poisson arrivals (seeded rate) of requests of 8-20 SCF
+                iterations for water clusters with n uniform in {2..48},
+                def2-SVP, PBE, each iteration's density the previous one plus
+                seeded symmetric noise of norm 1e-3, served through the
+                serving loop (continuous batching, 150 GB budget); p50 / p99
+                latency (submit to result ready) and throughput, mixed and
+                FP64.
+
+Every input is seeded synthetic data with the shapes of these workloads.
+Each function returns a dict for one JSON line.
+"""
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import workloads as wl
+from .xc import FP64, MIXED, Batch, DFT, Server, capture_scf_graph
+
+
+def _pct(v, q):
+    return float(np.percentile(np.asarray(v), q)) if len(v) else None
+
+
+def alkane_graph(torch, steps=3, warmup=3, iterations=15, seed=0, ncarbon=30):
+    mol = wl.alkane(ncarbon)
+    basis = wl.basis_for(mol, "def2-tzvp")
+    nbf = basis.nbf()
+    nocc = (6 * ncarbon + 2 * ncarbon + 2) // 2  # electrons / 2
+    D0 = wl.random_density(nbf, nocc, seed=seed)
+    Ds = [wl.perturbed(D0, 1e-3, seed + 1 + k) if k else D0 for k in range(iterations)]
+    t0 = time.perf_counter()
+    dft = DFT("b3lyp", basis)
+    setup_s = time.perf_counter() - t0
+    info = dft.info()
+    dD = [torch.from_numpy(np.ascontiguousarray(D.T)).cuda() for D in Ds]
+    out = {"workload": f"alkane_c{ncarbon}_def2tzvp_b3lyp_graph{iterations}",
+           "natoms": len(mol), "nbf": nbf, "npoints": info["npoints"],
+           "flops_per_build": info["flops_per_build"], "host_setup_s": setup_s}
+    stream = torch.cuda.Stream()
+    excs = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        dV = [torch.zeros((nbf, nbf), dtype=torch.float64, device="cuda") for _ in Ds]
+        dE = [torch.zeros(2, dtype=torch.float64, device="cuda") for _ in Ds]
+        torch.cuda.synchronize()
+        g = capture_scf_graph(dft, prec, [t.data_ptr() for t in dD], [t.data_ptr() for t in dV],
+                              [t.data_ptr() for t in dE])
+        for _ in range(warmup):
+            g.launch(stream.cuda_stream)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record(stream)
+        for i in range(steps):
+            g.launch(stream.cuda_stream)
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+        excs[name] = np.array([float(e[0].item()) for e in dE])
+        out[name] = {"builds_per_s": iterations * steps / (sum(per) / 1e3),
+                     "ms_per_graph": float(np.median(per)),
+                     "ms_per_build": float(np.median(per)) / iterations}
+        del g
+    de = excs["mixed"] - excs["fp64"]
+    out["max_abs_dE_xc_per_iteration"] = float(np.max(np.abs(de)))
+    out["dE_xc_sum_over_iterations"] = float(np.sum(de))
+    out["exc_fp64_first_last"] = [float(excs["fp64"][0]), float(excs["fp64"][-1])]
+    return out
+
+
+def clusters_batch(torch, steps=2, warmup=1, nclusters=512, seed=0, autotune=True):
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(1, 25, nclusters)
+    t0 = time.perf_counter()
+    dfts, Ds, bases = [], [], []
+    for i, n in enumerate(sizes):
+        mol = wl.water_cluster(int(n), box=3.1 * float(n) ** (1.0 / 3.0), seed=seed + 1000 + i)
+        b = wl.basis_for(mol, "def2-svp")
+        bases.append(b)
+        dfts.append(DFT("pbe", b))
+        Ds.append(wl.random_density(b.nbf(), 5 * int(n), seed=seed + 5000 + i))
+    setup_s = time.perf_counter() - t0
+    tuned = {}
+    t0 = time.perf_counter()
+    if autotune:
+        for i, n in enumerate(sizes):
+            n = int(n)
+            if n not in tuned:
+                tuned[n] = dfts[i].autotune(Ds[i], MIXED, tol_exc=1e-7)
+            else:
+                dfts[i].apply_tuning(tuned[n])
+    tune_s = time.perf_counter() - t0
+    npts = sum(d.info()["npoints"] for d in dfts)
+    out = {"workload": f"clusters{nclusters}_n1to24_def2svp_pbe_batch", "nclusters": nclusters,
+           "total_points": int(npts), "total_atoms": int(3 * sizes.sum()),
+           "host_setup_s": setup_s, "autotune_s": tune_s,
+           "tuned_leaf_targets": sorted({int(t["leaf_target"]) for t in tuned.values()})}
+    batch = Batch(dfts)
+    for i, D in enumerate(Ds):
+        batch.set_density(i, D)
+    lib = batch.ctx.lib
+    stream = torch.cuda.Stream()
+    res = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        def one():
+            rc = lib.occ_xc_batch_compute(batch.ctx.h, batch.h, prec,
+                                          C.c_void_p(stream.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(batch.ctx.error())
+        for _ in range(warmup):
+            one()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record(stream)
+        for i in range(steps):
+            one()
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        batch.check(C.c_void_p(stream.cuda_stream))
+        per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+        ms = float(np.median(per))
+        res[name] = np.array([batch.result(i)[1] for i in range(nclusters)])
+        out[name] = {"builds_per_s": nclusters / (ms / 1e3), "points_per_s": npts / (ms / 1e3),
+                     "ms_per_batch": ms}
+    de = np.abs(res["mixed"] - res["fp64"])
+    out["max_abs_dE_xc"] = float(de.max())
+    out["max_abs_dE_xc_per_atom"] = float(np.max(de / (3 * sizes)))
+    return out
+
+
+def serve_stream(precision, nreq=32, rate=10.0, seed=0, budget=150e9, sessions=None):
+    """One pass of the seeded request stream through a server.  `sessions`
+    (basis, D0, iterations) may be passed in to reuse the host inputs."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, nreq)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    if sessions is None:
+        sessions = []
+        for i in range(nreq):
+            n = int(rng.integers(2, 49))
+            mol = wl.water_cluster(n, box=10.0 * (n / 32.0) ** (1.0 / 3.0), seed=seed + 100 + i)
+            b = wl.basis_for(mol, "def2-svp")
+            sessions.append((b, wl.random_density(b.nbf(), 5 * n, seed=seed + 300 + i),
+                             int(rng.integers(8, 21))))
+    srv = Server(precision=precision, hbm_budget_bytes=budget)
+    try:
+        t0 = time.perf_counter()
+        sids = [srv.open("pbe", b) for b, _, _ in sessions]
+        open_s = time.perf_counter() - t0
+        state = {}  # request -> [iteration, ticket, D]
+        done_req, nxt, builds = 0, 0, 0
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        while done_req < nreq:
+            now = time.perf_counter() - t0
+            while nxt < nreq and arrivals[nxt] <= now:
+                b, D0, _ = sessions[nxt]
+                state[nxt] = [0, srv.submit(sids[nxt], D0), D0]
+                h2d += D0.size * 8
+                nxt += 1
+            progressed = False
+            for r in list(state):
+                it, ticket, D = state[r]
+                res = srv.poll(ticket)
+                if res is None:
+                    continue
+                progressed = True
+                builds += 1
+                d2h += res[0].size * 8 + 16
+                if it + 1 < sessions[r][2]:
+                    Dn = wl.perturbed(D, 1e-3, seed + 10000 * r + it + 1)
+                    state[r] = [it + 1, srv.submit(sids[r], Dn), Dn]
+                    h2d += Dn.size * 8
+                else:
+                    srv.close(sids[r])
+                    del state[r]
+                    done_req += 1
+            if not progressed:
+                time.sleep(0.0002)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    finally:
+        srv.shutdown()
+    return {"builds": builds, "wall_s": wall, "builds_per_s": builds / wall,
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+            "mean_batch": st["mean_batch"], "ticks": st["ticks"], "failed": st["failed"],
+            "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9, "host_open_s": open_s,
+            "h2d_bytes_per_build": h2d / max(builds, 1),
+            "d2h_bytes_per_build": d2h / max(builds, 1)}, sessions
+
+
+def stream(nreq=32, rate=10.0, seed=0):
+    out = {"workload": f"stream{nreq}_poisson{rate:g}_n2to48_def2svp_pbe", "requests": nreq,
+           "rate_per_s": rate, "budget_gb": 150}
+    m, sessions = serve_stream(MIXED, nreq, rate, seed)
+    out["mixed"] = m
+    f, _ = serve_stream(FP64, nreq, rate, seed, sessions=sessions)
+    out["fp64"] = f
+    return out

@@ -268,3 +268,33 @@ extern "C" int occ_xc_molecule_autotune(occ_xc_context *ctx, occ_xc_molecule *mo
     return OCC_XC_ERR_INTERNAL;
   }
 }
+
+extern "C" int occ_xc_molecule_apply_tuning(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                            const occ_xc_tune_result *t) {
+  if (!ctx || !mol || !t || (t->vxc_tile_n != 64 && t->vxc_tile_n != 128 && t->vxc_tile_n != 256) ||
+      t->persistent_ctas < 0)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  try {
+    cuda_check(cudaSetDevice(ctx->impl->device), "cudaSetDevice");
+    Molecule &M = *mol->impl;
+    Candidate c;
+    c.bs = M.bs;
+    c.bs.leaf_target = t->leaf_target;
+    c.bs.leaf_min = t->leaf_min;
+    c.bs.leaf_max = t->leaf_max;
+    c.vxc_n = t->vxc_tile_n;
+    c.ctas = t->persistent_ctas;
+    apply(M, c);
+    return OCC_XC_OK;
+  } catch (const ArgError &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_ARG;
+  } catch (const CudaError &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_CUDA;
+  } catch (const std::exception &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_INTERNAL;
+  }
+}

@@ -8,6 +8,8 @@ alkane(n)               n-CnH(2n+2), all-anti, C-C 1.54, C-H 1.09 Angstrom,
                         tetrahedral angles
 random_density(nbf, k)  mo.D = C_occ C_occ^T with C_occ the first k columns
                         of a seeded random orthonormal nbf x nbf matrix
+perturbed(D, norm, s)   D plus seeded symmetric noise of Frobenius norm `norm`
+                        (a stand-in for the density change of one SCF iteration)
 """
 import numpy as np
 
@@ -98,3 +100,10 @@ def basis_for(mol, name, pure=True):
     b = AOBasis.load(mol.atoms(), name)
     b.set_pure(pure)
     return b
+
+
+def perturbed(D, norm, seed):
+    rng = np.random.default_rng(seed)
+    E = rng.standard_normal(D.shape)
+    E = E + E.T
+    return D + E * (norm / np.linalg.norm(E))

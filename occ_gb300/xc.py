@@ -140,6 +140,7 @@ def library():
     lib.occ_xc_molecule_set_build_settings.argtypes = [_vp, _vp, C.POINTER(_BuildSettings)]
     lib.occ_xc_molecule_autotune.argtypes = [_vp, _vp, C.c_int, _dp, C.c_double, C.c_int,
                                              C.POINTER(_TuneResult)]
+    lib.occ_xc_molecule_apply_tuning.argtypes = [_vp, _vp, C.POINTER(_TuneResult)]
     lib.occ_xc_batch_set_density.argtypes = [_vp, _vp, C.c_int, _dp]
     lib.occ_xc_batch_get_result.argtypes = [_vp, _vp, C.c_int, _dp, _dp]
     _LIB = lib
@@ -398,6 +399,13 @@ class DFT:
             raise XCError(f"occ_xc_molecule_autotune failed ({rc}): {self.ctx.error()}", rc)
         return {f: getattr(r, f) for f, _ in _TuneResult._fields_}
 
+    def apply_tuning(self, tuning):
+        """Apply an autotune() result (e.g. of a molecule of the same size)."""
+        r = _TuneResult(**{f: tuning[f] for f, _ in _TuneResult._fields_})
+        rc = self.ctx.lib.occ_xc_molecule_apply_tuning(self.ctx.h, self.h, C.byref(r))
+        if rc != 0:
+            raise XCError(f"occ_xc_molecule_apply_tuning failed ({rc}): {self.ctx.error()}", rc)
+
     def exchange_correlation_energy(self):
         return self._exc
 
@@ -506,7 +514,8 @@ class Graph:
         self._keep = keep
 
     def launch(self, stream=None):
-        rc = self.ctx.lib.occ_xc_graph_launch(self.h, stream)
+        """stream: a cudaStream_t handle (int) or None for the context's."""
+        rc = self.ctx.lib.occ_xc_graph_launch(self.h, C.c_void_p(stream) if stream else None)
         if rc != 0:
             raise XCError(f"occ_xc_graph_launch failed ({rc})")
 
