@@ -17,13 +17,17 @@
 //                  segments of <= 512), epilogue rho = rowsum(phi o X),
 //                  grad rho = 2 rowsum(grad phi o X)   (src/gto/density.cpp:33-43)
 //   k_func         FP64 functional per leaf (shared with the FP64 path)
-//   k_vxc_mixed    K = phi^T Y (M = 128 AOs, N <= 256, K = 128 points),
-//                  Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi,
-//                  V += K + K^T with FP64 atomics   (src/dft/xc_potential_matrix.cpp:19-41)
+//   k_ymix         Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi per block
+//   k_vxc_tma      K = phi^T Y (M = 128 AOs, N <= 256, K = the points of up to
+//                  two blocks of a leaf), operands by TMA, V += K + K^T with
+//                  FP64 atomics   (src/dft/xc_potential_matrix.cpp:19-41)
 //   k_reduce       fixed-order FP64 sum of the per-leaf partials
 #include <algorithm>
 #include <cstring>
 #include <type_traits>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "../../include/occ_xc.h"
 #include "host/gto_eval.h"
@@ -106,11 +110,14 @@ struct MBlock {
   int lblock;       // index of the block within its molecule (row scales)
   long long ws_off; // float offset of the block's [4][mp][128] planes in the molecule's ws
 };
+// A V_xc work item: AO rows i0 .. i0 + 127 of nblk consecutive blocks of one
+// leaf (index block0 into the launch's block list); K runs over all their points.
 struct VItem {
-  int block, i0; // block (index into the launch's block list) and first AO row of the tile
+  int block0, nblk, i0;
 };
+// A leaf of the functional stage and its blocks (block0 .. block0 + nblk - 1).
 struct LeafItem {
-  int mol, leaf;
+  int mol, leaf, block0, nblk;
 };
 
 // Everything the mixed kernels need of one molecule; a launch covers a table
@@ -127,9 +134,10 @@ struct MixTab {
   float *colb;          // column bounds of D2
   double *rho, *coef, *epart;
   const double *D;      // this build's density (mo.D)
-  double *V;            // V_xc (upper triangle, then mirrored)
+  double *V;            // V_xc (A with V = A + A^T, then symmetrised)
   double *out2;         // {E_xc, integrated density}
   int vxc_n;            // N of the V_xc tile (64, 128 or 256)
+  long long ws_row0;    // row of ws in the launch's tensor map (rows of 128 floats)
 };
 
 // Per-launch replacement of a one-molecule table's D / V / out2 (so that a
@@ -556,7 +564,7 @@ __global__ void __launch_bounds__(256) k_prep_density(const MixTab *__restrict__
                                                       Override ov, int *queue) {
   __shared__ float red[256];
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 2)
-    queue[threadIdx.x] = 0; // work queues of k_rho_mixed and k_vxc_mixed
+    queue[threadIdx.x] = 0; // work queues of k_rho_mixed and k_vxc_tma
   const MixTab &T = tabs[blockIdx.y];
   const int nbf = T.m.nbf;
   const int j = blockIdx.x;
@@ -586,18 +594,24 @@ __global__ void __launch_bounds__(256) k_prep_density(const MixTab *__restrict__
     colb[j] = pow2_bound(red[0]);
 }
 
-// V holds only its upper triangle (row <= column) after the mixed build;
-// copy it to the lower one (the final FP64 symmetrisation).  Grid: (x, molecules).
-__global__ void __launch_bounds__(256) k_mirror_upper(const MixTab *__restrict__ tabs,
-                                                      Override ov) {
+// V holds A after the contractions, with V_xc = A + A^T: the final FP64
+// symmetrisation, each unordered pair (r, c) read and written by one thread.
+// Grid: (x, molecules).
+__global__ void __launch_bounds__(256) k_symmetrize(const MixTab *__restrict__ tabs,
+                                                    Override ov) {
   const MixTab &T = tabs[blockIdx.y];
   double *__restrict__ V = t_V(T, ov);
   const size_t n = static_cast<size_t>(T.m.nbf);
   for (size_t q = static_cast<size_t>(blockIdx.x) * 256 + threadIdx.x; q < n * n;
        q += static_cast<size_t>(gridDim.x) * 256) {
     const size_t c = q / n, r = q % n; // element (r, c), column-major
-    if (r > c)
-      V[q] = V[r * n + c];
+    if (r < c) {
+      const double v = V[q] + V[r * n + c];
+      V[q] = v;
+      V[r * n + c] = v;
+    } else if (r == c) {
+      V[q] = 2.0 * V[q];
+    }
   }
 }
 
@@ -738,138 +752,312 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(const MixTab *__restrict__
   pipe_finish(P);
 }
 
-// K = phi^T Y for one 128-row AO tile of one block; V += K + K^T (FP64).
-// Persistent over the item list (most expensive first), like k_rho_mixed.
-template <bool DERIV>
-__global__ void __launch_bounds__(256, 1) k_vxc_mixed(const MixTab *__restrict__ tabs,
-                                                      const MBlock *__restrict__ blocks,
-                                                      const VItem *__restrict__ items, int nitems,
-                                                      Override ov, int *queue, int *err) {
+// ---- V_xc: K = phi^T Y on tcgen05, operands staged by TMA ------------------
+// One CTA per SM, persistent over V items (AO rows i0 .. i0 + 127 of the
+// blocks of one leaf; K = their points) fetched from a global queue and
+// handed to the roles through a ring in shared memory:
+//   warp 4       TMA producer: per K chunk of 32 points, hi and lo of the A
+//                rows (phi) and of the B rows (Y), pre-split by k_ymix, as
+//                32 x 32 FP32 boxes with the 128-byte swizzle
+//   warp 5       MMA issuer: hi*hi + hi*lo + lo*hi ("3xTF32") into one of two
+//                TMEM accumulators of 256 columns; for a leaf with at most
+//                128 AOs also K^T (A and B swapped) beside it
+//   warps 0-3    epilogue: TMEM -> FP64 atomics, coalesced along the rows,
+//                into A with V_xc = A + A^T (K + K^T summed in registers and
+//                added once per pair when K^T was formed)
+// Stages and accumulators are double-buffered, so loads, MMAs and atomics of
+// consecutive chunks and passes overlap.  Every wait is bounded; on expiry
+// the error flag is set and all roles leave.
+constexpr int kItemBlocks = 2;   // blocks of a leaf accumulated in one V item
+constexpr int kRing = 4;         // depth of the work-item ring
+constexpr int kVxcEpi = 128;     // epilogue threads (warps 0-3)
+constexpr int kVxcThreads = 192; // + producer warp + MMA warp
+constexpr int kVxcMap = 2048;    // AO maps up to this size are staged in shared memory
+
+struct alignas(16) VxcSmem {
+  uint64_t full[2], empty[2];   // per stage: TMA landed, MMAs done
+  uint64_t tfull[2], tempty[2]; // per accumulator: ready, drained
+  uint64_t ifull[kRing], iempty[kRing];
+  uint64_t done;                // the MMA thread's final commit
+  uint32_t tmem_slot;
+  int ring[kRing];
+  int gmap[kVxcMap];            // the epilogue's current AO map
+};
+constexpr uint32_t kVxcSmem = 2 * kStageBytes + sizeof(VxcSmem) + 1024;
+
+struct VxcWork { // what every role derives from an item
+  int mp, rows_a, nblk, i0, nbf_leaf;
+  bool sym;
+};
+__device__ __forceinline__ VxcWork vxc_work(const MixTab *tabs, const MBlock *blocks,
+                                            const VItem &it) {
+  const MBlock B = blocks[it.block0];
+  VxcWork w;
+  w.mp = B.mp;
+  w.nblk = it.nblk;
+  w.i0 = it.i0;
+  w.rows_a = min(128, B.mp - it.i0); // a multiple of 32
+  w.nbf_leaf = tabs[B.mol].m.leaves[B.leaf].nbf;
+  w.sym = B.mp <= 128;
+  return w;
+}
+
+__device__ __forceinline__ void epi_bar() { // the 128 epilogue threads
+  asm volatile("bar.sync 1, 128;" ::: "memory");
+}
+// AND of v over the 128 epilogue threads (a barrier among them as well).
+__device__ __forceinline__ bool epi_all(bool v) {
+  uint32_t r;
+  asm volatile("{\n\t.reg .pred p, q;\n\t"
+               "setp.ne.u32 p, %1, 0;\n\t"
+               "barrier.red.and.pred q, 1, 128, p;\n\t"
+               "selp.u32 %0, 1, 0, q;\n\t}"
+               : "=r"(r)
+               : "r"(static_cast<uint32_t>(v))
+               : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(kVxcThreads, 1)
+    k_vxc_tma(const MixTab *__restrict__ tabs, const MBlock *__restrict__ blocks,
+              const VItem *__restrict__ items, int nitems, Override ov, int *queue, int *err,
+              const __grid_constant__ CUtensorMap tmap) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
-  SmemTail *tail = reinterpret_cast<SmemTail *>(smem + kSmemMain);
+  VxcSmem *sm = reinterpret_cast<VxcSmem *>(smem + 2 * kStageBytes);
+  uint8_t *stage[2] = {smem, smem + kStageBytes};
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int quad = warp & 3, half = warp >> 2;
-  Pipe P;
-  pipe_init(P, smem, tail->bars, &tail->tmem_slot, kMaxN);
-  for (;;) {
-  if (t == 0)
-    tail->next = atomicAdd(&queue[1], 1);
-  __syncthreads();
-  const int ii = tail->next;
-  if (ii >= nitems)
-    break;
-  const VItem it = items[ii];
-  const MBlock B = blocks[it.block];
-  const MixTab &T = tabs[B.mol];
-  const MolDev &m = T.m;
-  const DevLeaf L = m.leaves[B.leaf];
-  const int *g = m.leaf_ao + L.ao_begin;
-  const float *phi = T.ws + B.ws_off;
-  const double *__restrict__ coef = T.coef;
-  double *__restrict__ V = t_V(T, ov);
-  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
-  const size_t nbf = static_cast<size_t>(m.nbf);
-  const size_t Np = static_cast<size_t>(m.npts);
-  // the block's functional coefficients (0 beyond its points)
-  for (int q = t; q < 4 * kBlockPts; q += blockDim.x) {
-    const int c = q / kBlockPts, pp = q % kBlockPts;
-    float v = 0.f;
-    if (pp < B.cnt && (DERIV || c == 0))
-      v = static_cast<float>(coef[c * Np + L.off + B.p0 + pp]);
-    tail->coef[c][pp] = v;
+  if (t == 0) {
+    for (int s = 0; s < 2; s++) {
+      umma::mbar_init(&sm->full[s], 1);
+      umma::mbar_init(&sm->empty[s], 1);
+      umma::mbar_init(&sm->tfull[s], 1);
+      umma::mbar_init(&sm->tempty[s], kVxcEpi);
+    }
+    for (int r = 0; r < kRing; r++) {
+      umma::mbar_init(&sm->ifull[r], 1);
+      umma::mbar_init(&sm->iempty[r], 1 + kVxcEpi);
+    }
+    umma::mbar_init(&sm->done, 1);
+    umma::fence_proxy_async();
+    umma::tma_prefetch_desc(&tmap);
   }
+  if (warp == 0)
+    umma::tmem_alloc(&sm->tmem_slot, 512);
+  umma::fence_before_sync();
   __syncthreads();
-  const int rows = min(128, B.mp - it.i0);
-  const int NT = T.vxc_n; // tile N (a multiple of 32, at most kMaxN)
-  for (int n0 = 0; n0 < B.mp; n0 += NT) {
-    const int N = min(NT, B.mp - n0);
-    auto fa = [&](int c, uint8_t *st) {
-      const int r = t & 127, kh = t >> 7;
-      const bool rv = r < rows;
-      const float *src = phi + static_cast<size_t>(it.i0 + (rv ? r : 0)) * kBlockPts + c * kKc +
-                         kh * 16;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        float4 v = rv ? *reinterpret_cast<const float4 *>(src + 4 * q) : make_float4(0, 0, 0, 0);
-        store4(st + kOffAhi, st + kOffAlo, r, kh * 4 + q, v.x, v.y, v.z, v.w);
-      }
-    };
-    // all threads: (row j, 16-byte chunk q) pairs of the N x 32 B tile
-    auto fb = [&](int c, uint8_t *st) {
-      for (int idx = t; idx < N * 8; idx += 256) {
-        const int j = idx >> 3, q = idx & 7;
-        const size_t row = static_cast<size_t>(n0 + j) * kBlockPts + c * kKc;
-        const int pp = c * kKc + q * 4;
-        float4 a = *reinterpret_cast<const float4 *>(phi + row + 4 * q);
-        float y[4] = {a.x * tail->coef[0][pp], a.y * tail->coef[0][pp + 1],
-                      a.z * tail->coef[0][pp + 2], a.w * tail->coef[0][pp + 3]};
-        if (DERIV) {
-#pragma unroll
-          for (int d = 1; d < 4; d++) {
-            float4 gd = *reinterpret_cast<const float4 *>(phi + d * plane + row + 4 * q);
-            y[0] = fmaf(gd.x, tail->coef[d][pp], y[0]);
-            y[1] = fmaf(gd.y, tail->coef[d][pp + 1], y[1]);
-            y[2] = fmaf(gd.z, tail->coef[d][pp + 2], y[2]);
-            y[3] = fmaf(gd.w, tail->coef[d][pp + 3], y[3]);
+  umma::fence_after_sync();
+  const uint32_t tmem = sm->tmem_slot;
+  bool ok = true;
+  auto wait = [&](uint64_t *bar, uint32_t parity) {
+    if (ok && !umma::mbar_wait(bar, parity, kWaitIter)) {
+      ok = false;
+      atomicExch(err, kErrTimeout);
+    }
+    return ok;
+  };
+  // the epilogue warps issue warp-collective TMEM loads and share barriers:
+  // all 128 of their threads take every decision to stop together
+  const bool epi = warp < 4;
+  auto agree = [&] {
+    if (epi)
+      ok = epi_all(ok);
+    return ok;
+  };
+  // consumer side of the item ring: next item index or -1
+  auto next_item = [&](int k) {
+    const int slot = k % kRing;
+    wait(&sm->ifull[slot], (k / kRing) & 1);
+    if (!agree())
+      return -1;
+    const int it = sm->ring[slot];
+    umma::mbar_arrive(&sm->iempty[slot]);
+    return it;
+  };
+
+  if (warp == 4) {
+    // ---- TMA producer (lane 0) ----
+    if (lane == 0) {
+      uint32_t g = 0; // chunks issued
+      for (int k = 0;; k++) {
+        const int slot = k % kRing;
+        if (k >= kRing && !wait(&sm->iempty[slot], ((k / kRing) - 1) & 1))
+          break;
+        int it = atomicAdd(&queue[1], 1);
+        if (it >= nitems)
+          it = -1;
+        sm->ring[slot] = it;
+        umma::mbar_arrive(&sm->ifull[slot]);
+        if (it < 0)
+          break;
+        const VItem I = items[it];
+        const VxcWork W = vxc_work(tabs, blocks, I);
+        const MixTab &T = tabs[blocks[I.block0].mol];
+        const int NT = W.sym ? W.mp : T.vxc_n;
+        for (int n0 = 0; n0 < W.mp && ok; n0 += NT) {
+          const int N = min(NT, W.mp - n0);
+          for (int b = 0; b < W.nblk && ok; b++) {
+            const MBlock Bb = blocks[I.block0 + b];
+            const int r0 = static_cast<int>(T.ws_row0 + Bb.ws_off / kBlockPts);
+            const int mp = W.mp;
+            for (int c = 0; c < kBlockPts / kKc; c++, g++) {
+              const int s = g & 1;
+              if (g >= 2 && !wait(&sm->empty[s], ((g >> 1) - 1) & 1))
+                break;
+              umma::mbar_arrive_expect_tx(&sm->full[s],
+                                          static_cast<uint32_t>(W.rows_a + N) * 256u);
+              uint8_t *st = stage[s];
+              for (int r = 0; r < W.rows_a; r += 32) {
+                umma::tma_load_2d(st + kOffAhi + r * 128, &tmap, c * kKc, r0 + W.i0 + r,
+                                  &sm->full[s]);
+                umma::tma_load_2d(st + kOffAlo + r * 128, &tmap, c * kKc,
+                                  r0 + 3 * mp + W.i0 + r, &sm->full[s]);
+              }
+              for (int r = 0; r < N; r += 32) {
+                umma::tma_load_2d(st + kOffBhi + r * 128, &tmap, c * kKc, r0 + mp + n0 + r,
+                                  &sm->full[s]);
+                umma::tma_load_2d(st + kOffBlo + r * 128, &tmap, c * kKc,
+                                  r0 + 2 * mp + n0 + r, &sm->full[s]);
+              }
+            }
           }
         }
-        store4(st + kOffBhi, st + kOffBlo, j, q, y[0], y[1], y[2], y[3]);
+        if (!ok)
+          break;
       }
-    };
-    gemm_pass<false>(P, N, kBlockPts / kKc, fa, fb, err);
-    // epilogue: rows = AOs it.i0 + quad*32 + lane, this warp's half of N.
-    // V receives its upper triangle only (the AO map is ascending, so local
-    // order is global order); k_mirror_upper completes it.
-    const int li = it.i0 + quad * 32 + lane;
-    const bool iv = li < L.nbf;
-    const size_t gi = iv ? static_cast<size_t>(g[li]) : 0;
-    const int cols = N / 2;
-    const bool whole = (B.mp <= 128); // K of the block fits one tile: symmetrise here
-    float *kt = reinterpret_cast<float *>(P.stage[0]); // [128][129] after the GEMM
-    for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
-      uint32_t r[16];
-      umma::tmem_ld16(P.tmem + (static_cast<uint32_t>(quad * 32) << 16) + c0, r);
-      umma::tmem_wait_ld();
-      if (whole) {
+      // loads still in flight land before the CTA leaves
+      for (uint32_t q = (g >= 2 ? g - 2 : 0); q < g; q++)
+        umma::mbar_wait(&sm->full[q & 1], (q >> 1) & 1, kWaitIter);
+    }
+  } else if (warp == 5) {
+    // ---- MMA issuer (lane 0) ----
+    if (lane == 0) {
+      uint32_t g = 0, pc = 0; // chunks consumed, passes
+      bool issued = false;
+      for (int k = 0; ok; k++) {
+        const int it = next_item(k);
+        if (it < 0)
+          break;
+        const VItem I = items[it];
+        const VxcWork W = vxc_work(tabs, blocks, I);
+        const MixTab &T = tabs[blocks[I.block0].mol];
+        const int NT = W.sym ? W.mp : T.vxc_n;
+        for (int n0 = 0; n0 < W.mp && ok; n0 += NT, pc++) {
+          const int N = min(NT, W.mp - n0);
+          const uint32_t buf = pc & 1, ub = pc >> 1;
+          if (ub > 0 && !wait(&sm->tempty[buf], (ub - 1) & 1))
+            break;
+          umma::fence_after_sync();
+          const uint32_t d = tmem + buf * 256, dt = d + 128;
+          const uint32_t idesc = umma::idesc_tf32(128, N);
+          const int nch = W.nblk * (kBlockPts / kKc);
+          for (int c = 0; c < nch && ok; c++, g++) {
+            const int s = g & 1;
+            if (!wait(&sm->full[s], (g >> 1) & 1))
+              break;
+            umma::fence_after_sync();
+            const uint32_t base = umma::smem_u32(stage[s]);
 #pragma unroll
-        for (int i = 0; i < 16; i++)
-          kt[(quad * 32 + lane) * 129 + c0 + i] = __uint_as_float(r[i]);
-      } else if (iv) {
+            for (int kk = 0; kk < kKc / 8; kk++) {
+              const uint32_t o = kk * 32;
+              const uint64_t ahi = umma::desc_kmajor_sw128(base + kOffAhi + o);
+              const uint64_t alo = umma::desc_kmajor_sw128(base + kOffAlo + o);
+              const uint64_t bhi = umma::desc_kmajor_sw128(base + kOffBhi + o);
+              const uint64_t blo = umma::desc_kmajor_sw128(base + kOffBlo + o);
+              const uint32_t acc = (c == 0 && kk == 0) ? 0u : 1u;
+              umma::mma_tf32(d, alo, bhi, idesc, acc);
+              umma::mma_tf32(d, ahi, blo, idesc, 1u);
+              umma::mma_tf32(d, ahi, bhi, idesc, 1u);
+              if (W.sym) { // K^T: rows are the Y rows, columns the phi rows
+                umma::mma_tf32(dt, blo, ahi, idesc, acc);
+                umma::mma_tf32(dt, bhi, alo, idesc, 1u);
+                umma::mma_tf32(dt, bhi, ahi, idesc, 1u);
+              }
+            }
+            umma::commit(&sm->empty[s]);
+            issued = true;
+          }
+          umma::commit(&sm->tfull[buf]);
+        }
+      }
+      if (issued) { // every MMA done before TMEM is released
+        umma::commit(&sm->done);
+        umma::mbar_wait(&sm->done, 0, kWaitIter);
+      }
+    }
+  } else {
+    // ---- epilogue (warps 0-3) ----
+    const int quad = warp;
+    const int i = quad * 32 + lane; // row of the tile
+    uint32_t pc = 0;
+    for (int k = 0; ok; k++) {
+      const int it = next_item(k);
+      if (it < 0)
+        break;
+      const VItem I = items[it];
+      const VxcWork W = vxc_work(tabs, blocks, I);
+      const MBlock B0 = blocks[I.block0];
+      const MixTab &T = tabs[B0.mol];
+      const DevLeaf L = T.m.leaves[B0.leaf];
+      const int *gsrc = T.m.leaf_ao + L.ao_begin;
+      const bool gsh = W.nbf_leaf <= kVxcMap;
+      if (gsh) {
+        epi_bar(); // the previous item's map is no longer read
+        for (int q = t; q < W.nbf_leaf; q += kVxcEpi)
+          sm->gmap[q] = gsrc[q];
+        epi_bar();
+      }
+      const int *g = gsh ? sm->gmap : gsrc;
+      double *__restrict__ V = t_V(T, ov);
+      const size_t nbf = static_cast<size_t>(T.m.nbf);
+      const int NT = W.sym ? W.mp : T.vxc_n;
+      const int li = W.i0 + i;
+      const bool iv = li < W.nbf_leaf;
+      const size_t gi = iv ? static_cast<size_t>(g[li]) : 0;
+      for (int n0 = 0; n0 < W.mp && ok; n0 += NT, pc++) {
+        const int N = min(NT, W.mp - n0);
+        const uint32_t buf = pc & 1, ub = pc >> 1;
+        wait(&sm->tfull[buf], ub & 1);
+        if (!agree())
+          break;
+        umma::fence_after_sync();
+        const uint32_t lanebase = tmem + (static_cast<uint32_t>(quad * 32) << 16) + buf * 256;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+          uint32_t r[16], rt[16];
+          umma::tmem_ld16(lanebase + c0, r);
+          if (W.sym)
+            umma::tmem_ld16(lanebase + 128 + c0, rt);
+          umma::tmem_wait_ld();
+          if (!iv)
+            continue;
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
-          const int lj = n0 + c0 + i;
-          if (lj < L.nbf) {
+          for (int e = 0; e < 16; e++) {
+            const int lj = n0 + c0 + e;
+            if (lj >= W.nbf_leaf)
+              continue;
+            // V accumulates A with V_xc = A + A^T (k_symmetrize): K[i][j]
+            // goes to A[gi][gj], so a warp's lanes (consecutive rows i)
+            // update consecutive addresses of one column
             const size_t gj = static_cast<size_t>(g[lj]);
-            const double k = static_cast<double>(__uint_as_float(r[i]));
-            if (gi < gj)
-              atomicAdd(&V[gj * nbf + gi], k);
-            else if (gj < gi)
-              atomicAdd(&V[gi * nbf + gj], k);
-            else
-              atomicAdd(&V[gi * nbf + gi], 2.0 * k);
+            const double kv = static_cast<double>(__uint_as_float(r[e]));
+            if (!W.sym) {
+              atomicAdd(&V[gj * nbf + gi], kv);
+            } else if (lj > li) { // K[i][j] + K[j][i] once per unordered pair
+              atomicAdd(&V[gj * nbf + gi], kv + static_cast<double>(__uint_as_float(rt[e])));
+            } else if (lj == li) {
+              atomicAdd(&V[gi * nbf + gi], kv);
+            }
           }
         }
+        umma::fence_before_sync();
+        umma::mbar_arrive(&sm->tempty[buf]);
       }
     }
-    if (whole) {
-      __syncthreads();
-      // one atomic per unordered pair: V[a][b] += K[a][b] + K[b][a], a <= b
-      const int mm = L.nbf;
-      for (int idx = t; idx < mm * mm; idx += blockDim.x) {
-        const int a = idx / mm, b = idx - a * mm;
-        if (a > b)
-          continue;
-        const double k = static_cast<double>(kt[a * 129 + b]) +
-                         static_cast<double>(kt[b * 129 + a]);
-        atomicAdd(&V[static_cast<size_t>(g[b]) * nbf + g[a]], k);
-      }
-    }
-    umma::fence_before_sync();
-    __syncthreads();
   }
-  } // items
-  pipe_finish(P);
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0)
+    umma::tmem_dealloc(tmem, 512);
 }
 
 // Functional per leaf (one CTA per leaf item), the batched counterpart of the
@@ -897,6 +1085,77 @@ __global__ void __launch_bounds__(256) k_func_b(const MixTab *__restrict__ tabs,
   const MixTab &T = tabs[li.mol];
   leaf_functional<DERIV>(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts), T.fs,
                          T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
+}
+
+// Operands of k_vxc_tma for one block, pre-split for 3xTF32: with
+// Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi (FP32),
+// hi(x) = x rounded to the nearest TF32 and lo(x) = x - hi(x) rounded to the
+// nearest TF32 (both exact TF32 values, so the tensor core drops no bits and
+// the split error has no sign bias), the block's AO planes become
+//   plane 0: hi(phi)   plane 1: hi(Y)   plane 2: lo(Y)   plane 3: lo(phi)
+// (phi and grad phi are not needed after the density).  One CTA per block;
+// streams 4 planes in and out.
+__device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
+  uint32_t h, l;
+  umma::split_tf32(x, h, l);
+  hi = __uint_as_float(h);
+  lo = __uint_as_float(l);
+}
+template <bool DERIV>
+__global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
+                                              const MBlock *__restrict__ blocks) {
+  __shared__ float4 cf[kBlockPts]; // (c0, c1, c2, c3) per point
+  const MBlock B = blocks[blockIdx.x];
+  const MixTab &T = tabs[B.mol];
+  if (threadIdx.x < kBlockPts) {
+    const int p = threadIdx.x;
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (p < B.cnt) {
+      const size_t N = static_cast<size_t>(T.m.npts);
+      const size_t idx = static_cast<size_t>(T.m.leaves[B.leaf].off) + B.p0 + p;
+      c.x = static_cast<float>(T.coef[idx]);
+      if (DERIV) {
+        c.y = static_cast<float>(T.coef[N + idx]);
+        c.z = static_cast<float>(T.coef[2 * N + idx]);
+        c.w = static_cast<float>(T.coef[3 * N + idx]);
+      }
+    }
+    cf[p] = c;
+  }
+  __syncthreads();
+  float4 *__restrict__ base = reinterpret_cast<float4 *>(T.ws + B.ws_off);
+  const size_t plane = static_cast<size_t>(B.mp) * (kBlockPts / 4); // in float4
+  const int n4 = B.mp * (kBlockPts / 4);
+  auto split4 = [](float4 v, float4 &h, float4 &l) {
+    tf32_split(v.x, h.x, l.x);
+    tf32_split(v.y, h.y, l.y);
+    tf32_split(v.z, h.z, l.z);
+    tf32_split(v.w, h.w, l.w);
+  };
+#pragma unroll 2
+  for (int q = threadIdx.x; q < n4; q += blockDim.x) {
+    const int p = (q % (kBlockPts / 4)) * 4;
+    const float4 a = base[q];
+    float4 y;
+    y.x = a.x * cf[p].x;
+    y.y = a.y * cf[p + 1].x;
+    y.z = a.z * cf[p + 2].x;
+    y.w = a.w * cf[p + 3].x;
+    if (DERIV) {
+      const float4 gx = base[plane + q], gy = base[2 * plane + q], gz = base[3 * plane + q];
+      y.x = fmaf(gz.x, cf[p].w, fmaf(gy.x, cf[p].z, fmaf(gx.x, cf[p].y, y.x)));
+      y.y = fmaf(gz.y, cf[p + 1].w, fmaf(gy.y, cf[p + 1].z, fmaf(gx.y, cf[p + 1].y, y.y)));
+      y.z = fmaf(gz.z, cf[p + 2].w, fmaf(gy.z, cf[p + 2].z, fmaf(gx.z, cf[p + 2].y, y.z)));
+      y.w = fmaf(gz.w, cf[p + 3].w, fmaf(gy.w, cf[p + 3].z, fmaf(gx.w, cf[p + 3].y, y.w)));
+    }
+    float4 ah, al, yh, yl;
+    split4(a, ah, al);
+    split4(y, yh, yl);
+    base[q] = ah;
+    base[plane + q] = yh;
+    base[2 * plane + q] = yl;
+    base[3 * plane + q] = al;
+  }
 }
 
 // Fixed-order FP64 sums of the per-leaf partials, one CTA per molecule.
@@ -1013,10 +1272,8 @@ void set_smem_attributes() {
                                   kSmemTotal), "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_rho_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kSmemTotal), "cudaFuncSetAttribute");
-  cuda_check(cudaFuncSetAttribute(k_vxc_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kSmemTotal), "cudaFuncSetAttribute");
-  cuda_check(cudaFuncSetAttribute(k_vxc_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kSmemTotal), "cudaFuncSetAttribute");
+  cuda_check(cudaFuncSetAttribute(k_vxc_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kVxcSmem), "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_selftest_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kSmemTotal), "cudaFuncSetAttribute");
 }
@@ -1038,6 +1295,7 @@ struct LaunchPlan {
   LeafItem *d_litems = nullptr;
   MixTab *d_tabs = nullptr;
   int maxnbf = 0, deriv = 0;
+  CUtensorMap tmap;       // the workspace as rows of 128 floats (k_vxc_tma)
   std::vector<void *> owned;
   ~LaunchPlan() {
     for (void *p : owned)
@@ -1070,7 +1328,7 @@ WsLayout ws_layout(const Molecule &M) {
   size_t off = 0;
   auto put = [&](size_t bytes) {
     const size_t o = off;
-    off = (off + std::max<size_t>(bytes, 16) + 255) / 256 * 256;
+    off = (off + std::max<size_t>(bytes, 16) + 511) / 512 * 512; // whole tensor-map rows
     return o;
   };
   const size_t nbf = static_cast<size_t>(M.basis.nbf);
@@ -1088,10 +1346,13 @@ WsLayout ws_layout(const Molecule &M) {
   L.total = off;
   return L;
 }
-MixTab bind_ws(const Molecule &M, char *base) {
+// The molecule's workspace at `base` inside a region that starts at map_base
+// (the region the launch's tensor map covers).
+MixTab bind_ws(const Molecule &M, char *base, const char *map_base) {
   const WsLayout L = ws_layout(M);
   MixTab T = M.mixed->tab;
   T.ws = reinterpret_cast<float *>(base + L.ws);
+  T.ws_row0 = static_cast<long long>((base + L.ws) - map_base) / (kBlockPts * sizeof(float));
   T.rowscale = reinterpret_cast<float *>(base + L.rowscale);
   T.dhl = reinterpret_cast<float2 *>(base + L.dhl);
   T.colb = reinterpret_cast<float *>(base + L.colb);
@@ -1127,14 +1388,24 @@ void make_plan_lists(LaunchPlan &P, const std::vector<Molecule *> &mols,
     for (const MBlock &b0 : M.mixed->blocks) {
       MBlock b = b0;
       b.mol = static_cast<int>(mi);
-      const int bi = static_cast<int>(P.blocks.size());
-      for (int i0 = 0; i0 < b.mp; i0 += 128)
-        items.push_back({bi, i0});
       P.blocks.push_back(b);
     }
-    (void)base;
-    for (size_t l = 0; l < M.leaves.size(); l++)
-      P.litems.push_back({static_cast<int>(mi), static_cast<int>(l)});
+    // the blocks of a leaf are consecutive: V items over groups of up to
+    // kItemBlocks of them, one leaf item over all of them
+    const std::vector<MBlock> &mb = M.mixed->blocks;
+    for (size_t b = 0; b < mb.size();) {
+      size_t e = b;
+      while (e < mb.size() && mb[e].leaf == mb[b].leaf)
+        e++;
+      P.litems.push_back({static_cast<int>(mi), mb[b].leaf, base + static_cast<int>(b),
+                          static_cast<int>(e - b)});
+      for (size_t g = b; g < e; g += kItemBlocks) {
+        const int nb = static_cast<int>(std::min<size_t>(kItemBlocks, e - g));
+        for (int i0 = 0; i0 < mb[b].mp; i0 += 128)
+          items.push_back({base + static_cast<int>(g), nb, i0});
+      }
+      b = e;
+    }
   }
   // interleave (CTAs running together then work on distant parts of the
   // Morton order and touch different V elements), then order by decreasing
@@ -1145,8 +1416,8 @@ void make_plan_lists(LaunchPlan &P, const std::vector<Molecule *> &mols,
       if (q * stride + r < n)
         P.items.push_back(items[q * stride + r]);
   auto vcost = [&](const VItem &v) {
-    const MBlock &b = P.blocks[v.block];
-    return static_cast<long>(std::min(128, b.mp - v.i0)) * b.mp;
+    const MBlock &b = P.blocks[v.block0];
+    return static_cast<long>(std::min(128, b.mp - v.i0)) * b.mp * v.nblk;
   };
   std::stable_sort(P.items.begin(), P.items.end(),
                    [&](const VItem &a, const VItem &b) { return vcost(a) > vcost(b); });
@@ -1177,7 +1448,7 @@ int num_sms(int device) {
   return n;
 }
 
-// The mixed launch sequence of a plan (7 kernels whatever the molecule count).
+// The mixed launch sequence of a plan (8 kernels whatever the molecule count).
 void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st, int max_ctas) {
   const int nmol = static_cast<int>(P.tabs.size());
   const int nb = static_cast<int>(P.blocks.size());
@@ -1208,20 +1479,23 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
       else
         k_func_b<false><<<nl, 256, 0, st>>>(P.d_tabs, P.d_litems);
     });
+  if (nb > 0)
+    c.launch("ymix", st, [&] {
+      if (P.deriv)
+        k_ymix<true><<<nb, 256, 0, st>>>(P.d_tabs, P.d_blocks);
+      else
+        k_ymix<false><<<nb, 256, 0, st>>>(P.d_tabs, P.d_blocks);
+    });
   if (ni > 0)
     c.launch("vxc_mixed", st, [&] {
       const int g = std::min(ni, ctas);
-      if (P.deriv)
-        k_vxc_mixed<true><<<g, 256, kSmemTotal, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov,
-                                                      P.d_queue, err);
-      else
-        k_vxc_mixed<false><<<g, 256, kSmemTotal, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov,
-                                                       P.d_queue, err);
+      k_vxc_tma<<<g, kVxcThreads, kVxcSmem, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov, P.d_queue, err,
+                                          P.tmap);
     });
-  c.launch("mirror", st, [&] {
+  c.launch("symmetrize", st, [&] {
     const size_t n2 = static_cast<size_t>(P.maxnbf) * P.maxnbf;
     const int gx = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
-    k_mirror_upper<<<dim3(gx, nmol), 256, 0, st>>>(P.d_tabs, ov);
+    k_symmetrize<<<dim3(gx, nmol), 256, 0, st>>>(P.d_tabs, ov);
   });
   c.launch("reduce", st, [&] { k_reduce_b<<<nmol, 256, 0, st>>>(P.d_tabs, ov); });
   cuda_check(cudaGetLastError(), "kernel launch");
@@ -1302,13 +1576,42 @@ void Molecule::prepare_mixed() {
 
 size_t Molecule::mixed_workspace_bytes() const { return ws_layout(*this).total; }
 
+// Tensor map of a workspace region: rows of 128 FP32 (512 bytes), boxes of
+// 32 x 32 with the 128-byte swizzle that the UMMA descriptors expect.
+void encode_ws_map(CUtensorMap &map, const void *base, size_t bytes) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cuda_check(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                cudaEnableDefault, &q),
+               "cudaGetDriverEntryPointByVersion");
+    if (q != cudaDriverEntryPointSuccess || !fn)
+      throw CudaError("cuTensorMapEncodeTiled is not available from the driver");
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t rows = std::max<cuuint64_t>(bytes / (kBlockPts * sizeof(float)), 1);
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(kBlockPts), rows};
+  const cuuint64_t strides[1] = {kBlockPts * sizeof(float)};
+  const cuuint32_t box[2] = {static_cast<cuuint32_t>(kKc), 32u};
+  const cuuint32_t estr[2] = {1u, 1u};
+  const CUresult r = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base),
+                            dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    throw CudaError("cuTensorMapEncodeTiled failed (" + std::to_string(static_cast<int>(r)) + ")");
+}
+
 void Molecule::ensure_mixed_ws() {
   MixedState *S = mixed;
   if (S->d_private)
     return;
-  S->d_private = static_cast<char *>(alloc(ws_layout(*this).total));
+  const size_t bytes = ws_layout(*this).total;
+  S->d_private = static_cast<char *>(alloc(bytes));
   auto P = std::make_unique<LaunchPlan>();
-  make_plan(*P, {this}, {bind_ws(*this, S->d_private)});
+  make_plan(*P, {this}, {bind_ws(*this, S->d_private, S->d_private)});
+  encode_ws_map(P->tmap, S->d_private, bytes);
   S->single = std::move(P);
 }
 
@@ -1363,9 +1666,12 @@ void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListAren
         throw ArgError("a molecule may appear only once in a group build");
     const int g = mols[i]->deriv ? 1 : 0;
     group[g].push_back(mols[i]);
-    tabs[g].push_back(bind_ws(*mols[i], d_ws + wsoff));
+    tabs[g].push_back(bind_ws(*mols[i], d_ws + wsoff, d_ws));
     wsoff += mols[i]->mixed_workspace_bytes();
   }
+  for (int g = 0; g < 2; g++)
+    if (!group[g].empty())
+      encode_ws_map(P[g].tmap, d_ws, wsoff);
   // pack both plans' lists into the arena: one pinned staging area, one copy
   size_t off = 0;
   auto place = [&](size_t bytes) {
@@ -1502,7 +1808,7 @@ Batch *batch_create(Context *ctx, const std::vector<Molecule *> &mols, double ws
     size_t off = 0;
     for (size_t i : part) {
       Molecule *M = mols[i];
-      MixTab T = bind_ws(*M, B->d_ws + off);
+      MixTab T = bind_ws(*M, B->d_ws + off, B->d_ws);
       off += M->mixed_workspace_bytes();
       T.D = B->dD[i];
       T.V = B->dV[i];
@@ -1512,8 +1818,10 @@ Batch *batch_create(Context *ctx, const std::vector<Molecule *> &mols, double ws
       tabs[g].push_back(T);
     }
     for (int g = 0; g < 2; g++)
-      if (!group[g].empty())
+      if (!group[g].empty()) {
         make_plan(sb->plan[g], group[g], tabs[g]);
+        encode_ws_map(sb->plan[g].tmap, B->d_ws, std::max<size_t>(B->ws_bytes, 256));
+      }
     B->subs.push_back(std::move(sb));
   }
   cuda_check(cudaMalloc(&B->d_err, sizeof(int)), "cudaMalloc");
