@@ -250,15 +250,18 @@ void Molecule::prepare(int precision) {
 
 void Molecule::build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st,
                           double *ws) {
+  bool skip_colloc = false;
   if (!ws) {
     ensure_fp64_ws();
     ws = d_ws;
+    skip_colloc = fp64_ao_valid; // the private workspace keeps the AO values
   }
   const MolDev m = dev();
   const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
   Context &c = *ctx;
   cuda_check(cudaMemsetAsync(dV, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
-  c.launch("colloc_f64", st, [&] { launch_colloc_f64(m, deriv, ws, st); });
+  if (!skip_colloc)
+    c.launch("colloc_f64", st, [&] { launch_colloc_f64(m, deriv, ws, st); });
   c.launch("rho_f64", st, [&] {
     launch_rho_f64(m, deriv, dD, ws, d_slabs, static_cast<int>(slabs.size()), d_rho, st);
   });
@@ -270,6 +273,8 @@ void Molecule::build_fp64(const double *dD, double *dV, double *dout2, cudaStrea
   });
   c.launch("reduce", st, [&] { launch_reduce(d_epart, m.nleaves, dout2, st); });
   cuda_check(cudaGetLastError(), "kernel launch");
+  if (ws == d_ws)
+    fp64_ao_valid = true;
 }
 
 void Molecule::build(int precision, const double *dD, double *dV, double *dout2,
@@ -451,6 +456,7 @@ void Molecule::release_device() {
   d_slabs = nullptr;
   d_tiles = nullptr;
   d_ws = d_rho = d_coef = d_epart = d_out2 = d_D = d_V = nullptr;
+  fp64_ao_valid = false;
 }
 
 // Device bytes that materialise() allocates -- the resident state, without the

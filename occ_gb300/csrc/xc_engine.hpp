@@ -127,6 +127,7 @@ struct Molecule {
   double *d_ws = nullptr, *d_rho = nullptr, *d_coef = nullptr, *d_epart = nullptr;
   double *d_out2 = nullptr, *d_D = nullptr, *d_V = nullptr;
   MixedState *mixed = nullptr;
+  bool fp64_ao_valid = false; // d_ws holds this molecule's AO values (no collocation)
 
   ~Molecule();
   void *alloc(size_t bytes);

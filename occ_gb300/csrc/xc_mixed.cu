@@ -100,6 +100,12 @@ constexpr uint32_t kOffA1 = 0, kOffA2 = 16 * 1024, kOffA3 = 32 * 1024;
 constexpr uint32_t kOffB1 = 48 * 1024, kOffB2 = 64 * 1024, kOffB3 = 80 * 1024;
 constexpr uint32_t kWaitIter = 1u << 24; // bounded mbarrier waits
 constexpr int kErrTimeout = 1;
+// AO planes of a block, [plane][mp][128] FP32 each: phi, d/dx, d/dy, d/dz
+// (k_colloc_f32), hi and lo of Y (k_ymix, per build) and of phi (k_colloc_f32).
+// phi, its gradient and its split depend only on the grid and the basis: they
+// stay valid across builds of a molecule whose workspace is its own.
+constexpr int kPlanes = 8;
+constexpr int kPlaneYHi = 4, kPlaneYLo = 5, kPlanePhiHi = 6, kPlanePhiLo = 7;
 
 struct MBlock {
   int mol;          // molecule (row of the MixTab table)
@@ -108,7 +114,7 @@ struct MBlock {
   int cnt;          // points in the block (<= 128)
   int mp;           // significant AOs of the leaf, padded to 32
   int lblock;       // index of the block within its molecule (row scales)
-  long long ws_off; // float offset of the block's [4][mp][128] planes in the molecule's ws
+  long long ws_off; // float offset of the block's [kPlanes][mp][128] planes in the molecule's ws
 };
 // A V_xc work item: AO rows i0 .. i0 + 127 of nblk consecutive blocks of one
 // leaf (index block0 into the launch's block list); K runs over all their points.
@@ -128,7 +134,7 @@ struct MixTab {
   double dens_thr;
   const float4 *prim32; // primitives (alpha hi, alpha lo, c hi, c lo)
   const float4 *shA;    // shell centres (hi xyz, lo xyz)
-  float *ws;            // AO values [block][4][mp][128]
+  float *ws;            // AO planes [block][kPlanes][mp][128]
   float *rowscale;      // power-of-two bound of each block row of phi
   float2 *dhl;          // D2 as (hi, lo) floats
   float *colb;          // column bounds of D2
@@ -402,6 +408,16 @@ __device__ __forceinline__ void df_sub(float ah, float al, float bh, float bl, f
 
 // ---------------------------------------------------------------------------
 // FP32 collocation of one block: ws32[comp][mp][128]
+// x = hi + lo with hi = x rounded to the nearest TF32 and lo = (x - hi)
+// rounded to the nearest TF32: both exact TF32 values, so the tensor core
+// drops no bits and the split error has no sign bias (the 3xTF32 operands).
+__device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
+  uint32_t h, l;
+  umma::split_tf32(x, h, l);
+  hi = __uint_as_float(h);
+  lo = __uint_as_float(l);
+}
+
 template <int L>
 __device__ __forceinline__ float colloc_shell_f32(const DevShell &sh, bool pure, float x, float y,
                                                   float z, float R, float dR, bool valid,
@@ -453,6 +469,10 @@ __device__ __forceinline__ float colloc_shell_f32(const DevShell &sh, bool pure,
       out[plane + o] = valid ? gx[f] : 0.f;
       out[2 * plane + o] = valid ? gy[f] : 0.f;
       out[3 * plane + o] = valid ? gz[f] : 0.f;
+      float h, l;
+      tf32_split(val, h, l);
+      out[kPlanePhiHi * plane + o] = h;
+      out[kPlanePhiLo * plane + o] = l;
     }
   }
   return vmax;
@@ -533,6 +553,8 @@ __global__ void __launch_bounds__(128, 4) k_colloc_f32(const MixTab *__restrict_
     base[plane + o] = 0.f;
     base[2 * plane + o] = 0.f;
     base[3 * plane + o] = 0.f;
+    base[kPlanePhiHi * plane + o] = 0.f;
+    base[kPlanePhiLo * plane + o] = 0.f;
   }
   T.rowscale[static_cast<size_t>(B.lblock) * kBlockPts + p] = pow2_bound(vmax);
 }
@@ -757,7 +779,8 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(const MixTab *__restrict__
 // blocks of one leaf; K = their points) fetched from a global queue and
 // handed to the roles through a ring in shared memory:
 //   warp 4       TMA producer: per K chunk of 32 points, hi and lo of the A
-//                rows (phi) and of the B rows (Y), pre-split by k_ymix, as
+//                rows (phi, split by k_colloc_f32) and of the B rows (Y,
+//                split by k_ymix), as
 //                32 x 32 FP32 boxes with the 128-byte swizzle
 //   warp 5       MMA issuer: hi*hi + hi*lo + lo*hi ("3xTF32") into one of two
 //                TMEM accumulators of 256 columns; for a leaf with at most
@@ -908,16 +931,16 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
                                           static_cast<uint32_t>(W.rows_a + N) * 256u);
               uint8_t *st = stage[s];
               for (int r = 0; r < W.rows_a; r += 32) {
-                umma::tma_load_2d(st + kOffAhi + r * 128, &tmap, c * kKc, r0 + W.i0 + r,
-                                  &sm->full[s]);
+                umma::tma_load_2d(st + kOffAhi + r * 128, &tmap, c * kKc,
+                                  r0 + kPlanePhiHi * mp + W.i0 + r, &sm->full[s]);
                 umma::tma_load_2d(st + kOffAlo + r * 128, &tmap, c * kKc,
-                                  r0 + 3 * mp + W.i0 + r, &sm->full[s]);
+                                  r0 + kPlanePhiLo * mp + W.i0 + r, &sm->full[s]);
               }
               for (int r = 0; r < N; r += 32) {
-                umma::tma_load_2d(st + kOffBhi + r * 128, &tmap, c * kKc, r0 + mp + n0 + r,
-                                  &sm->full[s]);
+                umma::tma_load_2d(st + kOffBhi + r * 128, &tmap, c * kKc,
+                                  r0 + kPlaneYHi * mp + n0 + r, &sm->full[s]);
                 umma::tma_load_2d(st + kOffBlo + r * 128, &tmap, c * kKc,
-                                  r0 + 2 * mp + n0 + r, &sm->full[s]);
+                                  r0 + kPlaneYLo * mp + n0 + r, &sm->full[s]);
               }
             }
           }
@@ -1087,20 +1110,9 @@ __global__ void __launch_bounds__(256) k_func_b(const MixTab *__restrict__ tabs,
                          T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
 }
 
-// Operands of k_vxc_tma for one block, pre-split for 3xTF32: with
-// Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi (FP32),
-// hi(x) = x rounded to the nearest TF32 and lo(x) = x - hi(x) rounded to the
-// nearest TF32 (both exact TF32 values, so the tensor core drops no bits and
-// the split error has no sign bias), the block's AO planes become
-//   plane 0: hi(phi)   plane 1: hi(Y)   plane 2: lo(Y)   plane 3: lo(phi)
-// (phi and grad phi are not needed after the density).  One CTA per block;
-// streams 4 planes in and out.
-__device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
-  uint32_t h, l;
-  umma::split_tf32(x, h, l);
-  hi = __uint_as_float(h);
-  lo = __uint_as_float(l);
-}
+// The B operand of k_vxc_tma for one block, pre-split for 3xTF32 (tf32_split):
+// Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi (FP32) into the Y hi / lo
+// planes.  One CTA per block; streams 4 planes in, 2 out.
 template <bool DERIV>
 __global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
                                               const MBlock *__restrict__ blocks) {
@@ -1148,13 +1160,10 @@ __global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
       y.z = fmaf(gz.z, cf[p + 2].w, fmaf(gy.z, cf[p + 2].z, fmaf(gx.z, cf[p + 2].y, y.z)));
       y.w = fmaf(gz.w, cf[p + 3].w, fmaf(gy.w, cf[p + 3].z, fmaf(gx.w, cf[p + 3].y, y.w)));
     }
-    float4 ah, al, yh, yl;
-    split4(a, ah, al);
+    float4 yh, yl;
     split4(y, yh, yl);
-    base[q] = ah;
-    base[plane + q] = yh;
-    base[2 * plane + q] = yl;
-    base[3 * plane + q] = al;
+    base[kPlaneYHi * plane + q] = yh;
+    base[kPlaneYLo * plane + q] = yl;
   }
 }
 
@@ -1296,6 +1305,10 @@ struct LaunchPlan {
   MixTab *d_tabs = nullptr;
   int maxnbf = 0, deriv = 0;
   CUtensorMap tmap;       // the workspace as rows of 128 floats (k_vxc_tma)
+  // the workspace already holds these molecules' AO values (phi, its gradient,
+  // its TF32 split, row scales): collocation is skipped
+  bool ao_valid = false;
+  bool ao_cacheable = false; // the workspace belongs to this plan alone
   std::vector<void *> owned;
   ~LaunchPlan() {
     for (void *p : owned)
@@ -1337,7 +1350,7 @@ WsLayout ws_layout(const Molecule &M) {
     const size_t nb = (Lf.cnt + kBlockPts - 1) / kBlockPts;
     const size_t mp = (Lf.nbf + kKc - 1) / kKc * kKc;
     nblocks += nb;
-    ws_floats += nb * 4 * mp * kBlockPts;
+    ws_floats += nb * kPlanes * mp * kBlockPts;
   }
   L.ws = put(ws_floats * sizeof(float));
   L.rowscale = put(nblocks * kBlockPts * sizeof(float));
@@ -1461,7 +1474,10 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
     k_prep_density<<<dim3(P.maxnbf, nmol), 256, 0, st>>>(P.d_tabs, ov, P.d_queue);
   });
   if (nb > 0) {
-    c.launch("colloc_f32", st, [&] { k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks); });
+    if (!P.ao_valid)
+      c.launch("colloc_f32", st, [&] {
+        k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
     c.launch("rho_mixed", st, [&] {
       const int g = std::min(nb, ctas);
       if (P.deriv)
@@ -1499,6 +1515,8 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
   });
   c.launch("reduce", st, [&] { k_reduce_b<<<nmol, 256, 0, st>>>(P.d_tabs, ov); });
   cuda_check(cudaGetLastError(), "kernel launch");
+  if (P.ao_cacheable)
+    P.ao_valid = true;
 }
 
 } // namespace
@@ -1519,7 +1537,7 @@ void Molecule::prepare_mixed() {
       B.mp = mp;
       B.lblock = lblock++;
       B.ws_off = static_cast<long long>(S->ws_floats);
-      S->ws_floats += static_cast<size_t>(4) * mp * kBlockPts;
+      S->ws_floats += static_cast<size_t>(kPlanes) * mp * kBlockPts;
       S->blocks.push_back(B);
     }
   }
@@ -1611,6 +1629,7 @@ void Molecule::ensure_mixed_ws() {
   S->d_private = static_cast<char *>(alloc(bytes));
   auto P = std::make_unique<LaunchPlan>();
   make_plan(*P, {this}, {bind_ws(*this, S->d_private, S->d_private)});
+  P->ao_cacheable = true;
   encode_ws_map(P->tmap, S->d_private, bytes);
   S->single = std::move(P);
 }
@@ -1820,6 +1839,7 @@ Batch *batch_create(Context *ctx, const std::vector<Molecule *> &mols, double ws
     for (int g = 0; g < 2; g++)
       if (!group[g].empty()) {
         make_plan(sb->plan[g], group[g], tabs[g]);
+        sb->plan[g].ao_cacheable = parts.size() == 1; // else sub-batches share the space
         encode_ws_map(sb->plan[g].tmap, B->d_ws, std::max<size_t>(B->ws_bytes, 256));
       }
     B->subs.push_back(std::move(sb));
