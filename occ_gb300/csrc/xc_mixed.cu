@@ -99,13 +99,18 @@ constexpr uint32_t kOffAhi = 0, kOffAlo = 16 * 1024, kOffBhi = 32 * 1024, kOffBl
 constexpr uint32_t kOffA1 = 0, kOffA2 = 16 * 1024, kOffA3 = 32 * 1024;
 constexpr uint32_t kOffB1 = 48 * 1024, kOffB2 = 64 * 1024, kOffB3 = 80 * 1024;
 constexpr uint32_t kWaitIter = 1u << 24; // bounded mbarrier waits
+constexpr uint32_t kRhoStageA = 3 * 16384; // exact-grid A slices of one K chunk (128 x 32 each)
 constexpr int kErrTimeout = 1;
 // AO planes of a block, [plane][mp][128] FP32 each: phi, d/dx, d/dy, d/dz
-// (k_colloc_f32), hi and lo of Y (k_ymix, per build) and of phi (k_colloc_f32).
-// phi, its gradient and its split depend only on the grid and the basis: they
-// stay valid across builds of a molecule whose workspace is its own.
-constexpr int kPlanes = 8;
-constexpr int kPlaneYHi = 4, kPlaneYLo = 5, kPlanePhiHi = 6, kPlanePhiLo = 7;
+// (k_colloc_f32), hi and lo of Y (k_ymix, per build) and of phi (k_colloc_f32),
+// then three planes' worth of the exact-grid slices of phi as the density
+// GEMM's A operand: per K chunk of 32 AOs, three 128 x 32 K-major tiles in
+// the 128-byte-swizzled layout of shared memory (k_colloc_f32), so that
+// k_rho_mixed stages them with one bulk copy.  Everything but Y depends only
+// on the grid and the basis and stays valid across builds of a molecule whose
+// workspace is its own.
+constexpr int kPlanes = 11;
+constexpr int kPlaneYHi = 4, kPlaneYLo = 5, kPlanePhiHi = 6, kPlanePhiLo = 7, kPlaneASlices = 8;
 
 struct MBlock {
   int mol;          // molecule (row of the MixTab table)
@@ -481,7 +486,7 @@ __device__ __forceinline__ float colloc_shell_f32(const DevShell &sh, bool pure,
 // Exponents and coefficients as (hi, lo) float pairs: rounding alpha or c to
 // one float would bias every point a primitive touches the same way, an error
 // that does not average out over the grid.
-__global__ void __launch_bounds__(128, 4) k_colloc_f32(const MixTab *__restrict__ tabs,
+__global__ void __launch_bounds__(128, 3) k_colloc_f32(const MixTab *__restrict__ tabs,
                                                     const MBlock *__restrict__ blocks) {
   const MBlock B = blocks[blockIdx.x];
   const MixTab &T = tabs[B.mol];
@@ -556,7 +561,22 @@ __global__ void __launch_bounds__(128, 4) k_colloc_f32(const MixTab *__restrict_
     base[kPlanePhiHi * plane + o] = 0.f;
     base[kPlanePhiLo * plane + o] = 0.f;
   }
-  T.rowscale[static_cast<size_t>(B.lblock) * kBlockPts + p] = pow2_bound(vmax);
+  const float sA = pow2_bound(vmax), isA = 1.f / sA;
+  T.rowscale[static_cast<size_t>(B.lblock) * kBlockPts + p] = sA;
+  // the A operand of k_rho_mixed: this point's row of phi on the exact grid
+  // (scale sA), chunk by chunk, at its swizzled place in the three tiles
+  uint8_t *as = reinterpret_cast<uint8_t *>(base + kPlaneASlices * plane);
+  for (int c = 0; c < B.mp / kKc; c++) {
+    uint8_t *tile = as + static_cast<size_t>(c) * kRhoStageA;
+#pragma unroll 2
+    for (int q = 0; q < kKc / 4; q++) {
+      float v[4];
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+        v[e] = base[static_cast<size_t>(c * kKc + q * 4 + e) * kBlockPts + p];
+      store4_exact(tile, tile + 16384, tile + 32768, p, q, v, sA, isA);
+    }
+  }
 }
 
 constexpr uint32_t kSmemMain = 2 * kStageBytes;
@@ -637,141 +657,332 @@ __global__ void __launch_bounds__(256) k_symmetrize(const MixTab *__restrict__ t
   }
 }
 
-// rho, grad rho of one block.  X = phi D2 is computed on the exact grid:
-// row scales s_p (phi rows, from the collocation) and t_j (D2 columns, from
-// k_prep_density), slices a1, a2, a3 / b1, b2, b3 (slice3), three TMEM
-// accumulators; a K segment holds at most 512 AOs so that the integer sums
-// of the exact levels stay below 2^24.  The epilogue forms X = acc0 + acc1 +
-// acc2 per segment and accumulates rowsum(phi o X) with compensated sums.
-// Persistent (TMEM and barriers set up once per CTA): each CTA takes the next
-// block of `order` (most expensive first) from a global counter.
+// ---- density: X = phi D2 on tcgen05, rho = rowsum(phi o X) ----------------
+// (src/gto/density.cpp:33-43).  X is computed on an exact grid: phi rows
+// scaled by a power of two s_p, D2 columns by t_j, both operands split into
+// slices a1 (grid 2^-7), a2 (grid 2^-15), a3 (TF32 tail); acc0 = a1 b1 and
+// acc1 = a1 b2 + a2 b1 are exact integer sums while a K segment holds at most
+// 512 AOs, acc2 collects the tail products (at most 2^-15 of the result).
+// One CTA per SM, persistent over blocks (most AOs first) from a global
+// queue, with a ring of block indices in shared memory and these roles:
+//   warp 8       block fetch, and per K chunk of 32 AOs one bulk copy of the
+//                block's precomputed A slices (k_colloc_f32)
+//   warps 4-7    B producers: D2 (hi, lo) gathered through the block's AO map
+//                for 64 columns j x 32 AOs k, sliced with t_j, into the stage
+//   warp 9       MMA issuer: eight TF32 MMAs per K step into acc0..acc2 of one
+//                of two TMEM buffers (3 x 64 columns each)
+//   warps 0-3    epilogue, one point per thread: X = acc0 + acc1 + acc2 and
+//                compensated FP32 dot products with phi and grad phi; rho
+//                and grad rho (FP64) when the block is done
+// Every wait is bounded; on expiry the error flag is set and all roles leave.
+constexpr int kRing = 4;                                   // depth of the work-item rings
+constexpr int kRhoN = 64;                                  // columns j per pass
+constexpr uint32_t kRhoStageB = 3 * (kRhoN * 128);        // B slices (64 x 32 each)
+constexpr uint32_t kRhoStage = kRhoStageA + kRhoStageB;   // 72 KB
+constexpr int kRhoStages = 3;
+constexpr int kRhoThreads = 320;
+constexpr int kRhoProd = 128;  // B producer threads (warps 4-7)
+constexpr int kRhoEpi = 128;   // epilogue threads (warps 0-3)
+constexpr int kRhoMap = 1024;  // AO maps up to this size are staged in shared memory
+
+struct alignas(16) RhoSmem {
+  uint64_t full[kRhoStages], empty[kRhoStages]; // per stage: A and B landed, MMAs done
+  uint64_t tfull[2], tempty[2];
+  uint64_t ifull[kRing], iempty[kRing];
+  uint64_t done;
+  uint32_t tmem_slot;
+  int ring[kRing];
+  int gmap[kRhoMap]; // the producers' current AO map
+};
+constexpr uint32_t kRhoSmem = kRhoStages * kRhoStage + sizeof(RhoSmem) + 1024;
+static_assert(kRhoSmem <= 232448, "density kernel exceeds the shared memory of a CTA");
+
+__device__ __forceinline__ void bar_named(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+// AND of v over the n threads of named barrier id (a barrier among them too).
+__device__ __forceinline__ bool bar_all(int id, int n, bool v) {
+  uint32_t r;
+  asm volatile("{\n\t.reg .pred p, q;\n\t"
+               "setp.ne.u32 p, %1, 0;\n\t"
+               "barrier.red.and.pred q, %2, %3, p;\n\t"
+               "selp.u32 %0, 1, 0, q;\n\t}"
+               : "=r"(r)
+               : "r"(static_cast<uint32_t>(v)), "r"(id), "r"(n)
+               : "memory");
+  return r != 0;
+}
+
 template <bool DERIV>
-__global__ void __launch_bounds__(256, 1) k_rho_mixed(const MixTab *__restrict__ tabs,
-                                                      const MBlock *__restrict__ blocks,
-                                                      const int *__restrict__ order, int nblocks,
-                                                      int *queue, int *err) {
+__global__ void __launch_bounds__(kRhoThreads, 1)
+    k_rho_mixed(const MixTab *__restrict__ tabs, const MBlock *__restrict__ blocks,
+                const int *__restrict__ order, int nblocks, int *queue, int *err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
-  SmemTail *tail = reinterpret_cast<SmemTail *>(smem + kSmemMain);
+  RhoSmem *sm = reinterpret_cast<RhoSmem *>(smem + kRhoStages * kRhoStage);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int quad = warp & 3, half = warp >> 2;
-  Pipe P;
-  pipe_init(P, smem, tail->bars, &tail->tmem_slot, 512);
-  for (;;) {
-  if (t == 0)
-    tail->next = atomicAdd(&queue[0], 1);
+  if (t == 0) {
+    for (int s = 0; s < kRhoStages; s++) {
+      umma::mbar_init(&sm->full[s], 1 + kRhoProd);
+      umma::mbar_init(&sm->empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      umma::mbar_init(&sm->tfull[b], 1);
+      umma::mbar_init(&sm->tempty[b], kRhoEpi);
+    }
+    for (int r = 0; r < kRing; r++) {
+      umma::mbar_init(&sm->ifull[r], 1);
+      umma::mbar_init(&sm->iempty[r], 1 + kRhoProd + kRhoEpi);
+    }
+    umma::mbar_init(&sm->done, 1);
+    umma::fence_proxy_async();
+  }
+  if (warp == 0)
+    umma::tmem_alloc(&sm->tmem_slot, 512);
+  umma::fence_before_sync();
   __syncthreads();
-  const int qi = tail->next;
-  if (qi >= nblocks)
-    break;
-  const MBlock B = blocks[order[qi]];
-  const MixTab &T = tabs[B.mol];
-  const MolDev &m = T.m;
-  const DevLeaf L = m.leaves[B.leaf];
-  const int *g = m.leaf_ao + L.ao_begin;
-  const float *phi = T.ws + B.ws_off;
-  const float2 *__restrict__ dhl = T.dhl;
-  const float *__restrict__ colb = T.colb;
-  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
-  const size_t nbf = static_cast<size_t>(m.nbf);
-  // A producer rows: point t & 127; its scale
-  const float sA = T.rowscale[static_cast<size_t>(B.lblock) * kBlockPts + (t & 127)];
-  const float isA = 1.f / sA;
-  // the block's AO map in shared memory (gathers then need no dependent load)
-  const bool gsh = L.nbf <= kMaxMapSmem;
-  if (gsh)
-    for (int q = t; q < L.nbf; q += blockDim.x)
-      tail->gmap[q] = g[q];
-  const int *gm = gsh ? tail->gmap : g;
-  __syncthreads();
-  float acc[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
-  const int p = quad * 32 + lane; // this thread's point in the epilogue
-  for (int n0 = 0; n0 < B.mp; n0 += kExactN) {
-    const int N = min(kExactN, B.mp - n0);
-    if (t < N)
-      tail->bscale[t] = (n0 + t < L.nbf) ? colb[gm[n0 + t]] : 1.f;
-    __syncthreads();
-    auto fa = [&](int c, uint8_t *st) {
-      const int r = t & 127, kh = t >> 7;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int k = c * kKc + kh * 16 + q * 4;
-        float v[4];
-#pragma unroll
-        for (int e = 0; e < 4; e++)
-          v[e] = phi[static_cast<size_t>(k + e) * kBlockPts + r];
-        store4_exact(st + kOffA1, st + kOffA2, st + kOffA3, r, kh * 4 + q, v, sA, isA);
+  umma::fence_after_sync();
+  const uint32_t tmem = sm->tmem_slot;
+  bool ok = true;
+  auto wait = [&](uint64_t *bar, uint32_t parity) {
+    if (ok && !umma::mbar_wait(bar, parity, kWaitIter)) {
+      ok = false;
+      atomicExch(err, kErrTimeout);
+    }
+    return ok;
+  };
+  // groups that share named barriers take every decision to stop together
+  const bool epi = warp < 4, prod = warp >= 4 && warp < 8;
+  auto agree = [&] {
+    if (epi)
+      ok = bar_all(1, kRhoEpi, ok);
+    else if (prod)
+      ok = bar_all(2, kRhoProd, ok);
+    return ok;
+  };
+  auto next_block = [&](int k) {
+    const int slot = k % kRing;
+    wait(&sm->ifull[slot], (k / kRing) & 1);
+    if (!agree())
+      return -1;
+    const int bi = sm->ring[slot];
+    umma::mbar_arrive(&sm->iempty[slot]);
+    return bi;
+  };
+  auto segs = [](int mp) { return (mp + kExactKSeg - 1) / kExactKSeg; };
+  auto seg_chunks = [](int mp, int k0) { return min(kExactKSeg, mp - k0) / kKc; };
+
+  if (warp == 8) {
+    // ---- block fetch and A slices (lane 0) ----
+    if (lane == 0) {
+      uint32_t g = 0;
+      for (int k = 0;; k++) {
+        const int slot = k % kRing;
+        if (k >= kRing && !wait(&sm->iempty[slot], ((k / kRing) - 1) & 1))
+          break;
+        const int qi = atomicAdd(&queue[0], 1);
+        const int bi = qi < nblocks ? order[qi] : -1;
+        sm->ring[slot] = bi;
+        umma::mbar_arrive(&sm->ifull[slot]);
+        if (bi < 0)
+          break;
+        const MBlock B = blocks[bi];
+        const MixTab &T = tabs[B.mol];
+        const uint8_t *as = reinterpret_cast<const uint8_t *>(
+            T.ws + B.ws_off + static_cast<size_t>(kPlaneASlices) * B.mp * kBlockPts);
+        for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN)
+          for (int k0 = 0; k0 < B.mp && ok; k0 += kExactKSeg)
+            for (int c = 0; c < seg_chunks(B.mp, k0); c++, g++) {
+              const int s = g % kRhoStages;
+              const uint32_t use = g / kRhoStages;
+              if (use > 0 && !wait(&sm->empty[s], (use - 1) & 1))
+                break;
+              umma::mbar_arrive_expect_tx(&sm->full[s], kRhoStageA);
+              umma::bulk_load(smem + s * kRhoStage,
+                              as + static_cast<size_t>(k0 / kKc + c) * kRhoStageA, kRhoStageA,
+                              &sm->full[s]);
+            }
+        if (!ok)
+          break;
       }
-    };
-    for (int k0 = 0; k0 < B.mp; k0 += kExactKSeg) {
-      const int nk = min(kExactKSeg, B.mp - k0) / kKc;
-      auto fa_seg = [&](int c, uint8_t *st) { fa(k0 / kKc + c, st); };
-      // all threads: (row j, 16-byte chunk q) pairs of the N x 32 B tile
-      auto fb = [&](int c, uint8_t *st) {
-        for (int idx = t; idx < N * 8; idx += 256) {
-          const int j = idx >> 3, q = idx & 7;
-          const int lj = n0 + j;
-          const bool jv = lj < L.nbf;
-          const size_t gj = jv ? static_cast<size_t>(gm[lj]) : 0;
-          const float sB = tail->bscale[j], isB = 1.f / sB;
-          float v[4], lo[4];
+      for (uint32_t q = (g >= kRhoStages ? g - kRhoStages : 0); q < g; q++)
+        umma::mbar_wait(&sm->full[q % kRhoStages], (q / kRhoStages) & 1, kWaitIter);
+    }
+  } else if (prod) {
+    // ---- B producers ----
+    const int pt = t - 128;
+    const int jr = pt & 63;        // row j of the B tile this thread fills
+    const int qb = pt >> 6;        // first 16-byte chunk; then qb + 2, + 4, + 6
+    uint32_t g = 0;
+    for (int k = 0; ok; k++) {
+      const int bi = next_block(k);
+      if (bi < 0)
+        break;
+      const MBlock B = blocks[bi];
+      const MixTab &T = tabs[B.mol];
+      const DevLeaf L = T.m.leaves[B.leaf];
+      const int *gsrc = T.m.leaf_ao + L.ao_begin;
+      const bool gsh = L.nbf <= kRhoMap;
+      if (gsh) {
+        bar_named(2, kRhoProd);
+        for (int q = pt; q < L.nbf; q += kRhoProd)
+          sm->gmap[q] = gsrc[q];
+        bar_named(2, kRhoProd);
+      }
+      const int *gm = gsh ? sm->gmap : gsrc;
+      const float2 *__restrict__ dhl = T.dhl;
+      const size_t nbf = static_cast<size_t>(T.m.nbf);
+      for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN) {
+        const int lj = n0 + jr;
+        const bool jv = lj < L.nbf;
+        const size_t gj = jv ? static_cast<size_t>(gm[lj]) : 0;
+        const float sB = jv ? T.colb[gj] : 1.f, isB = 1.f / sB;
+        for (int k0 = 0; k0 < B.mp && ok; k0 += kExactKSeg)
+          for (int c = 0; c < seg_chunks(B.mp, k0); c++, g++) {
+            const int s = g % kRhoStages;
+            const uint32_t use = g / kRhoStages;
+            if (use > 0 && !wait(&sm->empty[s], (use - 1) & 1))
+              break;
+            uint8_t *st = smem + s * kRhoStage + kRhoStageA;
+            float2 d[4][4];
 #pragma unroll
-          for (int e = 0; e < 4; e++) {
-            const int lk = k0 + c * kKc + q * 4 + e;
-            const float2 d = (jv && lk < L.nbf)
-                                 ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
-                                 : make_float2(0.f, 0.f);
-            v[e] = d.x;
-            lo[e] = d.y;
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+              for (int e = 0; e < 4; e++) {
+                const int lk = k0 + c * kKc + (qb + 2 * r) * 4 + e;
+                d[r][e] = (jv && lk < L.nbf) ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
+                                             : make_float2(0.f, 0.f);
+              }
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+              const float v[4] = {d[r][0].x, d[r][1].x, d[r][2].x, d[r][3].x};
+              const float lo[4] = {d[r][0].y, d[r][1].y, d[r][2].y, d[r][3].y};
+              store4_exact(st, st + kRhoN * 128, st + 2 * kRhoN * 128, jr, qb + 2 * r, v, sB,
+                           isB, lo);
+            }
+            umma::fence_proxy_async();
+            umma::mbar_arrive(&sm->full[s]);
           }
-          store4_exact(st + kOffB1, st + kOffB2, st + kOffB3, j, q, v, sB, isB, lo);
-        }
-      };
-      gemm_pass<true>(P, N, nk, fa_seg, fb, err);
-      // epilogue of this segment: X = acc0 + acc1 + acc2 on this warp's
-      // 32 points and half of the pass's columns
-      const int cols = N / 2;
-      const uint32_t lanebase = P.tmem + (static_cast<uint32_t>(quad * 32) << 16);
-      for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
-        uint32_t r0[16], r1[16], r2[16];
-        umma::tmem_ld16(lanebase + c0, r0);
-        umma::tmem_ld16(lanebase + kExactN + c0, r1);
-        umma::tmem_ld16(lanebase + 2 * kExactN + c0, r2);
-        umma::tmem_wait_ld();
+      }
+    }
+  } else if (warp == 9) {
+    // ---- MMA issuer (lane 0) ----
+    if (lane == 0) {
+      uint32_t g = 0, sc = 0; // chunks, segments
+      bool issued = false;
+      for (int k = 0; ok; k++) {
+        const int bi = next_block(k);
+        if (bi < 0)
+          break;
+        const int mp = blocks[bi].mp;
+        for (int n0 = 0; n0 < mp && ok; n0 += kRhoN) {
+          const int N = min(kRhoN, mp - n0);
+          const uint32_t idesc = umma::idesc_tf32(128, N);
+          for (int k0 = 0; k0 < mp && ok; k0 += kExactKSeg, sc++) {
+            const uint32_t buf = sc & 1, ub = sc >> 1;
+            if (ub > 0 && !wait(&sm->tempty[buf], (ub - 1) & 1))
+              break;
+            umma::fence_after_sync();
+            const uint32_t d0 = tmem + buf * 256, d1 = d0 + kRhoN, d2 = d0 + 2 * kRhoN;
+            const int nch = seg_chunks(mp, k0);
+            for (int c = 0; c < nch && ok; c++, g++) {
+              const int s = g % kRhoStages;
+              if (!wait(&sm->full[s], (g / kRhoStages) & 1))
+                break;
+              umma::fence_after_sync();
+              const uint32_t base = umma::smem_u32(smem + s * kRhoStage);
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
-          const float x = __fadd_rn(__uint_as_float(r0[i]),
-                                    __fadd_rn(__uint_as_float(r1[i]), __uint_as_float(r2[i])));
-          const size_t o = static_cast<size_t>(n0 + c0 + i) * kBlockPts + p;
-          dot2_step(phi[o], x, acc[0], cmp[0]);
-          if (DERIV) {
-            dot2_step(phi[plane + o], x, acc[1], cmp[1]);
-            dot2_step(phi[2 * plane + o], x, acc[2], cmp[2]);
-            dot2_step(phi[3 * plane + o], x, acc[3], cmp[3]);
+              for (int kk = 0; kk < kKc / 8; kk++) {
+                const uint32_t o = kk * 32;
+                const uint64_t a1 = umma::desc_kmajor_sw128(base + o);
+                const uint64_t a2 = umma::desc_kmajor_sw128(base + 16384 + o);
+                const uint64_t a3 = umma::desc_kmajor_sw128(base + 32768 + o);
+                const uint64_t b1 = umma::desc_kmajor_sw128(base + kRhoStageA + o);
+                const uint64_t b2 = umma::desc_kmajor_sw128(base + kRhoStageA + kRhoN * 128 + o);
+                const uint64_t b3 =
+                    umma::desc_kmajor_sw128(base + kRhoStageA + 2 * kRhoN * 128 + o);
+                const uint32_t acc = (c == 0 && kk == 0) ? 0u : 1u;
+                umma::mma_tf32(d0, a1, b1, idesc, acc);
+                umma::mma_tf32(d1, a1, b2, idesc, acc);
+                umma::mma_tf32(d1, a2, b1, idesc, 1u);
+                umma::mma_tf32(d2, a2, b3, idesc, acc);
+                umma::mma_tf32(d2, a3, b2, idesc, 1u);
+                umma::mma_tf32(d2, a2, b2, idesc, 1u);
+                umma::mma_tf32(d2, a1, b3, idesc, 1u);
+                umma::mma_tf32(d2, a3, b1, idesc, 1u);
+              }
+              umma::commit(&sm->empty[s]);
+              issued = true;
+            }
+            umma::commit(&sm->tfull[buf]);
           }
         }
       }
-      umma::fence_before_sync();
-      __syncthreads();
+      if (issued) {
+        umma::commit(&sm->done);
+        umma::mbar_wait(&sm->done, 0, kWaitIter);
+      }
+    }
+  } else if (epi) {
+    // ---- epilogue: thread t holds point t of the block ----
+    const int quad = warp;
+    const int p = t;
+    uint32_t sc = 0;
+    for (int k = 0; ok; k++) {
+      const int bi = next_block(k);
+      if (bi < 0)
+        break;
+      const MBlock B = blocks[bi];
+      const MixTab &T = tabs[B.mol];
+      const float *phi = T.ws + B.ws_off;
+      const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN) {
+        const int N = min(kRhoN, B.mp - n0);
+        for (int k0 = 0; k0 < B.mp && ok; k0 += kExactKSeg, sc++) {
+          const uint32_t buf = sc & 1, ub = sc >> 1;
+          wait(&sm->tfull[buf], ub & 1);
+          if (!agree())
+            break;
+          umma::fence_after_sync();
+          const uint32_t lanebase = tmem + (static_cast<uint32_t>(quad * 32) << 16) + buf * 256;
+          for (int c0 = 0; c0 < N; c0 += 16) {
+            uint32_t r0[16], r1[16], r2[16];
+            umma::tmem_ld16(lanebase + c0, r0);
+            umma::tmem_ld16(lanebase + kRhoN + c0, r1);
+            umma::tmem_ld16(lanebase + 2 * kRhoN + c0, r2);
+            umma::tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+              const float x = __fadd_rn(__uint_as_float(r0[i]),
+                                        __fadd_rn(__uint_as_float(r1[i]), __uint_as_float(r2[i])));
+              const size_t o = static_cast<size_t>(n0 + c0 + i) * kBlockPts + p;
+              dot2_step(phi[o], x, acc[0], cmp[0]);
+              if (DERIV) {
+                dot2_step(phi[plane + o], x, acc[1], cmp[1]);
+                dot2_step(phi[2 * plane + o], x, acc[2], cmp[2]);
+                dot2_step(phi[3 * plane + o], x, acc[3], cmp[3]);
+              }
+            }
+          }
+          umma::fence_before_sync();
+          umma::mbar_arrive(&sm->tempty[buf]);
+        }
+      }
+      if (ok && p < B.cnt) {
+        const size_t idx = static_cast<size_t>(T.m.leaves[B.leaf].off) + B.p0 + p;
+        const size_t Np = static_cast<size_t>(T.m.npts);
+        T.rho[idx] = static_cast<double>(acc[0]) + static_cast<double>(cmp[0]);
+        if (DERIV)
+          for (int c = 1; c < 4; c++)
+            T.rho[c * Np + idx] = 2.0 * (static_cast<double>(acc[c]) + static_cast<double>(cmp[c]));
+      }
     }
   }
-#pragma unroll
-  for (int c = 0; c < 4; c++)
-    tail->red[half][c][p] = acc[c] + cmp[c];
+  umma::fence_before_sync();
   __syncthreads();
-  if (t < kBlockPts && t < B.cnt) {
-    double *rho = T.rho;
-    const size_t idx = static_cast<size_t>(L.off) + B.p0 + t;
-    const size_t Np = static_cast<size_t>(m.npts);
-    rho[idx] = static_cast<double>(tail->red[0][0][t]) + static_cast<double>(tail->red[1][0][t]);
-    if (DERIV)
-      for (int c = 1; c < 4; c++)
-        rho[c * Np + idx] = 2.0 * (static_cast<double>(tail->red[0][c][t]) +
-                                   static_cast<double>(tail->red[1][c][t]));
-  }
-  __syncthreads(); // tail->red and gmap are reused by the next block
-  } // blocks
-  pipe_finish(P);
+  if (warp == 0)
+    umma::tmem_dealloc(tmem, 512);
 }
 
 // ---- V_xc: K = phi^T Y on tcgen05, operands staged by TMA ------------------
@@ -792,7 +1003,6 @@ __global__ void __launch_bounds__(256, 1) k_rho_mixed(const MixTab *__restrict__
 // consecutive chunks and passes overlap.  Every wait is bounded; on expiry
 // the error flag is set and all roles leave.
 constexpr int kItemBlocks = 2;   // blocks of a leaf accumulated in one V item
-constexpr int kRing = 4;         // depth of the work-item ring
 constexpr int kVxcEpi = 128;     // epilogue threads (warps 0-3)
 constexpr int kVxcThreads = 192; // + producer warp + MMA warp
 constexpr int kVxcMap = 2048;    // AO maps up to this size are staged in shared memory
@@ -1278,9 +1488,9 @@ size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
 void set_smem_attributes() {
   cuda_check(cudaFuncSetAttribute(k_rho_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kSmemTotal), "cudaFuncSetAttribute");
+                                  kRhoSmem), "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_rho_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kSmemTotal), "cudaFuncSetAttribute");
+                                  kRhoSmem), "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_vxc_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kVxcSmem), "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_selftest_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1481,10 +1691,10 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
     c.launch("rho_mixed", st, [&] {
       const int g = std::min(nb, ctas);
       if (P.deriv)
-        k_rho_mixed<true><<<g, 256, kSmemTotal, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
+        k_rho_mixed<true><<<g, kRhoThreads, kRhoSmem, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
                                                       P.d_queue, err);
       else
-        k_rho_mixed<false><<<g, 256, kSmemTotal, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
+        k_rho_mixed<false><<<g, kRhoThreads, kRhoSmem, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
                                                        P.d_queue, err);
     });
   }
