@@ -80,107 +80,237 @@ __device__ __forceinline__ D3 dsqrt(D3 a) {
 __device__ __forceinline__ D3 datan(D3 a) { return apply(a, atan(a.v), 1.0 / fma(a.v, a.v, 1.0)); }
 __device__ __forceinline__ D3 dasinh(D3 a) { return apply(a, asinh(a.v), rsqrt(fma(a.v, a.v, 1.0))); }
 
+// ---- the mixed path's dual number: value in double-float FP32, derivatives
+// in FP32.  FP32 arithmetic is tens of times the FP64 rate on this GPU; the
+// value keeps about 44 bits (error-free transformations: Knuth's TwoSum,
+// FMA-based TwoProduct; Dekker/Shewchuk double-float algorithms), so energy
+// densities stay FP64-grade, while the derivatives feed V_xc, whose
+// tolerance FP32 meets.  Transcendental values (log, exp, cbrt, atan, asinh)
+// are taken in FP64 from the double-float argument; sqrt and divisions are
+// done in double-float.  The _rn intrinsics keep the compiler from fusing
+// the error-free transformations into FMAs.
+struct F2 {
+  float h, l; // value h + l, |l| <= ulp(h) / 2
+};
+__host__ __device__ constexpr F2 f2c(double x) {
+  return {static_cast<float>(x), static_cast<float>(x - static_cast<double>(static_cast<float>(x)))};
+}
+__device__ __forceinline__ F2 f2(double x) {
+  const float h = static_cast<float>(x);
+  return {h, static_cast<float>(x - static_cast<double>(h))};
+}
+__device__ __forceinline__ double to_d(F2 a) {
+  return static_cast<double>(a.h) + static_cast<double>(a.l);
+}
+__device__ __forceinline__ F2 quick_two_sum(float a, float b) { // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 two_sum_f(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const F2 s = two_sum_f(a.h, b.h);
+  const F2 t = two_sum_f(a.l, b.l);
+  F2 u = quick_two_sum(s.h, __fadd_rn(s.l, t.h));
+  return quick_two_sum(u.h, __fadd_rn(u.l, t.l));
+}
+__device__ __forceinline__ F2 f2_neg(F2 a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  const float p = __fmul_rn(a.h, b.h);
+  const float e = fmaf(a.h, b.h, -p);
+  return quick_two_sum(p, __fadd_rn(e, __fadd_rn(__fmul_rn(a.h, b.l), __fmul_rn(a.l, b.h))));
+}
+__device__ __forceinline__ F2 f2_div(F2 a, F2 b) {
+  // two correction steps of the float quotient
+  const float q1 = __fdiv_rn(a.h, b.h);
+  F2 r = f2_add(a, f2_neg(f2_mul({q1, 0.f}, b)));
+  const float q2 = __fdiv_rn(r.h, b.h);
+  r = f2_add(r, f2_neg(f2_mul({q2, 0.f}, b)));
+  const float q3 = __fdiv_rn(r.h, b.h);
+  return f2_add(quick_two_sum(q1, q2), {q3, 0.f});
+}
+__device__ __forceinline__ F2 f2_sqrt(F2 a) { // one Newton step from the float root
+  const float y = sqrtf(a.h);
+  const F2 yy = f2_mul({y, 0.f}, {y, 0.f});
+  const F2 r = f2_add(a, f2_neg(yy));
+  return quick_two_sum(y, __fdiv_rn(r.h, __fmul_rn(2.f, y)));
+}
+
+struct G {
+  F2 v;
+  float r, s;
+};
+__device__ __forceinline__ G operator+(G a, G b) { return {f2_add(a.v, b.v), a.r + b.r, a.s + b.s}; }
+__device__ __forceinline__ G operator-(G a, G b) {
+  return {f2_add(a.v, f2_neg(b.v)), a.r - b.r, a.s - b.s};
+}
+__device__ __forceinline__ G operator*(G a, G b) {
+  return {f2_mul(a.v, b.v), fmaf(a.r, b.v.h, a.v.h * b.r), fmaf(a.s, b.v.h, a.v.h * b.s)};
+}
+__device__ __forceinline__ G operator/(G a, G b) {
+  const F2 q = f2_div(a.v, b.v);
+  const float iv = 1.f / b.v.h;
+  return {q, (a.r - q.h * b.r) * iv, (a.s - q.h * b.s) * iv};
+}
+__device__ __forceinline__ G operator*(double c, G a) {
+  const F2 cc = f2c(c);
+  return {f2_mul(cc, a.v), cc.h * a.r, cc.h * a.s};
+}
+__device__ __forceinline__ G operator+(double c, G a) { return {f2_add(f2c(c), a.v), a.r, a.s}; }
+__device__ __forceinline__ G operator-(double c, G a) {
+  return {f2_add(f2c(c), f2_neg(a.v)), -a.r, -a.s};
+}
+__device__ __forceinline__ G operator/(double c, G b) {
+  const F2 q = f2_div(f2c(c), b.v);
+  const float iv = 1.f / b.v.h;
+  return {q, -q.h * b.r * iv, -q.h * b.s * iv};
+}
+__device__ __forceinline__ G neg(G a) { return {f2_neg(a.v), -a.r, -a.s}; }
+__device__ __forceinline__ G mkg(double v) { return {f2c(v), 0.f, 0.f}; }
+__device__ __forceinline__ G gapply(G a, double f, float df) { return {f2(f), df * a.r, df * a.s}; }
+__device__ __forceinline__ G dlog(G a) { return gapply(a, log(to_d(a.v)), 1.f / a.v.h); }
+__device__ __forceinline__ G dexp(G a) {
+  const double e = exp(to_d(a.v));
+  return gapply(a, e, static_cast<float>(e));
+}
+__device__ __forceinline__ G dsqrt(G a) {
+  const F2 s = f2_sqrt(a.v);
+  const float d = 0.5f / s.h;
+  return {s, d * a.r, d * a.s};
+}
+__device__ __forceinline__ G datan(G a) {
+  return gapply(a, atan(to_d(a.v)), 1.f / fmaf(a.v.h, a.v.h, 1.f));
+}
+__device__ __forceinline__ G dasinh(G a) {
+  return gapply(a, asinh(to_d(a.v)), rsqrtf(fmaf(a.v.h, a.v.h, 1.f)));
+}
+
+// constants of either dual type
+template <class T> struct Num;
+template <> struct Num<D3> {
+  __device__ __forceinline__ static D3 c(double v) { return mk(v); }
+};
+template <> struct Num<G> {
+  __device__ __forceinline__ static G c(double v) { return mkg(v); }
+};
+
 constexpr double kPi = 3.14159265358979323846;
 
 // rho^(1/3) and friends from one cube root
-struct RhoPowers {
-  D3 r13, r43, rm13; // rho^(1/3), rho^(4/3), rho^(-1/3)
+template <class T> struct RhoPowers {
+  T r13, r43, rm13; // rho^(1/3), rho^(4/3), rho^(-1/3)
 };
-__device__ __forceinline__ RhoPowers rho_powers(D3 rho) {
+__device__ __forceinline__ RhoPowers<D3> rho_powers(D3 rho) {
   double c = cbrt(rho.v);
   D3 r13 = apply(rho, c, c / (3.0 * rho.v));
   D3 r43 = rho * r13;
   D3 rm13 = apply(rho, 1.0 / c, -1.0 / (3.0 * c * rho.v));
   return {r13, r43, rm13};
 }
+__device__ __forceinline__ RhoPowers<G> rho_powers(G rho) {
+  const double rv = to_d(rho.v);
+  const double c = cbrt(rv);
+  const float cf = static_cast<float>(c), rf = rho.v.h;
+  G r13 = gapply(rho, c, cf / (3.f * rf));
+  G r43 = rho * r13;
+  G rm13 = gapply(rho, 1.0 / c, -1.f / (3.f * cf * rf));
+  return {r13, r43, rm13};
+}
 
-__device__ __forceinline__ D3 slater(const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T slater(const RhoPowers<T> &P) {
   const double cx = 0.7385587663820224; // (3/4)(3/pi)^(1/3)
   return -cx * P.r43;
 }
 
-__device__ __forceinline__ D3 vwn_eps(D3 rs, double A, double b, double c, double x0) {
-  D3 x = dsqrt(rs);
-  D3 X = x * x + b * x + mk(c);
+template <class T>
+__device__ __forceinline__ T vwn_eps(T rs, double A, double b, double c, double x0) {
+  using N = Num<T>;
+  T x = dsqrt(rs);
+  T X = x * x + b * x + N::c(c);
   double X0 = x0 * x0 + b * x0 + c;
   double Q = sqrt(4.0 * c - b * b);
-  D3 at = datan(mk(Q) / (2.0 * x + mk(b)));
-  D3 t1 = dlog(x * x / X) + (2.0 * b / Q) * at;
-  D3 xm = x - mk(x0);
-  D3 t2 = dlog(xm * xm / X) + (2.0 * (b + 2.0 * x0) / Q) * at;
+  T at = datan(N::c(Q) / (2.0 * x + N::c(b)));
+  T t1 = dlog(x * x / X) + (2.0 * b / Q) * at;
+  T xm = x - N::c(x0);
+  T t2 = dlog(xm * xm / X) + (2.0 * (b + 2.0 * x0) / Q) * at;
   return A * (t1 - (b * x0 / X0) * t2);
 }
 
-__device__ __forceinline__ D3 rs_of(const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T rs_of(const RhoPowers<T> &P) {
   const double k = 0.6203504908994001; // (3/(4 pi))^(1/3)
   return k * P.rm13;
 }
 
-__device__ __forceinline__ D3 vwn5(D3 rho, const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T vwn5(T rho, const RhoPowers<T> &P) {
   return rho * vwn_eps(rs_of(P), 0.0310907, 3.72744, 12.9352, -0.10498);
 }
-__device__ __forceinline__ D3 vwn_rpa(D3 rho, const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T vwn_rpa(T rho, const RhoPowers<T> &P) {
   return rho * vwn_eps(rs_of(P), 0.0310907, 13.0720, 42.7198, -0.409286);
 }
 
-__device__ __forceinline__ D3 b88(D3 rho, D3 sigma, const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T b88(T rho, T sigma, const RhoPowers<T> &P) {
   const double beta = 0.0042;
   const double cs = 0.9305257363491000; // (3/2)(3/(4 pi))^(1/3)
   // spin density rho/2: (rho/2)^(4/3) = rho^(4/3) / 2^(4/3)
-  D3 r43s = 0.39685026299204984 * P.r43;
-  D3 x2 = (0.25 * sigma) / (r43s * r43s);
-  D3 x = dsqrt(x2);
-  D3 per = neg(cs * r43s) - beta * r43s * x2 / (1.0 + 6.0 * beta * x * dasinh(x));
+  T r43s = 0.39685026299204984 * P.r43;
+  T x2 = (0.25 * sigma) / (r43s * r43s);
+  T x = dsqrt(x2);
+  T per = neg(cs * r43s) - beta * r43s * x2 / (1.0 + 6.0 * beta * x * dasinh(x));
   return 2.0 * per;
 }
 
-__device__ __forceinline__ D3 lyp(D3 rho, D3 sigma, const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T lyp(T rho, T sigma, const RhoPowers<T> &P) {
   const double a = 0.04918, b = 0.132, c = 0.2533, d = 0.349;
   const double cf = 2.8712340001881915; // (3/10)(3 pi^2)^(2/3)
-  D3 den = 1.0 + d * P.rm13;
-  D3 E = dexp(neg(c * P.rm13));
-  D3 delta = c * P.rm13 + d * P.rm13 / den;
-  D3 rm53 = P.rm13 / P.r43; // rho^(-5/3)
-  D3 t1 = neg(a * rho / den);
-  D3 t2 = neg((a * b * cf) * rho * E / den);
-  D3 t3 = (a * b / 72.0) * (3.0 + 7.0 * delta) * sigma * rm53 * E / den;
+  T den = 1.0 + d * P.rm13;
+  T E = dexp(neg(c * P.rm13));
+  T delta = c * P.rm13 + d * P.rm13 / den;
+  T rm53 = P.rm13 / P.r43; // rho^(-5/3)
+  T t1 = neg(a * rho / den);
+  T t2 = neg((a * b * cf) * rho * E / den);
+  T t3 = (a * b / 72.0) * (3.0 + 7.0 * delta) * sigma * rm53 * E / den;
   return t1 + t2 + t3;
 }
 
-__device__ __forceinline__ D3 kf2_of(const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T kf2_of(const RhoPowers<T> &P) {
   const double k = 3.0936677262801355; // (3 pi^2)^(1/3)
-  D3 kf = k * P.r13;
+  T kf = k * P.r13;
   return kf * kf;
 }
 
-__device__ __forceinline__ D3 pbe_x(D3 rho, D3 sigma, const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T pbe_x(T rho, T sigma, const RhoPowers<T> &P) {
   const double kappa = 0.8040, mu = 0.2195149727645171;
-  D3 s2 = sigma / (4.0 * kf2_of(P) * rho * rho);
-  D3 F = (1.0 + kappa) - kappa / (1.0 + (mu / kappa) * s2);
+  T s2 = sigma / (4.0 * kf2_of(P) * rho * rho);
+  T F = (1.0 + kappa) - kappa / (1.0 + (mu / kappa) * s2);
   return slater(P) * F;
 }
 
-__device__ __forceinline__ D3 pbe_c(D3 rho, D3 sigma, const RhoPowers &P) {
+template <class T> __device__ __forceinline__ T pbe_c(T rho, T sigma, const RhoPowers<T> &P) {
+  using N = Num<T>;
   const double beta = 0.06672455060314922;
   const double gamma = 0.031090690869654897; // (1 - ln 2) / pi^2
   const double A = 0.0310907, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382,
                b4 = 0.49294;
-  D3 rs = rs_of(P);
-  D3 srs = dsqrt(rs);
-  D3 den = 2.0 * A * (b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs);
-  D3 eps = (-2.0 * A) * (1.0 + a1 * rs) * dlog(1.0 + mk(1.0) / den);
+  T rs = rs_of(P);
+  T srs = dsqrt(rs);
+  T den = 2.0 * A * (b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs);
+  T eps = (-2.0 * A) * (1.0 + a1 * rs) * dlog(1.0 + N::c(1.0) / den);
   const double k = 3.0936677262801355;
-  D3 kf = k * P.r13;
-  D3 ks2 = (4.0 / kPi) * kf;
-  D3 t2 = sigma / (4.0 * ks2 * rho * rho);
-  D3 Af = (beta / gamma) / (dexp(neg(eps) / mk(gamma)) - mk(1.0));
-  D3 At2 = Af * t2;
-  D3 H = gamma * dlog(1.0 + (beta / gamma) * t2 * (1.0 + At2) / (1.0 + At2 + At2 * At2));
+  T kf = k * P.r13;
+  T ks2 = (4.0 / kPi) * kf;
+  T t2 = sigma / (4.0 * ks2 * rho * rho);
+  T Af = (beta / gamma) / (dexp(neg(eps) / N::c(gamma)) - N::c(1.0));
+  T At2 = Af * t2;
+  T H = gamma * dlog(1.0 + (beta / gamma) * t2 * (1.0 + At2) / (1.0 + At2 + At2 * At2));
   return rho * (eps + H);
 }
 
 // Energy density of one component (before its mixture coefficient).
-__device__ __forceinline__ D3 component(int id, D3 rho, D3 sigma, const RhoPowers &P) {
+template <class T>
+__device__ __forceinline__ T component(int id, T rho, T sigma, const RhoPowers<T> &P) {
   switch (id) {
   case kLdaX:
     return slater(P);
@@ -204,7 +334,7 @@ __device__ __forceinline__ D3 component(int id, D3 rho, D3 sigma, const RhoPower
     return 0.08 * slater(P) + 0.72 * b88(rho, sigma, P) + 0.19 * vwn5(rho, P) +
            0.81 * lyp(rho, sigma, P);
   }
-  return mk(0.0);
+  return Num<T>::c(0.0);
 }
 
 } // namespace fn
@@ -219,12 +349,34 @@ __device__ __forceinline__ void eval_xc(const FuncSet &fs, double rho, double si
     return;
   fn::D3 r{rho, 1.0, 0.0};
   fn::D3 s{fmax(sigma, 1e-40), 0.0, 1.0};
-  fn::RhoPowers P = fn::rho_powers(r);
+  fn::RhoPowers<fn::D3> P = fn::rho_powers(r);
   for (int i = 0; i < fs.n; i++) {
     fn::D3 c = fn::component(fs.id[i], r, s, P);
     e += fs.coef[i] * c.v;
     vrho += fs.coef[i] * c.r;
     vsigma += fs.coef[i] * c.s;
+  }
+}
+
+// The mixed path's evaluator: double-float values and FP32 derivatives
+// (fn::G) where rho >= 1e-10 and sigma >= 1e-30; FP64 (eval_xc) elsewhere,
+// where intermediate powers of rho would leave the FP32 exponent range or
+// sigma meets the FP64 path's clamp.
+__device__ __forceinline__ void eval_xc_mixed(const FuncSet &fs, double rho, double sigma,
+                                              double &e, double &vrho, double &vsigma) {
+  if (!(rho >= 1e-10) || !(sigma >= 1e-30)) {
+    eval_xc(fs, rho, sigma, e, vrho, vsigma);
+    return;
+  }
+  fn::G r{fn::f2(rho), 1.f, 0.f};
+  fn::G s{fn::f2(sigma), 0.f, 1.f};
+  fn::RhoPowers<fn::G> P = fn::rho_powers(r);
+  e = vrho = vsigma = 0.0;
+  for (int i = 0; i < fs.n; i++) {
+    fn::G c = fn::component(fs.id[i], r, s, P);
+    e += fs.coef[i] * fn::to_d(c.v);
+    vrho += fs.coef[i] * static_cast<double>(c.r);
+    vsigma += fs.coef[i] * static_cast<double>(c.s);
   }
 }
 

@@ -39,7 +39,8 @@ __device__ __forceinline__ double leaf_max256(double v, double *sh) {
   return s;
 }
 
-template <bool DERIV>
+// MIXED: the mixed path's evaluator (double-float values, FP32 derivatives).
+template <bool DERIV, bool MIXED = false>
 __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__restrict__ pts,
                                                 size_t N, const FuncSet &fs, double thr,
                                                 const double *__restrict__ rho,
@@ -64,8 +65,12 @@ __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__r
       sigma = gx * gx + gy * gy + gz * gz;
     }
     double e = 0, vr = 0, vs = 0;
-    if (!skip)
-      eval_xc(fs, r, sigma, e, vr, vs);
+    if (!skip) {
+      if (MIXED)
+        eval_xc_mixed(fs, r, sigma, e, vr, vs);
+      else
+        eval_xc(fs, r, sigma, e, vr, vs);
+    }
     coef[idx] = 0.5 * w * vr;
     if (DERIV) {
       const double f = 2.0 * w * vs;

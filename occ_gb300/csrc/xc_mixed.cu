@@ -1316,8 +1316,8 @@ __global__ void __launch_bounds__(256) k_func_b(const MixTab *__restrict__ tabs,
   __shared__ double sh[8];
   const LeafItem li = litems[blockIdx.x];
   const MixTab &T = tabs[li.mol];
-  leaf_functional<DERIV>(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts), T.fs,
-                         T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
+  leaf_functional<DERIV, true>(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts),
+                               T.fs, T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
 }
 
 // The B operand of k_vxc_tma for one block, pre-split for 3xTF32 (tf32_split):
@@ -2399,5 +2399,58 @@ extern "C" int occ_xc_batch_get_result(occ_xc_context *ctx, occ_xc_batch *b, int
     cuda_check(cudaMemcpyAsync(exc2, B.dE[i], 2 * sizeof(double), cudaMemcpyDeviceToHost, st),
                "D2H");
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  });
+}
+
+namespace occx {
+namespace {
+__global__ void k_selftest_func(FuncSet fs, int n, const double *rho, const double *sigma,
+                                double *out64, double *outm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  double e, vr, vs;
+  eval_xc(fs, rho[i], sigma[i], e, vr, vs);
+  out64[3 * i] = e;
+  out64[3 * i + 1] = vr;
+  out64[3 * i + 2] = vs;
+  eval_xc_mixed(fs, rho[i], sigma[i], e, vr, vs);
+  outm[3 * i] = e;
+  outm[3 * i + 1] = vr;
+  outm[3 * i + 2] = vs;
+}
+} // namespace
+} // namespace occx
+
+// The FP64 and the mixed-path functional evaluators at n points (host
+// arrays; out64 / outm receive e, vrho, vsigma per point), for testing.
+extern "C" int occ_xc_selftest_functional(occ_xc_context *ctx, const char *method, int n,
+                                          const double *rho, const double *sigma,
+                                          double *out64, double *outm) {
+  if (!ctx || !method || n <= 0 || !rho || !sigma || !out64 || !outm)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return api_guard(ctx, [&] {
+    const FuncSet fs = parse_method(method);
+    cudaStream_t st = ctx->impl->stream;
+    double *d = nullptr;
+    const size_t bytes = static_cast<size_t>(n) * 8 * sizeof(double);
+    cuda_check(cudaMalloc(&d, bytes), "cudaMalloc");
+    try {
+      cuda_check(cudaMemcpyAsync(d, rho, n * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+      cuda_check(cudaMemcpyAsync(d + n, sigma, n * sizeof(double), cudaMemcpyHostToDevice, st),
+                 "H2D");
+      k_selftest_func<<<(n + 127) / 128, 128, 0, st>>>(fs, n, d, d + n, d + 2 * n, d + 5 * n);
+      cuda_check(cudaGetLastError(), "kernel launch");
+      cuda_check(cudaMemcpyAsync(out64, d + 2 * n, 3 * n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, st), "D2H");
+      cuda_check(cudaMemcpyAsync(outm, d + 5 * n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost,
+                                 st), "D2H");
+      cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    } catch (...) {
+      cudaFree(d);
+      throw;
+    }
+    cudaFree(d);
   });
 }
