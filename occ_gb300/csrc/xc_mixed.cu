@@ -1311,7 +1311,7 @@ __device__ __forceinline__ double bsum256(double v, double *sh) {
 }
 
 template <bool DERIV>
-__global__ void __launch_bounds__(256) k_func_b(const MixTab *__restrict__ tabs,
+__global__ void __launch_bounds__(256, 2) k_func_b(const MixTab *__restrict__ tabs,
                                                 const LeafItem *__restrict__ litems) {
   __shared__ double sh[8];
   const LeafItem li = litems[blockIdx.x];
