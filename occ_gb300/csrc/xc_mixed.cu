@@ -989,22 +989,23 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 // One CTA per SM, persistent over V items (AO rows i0 .. i0 + 127 of the
 // blocks of one leaf; K = their points) fetched from a global queue and
 // handed to the roles through a ring in shared memory:
-//   warp 4       TMA producer: per K chunk of 32 points, hi and lo of the A
+//   warp 8       TMA producer: per K chunk of 32 points, hi and lo of the A
 //                rows (phi, split by k_colloc_f32) and of the B rows (Y,
 //                split by k_ymix), as
 //                32 x 32 FP32 boxes with the 128-byte swizzle
-//   warp 5       MMA issuer: hi*hi + hi*lo + lo*hi ("3xTF32") into one of two
+//   warp 9       MMA issuer: hi*hi + hi*lo + lo*hi ("3xTF32") into one of two
 //                TMEM accumulators of 256 columns; for a leaf with at most
 //                128 AOs also K^T (A and B swapped) beside it
-//   warps 0-3    epilogue: TMEM -> FP64 atomics, coalesced along the rows,
+//   warps 0-7    epilogue (two warps per TMEM lane quarter, each half of the
+//                columns): TMEM -> FP64 atomics, coalesced along the rows,
 //                into A with V_xc = A + A^T (K + K^T summed in registers and
 //                added once per pair when K^T was formed)
 // Stages and accumulators are double-buffered, so loads, MMAs and atomics of
 // consecutive chunks and passes overlap.  Every wait is bounded; on expiry
 // the error flag is set and all roles leave.
 constexpr int kItemBlocks = 2;   // blocks of a leaf accumulated in one V item
-constexpr int kVxcEpi = 128;     // epilogue threads (warps 0-3)
-constexpr int kVxcThreads = 192; // + producer warp + MMA warp
+constexpr int kVxcEpi = 256;     // epilogue threads (warps 0-7)
+constexpr int kVxcThreads = 320; // + producer warp + MMA warp
 constexpr int kVxcMap = 2048;    // AO maps up to this size are staged in shared memory
 
 struct alignas(16) VxcSmem {
@@ -1035,18 +1036,18 @@ __device__ __forceinline__ VxcWork vxc_work(const MixTab *tabs, const MBlock *bl
   return w;
 }
 
-__device__ __forceinline__ void epi_bar() { // the 128 epilogue threads
-  asm volatile("bar.sync 1, 128;" ::: "memory");
+__device__ __forceinline__ void epi_bar() { // the epilogue threads
+  asm volatile("bar.sync 1, %0;" ::"n"(kVxcEpi) : "memory");
 }
-// AND of v over the 128 epilogue threads (a barrier among them as well).
+// AND of v over the epilogue threads (a barrier among them as well).
 __device__ __forceinline__ bool epi_all(bool v) {
   uint32_t r;
   asm volatile("{\n\t.reg .pred p, q;\n\t"
                "setp.ne.u32 p, %1, 0;\n\t"
-               "barrier.red.and.pred q, 1, 128, p;\n\t"
+               "barrier.red.and.pred q, 1, %2, p;\n\t"
                "selp.u32 %0, 1, 0, q;\n\t}"
                : "=r"(r)
-               : "r"(static_cast<uint32_t>(v))
+               : "r"(static_cast<uint32_t>(v)), "n"(kVxcEpi)
                : "memory");
   return r != 0;
 }
@@ -1090,8 +1091,8 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     return ok;
   };
   // the epilogue warps issue warp-collective TMEM loads and share barriers:
-  // all 128 of their threads take every decision to stop together
-  const bool epi = warp < 4;
+  // all of their threads take every decision to stop together
+  const bool epi = warp < 8;
   auto agree = [&] {
     if (epi)
       ok = epi_all(ok);
@@ -1108,7 +1109,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     return it;
   };
 
-  if (warp == 4) {
+  if (warp == 8) {
     // ---- TMA producer (lane 0) ----
     if (lane == 0) {
       uint32_t g = 0; // chunks issued
@@ -1162,7 +1163,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       for (uint32_t q = (g >= 2 ? g - 2 : 0); q < g; q++)
         umma::mbar_wait(&sm->full[q & 1], (q >> 1) & 1, kWaitIter);
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     // ---- MMA issuer (lane 0) ----
     if (lane == 0) {
       uint32_t g = 0, pc = 0; // chunks consumed, passes
@@ -1219,8 +1220,8 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       }
     }
   } else {
-    // ---- epilogue (warps 0-3) ----
-    const int quad = warp;
+    // ---- epilogue (warps 0-7) ----
+    const int quad = warp & 3, half = warp >> 2;
     const int i = quad * 32 + lane; // row of the tile
     uint32_t pc = 0;
     for (int k = 0; ok; k++) {
@@ -1255,7 +1256,8 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
           break;
         umma::fence_after_sync();
         const uint32_t lanebase = tmem + (static_cast<uint32_t>(quad * 32) << 16) + buf * 256;
-        for (int c0 = 0; c0 < N; c0 += 16) {
+        const int cols = N / 2; // a multiple of 16
+        for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
           uint32_t r[16], rt[16];
           umma::tmem_ld16(lanebase + c0, r);
           if (W.sym)
