@@ -665,11 +665,11 @@ __global__ void __launch_bounds__(256) k_symmetrize(const MixTab *__restrict__ t
 // 512 AOs, acc2 collects the tail products (at most 2^-15 of the result).
 // One CTA per SM, persistent over blocks (most AOs first) from a global
 // queue, with a ring of block indices in shared memory and these roles:
-//   warp 8       block fetch, and per K chunk of 32 AOs one bulk copy of the
+//   warp 12      block fetch, and per K chunk of 32 AOs one bulk copy of the
 //                block's precomputed A slices (k_colloc_f32)
-//   warps 4-7    B producers: D2 (hi, lo) gathered through the block's AO map
+//   warps 4-11   B producers: D2 (hi, lo) gathered through the block's AO map
 //                for 64 columns j x 32 AOs k, sliced with t_j, into the stage
-//   warp 9       MMA issuer: eight TF32 MMAs per K step into acc0..acc2 of one
+//   warp 13      MMA issuer: eight TF32 MMAs per K step into acc0..acc2 of one
 //                of two TMEM buffers (3 x 64 columns each)
 //   warps 0-3    epilogue, one point per thread: X = acc0 + acc1 + acc2 and
 //                compensated FP32 dot products with phi and grad phi; rho
@@ -680,8 +680,8 @@ constexpr int kRhoN = 64;                                  // columns j per pass
 constexpr uint32_t kRhoStageB = 3 * (kRhoN * 128);        // B slices (64 x 32 each)
 constexpr uint32_t kRhoStage = kRhoStageA + kRhoStageB;   // 72 KB
 constexpr int kRhoStages = 3;
-constexpr int kRhoThreads = 320;
-constexpr int kRhoProd = 128;  // B producer threads (warps 4-7)
+constexpr int kRhoThreads = 448;
+constexpr int kRhoProd = 256;  // B producer threads (warps 4-11)
 constexpr int kRhoEpi = 128;   // epilogue threads (warps 0-3)
 constexpr int kRhoMap = 1024;  // AO maps up to this size are staged in shared memory
 
@@ -752,7 +752,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     return ok;
   };
   // groups that share named barriers take every decision to stop together
-  const bool epi = warp < 4, prod = warp >= 4 && warp < 8;
+  const bool epi = warp < 4, prod = warp >= 4 && warp < 12;
   auto agree = [&] {
     if (epi)
       ok = bar_all(1, kRhoEpi, ok);
@@ -772,7 +772,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
   auto segs = [](int mp) { return (mp + kExactKSeg - 1) / kExactKSeg; };
   auto seg_chunks = [](int mp, int k0) { return min(kExactKSeg, mp - k0) / kKc; };
 
-  if (warp == 8) {
+  if (warp == 12) {
     // ---- block fetch and A slices (lane 0) ----
     if (lane == 0) {
       uint32_t g = 0;
@@ -812,7 +812,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     // ---- B producers ----
     const int pt = t - 128;
     const int jr = pt & 63;        // row j of the B tile this thread fills
-    const int qb = pt >> 6;        // first 16-byte chunk; then qb + 2, + 4, + 6
+    const int qb = pt >> 6;        // first 16-byte chunk (0..3); then qb + 4
     uint32_t g = 0;
     for (int k = 0; ok; k++) {
       const int bi = next_block(k);
@@ -844,20 +844,20 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
             if (use > 0 && !wait(&sm->empty[s], (use - 1) & 1))
               break;
             uint8_t *st = smem + s * kRhoStage + kRhoStageA;
-            float2 d[4][4];
+            float2 d[2][4];
 #pragma unroll
-            for (int r = 0; r < 4; r++)
+            for (int r = 0; r < 2; r++)
 #pragma unroll
               for (int e = 0; e < 4; e++) {
-                const int lk = k0 + c * kKc + (qb + 2 * r) * 4 + e;
+                const int lk = k0 + c * kKc + (qb + 4 * r) * 4 + e;
                 d[r][e] = (jv && lk < L.nbf) ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
                                              : make_float2(0.f, 0.f);
               }
 #pragma unroll
-            for (int r = 0; r < 4; r++) {
+            for (int r = 0; r < 2; r++) {
               const float v[4] = {d[r][0].x, d[r][1].x, d[r][2].x, d[r][3].x};
               const float lo[4] = {d[r][0].y, d[r][1].y, d[r][2].y, d[r][3].y};
-              store4_exact(st, st + kRhoN * 128, st + 2 * kRhoN * 128, jr, qb + 2 * r, v, sB,
+              store4_exact(st, st + kRhoN * 128, st + 2 * kRhoN * 128, jr, qb + 4 * r, v, sB,
                            isB, lo);
             }
             umma::fence_proxy_async();
@@ -865,7 +865,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
           }
       }
     }
-  } else if (warp == 9) {
+  } else if (warp == 13) {
     // ---- MMA issuer (lane 0) ----
     if (lane == 0) {
       uint32_t g = 0, sc = 0; // chunks, segments
