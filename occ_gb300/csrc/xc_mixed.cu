@@ -957,11 +957,13 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
               const float x = __fadd_rn(__uint_as_float(r0[i]),
                                         __fadd_rn(__uint_as_float(r1[i]), __uint_as_float(r2[i])));
               const size_t o = static_cast<size_t>(n0 + c0 + i) * kBlockPts + p;
+              // rho (the energy's direct input) with compensation; its
+              // gradient, which enters through sigma, by plain FP32 FMAs
               dot2_step(phi[o], x, acc[0], cmp[0]);
               if (DERIV) {
-                dot2_step(phi[plane + o], x, acc[1], cmp[1]);
-                dot2_step(phi[2 * plane + o], x, acc[2], cmp[2]);
-                dot2_step(phi[3 * plane + o], x, acc[3], cmp[3]);
+                acc[1] = fmaf(phi[plane + o], x, acc[1]);
+                acc[2] = fmaf(phi[2 * plane + o], x, acc[2]);
+                acc[3] = fmaf(phi[3 * plane + o], x, acc[3]);
               }
             }
           }
