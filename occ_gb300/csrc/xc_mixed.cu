@@ -17,7 +17,8 @@
 //                  segments of <= 512), epilogue rho = rowsum(phi o X),
 //                  grad rho = 2 rowsum(grad phi o X)   (src/gto/density.cpp:33-43)
 //   k_func         FP64 functional per leaf (shared with the FP64 path)
-//   k_ymix         Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi per block
+//                  and, in the same launch, Y = 0.5 w vrho phi + 2 w vsigma
+//                  grad rho . grad phi per block (ymix_block)
 //   k_vxc_tma      K = phi^T Y (M = 128 AOs, N <= 256, K = the points of up to
 //                  two blocks of a leaf), operands by TMA, V += K + K^T with
 //                  FP64 atomics   (src/dft/xc_potential_matrix.cpp:19-41)
@@ -102,7 +103,7 @@ constexpr uint32_t kWaitIter = 1u << 24; // bounded mbarrier waits
 constexpr uint32_t kRhoStageA = 3 * 16384; // exact-grid A slices of one K chunk (128 x 32 each)
 constexpr int kErrTimeout = 1;
 // AO planes of a block, [plane][mp][128] FP32 each: phi, d/dx, d/dy, d/dz
-// (k_colloc_f32), hi and lo of Y (k_ymix, per build) and of phi (k_colloc_f32),
+// (k_colloc_f32), hi and lo of Y (ymix_block, per build) and of phi (k_colloc_f32),
 // then three planes' worth of the exact-grid slices of phi as the density
 // GEMM's A operand: per K chunk of 32 AOs, three 128 x 32 K-major tiles in
 // the 128-byte-swizzled layout of shared memory (k_colloc_f32), so that
@@ -993,7 +994,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 // handed to the roles through a ring in shared memory:
 //   warp 8       TMA producer: per K chunk of 32 points, hi and lo of the A
 //                rows (phi, split by k_colloc_f32) and of the B rows (Y,
-//                split by k_ymix), as
+//                split by ymix_block), as
 //                32 x 32 FP32 boxes with the 128-byte swizzle
 //   warp 9       MMA issuer: hi*hi + hi*lo + lo*hi ("3xTF32") into one of two
 //                TMEM accumulators of 256 columns; for a leaf with at most
@@ -1297,42 +1298,11 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     umma::tmem_dealloc(tmem, 512);
 }
 
-// Functional per leaf (one CTA per leaf item), the batched counterpart of the
-// FP64 path's k_func: block skip, FP64 functional, weights, coefficients and
-// the per-leaf energy / electron-count partials.
-__device__ __forceinline__ double bsum256(double v, double *sh) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
-    v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0)
-    sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double s = 0.0;
-  for (int i = 0; i < 8; i++)
-    s += sh[i];
-  __syncthreads();
-  return s;
-}
-
-template <bool DERIV>
-__global__ void __launch_bounds__(256, 2) k_func_b(const MixTab *__restrict__ tabs,
-                                                const LeafItem *__restrict__ litems) {
-  __shared__ double sh[8];
-  const LeafItem li = litems[blockIdx.x];
-  const MixTab &T = tabs[li.mol];
-  leaf_functional<DERIV, true>(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts),
-                               T.fs, T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
-}
-
 // The B operand of k_vxc_tma for one block, pre-split for 3xTF32 (tf32_split):
 // Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi (FP32) into the Y hi / lo
-// planes.  One CTA per block; streams 4 planes in, 2 out.
+// planes; streams 4 planes in, 2 out.  Run by a whole CTA; cf holds 128 float4.
 template <bool DERIV>
-__global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
-                                              const MBlock *__restrict__ blocks) {
-  __shared__ float4 cf[kBlockPts]; // (c0, c1, c2, c3) per point
-  const MBlock B = blocks[blockIdx.x];
-  const MixTab &T = tabs[B.mol];
+__device__ __forceinline__ void ymix_block(const MixTab &T, const MBlock &B, float4 *cf) {
   if (threadIdx.x < kBlockPts) {
     const int p = threadIdx.x;
     float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1379,6 +1349,42 @@ __global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
     base[kPlaneYHi * plane + q] = yh;
     base[kPlaneYLo * plane + q] = yl;
   }
+  __syncthreads(); // cf is reused by the next block
+}
+
+// Functional per leaf (one CTA per leaf item), the batched counterpart of the
+// FP64 path's k_func: block skip, FP64 functional, weights, coefficients and
+// the per-leaf energy / electron-count partials.
+__device__ __forceinline__ double bsum256(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < 8; i++)
+    s += sh[i];
+  __syncthreads();
+  return s;
+}
+
+// ... followed by the V_xc operand Y of each of the leaf's blocks (ymix_block):
+// the FP64-bound functional of one CTA overlaps the HBM-bound Y streaming of
+// the other CTA on the SM.
+template <bool DERIV>
+__global__ void __launch_bounds__(256, 2) k_func_b(const MixTab *__restrict__ tabs,
+                                                const MBlock *__restrict__ blocks,
+                                                const LeafItem *__restrict__ litems) {
+  __shared__ double sh[8];
+  __shared__ float4 cf[kBlockPts];
+  const LeafItem li = litems[blockIdx.x];
+  const MixTab &T = tabs[li.mol];
+  leaf_functional<DERIV, true>(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts),
+                               T.fs, T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
+  __syncthreads(); // the leaf's coefficients are written
+  for (int b = 0; b < li.nblk; b++)
+    ymix_block<DERIV>(T, blocks[li.block0 + b], cf);
 }
 
 // Fixed-order FP64 sums of the per-leaf partials, one CTA per molecule.
@@ -1675,7 +1681,7 @@ int num_sms(int device) {
   return n;
 }
 
-// The mixed launch sequence of a plan (8 kernels whatever the molecule count).
+// The mixed launch sequence of a plan (7 kernels whatever the molecule count).
 void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st, int max_ctas) {
   const int nmol = static_cast<int>(P.tabs.size());
   const int nb = static_cast<int>(P.blocks.size());
@@ -1705,16 +1711,9 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
   if (nl > 0)
     c.launch("func", st, [&] {
       if (P.deriv)
-        k_func_b<true><<<nl, 256, 0, st>>>(P.d_tabs, P.d_litems);
+        k_func_b<true><<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
       else
-        k_func_b<false><<<nl, 256, 0, st>>>(P.d_tabs, P.d_litems);
-    });
-  if (nb > 0)
-    c.launch("ymix", st, [&] {
-      if (P.deriv)
-        k_ymix<true><<<nb, 256, 0, st>>>(P.d_tabs, P.d_blocks);
-      else
-        k_ymix<false><<<nb, 256, 0, st>>>(P.d_tabs, P.d_blocks);
+        k_func_b<false><<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
     });
   if (ni > 0)
     c.launch("vxc_mixed", st, [&] {
