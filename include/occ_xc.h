@@ -206,9 +206,11 @@ void occ_xc_graph_destroy(occ_xc_graph *graph);
  * iteration and collects V_xc / E_xc by ticket.  A worker thread owns the
  * GPU: each tick it takes the oldest pending build of up to max_batch
  * sessions (one per session, so a session's builds run in submission order)
- * and runs them through one launch sequence.  A session's device state is
- * materialised when it is admitted, which happens only while the admitted
- * sessions' device bytes (an upper bound computed at open) fit the budget;
+ * and runs them through one launch sequence.  A session's device state --
+ * grid, screening and a workspace in which its AO values stay resident
+ * across iterations -- is materialised when it is admitted, which happens
+ * only while the admitted sessions' device bytes (an upper bound computed at
+ * open) fit the budget and its workspace fits the device pool;
  * a session that could never fit is refused at open with OCC_XC_ERR_NOMEM.
  * Closing a session frees its device state after its pending builds.  All
  * calls are thread-safe; errors are described by occ_xc_server_last_error()
@@ -219,6 +221,9 @@ typedef struct {
   int queue_capacity;      /* pending builds before submit returns BUSY (4096) */
   int max_batch;           /* builds per tick (64) */
   int precision;           /* OCC_XC_MIXED */
+  double pool_bytes;       /* device pool of the sessions' workspaces, allocated at the
+                              first admission (0: the budget, at most 40 % of the
+                              memory free then) */
 } occ_xc_server_settings;
 typedef struct {
   long completed, failed, pending, ticks;
@@ -257,8 +262,8 @@ int occ_xc_server_close(occ_xc_server *server, uint64_t session);
 /* paused != 0: no new ticks start (submissions still queue). */
 int occ_xc_server_pause(occ_xc_server *server, int paused);
 /* Molecule figures of the session; device_bytes = bytes held now (0 until
- * admitted).  Sessions hold only their resident state: per-build workspaces
- * come from one server-owned workspace sized for each tick. */
+ * admitted), resident_bytes = its admission charge (resident state, upper
+ * bound, plus its workspace in the pool, where its AO values stay resident). */
 int occ_xc_server_session_info(occ_xc_server *server, uint64_t session,
                                occ_xc_molecule_info *out, int *admitted);
 int occ_xc_server_stats_get(occ_xc_server *server, occ_xc_server_stats *out);

@@ -249,8 +249,8 @@ void Molecule::prepare(int precision) {
 }
 
 void Molecule::build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st,
-                          double *ws) {
-  bool skip_colloc = false;
+                          double *ws, bool ws_holds_ao) {
+  bool skip_colloc = ws && ws_holds_ao;
   if (!ws) {
     ensure_fp64_ws();
     ws = d_ws;

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+
 #include "../../include/occ_xc.h"
 #include "host/xc_host.hpp"
 #include "xc_device.cuh"
@@ -147,9 +149,10 @@ struct Molecule {
   void prepare(int precision); // the private workspace of `precision` (before a capture)
   MolDev dev() const;
   void build(int precision, const double *dD, double *dV, double *dout2, cudaStream_t st);
-  // ws: an FP64 workspace of fp64_workspace_bytes() (nullptr: the private one)
+  // ws: an FP64 workspace of fp64_workspace_bytes() (nullptr: the private one);
+  // ws_holds_ao: ws already holds this molecule's AO values
   void build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st,
-                  double *ws = nullptr);
+                  double *ws = nullptr, bool ws_holds_ao = false);
   void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
 };
 
@@ -179,6 +182,16 @@ void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListAren
                        char *d_ws, int *d_err, cudaStream_t st);
 // Bytes of the shared workspace mixed_build_group needs for `mols` (d_ws).
 size_t group_workspace_bytes(const std::vector<Molecule *> &mols);
+// The same over workspaces that persist in a pool (the server's sessions):
+// ws[i] is molecule i's region (mixed_workspace_bytes, 512-byte aligned from
+// pool), ao_valid[i] says it already holds the molecule's AO values, and
+// pool_map is encode_ws_map of the whole pool.
+void mixed_build_in_pool(Context &c, const std::vector<Molecule *> &mols,
+                         const std::vector<char *> &ws, const std::vector<int> &ao_valid,
+                         const char *pool, const CUtensorMap &pool_map, ListArena &arena,
+                         int *d_err, cudaStream_t st);
+// Tensor map of a workspace region as rows of 128 FP32.
+void encode_ws_map(CUtensorMap &map, const void *base, size_t bytes);
 
 } // namespace occx
 

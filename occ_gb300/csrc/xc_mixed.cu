@@ -150,6 +150,7 @@ struct MixTab {
   double *out2;         // {E_xc, integrated density}
   int vxc_n;            // N of the V_xc tile (64, 128 or 256)
   long long ws_row0;    // row of ws in the launch's tensor map (rows of 128 floats)
+  int ao_valid;         // ws already holds this molecule's AO values: no collocation
 };
 
 // Per-launch replacement of a one-molecule table's D / V / out2 (so that a
@@ -491,6 +492,8 @@ __global__ void __launch_bounds__(128, 3) k_colloc_f32(const MixTab *__restrict_
                                                     const MBlock *__restrict__ blocks) {
   const MBlock B = blocks[blockIdx.x];
   const MixTab &T = tabs[B.mol];
+  if (T.ao_valid)
+    return;
   const MolDev m = T.m;
   const float4 *__restrict__ prim32 = T.prim32;
   const float4 *__restrict__ shA = T.shA;
@@ -1586,6 +1589,7 @@ MixTab bind_ws(const Molecule &M, char *base, const char *map_base) {
   MixTab T = M.mixed->tab;
   T.ws = reinterpret_cast<float *>(base + L.ws);
   T.ws_row0 = static_cast<long long>((base + L.ws) - map_base) / (kBlockPts * sizeof(float));
+  T.ao_valid = 0;
   T.rowscale = reinterpret_cast<float *>(base + L.rowscale);
   T.dhl = reinterpret_cast<float2 *>(base + L.dhl);
   T.colb = reinterpret_cast<float *>(base + L.colb);
@@ -1886,24 +1890,24 @@ ListArena::~ListArena() {
     cudaFreeHost(h);
 }
 
-void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListArena &arena,
-                       char *d_ws, int *d_err, cudaStream_t st) {
+// One launch sequence per functional family over molecules whose workspaces
+// are already bound (tabs[i] for mols[i]) inside the region `map` covers.
+void mixed_build_bound(Context &c, const std::vector<Molecule *> &mols,
+                       const std::vector<MixTab> &bound, const CUtensorMap &map,
+                       ListArena &arena, int *d_err, cudaStream_t st) {
   LaunchPlan P[2];
   std::vector<Molecule *> group[2];
   std::vector<MixTab> tabs[2];
-  size_t wsoff = 0;
   for (size_t i = 0; i < mols.size(); i++) {
     for (size_t j = 0; j < i; j++)
       if (mols[j] == mols[i])
         throw ArgError("a molecule may appear only once in a group build");
     const int g = mols[i]->deriv ? 1 : 0;
     group[g].push_back(mols[i]);
-    tabs[g].push_back(bind_ws(*mols[i], d_ws + wsoff, d_ws));
-    wsoff += mols[i]->mixed_workspace_bytes();
+    tabs[g].push_back(bound[i]);
   }
   for (int g = 0; g < 2; g++)
-    if (!group[g].empty())
-      encode_ws_map(P[g].tmap, d_ws, wsoff);
+    P[g].tmap = map;
   // pack both plans' lists into the arena: one pinned staging area, one copy
   size_t off = 0;
   auto place = [&](size_t bytes) {
@@ -1956,6 +1960,32 @@ void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListAren
   for (int g = 0; g < 2; g++)
     if (!group[g].empty())
       run_plan(P[g], c, Override{nullptr, nullptr, nullptr}, d_err, st, c.max_ctas);
+}
+
+void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListArena &arena,
+                       char *d_ws, int *d_err, cudaStream_t st) {
+  std::vector<MixTab> tabs;
+  size_t wsoff = 0;
+  for (Molecule *M : mols) {
+    tabs.push_back(bind_ws(*M, d_ws + wsoff, d_ws));
+    wsoff += M->mixed_workspace_bytes();
+  }
+  CUtensorMap map;
+  encode_ws_map(map, d_ws, std::max<size_t>(wsoff, 512));
+  mixed_build_bound(c, mols, tabs, map, arena, d_err, st);
+}
+
+void mixed_build_in_pool(Context &c, const std::vector<Molecule *> &mols,
+                         const std::vector<char *> &ws, const std::vector<int> &ao_valid,
+                         const char *pool, const CUtensorMap &pool_map, ListArena &arena,
+                         int *d_err, cudaStream_t st) {
+  std::vector<MixTab> tabs;
+  for (size_t i = 0; i < mols.size(); i++) {
+    MixTab T = bind_ws(*mols[i], ws[i], pool);
+    T.ao_valid = ao_valid[i];
+    tabs.push_back(T);
+  }
+  mixed_build_bound(c, mols, tabs, pool_map, arena, d_err, st);
 }
 
 size_t group_workspace_bytes(const std::vector<Molecule *> &mols) {

@@ -13,8 +13,12 @@
 // A session is admitted -- its device state materialised -- only while the
 // sum of the admitted sessions' device bytes stays within the budget; a
 // session that does not fit waits (later, smaller ones may go first), one
-// that could never fit is refused at open.  Closing a session frees its
-// device state once its builds are done.
+// that could never fit is refused at open.  An admitted session keeps its
+// grid, weights, screening lists and its per-build workspace, AO values
+// included, resident until it closes: the AO values are computed on its first
+// build only.  The workspaces are carved from one device pool that one TMA
+// tensor map covers, so builds of any set of sessions share launches.
+// Closing a session frees its device state once its builds are done.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -39,8 +43,10 @@ thread_local std::string t_server_error;
 struct Session {
   uint64_t id = 0;
   std::unique_ptr<Molecule> mol;
-  double charge = 0.0; // admission charge: upper bound of the resident device bytes
-  size_t ws = 0;       // per-build workspace at the server's precision
+  double charge = 0.0; // admission charge: resident device bytes (upper bound) + ws
+  size_t ws = 0;       // workspace at the server's precision (AO values resident)
+  size_t ws_off = 0;   // its place in the pool while admitted
+  bool ao_valid = false;
   bool admitted = false;
   bool closing = false;
   long queued = 0; // builds submitted and not yet run
@@ -53,6 +59,45 @@ struct Job {
   Clock::time_point submitted, finished;
   int status = 1; // 1 pending, OCC_XC_OK done, < 0 failed
   std::string err;
+};
+
+// First-fit allocator of 512-byte-aligned ranges of the workspace pool.
+struct PoolAlloc {
+  std::map<size_t, size_t> free_; // offset -> bytes
+  void reset(size_t bytes) {
+    free_.clear();
+    if (bytes)
+      free_[0] = bytes;
+  }
+  bool alloc(size_t bytes, size_t &off) {
+    bytes = (bytes + 511) / 512 * 512;
+    for (auto it = free_.begin(); it != free_.end(); ++it)
+      if (it->second >= bytes) {
+        off = it->first;
+        const size_t rest = it->second - bytes;
+        free_.erase(it);
+        if (rest)
+          free_[off + bytes] = rest;
+        return true;
+      }
+    return false;
+  }
+  void release(size_t off, size_t bytes) {
+    bytes = (bytes + 511) / 512 * 512;
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
 };
 
 double pct(std::vector<double> v, double q) {
@@ -83,8 +128,10 @@ struct Server {
   long ticks = 0, tick_builds = 0, completed = 0, failed = 0;
   std::string fatal;
   ListArena arena;
-  char *d_ws = nullptr; // shared per-build workspace, sized for the tick
-  size_t ws_cap = 0;
+  char *pool = nullptr; // the sessions' workspaces (allocated at the first admission)
+  size_t pool_size = 0;
+  PoolAlloc pool_free;
+  CUtensorMap pool_map;
   int *d_err = nullptr;
   double *h_stage = nullptr; // pinned staging for D in / V out
   size_t stage_cap = 0;      // doubles
@@ -111,8 +158,24 @@ struct Server {
       cudaFreeHost(h_stage);
     if (d_err)
       cudaFree(d_err);
-    if (d_ws)
-      cudaFree(d_ws);
+    if (pool)
+      cudaFree(pool);
+  }
+
+  // The pool, at the first admission: settings.pool_bytes, or the budget,
+  // capped at 40 % of the device memory free then.
+  void ensure_pool() {
+    if (pool)
+      return;
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    double want = cfg.pool_bytes > 0 ? cfg.pool_bytes
+                                     : std::min(cfg.hbm_budget_bytes, 0.4 * static_cast<double>(fr));
+    const size_t bytes = std::max<size_t>(static_cast<size_t>(want) / 512 * 512, 512);
+    cuda_check(cudaMalloc(&pool, bytes), "cudaMalloc");
+    pool_size = bytes;
+    pool_free.reset(bytes);
+    encode_ws_map(pool_map, pool, bytes);
   }
 
   void stage(size_t doubles) {
@@ -130,12 +193,14 @@ struct Server {
   // Pick this tick's builds; sessions to admit are charged here and
   // materialised by the caller outside the lock.
   void select(std::vector<Job *> &tick, std::vector<Session *> &admit,
-              std::vector<std::unique_ptr<Session>> &retire, size_t &tick_ws) {
+              std::vector<std::unique_ptr<Session>> &retire) {
     for (auto it = sessions.begin(); it != sessions.end();) {
       Session &S = *it->second;
       if (S.closing && S.queued == 0) {
-        if (S.admitted)
+        if (S.admitted) {
           admitted_bytes -= S.charge;
+          pool_free.release(S.ws_off, S.ws);
+        }
         retire.push_back(std::move(it->second));
         it = sessions.erase(it);
       } else {
@@ -145,7 +210,6 @@ struct Server {
     if (paused)
       return;
     std::vector<uint64_t> taken;
-    tick_ws = 0;
     for (auto &kv : jobs) {
       Job &J = *kv.second;
       if (J.status != 1 || static_cast<int>(tick.size()) >= cfg.max_batch)
@@ -154,36 +218,29 @@ struct Server {
         continue; // one build per session per tick, in submission order
       taken.push_back(J.session);
       Session &S = *sessions.at(J.session);
-      // the tick's workspace: the sum over its molecules (one launch
-      // sequence) or the largest one (FP64 builds one after the other)
-      const size_t ws_after =
-          cfg.precision == OCC_XC_MIXED ? tick_ws + S.ws : std::max(tick_ws, S.ws);
-      const double resident_after = admitted_bytes + (S.admitted ? 0.0 : S.charge);
-      if (resident_after + static_cast<double>(ws_after) > cfg.hbm_budget_bytes)
-        continue; // waits for memory; a smaller session may go first
+      if (!S.admitted && S.ws > pool_size) { // can never be admitted
+        J.status = OCC_XC_ERR_NOMEM;
+        J.err = "the molecule's workspace is larger than the server's device pool";
+        J.finished = Clock::now();
+        pending--;
+        S.queued--;
+        failed++;
+        cv_done.notify_all();
+        continue;
+      }
       if (!S.admitted) {
+        if (admitted_bytes + S.charge > cfg.hbm_budget_bytes)
+          continue; // waits for memory; a smaller session may go first
+        if (!pool_free.alloc(S.ws, S.ws_off))
+          continue; // no room in the pool yet
         S.admitted = true;
+        S.ao_valid = false;
         admitted_bytes += S.charge;
+        peak_bytes = std::max(peak_bytes, admitted_bytes);
         admit.push_back(&S);
       }
-      tick_ws = ws_after;
       tick.push_back(&J);
     }
-  }
-
-  // Shared workspace of at least `need` bytes within the budget.
-  void workspace(size_t need) {
-    const bool over = admitted_bytes + static_cast<double>(ws_cap) > cfg.hbm_budget_bytes;
-    if (need <= ws_cap && !over)
-      return;
-    if (d_ws)
-      cudaFree(d_ws);
-    d_ws = nullptr;
-    ws_cap = 0;
-    cuda_check(cudaMalloc(&d_ws, std::max<size_t>(need, 256)), "cudaMalloc");
-    ws_cap = need;
-    std::lock_guard<std::mutex> lk(mu);
-    peak_bytes = std::max(peak_bytes, admitted_bytes + static_cast<double>(ws_cap));
   }
 
   void run() {
@@ -196,13 +253,20 @@ struct Server {
       std::vector<Job *> tick;
       std::vector<Session *> admit;
       std::vector<std::unique_ptr<Session>> retire;
-      size_t tick_ws = 0;
       {
         std::unique_lock<std::mutex> lk(mu);
         cv_work.wait(lk, [&] { return stop || work_ready(); });
         if (stop)
           return;
-        select(tick, admit, retire, tick_ws);
+        if (!pool) {
+          try {
+            ensure_pool();
+          } catch (const std::exception &e) {
+            fatal = e.what();
+            return;
+          }
+        }
+        select(tick, admit, retire);
       }
       retire.clear(); // device memory freed outside the lock
       if (tick.empty()) {
@@ -212,7 +276,7 @@ struct Server {
         cv_work.wait_for(lk, std::chrono::milliseconds(50));
         continue;
       }
-      execute(tick, admit, tick_ws);
+      execute(tick, admit);
     }
   }
 
@@ -246,7 +310,7 @@ struct Server {
     cv_work.notify_all();
   }
 
-  void execute(std::vector<Job *> &tick, std::vector<Session *> &admit, size_t tick_ws) {
+  void execute(std::vector<Job *> &tick, std::vector<Session *> &admit) {
     // materialise newly admitted sessions; one that does not get its memory
     // (the budget is an accounting limit, the device may hold less) is
     // returned to the waiting state and its build fails with NOMEM
@@ -259,6 +323,7 @@ struct Server {
         std::lock_guard<std::mutex> lk(mu);
         S->admitted = false;
         admitted_bytes -= S->charge;
+        pool_free.release(S->ws_off, S->ws);
         failed_sessions.push_back(S->id);
       }
     }
@@ -276,21 +341,16 @@ struct Server {
         return;
     }
     std::vector<Molecule *> mols;
+    std::vector<Session *> sess;
     {
       std::lock_guard<std::mutex> lk(mu);
-      for (Job *J : tick)
-        mols.push_back(sessions.at(J->session)->mol.get());
+      for (Job *J : tick) {
+        sess.push_back(sessions.at(J->session).get());
+        mols.push_back(sess.back()->mol.get());
+      }
     }
     cudaStream_t st = ctx->stream;
     try {
-      if (!failed_sessions.empty()) {
-        tick_ws = 0;
-        for (Molecule *M : mols)
-          tick_ws = cfg.precision == OCC_XC_MIXED
-                        ? tick_ws + M->mixed_workspace_bytes()
-                        : std::max(tick_ws, M->fp64_workspace_bytes());
-      }
-      workspace(tick_ws);
       size_t total = 0;
       for (Molecule *M : mols)
         total += 2 * static_cast<size_t>(M->basis.nbf) * M->basis.nbf + 2;
@@ -307,11 +367,20 @@ struct Server {
         off += 2 * n2 + 2;
       }
       if (cfg.precision == OCC_XC_MIXED) {
-        mixed_build_group(*ctx, mols, arena, d_ws, d_err, st);
+        std::vector<char *> ws;
+        std::vector<int> aov;
+        for (Session *S : sess) {
+          ws.push_back(pool + S->ws_off);
+          aov.push_back(S->ao_valid ? 1 : 0);
+        }
+        mixed_build_in_pool(*ctx, mols, ws, aov, pool, pool_map, arena, d_err, st);
       } else {
-        for (Molecule *M : mols)
-          M->build_fp64(M->d_D, M->d_V, M->d_out2, st, reinterpret_cast<double *>(d_ws));
+        for (Session *S : sess)
+          S->mol->build_fp64(S->mol->d_D, S->mol->d_V, S->mol->d_out2, st,
+                             reinterpret_cast<double *>(pool + S->ws_off), S->ao_valid);
       }
+      for (Session *S : sess)
+        S->ao_valid = true; // the launches above left the AO values in place
       for (size_t i = 0; i < mols.size(); i++) {
         Molecule &M = *mols[i];
         const size_t n2 = static_cast<size_t>(M.basis.nbf) * M.basis.nbf;
@@ -388,6 +457,7 @@ void occ_xc_default_server_settings(occ_xc_server_settings *s) {
   if (!s)
     return;
   s->hbm_budget_bytes = 150e9;
+  s->pool_bytes = 0.0;
   s->queue_capacity = 4096;
   s->max_batch = 64;
   s->precision = OCC_XC_MIXED;
@@ -433,12 +503,14 @@ int occ_xc_server_open(occ_xc_server *srv, int natoms, const int *Z, const doubl
                    coefficients, pure, method, grid, build};
     auto sess = std::make_unique<Session>();
     sess->mol = molecule_host(S.ctx.get(), a); // host work on the caller's thread
-    sess->charge = sess->mol->estimate_resident_bytes();
     sess->ws = S.cfg.precision == OCC_XC_MIXED ? sess->mol->mixed_workspace_bytes()
                                                : sess->mol->fp64_workspace_bytes();
-    if (sess->charge + static_cast<double>(sess->ws) > S.cfg.hbm_budget_bytes) {
-      t_server_error = "molecule needs " +
-                       std::to_string((sess->charge + static_cast<double>(sess->ws)) / 1e9) +
+    sess->ws = (sess->ws + 511) / 512 * 512;
+    sess->charge = sess->mol->estimate_resident_bytes() + static_cast<double>(sess->ws);
+    const double cap = S.cfg.pool_bytes > 0 ? std::min(S.cfg.hbm_budget_bytes, S.cfg.pool_bytes)
+                                            : S.cfg.hbm_budget_bytes;
+    if (sess->charge > S.cfg.hbm_budget_bytes || static_cast<double>(sess->ws) > cap) {
+      t_server_error = "molecule needs " + std::to_string(sess->charge / 1e9) +
                        " GB of device memory, more than the server's budget";
       return static_cast<int>(OCC_XC_ERR_NOMEM);
     }
@@ -605,7 +677,7 @@ int occ_xc_server_session_info(occ_xc_server *srv, uint64_t session, occ_xc_mole
   out->npoints = M.plan.npts;
   out->nleaves = static_cast<long>(M.leaves.size());
   out->flops_per_build = M.flops;
-  out->device_bytes = it->second->admitted ? M.device_bytes : 0.0;
+  out->device_bytes = it->second->admitted ? M.device_bytes + it->second->ws : 0.0;
   out->workspace_bytes = static_cast<double>(M.fp64_workspace_bytes());
   out->mixed_workspace_bytes = static_cast<double>(M.mixed_workspace_bytes());
   out->resident_bytes = it->second->charge;
@@ -633,7 +705,7 @@ int occ_xc_server_stats_get(occ_xc_server *srv, occ_xc_server_stats *o) {
     (kv.second->admitted ? adm : wait)++;
   o->sessions_admitted = adm;
   o->sessions_waiting = wait;
-  o->admitted_bytes = S.admitted_bytes + static_cast<double>(S.ws_cap);
+  o->admitted_bytes = S.admitted_bytes;
   o->peak_admitted_bytes = S.peak_bytes;
   return OCC_XC_OK;
 }

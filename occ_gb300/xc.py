@@ -70,7 +70,7 @@ class _TuneResult(C.Structure):
 
 class _ServerSettings(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("queue_capacity", C.c_int),
-                ("max_batch", C.c_int), ("precision", C.c_int)]
+                ("max_batch", C.c_int), ("precision", C.c_int), ("pool_bytes", C.c_double)]
 
 
 class _ServerStats(C.Structure):
@@ -555,10 +555,10 @@ class Server:
     a device-memory budget (occ_xc_server_* in include/occ_xc.h)."""
 
     def __init__(self, device=0, hbm_budget_bytes=150e9, queue_capacity=4096, max_batch=64,
-                 precision=MIXED):
+                 precision=MIXED, pool_bytes=0.0):
         self.lib = library()
         cfg = _ServerSettings(float(hbm_budget_bytes), int(queue_capacity), int(max_batch),
-                              int(precision))
+                              int(precision), float(pool_bytes))
         h = C.c_void_p()
         rc = self.lib.occ_xc_server_create(device, C.byref(cfg), C.byref(h))
         if rc != 0:
