@@ -225,6 +225,42 @@ def leaf_stats(dft):
     return cnt, m
 
 
+def algorithmic_bytes(kernel, cnt, m, npts, nbf, deriv):
+    """Bytes a mixed-path kernel must move once per build in this layout
+    (each AO plane is FP32 [block][mp][128]):
+      rho_mixed  phi (+ gradient) planes and the three exact-grid A-slice
+                 planes read once, rho (+ gradient) written, D2 read once
+      func       rho and the grid read, Y hi / lo written from the phi
+                 (+ gradient) planes, coefficients written
+      vxc_mixed  phi hi / lo and Y hi / lo read once, V written once"""
+    blocks = np.ceil(cnt / 128.0)
+    mp = np.ceil(m / 32.0) * 32
+    pairs = float(np.sum(blocks * 128 * mp))  # point-AO entries of one plane
+    ncomp = 4 if deriv else 1
+    if kernel == "rho_mixed":
+        return (ncomp + 3) * 4 * pairs + 8 * ncomp * npts + 8.0 * nbf * nbf
+    if kernel == "func":
+        return (ncomp + 2) * 4 * pairs + (32 + 8 * ncomp + 8 * ncomp) * npts
+    if kernel == "vxc_mixed":
+        return 4 * 4 * pairs + 8.0 * nbf * nbf
+    return float("nan")
+
+
+def measured_traffic(kernel):
+    """dram__bytes_read.sum + dram__bytes_write.sum per launch of `kernel` on
+    this workload, from the ncu summary committed in profiles/ (None if
+    absent)."""
+    path = os.path.join(ROOT, "profiles", "mixed_traffic_water32_def2svp_pbe.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch") and f" {kernel} " in line:
+                    return float(line.split("=")[1].split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
 def cpu_baseline(basis, P, W, D, target_s=15.0):
     """Oracle (CPU restatement of the reference algorithm) on every host core,
     on a strided sample of leaves; scaled to builds/s by the sampled share of
@@ -375,10 +411,17 @@ def main():
                 "frac": None, "traffic": None, "kernel": dom_name,
                 "note": "FP64 DFMA pipe; MEASURED_PEAKS.json has no FP64 figure"}
     else:
-        peak = peaks.get("bf16_tflops", 1900.0)
-        achieved = 3 * 2 * flops_half / (dom_avg_ms / 1e3) / 1e12  # 3 TF32 products, bf16-equivalent
-        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "kernel": dom_name}
+        cnt, m = leaf_stats(dft)
+        nbytes = algorithmic_bytes(dom_name, cnt, m, info["npoints"], nbf, info["deriv"])
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = nbytes / (dom_avg_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": measured_traffic(dom_name),
+                "kernel": dom_name, "algorithmic_bytes": nbytes,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                # the contraction it carries, for reference (not the bound)
+                "useful_tflops": (flops_half / (dom_avg_ms / 1e3) / 1e12
+                                  if dom_name in ("rho_mixed", "vxc_mixed") else None)}
     roof["kernel_share"] = dom_ms / tot if tot else None
     roof["kernels_ms_per_build"] = {k: v[0] / v[1] for k, v in prof.items()}
 
