@@ -78,7 +78,7 @@ def collocation(l, pure, exps, coefs, origin, xyz, deriv=1):
     origin = np.ascontiguousarray(origin, dtype=np.float64)
     xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
     nf = 2 * l + 1 if pure else (l + 1) * (l + 2) // 2
-    out = np.zeros((4 if deriv else 1, nf, len(xyz)))
+    out = np.zeros(({0: 1, 1: 4, 2: 10}[int(deriv)], nf, len(xyz)))
     lib().oracle_collocation(l, int(pure), len(exps), _p(exps), _p(coefs), _p(origin), len(xyz),
                              _p(xyz), int(deriv), _p(out))
     return out
@@ -134,3 +134,29 @@ def xc_build(basis, points, weights, D, method, screen=1e-10, density_threshold=
     if rc != 0:
         raise RuntimeError(f"oracle_xc_build failed ({rc})")
     return exc.value, V, nel.value
+
+
+def xc_gradient(basis, points, weights, D, method, screen=1e-10, density_threshold=1e-10,
+                leaf=(128, 32, 256), nthreads=0):
+    """dE_xc/dR (natoms x 3, Hartree/Bohr) for mo.D = D, grid weights fixed
+    (include/occ/dft/dft.h:599-749)."""
+    l, nprim, off, exps, coefs, origin = _basis_arrays(basis)
+    atom = np.array([s.atom for s in basis.shells], dtype=np.int32)
+    natoms = len(basis.atoms())
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    Df = np.asfortranarray(D, dtype=np.float64)
+    ids = np.array(METHODS[method.lower()], dtype=np.int32)
+    coef = np.ones(len(ids))
+    g = np.zeros(3 * natoms)
+    L = lib()
+    L.oracle_xc_gradient.restype = C.c_int
+    rc = L.oracle_xc_gradient(len(l), _p(l, _ip), _p(nprim, _ip), _p(off, _ip), _p(exps),
+                              _p(coefs), _p(origin), _p(atom, _ip), natoms, int(basis.pure),
+                              len(w), _p(pts), _p(w), Df.ctypes.data_as(_dp), len(ids),
+                              _p(ids, _ip), _p(coef), C.c_double(screen),
+                              C.c_double(density_threshold), C.c_long(leaf[0]),
+                              C.c_long(leaf[1]), C.c_long(leaf[2]), nthreads, _p(g))
+    if rc != 0:
+        raise RuntimeError(f"oracle_xc_gradient failed ({rc})")
+    return g.reshape(natoms, 3)

@@ -83,10 +83,23 @@ inline double ipow(double x, int n) {
   return r;
 }
 
+// d^k/dx^k of x^a (k = 0, 1, 2), 0 where the power runs out.
+inline double dpow(double x, int a, int k) {
+  if (k == 0)
+    return ipow(x, a);
+  if (k == 1)
+    return a > 0 ? a * ipow(x, a - 1) : 0.0;
+  return a > 1 ? a * (a - 1) * ipow(x, a - 2) : 0.0;
+}
+
 // Collocation of one shell at points; out[comp][func][p], comp 0 = value,
-// 1..3 = d/dx, d/dy, d/dz.  Restates what src/gto/gto.cpp:212-287 obtains from
-// gau2grid (contracted Cartesian Gaussians, CCA order, optional spherical
-// transform) including the common_fac scaling.
+// 1..3 = d/dx, d/dy, d/dz and, for deriv 2, 4..9 = d2/dxx, dxy, dxz, dyy,
+// dyz, dzz (the order of OCC's GTOValues).  Restates what src/gto/gto.cpp
+// :212-287 obtains from gau2grid (contracted Cartesian Gaussians, CCA order,
+// optional spherical transform) including the common_fac scaling.  With the
+// radial part R(s), s = r^2, dR = 2 R'(s) and d2R = 4 R''(s), the second
+// derivatives of M(x, y, z) R are M_ij R + (M_i x_j + M_j x_i) dR
+// + M (x_i x_j d2R + delta_ij dR).
 void collocate(int l, bool pure, int nprim, const double *exps, const double *coefs,
                const double *A, long n, const double *xyz, long stride, int deriv,
                double *out, long out_stride) {
@@ -96,16 +109,19 @@ void collocate(int l, bool pure, int nprim, const double *exps, const double *co
   if (pure)
     T = spherical_transform(l);
   const double fac = common_fac(l, pure);
-  std::vector<double> cart(4 * nc);
+  std::vector<double> cart(10 * nc);
+  static const int hi[6] = {0, 0, 0, 1, 1, 2}, hj[6] = {0, 1, 2, 1, 2, 2};
   for (long p = 0; p < n; p++) {
     double x = xyz[3 * p] - A[0], y = xyz[3 * p + 1] - A[1], z = xyz[3 * p + 2] - A[2];
     double r2 = x * x + y * y + z * z;
-    double R = 0.0, dR = 0.0;
+    double R = 0.0, dR = 0.0, d2R = 0.0;
     for (int k = 0; k < nprim; k++) {
       double e = coefs[k] * std::exp(-exps[k] * r2);
       R += e;
       dR += -2.0 * exps[k] * e;
+      d2R += 4.0 * exps[k] * exps[k] * e;
     }
+    const double r[3] = {x, y, z};
     for (int a = l; a >= 0; a--)
       for (int b = l - a; b >= 0; b--) {
         int c = l - a - b;
@@ -119,9 +135,22 @@ void collocate(int l, bool pure, int nprim, const double *exps, const double *co
           cart[nc + i] = gx * R + mono * x * dR;
           cart[2 * nc + i] = gy * R + mono * y * dR;
           cart[3 * nc + i] = gz * R + mono * z * dR;
+          if (deriv > 1) {
+            const double M1[3] = {gx, gy, gz};
+            const int pw[3] = {a, b, c};
+            for (int q = 0; q < 6; q++) {
+              const int u = hi[q], v = hj[q];
+              int k[3] = {0, 0, 0};
+              k[u]++;
+              k[v]++;
+              const double Mij = dpow(x, pw[0], k[0]) * dpow(y, pw[1], k[1]) * dpow(z, pw[2], k[2]);
+              cart[(4 + q) * nc + i] = Mij * R + (M1[u] * r[v] + M1[v] * r[u]) * dR +
+                                       mono * (r[u] * r[v] * d2R + (u == v ? dR : 0.0));
+            }
+          }
         }
       }
-    int ncomp = deriv ? 4 : 1;
+    int ncomp = deriv > 1 ? 10 : (deriv ? 4 : 1);
     for (int q = 0; q < ncomp; q++)
       for (int f = 0; f < nf; f++) {
         double v;
@@ -565,5 +594,235 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
   *exc_out = E;
   if (nelec_out)
     *nelec_out = Ne;
+  return 0;
+}
+
+// The restricted XC nuclear gradient, screened path: include/occ/dft/dft.h
+// :599-749 (leaf loop, D2 = 2 D gathered per leaf, AO second derivatives for
+// a GGA) with src/dft/dft_gradient_kernels.cpp:472-595 per leaf:
+//   LDA: Vx = phi_x^T (w vrho phi)
+//   GGA: aow = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi,
+//        Vx = phi_x^T aow + (phi^T aow_x)^T, aow_x = 0.5 w vrho phi_x
+//             + 2 w vsigma grad rho . grad phi_x          (y, z alike)
+//   gradient(:, atom(mu)) -= V(mu, nu) * 2 D2(mu, nu), |2 D2| >= 1e-12.
+// Grid weights are held fixed (no weight derivatives), as there.
+extern "C" int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim,
+                                  const int *sh_off, const double *exps, const double *coefs,
+                                  const double *sh_origin, const int *sh_atom, int natoms,
+                                  int pure, long npts, const double *points,
+                                  const double *weights, const double *D, int nfunc,
+                                  const int *func_ids, const double *func_coefs,
+                                  double screen_threshold, double density_threshold,
+                                  long leaf_target, long leaf_min, long leaf_max, int nthreads,
+                                  double *grad) {
+  Basis bs{nsh, sh_l, sh_nprim, sh_off, exps, coefs, sh_origin, pure != 0, {}, 0};
+  bs.first_bf.resize(nsh);
+  int nbf = 0;
+  for (int s = 0; s < nsh; s++) {
+    bs.first_bf[s] = nbf;
+    nbf += bs.size(s);
+  }
+  int deriv = 0;
+  for (int f = 0; f < nfunc; f++) {
+    if (oracle_functional_is_gga(func_ids[f]) < 0)
+      return -1;
+    deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
+  }
+  const int ncomp = deriv ? 10 : 4;
+  std::vector<double> ext(nsh);
+  decay_cutoff(bs, screen_threshold, ext.data());
+  std::vector<long> perm;
+  auto leaves = morton_leaves(npts, points, leaf_target, leaf_min, leaf_max, perm);
+  const long nleaves = static_cast<long>(leaves.size());
+  std::vector<double> D2(static_cast<size_t>(nbf) * nbf);
+  for (size_t i = 0; i < D2.size(); i++)
+    D2[i] = 2.0 * D[i];
+#ifdef _OPENMP
+  int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  int nt = 1;
+  (void)nthreads;
+#endif
+  std::vector<std::vector<double>> gloc(nt, std::vector<double>(3 * natoms, 0.0));
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    std::vector<double> &G = gloc[tid];
+    std::vector<double> xyz, w, phi, Dloc, Dphi, rho, sigma, e1, v1, s1, vrho, vsig, aow,
+        Vx, Vy, Vz, tmp;
+    std::vector<int> sig, loc0, bf_atom;
+#pragma omp for schedule(dynamic, 4)
+    for (long li = 0; li < nleaves; li++) {
+      const Leaf &lf = leaves[li];
+      const long n = lf.cnt;
+      if (n == 0)
+        continue;
+      sig.clear();
+      for (int s = 0; s < nsh; s++) {
+        const double *A = sh_origin + 3 * s;
+        double dx = A[0] - lf.c[0], dy = A[1] - lf.c[1], dz = A[2] - lf.c[2];
+        if (std::sqrt(dx * dx + dy * dy + dz * dz) - ext[s] < lf.r)
+          sig.push_back(s);
+      }
+      if (sig.empty())
+        continue;
+      loc0.assign(sig.size(), 0);
+      bf_atom.clear();
+      int m = 0;
+      for (size_t k = 0; k < sig.size(); k++) {
+        loc0[k] = m;
+        for (int f = 0; f < bs.size(sig[k]); f++)
+          bf_atom.push_back(sh_atom[sig[k]]);
+        m += bs.size(sig[k]);
+      }
+      xyz.resize(3 * n);
+      w.resize(n);
+      for (long i = 0; i < n; i++) {
+        long o = perm[lf.off + i];
+        for (int d = 0; d < 3; d++)
+          xyz[3 * i + d] = points[3 * o + d];
+        w[i] = weights[o];
+      }
+      Dloc.assign(static_cast<size_t>(m) * m, 0.0);
+      for (size_t a = 0; a < sig.size(); a++)
+        for (size_t b = 0; b < sig.size(); b++) {
+          int la = bs.size(sig[a]), lb = bs.size(sig[b]);
+          for (int j = 0; j < lb; j++)
+            for (int i = 0; i < la; i++)
+              Dloc[(loc0[b] + j) * static_cast<size_t>(m) + loc0[a] + i] =
+                  D2[(bs.first_bf[sig[b]] + j) * static_cast<size_t>(nbf) + bs.first_bf[sig[a]] + i];
+        }
+      phi.assign(static_cast<size_t>(ncomp) * m * n, 0.0);
+      for (size_t k = 0; k < sig.size(); k++) {
+        int s = sig[k], nf = bs.size(s);
+        tmp.assign(static_cast<size_t>(ncomp) * nf * n, 0.0);
+        collocate(sh_l[s], bs.pure, sh_nprim[s], exps + sh_off[s], coefs + sh_off[s],
+                  sh_origin + 3 * s, n, xyz.data(), 3, deriv ? 2 : 1, tmp.data(), n);
+        for (int q = 0; q < ncomp; q++)
+          for (int f = 0; f < nf; f++)
+            std::memcpy(&phi[(static_cast<size_t>(q) * m + loc0[k] + f) * n],
+                        &tmp[(static_cast<size_t>(q) * nf + f) * n], sizeof(double) * n);
+      }
+      auto P = [&](int q, int j) { return &phi[(static_cast<size_t>(q) * m + j) * n]; };
+      // density (src/gto/density.cpp:33-43) with D2
+      Dphi.assign(static_cast<size_t>(m) * n, 0.0);
+      for (int j = 0; j < m; j++)
+        for (int k = 0; k < m; k++) {
+          double d = Dloc[static_cast<size_t>(j) * m + k];
+          if (d == 0.0)
+            continue;
+          for (long p = 0; p < n; p++)
+            Dphi[static_cast<size_t>(j) * n + p] += P(0, k)[p] * d;
+        }
+      rho.assign(4 * n, 0.0);
+      for (int j = 0; j < m; j++)
+        for (long p = 0; p < n; p++) {
+          const double dp = Dphi[static_cast<size_t>(j) * n + p];
+          rho[p] += P(0, j)[p] * dp;
+          for (int q = 1; q < 4; q++)
+            rho[q * n + p] += 2.0 * P(q, j)[p] * dp;
+        }
+      double maxrho = -1e300;
+      for (long p = 0; p < n; p++)
+        maxrho = std::max(maxrho, rho[p]);
+      if (maxrho < density_threshold)
+        continue;
+      sigma.assign(n, 0.0);
+      for (long p = 0; p < n; p++)
+        sigma[p] = rho[n + p] * rho[n + p] + rho[2 * n + p] * rho[2 * n + p] +
+                   rho[3 * n + p] * rho[3 * n + p];
+      vrho.assign(n, 0.0);
+      vsig.assign(n, 0.0);
+      e1.resize(n);
+      v1.resize(n);
+      s1.resize(n);
+      for (int f = 0; f < nfunc; f++) {
+        std::fill(s1.begin(), s1.end(), 0.0);
+        oracle_functional(func_ids[f], n, rho.data(), sigma.data(), e1.data(), v1.data(),
+                          s1.data());
+        double c = func_coefs ? func_coefs[f] : 1.0;
+        for (long p = 0; p < n; p++) {
+          vrho[p] += c * v1[p];
+          vsig[p] += c * s1[p];
+        }
+      }
+      for (long p = 0; p < n; p++) {
+        vrho[p] *= w[p];
+        vsig[p] *= w[p];
+      }
+      Vx.assign(static_cast<size_t>(m) * m, 0.0);
+      Vy.assign(static_cast<size_t>(m) * m, 0.0);
+      Vz.assign(static_cast<size_t>(m) * m, 0.0);
+      double *VV[3] = {Vx.data(), Vy.data(), Vz.data()};
+      aow.assign(static_cast<size_t>(m) * n, 0.0);
+      if (!deriv) { // accumulate_gradient_contribution_R<0>
+        for (int nu = 0; nu < m; nu++)
+          for (long p = 0; p < n; p++)
+            aow[static_cast<size_t>(nu) * n + p] = P(0, nu)[p] * vrho[p];
+        for (int c = 0; c < 3; c++)
+          for (int nu = 0; nu < m; nu++)
+            for (int mu = 0; mu < m; mu++) {
+              double acc = 0.0;
+              for (long p = 0; p < n; p++)
+                acc += P(1 + c, mu)[p] * aow[static_cast<size_t>(nu) * n + p];
+              VV[c][static_cast<size_t>(nu) * m + mu] += acc;
+            }
+      } else { // accumulate_gradient_contribution_R<1>
+        for (int nu = 0; nu < m; nu++)
+          for (long p = 0; p < n; p++)
+            aow[static_cast<size_t>(nu) * n + p] =
+                0.5 * vrho[p] * P(0, nu)[p] +
+                2.0 * vsig[p] * (rho[n + p] * P(1, nu)[p] + rho[2 * n + p] * P(2, nu)[p] +
+                                 rho[3 * n + p] * P(3, nu)[p]);
+        for (int c = 0; c < 3; c++)
+          for (int nu = 0; nu < m; nu++)
+            for (int mu = 0; mu < m; mu++) {
+              double acc = 0.0;
+              for (long p = 0; p < n; p++)
+                acc += P(1 + c, mu)[p] * aow[static_cast<size_t>(nu) * n + p];
+              VV[c][static_cast<size_t>(nu) * m + mu] += acc;
+            }
+        // second-derivative planes (xx, xy, xz, yy, yz, zz) for d/dc of grad phi
+        static const int hq[3][3] = {{4, 5, 6}, {5, 7, 8}, {6, 8, 9}};
+        std::vector<double> aowc(static_cast<size_t>(m) * n);
+        for (int c = 0; c < 3; c++) {
+          for (int mu = 0; mu < m; mu++)
+            for (long p = 0; p < n; p++)
+              aowc[static_cast<size_t>(mu) * n + p] =
+                  0.5 * vrho[p] * P(1 + c, mu)[p] +
+                  2.0 * vsig[p] *
+                      (rho[n + p] * P(hq[c][0], mu)[p] + rho[2 * n + p] * P(hq[c][1], mu)[p] +
+                       rho[3 * n + p] * P(hq[c][2], mu)[p]);
+          // V_c += (phi^T aow_c)^T: V_c(mu, nu) += sum_p aow_c(p, mu) phi(p, nu)
+          for (int nu = 0; nu < m; nu++)
+            for (int mu = 0; mu < m; mu++) {
+              double acc = 0.0;
+              for (long p = 0; p < n; p++)
+                acc += aowc[static_cast<size_t>(mu) * n + p] * P(0, nu)[p];
+              VV[c][static_cast<size_t>(nu) * m + mu] += acc;
+            }
+        }
+      }
+      // distribute to atoms (dft_gradient_kernels.cpp:535-547)
+      for (int mu = 0; mu < m; mu++) {
+        const int atom = bf_atom[mu];
+        for (int nu = 0; nu < m; nu++) {
+          const double Dval = 2.0 * Dloc[static_cast<size_t>(nu) * m + mu];
+          if (std::abs(Dval) < 1e-12)
+            continue;
+          for (int c = 0; c < 3; c++)
+            G[3 * atom + c] -= VV[c][static_cast<size_t>(nu) * m + mu] * Dval;
+        }
+      }
+    }
+  }
+  std::memset(grad, 0, sizeof(double) * 3 * natoms);
+  for (int t = 0; t < nt; t++)
+    for (int i = 0; i < 3 * natoms; i++)
+      grad[i] += gloc[t][i];
   return 0;
 }

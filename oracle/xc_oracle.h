@@ -38,8 +38,9 @@ int oracle_functional(int id, long n, const double *rho, const double *sigma,
                       double *exc, double *vrho, double *vsigma);
 int oracle_functional_is_gga(int id);
 
-// Collocation of one shell (values and, if deriv, gradients) at n points
-// (xyz interleaved).  Output layout: [ncomp][nfunc][n].
+// Collocation of one shell (values and, if deriv, gradients; deriv 2 adds the
+// second derivatives xx, xy, xz, yy, yz, zz) at n points (xyz interleaved).
+// Output layout: [ncomp][nfunc][n], ncomp = 1, 4 or 10.
 int oracle_collocation(int l, int pure, int nprim, const double *exps,
                        const double *coefs, const double *origin, long n,
                        const double *xyz, int deriv, double *out);
@@ -73,6 +74,18 @@ int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
                     double density_threshold, long leaf_target, long leaf_min,
                     long leaf_max, int nthreads, long leaf_stride, double *V,
                     double *exc_out, double *nelec_out);
+
+// The restricted XC nuclear gradient (include/occ/dft/dft.h:599-749,
+// src/dft/dft_gradient_kernels.cpp:472-595), screened path, grid weights held
+// fixed.  sh_atom: atom of each shell; grad[3 * natoms] (x, y, z per atom)
+// receives dE_xc/dR.  Collocation deriv 2 (out[10][nfunc][n]) serves it.
+int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim, const int *sh_off,
+                       const double *exps, const double *coefs, const double *sh_origin,
+                       const int *sh_atom, int natoms, int pure, long npts,
+                       const double *points, const double *weights, const double *D,
+                       int nfunc, const int *func_ids, const double *func_coefs,
+                       double screen_threshold, double density_threshold, long leaf_target,
+                       long leaf_min, long leaf_max, int nthreads, double *grad);
 
 #ifdef __cplusplus
 }

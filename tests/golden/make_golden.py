@@ -8,6 +8,8 @@ gau2grid_ref.npz  AO values and gradients from gau2grid (src/3rdparty/gau2grid,
                   the collocation OCC's src/gto/gto.cpp:212-287 calls) for
                   l = 0..4, pure and Cartesian, seeded points and primitives,
                   scaled by OCC's common_fac (src/gto/gto.cpp:7-16)
+gau2grid_deriv2_ref.npz  the same with second derivatives (xx, xy, xz, yy,
+                  yz, zz), as the XC gradient evaluates them
 
 usage: python tests/golden/make_golden.py
 """
@@ -65,6 +67,32 @@ def main():
             gg[key + "_coefs"] = coefs
             gg[key + "_vals"] = vals * common_fac(l, pure)
     np.savez_compressed(os.path.join(HERE, "gau2grid_ref.npz"), **gg)
+
+    # second derivatives (gg_collocation_deriv2: phi, x, y, z, xx, xy, xz,
+    # yy, yz, zz), the AO Hessians of the XC gradient (dft.h:628-631)
+    rng = np.random.default_rng(2025)
+    g2 = {}
+    for pure in (1, 0):
+        for l in range(5):
+            npt, nprim = 40, 3
+            xyz = rng.normal(size=(npt, 3)) * 1.3
+            A = rng.normal(size=3) * 0.5
+            exps = np.sort(rng.uniform(0.1, 8.0, nprim))[::-1].copy()
+            coefs = rng.uniform(0.2, 1.0, nprim)
+            nf = 2 * l + 1 if pure else (l + 1) * (l + 2) // 2
+            vals = np.zeros((10, nf, npt))
+            lib.gg_collocation_deriv2(
+                C.c_int(l), C.c_ulong(npt), xyz.ctypes.data_as(dp), C.c_ulong(3), C.c_int(nprim),
+                coefs.ctypes.data_as(dp), exps.ctypes.data_as(dp), A.ctypes.data_as(dp),
+                C.c_int(GG_SPHERICAL_CCA if pure else GG_CARTESIAN_CCA),
+                *[vals[q].ctypes.data_as(dp) for q in range(10)])
+            key = f"{'pure' if pure else 'cart'}_l{l}"
+            g2[key + "_xyz"] = xyz
+            g2[key + "_A"] = A
+            g2[key + "_exps"] = exps
+            g2[key + "_coefs"] = coefs
+            g2[key + "_vals"] = vals * common_fac(l, pure)
+    np.savez_compressed(os.path.join(HERE, "gau2grid_deriv2_ref.npz"), **g2)
 
 
 if __name__ == "__main__":

@@ -145,3 +145,15 @@ def test_slater_closed_form():
     cx = 0.75 * (3 / np.pi) ** (1 / 3)
     assert np.allclose(e, -cx * rho ** (1 / 3), rtol=1e-14)
     assert np.allclose(v, -4 / 3 * cx * rho ** (1 / 3), rtol=1e-14)
+
+
+@pytest.mark.parametrize("pure", [1, 0])
+@pytest.mark.parametrize("l", [0, 1, 2, 3, 4])
+def test_oracle_second_derivatives_vs_gau2grid(pure, l):
+    """AO Hessians (the XC gradient's GGA term) against the reference's gau2grid."""
+    g = np.load(os.path.join(GOLDEN, "gau2grid_deriv2_ref.npz"))
+    key = f"{'pure' if pure else 'cart'}_l{l}"
+    out = oracle.collocation(l, pure, g[key + "_exps"], g[key + "_coefs"], g[key + "_A"],
+                             g[key + "_xyz"], deriv=2)
+    ref = g[key + "_vals"]
+    assert np.max(np.abs(out - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref)))
