@@ -144,6 +144,29 @@ int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *
 int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
                               int precision, double *d_V, double *d_exc2, void *stream);
 
+/* Replaces DFT::compute_xc_gradient(mo) for a restricted wavefunction
+ * (include/occ/dft/dft.h:599-749, src/dft/dft_gradient_kernels.cpp:472-595):
+ * dE_xc/dR with the grid held fixed, FP64.  grad[3*natoms] receives
+ * x, y, z per atom in Hartree/Bohr (the memory of OCC's 3 x natoms Mat3N);
+ * exc (may be NULL) the E_xc of the same density.  Host buffers; blocking.
+ * The first call allocates the gradient's workspace (AO values with second
+ * derivatives for a GGA, capped at 2 GiB per leaf group). */
+int occ_xc_compute_xc_gradient(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D,
+                               double *grad, double *exc);
+
+/* Same on device buffers, asynchronous on `stream` (NULL: the context's).
+ * d_exc2 (may be NULL) receives {E_xc, integrated density}.  Allocates on a
+ * molecule's first gradient only. */
+int occ_xc_compute_xc_gradient_device(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                      const double *d_D, double *d_grad, double *d_exc2,
+                                      void *stream);
+
+/* Cap (bytes) of the gradient workspace of one leaf group; leaves are
+ * processed in groups under it (0: the default, 2 GiB).  Frees the
+ * molecule's gradient state, which the next gradient rebuilds. */
+int occ_xc_molecule_set_gradient_workspace_cap(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                              double bytes);
+
 /* ---- batches: many molecules' XC builds in one launch sequence -------------
  * OCC builds one molecule at a time (a TBB loop over one grid); a batch runs
  * the blocks of all its molecules through the same kernel launches (the

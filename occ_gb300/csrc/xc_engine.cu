@@ -99,17 +99,6 @@ FuncSet parse_method(const std::string &method_in) {
   return fs;
 }
 
-template <typename T> static T *dev_upload(const std::vector<T> &h, size_t &bytes) {
-  T *d = nullptr;
-  size_t n = std::max<size_t>(h.size(), 1);
-  cuda_check(cudaMalloc(&d, n * sizeof(T)), "cudaMalloc");
-  if (!h.empty())
-    cuda_check(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice),
-               "cudaMemcpy H2D");
-  bytes += n * sizeof(T);
-  return d;
-}
-
 Molecule::~Molecule() {
   for (void *p : allocations)
     cudaFree(p);
@@ -341,6 +330,7 @@ Context::Context(int dev) : device(dev) {
   cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   upload_sph_table();
   upload_sph_table_mixed();
+  upload_sph_table_grad();
 }
 Context::~Context() {
   if (stream)
@@ -457,6 +447,12 @@ void Molecule::release_device() {
   d_tiles = nullptr;
   d_ws = d_rho = d_coef = d_epart = d_out2 = d_D = d_V = nullptr;
   fp64_ao_valid = false;
+  ggroups.clear();
+  d_gleaves = nullptr;
+  d_gslabs = nullptr;
+  d_ao_atom = nullptr;
+  d_gws = d_grad = nullptr;
+  grad_bytes = 0.0;
 }
 
 // Device bytes that materialise() allocates -- the resident state, without the
@@ -494,38 +490,6 @@ size_t Molecule::fp64_workspace_bytes() const {
 
 using namespace occx;
 
-namespace {
-template <typename F> int guarded(occ_xc_context *ctx, F &&f) {
-  try {
-    f();
-    return OCC_XC_OK;
-  } catch (const MethodError &e) {
-    if (ctx)
-      ctx->err = e.what();
-    return OCC_XC_ERR_METHOD;
-  } catch (const CudaError &e) {
-    if (ctx)
-      ctx->err = e.what();
-    return OCC_XC_ERR_CUDA;
-  } catch (const ArgError &e) {
-    if (ctx)
-      ctx->err = e.what();
-    return OCC_XC_ERR_ARG;
-  } catch (const TimeoutError &e) {
-    if (ctx)
-      ctx->err = e.what();
-    return OCC_XC_ERR_TIMEOUT;
-  } catch (const std::bad_alloc &) {
-    if (ctx)
-      ctx->err = "host allocation failed";
-    return OCC_XC_ERR_NOMEM;
-  } catch (const std::exception &e) {
-    if (ctx)
-      ctx->err = e.what();
-    return OCC_XC_ERR_INTERNAL;
-  }
-}
-} // namespace
 
 extern "C" {
 

@@ -1,5 +1,6 @@
 // Engine internals shared by the C ABI and the precision-specific build paths.
 #pragma once
+#include <algorithm>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -28,6 +29,20 @@ struct TimeoutError : std::runtime_error {
 };
 
 void cuda_check(cudaError_t e, const char *what);
+
+// cudaMalloc of max(size, 1) elements and a copy of h; adds the bytes to `bytes`.
+template <typename T> T *dev_upload(const std::vector<T> &h, size_t &bytes) {
+  T *d = nullptr;
+  size_t n = std::max<size_t>(h.size(), 1);
+  cuda_check(cudaMalloc(&d, n * sizeof(T)), "cudaMalloc");
+  if (!h.empty())
+    cuda_check(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice),
+               "cudaMemcpy H2D");
+  bytes += n * sizeof(T);
+  return d;
+}
+void fill_sph_table(double *out);
+void upload_sph_table_grad();
 FuncSet parse_method(const std::string &method);
 void upload_sph_table_mixed();
 struct MixedState;
@@ -81,6 +96,9 @@ struct Context {
 
 struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)
 
+// Default cap of the XC gradient's workspace per leaf group (bytes).
+constexpr size_t kGradWsCapDefault = size_t(2) << 30;
+
 // The molecule arguments of occ_xc_molecule_create.
 struct MoleculeArgs {
   int natoms;
@@ -130,6 +148,18 @@ struct Molecule {
   double *d_out2 = nullptr, *d_D = nullptr, *d_V = nullptr;
   MixedState *mixed = nullptr;
   bool fp64_ao_valid = false; // d_ws holds this molecule's AO values (no collocation)
+  // XC nuclear gradient: leaves with 4 (LDA) or 10 (GGA) AO planes, grouped
+  // under a workspace cap; allocated on the molecule's first gradient
+  struct GradGroup {
+    int leaf0, nleaf, slab0, nslab;
+  };
+  std::vector<GradGroup> ggroups;
+  DevLeaf *d_gleaves = nullptr;
+  SlabItem *d_gslabs = nullptr;
+  int *d_ao_atom = nullptr;
+  double *d_gws = nullptr, *d_grad = nullptr;
+  size_t grad_ws_cap_bytes = kGradWsCapDefault;
+  double grad_bytes = 0.0; // device bytes of the gradient's state
 
   ~Molecule();
   void *alloc(size_t bytes);
@@ -154,6 +184,10 @@ struct Molecule {
   void build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st,
                   double *ws = nullptr, bool ws_holds_ao = false);
   void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
+  void prepare_gradient();
+  void release_gradient(); // frees the gradient's device state
+  // dE_xc/dR (3 per atom, grid fixed) for mo.D = dD; dout2 = {E_xc, density}
+  void xc_gradient(const double *dD, double *dgrad, double *dout2, cudaStream_t st);
 };
 
 // Host part of a molecule: basis, molecular grid, Morton leaves and screening
@@ -205,3 +239,38 @@ struct occ_xc_molecule {
   std::unique_ptr<occx::Molecule> impl;
   occ_xc_context *ctx;
 };
+
+namespace occx {
+// Runs f, mapping the engine's exceptions to OCC_XC_ERR_* codes with the
+// message kept in the context.
+template <typename F> int guarded(occ_xc_context *ctx, F &&f) {
+  try {
+    f();
+    return OCC_XC_OK;
+  } catch (const MethodError &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_METHOD;
+  } catch (const CudaError &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_CUDA;
+  } catch (const ArgError &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_ARG;
+  } catch (const TimeoutError &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_TIMEOUT;
+  } catch (const std::bad_alloc &) {
+    if (ctx)
+      ctx->err = "host allocation failed";
+    return OCC_XC_ERR_NOMEM;
+  } catch (const std::exception &e) {
+    if (ctx)
+      ctx->err = e.what();
+    return OCC_XC_ERR_INTERNAL;
+  }
+}
+} // namespace occx

@@ -104,6 +104,11 @@ def library():
     lib.occ_xc_molecule_info_get.argtypes = [C.c_void_p, C.POINTER(_MolInfo)]
     lib.occ_xc_molecule_grid.argtypes = [C.c_void_p, _dp, _dp]
     lib.occ_xc_compute_vxc.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp, _dp, _dp]
+    lib.occ_xc_compute_xc_gradient.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp]
+    lib.occ_xc_molecule_set_gradient_workspace_cap.argtypes = [C.c_void_p, C.c_void_p,
+                                                               C.c_double]
+    lib.occ_xc_compute_xc_gradient_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
+                                                      C.c_void_p, C.c_void_p, C.c_void_p]
     lib.occ_xc_compute_vxc_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                               C.c_void_p, C.c_void_p, C.c_void_p]
     _vp = C.c_void_p
@@ -376,6 +381,33 @@ class DFT:
         self._exc = exc.value
         self._nelec = nel.value
         return V
+
+    def compute_xc_gradient(self, D):
+        """dE_xc/dR (natoms x 3, Hartree/Bohr) for mo.D = D with the grid held
+        fixed, FP64 (DFT::compute_xc_gradient, include/occ/dft/dft.h:599-749);
+        E_xc of the same density via exchange_correlation_energy()."""
+        nbf = self.nbf()
+        Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if Dm.shape != (nbf, nbf):
+            raise XCError(f"density matrix must be {nbf}x{nbf}")
+        natoms = len(self.basis.atoms())
+        g = np.zeros((natoms, 3))
+        exc = C.c_double()
+        rc = self.ctx.lib.occ_xc_compute_xc_gradient(self.ctx.h, self.h, _ptr(Dm), _ptr(g),
+                                                     C.byref(exc))
+        if rc != 0:
+            raise XCError(f"occ_xc_compute_xc_gradient failed ({rc}): {self.ctx.error()}", rc)
+        self._exc = exc.value
+        return g
+
+    def set_gradient_workspace_cap(self, nbytes):
+        """Leaves are processed in groups whose gradient workspace stays under
+        nbytes (0: the default, 2 GiB)."""
+        rc = self.ctx.lib.occ_xc_molecule_set_gradient_workspace_cap(self.ctx.h, self.h,
+                                                                     float(nbytes))
+        if rc != 0:
+            raise XCError(f"occ_xc_molecule_set_gradient_workspace_cap failed ({rc}): "
+                          f"{self.ctx.error()}", rc)
 
     def set_build_settings(self, build_settings):
         """New leaves and screening (DFT::set_xc_screening_threshold and the

@@ -48,3 +48,73 @@ def test_oracle_gradient_screened_matches_dense():
     gs = oracle.xc_gradient(b, P, W, D, "pbe", screen=1e-10)
     gd = oracle.xc_gradient(b, P, W, D, "pbe", screen=0.0)
     assert np.max(np.abs(gs - gd)) < 1e-8
+
+
+TOL_GRAD = 1e-9  # Ha/Bohr, FP64 gradient against the oracle
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["lda", "svwn5", "pbe", "blyp", "b3lyp"])
+def test_gradient_converged_water_gpu_parity(method):
+    b, D, _ = fchk_case()
+    dft = og.DFT(method, b)
+    g = dft.compute_xc_gradient(D)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient(b, P, W, D, method)
+    assert g.shape == (3, 3)
+    assert np.max(np.abs(g - g_ref)) <= TOL_GRAD, np.max(np.abs(g - g_ref))
+    e_ref = oracle.xc_build(b, P, W, D, method)[0]
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= 1e-8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("basis_name,pure,method", [("def2-svp", True, "pbe"),
+                                                    ("6-31g(d,p)", False, "b3lyp"),
+                                                    ("def2-tzvp", True, "lda")])
+def test_gradient_water_cluster_gpu_parity(basis_name, pure, method):
+    """Several waters: leaves with more than one 64-AO tile, d and f shells,
+    Cartesian and pure."""
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(4, box=6.0, seed=3)
+    b = wl.basis_for(mol, basis_name, pure)
+    D = wl.random_density(b.nbf(), 20, seed=4)
+    dft = og.DFT(method, b)
+    g = dft.compute_xc_gradient(D)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient(b, P, W, D, method)
+    scale = max(1.0, np.max(np.abs(g_ref)))
+    assert np.max(np.abs(g - g_ref)) <= TOL_GRAD * scale, np.max(np.abs(g - g_ref))
+
+
+@pytest.mark.gpu
+def test_gradient_leaf_groups_match_one_group():
+    """A small workspace cap splits the leaves into many groups; the gradient
+    is the same (up to the order of the atomic adds)."""
+    b, D, _ = fchk_case()
+    dft = og.DFT("pbe", b)
+    g1 = dft.compute_xc_gradient(D)
+    dft.set_gradient_workspace_cap(2 << 20)
+    g2 = dft.compute_xc_gradient(D)
+    assert np.max(np.abs(g1 - g2)) < 1e-12
+    dft.set_gradient_workspace_cap(0)
+    assert np.max(np.abs(dft.compute_xc_gradient(D) - g1)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_gradient_device_entry_point():
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    b, D, _ = fchk_case()
+    dft = og.DFT("b3lyp", b)
+    g_host = dft.compute_xc_gradient(D)
+    dD = torch.from_numpy(np.ascontiguousarray(D.T)).cuda()
+    dg = torch.zeros(9, dtype=torch.float64, device="cuda")
+    de = torch.zeros(2, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    rc = dft.ctx.lib.occ_xc_compute_xc_gradient_device(
+        dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), C.c_void_p(dg.data_ptr()),
+        C.c_void_p(de.data_ptr()), None)
+    assert rc == 0, dft.ctx.error()
+    torch.cuda.synchronize()
+    assert np.max(np.abs(dg.cpu().numpy().reshape(3, 3) - g_host)) < 1e-12
+    assert abs(de[0].item() - dft.exchange_correlation_energy()) < 1e-12
