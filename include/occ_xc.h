@@ -150,7 +150,7 @@ int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const d
  * x, y, z per atom in Hartree/Bohr (the memory of OCC's 3 x natoms Mat3N);
  * exc (may be NULL) the E_xc of the same density.  Host buffers; blocking.
  * The first call allocates the gradient's workspace (AO values with second
- * derivatives for a GGA, capped at 2 GiB per leaf group). */
+ * derivatives for a GGA, capped at 8 GiB per leaf group). */
 int occ_xc_compute_xc_gradient(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D,
                                double *grad, double *exc);
 
@@ -162,7 +162,7 @@ int occ_xc_compute_xc_gradient_device(occ_xc_context *ctx, occ_xc_molecule *mol,
                                       void *stream);
 
 /* Cap (bytes) of the gradient workspace of one leaf group; leaves are
- * processed in groups under it (0: the default, 2 GiB).  Frees the
+ * processed in groups under it (0: the default, 8 GiB).  Frees the
  * molecule's gradient state, which the next gradient rebuilds. */
 int occ_xc_molecule_set_gradient_workspace_cap(occ_xc_context *ctx, occ_xc_molecule *mol,
                                               double bytes);

@@ -108,7 +108,7 @@ public:
   // are built here and kept on the GPU.
   DFT(const std::string &method, const AOBasis &basis, const GridSettings &grid = {},
       int device = 0)
-      : ctx_(detail::context(device)), nbf_(basis.nbf()) {
+      : ctx_(detail::context(device)), nbf_(basis.nbf()), natoms_(basis.atoms().size()) {
     std::vector<int> Z, l, atom, nprim;
     std::vector<double> xyz, exps, coefs;
     for (const Atom &a : basis.atoms()) {
@@ -146,6 +146,17 @@ public:
     return V;
   }
 
+  // compute_xc_gradient(mo) (dft.h:599-749): dE_xc/dR with the grid held
+  // fixed, FP64; 3 * natoms values, x, y, z per atom (the memory of OCC's
+  // 3 x natoms Mat3N).  Also sets exchange_correlation_energy().
+  std::vector<double> compute_xc_gradient(const std::vector<double> &D) {
+    if (D.size() != nbf_ * nbf_)
+      throw Error("density matrix must be nbf x nbf", OCC_XC_ERR_ARG);
+    std::vector<double> g(3 * natoms_);
+    check(occ_xc_compute_xc_gradient(ctx_, mol_.get(), D.data(), g.data(), &exc_));
+    return g;
+  }
+
   double exchange_correlation_energy() const { return exc_; } // dft.h:83
   double integrated_density() const { return nelec_; }
   size_t nbf() const { return nbf_; }
@@ -169,6 +180,7 @@ private:
   occ_xc_context *ctx_;
   std::unique_ptr<occ_xc_molecule, Del> mol_;
   size_t nbf_;
+  size_t natoms_;
   double exc_ = 0.0, nelec_ = 0.0;
 };
 

@@ -156,6 +156,14 @@ void Molecule::build_plan() {
     flops += 4.0 * L.cnt * static_cast<double>(m) * m;
     leaves.push_back(L);
   }
+  // longest slabs (cost m^2) first, so that the launch does not end on a
+  // tail of a few long CTAs
+  std::stable_sort(slabs.begin(), slabs.end(), [&](const SlabItem &a, const SlabItem &b) {
+    return leaves[a.leaf].mpad > leaves[b.leaf].mpad;
+  });
+  std::stable_sort(tiles.begin(), tiles.end(), [&](const TileItem &a, const TileItem &b) {
+    return leaves[a.leaf].npad > leaves[b.leaf].npad; // tile cost: its K = npad points
+  });
 }
 
 void Molecule::upload() {

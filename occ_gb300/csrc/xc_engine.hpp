@@ -97,7 +97,7 @@ struct Context {
 struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)
 
 // Default cap of the XC gradient's workspace per leaf group (bytes).
-constexpr size_t kGradWsCapDefault = size_t(2) << 30;
+constexpr size_t kGradWsCapDefault = size_t(8) << 30;
 
 // The molecule arguments of occ_xc_molecule_create.
 struct MoleculeArgs {

@@ -360,22 +360,33 @@ void Molecule::prepare_gradient() {
   const double bytes_before = device_bytes;
   const int nq = deriv ? 10 : 4;
   const size_t cap = std::max<size_t>(grad_ws_cap_bytes / sizeof(double), 1);
-  std::vector<DevLeaf> gl = leaves;
+  // leaves by descending cost (m^2 n): groups of similar leaves, and within a
+  // launch the longest slabs first, so that no launch ends on a tail of a
+  // few long CTAs
+  std::vector<int> order(leaves.size());
+  for (size_t i = 0; i < order.size(); i++)
+    order[i] = static_cast<int>(i);
+  auto cost = [&](int i) {
+    return static_cast<double>(leaves[i].mpad) * leaves[i].mpad * leaves[i].npad;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+  std::vector<DevLeaf> gl(leaves.size());
   std::vector<SlabItem> gsl;
   ggroups.clear();
   size_t off = 0, max_ws = 0;
   GradGroup cur{0, 0, 0, 0};
-  for (size_t li = 0; li < gl.size(); li++) {
-    const size_t e = static_cast<size_t>(nq) * gl[li].mpad * gl[li].npad;
+  for (size_t k = 0; k < order.size(); k++) {
+    gl[k] = leaves[order[k]];
+    const size_t e = static_cast<size_t>(nq) * gl[k].mpad * gl[k].npad;
     if (cur.nleaf > 0 && off + e > cap) {
       ggroups.push_back(cur);
-      cur = GradGroup{static_cast<int>(li), 0, static_cast<int>(gsl.size()), 0};
+      cur = GradGroup{static_cast<int>(k), 0, static_cast<int>(gsl.size()), 0};
       off = 0;
     }
-    gl[li].ws_off = static_cast<long long>(off);
+    gl[k].ws_off = static_cast<long long>(off);
     off += e;
     max_ws = std::max(max_ws, off);
-    for (int p0 = 0; p0 < gl[li].npad; p0 += kPtTile) {
+    for (int p0 = 0; p0 < gl[k].npad; p0 += kPtTile) {
       gsl.push_back({cur.nleaf, p0});
       cur.nslab++;
     }

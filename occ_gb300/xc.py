@@ -402,7 +402,7 @@ class DFT:
 
     def set_gradient_workspace_cap(self, nbytes):
         """Leaves are processed in groups whose gradient workspace stays under
-        nbytes (0: the default, 2 GiB)."""
+        nbytes (0: the default, 8 GiB)."""
         rc = self.ctx.lib.occ_xc_molecule_set_gradient_workspace_cap(self.ctx.h, self.h,
                                                                      float(nbytes))
         if rc != 0:

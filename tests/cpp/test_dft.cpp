@@ -34,6 +34,7 @@ struct Input {
   occ_gb300::AOBasis basis{{}, {}};
   std::vector<double> D;
   std::vector<std::pair<std::string, double>> expected; // method, oracle E_xc
+  std::vector<std::pair<std::string, std::vector<double>>> gradients; // method, oracle dE/dR
   double nelec = 0.0;
 } in;
 
@@ -64,9 +65,19 @@ bool read_input(const char *path) {
   for (double &x : in.D)
     f >> x;
   std::string m;
-  double e;
-  while (f >> m >> e)
+  while (f >> m) {
+    if (m == "grad") { // grad <method> <3 natoms values>
+      std::vector<double> g(3 * static_cast<size_t>(natoms));
+      f >> m;
+      for (double &x : g)
+        f >> x;
+      in.gradients.emplace_back(m, g);
+      continue;
+    }
+    double e;
+    f >> e;
     in.expected.emplace_back(m, e);
+  }
   return static_cast<bool>(in.basis.nbf() == nbf);
 }
 
@@ -97,6 +108,22 @@ void compute_vxc_matches_oracle() {
   }
 }
 TEST_CASE("DFT::compute_vxc against the oracle, FP64 and mixed", compute_vxc_matches_oracle);
+
+void xc_gradient_matches_oracle() {
+  REQUIRE(!in.gradients.empty());
+  for (const auto &[method, g_ref] : in.gradients) {
+    occ_gb300::DFT dft(method, in.basis);
+    auto g = dft.compute_xc_gradient(in.D);
+    REQUIRE(g.size() == g_ref.size());
+    double dg = 0.0;
+    for (size_t i = 0; i < g.size() && i < g_ref.size(); i++)
+      dg = std::fmax(dg, std::fabs(g[i] - g_ref[i]));
+    std::printf("  %-6s dE_xc/dR  O = (%.8f, %.8f, %.8f)  max|d| = %.2e\n", method.c_str(), g[0],
+                g[1], g[2], dg);
+    REQUIRE(dg <= 1e-9);
+  }
+}
+TEST_CASE("DFT::compute_xc_gradient against the oracle", xc_gradient_matches_oracle);
 
 void screening_threshold() {
   occ_gb300::DFT dft("pbe", in.basis);

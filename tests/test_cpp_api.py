@@ -53,6 +53,9 @@ def test_cpp_dft_interface(tmp_path):
     for method in ("lda", "pbe", "b3lyp"):
         e_ref, _, _ = oracle.xc_build(b, P, W, D, method)
         lines.append(f"{method} {float(e_ref)!r}")
+    for method in ("lda", "pbe"):
+        g_ref = oracle.xc_gradient(b, P, W, D, method)
+        lines.append(f"grad {method} " + " ".join(repr(float(x)) for x in g_ref.ravel()))
     inp = tmp_path / "input.txt"
     inp.write_text("\n".join(lines) + "\n")
     exe = _compile(str(tmp_path / "test_dft"))
