@@ -50,11 +50,12 @@ def parse():
     ap.add_argument("--ctas", type=int, default=0,
                     help="CTAs of the persistent tensor-core kernels (0: one per SM)")
     ap.add_argument("--workload", default="water32",
-                    choices=["water32", "alkane", "clusters", "stream", "gradient"],
+                    choices=["water32", "alkane", "clusters", "stream", "gradient", "grid"],
                     help="water32: the headline build (default); alkane: C30H62 def2-TZVP "
                          "B3LYP, 15 iterations as one CUDA graph; clusters: 512 clusters "
                          "as one batch; stream: served Poisson request stream; gradient: "
-                         "the FP64 XC nuclear gradient of the water32 molecule")
+                         "the FP64 XC nuclear gradient of the water32 molecule; grid: its molecular "
+                         "grid with the Becke partition on the GPU")
     ap.add_argument("--clusters", type=int, default=512)
     ap.add_argument("--requests", type=int, default=32)
     ap.add_argument("--rate", type=float, default=10.0, help="stream arrivals per second")
@@ -74,8 +75,20 @@ def run_workload(args):
                                   nclusters=args.clusters)
         elif args.workload == "gradient":
             r = bw.xc_gradient(torch, steps=args.steps, warmup=args.warmup, waters=args.waters)
+        elif args.workload == "grid":
+            r = bw.grid_setup(steps=args.steps, warmup=args.warmup, waters=args.waters)
         else:
             r = bw.stream(nreq=args.requests, rate=args.rate)
+    if args.workload == "grid":
+        line = {"metric": "molecular grid points/s (Becke partition)",
+                "value": r.pop("points_per_s"), "unit": "points/s", "n_gpus": 1,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic", "config": {"workload": r.pop("workload")},
+                "clocks": cs.summary()}
+        line.update(r)
+        print(json.dumps(line))
+        return
     if args.workload == "gradient":
         line = {"metric": "XC nuclear gradients/s (FP64)", "value": r.pop("gradients_per_s"),
                 "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,

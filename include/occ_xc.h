@@ -100,6 +100,19 @@ int occ_xc_molecular_grid(int natoms, const int *atomic_numbers, const double *x
                           const double *coefficients, int pure, const occ_xc_grid_settings *grid,
                           long *npoints, double *points, double *weights);
 
+/* The same grid with the Becke partition weights computed on the context's
+ * device (an FP32 pass finds the atoms whose cell functions matter at each
+ * point, an FP64 pass evaluates those with OCC's formula); equal to the
+ * host's to rounding.  Molecules created on a context build their grid this
+ * way.  OCC_XC_ERR_ARG for more atoms than the kernel's shared memory holds
+ * (about 2,500 on GB300). */
+int occ_xc_molecular_grid_device(occ_xc_context *ctx, int natoms, const int *atomic_numbers,
+                                 const double *xyz_bohr, int nshells, const int *shell_l,
+                                 const int *shell_atom, const int *shell_nprim,
+                                 const double *exponents, const double *coefficients, int pure,
+                                 const occ_xc_grid_settings *grid, long *npoints, double *points,
+                                 double *weights);
+
 /* Replaces occ::numint::grid::lebedev(n) (include/occ/numint/lebedev.h,
  * src/numint/lebedev.cpp:5388-5503) for n in {6, 14, 26, 38, 50, 74, 86, 110,
  * 146, 170, 194, 230, 266, 302}: xyzw[4*n] receives x, y, z, weight per point

@@ -22,5 +22,6 @@ from .xc import (  # noqa: F401
     capture_scf_graph,
     library,
     library_path,
+    molecular_grid,
     set_persistent_ctas,
 )

@@ -21,6 +21,10 @@ gradient        XC nuclear gradient (FP64) of 32 waters, def2-SVP, PBE (the
                 (CUDA events) and through the host one (D in, gradient out),
                 parity with the oracle, the oracle's own time on the host
                 cores, and the FP64 rate of the contractions.
+grid            molecular grid of 32 waters (def2-SVP, 965,504 points): the
+                Becke partition on the GPU against the host restatement on all
+                host cores, and the whole molecule set-up (grid, leaves,
+                screening, upload) that a DFT object or a served session pays.
 
 Every input is seeded synthetic data with the shapes of these workloads.
 Each function returns a dict for one JSON line.
@@ -282,3 +286,32 @@ def xc_gradient(torch, steps=5, warmup=3, waters=32, method="pbe", seed=0):
             "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "gradients/s",
                              "cores": os.cpu_count(), "kind": "port",
                              "sample": "one full gradient of the same molecule"}}
+
+
+def grid_setup(steps=3, warmup=1, waters=32, seed=0):
+    import os
+    from .xc import molecular_grid
+    box = 10.0 * (waters / 32.0) ** (1.0 / 3.0)
+    mol = wl.water_cluster(waters, box=box, seed=seed)
+    b = wl.basis_for(mol, "def2-svp")
+    for _ in range(warmup):
+        molecular_grid(b, device=0)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        P_d, W_d = molecular_grid(b, device=0)
+    t_dev = (time.perf_counter() - t0) / steps
+    t0 = time.perf_counter()
+    P_h, W_h = molecular_grid(b)
+    t_host = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dft = DFT("pbe", b)
+    t_create = time.perf_counter() - t0
+    n = len(W_d)
+    return {"workload": f"water{waters}_def2svp_grid_becke", "natoms": len(b.atoms()),
+            "npoints": n, "points_per_s": n / t_dev, "s_per_grid": t_dev,
+            "max_rel_dw_vs_host": float(np.max(np.abs(W_d - W_h)) / np.max(np.abs(W_h))),
+            "positions_equal": bool(np.array_equal(P_d, P_h)),
+            "molecule_create_s": t_create, "device_bytes": dft.info()["device_bytes"],
+            "cpu_baseline": {"value": n / t_host, "unit": "points/s", "cores": os.cpu_count(),
+                             "kind": "port", "sample": "the whole grid of the same molecule",
+                             "s_per_grid": t_host}}

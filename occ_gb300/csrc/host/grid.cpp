@@ -263,7 +263,8 @@ int lebedev_rule(int npoints, std::vector<double> &out) {
 }
 
 MolecularGrid build_molecular_grid(const std::vector<int> &Z, const std::vector<double> &xyz,
-                                   const Basis &basis, const GridSettings &gs_in, int nthreads) {
+                                   const Basis &basis, const GridSettings &gs_in, int nthreads,
+                                   const PartitionFn *partition) {
   GridSettings gs = gs_in;
   // src/numint/molecular_grid.cpp:142-181 (ensure_settings)
   if (gs.max_angular_points < gs.min_angular_points)
@@ -329,6 +330,41 @@ MolecularGrid build_molecular_grid(const std::vector<int> &Z, const std::vector<
   }
   mg.xyz.resize(3 * total);
   mg.w.resize(total);
+
+  if (partition && *partition) {
+    // positions, owners and radial x angular weights here; the partition elsewhere
+    std::vector<int> owner(total);
+    std::vector<double> wra(total), inv_dist(natom * natom, 0.0), adj_ab(natom * natom, 0.0);
+    for (size_t a = 0; a < natom; a++) {
+      const AtomGrid &g = egrid[which[a]];
+      for (long k = 0; k < mg.atom_count[a]; k++) {
+        const long gp = mg.atom_offset[a] + k;
+        for (int dd = 0; dd < 3; dd++)
+          mg.xyz[3 * gp + dd] = g.xyz[3 * k + dd] + xyz[3 * a + dd];
+        owner[gp] = static_cast<int>(a);
+        wra[gp] = g.w[k];
+      }
+    }
+    for (size_t i = 0; i < natom; i++)
+      for (size_t j = 0; j < natom; j++) {
+        if (i != j)
+          inv_dist[i * natom + j] = 1.0 / dist[i * natom + j];
+        const size_t hi = std::max(i, j), lo = std::min(i, j);
+        if (hi != lo && adj[hi * natom + lo])
+          adj_ab[i * natom + j] = aij[hi * natom + lo];
+      }
+    PartitionInput in;
+    in.natom = static_cast<int>(natom);
+    in.atom_xyz = xyz.data();
+    in.inv_dist = inv_dist.data();
+    in.adj_ab = adj_ab.data();
+    in.npts = total;
+    in.xyz = mg.xyz.data();
+    in.owner = owner.data();
+    in.wra = wra.data();
+    (*partition)(in, mg.w.data());
+    return mg;
+  }
 
 #ifdef _OPENMP
   int nt = nthreads > 0 ? nthreads : omp_get_max_threads();

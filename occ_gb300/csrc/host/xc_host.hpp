@@ -4,6 +4,7 @@
 // build runs on the device (xc_device.cuh).
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -61,8 +62,31 @@ struct MolecularGrid {
 };
 
 int lebedev_rule(int npoints, std::vector<double> &xyzw); // returns count or 0
+
+// The Becke partition step (src/numint/grid_utils.cpp:149-200,
+// src/numint/molecular_grid.cpp:46-82) as data: atoms, the pair tables, and
+// per point its position, owning atom and radial x angular weight.  inv_dist
+// is 1/|R_i - R_j| (0 on the diagonal); adj_ab[i * natom + j] is the
+// Treutler-Ahlrichs a_ij of the ordered pair (max(i, j), min(i, j)), 0 where
+// the radii are equal.  A partition function writes w[p] = wra[p] *
+// P_owner(p) / sum_i P_i(p).
+struct PartitionInput {
+  int natom = 0;
+  const double *atom_xyz = nullptr;
+  const double *inv_dist = nullptr;
+  const double *adj_ab = nullptr;
+  long npts = 0;
+  const double *xyz = nullptr;
+  const int *owner = nullptr;
+  const double *wra = nullptr;
+};
+using PartitionFn = std::function<void(const PartitionInput &, double *w)>;
+
+// partition: nullptr for the host loop (OpenMP over nthreads), else e.g. the
+// device kernel of xc_grid.cu.
 MolecularGrid build_molecular_grid(const std::vector<int> &Z, const std::vector<double> &xyz,
-                                   const Basis &basis, const GridSettings &gs, int nthreads);
+                                   const Basis &basis, const GridSettings &gs, int nthreads,
+                                   const PartitionFn *partition = nullptr);
 
 // Per-build settings (include/occ/dft/dft.h:760-761, spatial_grid_hierarchy.h:26-30).
 struct BuildSettings {

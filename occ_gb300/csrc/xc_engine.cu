@@ -418,7 +418,13 @@ std::unique_ptr<Molecule> molecule_host(Context *ctx, const MoleculeArgs &a) {
     M->bs.leaf_max = a.build->leaf_max;
     check_build_settings(M->bs);
   }
-  M->grid = build_molecular_grid(M->Z, M->xyz, M->basis, M->gs, 0);
+  // the Becke partition on the molecule's device when it fits there
+  PartitionFn part;
+  if (device_partition_fits(ctx->device, a.natoms))
+    part = [dev = ctx->device](const PartitionInput &in, double *w) {
+      device_partition(dev, in, w);
+    };
+  M->grid = build_molecular_grid(M->Z, M->xyz, M->basis, M->gs, 0, part ? &part : nullptr);
   M->build_plan();
   return M;
 }
@@ -528,33 +534,78 @@ int occ_xc_normalize_shell(int l, int nprim, const double *exps, double *coefs) 
   return OCC_XC_OK;
 }
 
-int occ_xc_molecular_grid(int natoms, const int *Z, const double *xyz, int nshells,
-                          const int *shell_l, const int *shell_atom, const int *shell_nprim,
-                          const double *exponents, const double *coefficients, int pure,
-                          const occ_xc_grid_settings *grid, long *npoints, double *points,
-                          double *weights) {
+} // extern "C"
+
+namespace {
+// occ_xc_molecular_grid[_device]: the count alone needs no partition weights.
+int molecular_grid_impl(occ_xc_context *ctx, int natoms, const int *Z, const double *xyz,
+                        int nshells, const int *shell_l, const int *shell_atom,
+                        const int *shell_nprim, const double *exponents,
+                        const double *coefficients, int pure, const occ_xc_grid_settings *grid,
+                        long *npoints, double *points, double *weights) {
   if (natoms <= 0 || nshells <= 0 || !Z || !xyz || !shell_l || !shell_atom || !shell_nprim ||
       !exponents || !coefficients || !npoints)
     return OCC_XC_ERR_ARG;
-  try {
+  auto run = [&] {
     Basis basis = make_basis(natoms, xyz, nshells, shell_l, shell_atom, shell_nprim, exponents,
                              coefficients, pure);
     GridSettings gs = grid_settings_from(grid);
+    const bool fill = points && weights;
+    PartitionFn part;
+    if (!fill)
+      part = [](const PartitionInput &, double *) {};
+    else if (ctx)
+      part = [dev = ctx->impl->device](const PartitionInput &in, double *w) {
+        device_partition(dev, in, w);
+      };
     MolecularGrid mg = build_molecular_grid(std::vector<int>(Z, Z + natoms),
                                             std::vector<double>(xyz, xyz + 3 * natoms), basis, gs,
-                                            0);
-    if (points && weights) {
+                                            0, part ? &part : nullptr);
+    if (fill) {
       if (*npoints < mg.npts())
-        return OCC_XC_ERR_ARG;
+        throw ArgError("point buffers smaller than the grid");
       std::memcpy(points, mg.xyz.data(), mg.xyz.size() * sizeof(double));
       std::memcpy(weights, mg.w.data(), mg.w.size() * sizeof(double));
     }
     *npoints = mg.npts();
+  };
+  if (ctx) {
+    if (!device_partition_fits(ctx->impl->device, natoms))
+      return OCC_XC_ERR_ARG;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    return guarded(ctx, run);
+  }
+  try {
+    run();
     return OCC_XC_OK;
   } catch (const std::exception &e) {
     std::fprintf(stderr, "occ_xc_molecular_grid: %s\n", e.what());
     return OCC_XC_ERR_ARG;
   }
+}
+} // namespace
+
+extern "C" {
+
+int occ_xc_molecular_grid(int natoms, const int *Z, const double *xyz, int nshells,
+                          const int *shell_l, const int *shell_atom, const int *shell_nprim,
+                          const double *exponents, const double *coefficients, int pure,
+                          const occ_xc_grid_settings *grid, long *npoints, double *points,
+                          double *weights) {
+  return molecular_grid_impl(nullptr, natoms, Z, xyz, nshells, shell_l, shell_atom, shell_nprim,
+                             exponents, coefficients, pure, grid, npoints, points, weights);
+}
+
+int occ_xc_molecular_grid_device(occ_xc_context *ctx, int natoms, const int *Z,
+                                 const double *xyz, int nshells, const int *shell_l,
+                                 const int *shell_atom, const int *shell_nprim,
+                                 const double *exponents, const double *coefficients, int pure,
+                                 const occ_xc_grid_settings *grid, long *npoints, double *points,
+                                 double *weights) {
+  if (!ctx)
+    return OCC_XC_ERR_ARG;
+  return molecular_grid_impl(ctx, natoms, Z, xyz, nshells, shell_l, shell_atom, shell_nprim,
+                             exponents, coefficients, pure, grid, npoints, points, weights);
 }
 
 int occ_xc_lebedev(int n, double *xyzw) {

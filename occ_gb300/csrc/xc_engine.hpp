@@ -43,6 +43,10 @@ template <typename T> T *dev_upload(const std::vector<T> &h, size_t &bytes) {
 }
 void fill_sph_table(double *out);
 void upload_sph_table_grad();
+// Becke partition weights on `device` (xc_grid.cu); fits: the kernel's
+// shared memory holds natom atoms.
+bool device_partition_fits(int device, int natom);
+void device_partition(int device, const PartitionInput &in, double *w);
 FuncSet parse_method(const std::string &method);
 void upload_sph_table_mixed();
 struct MixedState;

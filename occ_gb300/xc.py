@@ -104,6 +104,10 @@ def library():
     lib.occ_xc_molecule_info_get.argtypes = [C.c_void_p, C.POINTER(_MolInfo)]
     lib.occ_xc_molecule_grid.argtypes = [C.c_void_p, _dp, _dp]
     lib.occ_xc_compute_vxc.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp, _dp, _dp]
+    lib.occ_xc_molecular_grid.argtypes = [C.c_int, _ip, _dp, C.c_int, _ip, _ip, _ip, _dp, _dp,
+                                          C.c_int, C.POINTER(_GridSettings),
+                                          C.POINTER(C.c_long), _dp, _dp]
+    lib.occ_xc_molecular_grid_device.argtypes = [C.c_void_p] + lib.occ_xc_molecular_grid.argtypes
     lib.occ_xc_compute_xc_gradient.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp]
     lib.occ_xc_molecule_set_gradient_workspace_cap.argtypes = [C.c_void_p, C.c_void_p,
                                                                C.c_double]
@@ -310,6 +314,36 @@ def _context(device):
     if device not in _CONTEXTS:
         _CONTEXTS[device] = _Context(device)
     return _CONTEXTS[device]
+
+
+def molecular_grid(basis, grid_settings=None, device=None):
+    """MolecularGrid(basis, settings).get_molecular_grid_points()
+    (src/numint/molecular_grid.cpp:11-140): points (N x 3, Bohr) and weights
+    in OCC's atom-block layout.  device=None: the host restatement (OpenMP);
+    a device index: the Becke partition on that GPU."""
+    lib = library()
+    atoms = basis.atoms()
+    Z = np.array([a.atomic_number for a in atoms], dtype=np.int32)
+    xyz = np.array([[a.x, a.y, a.z] for a in atoms], dtype=np.float64).ravel()
+    l, at, npr, ex, co = basis.arrays()
+    gs = (grid_settings or GridSettings())._c()
+    n = C.c_long(0)
+    args = (len(Z), _ptr(Z, _ip), _ptr(xyz), len(l), _ptr(l, _ip), _ptr(at, _ip),
+            _ptr(npr, _ip), _ptr(ex), _ptr(co), int(basis.pure), C.byref(gs), C.byref(n))
+    if device is None:
+        fn, pre = lib.occ_xc_molecular_grid, ()
+    else:
+        ctx = _context(device)
+        fn, pre = lib.occ_xc_molecular_grid_device, (ctx.h,)
+    rc = fn(*pre, *args, None, None)
+    if rc != 0:
+        raise XCError(f"molecular grid failed ({rc})", rc)
+    P = np.zeros((n.value, 3))
+    W = np.zeros(n.value)
+    rc = fn(*pre, *args, _ptr(P), _ptr(W))
+    if rc != 0:
+        raise XCError(f"molecular grid failed ({rc})", rc)
+    return P, W
 
 
 def _molecule_args(method, basis, grid_settings=None, build_settings=None):
