@@ -157,6 +157,20 @@ int occ_xc_compute_vxc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *
 int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
                               int precision, double *d_V, double *d_exc2, void *stream);
 
+/* Replaces DFT::compute_vxc(mo) for an unrestricted wavefunction
+ * (dft.h:395-429 -> compute_K_dft<deriv, Unrestricted>): D and V are
+ * 2 nbf x nbf column-major, the alpha block above the beta block, D = OCC's
+ * mo.D (each block 0.5 C_s C_s^T, src/qm/orb.h:68-83); the polarised forms of
+ * the method's functionals.  FP64 only (precision must be OCC_XC_FP64).
+ * nelec2 (may be NULL) receives the integrated alpha and beta densities. */
+int occ_xc_compute_vxc_unrestricted(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D,
+                                    int precision, double *V, double *exc, double *nelec2);
+/* Same on device buffers, asynchronous on `stream` (NULL: the context's);
+ * d_out3 (may be NULL) receives {E_xc, integrated rho_a, integrated rho_b}. */
+int occ_xc_compute_vxc_unrestricted_device(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                           const double *d_D, int precision, double *d_V,
+                                           double *d_out3, void *stream);
+
 /* Replaces DFT::compute_xc_gradient(mo) for a restricted wavefunction
  * (include/occ/dft/dft.h:599-749, src/dft/dft_gradient_kernels.cpp:472-595):
  * dE_xc/dR with the grid held fixed, FP64.  grad[3*natoms] receives

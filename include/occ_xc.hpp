@@ -136,10 +136,21 @@ public:
 
   // compute_vxc(mo) for a restricted wavefunction (dft.h:395-429): D = mo.D
   // (nbf x nbf, column-major), returns V_xc (nbf x nbf, column-major).
+  // As OCC dispatches on mo.kind, the size of D decides: nbf x nbf is
+  // restricted; 2 nbf x nbf (alpha block above beta, OCC's unrestricted
+  // mo.D) is unrestricted, FP64, and returns V_xc of the same shape.
   std::vector<double> compute_vxc(const std::vector<double> &D,
                                   Precision precision = Precision::Mixed) {
+    if (D.size() == 2 * nbf_ * nbf_) {
+      std::vector<double> V(2 * nbf_ * nbf_);
+      double n2[2];
+      check(occ_xc_compute_vxc_unrestricted(ctx_, mol_.get(), D.data(), OCC_XC_FP64, V.data(),
+                                            &exc_, n2));
+      nelec_ = n2[0] + n2[1];
+      return V;
+    }
     if (D.size() != nbf_ * nbf_)
-      throw Error("density matrix must be nbf x nbf", OCC_XC_ERR_ARG);
+      throw Error("density matrix must be nbf x nbf or 2 nbf x nbf", OCC_XC_ERR_ARG);
     std::vector<double> V(nbf_ * nbf_);
     check(occ_xc_compute_vxc(ctx_, mol_.get(), D.data(), static_cast<int>(precision), V.data(),
                              &exc_, &nelec_));

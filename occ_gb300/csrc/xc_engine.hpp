@@ -163,6 +163,10 @@ struct Molecule {
   int *d_ao_atom = nullptr;
   double *d_gws = nullptr, *d_grad = nullptr;
   size_t grad_ws_cap_bytes = kGradWsCapDefault;
+  // unrestricted (UKS) build: beta density and coefficients, per-spin D / V
+  // blocks, OCC-layout D / V of the host entry point (first UKS build)
+  double *d_rho_b = nullptr, *d_coef_b = nullptr, *d_epart_u = nullptr, *d_Dab = nullptr,
+         *d_Vab = nullptr, *d_Duks = nullptr, *d_Vuks = nullptr, *d_out3 = nullptr;
   double grad_bytes = 0.0; // device bytes of the gradient's state
 
   ~Molecule();
@@ -189,6 +193,10 @@ struct Molecule {
                   double *ws = nullptr, bool ws_holds_ao = false);
   void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
   void prepare_gradient();
+  void prepare_uks();
+  // UKS build (FP64): dD, dV 2 nbf x nbf in OCC's layout; dout3 = {E_xc,
+  // integrated rho_a, integrated rho_b}
+  void build_fp64_uks(const double *dD, double *dV, double *dout3, cudaStream_t st);
   void release_gradient(); // frees the gradient's device state
   // dE_xc/dR (3 per atom, grid fixed) for mo.D = dD; dout2 = {E_xc, density}
   void xc_gradient(const double *dD, double *dgrad, double *dout2, cudaStream_t st);

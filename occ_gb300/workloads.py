@@ -96,6 +96,17 @@ def random_density(nbf, nocc, seed=0):
     return C @ C.T
 
 
+def random_density_unrestricted(nbf, nalpha, nbeta, seed=0):
+    """OCC's unrestricted mo.D (2 nbf x nbf, alpha block above beta, each
+    0.5 C_s C_s^T, src/qm/orb.h:68-83) from seeded orthonormal orbitals,
+    different for the two spins."""
+    rng = np.random.default_rng(seed)
+    Qa, _ = np.linalg.qr(rng.standard_normal((nbf, nbf)))
+    Qb, _ = np.linalg.qr(rng.standard_normal((nbf, nbf)))
+    Ca, Cb = Qa[:, :nalpha], Qb[:, :nbeta]
+    return 0.5 * np.vstack([Ca @ Ca.T, Cb @ Cb.T])
+
+
 def basis_for(mol, name, pure=True):
     b = AOBasis.load(mol.atoms(), name)
     b.set_pure(pure)

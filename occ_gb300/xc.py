@@ -109,6 +109,11 @@ def library():
                                           C.POINTER(C.c_long), _dp, _dp]
     lib.occ_xc_molecular_grid_device.argtypes = [C.c_void_p] + lib.occ_xc_molecular_grid.argtypes
     lib.occ_xc_compute_xc_gradient.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp]
+    lib.occ_xc_compute_vxc_unrestricted.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp,
+                                                    _dp, _dp]
+    lib.occ_xc_compute_vxc_unrestricted_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
+                                                           C.c_int, C.c_void_p, C.c_void_p,
+                                                           C.c_void_p]
     lib.occ_xc_molecule_set_gradient_workspace_cap.argtypes = [C.c_void_p, C.c_void_p,
                                                                C.c_double]
     lib.occ_xc_compute_xc_gradient_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
@@ -400,11 +405,15 @@ class DFT:
         return pts, w
 
     def compute_vxc(self, D, precision=FP64):
-        """V_xc for mo.D (nbf x nbf); E_xc via exchange_correlation_energy()."""
+        """V_xc for mo.D; E_xc via exchange_correlation_energy().  As OCC's
+        compute_vxc dispatches on mo.kind, the shape of D decides: nbf x nbf is
+        restricted, 2 nbf x nbf (alpha block above beta) unrestricted."""
         nbf = self.nbf()
         Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if Dm.shape == (2 * nbf, nbf):
+            return self.compute_vxc_unrestricted(Dm, precision)
         if Dm.shape != (nbf, nbf):
-            raise XCError(f"density matrix must be {nbf}x{nbf}")
+            raise XCError(f"density matrix must be {nbf}x{nbf} or {2 * nbf}x{nbf}")
         V = np.zeros((nbf, nbf), order="F")
         exc = C.c_double()
         nel = C.c_double()
@@ -415,6 +424,31 @@ class DFT:
         self._exc = exc.value
         self._nelec = nel.value
         return V
+
+    def compute_vxc_unrestricted(self, D, precision=FP64):
+        """UKS V_xc (2 nbf x nbf, alpha block above beta) for OCC's
+        unrestricted mo.D (2 nbf x nbf, each block 0.5 C_s C_s^T); FP64."""
+        nbf = self.nbf()
+        Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if Dm.shape != (2 * nbf, nbf):
+            raise XCError(f"unrestricted density matrix must be {2 * nbf}x{nbf}")
+        V = np.zeros((2 * nbf, nbf), order="F")
+        exc = C.c_double()
+        nel = np.zeros(2)
+        rc = self.ctx.lib.occ_xc_compute_vxc_unrestricted(self.ctx.h, self.h, _ptr(Dm),
+                                                          int(precision), _ptr(V),
+                                                          C.byref(exc), _ptr(nel))
+        if rc != 0:
+            raise XCError(f"occ_xc_compute_vxc_unrestricted failed ({rc}): {self.ctx.error()}",
+                          rc)
+        self._exc = exc.value
+        self._nelec = float(nel.sum())
+        self._nelec_ab = (float(nel[0]), float(nel[1]))
+        return V
+
+    def integrated_spin_densities(self):
+        """(alpha, beta) electron counts of the last unrestricted build."""
+        return self._nelec_ab
 
     def compute_xc_gradient(self, D):
         """dE_xc/dR (natoms x 3, Hartree/Bohr) for mo.D = D with the grid held

@@ -160,3 +160,56 @@ def xc_gradient(basis, points, weights, D, method, screen=1e-10, density_thresho
     if rc != 0:
         raise RuntimeError(f"oracle_xc_gradient failed ({rc})")
     return g.reshape(natoms, 3)
+
+
+def functional_polarized(fid, ra, rb, saa=None, sab=None, sbb=None):
+    """Polarised functional at n points: exc (per particle), vrho (n x 2),
+    vsigma (n x 3; zeros for an LDA)."""
+    ra = np.ascontiguousarray(ra, dtype=np.float64)
+    rb = np.ascontiguousarray(rb, dtype=np.float64)
+    n = len(ra)
+    z = np.zeros(n)
+    s = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else z
+         for x in (saa, sab, sbb)]
+    exc = np.zeros(n)
+    v = [np.zeros(n) for _ in range(5)]
+    L = lib()
+    L.oracle_functional_polarized.restype = C.c_int
+    L.oracle_functional_polarized.argtypes = [C.c_int, C.c_long] + [_dp] * 11
+    rc = L.oracle_functional_polarized(int(fid), n, _p(ra), _p(rb), _p(s[0]), _p(s[1]),
+                                       _p(s[2]), _p(exc), *[_p(x) for x in v])
+    if rc != 0:
+        raise ValueError(f"unknown functional {fid}")
+    return exc, np.stack(v[:2], axis=1), np.stack(v[2:], axis=1)
+
+
+def xc_build_unrestricted(basis, points, weights, D, method, screen=1e-10,
+                          density_threshold=1e-10, leaf=(128, 32, 256), nthreads=0):
+    """E_xc, V (2 nbf x nbf, alpha block above beta) and the integrated
+    (alpha, beta) densities for OCC's unrestricted mo.D (2 nbf x nbf)."""
+    l, nprim, off, exps, coefs, origin = _basis_arrays(basis)
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    nbf = basis.nbf()
+    Df = np.asfortranarray(D, dtype=np.float64)
+    if Df.shape != (2 * nbf, nbf):
+        raise ValueError("D must be 2 nbf x nbf")
+    ids = np.array(METHODS[method.lower()], dtype=np.int32)
+    coef = np.ones(len(ids))
+    V = np.zeros((2 * nbf, nbf), order="F")
+    exc = C.c_double()
+    nel = np.zeros(2)
+    L = lib()
+    L.oracle_xc_build_unrestricted.restype = C.c_int
+    L.oracle_xc_build_unrestricted.argtypes = [
+        C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, C.c_int, C.c_long, _dp, _dp, _dp, C.c_int, _ip,
+        _dp, C.c_double, C.c_double, C.c_long, C.c_long, C.c_long, C.c_int, _dp, _dp, _dp]
+    rc = L.oracle_xc_build_unrestricted(
+        len(l), _p(l, _ip), _p(nprim, _ip), _p(off, _ip), _p(exps), _p(coefs), _p(origin),
+        int(basis.pure), len(w), _p(pts), _p(w), Df.ctypes.data_as(_dp), len(ids), _p(ids, _ip),
+        _p(coef), C.c_double(screen), C.c_double(density_threshold), C.c_long(leaf[0]),
+        C.c_long(leaf[1]), C.c_long(leaf[2]), nthreads, V.ctypes.data_as(_dp), C.byref(exc),
+        _p(nel))
+    if rc != 0:
+        raise RuntimeError(f"oracle_xc_build_unrestricted failed ({rc})")
+    return exc.value, V, nel

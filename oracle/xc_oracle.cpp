@@ -826,3 +826,247 @@ extern "C" int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim,
       grad[i] += gloc[t][i];
   return 0;
 }
+
+// The unrestricted build, screened path: include/occ/dft/dft.h:192-388 with
+// nspin = 2 (D2 = 2 D per spin block, dft.h:205, 336-348), the unrestricted
+// density (src/gto/density.cpp:44-70), set_params for two spins
+// (include/occ/dft/dft_kernels.h:16-60), the block skip on the largest rho_a
+// or rho_b (src/dft/dft_kernels.cpp:18-40) and the per-spin potential
+// (src/dft/xc_potential_matrix.cpp:61-105):
+//   V_s = phi^T (w vrho_s phi) + k + k^T,  k = phi^T G_s,
+//   G_a = (2 w vs_aa grad rho_a + w vs_ab grad rho_b) . grad phi.
+extern "C" int oracle_xc_build_unrestricted(
+    int nsh, const int *sh_l, const int *sh_nprim, const int *sh_off, const double *exps,
+    const double *coefs, const double *sh_origin, int pure, long npts, const double *points,
+    const double *weights, const double *D, int nfunc, const int *func_ids,
+    const double *func_coefs, double screen_threshold, double density_threshold,
+    long leaf_target, long leaf_min, long leaf_max, int nthreads, double *V, double *exc_out,
+    double *nelec2) {
+  Basis bs{nsh, sh_l, sh_nprim, sh_off, exps, coefs, sh_origin, pure != 0, {}, 0};
+  bs.first_bf.resize(nsh);
+  int nbf = 0;
+  for (int s = 0; s < nsh; s++) {
+    bs.first_bf[s] = nbf;
+    nbf += bs.size(s);
+  }
+  bs.nbf = nbf;
+  int deriv = 0;
+  for (int f = 0; f < nfunc; f++) {
+    if (oracle_functional_is_gga(func_ids[f]) < 0)
+      return -1;
+    deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
+  }
+  std::vector<double> ext(nsh);
+  decay_cutoff(bs, screen_threshold, ext.data());
+  std::vector<long> perm;
+  auto leaves = morton_leaves(npts, points, leaf_target, leaf_min, leaf_max, perm);
+  const long nleaves = static_cast<long>(leaves.size());
+  const size_t ld = 2 * static_cast<size_t>(nbf); // rows of OCC's 2 nbf x nbf D and V
+
+#ifdef _OPENMP
+  int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  int nt = 1;
+  (void)nthreads;
+#endif
+  std::vector<std::vector<double>> Vloc(nt);
+  std::vector<double> eloc(nt, 0.0), naloc(nt, 0.0), nbloc(nt, 0.0);
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    std::vector<double> &K = Vloc[tid];
+    K.assign(ld * nbf, 0.0);
+    std::vector<double> xyz, w, phi, Dloc, Dphi, rho[2], exc, e1, vr[2], v1[2], vs[3], s1[3],
+        G, Kb, kt;
+    std::vector<int> sig, loc0;
+#pragma omp for schedule(dynamic, 4)
+    for (long li = 0; li < nleaves; li++) {
+      const Leaf &lf = leaves[li];
+      const long n = lf.cnt;
+      if (n == 0)
+        continue;
+      sig.clear();
+      for (int s = 0; s < nsh; s++) {
+        const double *A = sh_origin + 3 * s;
+        double dx = A[0] - lf.c[0], dy = A[1] - lf.c[1], dz = A[2] - lf.c[2];
+        if (std::sqrt(dx * dx + dy * dy + dz * dz) - ext[s] < lf.r)
+          sig.push_back(s);
+      }
+      if (sig.empty())
+        continue;
+      loc0.assign(sig.size(), 0);
+      int m = 0;
+      for (size_t k = 0; k < sig.size(); k++) {
+        loc0[k] = m;
+        m += bs.size(sig[k]);
+      }
+      xyz.resize(3 * n);
+      w.resize(n);
+      for (long i = 0; i < n; i++) {
+        long o = perm[lf.off + i];
+        for (int d = 0; d < 3; d++)
+          xyz[3 * i + d] = points[3 * o + d];
+        w[i] = weights[o];
+      }
+      const int ncomp = deriv ? 4 : 1;
+      phi.assign(static_cast<size_t>(ncomp) * m * n, 0.0);
+      {
+        std::vector<double> tmp;
+        for (size_t k = 0; k < sig.size(); k++) {
+          int s = sig[k], nf = bs.size(s);
+          tmp.assign(static_cast<size_t>(ncomp) * nf * n, 0.0);
+          collocate(sh_l[s], bs.pure, sh_nprim[s], exps + sh_off[s], coefs + sh_off[s],
+                    sh_origin + 3 * s, n, xyz.data(), 3, deriv, tmp.data(), n);
+          for (int q = 0; q < ncomp; q++)
+            for (int f = 0; f < nf; f++)
+              std::memcpy(&phi[(static_cast<size_t>(q) * m + loc0[k] + f) * n],
+                          &tmp[(static_cast<size_t>(q) * nf + f) * n], sizeof(double) * n);
+        }
+      }
+      // per spin: D2_s local block, Dphi = phi D2_s, rho_s and grad rho_s
+      double maxrho = -1e300;
+      for (int sp = 0; sp < 2; sp++) {
+        Dloc.assign(static_cast<size_t>(m) * m, 0.0);
+        for (size_t a = 0; a < sig.size(); a++)
+          for (size_t b = 0; b < sig.size(); b++) {
+            int la = bs.size(sig[a]), lb = bs.size(sig[b]);
+            for (int j = 0; j < lb; j++)
+              for (int i = 0; i < la; i++)
+                Dloc[(loc0[b] + j) * static_cast<size_t>(m) + loc0[a] + i] =
+                    2.0 * D[(bs.first_bf[sig[b]] + j) * ld + sp * static_cast<size_t>(nbf) +
+                            bs.first_bf[sig[a]] + i];
+          }
+        Dphi.assign(static_cast<size_t>(m) * n, 0.0);
+        for (int j = 0; j < m; j++)
+          for (int k = 0; k < m; k++) {
+            double d = Dloc[static_cast<size_t>(j) * m + k];
+            if (d == 0.0)
+              continue;
+            const double *ph = &phi[static_cast<size_t>(k) * n];
+            double *out = &Dphi[static_cast<size_t>(j) * n];
+            for (long p = 0; p < n; p++)
+              out[p] += ph[p] * d;
+          }
+        rho[sp].assign(4 * n, 0.0);
+        for (int j = 0; j < m; j++) {
+          const double *dp = &Dphi[static_cast<size_t>(j) * n];
+          for (long p = 0; p < n; p++)
+            rho[sp][p] += phi[static_cast<size_t>(j) * n + p] * dp[p];
+          if (deriv)
+            for (int q = 1; q < 4; q++)
+              for (long p = 0; p < n; p++)
+                rho[sp][q * n + p] += 2.0 * phi[(static_cast<size_t>(q) * m + j) * n + p] * dp[p];
+        }
+        for (long p = 0; p < n; p++) {
+          (sp == 0 ? naloc : nbloc)[tid] += rho[sp][p] * w[p];
+          maxrho = std::max(maxrho, rho[sp][p]);
+        }
+      }
+      if (maxrho < density_threshold)
+        continue;
+      // polarised functional, summed over components, weighted
+      std::vector<double> saa(n, 0.0), sab(n, 0.0), sbb(n, 0.0);
+      if (deriv)
+        for (long p = 0; p < n; p++)
+          for (int q = 1; q < 4; q++) {
+            saa[p] += rho[0][q * n + p] * rho[0][q * n + p];
+            sab[p] += rho[0][q * n + p] * rho[1][q * n + p];
+            sbb[p] += rho[1][q * n + p] * rho[1][q * n + p];
+          }
+      exc.assign(n, 0.0);
+      e1.resize(n);
+      for (int sp = 0; sp < 2; sp++) {
+        vr[sp].assign(n, 0.0);
+        v1[sp].resize(n);
+      }
+      for (int k = 0; k < 3; k++) {
+        vs[k].assign(n, 0.0);
+        s1[k].assign(n, 0.0);
+      }
+      for (int f = 0; f < nfunc; f++) {
+        oracle_functional_polarized(func_ids[f], n, rho[0].data(), rho[1].data(), saa.data(),
+                                    sab.data(), sbb.data(), e1.data(), v1[0].data(),
+                                    v1[1].data(), s1[0].data(), s1[1].data(), s1[2].data());
+        double c = func_coefs ? func_coefs[f] : 1.0;
+        for (long p = 0; p < n; p++) {
+          exc[p] += c * e1[p];
+          vr[0][p] += c * v1[0][p];
+          vr[1][p] += c * v1[1][p];
+          for (int k = 0; k < 3; k++)
+            vs[k][p] += c * s1[k][p];
+        }
+      }
+      for (long p = 0; p < n; p++) {
+        exc[p] *= w[p];
+        vr[0][p] *= w[p];
+        vr[1][p] *= w[p];
+        for (int k = 0; k < 3; k++)
+          vs[k][p] *= w[p];
+        eloc[tid] += exc[p] * (rho[0][p] + rho[1][p]);
+      }
+      for (int sp = 0; sp < 2; sp++) {
+        const int ot = 1 - sp;
+        const std::vector<double> &vss = vs[sp == 0 ? 0 : 2];
+        Kb.assign(static_cast<size_t>(m) * m, 0.0);
+        for (int j = 0; j < m; j++)
+          for (int i = 0; i < m; i++) {
+            double acc = 0.0;
+            for (long p = 0; p < n; p++)
+              acc += phi[static_cast<size_t>(i) * n + p] * phi[static_cast<size_t>(j) * n + p] *
+                     vr[sp][p];
+            Kb[static_cast<size_t>(j) * m + i] = acc;
+          }
+        if (deriv) {
+          G.assign(static_cast<size_t>(m) * n, 0.0);
+          for (int j = 0; j < m; j++)
+            for (long p = 0; p < n; p++) {
+              double g = 0.0;
+              for (int q = 1; q < 4; q++)
+                g += phi[(static_cast<size_t>(q) * m + j) * n + p] *
+                     (2.0 * vss[p] * rho[sp][q * n + p] + vs[1][p] * rho[ot][q * n + p]);
+              G[static_cast<size_t>(j) * n + p] = g;
+            }
+          kt.assign(static_cast<size_t>(m) * m, 0.0);
+          for (int j = 0; j < m; j++)
+            for (int i = 0; i < m; i++) {
+              double acc = 0.0;
+              for (long p = 0; p < n; p++)
+                acc += phi[static_cast<size_t>(i) * n + p] * G[static_cast<size_t>(j) * n + p];
+              kt[static_cast<size_t>(j) * m + i] = acc;
+            }
+          for (int j = 0; j < m; j++)
+            for (int i = 0; i < m; i++)
+              Kb[static_cast<size_t>(j) * m + i] +=
+                  kt[static_cast<size_t>(j) * m + i] + kt[static_cast<size_t>(i) * m + j];
+        }
+        for (size_t a = 0; a < sig.size(); a++)
+          for (size_t b = 0; b < sig.size(); b++) {
+            int la = bs.size(sig[a]), lb = bs.size(sig[b]);
+            for (int j = 0; j < lb; j++)
+              for (int i = 0; i < la; i++)
+                K[(bs.first_bf[sig[b]] + j) * ld + sp * static_cast<size_t>(nbf) +
+                  bs.first_bf[sig[a]] + i] += Kb[(loc0[b] + j) * static_cast<size_t>(m) + loc0[a] + i];
+          }
+      }
+    }
+  }
+  std::memset(V, 0, sizeof(double) * ld * nbf);
+  double E = 0.0, Na = 0.0, Nb = 0.0;
+  for (int t = 0; t < nt; t++) {
+    for (size_t i = 0; i < ld * nbf; i++)
+      V[i] += Vloc[t][i];
+    E += eloc[t];
+    Na += naloc[t];
+    Nb += nbloc[t];
+  }
+  *exc_out = E;
+  if (nelec2) {
+    nelec2[0] = Na;
+    nelec2[1] = Nb;
+  }
+  return 0;
+}

@@ -37,6 +37,13 @@ enum {
 int oracle_functional(int id, long n, const double *rho, const double *sigma,
                       double *exc, double *vrho, double *vsigma);
 int oracle_functional_is_gga(int id);
+// The polarised form (UKS): rho_a, rho_b, s_aa, s_ab, s_bb in; exc (per
+// particle), vrho_a, vrho_b, vs_aa, vs_ab, vs_bb out (sigma arrays and
+// their outputs may be null for an LDA).
+int oracle_functional_polarized(int id, long n, const double *ra, const double *rb,
+                                const double *saa, const double *sab, const double *sbb,
+                                double *exc, double *vra, double *vrb, double *vsaa,
+                                double *vsab, double *vsbb);
 
 // Collocation of one shell (values and, if deriv, gradients; deriv 2 adds the
 // second derivatives xx, xy, xz, yy, yz, zz) at n points (xyz interleaved).
@@ -74,6 +81,19 @@ int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
                     double density_threshold, long leaf_target, long leaf_min,
                     long leaf_max, int nthreads, long leaf_stride, double *V,
                     double *exc_out, double *nelec_out);
+
+// The unrestricted (UKS) build: compute_K_dft<deriv, Unrestricted>
+// (include/occ/dft/dft.h:192-388) with the polarised functionals.  D and V
+// are 2 nbf x nbf column-major (alpha block above beta, OCC's mo.D);
+// nelec2 (may be null) receives the integrated alpha and beta densities.
+int oracle_xc_build_unrestricted(int nsh, const int *sh_l, const int *sh_nprim,
+                                 const int *sh_off, const double *exps, const double *coefs,
+                                 const double *sh_origin, int pure, long npts,
+                                 const double *points, const double *weights, const double *D,
+                                 int nfunc, const int *func_ids, const double *func_coefs,
+                                 double screen_threshold, double density_threshold,
+                                 long leaf_target, long leaf_min, long leaf_max, int nthreads,
+                                 double *V, double *exc_out, double *nelec2);
 
 // The restricted XC nuclear gradient (include/occ/dft/dft.h:599-749,
 // src/dft/dft_gradient_kernels.cpp:472-595), screened path, grid weights held

@@ -231,3 +231,211 @@ extern "C" int oracle_functional(int id, long n, const double *rho,
   }
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Spin-polarised forms (the UKS build, m_method.functionals_polarized,
+// include/occ/dft/dft.h:207-209), restated from the same papers:
+//   exchange (Slater, B88, PBE) by the exact spin scaling
+//     E_x[rho_a, rho_b] = (E_x[2 rho_a] + E_x[2 rho_b]) / 2;
+//   VWN: eps = eps_P + alpha_c f(z)/f''(0) (1 - z^4) + (eps_F - eps_P) f(z) z^4
+//     (VWN 1980, CA and RPA fits; VWN3 scales the RPA spin stiffness by the
+//     CA / RPA polarisation energies);
+//   PW92: the same interpolation with alpha_c = -G(rs) of its third fit, in
+//     PBE correlation with phi(z) = ((1+z)^(2/3) + (1-z)^(2/3)) / 2;
+//   LYP: Miehlich, Savin, Stoll, Preuss, CPL 157, 200 (1989), eq. 2.
+// Derivatives by the complex step, dE/dx = Im E(x + i h) / h with h = 1e-30
+// (W. Squire, G. Trapp, SIAM Review 40, 110 (1998)), exact to rounding for
+// these analytic forms and independent of dual-number code.
+#include <complex>
+
+namespace {
+
+using Cx = std::complex<double>;
+const double kEps = 2.220446049250313e-16;
+
+Cx c13(Cx x) { return std::pow(x, 1.0 / 3.0); }
+Cx p43(Cx x) { return std::pow(x, 4.0 / 3.0); }
+
+Cx vwn_fit_c(Cx rs, double A, double b, double c, double x0) {
+  Cx x = std::sqrt(rs);
+  Cx X = x * x + b * x + c;
+  double X0 = x0 * x0 + b * x0 + c;
+  double Q = std::sqrt(4.0 * c - b * b);
+  Cx at = std::atan(Q / (2.0 * x + b));
+  Cx t1 = std::log(x * x / X) + (2.0 * b / Q) * at;
+  Cx t2 = std::log((x - x0) * (x - x0) / X) + (2.0 * (b + 2.0 * x0) / Q) * at;
+  return A * (t1 - (b * x0 / X0) * t2);
+}
+
+Cx pw_g_c(Cx rs, double A, double a1, double b1, double b2, double b3, double b4) {
+  Cx srs = std::sqrt(rs);
+  Cx den = 2.0 * A * (b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs);
+  return -2.0 * A * (1.0 + a1 * rs) * std::log(1.0 + 1.0 / den);
+}
+
+struct PolPoint {
+  Cx ra, rb, saa, sab, sbb;
+  bool sa, sb; // spin channel above the density threshold
+};
+
+Cx slater_c(Cx r) { return -0.75 * std::cbrt(3.0 / kPi) * std::cbrt(2.0) * p43(r); }
+Cx b88_c(Cx r, Cx s) {
+  const double beta = 0.0042, cs = 1.5 * std::cbrt(3.0 / (4.0 * kPi));
+  Cx r43 = p43(r);
+  Cx x = std::sqrt(s) / r43;
+  return -cs * r43 - beta * r43 * x * x / (1.0 + 6.0 * beta * x * std::asinh(x));
+}
+Cx pbe_x_c(Cx r, Cx s) { // E_x^PBE[2 r, 4 s] / 2
+  const double kappa = 0.8040, mu = 0.2195149727645171;
+  Cx n = 2.0 * r;
+  Cx kf = c13(3.0 * kPi * kPi * n);
+  Cx s2 = 4.0 * s / (4.0 * kf * kf * n * n);
+  Cx F = (1.0 + kappa) - kappa / (1.0 + (mu / kappa) * s2);
+  return 0.5 * (-0.75 * std::cbrt(3.0 / kPi) * p43(n) * F);
+}
+
+Cx pol_energy(int id, const PolPoint &P) {
+  Cx rho = P.ra + P.rb;
+  Cx z = (P.ra - P.rb) / rho;
+  Cx opz = 1.0 + z, omz = 1.0 - z;
+  if (opz.real() < kEps)
+    opz = kEps;
+  if (omz.real() < kEps)
+    omz = kEps;
+  const double fpp = 4.0 / (9.0 * (std::cbrt(2.0) - 1.0));
+  Cx f = (p43(opz) + p43(omz) - 2.0) / (std::pow(2.0, 4.0 / 3.0) - 2.0);
+  Cx z4 = z * z * z * z;
+  Cx rs = c13(3.0 / (4.0 * kPi * rho));
+  auto X = [&](Cx (*fx)(Cx, Cx)) {
+    Cx e = 0.0;
+    if (P.sa)
+      e += fx(P.ra, P.saa);
+    if (P.sb)
+      e += fx(P.rb, P.sbb);
+    return e;
+  };
+  auto slater = [&] {
+    Cx e = 0.0;
+    if (P.sa)
+      e += slater_c(P.ra);
+    if (P.sb)
+      e += slater_c(P.rb);
+    return e;
+  };
+  const double Avwn[3] = {0.0310907, 0.01554535, -1.0 / (6.0 * kPi * kPi)};
+  const double bca[3] = {3.72744, 7.06042, 1.13107}, cca[3] = {12.9352, 18.0578, 13.0045},
+               xca[3] = {-0.10498, -0.32500, -0.0047584};
+  const double brp[3] = {13.0720, 20.1231, 1.06835}, crp[3] = {42.7198, 101.578, 11.4813},
+               xrp[3] = {-0.409286, -0.743294, -0.228344};
+  auto vwn = [&](int variant) {
+    if (variant < 2) {
+      const double *b = variant == 0 ? bca : brp, *c = variant == 0 ? cca : crp,
+                   *x0 = variant == 0 ? xca : xrp;
+      Cx eP = vwn_fit_c(rs, Avwn[0], b[0], c[0], x0[0]);
+      Cx eF = vwn_fit_c(rs, Avwn[1], b[1], c[1], x0[1]);
+      Cx ac = vwn_fit_c(rs, Avwn[2], b[2], c[2], x0[2]);
+      return rho * (eP + ac * f / fpp * (1.0 - z4) + (eF - eP) * f * z4);
+    }
+    Cx eP = vwn_fit_c(rs, Avwn[0], bca[0], cca[0], xca[0]);
+    Cx dca = vwn_fit_c(rs, Avwn[1], bca[1], cca[1], xca[1]) - eP;
+    Cx drpa = vwn_fit_c(rs, Avwn[1], brp[1], crp[1], xrp[1]) -
+              vwn_fit_c(rs, Avwn[0], brp[0], crp[0], xrp[0]);
+    Cx ar = vwn_fit_c(rs, Avwn[2], brp[2], crp[2], xrp[2]);
+    return rho * (eP + ar * f / fpp * (1.0 - z4) * dca / drpa + dca * f * z4);
+  };
+  auto lyp = [&] {
+    const double a = 0.04918, b = 0.132, c = 0.2533, d = 0.349;
+    const double cf = 0.3 * std::pow(3.0 * kPi * kPi, 2.0 / 3.0);
+    Cx rm13 = 1.0 / c13(rho);
+    Cx den = 1.0 + d * rm13;
+    Cx omega = std::exp(-c * rm13) / den * std::pow(rho, -11.0 / 3.0);
+    Cx delta = c * rm13 + d * rm13 / den;
+    Cx gg = P.saa + 2.0 * P.sab + P.sbb;
+    Cx ab = P.ra * P.rb;
+    auto p83 = [](Cx x) { return x.real() > 0.0 ? std::pow(x, 8.0 / 3.0) : Cx(0.0); };
+    Cx br = std::pow(2.0, 11.0 / 3.0) * cf * (p83(P.ra) + p83(P.rb)) +
+            (47.0 / 18.0 - 7.0 / 18.0 * delta) * gg - (2.5 - delta / 18.0) * (P.saa + P.sbb) -
+            (delta - 11.0) / 9.0 * (P.ra / rho * P.saa + P.rb / rho * P.sbb);
+    Cx rest = -2.0 / 3.0 * rho * rho * gg + (2.0 / 3.0 * rho * rho - P.ra * P.ra) * P.sbb +
+              (2.0 / 3.0 * rho * rho - P.rb * P.rb) * P.saa;
+    return -4.0 * a / den * ab / rho - a * b * omega * (ab * br + rest);
+  };
+  auto pbe_c = [&] {
+    const double beta = 0.06672455060314922, gamma = (1.0 - std::log(2.0)) / (kPi * kPi);
+    Cx e0 = pw_g_c(rs, 0.0310907, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294);
+    Cx e1 = pw_g_c(rs, 0.01554535, 0.20548, 14.1189, 6.1977, 3.3662, 0.62517);
+    Cx ac = -pw_g_c(rs, 0.0168869, 0.11125, 10.357, 3.6231, 0.88026, 0.49671);
+    Cx eps = e0 + ac * f / fpp * (1.0 - z4) + (e1 - e0) * f * z4;
+    Cx phi = 0.5 * (std::pow(opz, 2.0 / 3.0) + std::pow(omz, 2.0 / 3.0));
+    Cx phi3 = phi * phi * phi;
+    Cx kf = c13(3.0 * kPi * kPi * rho);
+    Cx ks2 = 4.0 / kPi * kf;
+    Cx t2 = (P.saa + 2.0 * P.sab + P.sbb) / (4.0 * phi * phi * ks2 * rho * rho);
+    Cx A = beta / gamma / (std::exp(-eps / (gamma * phi3)) - 1.0);
+    Cx At2 = A * t2;
+    Cx H = gamma * phi3 * std::log(1.0 + beta / gamma * t2 * (1.0 + At2) / (1.0 + At2 + At2 * At2));
+    return rho * (eps + H);
+  };
+  switch (id) {
+  case ORC_LDA_X: return slater();
+  case ORC_LDA_C_VWN: return vwn(0);
+  case ORC_LDA_C_VWN_RPA: return vwn(1);
+  case ORC_LDA_C_VWN_3: return vwn(2);
+  case ORC_GGA_X_PBE: return X(pbe_x_c);
+  case ORC_GGA_C_PBE: return pbe_c();
+  case ORC_GGA_X_B88: return X(b88_c);
+  case ORC_GGA_C_LYP: return lyp();
+  case ORC_HYB_GGA_XC_B3LYP:
+    return 0.08 * slater() + 0.72 * X(b88_c) + 0.19 * vwn(1) + 0.81 * lyp();
+  case ORC_HYB_GGA_XC_B3LYP5:
+    return 0.08 * slater() + 0.72 * X(b88_c) + 0.19 * vwn(0) + 0.81 * lyp();
+  }
+  return 0.0;
+}
+
+} // namespace
+
+// Polarised evaluation at n points: rho_a, rho_b, s_aa, s_ab, s_bb in;
+// exc (per particle), vrho_a, vrho_b, vs_aa, vs_ab, vs_bb out (the sigma
+// arrays and outputs may be NULL for an LDA).
+extern "C" int oracle_functional_polarized(int id, long n, const double *ra, const double *rb,
+                                           const double *saa, const double *sab,
+                                           const double *sbb, double *exc, double *vra,
+                                           double *vrb, double *vsaa, double *vsab,
+                                           double *vsbb) {
+  if (!known(id))
+    return -1;
+  const bool gga = is_gga(id);
+  const double h = 1e-30;
+  for (long i = 0; i < n; i++) {
+    const double a = std::fmax(ra[i], 0.0), b = std::fmax(rb[i], 0.0);
+    double x[5] = {a, b, gga ? std::fmax(saa[i], 1e-40) : 0.0, gga ? sab[i] : 0.0,
+                   gga ? std::fmax(sbb[i], 1e-40) : 0.0};
+    double out[6] = {0, 0, 0, 0, 0, 0};
+    if (a + b >= 1e-15) {
+      for (int k = -1; k < (gga ? 5 : 2); k++) {
+        PolPoint P{x[0], x[1], x[2], x[3], x[4], a >= 1e-15, b >= 1e-15};
+        Cx *v[5] = {&P.ra, &P.rb, &P.saa, &P.sab, &P.sbb};
+        if (k >= 0)
+          *v[k] += Cx(0.0, h);
+        Cx e = pol_energy(id, P);
+        if (k < 0)
+          out[0] = e.real() / (a + b);
+        else
+          out[1 + k] = e.imag() / h;
+      }
+    }
+    exc[i] = out[0];
+    vra[i] = out[1];
+    vrb[i] = out[2];
+    if (gga) {
+      if (vsaa)
+        vsaa[i] = out[3];
+      if (vsab)
+        vsab[i] = out[4];
+      if (vsbb)
+        vsbb[i] = out[5];
+    }
+  }
+  return 0;
+}
