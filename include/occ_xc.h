@@ -171,6 +171,21 @@ int occ_xc_compute_vxc_unrestricted_device(occ_xc_context *ctx, occ_xc_molecule 
                                            const double *d_D, int precision, double *d_V,
                                            double *d_out3, void *stream);
 
+/* VV10 non-local correlation: replaces NonLocalCorrelationFunctional's
+ * operator()(basis, mo) (src/dft/nonlocal_correlation.cpp:331-388), the
+ * energy DFT::post_scf_nlc_correction (include/occ/dft/dft.h:476-483) adds
+ * for the "-V" methods, restricted.  Parameters b and C (OCC's defaults 6.0
+ * and 0.01); energy receives E_nlc, V (may be NULL) its nbf x nbf potential.
+ * precision: OCC_XC_FP64, or OCC_XC_MIXED for the O(N^2) pair sums in FP32
+ * (compensated; everything else FP64).  The first call builds the NLC grid
+ * (OCC's GridSettings{110, 50, 50, 1e-7}) as a second resident grid. */
+int occ_xc_nlc_vv10(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D, double b,
+                    double C, int precision, double *energy, double *V);
+/* The NLC grid in OCC's layout once built: its point count (-1 before the
+ * first VV10 call), then points[3 * n] and weights[n]. */
+int occ_xc_nlc_grid_points(const occ_xc_molecule *mol, long *npoints);
+int occ_xc_nlc_grid(const occ_xc_molecule *mol, double *points, double *weights);
+
 /* Replaces DFT::compute_xc_gradient(mo) for a restricted wavefunction
  * (include/occ/dft/dft.h:599-749, src/dft/dft_gradient_kernels.cpp:472-595):
  * dE_xc/dR with the grid held fixed, FP64.  grad[3*natoms] receives

@@ -167,6 +167,12 @@ struct Molecule {
   // blocks, OCC-layout D / V of the host entry point (first UKS build)
   double *d_rho_b = nullptr, *d_coef_b = nullptr, *d_epart_u = nullptr, *d_Dab = nullptr,
          *d_Vab = nullptr, *d_Duks = nullptr, *d_Vuks = nullptr, *d_out3 = nullptr;
+  // VV10: the molecule on OCC's NLC grid (first VV10 call) and, on that
+  // molecule, its sorted -> grid-order map and the pair kernel's buffers
+  std::unique_ptr<Molecule> nlc;
+  int *d_nlc_perm = nullptr;
+  void *d_nlc_pts = nullptr, *d_nlc_pts32 = nullptr;
+  double *d_nlc_fuw = nullptr, *d_nlc_epart = nullptr;
   double grad_bytes = 0.0; // device bytes of the gradient's state
 
   ~Molecule();
@@ -194,6 +200,11 @@ struct Molecule {
   void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
   void prepare_gradient();
   void prepare_uks();
+  void prepare_nlc();
+  // VV10 energy (dE, one double) and, if dV, its V (nbf x nbf) for mo.D = dD;
+  // precision OCC_XC_FP64 or OCC_XC_MIXED (FP32 pair sums)
+  void nlc_vv10(const double *dD, double b, double C, int precision, double *dV, double *dE,
+                cudaStream_t st);
   // UKS build (FP64): dD, dV 2 nbf x nbf in OCC's layout; dout3 = {E_xc,
   // integrated rho_a, integrated rho_b}
   void build_fp64_uks(const double *dD, double *dV, double *dout3, cudaStream_t st);

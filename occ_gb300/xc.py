@@ -109,6 +109,10 @@ def library():
                                           C.POINTER(C.c_long), _dp, _dp]
     lib.occ_xc_molecular_grid_device.argtypes = [C.c_void_p] + lib.occ_xc_molecular_grid.argtypes
     lib.occ_xc_compute_xc_gradient.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp]
+    lib.occ_xc_nlc_vv10.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_double, C.c_double,
+                                    C.c_int, _dp, _dp]
+    lib.occ_xc_nlc_grid_points.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
+    lib.occ_xc_nlc_grid.argtypes = [C.c_void_p, _dp, _dp]
     lib.occ_xc_compute_vxc_unrestricted.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp,
                                                     _dp, _dp]
     lib.occ_xc_compute_vxc_unrestricted_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
@@ -449,6 +453,34 @@ class DFT:
     def integrated_spin_densities(self):
         """(alpha, beta) electron counts of the last unrestricted build."""
         return self._nelec_ab
+
+    def nlc_vv10(self, D, b=6.0, C_vv10=0.01, want_V=True, precision=FP64):
+        """VV10 non-local correlation (NonLocalCorrelationFunctional, the
+        post-SCF NLC correction of OCC's "-V" methods): (E_nlc, V or None)
+        for mo.D = D, restricted, FP64, on OCC's NLC grid."""
+        nbf = self.nbf()
+        Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if Dm.shape != (nbf, nbf):
+            raise XCError(f"density matrix must be {nbf}x{nbf}")
+        V = np.zeros((nbf, nbf), order="F") if want_V else None
+        e = C.c_double()
+        rc = self.ctx.lib.occ_xc_nlc_vv10(self.ctx.h, self.h, _ptr(Dm), float(b), float(C_vv10),
+                                          int(precision), C.byref(e),
+                                          _ptr(V) if want_V else None)
+        if rc != 0:
+            raise XCError(f"occ_xc_nlc_vv10 failed ({rc}): {self.ctx.error()}", rc)
+        return e.value, V
+
+    def nlc_grid(self):
+        """Points (N x 3) and weights of the NLC grid (after nlc_vv10)."""
+        n = C.c_long(-1)
+        self.ctx.lib.occ_xc_nlc_grid_points(self.h, C.byref(n))
+        if n.value < 0:
+            raise XCError("the NLC grid is built by the first nlc_vv10 call")
+        P = np.zeros((n.value, 3))
+        W = np.zeros(n.value)
+        self.ctx.lib.occ_xc_nlc_grid(self.h, _ptr(P), _ptr(W))
+        return P, W
 
     def compute_xc_gradient(self, D):
         """dE_xc/dR (natoms x 3, Hartree/Bohr) for mo.D = D with the grid held

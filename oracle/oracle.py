@@ -213,3 +213,43 @@ def xc_build_unrestricted(basis, points, weights, D, method, screen=1e-10,
     if rc != 0:
         raise RuntimeError(f"oracle_xc_build_unrestricted failed ({rc})")
     return exc.value, V, nel
+
+
+NLC_GRID = dict(max_angular_points=110, min_angular_points=50, radial_points=50,
+                radial_precision=1e-7)  # src/dft/nonlocal_correlation.cpp set_integration_grid
+
+
+def vv10_kernel(points, weights, rho, sigma, b=6.0, c=0.01, nthreads=0):
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    r = np.ascontiguousarray(rho, dtype=np.float64)
+    s = np.ascontiguousarray(sigma, dtype=np.float64)
+    n = len(w)
+    out = [np.zeros(n) for _ in range(3)]
+    L = lib()
+    L.oracle_vv10_kernel.argtypes = [C.c_long, _dp, _dp, _dp, _dp, C.c_double, C.c_double,
+                                     C.c_int, _dp, _dp, _dp]
+    L.oracle_vv10_kernel(n, _p(pts), _p(w), _p(r), _p(s), b, c, nthreads, *[_p(x) for x in out])
+    return out
+
+
+def nlc_vv10(basis, points, weights, D, b=6.0, c=0.01, nthreads=0, want_V=True):
+    """Energy and V (nbf x nbf) of VV10 on the given NLC grid (in grid order)."""
+    l, nprim, off, exps, coefs, origin = _basis_arrays(basis)
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    nbf = basis.nbf()
+    Df = np.asfortranarray(D, dtype=np.float64)
+    V = np.zeros((nbf, nbf), order="F") if want_V else None
+    e = C.c_double()
+    L = lib()
+    L.oracle_nlc_vv10.restype = C.c_int
+    L.oracle_nlc_vv10.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, C.c_int, C.c_long, _dp,
+                                  _dp, _dp, C.c_double, C.c_double, C.c_int, _dp, _dp]
+    rc = L.oracle_nlc_vv10(len(l), _p(l, _ip), _p(nprim, _ip), _p(off, _ip), _p(exps),
+                           _p(coefs), _p(origin), int(basis.pure), len(w), _p(pts), _p(w),
+                           Df.ctypes.data_as(_dp), b, c, nthreads,
+                           V.ctypes.data_as(_dp) if want_V else None, C.byref(e))
+    if rc != 0:
+        raise RuntimeError("oracle_nlc_vv10 failed")
+    return e.value, V

@@ -1070,3 +1070,148 @@ extern "C" int oracle_xc_build_unrestricted(
   }
   return 0;
 }
+
+// VV10 non-local correlation, restated from src/dft/nonlocal_correlation.cpp:
+// vv10_kernel (:37-110) over the points in the given (grid) order -- as the
+// reference writes it, each point i sums its partners j < i only, with half
+// of its own r = 0 term -- and vv10 (:331-388): the density with the whole
+// basis (no screening) on the NLC grid, E = sum exc rho, V = k + k^T with
+// k = phi^T (0.5 vrho phi + 2 vsigma grad rho . grad phi).
+extern "C" void oracle_vv10_kernel(long n, const double *points, const double *weights,
+                                   const double *rho, const double *sigma, double b, double C,
+                                   int nthreads, double *exc, double *vrho, double *vsigma) {
+  const double pi = 3.14159265358979323846, pi4_3 = 4.0 * pi / 3.0;
+  const double kappa_factor = b * 1.5 * pi * std::pow(9.0 * pi, -1.0 / 6.0);
+  const double beta = std::pow(3.0 / (b * b), 0.75) / 32.0;
+  std::vector<double> rw(n), tmp(n), om(n), dom_r(n), dom_g(n), kap(n), dkap(n), F(n, 0.0),
+      U(n, 0.0), W(n, 0.0);
+  for (long i = 0; i < n; i++) {
+    rw[i] = rho[i] * weights[i];
+    double t = sigma[i] / (rho[i] * rho[i]);
+    t = C * t * t;
+    tmp[i] = t;
+    om[i] = std::sqrt(t + pi4_3 * rho[i]);
+    dom_r[i] = (0.5 * pi4_3 * rho[i] - 2.0 * t) / om[i];
+    dom_g[i] = t * rho[i] / (sigma[i] * om[i]);
+    kap[i] = kappa_factor * std::pow(rho[i], 1.0 / 6.0);
+    dkap[i] = kap[i] / 6.0;
+  }
+#ifdef _OPENMP
+  int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  int nt = 1;
+  (void)nthreads;
+#endif
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
+  for (long i = 0; i < n; i++) {
+    if (rho[i] < 1e-8)
+      continue;
+    const double k = kap[i];
+    double f = rw[i] / (2 * k * k * k);
+    double u = f * (1.0 / k + 1.0 / (2 * k));
+    double w = 0.0;
+    for (long j = 0; j < i; j++) {
+      if (rho[j] < 1e-8)
+        continue;
+      const double dx = points[3 * i] - points[3 * j], dy = points[3 * i + 1] - points[3 * j + 1],
+                   dz = points[3 * i + 2] - points[3 * j + 2];
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      const double gi = r2 * om[i] + kap[i];
+      const double gj = r2 * om[j] + kap[j];
+      double t = 2 * rw[j] / (gi * gj * (gi + gj));
+      f += t;
+      t *= 1.0 / gi + 1.0 / (gi + gj);
+      u += t;
+      w += t * r2;
+    }
+    F[i] = f * -1.5;
+    U[i] = u;
+    W[i] = w;
+  }
+  for (long i = 0; i < n; i++) {
+    exc[i] = (beta + 0.5 * F[i]) * weights[i];
+    vrho[i] = (beta + F[i] + 1.5 * (U[i] * dkap[i] + W[i] * dom_r[i])) * weights[i];
+    vsigma[i] = (1.5 * W[i] * dom_g[i]) * weights[i];
+  }
+}
+
+extern "C" int oracle_nlc_vv10(int nsh, const int *sh_l, const int *sh_nprim, const int *sh_off,
+                               const double *exps, const double *coefs, const double *sh_origin,
+                               int pure, long npts, const double *points, const double *weights,
+                               const double *D, double b, double C, int nthreads, double *V,
+                               double *energy) {
+  Basis bs{nsh, sh_l, sh_nprim, sh_off, exps, coefs, sh_origin, pure != 0, {}, 0};
+  bs.first_bf.resize(nsh);
+  int nbf = 0;
+  for (int s = 0; s < nsh; s++) {
+    bs.first_bf[s] = nbf;
+    nbf += bs.size(s);
+  }
+  bs.nbf = nbf;
+  const long n = npts;
+  // phi, grad phi of every AO at every point: [comp][nbf][n]
+  std::vector<double> phi(static_cast<size_t>(4) * nbf * n, 0.0);
+#ifdef _OPENMP
+  int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  int nt = 1;
+#endif
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 1)
+  for (int s = 0; s < nsh; s++) {
+    int nf = bs.size(s);
+    std::vector<double> tmp(static_cast<size_t>(4) * nf * n);
+    collocate(sh_l[s], bs.pure, sh_nprim[s], exps + sh_off[s], coefs + sh_off[s],
+              sh_origin + 3 * s, n, points, 3, 1, tmp.data(), n);
+    for (int q = 0; q < 4; q++)
+      for (int f = 0; f < nf; f++)
+        std::memcpy(&phi[(static_cast<size_t>(q) * nbf + bs.first_bf[s] + f) * n],
+                    &tmp[(static_cast<size_t>(q) * nf + f) * n], sizeof(double) * n);
+  }
+  // density with D2 = 2 D (src/gto/density.cpp:33-43)
+  std::vector<double> rho(4 * n, 0.0);
+#pragma omp parallel for num_threads(nt) schedule(static)
+  for (long p = 0; p < n; p++) {
+    for (int j = 0; j < nbf; j++) {
+      double x = 0.0;
+      for (int k = 0; k < nbf; k++)
+        x += phi[static_cast<size_t>(k) * n + p] * 2.0 * D[static_cast<size_t>(j) * nbf + k];
+      rho[p] += phi[static_cast<size_t>(j) * n + p] * x;
+      for (int q = 1; q < 4; q++)
+        rho[q * n + p] += 2.0 * phi[(static_cast<size_t>(q) * nbf + j) * n + p] * x;
+    }
+  }
+  std::vector<double> sigma(n), exc(n), vr(n), vs(n);
+  for (long p = 0; p < n; p++)
+    sigma[p] = rho[n + p] * rho[n + p] + rho[2 * n + p] * rho[2 * n + p] +
+               rho[3 * n + p] * rho[3 * n + p];
+  oracle_vv10_kernel(n, points, weights, rho.data(), sigma.data(), b, C, nthreads, exc.data(),
+                     vr.data(), vs.data());
+  double e = 0.0;
+  for (long p = 0; p < n; p++)
+    e += exc[p] * rho[p];
+  *energy = e;
+  if (V) {
+    // Y = 0.5 vrho phi + 2 vsigma grad rho . grad phi; k = phi^T Y; V = k + k^T
+    std::vector<double> Y(static_cast<size_t>(nbf) * n), K(static_cast<size_t>(nbf) * nbf);
+    for (int j = 0; j < nbf; j++)
+      for (long p = 0; p < n; p++) {
+        double y = 0.5 * vr[p] * phi[static_cast<size_t>(j) * n + p];
+        for (int q = 1; q < 4; q++)
+          y += 2.0 * vs[p] * rho[q * n + p] * phi[(static_cast<size_t>(q) * nbf + j) * n + p];
+        Y[static_cast<size_t>(j) * n + p] = y;
+      }
+#pragma omp parallel for num_threads(nt) schedule(static)
+    for (int j = 0; j < nbf; j++)
+      for (int i = 0; i < nbf; i++) {
+        double acc = 0.0;
+        for (long p = 0; p < n; p++)
+          acc += phi[static_cast<size_t>(i) * n + p] * Y[static_cast<size_t>(j) * n + p];
+        K[static_cast<size_t>(j) * nbf + i] = acc;
+      }
+    for (int j = 0; j < nbf; j++)
+      for (int i = 0; i < nbf; i++)
+        V[static_cast<size_t>(j) * nbf + i] =
+            K[static_cast<size_t>(j) * nbf + i] + K[static_cast<size_t>(i) * nbf + j];
+  }
+  return 0;
+}

@@ -95,6 +95,18 @@ int oracle_xc_build_unrestricted(int nsh, const int *sh_l, const int *sh_nprim,
                                  long leaf_target, long leaf_min, long leaf_max, int nthreads,
                                  double *V, double *exc_out, double *nelec2);
 
+// VV10 non-local correlation (src/dft/nonlocal_correlation.cpp:37-110):
+// per point exc, vrho, vsigma (weighted) from rho, sigma in the given order.
+void oracle_vv10_kernel(long n, const double *points, const double *weights, const double *rho,
+                        const double *sigma, double b, double C, int nthreads, double *exc,
+                        double *vrho, double *vsigma);
+// NonLocalCorrelationFunctional::vv10 (nonlocal_correlation.cpp:331-388) on
+// the given NLC grid: energy and (if V) V (nbf x nbf) for mo.D = D.
+int oracle_nlc_vv10(int nsh, const int *sh_l, const int *sh_nprim, const int *sh_off,
+                    const double *exps, const double *coefs, const double *sh_origin, int pure,
+                    long npts, const double *points, const double *weights, const double *D,
+                    double b, double C, int nthreads, double *V, double *energy);
+
 // The restricted XC nuclear gradient (include/occ/dft/dft.h:599-749,
 // src/dft/dft_gradient_kernels.cpp:472-595), screened path, grid weights held
 // fixed.  sh_atom: atom of each shell; grad[3 * natoms] (x, y, z per atom)
