@@ -50,12 +50,14 @@ def parse():
     ap.add_argument("--ctas", type=int, default=0,
                     help="CTAs of the persistent tensor-core kernels (0: one per SM)")
     ap.add_argument("--workload", default="water32",
-                    choices=["water32", "alkane", "clusters", "stream", "gradient", "grid"],
+                    choices=["water32", "alkane", "clusters", "stream", "gradient", "grid", "uks",
+                             "vv10"],
                     help="water32: the headline build (default); alkane: C30H62 def2-TZVP "
                          "B3LYP, 15 iterations as one CUDA graph; clusters: 512 clusters "
                          "as one batch; stream: served Poisson request stream; gradient: "
                          "the FP64 XC nuclear gradient of the water32 molecule; grid: its molecular "
-                         "grid with the Becke partition on the GPU")
+                         "grid with the Becke partition on the GPU; uks: an unrestricted FP64 "
+                         "build of its cation radical; vv10: its VV10 non-local correlation")
     ap.add_argument("--clusters", type=int, default=512)
     ap.add_argument("--requests", type=int, default=32)
     ap.add_argument("--rate", type=float, default=10.0, help="stream arrivals per second")
@@ -77,8 +79,25 @@ def run_workload(args):
             r = bw.xc_gradient(torch, steps=args.steps, warmup=args.warmup, waters=args.waters)
         elif args.workload == "grid":
             r = bw.grid_setup(steps=args.steps, warmup=args.warmup, waters=args.waters)
+        elif args.workload == "uks":
+            r = bw.uks_build(torch, steps=args.steps, warmup=args.warmup, waters=args.waters)
+        elif args.workload == "vv10":
+            r = bw.vv10(steps=args.steps, warmup=args.warmup, waters=args.waters)
         else:
             r = bw.stream(nreq=args.requests, rate=args.rate)
+    if args.workload in ("uks", "vv10"):
+        unit = "builds/s" if args.workload == "uks" else "calls/s"
+        value = r.pop("builds_per_s") if args.workload == "uks" else r["mixed"]["calls_per_s"]
+        line = {"metric": ("UKS XC builds/s (FP64)" if args.workload == "uks"
+                           else "VV10 non-local correlation calls/s (FP32 pair sums)"),
+                "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if args.workload == "uks" else "f32+f64",
+                "data": "synthetic", "config": {"workload": r.pop("workload")},
+                "clocks": cs.summary()}
+        line.update(r)
+        print(json.dumps(line))
+        return
     if args.workload == "grid":
         line = {"metric": "molecular grid points/s (Becke partition)",
                 "value": r.pop("points_per_s"), "unit": "points/s", "n_gpus": 1,

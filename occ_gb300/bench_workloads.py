@@ -25,6 +25,12 @@ grid            molecular grid of 32 waters (def2-SVP, 965,504 points): the
                 Becke partition on the GPU against the host restatement on all
                 host cores, and the whole molecule set-up (grid, leaves,
                 screening, upload) that a DFT object or a served session pays.
+uks             unrestricted (UKS) FP64 build of a 32-water cation radical
+                (def2-SVP, PBE, 160 alpha / 159 beta orbitals): builds/s through
+                the device entry point (CUDA events) and the host one, and the
+                restricted FP64 build of the same molecule for scale.
+vv10            VV10 non-local correlation of 32 waters (def2-SVP, 254,976
+                NLC points): FP64 and FP32-pair-sum calls, their difference.
 
 Every input is seeded synthetic data with the shapes of these workloads.
 Each function returns a dict for one JSON line.
@@ -315,3 +321,74 @@ def grid_setup(steps=3, warmup=1, waters=32, seed=0):
             "cpu_baseline": {"value": n / t_host, "unit": "points/s", "cores": os.cpu_count(),
                              "kind": "port", "sample": "the whole grid of the same molecule",
                              "s_per_grid": t_host}}
+
+
+def uks_build(torch, steps=5, warmup=2, waters=32, seed=0):
+    box = 10.0 * (waters / 32.0) ** (1.0 / 3.0)
+    mol = wl.water_cluster(waters, box=box, seed=seed)
+    b = wl.basis_for(mol, "def2-svp")
+    nbf = b.nbf()
+    D = wl.random_density_unrestricted(nbf, 5 * waters, 5 * waters - 1, seed=seed)
+    Dr = wl.random_density(nbf, 5 * waters, seed=seed)
+    dft = DFT("pbe", b)
+    lib = dft.ctx.lib
+    dD = torch.from_numpy(np.asfortranarray(D).ravel(order="F").copy()).cuda()
+    dV = torch.zeros_like(dD)
+    d3 = torch.zeros(3, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def one():
+        rc = lib.occ_xc_compute_vxc_unrestricted_device(
+            dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), FP64, C.c_void_p(dV.data_ptr()),
+            C.c_void_p(d3.data_ptr()), C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(dft.ctx.error())
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for i in range(steps):
+        one()
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        V = dft.compute_vxc(D, FP64)
+    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    t0 = time.perf_counter()
+    dft.compute_vxc(Dr, FP64)
+    r_ms = (time.perf_counter() - t0) * 1e3
+    return {"workload": f"water{waters}_cation_def2svp_pbe_uks_fp64", "nbf": nbf,
+            "builds_per_s": 1e3 / ms, "ms_per_build": ms,
+            "e2e": {"value": 1e3 / e2e_ms, "unit": "builds/s",
+                    "h2d_bytes_per_step": int(D.size * 8), "d2h_bytes_per_step": int(D.size * 8 + 8)},
+            "exc": float(d3[0].item()), "nelec_ab": [float(d3[1].item()), float(d3[2].item())],
+            "restricted_fp64_ms_e2e": r_ms}
+
+
+def vv10(steps=3, warmup=1, waters=32, seed=0):
+    box = 10.0 * (waters / 32.0) ** (1.0 / 3.0)
+    mol = wl.water_cluster(waters, box=box, seed=seed)
+    b = wl.basis_for(mol, "def2-svp")
+    D = wl.random_density(b.nbf(), 5 * waters, seed=seed)
+    dft = DFT("pbe", b)
+    out = {"workload": f"water{waters}_def2svp_vv10"}
+    res = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        for _ in range(warmup):
+            dft.nlc_vv10(D, precision=prec)
+        t0 = time.perf_counter()
+        for _ in range(steps if name == "mixed" else 1):
+            e, V = dft.nlc_vv10(D, precision=prec)
+        s = (time.perf_counter() - t0) / (steps if name == "mixed" else 1)
+        res[name] = (e, V)
+        out[name] = {"calls_per_s": 1.0 / s, "s_per_call": s, "energy": e}
+    P, W = dft.nlc_grid()
+    n = len(W)
+    out["nlc_points"] = n
+    out["pairs"] = n * (n - 1) / 2
+    out["abs_dE_mixed_vs_fp64"] = abs(res["mixed"][0] - res["fp64"][0])
+    out["max_abs_dV_mixed_vs_fp64"] = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1])))
+    return out

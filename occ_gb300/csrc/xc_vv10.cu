@@ -25,8 +25,9 @@
 //                             the longest rows of the triangle first;
 //                             OCC_XC_MIXED: k_vv10_pairs32, the same sums in
 //                             FP32 (double-float coordinate differences,
-//                             Kahan sums flushed to FP64 per tile), about 50x
-//                             the FP64 pipe's rate on this GPU
+//                             one approximate reciprocal, Kahan sums flushed
+//                             to FP64 per tile), the triangle spread over
+//                             CTAs of 16 partner tiles each
 //   k_vv10_final              exc, vrho, vsigma (:97-108), E partials, and
 //                             the V coefficients 0.5 vrho, 2 vsigma grad rho
 //   k_vxc_f64                 V = k + k^T (:373-386), the build's own kernel
@@ -101,10 +102,13 @@ __global__ void k_vv10_prep32(long n, const VvPoint *__restrict__ p,
   f32_pair(P.x, Q.xh, Q.xl);
   f32_pair(P.y, Q.yh, Q.yl);
   f32_pair(P.z, Q.zh, Q.zl);
-  Q.om = static_cast<float>(P.om);
-  Q.kap = static_cast<float>(P.kap);
-  Q.rw2 = static_cast<float>(P.rw2);
-  Q.active = static_cast<float>(P.active);
+  // a point below the density cut takes part as an exact zero (finite
+  // omega0 and kappa, no weight), so that the pair loop needs no branch
+  const bool act = P.active != 0.0;
+  Q.om = act ? static_cast<float>(P.om) : 1.0f;
+  Q.kap = act ? static_cast<float>(P.kap) : 1.0f;
+  Q.rw2 = act ? static_cast<float>(P.rw2) : 0.0f;
+  Q.active = act ? 1.0f : 0.0f;
   q[i] = Q;
 }
 
@@ -180,15 +184,48 @@ __global__ void __launch_bounds__(kVvTile)
   }
 }
 
-// The pair sums alone (no self term) in FP32 with Kahan-compensated sums per
-// tile, flushed to FP64 after every tile of 128 partners.  Each term is
-// within a few FP32 roundings of the FP64 term; the sums keep FP32's
-// relative precision.
+// The pair sums alone (no self term) in FP32.  Block (x, y): rows of tile
+// b = ntiles - 1 - x against partner tiles [16 y, 16 y + 15] (clipped to
+// b), so that the triangle spreads over many CTAs; two Kahan-compensated
+// accumulator sets per thread (even and odd partners), flushed to FP64 per
+// partner tile, and one FP64 atomic add per row and sum at the end (FUW
+// zeroed before).
+constexpr int kVvChunk = 16; // partner tiles per CTA
+
+// 1/x to about one ulp in one instruction (the pair sums' other roundings
+// are of the same size)
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void vv_pair32(const VvPoint32 &P, const VvPoint32 &Q, float &fs,
+                                          float &fc, float &us, float &uc, float &ws, float &wc) {
+  const float dx = __fadd_rn(__fsub_rn(P.xh, Q.xh), __fsub_rn(P.xl, Q.xl));
+  const float dy = __fadd_rn(__fsub_rn(P.yh, Q.yh), __fsub_rn(P.yl, Q.yl));
+  const float dz = __fadd_rn(__fsub_rn(P.zh, Q.zh), __fsub_rn(P.zl, Q.zl));
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float gi = fmaf(r2, P.om, P.kap);
+  const float gj = fmaf(r2, Q.om, Q.kap);
+  const float sg = gi + gj;
+  const float inv = rcp_approx(gi * gj * sg);
+  const float t = Q.rw2 * inv;
+  kahan(fs, fc, t);
+  const float t2 = t * ((sg + gi) * gj * inv); // t (1/g_i + 1/(g_i + g_j))
+  kahan(us, uc, t2);
+  kahan(ws, wc, t2 * r2);
+}
+
 __global__ void __launch_bounds__(kVvTile)
     k_vv10_pairs32(long n, const VvPoint32 *__restrict__ pts, double *__restrict__ FUW) {
   __shared__ VvPoint32 sp[kVvTile];
   const long ntiles = (n + kVvTile - 1) / kVvTile;
   const long b = ntiles - 1 - blockIdx.x;
+  const long jt0 = static_cast<long>(blockIdx.y) * kVvChunk;
+  if (jt0 > b)
+    return; // the whole CTA: beyond this row tile's triangle
+  const long jt1 = min(jt0 + kVvChunk - 1, b);
   const long i = b * kVvTile + threadIdx.x;
   const bool iv = i < n;
   VvPoint32 P{};
@@ -196,49 +233,39 @@ __global__ void __launch_bounds__(kVvTile)
     P = pts[i];
   const bool act = iv && P.active != 0.0f;
   double F = 0.0, U = 0.0, W = 0.0;
-  for (long jt = 0; jt <= b; jt++) {
+  for (long jt = jt0; jt <= jt1; jt++) {
     const long jl = jt * kVvTile + threadIdx.x;
-    if (jl < n)
+    if (jl < n) {
       sp[threadIdx.x] = pts[jl];
-    else
-      sp[threadIdx.x].active = 0.0f;
+    } else {
+      VvPoint32 z{};
+      z.om = z.kap = 1.0f;
+      sp[threadIdx.x] = z;
+    }
     __syncthreads();
     if (act) {
-      float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
+      float a[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, c[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       const int jmax = (jt == b) ? static_cast<int>(threadIdx.x) : kVvTile;
-      for (int jj = 0; jj < jmax; jj++) {
-        const VvPoint32 &Q = sp[jj];
-        if (Q.active == 0.0f)
-          continue;
-        const float dx = __fadd_rn(__fsub_rn(P.xh, Q.xh), __fsub_rn(P.xl, Q.xl));
-        const float dy = __fadd_rn(__fsub_rn(P.yh, Q.yh), __fsub_rn(P.yl, Q.yl));
-        const float dz = __fadd_rn(__fsub_rn(P.zh, Q.zh), __fsub_rn(P.zl, Q.zl));
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float gi = fmaf(r2, P.om, P.kap);
-        const float gj = fmaf(r2, Q.om, Q.kap);
-        const float sg = gi + gj;
-        const float inv = __frcp_rn(gi * gj * sg);
-        const float t = Q.rw2 * inv;
-        kahan(fs, fc, t);
-        const float t2 = t * ((sg + gi) * gj * inv);
-        kahan(us, uc, t2);
-        kahan(ws, wc, t2 * r2);
+      int jj = 0;
+      for (; jj + 1 < jmax; jj += 2) {
+        vv_pair32(P, sp[jj], a[0], a[1], a[2], a[3], a[4], a[5]);
+        vv_pair32(P, sp[jj + 1], c[0], c[1], c[2], c[3], c[4], c[5]);
       }
-      F += static_cast<double>(fs) - static_cast<double>(fc);
-      U += static_cast<double>(us) - static_cast<double>(uc);
-      W += static_cast<double>(ws) - static_cast<double>(wc);
+      if (jj < jmax)
+        vv_pair32(P, sp[jj], a[0], a[1], a[2], a[3], a[4], a[5]);
+      F += (static_cast<double>(a[0]) - a[1]) + (static_cast<double>(c[0]) - c[1]);
+      U += (static_cast<double>(a[2]) - a[3]) + (static_cast<double>(c[2]) - c[3]);
+      W += (static_cast<double>(a[4]) - a[5]) + (static_cast<double>(c[4]) - c[5]);
     }
     __syncthreads();
   }
-  if (iv) {
-    FUW[3 * i] = F;
-    FUW[3 * i + 1] = U;
-    FUW[3 * i + 2] = W;
+  if (act) {
+    atomicAdd(&FUW[3 * i], F);
+    atomicAdd(&FUW[3 * i + 1], U);
+    atomicAdd(&FUW[3 * i + 2], W);
   }
 }
 
-// Per sorted point: exc, vrho, vsigma (weighted) -> E partial per block and
-// the V coefficients (0.5 vrho, 2 vsigma grad rho) in sorted order.
 // pair_only: FUW holds the pair sums alone; the self term (rho w / (2 k^3)
 // in f, f (1/k + 1/(2k)) in u) and the -1.5 are applied here.
 __global__ void __launch_bounds__(256)
@@ -376,9 +403,12 @@ void Molecule::nlc_vv10(const double *dD, double b, double C, int precision, dou
       k_vv10_prep32<<<blocks, 256, 0, st>>>(n, static_cast<const VvPoint *>(N.d_nlc_pts),
                                             static_cast<VvPoint32 *>(N.d_nlc_pts32));
     });
+    cuda_check(cudaMemsetAsync(N.d_nlc_fuw, 0, 3 * static_cast<size_t>(std::max<long>(n, 1)) *
+                                                  sizeof(double), st),
+               "cudaMemsetAsync");
     c.launch("vv10_pairs32", st, [&] {
       if (tiles > 0)
-        k_vv10_pairs32<<<tiles, kVvTile, 0, st>>>(
+        k_vv10_pairs32<<<dim3(tiles, (tiles + kVvChunk - 1) / kVvChunk), kVvTile, 0, st>>>(
             n, static_cast<const VvPoint32 *>(N.d_nlc_pts32), N.d_nlc_fuw);
     });
   } else {
