@@ -55,7 +55,7 @@ def parse():
                     help="water32: the headline build (default); alkane: C30H62 def2-TZVP "
                          "B3LYP, 15 iterations as one CUDA graph; clusters: 512 clusters "
                          "as one batch; stream: served Poisson request stream; gradient: "
-                         "the FP64 XC nuclear gradient of the water32 molecule; grid: its molecular "
+                         "the XC nuclear gradient of the water32 molecule; grid: its molecular "
                          "grid with the Becke partition on the GPU; uks: an unrestricted FP64 "
                          "build of its cation radical; vv10: its VV10 non-local correlation")
     ap.add_argument("--clusters", type=int, default=512)
@@ -109,9 +109,11 @@ def run_workload(args):
         print(json.dumps(line))
         return
     if args.workload == "gradient":
-        line = {"metric": "XC nuclear gradients/s (FP64)", "value": r.pop("gradients_per_s"),
+        line = {"metric": "XC nuclear gradients/s (tensor-core 3xTF32, FP64 beside it)",
+                "value": r["mixed"]["gradients_per_s"],
                 "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "tf32x3+f64",
                 "data": "synthetic", "config": {"workload": r.pop("workload")},
                 "clocks": cs.summary()}
         line.update(r)

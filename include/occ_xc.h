@@ -188,20 +188,22 @@ int occ_xc_nlc_grid(const occ_xc_molecule *mol, double *points, double *weights)
 
 /* Replaces DFT::compute_xc_gradient(mo) for a restricted wavefunction
  * (include/occ/dft/dft.h:599-749, src/dft/dft_gradient_kernels.cpp:472-595):
- * dE_xc/dR with the grid held fixed, FP64.  grad[3*natoms] receives
- * x, y, z per atom in Hartree/Bohr (the memory of OCC's 3 x natoms Mat3N);
- * exc (may be NULL) the E_xc of the same density.  Host buffers; blocking.
- * The first call allocates the gradient's workspace (AO values with second
- * derivatives for a GGA, capped at 8 GiB per leaf group). */
+ * dE_xc/dR with the grid held fixed.  grad[3*natoms] receives x, y, z per
+ * atom in Hartree/Bohr (the memory of OCC's 3 x natoms Mat3N); exc (may be
+ * NULL) the E_xc of the same density.  precision: OCC_XC_FP64 (every
+ * operation FP64; the first call allocates a workspace of AO values with
+ * second derivatives, capped at 8 GiB per leaf group), or OCC_XC_MIXED (the
+ * contractions on the tensor cores in 3xTF32, in a workspace beside the
+ * build's).  Host buffers; blocking. */
 int occ_xc_compute_xc_gradient(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D,
-                               double *grad, double *exc);
+                               int precision, double *grad, double *exc);
 
 /* Same on device buffers, asynchronous on `stream` (NULL: the context's).
  * d_exc2 (may be NULL) receives {E_xc, integrated density}.  Allocates on a
- * molecule's first gradient only. */
+ * molecule's first gradient of each precision only. */
 int occ_xc_compute_xc_gradient_device(occ_xc_context *ctx, occ_xc_molecule *mol,
-                                      const double *d_D, double *d_grad, double *d_exc2,
-                                      void *stream);
+                                      const double *d_D, int precision, double *d_grad,
+                                      double *d_exc2, void *stream);
 
 /* Cap (bytes) of the gradient workspace of one leaf group; leaves are
  * processed in groups under it (0: the default, 8 GiB).  Frees the

@@ -158,13 +158,15 @@ public:
   }
 
   // compute_xc_gradient(mo) (dft.h:599-749): dE_xc/dR with the grid held
-  // fixed, FP64; 3 * natoms values, x, y, z per atom (the memory of OCC's
+  // fixed; 3 * natoms values, x, y, z per atom (the memory of OCC's
   // 3 x natoms Mat3N).  Also sets exchange_correlation_energy().
-  std::vector<double> compute_xc_gradient(const std::vector<double> &D) {
+  std::vector<double> compute_xc_gradient(const std::vector<double> &D,
+                                          Precision precision = Precision::FP64) {
     if (D.size() != nbf_ * nbf_)
       throw Error("density matrix must be nbf x nbf", OCC_XC_ERR_ARG);
     std::vector<double> g(3 * natoms_);
-    check(occ_xc_compute_xc_gradient(ctx_, mol_.get(), D.data(), g.data(), &exc_));
+    check(occ_xc_compute_xc_gradient(ctx_, mol_.get(), D.data(), static_cast<int>(precision),
+                                     g.data(), &exc_));
     return g;
   }
 

@@ -16,11 +16,11 @@ stream          Poisson arrivals (seeded rate) of requests of 8-20 SCF
                 serving loop (continuous batching, 150 GB budget); p50 / p99
                 latency (submit to result ready) and throughput, mixed and
                 FP64.
-gradient        XC nuclear gradient (FP64) of 32 waters, def2-SVP, PBE (the
-                headline molecule): gradients/s through the device entry point
-                (CUDA events) and through the host one (D in, gradient out),
-                parity with the oracle, the oracle's own time on the host
-                cores, and the FP64 rate of the contractions.
+gradient        XC nuclear gradient of 32 waters, def2-SVP, PBE (the headline
+                molecule), FP64 and tensor-core (mixed): gradients/s through
+                the device entry point (CUDA events) and through the host one
+                (D in, gradient out), parity with the oracle, the oracle's own
+                time on the host cores, and the FP64 rate of the contractions.
 grid            molecular grid of 32 waters (def2-SVP, 965,504 points): the
                 Becke partition on the GPU against the host restatement on all
                 host cores, and the whole molecule set-up (grid, leaves,
@@ -242,31 +242,44 @@ def xc_gradient(torch, steps=5, warmup=3, waters=32, method="pbe", seed=0):
     dg = torch.zeros(3 * natoms, dtype=torch.float64, device="cuda")
     de = torch.zeros(2, dtype=torch.float64, device="cuda")
     stream = torch.cuda.Stream()
-
-    def one():
-        rc = lib.occ_xc_compute_xc_gradient_device(dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()),
-                                                   C.c_void_p(dg.data_ptr()),
-                                                   C.c_void_p(de.data_ptr()),
-                                                   C.c_void_p(stream.cuda_stream))
-        if rc != 0:
-            raise RuntimeError(dft.ctx.error())
-    for _ in range(warmup):
-        one()
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-    ev[0].record(stream)
-    for i in range(steps):
-        one()
-        ev[i + 1].record(stream)
-    torch.cuda.synchronize()
-    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
-    ms = float(np.median(per))
-    g_dev = dg.cpu().numpy().reshape(natoms, 3)
-    # end to end through the host entry point: D from host memory, gradient back
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        g = dft.compute_xc_gradient(D)
-    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    flops = info["flops_per_build"] * (1.5 if info["deriv"] else 1.0)
+    out = {"workload": f"water{waters}_def2svp_{method}_xc_gradient", "natoms": natoms,
+           "nbf": b.nbf(), "npoints": info["npoints"], "useful_flops_per_gradient": flops}
+    grads = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        def one():
+            rc = lib.occ_xc_compute_xc_gradient_device(
+                dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), prec, C.c_void_p(dg.data_ptr()),
+                C.c_void_p(de.data_ptr()), C.c_void_p(stream.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(dft.ctx.error())
+        for _ in range(warmup):
+            one()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record(stream)
+        for i in range(steps):
+            one()
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
+        g_dev = dg.cpu().numpy().reshape(natoms, 3)
+        # end to end through the host entry point: D from host memory, gradient back
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            g = dft.compute_xc_gradient(D, prec)
+        e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+        grads[name] = g
+        out[name] = {"gradients_per_s": 1e3 / ms, "ms_per_gradient": ms,
+                     "e2e": {"value": 1e3 / e2e_ms, "unit": "gradients/s",
+                             "h2d_bytes_per_step": int(D.size * 8),
+                             "d2h_bytes_per_step": int(3 * natoms * 8 + 16)},
+                     "max_abs_dgrad_device_vs_host": float(np.max(np.abs(g_dev - g)))}
+    out["fp64"]["roofline"] = {
+        "bound": "fp64", "achieved": flops / (out["fp64"]["ms_per_gradient"] * 1e-3) / 1e12,
+        "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+        "frac": flops / (out["fp64"]["ms_per_gradient"] * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
+        "peak_source": "nominal GB300 FP64"}
     # the oracle on the host cores, and parity
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     sys.path.insert(0, os.path.join(root, "oracle"))
@@ -275,23 +288,12 @@ def xc_gradient(torch, steps=5, warmup=3, waters=32, method="pbe", seed=0):
     t0 = time.perf_counter()
     g_ref = oracle.xc_gradient(b, P, W, D, method)
     cpu_s = time.perf_counter() - t0
-    flops = info["flops_per_build"] * (1.5 if info["deriv"] else 1.0)
-    return {"workload": f"water{waters}_def2svp_{method}_xc_gradient_fp64",
-            "natoms": natoms, "nbf": b.nbf(), "npoints": info["npoints"],
-            "gradients_per_s": 1e3 / ms, "ms_per_gradient": ms,
-            "e2e": {"value": 1e3 / e2e_ms, "unit": "gradients/s",
-                    "h2d_bytes_per_step": int(D.size * 8),
-                    "d2h_bytes_per_step": int(3 * natoms * 8 + 16)},
-            "max_abs_dgrad_vs_oracle": float(np.max(np.abs(g - g_ref))),
-            "max_abs_dgrad_device_vs_host": float(np.max(np.abs(g_dev - g))),
-            "useful_flops_per_gradient": flops,
-            "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12,
-                         "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                         "frac": flops / (ms * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
-                         "peak_source": "nominal GB300 FP64"},
-            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "gradients/s",
-                             "cores": os.cpu_count(), "kind": "port",
-                             "sample": "one full gradient of the same molecule"}}
+    out["max_abs_dgrad_fp64_vs_oracle"] = float(np.max(np.abs(grads["fp64"] - g_ref)))
+    out["max_abs_dgrad_mixed_vs_oracle"] = float(np.max(np.abs(grads["mixed"] - g_ref)))
+    out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "gradients/s", "cores": os.cpu_count(),
+                           "kind": "port", "sample": "one full gradient of the same molecule"}
+    out["e2e"] = out["mixed"]["e2e"]
+    return out
 
 
 def grid_setup(steps=3, warmup=1, waters=32, seed=0):

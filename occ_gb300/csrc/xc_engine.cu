@@ -103,6 +103,7 @@ Molecule::~Molecule() {
   for (void *p : allocations)
     cudaFree(p);
   free_mixed(mixed);
+  free_grad_mixed(gmixed);
 }
 
 void *Molecule::alloc(size_t bytes) {
@@ -469,6 +470,8 @@ void Molecule::release_device() {
   grad_bytes = 0.0;
   d_rho_b = d_coef_b = d_epart_u = d_Dab = d_Vab = d_Duks = d_Vuks = d_out3 = nullptr;
   nlc.reset();
+  free_grad_mixed(gmixed);
+  gmixed = nullptr;
 }
 
 // Device bytes that materialise() allocates -- the resident state, without the

@@ -99,6 +99,8 @@ struct Context {
 };
 
 struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)
+struct GradMixed;  // the tensor-core XC gradient's workspace and plan (xc_mixed.cu)
+void free_grad_mixed(GradMixed *g);
 
 // Default cap of the XC gradient's workspace per leaf group (bytes).
 constexpr size_t kGradWsCapDefault = size_t(8) << 30;
@@ -170,6 +172,7 @@ struct Molecule {
   // VV10: the molecule on OCC's NLC grid (first VV10 call) and, on that
   // molecule, its sorted -> grid-order map and the pair kernel's buffers
   std::unique_ptr<Molecule> nlc;
+  GradMixed *gmixed = nullptr;
   int *d_nlc_perm = nullptr;
   void *d_nlc_pts = nullptr, *d_nlc_pts32 = nullptr;
   double *d_nlc_fuw = nullptr, *d_nlc_epart = nullptr;
@@ -200,6 +203,9 @@ struct Molecule {
   void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
   void prepare_gradient();
   void prepare_uks();
+  void prepare_gradient_mixed();
+  // the same gradient with the contractions on the tensor cores (3xTF32)
+  void xc_gradient_mixed(const double *dD, double *dgrad, double *dout2, cudaStream_t st);
   void prepare_nlc();
   // VV10 energy (dE, one double) and, if dV, its V (nbf x nbf) for mo.D = dD;
   // precision OCC_XC_FP64 or OCC_XC_MIXED (FP32 pair sums)

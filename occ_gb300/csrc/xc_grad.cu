@@ -471,25 +471,41 @@ using namespace occx;
 extern "C" {
 
 int occ_xc_compute_xc_gradient(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D,
-                               double *grad, double *exc) {
+                               int precision, double *grad, double *exc) {
   if (!ctx || !mol || !D || !grad)
+    return OCC_XC_ERR_ARG;
+  if (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED)
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   return guarded(ctx, [&] {
     Molecule &M = *mol->impl;
     cudaStream_t st = ctx->impl->stream;
     const size_t nbf2 = static_cast<size_t>(M.basis.nbf) * M.basis.nbf;
-    M.prepare_gradient();
+    double *dgrad;
+    if (precision == OCC_XC_MIXED) {
+      M.prepare_gradient_mixed();
+      if (!M.d_grad)
+        M.d_grad = static_cast<double *>(M.alloc(std::max<size_t>(3 * M.Z.size(), 1) *
+                                                 sizeof(double)));
+    } else {
+      M.prepare_gradient();
+    }
+    dgrad = M.d_grad;
     cuda_check(cudaMemcpyAsync(M.d_D, D, nbf2 * sizeof(double), cudaMemcpyHostToDevice, st),
                "cudaMemcpyAsync H2D");
-    M.xc_gradient(M.d_D, M.d_grad, M.d_out2, st);
+    if (precision == OCC_XC_MIXED)
+      M.xc_gradient_mixed(M.d_D, dgrad, M.d_out2, st);
+    else
+      M.xc_gradient(M.d_D, dgrad, M.d_out2, st);
     double out2[2];
-    cuda_check(cudaMemcpyAsync(grad, M.d_grad, 3 * M.Z.size() * sizeof(double),
+    cuda_check(cudaMemcpyAsync(grad, dgrad, 3 * M.Z.size() * sizeof(double),
                                cudaMemcpyDeviceToHost, st),
                "cudaMemcpyAsync D2H");
     cuda_check(cudaMemcpyAsync(out2, M.d_out2, sizeof(out2), cudaMemcpyDeviceToHost, st),
                "cudaMemcpyAsync D2H");
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (precision == OCC_XC_MIXED && mixed_error_flag(M, st))
+      throw TimeoutError("a bounded wait of the tensor-core pipeline gave up");
     if (exc)
       *exc = out2[0];
   });
@@ -508,15 +524,20 @@ int occ_xc_molecule_set_gradient_workspace_cap(occ_xc_context *ctx, occ_xc_molec
 }
 
 int occ_xc_compute_xc_gradient_device(occ_xc_context *ctx, occ_xc_molecule *mol,
-                                      const double *d_D, double *d_grad, double *d_exc2,
-                                      void *stream) {
+                                      const double *d_D, int precision, double *d_grad,
+                                      double *d_exc2, void *stream) {
   if (!ctx || !mol || !d_D || !d_grad)
+    return OCC_XC_ERR_ARG;
+  if (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED)
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   return guarded(ctx, [&] {
     Molecule &M = *mol->impl;
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
-    M.xc_gradient(d_D, d_grad, d_exc2 ? d_exc2 : M.d_out2, st);
+    if (precision == OCC_XC_MIXED)
+      M.xc_gradient_mixed(d_D, d_grad, d_exc2 ? d_exc2 : M.d_out2, st);
+    else
+      M.xc_gradient(d_D, d_grad, d_exc2 ? d_exc2 : M.d_out2, st);
   });
 }
 

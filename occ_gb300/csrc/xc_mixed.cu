@@ -1025,12 +1025,23 @@ struct alignas(16) VxcSmem {
 };
 constexpr uint32_t kVxcSmem = 2 * kStageBytes + sizeof(VxcSmem) + 1024;
 
+// Operand planes of k_vxc_tma: K = sum over npairs of (A pair)^T (B pair),
+// each operand as its (hi, lo) TF32 planes.  The build: one pair (phi, Y),
+// the symmetric form for small leaves allowed.  The XC gradient: two pairs
+// (d_c phi, Y) and (Z_c, phi), no symmetry.
+struct VxcPlanes {
+  int a_hi[2], a_lo[2], b_hi[2], b_lo[2];
+  int npairs, allow_sym;
+};
+constexpr VxcPlanes kVxcBuildPlanes{{kPlanePhiHi, 0}, {kPlanePhiLo, 0}, {kPlaneYHi, 0},
+                                    {kPlaneYLo, 0}, 1, 1};
+
 struct VxcWork { // what every role derives from an item
   int mp, rows_a, nblk, i0, nbf_leaf;
   bool sym;
 };
 __device__ __forceinline__ VxcWork vxc_work(const MixTab *tabs, const MBlock *blocks,
-                                            const VItem &it) {
+                                            const VItem &it, const VxcPlanes &pl) {
   const MBlock B = blocks[it.block0];
   VxcWork w;
   w.mp = B.mp;
@@ -1038,7 +1049,7 @@ __device__ __forceinline__ VxcWork vxc_work(const MixTab *tabs, const MBlock *bl
   w.i0 = it.i0;
   w.rows_a = min(128, B.mp - it.i0); // a multiple of 32
   w.nbf_leaf = tabs[B.mol].m.leaves[B.leaf].nbf;
-  w.sym = B.mp <= 128;
+  w.sym = pl.allow_sym && B.mp <= 128;
   return w;
 }
 
@@ -1061,7 +1072,7 @@ __device__ __forceinline__ bool epi_all(bool v) {
 __global__ void __launch_bounds__(kVxcThreads, 1)
     k_vxc_tma(const MixTab *__restrict__ tabs, const MBlock *__restrict__ blocks,
               const VItem *__restrict__ items, int nitems, Override ov, int *queue, int *err,
-              const __grid_constant__ CUtensorMap tmap) {
+              const __grid_constant__ CUtensorMap tmap, VxcPlanes pl) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
   VxcSmem *sm = reinterpret_cast<VxcSmem *>(smem + 2 * kStageBytes);
@@ -1131,11 +1142,12 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
         if (it < 0)
           break;
         const VItem I = items[it];
-        const VxcWork W = vxc_work(tabs, blocks, I);
+        const VxcWork W = vxc_work(tabs, blocks, I, pl);
         const MixTab &T = tabs[blocks[I.block0].mol];
         const int NT = W.sym ? W.mp : T.vxc_n;
         for (int n0 = 0; n0 < W.mp && ok; n0 += NT) {
           const int N = min(NT, W.mp - n0);
+          for (int pr = 0; pr < pl.npairs && ok; pr++)
           for (int b = 0; b < W.nblk && ok; b++) {
             const MBlock Bb = blocks[I.block0 + b];
             const int r0 = static_cast<int>(T.ws_row0 + Bb.ws_off / kBlockPts);
@@ -1149,15 +1161,15 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
               uint8_t *st = stage[s];
               for (int r = 0; r < W.rows_a; r += 32) {
                 umma::tma_load_2d(st + kOffAhi + r * 128, &tmap, c * kKc,
-                                  r0 + kPlanePhiHi * mp + W.i0 + r, &sm->full[s]);
+                                  r0 + pl.a_hi[pr] * mp + W.i0 + r, &sm->full[s]);
                 umma::tma_load_2d(st + kOffAlo + r * 128, &tmap, c * kKc,
-                                  r0 + kPlanePhiLo * mp + W.i0 + r, &sm->full[s]);
+                                  r0 + pl.a_lo[pr] * mp + W.i0 + r, &sm->full[s]);
               }
               for (int r = 0; r < N; r += 32) {
                 umma::tma_load_2d(st + kOffBhi + r * 128, &tmap, c * kKc,
-                                  r0 + kPlaneYHi * mp + n0 + r, &sm->full[s]);
+                                  r0 + pl.b_hi[pr] * mp + n0 + r, &sm->full[s]);
                 umma::tma_load_2d(st + kOffBlo + r * 128, &tmap, c * kKc,
-                                  r0 + kPlaneYLo * mp + n0 + r, &sm->full[s]);
+                                  r0 + pl.b_lo[pr] * mp + n0 + r, &sm->full[s]);
               }
             }
           }
@@ -1179,7 +1191,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
         if (it < 0)
           break;
         const VItem I = items[it];
-        const VxcWork W = vxc_work(tabs, blocks, I);
+        const VxcWork W = vxc_work(tabs, blocks, I, pl);
         const MixTab &T = tabs[blocks[I.block0].mol];
         const int NT = W.sym ? W.mp : T.vxc_n;
         for (int n0 = 0; n0 < W.mp && ok; n0 += NT, pc++) {
@@ -1190,7 +1202,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
           umma::fence_after_sync();
           const uint32_t d = tmem + buf * 256, dt = d + 128;
           const uint32_t idesc = umma::idesc_tf32(128, N);
-          const int nch = W.nblk * (kBlockPts / kKc);
+          const int nch = pl.npairs * W.nblk * (kBlockPts / kKc);
           for (int c = 0; c < nch && ok; c++, g++) {
             const int s = g & 1;
             if (!wait(&sm->full[s], (g >> 1) & 1))
@@ -1235,7 +1247,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       if (it < 0)
         break;
       const VItem I = items[it];
-      const VxcWork W = vxc_work(tabs, blocks, I);
+      const VxcWork W = vxc_work(tabs, blocks, I, pl);
       const MBlock B0 = blocks[I.block0];
       const MixTab &T = tabs[B0.mol];
       const DevLeaf L = T.m.leaves[B0.leaf];
@@ -1559,7 +1571,7 @@ struct MixedState {
 struct WsLayout {
   size_t ws, rowscale, dhl, colb, total;
 };
-WsLayout ws_layout(const Molecule &M) {
+WsLayout ws_layout(const Molecule &M, int planes = kPlanes) {
   WsLayout L{};
   size_t off = 0;
   auto put = [&](size_t bytes) {
@@ -1573,7 +1585,7 @@ WsLayout ws_layout(const Molecule &M) {
     const size_t nb = (Lf.cnt + kBlockPts - 1) / kBlockPts;
     const size_t mp = (Lf.nbf + kKc - 1) / kKc * kKc;
     nblocks += nb;
-    ws_floats += nb * kPlanes * mp * kBlockPts;
+    ws_floats += nb * planes * mp * kBlockPts;
   }
   L.ws = put(ws_floats * sizeof(float));
   L.rowscale = put(nblocks * kBlockPts * sizeof(float));
@@ -1584,8 +1596,8 @@ WsLayout ws_layout(const Molecule &M) {
 }
 // The molecule's workspace at `base` inside a region that starts at map_base
 // (the region the launch's tensor map covers).
-MixTab bind_ws(const Molecule &M, char *base, const char *map_base) {
-  const WsLayout L = ws_layout(M);
+MixTab bind_ws(const Molecule &M, char *base, const char *map_base, int planes = kPlanes) {
+  const WsLayout L = ws_layout(M, planes);
   MixTab T = M.mixed->tab;
   T.ws = reinterpret_cast<float *>(base + L.ws);
   T.ws_row0 = static_cast<long long>((base + L.ws) - map_base) / (kBlockPts * sizeof(float));
@@ -1723,7 +1735,7 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
     c.launch("vxc_mixed", st, [&] {
       const int g = std::min(ni, ctas);
       k_vxc_tma<<<g, kVxcThreads, kVxcSmem, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov, P.d_queue, err,
-                                          P.tmap);
+                                          P.tmap, kVxcBuildPlanes);
     });
   c.launch("symmetrize", st, [&] {
     const size_t n2 = static_cast<size_t>(P.maxnbf) * P.maxnbf;
@@ -2487,3 +2499,355 @@ extern "C" int occ_xc_selftest_functional(occ_xc_context *ctx, const char *metho
     cudaFree(d);
   });
 }
+
+// ---- XC nuclear gradient on the tensor cores ------------------------------
+// DFT::compute_xc_gradient (include/occ/dft/dft.h:599-749) as
+//   G_c(mu, nu) = sum_p d_c phi_mu Y_nu + Z_c,mu phi_nu   (c = x, y, z)
+//   g_A,c = - sum_{mu on A} sum_nu 4 D(mu, nu) G_c(mu, nu), |4 D| < 1e-12 skipped
+// (src/dft/dft_gradient_kernels.cpp:472-595): the three G_c are the V_xc
+// kernel's K with two operand pairs each, accumulated over the leaves into
+// nbf x nbf FP64 matrices, then contracted with D.  The blocks carry, beside
+// the build's eleven planes, the hi and lo TF32 planes of d_c phi and of
+//   Z_c = 0.5 w vrho d_c phi + 2 w vsigma grad rho . grad d_c phi
+// (k_grad_ops, with the AO second derivatives in FP32).
+namespace occx {
+
+constexpr int kPlanesGrad = 23;
+constexpr int kPlaneDphi = 11; // hi, lo of d_c phi: planes 11 + 2c, 12 + 2c
+constexpr int kPlaneZ = 17;    // hi, lo of Z_c: planes 17 + 2c, 18 + 2c
+
+namespace {
+
+// sum_k cg_k d_c d_k of the Cartesian functions of one shell (CCA order), for
+// c = x, y, z, from
+// d_ij (M R) = M_ij R + (M_i x_j + M_j x_i) dR + M (delta_ij dR + x_i x_j d2R)
+template <int L>
+__device__ __forceinline__ void cart_hess_dot_f32(float x, float y, float z, float R, float dR,
+                                                  float d2R, const float *cg, float (*hz)[3]) {
+  float px[L + 1], py[L + 1], pz[L + 1];
+  px[0] = py[0] = pz[0] = 1.f;
+#pragma unroll
+  for (int i = 1; i <= L; i++) {
+    px[i] = px[i - 1] * x;
+    py[i] = py[i - 1] * y;
+    pz[i] = pz[i - 1] * z;
+  }
+  const float r[3] = {x, y, z};
+  int k = 0;
+#pragma unroll
+  for (int a = L; a >= 0; a--) {
+#pragma unroll
+    for (int b = L - a; b >= 0; b--) {
+      const int c = L - a - b;
+      const int e[3] = {a, b, c};
+      const float *pp[3] = {px, py, pz};
+      const float M = px[a] * py[b] * pz[c];
+      float Mi[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const int o1 = (i + 1) % 3, o2 = (i + 2) % 3;
+        Mi[i] = e[i] > 0 ? e[i] * pp[i][e[i] > 0 ? e[i] - 1 : 0] * pp[o1][e[o1]] * pp[o2][e[o2]]
+                         : 0.f;
+      }
+      float H[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+#pragma unroll
+        for (int j = i; j < 3; j++) {
+          float Mij;
+          if (i == j) {
+            const int o1 = (i + 1) % 3, o2 = (i + 2) % 3;
+            Mij = e[i] > 1 ? e[i] * (e[i] - 1) * pp[i][e[i] > 1 ? e[i] - 2 : 0] * pp[o1][e[o1]] *
+                                 pp[o2][e[o2]]
+                           : 0.f;
+          } else {
+            const int l3 = 3 - i - j;
+            Mij = (e[i] > 0 && e[j] > 0)
+                      ? e[i] * e[j] * pp[i][e[i] > 0 ? e[i] - 1 : 0] *
+                            pp[j][e[j] > 0 ? e[j] - 1 : 0] * pp[l3][e[l3]]
+                      : 0.f;
+          }
+          const float h = Mij * R + (Mi[i] * r[j] + Mi[j] * r[i]) * dR +
+                          M * ((i == j ? dR : 0.f) + r[i] * r[j] * d2R);
+          H[i][j] = h;
+          H[j][i] = h;
+        }
+      }
+#pragma unroll
+      for (int cc = 0; cc < 3; cc++)
+        hz[k][cc] = fmaf(cg[0], H[cc][0], fmaf(cg[1], H[cc][1], cg[2] * H[cc][2]));
+      k++;
+    }
+  }
+}
+
+template <int L>
+__device__ __forceinline__ void grad_ops_shell(bool pure, float x, float y, float z, float R,
+                                               float dR, float d2R, bool valid, float c0,
+                                               const float *cg, float *out, size_t plane) {
+  constexpr int NC = ncart_of(L);
+  constexpr int NF = 2 * L + 1 > NC ? 2 * L + 1 : NC;
+  float hz[NC][3];
+  cart_hess_dot_f32<L>(x, y, z, R, dR, d2R, cg, hz);
+  const int nf = pure ? 2 * L + 1 : NC;
+#pragma unroll
+  for (int f = 0; f < NF; f++) { // compile-time bound keeps hz in registers
+    if (f >= nf)
+      continue;
+    float zh[3];
+    if (!pure || L == 0) {
+#pragma unroll
+      for (int cc = 0; cc < 3; cc++)
+        zh[cc] = hz[f < NC ? f : 0][cc];
+    } else {
+      const float *Tm = c_spht + sph_offset(L) + f * NC;
+      const float2 n = c_sphn[L * L + f];
+#pragma unroll
+      for (int cc = 0; cc < 3; cc++) {
+        float a = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < NC; kk++)
+          a = fmaf(Tm[kk], hz[kk][cc], a);
+        zh[cc] = fmaf(n.x, a, n.y * a);
+      }
+    }
+    const size_t o = static_cast<size_t>(f) * kBlockPts;
+#pragma unroll
+    for (int cc = 0; cc < 3; cc++) {
+      const float dphi = out[(1 + cc) * plane + o];
+      const float zc = fmaf(c0, dphi, zh[cc]);
+      float h, l;
+      tf32_split(valid ? dphi : 0.f, h, l);
+      out[(kPlaneDphi + 2 * cc) * plane + o] = h;
+      out[(kPlaneDphi + 2 * cc + 1) * plane + o] = l;
+      tf32_split(valid ? zc : 0.f, h, l);
+      out[(kPlaneZ + 2 * cc) * plane + o] = h;
+      out[(kPlaneZ + 2 * cc + 1) * plane + o] = l;
+    }
+  }
+}
+
+// One CTA of 128 threads (one point each) per block, after the functional
+// stage: the gradient operand planes from the collocation's d_c phi, the
+// functional's coefficients and the AO second derivatives.
+__global__ void __launch_bounds__(128) k_grad_ops(const MixTab *__restrict__ tabs,
+                                                 const MBlock *__restrict__ blocks, int deriv) {
+  const MBlock B = blocks[blockIdx.x];
+  const MixTab &T = tabs[B.mol];
+  const MolDev m = T.m;
+  const float4 *__restrict__ prim32 = T.prim32;
+  const float4 *__restrict__ shA = T.shA;
+  const DevLeaf L = m.leaves[B.leaf];
+  const int p = threadIdx.x;
+  const bool valid = p < B.cnt;
+  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+  float *base = T.ws + B.ws_off;
+  const size_t N = static_cast<size_t>(m.npts);
+  const size_t gp = static_cast<size_t>(L.off) + B.p0 + (valid ? p : 0);
+  const float c0 = valid ? static_cast<float>(T.coef[gp]) : 0.f;
+  float cg[3] = {0.f, 0.f, 0.f};
+  if (deriv && valid)
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      cg[k] = static_cast<float>(T.coef[(k + 1) * N + gp]);
+  const Pt4 P = valid ? m.pts[gp] : make_pt4(0.0, 0.0, 0.0, 0.0);
+  const float pxh = static_cast<float>(P.x), pyh = static_cast<float>(P.y),
+              pzh = static_cast<float>(P.z);
+  const float pxl = static_cast<float>(P.x - pxh), pyl = static_cast<float>(P.y - pyh),
+              pzl = static_cast<float>(P.z - pzh);
+  int loc = 0;
+  for (int k = L.sh_begin; k < L.sh_end; k++) {
+    const int si = m.leaf_sh[k];
+    const DevShell sh = m.shells[si];
+    const float4 ah = shA[2 * si], al = shA[2 * si + 1];
+    float x, y, z, xl, yl, zl;
+    df_sub(pxh, pxl, ah.x, al.x, x, xl);
+    df_sub(pyh, pyl, ah.y, al.y, y, yl);
+    df_sub(pzh, pzl, ah.z, al.z, z, zl);
+    // r^2 and alpha r^2 as double-float pairs, as the collocation forms them
+    float r2h, r2l;
+    {
+      const float p1 = __fmul_rn(x, x), p2 = __fmul_rn(y, y), p3 = __fmul_rn(z, z);
+      const float q = (fmaf(x, x, -p1) + fmaf(y, y, -p2) + fmaf(z, z, -p3)) +
+                      2.f * (x * xl + y * yl + z * zl);
+      float s12, e12, e3;
+      two_sum(p1, p2, s12, e12);
+      two_sum(s12, p3, r2h, e3);
+      r2l = (e12 + e3) + q;
+    }
+    float R = 0.f, dR = 0.f, d2R = 0.f;
+    for (int q = 0; q < sh.nprim; q++) {
+      const float4 pc = prim32[sh.prim_off + q]; // alpha hi, alpha lo, c hi, c lo
+      const float th = __fmul_rn(pc.x, r2h);
+      const float tl = fmaf(pc.x, r2h, -th) + fmaf(pc.x, r2l, pc.y * r2h);
+      const float e0 = exp_neg(th);
+      const float ex = fmaf(-e0, tl, e0);
+      const float e = fmaf(pc.z, ex, pc.w * ex);
+      const float a = pc.x + pc.y;
+      R += e;
+      dR = fmaf(-2.f * a, e, dR);
+      d2R = fmaf(4.f * a * a, e, d2R);
+    }
+    float *out = base + static_cast<size_t>(loc) * kBlockPts + p;
+    switch (sh.l) {
+    case 0: grad_ops_shell<0>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+    case 1: grad_ops_shell<1>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+    case 2: grad_ops_shell<2>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+    case 3: grad_ops_shell<3>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+    default: grad_ops_shell<4>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+    }
+    loc += sh.nfunc;
+  }
+  for (int f = loc; f < B.mp; f++) {
+    const size_t o = static_cast<size_t>(f) * kBlockPts + p;
+#pragma unroll
+    for (int q = kPlaneDphi; q < kPlanesGrad; q++)
+      base[q * plane + o] = 0.f;
+  }
+}
+
+// g[atom(mu)][c] -= sum_nu 4 D(mu, nu) G_c(mu, nu), |4 D| < 1e-12 skipped
+// (dft_gradient_kernels.cpp:535-547).  One CTA per row mu.
+__global__ void __launch_bounds__(256) k_grad_contract(const double *__restrict__ D,
+                                                       const double *__restrict__ G, int nbf,
+                                                       const int *__restrict__ ao_atom,
+                                                       double *__restrict__ grad) {
+  __shared__ double sh[8];
+  const int mu = blockIdx.x;
+  const size_t n2 = static_cast<size_t>(nbf) * nbf;
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int nu = threadIdx.x; nu < nbf; nu += 256) {
+    const size_t o = static_cast<size_t>(nu) * nbf + mu;
+    const double d4 = 4.0 * D[o];
+    if (fabs(d4) < 1e-12)
+      continue;
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      s[c] = fma(d4, G[c * n2 + o], s[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const double t = leaf_sum256(s[c], sh);
+    if (threadIdx.x == 0)
+      atomicAdd(&grad[3 * ao_atom[mu] + c], -t);
+  }
+}
+
+} // namespace
+
+struct GradMixed {
+  char *ws = nullptr;
+  size_t bytes = 0;
+  LaunchPlan plan;
+  double *G = nullptr;
+  int *ao_atom = nullptr;
+};
+
+void free_grad_mixed(GradMixed *g) { delete g; }
+
+void Molecule::prepare_gradient_mixed() {
+  if (gmixed)
+    return;
+  if (!mixed)
+    throw ArgError("the molecule has no device state");
+  auto g = std::make_unique<GradMixed>();
+  const WsLayout Lw = ws_layout(*this, kPlanesGrad);
+  g->bytes = Lw.total;
+  g->ws = static_cast<char *>(alloc(g->bytes));
+  LaunchPlan &P = g->plan;
+  make_plan_lists(P, {this}, {bind_ws(*this, g->ws, g->ws, kPlanesGrad)});
+  long long off = 0; // the blocks' offsets for 23 planes (same order as prepare_mixed)
+  for (MBlock &B : P.blocks) {
+    B.ws_off = off;
+    off += static_cast<long long>(kPlanesGrad) * B.mp * kBlockPts;
+  }
+  P.d_blocks = plan_upload(P, P.blocks);
+  P.d_order = plan_upload(P, P.order);
+  P.d_queue = plan_upload(P, std::vector<int>(2, 0));
+  P.d_items = plan_upload(P, P.items);
+  P.d_litems = plan_upload(P, P.litems);
+  P.d_tabs = plan_upload(P, P.tabs);
+  encode_ws_map(P.tmap, g->ws, g->bytes);
+  P.ao_cacheable = true;
+  const size_t nbf2 = std::max<size_t>(static_cast<size_t>(basis.nbf) * basis.nbf, 1);
+  g->G = static_cast<double *>(alloc(3 * nbf2 * sizeof(double)));
+  std::vector<int> ao_atom(std::max(basis.nbf, 1));
+  for (size_t s = 0; s < basis.shells.size(); s++)
+    for (int f = 0; f < basis.shell_size(static_cast<int>(s)); f++)
+      ao_atom[basis.first_bf[s] + f] = basis.shells[s].atom;
+  g->ao_atom = static_cast<int *>(alloc(ao_atom.size() * sizeof(int)));
+  cuda_check(cudaMemcpy(g->ao_atom, ao_atom.data(), ao_atom.size() * sizeof(int),
+                        cudaMemcpyHostToDevice),
+             "cudaMemcpy H2D");
+  gmixed = g.release();
+}
+
+void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
+                                 cudaStream_t st) {
+  prepare_gradient_mixed();
+  GradMixed &g = *gmixed;
+  LaunchPlan &P = g.plan;
+  Context &c = *ctx;
+  int *err = mixed->d_err;
+  const int nb = static_cast<int>(P.blocks.size());
+  const int ni = static_cast<int>(P.items.size());
+  const int nl = static_cast<int>(P.litems.size());
+  const int sms = this->ctas > 0 ? this->ctas
+                                 : (ctx->max_ctas > 0 ? ctx->max_ctas : num_sms(device));
+  const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
+  Override ov{dD, nullptr, dout2};
+  c.launch("prep_density", st, [&] {
+    k_prep_density<<<dim3(P.maxnbf, 1), 256, 0, st>>>(P.d_tabs, ov, P.d_queue);
+  });
+  if (nb > 0) {
+    if (!P.ao_valid)
+      c.launch("colloc_f32", st, [&] {
+        k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+    c.launch("rho_mixed", st, [&] {
+      const int gg = std::min(nb, sms);
+      if (P.deriv)
+        k_rho_mixed<true><<<gg, kRhoThreads, kRhoSmem, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
+                                                       P.d_queue, err);
+      else
+        k_rho_mixed<false><<<gg, kRhoThreads, kRhoSmem, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
+                                                        P.d_queue, err);
+    });
+  }
+  if (nl > 0)
+    c.launch("func", st, [&] {
+      if (P.deriv)
+        k_func_b<true><<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+      else
+        k_func_b<false><<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+    });
+  if (nb > 0)
+    c.launch("grad_ops", st, [&] {
+      k_grad_ops<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks, P.deriv);
+    });
+  cuda_check(cudaMemsetAsync(g.G, 0, 3 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
+  for (int cc = 0; cc < 3 && ni > 0; cc++) {
+    cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
+    const VxcPlanes pl{{kPlaneDphi + 2 * cc, kPlaneZ + 2 * cc},
+                       {kPlaneDphi + 2 * cc + 1, kPlaneZ + 2 * cc + 1},
+                       {kPlaneYHi, kPlanePhiHi},
+                       {kPlaneYLo, kPlanePhiLo},
+                       2,
+                       0};
+    Override ovc{dD, g.G + cc * nbf2, dout2};
+    c.launch("grad_vxc", st, [&] {
+      k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+          P.d_tabs, P.d_blocks, P.d_items, ni, ovc, P.d_queue, err, P.tmap, pl);
+    });
+  }
+  cuda_check(cudaMemsetAsync(dgrad, 0, 3 * Z.size() * sizeof(double), st), "cudaMemsetAsync");
+  c.launch("grad_contract", st, [&] {
+    if (basis.nbf > 0)
+      k_grad_contract<<<basis.nbf, 256, 0, st>>>(dD, g.G, basis.nbf, g.ao_atom, dgrad);
+  });
+  c.launch("reduce", st, [&] { k_reduce_b<<<1, 256, 0, st>>>(P.d_tabs, ov); });
+  cuda_check(cudaGetLastError(), "kernel launch");
+  P.ao_valid = true;
+}
+
+} // namespace occx

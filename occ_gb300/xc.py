@@ -108,7 +108,7 @@ def library():
                                           C.c_int, C.POINTER(_GridSettings),
                                           C.POINTER(C.c_long), _dp, _dp]
     lib.occ_xc_molecular_grid_device.argtypes = [C.c_void_p] + lib.occ_xc_molecular_grid.argtypes
-    lib.occ_xc_compute_xc_gradient.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp]
+    lib.occ_xc_compute_xc_gradient.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp, _dp]
     lib.occ_xc_nlc_vv10.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_double, C.c_double,
                                     C.c_int, _dp, _dp]
     lib.occ_xc_nlc_grid_points.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
@@ -121,7 +121,8 @@ def library():
     lib.occ_xc_molecule_set_gradient_workspace_cap.argtypes = [C.c_void_p, C.c_void_p,
                                                                C.c_double]
     lib.occ_xc_compute_xc_gradient_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
-                                                      C.c_void_p, C.c_void_p, C.c_void_p]
+                                                      C.c_int, C.c_void_p, C.c_void_p,
+                                                      C.c_void_p]
     lib.occ_xc_compute_vxc_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                               C.c_void_p, C.c_void_p, C.c_void_p]
     _vp = C.c_void_p
@@ -482,10 +483,11 @@ class DFT:
         self.ctx.lib.occ_xc_nlc_grid(self.h, _ptr(P), _ptr(W))
         return P, W
 
-    def compute_xc_gradient(self, D):
+    def compute_xc_gradient(self, D, precision=FP64):
         """dE_xc/dR (natoms x 3, Hartree/Bohr) for mo.D = D with the grid held
-        fixed, FP64 (DFT::compute_xc_gradient, include/occ/dft/dft.h:599-749);
-        E_xc of the same density via exchange_correlation_energy()."""
+        fixed (DFT::compute_xc_gradient, include/occ/dft/dft.h:599-749);
+        precision FP64 or MIXED (contractions on the tensor cores).  E_xc of
+        the same density via exchange_correlation_energy()."""
         nbf = self.nbf()
         Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
         if Dm.shape != (nbf, nbf):
@@ -493,8 +495,8 @@ class DFT:
         natoms = len(self.basis.atoms())
         g = np.zeros((natoms, 3))
         exc = C.c_double()
-        rc = self.ctx.lib.occ_xc_compute_xc_gradient(self.ctx.h, self.h, _ptr(Dm), _ptr(g),
-                                                     C.byref(exc))
+        rc = self.ctx.lib.occ_xc_compute_xc_gradient(self.ctx.h, self.h, _ptr(Dm),
+                                                     int(precision), _ptr(g), C.byref(exc))
         if rc != 0:
             raise XCError(f"occ_xc_compute_xc_gradient failed ({rc}): {self.ctx.error()}", rc)
         self._exc = exc.value

@@ -112,9 +112,40 @@ def test_gradient_device_entry_point():
     de = torch.zeros(2, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
     rc = dft.ctx.lib.occ_xc_compute_xc_gradient_device(
-        dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), C.c_void_p(dg.data_ptr()),
+        dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), og.FP64, C.c_void_p(dg.data_ptr()),
         C.c_void_p(de.data_ptr()), None)
     assert rc == 0, dft.ctx.error()
     torch.cuda.synchronize()
     assert np.max(np.abs(dg.cpu().numpy().reshape(3, 3) - g_host)) < 1e-12
     assert abs(de[0].item() - dft.exchange_correlation_energy()) < 1e-12
+
+
+TOL_GRAD_MIXED = 3e-5  # Ha/Bohr, tensor-core (3xTF32) gradient against the FP64 oracle
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["lda", "pbe", "b3lyp"])
+def test_mixed_gradient_converged_water(method):
+    b, D, _ = fchk_case()
+    dft = og.DFT(method, b)
+    g = dft.compute_xc_gradient(D, og.MIXED)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient(b, P, W, D, method)
+    assert np.max(np.abs(g - g_ref)) <= TOL_GRAD_MIXED, np.max(np.abs(g - g_ref))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("basis_name,pure,method", [("def2-svp", True, "pbe"),
+                                                    ("6-31g(d,p)", False, "blyp"),
+                                                    ("def2-tzvp", True, "lda")])
+def test_mixed_gradient_water_cluster(basis_name, pure, method):
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(4, box=6.0, seed=3)
+    b = wl.basis_for(mol, basis_name, pure)
+    D = wl.random_density(b.nbf(), 20, seed=4)
+    dft = og.DFT(method, b)
+    g = dft.compute_xc_gradient(D, og.MIXED)
+    g64 = dft.compute_xc_gradient(D, og.FP64)
+    assert np.max(np.abs(g - g64)) <= TOL_GRAD_MIXED, np.max(np.abs(g - g64))
+    # repeated calls reuse the resident AO values
+    assert np.max(np.abs(dft.compute_xc_gradient(D, og.MIXED) - g)) < 1e-9
