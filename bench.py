@@ -87,12 +87,13 @@ def run_workload(args):
             r = bw.stream(nreq=args.requests, rate=args.rate)
     if args.workload in ("uks", "vv10"):
         unit = "builds/s" if args.workload == "uks" else "calls/s"
-        value = r.pop("builds_per_s") if args.workload == "uks" else r["mixed"]["calls_per_s"]
-        line = {"metric": ("UKS XC builds/s (FP64)" if args.workload == "uks"
+        value = r["mixed"]["builds_per_s"] if args.workload == "uks" else r["mixed"]["calls_per_s"]
+        line = {"metric": ("UKS XC builds/s (tensor-core 3xTF32, FP64 beside it)"
+                           if args.workload == "uks"
                            else "VV10 non-local correlation calls/s (FP32 pair sums)"),
                 "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
                 "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64" if args.workload == "uks" else "f32+f64",
+                "vs_baseline": None, "dtype": "tf32x3+f64" if args.workload == "uks" else "f32+f64",
                 "data": "synthetic", "config": {"workload": r.pop("workload")},
                 "clocks": cs.summary()}
         line.update(r)

@@ -161,7 +161,8 @@ int occ_xc_compute_vxc_device(occ_xc_context *ctx, occ_xc_molecule *mol, const d
  * (dft.h:395-429 -> compute_K_dft<deriv, Unrestricted>): D and V are
  * 2 nbf x nbf column-major, the alpha block above the beta block, D = OCC's
  * mo.D (each block 0.5 C_s C_s^T, src/qm/orb.h:68-83); the polarised forms of
- * the method's functionals.  FP64 only (precision must be OCC_XC_FP64).
+ * the method's functionals.  precision: OCC_XC_FP64, or OCC_XC_MIXED (the
+ * density and potential contractions on the tensor cores, once per spin).
  * nelec2 (may be NULL) receives the integrated alpha and beta densities. */
 int occ_xc_compute_vxc_unrestricted(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D,
                                     int precision, double *V, double *exc, double *nelec2);

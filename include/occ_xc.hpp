@@ -138,14 +138,14 @@ public:
   // (nbf x nbf, column-major), returns V_xc (nbf x nbf, column-major).
   // As OCC dispatches on mo.kind, the size of D decides: nbf x nbf is
   // restricted; 2 nbf x nbf (alpha block above beta, OCC's unrestricted
-  // mo.D) is unrestricted, FP64, and returns V_xc of the same shape.
+  // mo.D) is unrestricted and returns V_xc of the same shape.
   std::vector<double> compute_vxc(const std::vector<double> &D,
                                   Precision precision = Precision::Mixed) {
     if (D.size() == 2 * nbf_ * nbf_) {
       std::vector<double> V(2 * nbf_ * nbf_);
       double n2[2];
-      check(occ_xc_compute_vxc_unrestricted(ctx_, mol_.get(), D.data(), OCC_XC_FP64, V.data(),
-                                            &exc_, n2));
+      check(occ_xc_compute_vxc_unrestricted(ctx_, mol_.get(), D.data(),
+                                            static_cast<int>(precision), V.data(), &exc_, n2));
       nelec_ = n2[0] + n2[1];
       return V;
     }

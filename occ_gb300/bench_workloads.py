@@ -25,10 +25,10 @@ grid            molecular grid of 32 waters (def2-SVP, 965,504 points): the
                 Becke partition on the GPU against the host restatement on all
                 host cores, and the whole molecule set-up (grid, leaves,
                 screening, upload) that a DFT object or a served session pays.
-uks             unrestricted (UKS) FP64 build of a 32-water cation radical
-                (def2-SVP, PBE, 160 alpha / 159 beta orbitals): builds/s through
-                the device entry point (CUDA events) and the host one, and the
-                restricted FP64 build of the same molecule for scale.
+uks             unrestricted (UKS) build of a 32-water cation radical (def2-SVP,
+                PBE, 160 alpha / 159 beta orbitals), FP64 and tensor-core:
+                builds/s through the device entry point (CUDA events) and the
+                host one, and the mixed result against FP64.
 vv10            VV10 non-local correlation of 32 waters (def2-SVP, 254,976
                 NLC points): FP64 and FP32-pair-sum calls, their difference.
 
@@ -331,43 +331,45 @@ def uks_build(torch, steps=5, warmup=2, waters=32, seed=0):
     b = wl.basis_for(mol, "def2-svp")
     nbf = b.nbf()
     D = wl.random_density_unrestricted(nbf, 5 * waters, 5 * waters - 1, seed=seed)
-    Dr = wl.random_density(nbf, 5 * waters, seed=seed)
     dft = DFT("pbe", b)
     lib = dft.ctx.lib
     dD = torch.from_numpy(np.asfortranarray(D).ravel(order="F").copy()).cuda()
     dV = torch.zeros_like(dD)
     d3 = torch.zeros(3, dtype=torch.float64, device="cuda")
     stream = torch.cuda.Stream()
-
-    def one():
-        rc = lib.occ_xc_compute_vxc_unrestricted_device(
-            dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), FP64, C.c_void_p(dV.data_ptr()),
-            C.c_void_p(d3.data_ptr()), C.c_void_p(stream.cuda_stream))
-        if rc != 0:
-            raise RuntimeError(dft.ctx.error())
-    for _ in range(warmup):
-        one()
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-    ev[0].record(stream)
-    for i in range(steps):
-        one()
-        ev[i + 1].record(stream)
-    torch.cuda.synchronize()
-    ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        V = dft.compute_vxc(D, FP64)
-    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
-    t0 = time.perf_counter()
-    dft.compute_vxc(Dr, FP64)
-    r_ms = (time.perf_counter() - t0) * 1e3
-    return {"workload": f"water{waters}_cation_def2svp_pbe_uks_fp64", "nbf": nbf,
-            "builds_per_s": 1e3 / ms, "ms_per_build": ms,
-            "e2e": {"value": 1e3 / e2e_ms, "unit": "builds/s",
-                    "h2d_bytes_per_step": int(D.size * 8), "d2h_bytes_per_step": int(D.size * 8 + 8)},
-            "exc": float(d3[0].item()), "nelec_ab": [float(d3[1].item()), float(d3[2].item())],
-            "restricted_fp64_ms_e2e": r_ms}
+    out = {"workload": f"water{waters}_cation_def2svp_pbe_uks", "nbf": nbf}
+    res = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        def one():
+            rc = lib.occ_xc_compute_vxc_unrestricted_device(
+                dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), prec, C.c_void_p(dV.data_ptr()),
+                C.c_void_p(d3.data_ptr()), C.c_void_p(stream.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(dft.ctx.error())
+        for _ in range(warmup):
+            one()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record(stream)
+        for i in range(steps):
+            one()
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            V = dft.compute_vxc(D, prec)
+        e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+        res[name] = (dft.exchange_correlation_energy(), V)
+        out[name] = {"builds_per_s": 1e3 / ms, "ms_per_build": ms,
+                     "e2e": {"value": 1e3 / e2e_ms, "unit": "builds/s",
+                             "h2d_bytes_per_step": int(D.size * 8),
+                             "d2h_bytes_per_step": int(D.size * 8 + 8)},
+                     "exc": res[name][0]}
+    out["abs_dE_mixed_vs_fp64"] = abs(res["mixed"][0] - res["fp64"][0])
+    out["max_abs_dV_mixed_vs_fp64"] = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1])))
+    out["e2e"] = out["mixed"]["e2e"]
+    return out
 
 
 def vv10(steps=3, warmup=1, waters=32, seed=0):

@@ -469,6 +469,7 @@ void Molecule::release_device() {
   d_gws = d_grad = nullptr;
   grad_bytes = 0.0;
   d_rho_b = d_coef_b = d_epart_u = d_Dab = d_Vab = d_Duks = d_Vuks = d_out3 = nullptr;
+  d_uks_tabs = nullptr;
   nlc.reset();
   free_grad_mixed(gmixed);
   gmixed = nullptr;

@@ -43,6 +43,11 @@ template <typename T> T *dev_upload(const std::vector<T> &h, size_t &bytes) {
 }
 void fill_sph_table(double *out);
 void upload_sph_table_grad();
+// the unrestricted build's polarised functional stage and its sums (xc_uks.cu)
+void launch_func_pol(const MolDev &m, int deriv, const FuncSet &fs, double thr,
+                     const double *rho_a, const double *rho_b, double *coef_a, double *coef_b,
+                     double *epart3, cudaStream_t st);
+void launch_reduce3(const double *epart3, int n, double *out3, cudaStream_t st);
 // Becke partition weights on `device` (xc_grid.cu); fits: the kernel's
 // shared memory holds natom atoms.
 bool device_partition_fits(int device, int natom);
@@ -214,6 +219,9 @@ struct Molecule {
   // UKS build (FP64): dD, dV 2 nbf x nbf in OCC's layout; dout3 = {E_xc,
   // integrated rho_a, integrated rho_b}
   void build_fp64_uks(const double *dD, double *dV, double *dout3, cudaStream_t st);
+  // the same with the density and potential contractions on the tensor cores
+  void build_mixed_uks(const double *dD, double *dV, double *dout3, cudaStream_t st);
+  void *d_uks_tabs = nullptr; // the mixed plan's table with the beta rho / coef arrays
   void release_gradient(); // frees the gradient's device state
   // dE_xc/dR (3 per atom, grid fixed) for mo.D = dD; dout2 = {E_xc, density}
   void xc_gradient(const double *dD, double *dgrad, double *dout2, cudaStream_t st);

@@ -2851,3 +2851,105 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
 }
 
 } // namespace occx
+
+// ---- unrestricted (UKS) build on the tensor cores -------------------------
+// compute_K_dft<deriv, Unrestricted> (include/occ/dft/dft.h:192-388): the
+// mixed density kernel once per spin (k_prep_density splits D2_s before each),
+// the polarised FP64 functional (k_func_pol), then per spin the V_xc operand
+// Y_s (k_ymix) and the V_xc kernel into A_s, V_s = A_s + A_s^T.  The AO planes
+// are the restricted build's, in the molecule's private workspace.
+namespace occx {
+namespace {
+template <bool DERIV>
+__global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
+                                             const MBlock *__restrict__ blocks) {
+  __shared__ float4 cf[kBlockPts];
+  const MBlock B = blocks[blockIdx.x];
+  ymix_block<DERIV>(tabs[B.mol], B, cf);
+}
+} // namespace
+
+void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cudaStream_t st) {
+  ensure_mixed_ws();
+  prepare_uks();
+  LaunchPlan &P = *mixed->single;
+  if (!d_uks_tabs) {
+    MixTab tb = P.tabs[0];
+    tb.rho = d_rho_b;
+    tb.coef = d_coef_b;
+    d_uks_tabs = alloc(sizeof(MixTab));
+    cuda_check(cudaMemcpy(d_uks_tabs, &tb, sizeof(MixTab), cudaMemcpyHostToDevice),
+               "cudaMemcpy H2D");
+  }
+  const MixTab *tabs[2] = {P.d_tabs, static_cast<const MixTab *>(d_uks_tabs)};
+  Context &c = *ctx;
+  int *err = mixed->d_err;
+  const size_t nbf = static_cast<size_t>(basis.nbf), nbf2 = nbf * nbf;
+  const int nb = static_cast<int>(P.blocks.size());
+  const int ni = static_cast<int>(P.items.size());
+  const int sms = this->ctas > 0 ? this->ctas
+                                 : (ctx->max_ctas > 0 ? ctx->max_ctas : num_sms(device));
+  // OCC's 2 nbf x nbf -> two contiguous nbf x nbf blocks
+  for (int s = 0; s < 2; s++)
+    cuda_check(cudaMemcpy2DAsync(d_Dab + s * nbf2, nbf * sizeof(double), dD + s * nbf,
+                                 2 * nbf * sizeof(double), nbf * sizeof(double), nbf,
+                                 cudaMemcpyDeviceToDevice, st),
+               "cudaMemcpy2DAsync");
+  cuda_check(cudaMemsetAsync(d_Vab, 0, 2 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
+  Override ov[2] = {{d_Dab, d_Vab, nullptr}, {d_Dab + nbf2, d_Vab + nbf2, nullptr}};
+  for (int s = 0; s < 2; s++) {
+    c.launch("prep_density", st, [&] {
+      k_prep_density<<<dim3(P.maxnbf, 1), 256, 0, st>>>(tabs[s], ov[s], P.d_queue);
+    });
+    if (nb == 0)
+      continue;
+    if (s == 0 && !P.ao_valid)
+      c.launch("colloc_f32", st, [&] {
+        k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+    c.launch("rho_mixed", st, [&] {
+      const int g = std::min(nb, sms);
+      if (P.deriv)
+        k_rho_mixed<true><<<g, kRhoThreads, kRhoSmem, st>>>(tabs[s], P.d_blocks, P.d_order, nb,
+                                                      P.d_queue, err);
+      else
+        k_rho_mixed<false><<<g, kRhoThreads, kRhoSmem, st>>>(tabs[s], P.d_blocks, P.d_order, nb,
+                                                       P.d_queue, err);
+    });
+  }
+  const MolDev m = dev();
+  c.launch("func_pol", st, [&] {
+    launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
+                    d_epart_u, st);
+  });
+  for (int s = 0; s < 2 && nb > 0; s++) {
+    c.launch("ymix", st, [&] {
+      if (P.deriv)
+        k_ymix<true><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
+      else
+        k_ymix<false><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
+    });
+    if (ni > 0) {
+      cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
+      c.launch("vxc_mixed", st, [&] {
+        k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+            tabs[s], P.d_blocks, P.d_items, ni, ov[s], P.d_queue, err, P.tmap, kVxcBuildPlanes);
+      });
+    }
+    c.launch("symmetrize", st, [&] {
+      const int gx = static_cast<int>(std::min<size_t>((nbf2 + 255) / 256, 1024));
+      k_symmetrize<<<dim3(std::max(gx, 1), 1), 256, 0, st>>>(tabs[s], ov[s]);
+    });
+  }
+  c.launch("reduce", st, [&] { launch_reduce3(d_epart_u, m.nleaves, dout3, st); });
+  for (int s = 0; s < 2; s++)
+    cuda_check(cudaMemcpy2DAsync(dV + s * nbf, 2 * nbf * sizeof(double), d_Vab + s * nbf2,
+                                 nbf * sizeof(double), nbf * sizeof(double), nbf,
+                                 cudaMemcpyDeviceToDevice, st),
+               "cudaMemcpy2DAsync");
+  cuda_check(cudaGetLastError(), "kernel launch");
+  if (P.ao_cacheable)
+    P.ao_valid = true;
+}
+
+} // namespace occx

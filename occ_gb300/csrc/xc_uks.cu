@@ -15,6 +15,8 @@
 // path's K + K^T with Y = 0.5 w vrho_s phi + c_s . grad phi, so the density
 // and potential kernels of the restricted build run once per spin on the
 // same resident AO values; only the functional stage is new (k_func_pol).
+// The tensor-core form (Molecule::build_mixed_uks, xc_mixed.cu) runs the
+// mixed density and potential kernels once per spin in the same way.
 #include "functionals_pol.cuh"
 #include "xc_device.cuh"
 #include "xc_engine.hpp"
@@ -103,6 +105,22 @@ __global__ void __launch_bounds__(256) k_reduce3(const double *__restrict__ epar
 
 } // namespace
 
+void launch_func_pol(const MolDev &m, int deriv, const FuncSet &fs, double thr,
+                     const double *rho_a, const double *rho_b, double *coef_a, double *coef_b,
+                     double *epart3, cudaStream_t st) {
+  if (m.nleaves == 0)
+    return;
+  if (deriv)
+    k_func_pol<true><<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
+  else
+    k_func_pol<false><<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b,
+                                                 epart3);
+}
+
+void launch_reduce3(const double *epart3, int n, double *out3, cudaStream_t st) {
+  k_reduce3<<<1, 256, 0, st>>>(epart3, n, out3);
+}
+
 void Molecule::prepare_uks() {
   if (d_rho_b)
     return;
@@ -144,23 +162,15 @@ void Molecule::build_fp64_uks(const double *dD, double *dV, double *dout3, cudaS
                      rho[s], st);
     });
   c.launch("func_pol", st, [&] {
-    if (m.nleaves == 0)
-      return;
-    if (deriv)
-      k_func_pol<true><<<m.nleaves, 256, 0, st>>>(m, fs, bs.density_threshold, d_rho, d_rho_b,
-                                                  d_coef, d_coef_b, d_epart_u);
-    else
-      k_func_pol<false><<<m.nleaves, 256, 0, st>>>(m, fs, bs.density_threshold, d_rho, d_rho_b,
-                                                   d_coef, d_coef_b, d_epart_u);
+    launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
+                    d_epart_u, st);
   });
   for (int s = 0; s < 2; s++)
     c.launch("vxc_f64", st, [&] {
       launch_vxc_f64(m, deriv, d_ws, coef[s], d_tiles, static_cast<int>(tiles.size()),
                      d_Vab + s * nbf2, st);
     });
-  c.launch("reduce", st, [&] {
-    k_reduce3<<<1, 256, 0, st>>>(d_epart_u, m.nleaves, dout3);
-  });
+  c.launch("reduce", st, [&] { launch_reduce3(d_epart_u, m.nleaves, dout3, st); });
   for (int s = 0; s < 2; s++)
     cuda_check(cudaMemcpy2DAsync(dV + s * nbf, 2 * nbf * sizeof(double), d_Vab + s * nbf2,
                                  nbf * sizeof(double), nbf * sizeof(double), nbf,
@@ -182,21 +192,26 @@ int occ_xc_compute_vxc_unrestricted(occ_xc_context *ctx, occ_xc_molecule *mol, c
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   return guarded(ctx, [&] {
-    if (precision != OCC_XC_FP64)
-      throw ArgError("the unrestricted build runs in FP64 only (precision OCC_XC_FP64)");
+    if (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED)
+      throw ArgError("precision must be OCC_XC_FP64 or OCC_XC_MIXED");
     Molecule &M = *mol->impl;
     cudaStream_t st = ctx->impl->stream;
     M.prepare_uks();
     const size_t n2 = 2 * static_cast<size_t>(M.basis.nbf) * M.basis.nbf;
     cuda_check(cudaMemcpyAsync(M.d_Duks, D, n2 * sizeof(double), cudaMemcpyHostToDevice, st),
                "cudaMemcpyAsync H2D");
-    M.build_fp64_uks(M.d_Duks, M.d_Vuks, M.d_out3, st);
+    if (precision == OCC_XC_MIXED)
+      M.build_mixed_uks(M.d_Duks, M.d_Vuks, M.d_out3, st);
+    else
+      M.build_fp64_uks(M.d_Duks, M.d_Vuks, M.d_out3, st);
     double out3[3];
     cuda_check(cudaMemcpyAsync(V, M.d_Vuks, n2 * sizeof(double), cudaMemcpyDeviceToHost, st),
                "cudaMemcpyAsync D2H");
     cuda_check(cudaMemcpyAsync(out3, M.d_out3, sizeof(out3), cudaMemcpyDeviceToHost, st),
                "cudaMemcpyAsync D2H");
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (precision == OCC_XC_MIXED && mixed_error_flag(M, st))
+      throw TimeoutError("a bounded wait of the tensor-core pipeline gave up");
     *exc = out3[0];
     if (nelec2) {
       nelec2[0] = out3[1];
@@ -212,12 +227,15 @@ int occ_xc_compute_vxc_unrestricted_device(occ_xc_context *ctx, occ_xc_molecule 
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   return guarded(ctx, [&] {
-    if (precision != OCC_XC_FP64)
-      throw ArgError("the unrestricted build runs in FP64 only (precision OCC_XC_FP64)");
+    if (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED)
+      throw ArgError("precision must be OCC_XC_FP64 or OCC_XC_MIXED");
     Molecule &M = *mol->impl;
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
     M.prepare_uks();
-    M.build_fp64_uks(d_D, d_V, d_out3 ? d_out3 : M.d_out3, st);
+    if (precision == OCC_XC_MIXED)
+      M.build_mixed_uks(d_D, d_V, d_out3 ? d_out3 : M.d_out3, st);
+    else
+      M.build_fp64_uks(d_D, d_V, d_out3 ? d_out3 : M.d_out3, st);
   });
 }
 

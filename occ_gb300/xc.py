@@ -432,7 +432,8 @@ class DFT:
 
     def compute_vxc_unrestricted(self, D, precision=FP64):
         """UKS V_xc (2 nbf x nbf, alpha block above beta) for OCC's
-        unrestricted mo.D (2 nbf x nbf, each block 0.5 C_s C_s^T); FP64."""
+        unrestricted mo.D (2 nbf x nbf, each block 0.5 C_s C_s^T); FP64 or
+        MIXED."""
         nbf = self.nbf()
         Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
         if Dm.shape != (2 * nbf, nbf):

@@ -140,12 +140,26 @@ def test_unrestricted_closed_shell_equals_restricted_gpu():
 
 
 @pytest.mark.gpu
-def test_unrestricted_mixed_precision_is_rejected():
-    b, D = radical_case("6-31g")
-    dft = og.DFT("lda", b)
-    with pytest.raises(og.XCError) as e:
-        dft.compute_vxc(D, og.MIXED)
-    assert e.value.code == og.xc.ERR_ARG
+@pytest.mark.parametrize("method", ["lda", "pbe", "b3lyp"])
+def test_unrestricted_mixed_against_oracle(method):
+    """The tensor-core UKS build against the FP64 oracle, at the restricted
+    mixed path's bars."""
+    from helpers import TOL_E_MIXED, TOL_V_MIXED
+    b, D = radical_case()
+    dft = og.DFT(method, b)
+    V = dft.compute_vxc(D, og.MIXED)
+    P, W = dft.grid()
+    e_ref, V_ref, n_ref = oracle.xc_build_unrestricted(b, P, W, D, method)
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= TOL_E_MIXED
+    assert np.max(np.abs(V - V_ref)) <= TOL_V_MIXED
+    na, nb = dft.integrated_spin_densities()
+    assert abs(na - n_ref[0]) < 1e-6 and abs(nb - n_ref[1]) < 1e-6
+    # the restricted build of the same molecule still works after it
+    Dr = wl.random_density(b.nbf(), 4, seed=1)
+    Vr = dft.compute_vxc(Dr, og.MIXED)
+    e_r, V_r, _ = oracle.xc_build(b, P, W, Dr, method)
+    assert abs(dft.exchange_correlation_energy() - e_r) <= TOL_E_MIXED
+    assert np.max(np.abs(Vr - V_r)) <= TOL_V_MIXED
 
 
 @pytest.mark.gpu
