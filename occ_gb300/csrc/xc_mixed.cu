@@ -1029,12 +1029,14 @@ constexpr uint32_t kVxcSmem = 2 * kStageBytes + sizeof(VxcSmem) + 1024;
 // each operand as its (hi, lo) TF32 planes.  The build: one pair (phi, Y),
 // the symmetric form for small leaves allowed.  The XC gradient: two pairs
 // (d_c phi, Y) and (Z_c, phi), no symmetry.
+// (scalar fields, selected without indexing, so that the kernel parameters
+// stay in the constant bank)
 struct VxcPlanes {
-  int a_hi[2], a_lo[2], b_hi[2], b_lo[2];
+  int a_hi0, a_lo0, b_hi0, b_lo0, a_hi1, a_lo1, b_hi1, b_lo1;
   int npairs, allow_sym;
 };
-constexpr VxcPlanes kVxcBuildPlanes{{kPlanePhiHi, 0}, {kPlanePhiLo, 0}, {kPlaneYHi, 0},
-                                    {kPlaneYLo, 0}, 1, 1};
+constexpr VxcPlanes kVxcBuildPlanes{kPlanePhiHi, kPlanePhiLo, kPlaneYHi, kPlaneYLo, 0, 0, 0, 0,
+                                    1, 1};
 
 struct VxcWork { // what every role derives from an item
   int mp, rows_a, nblk, i0, nbf_leaf;
@@ -1067,6 +1069,18 @@ __device__ __forceinline__ bool epi_all(bool v) {
                : "r"(static_cast<uint32_t>(v)), "n"(kVxcEpi)
                : "memory");
   return r != 0;
+}
+
+// The FP64 value of FP32 bits by integer operations (rebias the exponent,
+// widen the mantissa), off the FP64 pipe, which GB300 has little of and
+// which the epilogue's conversions would otherwise occupy.  Zero and FP32
+// subnormals (below 1.2e-38) give a signed zero; the accumulators hold
+// neither infinities nor NaNs.
+__device__ __forceinline__ double f32_bits_to_f64(uint32_t u) {
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint32_t hi = (u & 0x80000000u) | (e ? (((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)) : 0u);
+  const uint32_t lo = e ? (u << 29) : 0u;
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
 }
 
 __global__ void __launch_bounds__(kVxcThreads, 1)
@@ -1159,17 +1173,19 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
               umma::mbar_arrive_expect_tx(&sm->full[s],
                                           static_cast<uint32_t>(W.rows_a + N) * 256u);
               uint8_t *st = stage[s];
+              const int ah = pr ? pl.a_hi1 : pl.a_hi0, al = pr ? pl.a_lo1 : pl.a_lo0;
+              const int bh = pr ? pl.b_hi1 : pl.b_hi0, bl = pr ? pl.b_lo1 : pl.b_lo0;
               for (int r = 0; r < W.rows_a; r += 32) {
                 umma::tma_load_2d(st + kOffAhi + r * 128, &tmap, c * kKc,
-                                  r0 + pl.a_hi[pr] * mp + W.i0 + r, &sm->full[s]);
+                                  r0 + ah * mp + W.i0 + r, &sm->full[s]);
                 umma::tma_load_2d(st + kOffAlo + r * 128, &tmap, c * kKc,
-                                  r0 + pl.a_lo[pr] * mp + W.i0 + r, &sm->full[s]);
+                                  r0 + al * mp + W.i0 + r, &sm->full[s]);
               }
               for (int r = 0; r < N; r += 32) {
                 umma::tma_load_2d(st + kOffBhi + r * 128, &tmap, c * kKc,
-                                  r0 + pl.b_hi[pr] * mp + n0 + r, &sm->full[s]);
+                                  r0 + bh * mp + n0 + r, &sm->full[s]);
                 umma::tma_load_2d(st + kOffBlo + r * 128, &tmap, c * kKc,
-                                  r0 + pl.b_lo[pr] * mp + n0 + r, &sm->full[s]);
+                                  r0 + bl * mp + n0 + r, &sm->full[s]);
               }
             }
           }
@@ -1292,13 +1308,14 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
             // goes to A[gi][gj], so a warp's lanes (consecutive rows i)
             // update consecutive addresses of one column
             const size_t gj = static_cast<size_t>(g[lj]);
-            const double kv = static_cast<double>(__uint_as_float(r[e]));
             if (!W.sym) {
-              atomicAdd(&V[gj * nbf + gi], kv);
+              atomicAdd(&V[gj * nbf + gi], f32_bits_to_f64(r[e]));
             } else if (lj > li) { // K[i][j] + K[j][i] once per unordered pair
-              atomicAdd(&V[gj * nbf + gi], kv + static_cast<double>(__uint_as_float(rt[e])));
+              atomicAdd(&V[gj * nbf + gi],
+                        f32_bits_to_f64(__float_as_uint(__uint_as_float(r[e]) +
+                                                        __uint_as_float(rt[e]))));
             } else if (lj == li) {
-              atomicAdd(&V[gi * nbf + gi], kv);
+              atomicAdd(&V[gi * nbf + gi], f32_bits_to_f64(r[e]));
             }
           }
         }
@@ -2828,10 +2845,8 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
   cuda_check(cudaMemsetAsync(g.G, 0, 3 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
   for (int cc = 0; cc < 3 && ni > 0; cc++) {
     cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
-    const VxcPlanes pl{{kPlaneDphi + 2 * cc, kPlaneZ + 2 * cc},
-                       {kPlaneDphi + 2 * cc + 1, kPlaneZ + 2 * cc + 1},
-                       {kPlaneYHi, kPlanePhiHi},
-                       {kPlaneYLo, kPlanePhiLo},
+    const VxcPlanes pl{kPlaneDphi + 2 * cc, kPlaneDphi + 2 * cc + 1, kPlaneYHi, kPlaneYLo,
+                       kPlaneZ + 2 * cc,    kPlaneZ + 2 * cc + 1,    kPlanePhiHi, kPlanePhiLo,
                        2,
                        0};
     Override ovc{dD, g.G + cc * nbf2, dout2};
