@@ -103,6 +103,11 @@ struct Context {
   }
 };
 
+// Tensor maps of a workspace region as rows of 128 FP32: boxes of 32 points
+// x 32 rows and of 32 points x 128 rows (one copy for a whole 128-row tile).
+struct WsMaps {
+  CUtensorMap rows32, rows128;
+};
 struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)
 struct GradMixed;  // the tensor-core XC gradient's workspace and plan (xc_mixed.cu)
 void free_grad_mixed(GradMixed *g);
@@ -259,10 +264,9 @@ size_t group_workspace_bytes(const std::vector<Molecule *> &mols);
 // pool_map is encode_ws_map of the whole pool.
 void mixed_build_in_pool(Context &c, const std::vector<Molecule *> &mols,
                          const std::vector<char *> &ws, const std::vector<int> &ao_valid,
-                         const char *pool, const CUtensorMap &pool_map, ListArena &arena,
+                         const char *pool, const WsMaps &pool_map, ListArena &arena,
                          int *d_err, cudaStream_t st);
-// Tensor map of a workspace region as rows of 128 FP32.
-void encode_ws_map(CUtensorMap &map, const void *base, size_t bytes);
+void encode_ws_map(WsMaps &map, const void *base, size_t bytes);
 
 } // namespace occx
 

@@ -997,15 +997,19 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 // handed to the roles through a ring in shared memory:
 //   warp 8       TMA producer: per K chunk of 32 points, hi and lo of the A
 //                rows (phi, split by k_colloc_f32) and of the B rows (Y,
-//                split by ymix_block), as
-//                32 x 32 FP32 boxes with the 128-byte swizzle
+//                split by ymix_block), with the 128-byte swizzle: one
+//                32 x 128 box per whole 128-row tile, 32 x 32 boxes for the
+//                rest (the copies issued by the one producer thread bound
+//                this kernel more than its atomics: the 128-row boxes took
+//                it from 1.02 to 0.90 ms at 32 waters)
 //   warp 9       MMA issuer: hi*hi + hi*lo + lo*hi ("3xTF32") into one of two
-//                TMEM accumulators of 256 columns; for a leaf with at most
-//                128 AOs also K^T (A and B swapped) beside it
+//                TMEM accumulators of 256 columns
 //   warps 0-7    epilogue (two warps per TMEM lane quarter, each half of the
 //                columns): TMEM -> FP64 atomics, coalesced along the rows,
-//                into A with V_xc = A + A^T (K + K^T summed in registers and
-//                added once per pair when K^T was formed)
+//                into A with V_xc = A + A^T.  (Forming K^T beside K to add
+//                each unordered pair once halves the atomics but measured
+//                slower: 1.07 ms with it for leaves of at most 128 AOs,
+//                1.22 ms with paired 128 x 128 tiles.)
 // Stages and accumulators are double-buffered, so loads, MMAs and atomics of
 // consecutive chunks and passes overlap.  Every wait is bounded; on expiry
 // the error flag is set and all roles leave.
@@ -1026,24 +1030,22 @@ struct alignas(16) VxcSmem {
 constexpr uint32_t kVxcSmem = 2 * kStageBytes + sizeof(VxcSmem) + 1024;
 
 // Operand planes of k_vxc_tma: K = sum over npairs of (A pair)^T (B pair),
-// each operand as its (hi, lo) TF32 planes.  The build: one pair (phi, Y),
-// the symmetric form for small leaves allowed.  The XC gradient: two pairs
-// (d_c phi, Y) and (Z_c, phi), no symmetry.
-// (scalar fields, selected without indexing, so that the kernel parameters
-// stay in the constant bank)
+// each operand as its (hi, lo) TF32 planes.  The build: one pair (phi, Y);
+// the XC gradient: two pairs (d_c phi, Y) and (Z_c, phi).  Scalar fields,
+// selected without indexing, so that the parameters stay in the constant
+// bank.
 struct VxcPlanes {
   int a_hi0, a_lo0, b_hi0, b_lo0, a_hi1, a_lo1, b_hi1, b_lo1;
-  int npairs, allow_sym;
+  int npairs;
 };
 constexpr VxcPlanes kVxcBuildPlanes{kPlanePhiHi, kPlanePhiLo, kPlaneYHi, kPlaneYLo, 0, 0, 0, 0,
-                                    1, 1};
+                                    1};
 
 struct VxcWork { // what every role derives from an item
   int mp, rows_a, nblk, i0, nbf_leaf;
-  bool sym;
 };
 __device__ __forceinline__ VxcWork vxc_work(const MixTab *tabs, const MBlock *blocks,
-                                            const VItem &it, const VxcPlanes &pl) {
+                                            const VItem &it) {
   const MBlock B = blocks[it.block0];
   VxcWork w;
   w.mp = B.mp;
@@ -1051,7 +1053,6 @@ __device__ __forceinline__ VxcWork vxc_work(const MixTab *tabs, const MBlock *bl
   w.i0 = it.i0;
   w.rows_a = min(128, B.mp - it.i0); // a multiple of 32
   w.nbf_leaf = tabs[B.mol].m.leaves[B.leaf].nbf;
-  w.sym = pl.allow_sym && B.mp <= 128;
   return w;
 }
 
@@ -1086,7 +1087,8 @@ __device__ __forceinline__ double f32_bits_to_f64(uint32_t u) {
 __global__ void __launch_bounds__(kVxcThreads, 1)
     k_vxc_tma(const MixTab *__restrict__ tabs, const MBlock *__restrict__ blocks,
               const VItem *__restrict__ items, int nitems, Override ov, int *queue, int *err,
-              const __grid_constant__ CUtensorMap tmap, VxcPlanes pl) {
+              const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmap128,
+              VxcPlanes pl) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
   VxcSmem *sm = reinterpret_cast<VxcSmem *>(smem + 2 * kStageBytes);
@@ -1106,6 +1108,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     umma::mbar_init(&sm->done, 1);
     umma::fence_proxy_async();
     umma::tma_prefetch_desc(&tmap);
+    umma::tma_prefetch_desc(&tmap128);
   }
   if (warp == 0)
     umma::tmem_alloc(&sm->tmem_slot, 512);
@@ -1156,9 +1159,9 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
         if (it < 0)
           break;
         const VItem I = items[it];
-        const VxcWork W = vxc_work(tabs, blocks, I, pl);
+        const VxcWork W = vxc_work(tabs, blocks, I);
         const MixTab &T = tabs[blocks[I.block0].mol];
-        const int NT = W.sym ? W.mp : T.vxc_n;
+        const int NT = T.vxc_n;
         for (int n0 = 0; n0 < W.mp && ok; n0 += NT) {
           const int N = min(NT, W.mp - n0);
           for (int pr = 0; pr < pl.npairs && ok; pr++)
@@ -1175,17 +1178,24 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
               uint8_t *st = stage[s];
               const int ah = pr ? pl.a_hi1 : pl.a_hi0, al = pr ? pl.a_lo1 : pl.a_lo0;
               const int bh = pr ? pl.b_hi1 : pl.b_hi0, bl = pr ? pl.b_lo1 : pl.b_lo0;
-              for (int r = 0; r < W.rows_a; r += 32) {
-                umma::tma_load_2d(st + kOffAhi + r * 128, &tmap, c * kKc,
+              // whole 128-row tiles in one copy each, the rest 32 rows at a time
+              for (int r = 0; r < W.rows_a;) {
+                const bool big = W.rows_a - r >= 128;
+                const CUtensorMap *mp_ = big ? &tmap128 : &tmap;
+                umma::tma_load_2d(st + kOffAhi + r * 128, mp_, c * kKc,
                                   r0 + ah * mp + W.i0 + r, &sm->full[s]);
-                umma::tma_load_2d(st + kOffAlo + r * 128, &tmap, c * kKc,
+                umma::tma_load_2d(st + kOffAlo + r * 128, mp_, c * kKc,
                                   r0 + al * mp + W.i0 + r, &sm->full[s]);
+                r += big ? 128 : 32;
               }
-              for (int r = 0; r < N; r += 32) {
-                umma::tma_load_2d(st + kOffBhi + r * 128, &tmap, c * kKc,
+              for (int r = 0; r < N;) {
+                const bool big = N - r >= 128;
+                const CUtensorMap *mp_ = big ? &tmap128 : &tmap;
+                umma::tma_load_2d(st + kOffBhi + r * 128, mp_, c * kKc,
                                   r0 + bh * mp + n0 + r, &sm->full[s]);
-                umma::tma_load_2d(st + kOffBlo + r * 128, &tmap, c * kKc,
+                umma::tma_load_2d(st + kOffBlo + r * 128, mp_, c * kKc,
                                   r0 + bl * mp + n0 + r, &sm->full[s]);
+                r += big ? 128 : 32;
               }
             }
           }
@@ -1207,16 +1217,16 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
         if (it < 0)
           break;
         const VItem I = items[it];
-        const VxcWork W = vxc_work(tabs, blocks, I, pl);
+        const VxcWork W = vxc_work(tabs, blocks, I);
         const MixTab &T = tabs[blocks[I.block0].mol];
-        const int NT = W.sym ? W.mp : T.vxc_n;
+        const int NT = T.vxc_n;
         for (int n0 = 0; n0 < W.mp && ok; n0 += NT, pc++) {
           const int N = min(NT, W.mp - n0);
           const uint32_t buf = pc & 1, ub = pc >> 1;
           if (ub > 0 && !wait(&sm->tempty[buf], (ub - 1) & 1))
             break;
           umma::fence_after_sync();
-          const uint32_t d = tmem + buf * 256, dt = d + 128;
+          const uint32_t d = tmem + buf * 256;
           const uint32_t idesc = umma::idesc_tf32(128, N);
           const int nch = pl.npairs * W.nblk * (kBlockPts / kKc);
           for (int c = 0; c < nch && ok; c++, g++) {
@@ -1236,11 +1246,6 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
               umma::mma_tf32(d, alo, bhi, idesc, acc);
               umma::mma_tf32(d, ahi, blo, idesc, 1u);
               umma::mma_tf32(d, ahi, bhi, idesc, 1u);
-              if (W.sym) { // K^T: rows are the Y rows, columns the phi rows
-                umma::mma_tf32(dt, blo, ahi, idesc, acc);
-                umma::mma_tf32(dt, bhi, alo, idesc, 1u);
-                umma::mma_tf32(dt, bhi, ahi, idesc, 1u);
-              }
             }
             umma::commit(&sm->empty[s]);
             issued = true;
@@ -1263,7 +1268,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       if (it < 0)
         break;
       const VItem I = items[it];
-      const VxcWork W = vxc_work(tabs, blocks, I, pl);
+      const VxcWork W = vxc_work(tabs, blocks, I);
       const MBlock B0 = blocks[I.block0];
       const MixTab &T = tabs[B0.mol];
       const DevLeaf L = T.m.leaves[B0.leaf];
@@ -1278,7 +1283,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       const int *g = gsh ? sm->gmap : gsrc;
       double *__restrict__ V = t_V(T, ov);
       const size_t nbf = static_cast<size_t>(T.m.nbf);
-      const int NT = W.sym ? W.mp : T.vxc_n;
+      const int NT = T.vxc_n;
       const int li = W.i0 + i;
       const bool iv = li < W.nbf_leaf;
       const size_t gi = iv ? static_cast<size_t>(g[li]) : 0;
@@ -1292,10 +1297,8 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
         const uint32_t lanebase = tmem + (static_cast<uint32_t>(quad * 32) << 16) + buf * 256;
         const int cols = N / 2; // a multiple of 16
         for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
-          uint32_t r[16], rt[16];
+          uint32_t r[16];
           umma::tmem_ld16(lanebase + c0, r);
-          if (W.sym)
-            umma::tmem_ld16(lanebase + 128 + c0, rt);
           umma::tmem_wait_ld();
           if (!iv)
             continue;
@@ -1308,15 +1311,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
             // goes to A[gi][gj], so a warp's lanes (consecutive rows i)
             // update consecutive addresses of one column
             const size_t gj = static_cast<size_t>(g[lj]);
-            if (!W.sym) {
-              atomicAdd(&V[gj * nbf + gi], f32_bits_to_f64(r[e]));
-            } else if (lj > li) { // K[i][j] + K[j][i] once per unordered pair
-              atomicAdd(&V[gj * nbf + gi],
-                        f32_bits_to_f64(__float_as_uint(__uint_as_float(r[e]) +
-                                                        __uint_as_float(rt[e]))));
-            } else if (lj == li) {
-              atomicAdd(&V[gi * nbf + gi], f32_bits_to_f64(r[e]));
-            }
+            atomicAdd(&V[gj * nbf + gi], f32_bits_to_f64(r[e]));
           }
         }
         umma::fence_before_sync();
@@ -1556,7 +1551,7 @@ struct LaunchPlan {
   LeafItem *d_litems = nullptr;
   MixTab *d_tabs = nullptr;
   int maxnbf = 0, deriv = 0;
-  CUtensorMap tmap;       // the workspace as rows of 128 floats (k_vxc_tma)
+  WsMaps tmap;            // the workspace as rows of 128 floats (k_vxc_tma)
   // the workspace already holds these molecules' AO values (phi, its gradient,
   // its TF32 split, row scales): collocation is skipped
   bool ao_valid = false;
@@ -1667,8 +1662,9 @@ void make_plan_lists(LaunchPlan &P, const std::vector<Molecule *> &mols,
                           static_cast<int>(e - b)});
       for (size_t g = b; g < e; g += kItemBlocks) {
         const int nb = static_cast<int>(std::min<size_t>(kItemBlocks, e - g));
+        const int blk = base + static_cast<int>(g);
         for (int i0 = 0; i0 < mb[b].mp; i0 += 128)
-          items.push_back({base + static_cast<int>(g), nb, i0});
+          items.push_back({blk, nb, i0});
       }
       b = e;
     }
@@ -1752,7 +1748,7 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
     c.launch("vxc_mixed", st, [&] {
       const int g = std::min(ni, ctas);
       k_vxc_tma<<<g, kVxcThreads, kVxcSmem, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov, P.d_queue, err,
-                                          P.tmap, kVxcBuildPlanes);
+                                          P.tmap.rows32, P.tmap.rows128, kVxcBuildPlanes);
     });
   c.launch("symmetrize", st, [&] {
     const size_t n2 = static_cast<size_t>(P.maxnbf) * P.maxnbf;
@@ -1842,7 +1838,8 @@ size_t Molecule::mixed_workspace_bytes() const { return ws_layout(*this).total; 
 
 // Tensor map of a workspace region: rows of 128 FP32 (512 bytes), boxes of
 // 32 x 32 with the 128-byte swizzle that the UMMA descriptors expect.
-void encode_ws_map(CUtensorMap &map, const void *base, size_t bytes) {
+static void encode_ws_map_box(CUtensorMap &map, const void *base, size_t bytes,
+                              uint32_t box_rows) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     void *fn = nullptr;
@@ -1857,7 +1854,7 @@ void encode_ws_map(CUtensorMap &map, const void *base, size_t bytes) {
   const cuuint64_t rows = std::max<cuuint64_t>(bytes / (kBlockPts * sizeof(float)), 1);
   const cuuint64_t dims[2] = {static_cast<cuuint64_t>(kBlockPts), rows};
   const cuuint64_t strides[1] = {kBlockPts * sizeof(float)};
-  const cuuint32_t box[2] = {static_cast<cuuint32_t>(kKc), 32u};
+  const cuuint32_t box[2] = {static_cast<cuuint32_t>(kKc), box_rows};
   const cuuint32_t estr[2] = {1u, 1u};
   const CUresult r = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base),
                             dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -1865,6 +1862,11 @@ void encode_ws_map(CUtensorMap &map, const void *base, size_t bytes) {
                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
     throw CudaError("cuTensorMapEncodeTiled failed (" + std::to_string(static_cast<int>(r)) + ")");
+}
+
+void encode_ws_map(WsMaps &map, const void *base, size_t bytes) {
+  encode_ws_map_box(map.rows32, base, bytes, 32u);
+  encode_ws_map_box(map.rows128, base, bytes, 128u);
 }
 
 void Molecule::ensure_mixed_ws() {
@@ -1922,7 +1924,7 @@ ListArena::~ListArena() {
 // One launch sequence per functional family over molecules whose workspaces
 // are already bound (tabs[i] for mols[i]) inside the region `map` covers.
 void mixed_build_bound(Context &c, const std::vector<Molecule *> &mols,
-                       const std::vector<MixTab> &bound, const CUtensorMap &map,
+                       const std::vector<MixTab> &bound, const WsMaps &map,
                        ListArena &arena, int *d_err, cudaStream_t st) {
   LaunchPlan P[2];
   std::vector<Molecule *> group[2];
@@ -1999,14 +2001,14 @@ void mixed_build_group(Context &c, const std::vector<Molecule *> &mols, ListAren
     tabs.push_back(bind_ws(*M, d_ws + wsoff, d_ws));
     wsoff += M->mixed_workspace_bytes();
   }
-  CUtensorMap map;
+  WsMaps map;
   encode_ws_map(map, d_ws, std::max<size_t>(wsoff, 512));
   mixed_build_bound(c, mols, tabs, map, arena, d_err, st);
 }
 
 void mixed_build_in_pool(Context &c, const std::vector<Molecule *> &mols,
                          const std::vector<char *> &ws, const std::vector<int> &ao_valid,
-                         const char *pool, const CUtensorMap &pool_map, ListArena &arena,
+                         const char *pool, const WsMaps &pool_map, ListArena &arena,
                          int *d_err, cudaStream_t st) {
   std::vector<MixTab> tabs;
   for (size_t i = 0; i < mols.size(); i++) {
@@ -2847,12 +2849,12 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
     cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
     const VxcPlanes pl{kPlaneDphi + 2 * cc, kPlaneDphi + 2 * cc + 1, kPlaneYHi, kPlaneYLo,
                        kPlaneZ + 2 * cc,    kPlaneZ + 2 * cc + 1,    kPlanePhiHi, kPlanePhiLo,
-                       2,
-                       0};
+                       2};
     Override ovc{dD, g.G + cc * nbf2, dout2};
     c.launch("grad_vxc", st, [&] {
       k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
-          P.d_tabs, P.d_blocks, P.d_items, ni, ovc, P.d_queue, err, P.tmap, pl);
+          P.d_tabs, P.d_blocks, P.d_items, ni, ovc, P.d_queue, err, P.tmap.rows32, P.tmap.rows128,
+          pl);
     });
   }
   cuda_check(cudaMemsetAsync(dgrad, 0, 3 * Z.size() * sizeof(double), st), "cudaMemsetAsync");
@@ -2948,7 +2950,8 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
       cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
       c.launch("vxc_mixed", st, [&] {
         k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
-            tabs[s], P.d_blocks, P.d_items, ni, ov[s], P.d_queue, err, P.tmap, kVxcBuildPlanes);
+            tabs[s], P.d_blocks, P.d_items, ni, ov[s], P.d_queue, err, P.tmap.rows32,
+            P.tmap.rows128, kVxcBuildPlanes);
       });
     }
     c.launch("symmetrize", st, [&] {

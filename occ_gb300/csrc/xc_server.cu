@@ -131,7 +131,7 @@ struct Server {
   char *pool = nullptr; // the sessions' workspaces (allocated at the first admission)
   size_t pool_size = 0;
   PoolAlloc pool_free;
-  CUtensorMap pool_map;
+  WsMaps pool_map;
   int *d_err = nullptr;
   double *h_stage = nullptr; // pinned staging for D in / V out
   size_t stage_cap = 0;      // doubles
