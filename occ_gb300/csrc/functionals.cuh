@@ -85,9 +85,9 @@ __device__ __forceinline__ D3 dasinh(D3 a) { return apply(a, asinh(a.v), rsqrt(f
 // value keeps about 44 bits (error-free transformations: Knuth's TwoSum,
 // FMA-based TwoProduct; Dekker/Shewchuk double-float algorithms), so energy
 // densities stay FP64-grade, while the derivatives feed V_xc, whose
-// tolerance FP32 meets.  Transcendental values (log, exp, cbrt, atan, asinh)
-// are taken in FP64 from the double-float argument; sqrt and divisions are
-// done in double-float.  The _rn intrinsics keep the compiler from fusing
+// tolerance FP32 meets.  exp, log, cube roots, sqrt and divisions are done in
+// double-float (f2_exp, f2_log, f2_cbrt below); atan and asinh (VWN, B88)
+// take FP64 from the double-float argument.  The _rn intrinsics keep the compiler from fusing
 // the error-free transformations into FMAs.
 struct F2 {
   float h, l; // value h + l, |l| <= ulp(h) / 2
@@ -139,6 +139,78 @@ __device__ __forceinline__ F2 f2_sqrt(F2 a) { // one Newton step from the float 
   return quick_two_sum(y, __fdiv_rn(r.h, __fmul_rn(2.f, y)));
 }
 
+// Double-float transcendentals from FP32 operations (the FP64 pipe is a
+// small fraction of this GPU's), accurate to about 1e-14 relative:
+// e^x by Cody-Waite reduction x = n ln2 + r (W.J. Cody, W. Waite, Software
+// Manual for the Elementary Functions, 1980) with ln2 in three floats, e^r
+// from e^(r/4) by its Taylor series (degree 11) and two squarings, then the
+// exact scaling 2^n; log x by one Newton step y + x e^-y - 1 from the
+// FP32 logarithm, and x^(1/3) by one Newton step from the FP32 cube root
+// (each step squares the FP32 starting error, ~1e-7, to ~1e-14).
+__device__ __forceinline__ F2 f2_scale(F2 a, float c) { // c a power of two
+  return {a.h * c, a.l * c};
+}
+// e^r - 1 for |r| <= 0.35 (so that the result keeps its relative accuracy
+// when it is small): from t = r / 4 and two squarings.
+__device__ __forceinline__ F2 f2_expm1_small(F2 r) {
+  r = f2_scale(r, 0.25f);
+  // e^t - 1 for |t| <= 0.087 by Taylor, degree 11 (truncation < 1e-21); the
+  // 1/k! as double-floats
+  const float ih[9] = {2.755731998e-07f, 2.755731884e-06f, 2.480158764e-05f, 1.984127011e-04f,
+                        1.388888923e-03f, 8.333333768e-03f, 4.166666791e-02f, 1.666666716e-01f,
+                        5.000000000e-01f};
+  const float il[9] = {-7.575112209e-15f, 3.793571224e-14f, -3.406996094e-13f, -2.725596875e-12f,
+                        -3.363109444e-11f, -4.346172033e-10f, -1.241763470e-09f, -4.967053879e-09f,
+                        0.000000000e+00f};
+  F2 q = {2.505210794e-08f, 4.417623045e-16f}; // 1/11!
+#pragma unroll
+  for (int k = 0; k < 9; k++) // + 1/10!, ..., 1/2!
+    q = f2_add(f2_mul(q, r), {ih[k], il[k]});
+  q = f2_add(f2_mul(q, r), {1.f, 0.f});
+  F2 em1 = f2_mul(q, r); // e^t - 1
+  // (1 + u)^2 = 1 + (2u + u^2): square twice keeping the "- 1" form
+#pragma unroll
+  for (int k = 0; k < 2; k++)
+    em1 = f2_add(f2_scale(em1, 2.f), f2_mul(em1, em1));
+  return em1;
+}
+__device__ __forceinline__ F2 f2_exp(F2 x) {
+  const float n = rintf(x.h * 1.44269504088896341f);
+  const float c1 = 0.693145751953125f;             // 15 bits: n c1 exact
+  const float c2h = 1.42860677e-06f, c2l = 5.4979231e-14f; // ln2 - c1 in two floats
+  F2 r = two_sum_f(x.h, -n * c1);
+  const float p2 = __fmul_rn(n, c2h);
+  r = f2_add(r, {-p2, -fmaf(n, c2h, -p2)});
+  r = f2_add(r, {-n * c2l, 0.f});
+  r = f2_add(r, {x.l, 0.f});
+  const F2 e = f2_add({1.f, 0.f}, f2_expm1_small(r));
+  const float s = n < -126.f ? 0.f : __int_as_float((static_cast<int>(n) + 127) << 23);
+  return f2_scale(e, s);
+}
+__device__ __forceinline__ F2 f2_log(F2 x) { // x > 0
+  F2 d;
+  float y0;
+  if (fabsf(x.h - 1.f) < 0.25f) {
+    // near 1 the result is small: d = (1 + u) e^-y0 - 1 = m + u (1 + m),
+    // m = e^-y0 - 1, each term with its own relative accuracy
+    const F2 u = f2_add(x, {-1.f, 0.f}); // exact (Sterbenz)
+    y0 = log1pf(u.h);
+    const F2 m = f2_expm1_small({-y0, 0.f});
+    d = f2_add(m, f2_mul(u, f2_add({1.f, 0.f}, m)));
+  } else {
+    y0 = logf(x.h);
+    d = f2_add(f2_mul(x, f2_exp({-y0, 0.f})), {-1.f, 0.f}); // x e^-y0 - 1, ~1e-7
+  }
+  // log(1 + d) = d - d^2 / 2 + O(d^3)
+  return f2_add({y0, 0.f}, f2_add(d, {-0.5f * d.h * d.h, 0.f}));
+}
+__device__ __forceinline__ F2 f2_cbrt(F2 x) { // x > 0
+  const float y0 = cbrtf(x.h);
+  const F2 y3 = f2_mul(f2_mul({y0, 0.f}, {y0, 0.f}), {y0, 0.f});
+  const F2 r = f2_add(x, f2_neg(y3));
+  return quick_two_sum(y0, __fdiv_rn(r.h, 3.f * y0 * y0));
+}
+
 struct G {
   F2 v;
   float r, s;
@@ -171,10 +243,13 @@ __device__ __forceinline__ G operator/(double c, G b) {
 __device__ __forceinline__ G neg(G a) { return {f2_neg(a.v), -a.r, -a.s}; }
 __device__ __forceinline__ G mkg(double v) { return {f2c(v), 0.f, 0.f}; }
 __device__ __forceinline__ G gapply(G a, double f, float df) { return {f2(f), df * a.r, df * a.s}; }
-__device__ __forceinline__ G dlog(G a) { return gapply(a, log(to_d(a.v)), 1.f / a.v.h); }
+__device__ __forceinline__ G dlog(G a) {
+  const float d = 1.f / a.v.h;
+  return {f2_log(a.v), d * a.r, d * a.s};
+}
 __device__ __forceinline__ G dexp(G a) {
-  const double e = exp(to_d(a.v));
-  return gapply(a, e, static_cast<float>(e));
+  const F2 e = f2_exp(a.v);
+  return {e, e.h * a.r, e.h * a.s};
 }
 __device__ __forceinline__ G dsqrt(G a) {
   const F2 s = f2_sqrt(a.v);
@@ -211,12 +286,12 @@ __device__ __forceinline__ RhoPowers<D3> rho_powers(D3 rho) {
   return {r13, r43, rm13};
 }
 __device__ __forceinline__ RhoPowers<G> rho_powers(G rho) {
-  const double rv = to_d(rho.v);
-  const double c = cbrt(rv);
-  const float cf = static_cast<float>(c), rf = rho.v.h;
-  G r13 = gapply(rho, c, cf / (3.f * rf));
+  const F2 c = f2_cbrt(rho.v);
+  const float cf = c.h, rf = rho.v.h;
+  const float d13 = cf / (3.f * rf), dm13 = -1.f / (3.f * cf * rf);
+  G r13 = {c, d13 * rho.r, d13 * rho.s};
   G r43 = rho * r13;
-  G rm13 = gapply(rho, 1.0 / c, -1.f / (3.f * cf * rf));
+  G rm13 = {f2_div({1.f, 0.f}, c), dm13 * rho.r, dm13 * rho.s};
   return {r13, r43, rm13};
 }
 
