@@ -409,17 +409,25 @@ class DFT:
         self.ctx.lib.occ_xc_molecule_grid(self.h, _ptr(pts), _ptr(w))
         return pts, w
 
-    def compute_vxc(self, D, precision=FP64):
+    def compute_vxc(self, D, precision=FP64, out=None):
         """V_xc for mo.D; E_xc via exchange_correlation_energy().  As OCC's
         compute_vxc dispatches on mo.kind, the shape of D decides: nbf x nbf is
-        restricted, 2 nbf x nbf (alpha block above beta) unrestricted."""
+        restricted, 2 nbf x nbf (alpha block above beta) unrestricted.  out
+        (optional): a Fortran-ordered float64 nbf x nbf array to receive V,
+        e.g. in pinned memory."""
         nbf = self.nbf()
         Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
         if Dm.shape == (2 * nbf, nbf):
             return self.compute_vxc_unrestricted(Dm, precision)
         if Dm.shape != (nbf, nbf):
             raise XCError(f"density matrix must be {nbf}x{nbf} or {2 * nbf}x{nbf}")
-        V = np.zeros((nbf, nbf), order="F")
+        if out is not None:
+            if (out.shape != (nbf, nbf) or out.dtype != np.float64
+                    or not out.flags["F_CONTIGUOUS"]):
+                raise XCError(f"out must be a Fortran-ordered float64 {nbf}x{nbf} array")
+            V = out
+        else:
+            V = np.zeros((nbf, nbf), order="F")
         exc = C.c_double()
         nel = C.c_double()
         rc = self.ctx.lib.occ_xc_compute_vxc(self.ctx.h, self.h, _ptr(Dm), int(precision),
