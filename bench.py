@@ -52,13 +52,14 @@ def parse():
                     help="CTAs of the persistent tensor-core kernels (0: one per SM)")
     ap.add_argument("--workload", default="water32",
                     choices=["water32", "alkane", "clusters", "stream", "gradient", "grid", "uks",
-                             "vv10"],
+                             "vv10", "mgga"],
                     help="water32: the headline build (default); alkane: C30H62 def2-TZVP "
                          "B3LYP, 15 iterations as one CUDA graph; clusters: 512 clusters "
                          "as one batch; stream: served Poisson request stream; gradient: "
                          "the XC nuclear gradient of the water32 molecule; grid: its molecular "
                          "grid with the Becke partition on the GPU; uks: an unrestricted FP64 "
-                         "build of its cation radical; vv10: its VV10 non-local correlation")
+                         "build of its cation radical; vv10: its VV10 non-local correlation; "
+                         "mgga: its meta-GGA (TPSS) FP64 build")
     ap.add_argument("--clusters", type=int, default=512)
     ap.add_argument("--requests", type=int, default=32)
     ap.add_argument("--rate", type=float, default=10.0, help="stream arrivals per second")
@@ -84,6 +85,8 @@ def run_workload(args):
             r = bw.uks_build(torch, steps=args.steps, warmup=args.warmup, waters=args.waters)
         elif args.workload == "vv10":
             r = bw.vv10(steps=args.steps, warmup=args.warmup, waters=args.waters)
+        elif args.workload == "mgga":
+            r = bw.mgga_build(torch, steps=args.steps, warmup=args.warmup, waters=args.waters)
         else:
             r = bw.stream(nreq=args.requests, rate=args.rate)
     if args.workload in ("uks", "vv10"):
@@ -95,6 +98,16 @@ def run_workload(args):
                 "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
                 "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "tf32x3+f64" if args.workload == "uks" else "f32+f64",
+                "data": "synthetic", "config": {"workload": r.pop("workload")},
+                "clocks": cs.summary()}
+        line.update(r)
+        print(json.dumps(line))
+        return
+    if args.workload == "mgga":
+        line = {"metric": "meta-GGA (TPSS) XC builds/s, FP64",
+                "value": r["fp64"]["builds_per_s"], "unit": "builds/s", "n_gpus": 1,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": {"workload": r.pop("workload")},
                 "clocks": cs.summary()}
         line.update(r)

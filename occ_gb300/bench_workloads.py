@@ -372,6 +372,85 @@ def uks_build(torch, steps=5, warmup=2, waters=32, seed=0):
     return out
 
 
+def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
+    """The restricted meta-GGA (TPSS) build of the water cluster, FP64, D and
+    V resident; the full-size oracle build beside it (parity and the CPU
+    baseline)."""
+    import os
+    import sys
+    box = 10.0 * (waters / 32.0) ** (1.0 / 3.0)
+    mol = wl.water_cluster(waters, box=box, seed=seed)
+    b = wl.basis_for(mol, "def2-svp")
+    nbf = b.nbf()
+    D = wl.random_density(nbf, 5 * waters, seed=seed)
+    dft = DFT("tpss", b)
+    lib = dft.ctx.lib
+    dD = torch.from_numpy(np.asfortranarray(D).ravel(order="F").copy()).cuda()
+    dV = torch.zeros_like(dD)
+    d2 = torch.zeros(2, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def one():
+        rc = lib.occ_xc_compute_vxc_device(dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), FP64,
+                                           C.c_void_p(dV.data_ptr()), C.c_void_p(d2.data_ptr()),
+                                           C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(dft.ctx.error())
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for i in range(steps):
+        one()
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        V = dft.compute_vxc(D)
+    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    e = dft.exchange_correlation_energy()
+    # per-kernel device time (the library's CUDA-event profiler), two builds
+    lib.occ_xc_profile_enable.argtypes = [C.c_void_p, C.c_int]
+    lib.occ_xc_profile_reset.argtypes = [C.c_void_p]
+    lib.occ_xc_profile_count.argtypes = [C.c_void_p]
+    lib.occ_xc_profile_entry.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_char_p),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_long)]
+    lib.occ_xc_profile_reset(dft.ctx.h)
+    lib.occ_xc_profile_enable(dft.ctx.h, 1)
+    for _ in range(2):
+        dft.compute_vxc(D)
+    prof = {}
+    for i in range(lib.occ_xc_profile_count(dft.ctx.h)):
+        name, kms, cnt = C.c_char_p(), C.c_double(), C.c_long()
+        lib.occ_xc_profile_entry(dft.ctx.h, i, C.byref(name), C.byref(kms), C.byref(cnt))
+        prof[name.value.decode()] = kms.value / max(cnt.value, 1)
+    lib.occ_xc_profile_enable(dft.ctx.h, 0)
+    lib.occ_xc_profile_reset(dft.ctx.h)
+    out = {"workload": f"water{waters}_def2svp_tpss", "nbf": nbf,
+           "npoints": int(dft.info()["npoints"]), "fp64": {"builds_per_s": 1e3 / ms,
+                                                          "ms_per_build": ms, "exc": e},
+           "e2e": {"value": 1e3 / e2e_ms, "unit": "builds/s",
+                   "h2d_bytes_per_step": int(D.size * 8),
+                   "d2h_bytes_per_step": int(D.size * 8 + 16)}}
+    out["kernels_ms_per_launch"] = prof
+    if oracle_check:
+        root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+        sys.path.insert(0, os.path.join(root, "oracle"))
+        import oracle
+        P, W = dft.grid()
+        t0 = time.perf_counter()
+        e_ref, V_ref, _ = oracle.xc_build(b, P, W, D, "tpss")
+        t_cpu = time.perf_counter() - t0
+        out["abs_dE_vs_oracle"] = abs(e - e_ref)
+        out["max_abs_dV_vs_oracle"] = float(np.max(np.abs(V - V_ref)))
+        out["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "builds/s",
+                               "cores": os.cpu_count(), "kind": "port",
+                               "sample": "one whole build of the same molecule"}
+    return out
+
+
 def vv10(steps=3, warmup=1, waters=32, seed=0):
     box = 10.0 * (waters / 32.0) ** (1.0 / 3.0)
     mol = wl.water_cluster(waters, box=box, seed=seed)

@@ -70,6 +70,9 @@ void upload_sph_table();
 void launch_colloc_f64(const MolDev &m, int deriv, double *ws, cudaStream_t st);
 void launch_rho_f64(const MolDev &m, int deriv, const double *D, const double *ws,
                     const SlabItem *slabs, int nslabs, double *rho, cudaStream_t st);
+// meta-GGA: the three (d_k phi) D2 (d_k phi) sums into rho components 4-6
+void launch_tau_f64(const MolDev &m, const double *D, const double *ws, const SlabItem *slabs,
+                    int nslabs, double *rho, cudaStream_t st);
 void launch_func(const MolDev &m, int deriv, const FuncSet &fs, double dens_thr, const double *rho,
                  double *coef, double *epart, cudaStream_t st);
 void launch_vxc_f64(const MolDev &m, int deriv, const double *ws, const double *coef,

@@ -18,6 +18,7 @@
 #include "../../include/occ_xc.h"
 #include "host/gto_eval.h"
 #include "host/xc_host.hpp"
+#include "functionals_mgga.cuh"
 #include "xc_device.cuh"
 #include "xc_engine.hpp"
 
@@ -74,6 +75,13 @@ FuncSet parse_method(const std::string &method_in) {
       add(kHybB3lyp);
     } else if (tok == "b3lyp5") {
       add(kHybB3lyp5);
+    } else if (tok == "tpss") {
+      add(kMggaXTpss);
+      add(kMggaCTpss);
+    } else if (tok == "mgga_x_tpss" || tok == "xc_mgga_x_tpss") {
+      add(kMggaXTpss);
+    } else if (tok == "mgga_c_tpss" || tok == "xc_mgga_c_tpss") {
+      add(kMggaCTpss);
     } else if (tok == "lda_x" || tok == "xc_lda_x") {
       add(kLdaX);
     } else if (tok == "lda_c_vwn" || tok == "xc_lda_c_vwn") {
@@ -97,6 +105,12 @@ FuncSet parse_method(const std::string &method_in) {
   if (fs.n == 0)
     throw MethodError("empty method string");
   return fs;
+}
+
+void require_not_mgga(int deriv, const char *what) {
+  if (deriv == 2)
+    throw ArgError(std::string(what) + ": not available for meta-GGA functionals "
+                   "(the restricted FP64 build is)");
 }
 
 Molecule::~Molecule() {
@@ -208,14 +222,14 @@ void Molecule::upload() {
 
   const size_t N = static_cast<size_t>(std::max<long>(plan.npts, 1));
   const size_t nl = std::max<size_t>(leaves.size(), 1);
-  d_rho = static_cast<double *>(alloc(4 * N * sizeof(double)));
-  d_coef = static_cast<double *>(alloc(4 * N * sizeof(double)));
+  d_rho = static_cast<double *>(alloc(rho_components(deriv) * N * sizeof(double)));
+  d_coef = static_cast<double *>(alloc(coef_components(deriv) * N * sizeof(double)));
   d_epart = static_cast<double *>(alloc(2 * nl * sizeof(double)));
   d_out2 = static_cast<double *>(alloc(2 * sizeof(double)));
   const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
   d_D = static_cast<double *>(alloc(std::max<size_t>(nbf2, 1) * sizeof(double)));
   d_V = static_cast<double *>(alloc(std::max<size_t>(nbf2, 1) * sizeof(double)));
-  cuda_check(cudaMemset(d_rho, 0, 4 * N * sizeof(double)), "cudaMemset");
+  cuda_check(cudaMemset(d_rho, 0, rho_components(deriv) * N * sizeof(double)), "cudaMemset");
 }
 
 MolDev Molecule::dev() const {
@@ -263,6 +277,10 @@ void Molecule::build_fp64(const double *dD, double *dV, double *dout2, cudaStrea
   c.launch("rho_f64", st, [&] {
     launch_rho_f64(m, deriv, dD, ws, d_slabs, static_cast<int>(slabs.size()), d_rho, st);
   });
+  if (deriv == 2)
+    c.launch("tau_f64", st, [&] {
+      launch_tau_f64(m, dD, ws, d_slabs, static_cast<int>(slabs.size()), d_rho, st);
+    });
   c.launch("func", st, [&] {
     launch_func(m, deriv, fs, bs.density_threshold, d_rho, d_coef, d_epart, st);
   });
@@ -405,7 +423,9 @@ std::unique_ptr<Molecule> molecule_host(Context *ctx, const MoleculeArgs &a) {
   M->fs = parse_method(a.method);
   M->deriv = 0;
   for (int i = 0; i < M->fs.n; i++)
-    M->deriv = std::max(M->deriv, func_is_gga(M->fs.id[i]) ? 1 : 0);
+    M->deriv = std::max(M->deriv, func_is_mgga(M->fs.id[i]) ? 2
+                                  : func_is_gga(M->fs.id[i]) ? 1
+                                                             : 0);
   M->Z.assign(a.Z, a.Z + a.natoms);
   M->xyz.assign(a.xyz, a.xyz + 3 * a.natoms);
   M->basis = make_basis(a.natoms, a.xyz, a.nshells, a.shell_l, a.shell_atom,
@@ -490,7 +510,7 @@ double Molecule::estimate_resident_bytes() const {
   double b = r(N * sizeof(Pt4)) + r(nsh * sizeof(DevShell)) + r(nprim * sizeof(double2)) +
              r(nl * sizeof(DevLeaf)) + r(leaf_sh.size() * 4.0) + r(leaf_ao.size() * 4.0) +
              r(slabs.size() * sizeof(SlabItem)) + r(tiles.size() * sizeof(TileItem));
-  b += 2 * r(4 * N * 8.0) + r(2 * nl * 8.0) + r(16.0) + 2 * r(nbf2 * 8.0);
+  b += r(rho_components(deriv) * N * 8.0) + r(coef_components(deriv) * N * 8.0) + r(2 * nl * 8.0) + r(16.0) + 2 * r(nbf2 * 8.0);
   double blocks = 0, items = 0;
   for (const DevLeaf &L : leaves) {
     const double nb = std::ceil(L.cnt / 128.0);

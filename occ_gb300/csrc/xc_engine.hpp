@@ -43,6 +43,12 @@ template <typename T> T *dev_upload(const std::vector<T> &h, size_t &bytes) {
 }
 void fill_sph_table(double *out);
 void upload_sph_table_grad();
+// Components of the FP64 path's per-point density array (rho, grad rho and,
+// for a meta-GGA, the three tau sums) and of its V_xc coefficient array.
+inline int rho_components(int deriv) { return deriv == 2 ? 7 : deriv ? 4 : 1; }
+inline int coef_components(int deriv) { return deriv == 2 ? 5 : deriv ? 4 : 1; }
+// Entry points that have no meta-GGA form throw ArgError for one.
+void require_not_mgga(int deriv, const char *what);
 // the unrestricted build's polarised functional stage and its sums (xc_uks.cu)
 void launch_func_pol(const MolDev &m, int deriv, const FuncSet &fs, double thr,
                      const double *rho_a, const double *rho_b, double *coef_a, double *coef_b,
@@ -139,7 +145,7 @@ struct Molecule {
   GridSettings gs;
   BuildSettings bs;
   FuncSet fs{};
-  int deriv = 0;
+  int deriv = 0; // OCC's density_derivative(): 0 LDA, 1 GGA, 2 meta-GGA
   int vxc_n = 256; // tuning: N of the mixed path's V_xc tile
   int ctas = 0;    // tuning: CTAs of its persistent kernels (0: the context's setting)
   MolecularGrid grid;

@@ -141,20 +141,23 @@ __global__ void __launch_bounds__(128) k_colloc_f64(MolDev m, double *__restrict
 
 // rho for one 64-point slab of one leaf.  Thread (tx, ty): points
 // p0 + tx + 16 i, AOs j0 + ty + 16 jj.
-template <bool DERIV>
+// TAU (meta-GGA, grid.y = 3): the same GEMM on the derivative plane
+// k = 1 + blockIdx.y, (d_k phi) D2 (d_k phi) into rho component 4 + blockIdx.y
+// (tau = half their sum, src/gto/density.cpp:84-96).
+template <bool DERIV, bool TAU = false>
 __global__ void __launch_bounds__(256) k_rho_f64(MolDev m, const double *__restrict__ D,
                                                  const double *__restrict__ ws,
                                                  const SlabItem *__restrict__ slabs,
                                                  double *__restrict__ rho) {
-  constexpr int NC = DERIV ? 4 : 1;
+  constexpr int NC = (DERIV && !TAU) ? 4 : 1;
   __shared__ double As[kKChunk][kPtTile];
   __shared__ double Bs[kKChunk][kAoTile];
   __shared__ double red[16][NC][kPtTile];
   const SlabItem it = slabs[blockIdx.x];
   const DevLeaf L = m.leaves[it.leaf];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const double *phi = ws + L.ws_off;
   const size_t plane = static_cast<size_t>(L.mpad) * L.npad;
+  const double *phi = ws + L.ws_off + (TAU ? (1 + blockIdx.y) * plane : 0);
   const int *g = m.leaf_ao + L.ao_begin;
   const size_t nbf = static_cast<size_t>(m.nbf);
   double part[NC][4];
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(256) k_rho_f64(MolDev m, const double *__restr
       for (int i = 0; i < 4; i++) {
         const size_t o = row + tx + 16 * i;
         part[0][i] = fma(phi[o], acc[i][j], part[0][i]);
-        if (DERIV) {
+        if (DERIV && !TAU) {
           part[1][i] = fma(phi[plane + o], acc[i][j], part[1][i]);
           part[2][i] = fma(phi[2 * plane + o], acc[i][j], part[2][i]);
           part[3][i] = fma(phi[3 * plane + o], acc[i][j], part[3][i]);
@@ -229,7 +232,11 @@ __global__ void __launch_bounds__(256) k_rho_f64(MolDev m, const double *__restr
     for (int t = 0; t < 16; t++)
       s += red[t][c][p];
     const int lp = it.p0 + p;
-    if (lp < L.cnt)
+    if (lp >= L.cnt)
+      continue;
+    if (TAU)
+      rho[static_cast<size_t>(4 + blockIdx.y) * m.npts + L.off + lp] = s;
+    else
       rho[static_cast<size_t>(c) * m.npts + L.off + lp] = (c == 0) ? s : 2.0 * s;
   }
 }
@@ -262,9 +269,21 @@ __global__ void __launch_bounds__(256) k_func(MolDev m, FuncSet fs, double thr,
                          coef, epart + 2 * blockIdx.x, sh);
 }
 
+__global__ void __launch_bounds__(256) k_func_mgga(MolDev m, FuncSet fs, double thr,
+                                                   const double *__restrict__ rho,
+                                                   double *__restrict__ coef,
+                                                   double *__restrict__ epart) {
+  __shared__ double sh[8];
+  leaf_functional_mgga(m.leaves[blockIdx.x], m.pts, static_cast<size_t>(m.npts), fs, thr, rho,
+                       coef, epart + 2 * blockIdx.x, sh);
+}
+
 // K = phi_I^T Y_J for one 64x64 AO tile of one leaf; V += K + K^T.
 // Thread (tx, ty): K rows i0 + ty + 16 a, columns j0 + tx + 16 b.
-template <bool DERIV>
+// META adds sum_k (d_k phi_I)^T diag(c_tau) (d_k phi_J) with c_tau =
+// 0.25 w vtau (coefficient component 4), so that K + K^T carries the
+// tau term of src/dft/xc_potential_matrix.cpp:43-56 once.
+template <bool DERIV, bool META = false>
 __global__ void __launch_bounds__(256) k_vxc_f64(MolDev m, const double *__restrict__ ws,
                                                  const double *__restrict__ coef,
                                                  const TileItem *__restrict__ tiles,
@@ -283,21 +302,28 @@ __global__ void __launch_bounds__(256) k_vxc_f64(MolDev m, const double *__restr
 #pragma unroll
     for (int b = 0; b < 4; b++)
       acc[a][b] = 0.0;
+  constexpr int NSEG = META ? 4 : 1;
+  for (int seg = 0; seg < NSEG; seg++)
   for (int p0 = 0; p0 < L.npad; p0 += kKChunk) {
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const int idx = threadIdx.x + r * 256;
       const int pp = idx & 15, aa = idx >> 4;
       const int p = p0 + pp;
-      As[pp][aa] = phi[static_cast<size_t>(it.i0 + aa) * L.npad + p];
+      const double *a = phi + seg * plane; // seg 0: phi; 1..3: d_k phi
+      As[pp][aa] = a[static_cast<size_t>(it.i0 + aa) * L.npad + p];
       const size_t o = static_cast<size_t>(it.j0 + aa) * L.npad + p;
       double y = 0.0;
       if (p < L.cnt) {
         const size_t gi = static_cast<size_t>(L.off) + p;
-        y = coef[gi] * phi[o];
-        if (DERIV)
-          y += coef[N + gi] * phi[plane + o] + coef[2 * N + gi] * phi[2 * plane + o] +
-               coef[3 * N + gi] * phi[3 * plane + o];
+        if (seg == 0) {
+          y = coef[gi] * phi[o];
+          if (DERIV)
+            y += coef[N + gi] * phi[plane + o] + coef[2 * N + gi] * phi[2 * plane + o] +
+                 coef[3 * N + gi] * phi[3 * plane + o];
+        } else {
+          y = coef[4 * N + gi] * a[o];
+        }
       }
       Bs[pp][aa] = y;
     }
@@ -382,11 +408,20 @@ void launch_rho_f64(const MolDev &m, int deriv, const double *D, const double *w
     k_rho_f64<false><<<nslabs, 256, 0, st>>>(m, D, ws, slabs, rho);
 }
 
+void launch_tau_f64(const MolDev &m, const double *D, const double *ws, const SlabItem *slabs,
+                    int nslabs, double *rho, cudaStream_t st) {
+  if (nslabs == 0)
+    return;
+  k_rho_f64<true, true><<<dim3(nslabs, 3), 256, 0, st>>>(m, D, ws, slabs, rho);
+}
+
 void launch_func(const MolDev &m, int deriv, const FuncSet &fs, double thr, const double *rho,
                  double *coef, double *epart, cudaStream_t st) {
   if (m.nleaves == 0)
     return;
-  if (deriv)
+  if (deriv == 2)
+    k_func_mgga<<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho, coef, epart);
+  else if (deriv)
     k_func<true><<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho, coef, epart);
   else
     k_func<false><<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho, coef, epart);
@@ -396,7 +431,9 @@ void launch_vxc_f64(const MolDev &m, int deriv, const double *ws, const double *
                     const TileItem *tiles, int ntiles, double *V, cudaStream_t st) {
   if (ntiles == 0)
     return;
-  if (deriv)
+  if (deriv == 2)
+    k_vxc_f64<true, true><<<ntiles, 256, 0, st>>>(m, ws, coef, tiles, V);
+  else if (deriv)
     k_vxc_f64<true><<<ntiles, 256, 0, st>>>(m, ws, coef, tiles, V);
   else
     k_vxc_f64<false><<<ntiles, 256, 0, st>>>(m, ws, coef, tiles, V);

@@ -353,6 +353,7 @@ void upload_sph_table_grad() {
 // relative to their group), their slabs, leaf groups under the workspace cap,
 // and the AO -> atom map.  Allocated on the first gradient of a molecule.
 void Molecule::prepare_gradient() {
+  require_not_mgga(deriv, "XC gradient");
   if (d_gws)
     return;
   if (!d_pts)

@@ -7,6 +7,7 @@
 // coef1..3 = 2 w vsigma grad rho.  epart2 receives {sum w e_xc rho, sum w rho}.
 #pragma once
 #include "functionals.cuh"
+#include "functionals_mgga.cuh"
 #include "xc_device.cuh"
 
 namespace occx {
@@ -78,6 +79,50 @@ __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__r
       coef[2 * N + idx] = f * gy;
       coef[3 * N + idx] = f * gz;
     }
+    ew += w * e;
+  }
+  nel = leaf_sum256(nel, sh);
+  ew = leaf_sum256(ew, sh);
+  if (threadIdx.x == 0) {
+    epart2[0] = ew;
+    epart2[1] = nel;
+  }
+}
+
+// The meta-GGA functional stage (FP64): rho components 0-3 as for a GGA and
+// 4-6 the three (d_k phi) D2 (d_k phi) sums, tau = half their sum
+// (src/gto/density.cpp:84-96, include/occ/dft/dft_kernels.h:49-58).
+// Coefficients 0-3 as for a GGA and coef4 = 0.25 w vtau (the V kernel's
+// K + K^T then carries src/dft/xc_potential_matrix.cpp:43-56's 0.5 w vtau).
+__device__ __forceinline__ void leaf_functional_mgga(const DevLeaf &L,
+                                                     const Pt4 *__restrict__ pts, size_t N,
+                                                     const FuncSet &fs, double thr,
+                                                     const double *__restrict__ rho,
+                                                     double *__restrict__ coef, double *epart2,
+                                                     double *sh) {
+  double mx = -1e300;
+  for (int p = threadIdx.x; p < L.cnt; p += 256)
+    mx = fmax(mx, rho[static_cast<size_t>(L.off) + p]);
+  mx = leaf_max256(mx, sh);
+  const bool skip = mx < thr;
+  double nel = 0.0, ew = 0.0;
+  for (int p = threadIdx.x; p < L.cnt; p += 256) {
+    const size_t idx = static_cast<size_t>(L.off) + p;
+    const double r = rho[idx];
+    const double w = pts[idx].w;
+    nel += w * r;
+    const double gx = rho[N + idx], gy = rho[2 * N + idx], gz = rho[3 * N + idx];
+    const double sigma = gx * gx + gy * gy + gz * gz;
+    const double tau = 0.5 * (rho[4 * N + idx] + rho[5 * N + idx] + rho[6 * N + idx]);
+    double e = 0, vr = 0, vs = 0, vt = 0;
+    if (!skip)
+      eval_xc_mgga(fs, r, sigma, tau, e, vr, vs, vt);
+    coef[idx] = 0.5 * w * vr;
+    const double f = 2.0 * w * vs;
+    coef[N + idx] = f * gx;
+    coef[2 * N + idx] = f * gy;
+    coef[3 * N + idx] = f * gz;
+    coef[4 * N + idx] = 0.25 * w * vt;
     ew += w * e;
   }
   nel = leaf_sum256(nel, sh);

@@ -1639,6 +1639,7 @@ void make_plan_lists(LaunchPlan &P, const std::vector<Molecule *> &mols,
                      const std::vector<MixTab> &tabs) {
   P.tabs = tabs;
   P.deriv = mols.empty() ? 0 : mols[0]->deriv;
+  require_not_mgga(P.deriv, "mixed precision");
   std::vector<VItem> items;
   for (size_t mi = 0; mi < mols.size(); mi++) {
     Molecule &M = *mols[mi];
@@ -2765,6 +2766,7 @@ struct GradMixed {
 void free_grad_mixed(GradMixed *g) { delete g; }
 
 void Molecule::prepare_gradient_mixed() {
+  require_not_mgga(deriv, "XC gradient");
   if (gmixed)
     return;
   if (!mixed)

@@ -73,7 +73,9 @@ extern "C" int occ_xc_compute_vxc_noalloc(occ_xc_context *ctx, occ_xc_molecule *
     Molecule &M = *mol->impl;
     const size_t N = static_cast<size_t>(M.plan.npts);
     const size_t nl = M.leaves.size();
-    const size_t need = align_elems(M.ws_elems) + 2 * align_elems(4 * N) + align_elems(2 * nl);
+    const size_t nrho = rho_components(M.deriv) * N, ncoef = coef_components(M.deriv) * N;
+    const size_t need = align_elems(M.ws_elems) + align_elems(nrho) + align_elems(ncoef) +
+                        align_elems(2 * nl);
     if (need * sizeof(double) > kNoAllocScratchBytes) {
       ctx->err = "occ_xc_compute_vxc_noalloc: this molecule needs " +
                  std::to_string(need * sizeof(double)) +
@@ -84,18 +86,20 @@ extern "C" int occ_xc_compute_vxc_noalloc(occ_xc_context *ctx, occ_xc_molecule *
     cuda_check(cudaSetDevice(c.device), "cudaSetDevice");
     double *ws = noalloc_scratch(c.device);
     double *rho = ws + align_elems(M.ws_elems);
-    double *coef = rho + align_elems(4 * N);
-    double *epart = coef + align_elems(4 * N);
+    double *coef = rho + align_elems(nrho);
+    double *epart = coef + align_elems(ncoef);
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c.stream;
     const MolDev m = M.dev();
     const size_t nbf2 = static_cast<size_t>(M.basis.nbf) * M.basis.nbf;
     cuda_check(cudaMemsetAsync(d_V, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
     launch_colloc_f64(m, M.deriv, ws, st);
     launch_rho_f64(m, M.deriv, d_D, ws, M.d_slabs, static_cast<int>(M.slabs.size()), rho, st);
+    if (M.deriv == 2)
+      launch_tau_f64(m, d_D, ws, M.d_slabs, static_cast<int>(M.slabs.size()), rho, st);
     launch_func(m, M.deriv, M.fs, M.bs.density_threshold, rho, coef, epart, st);
     launch_vxc_f64(m, M.deriv, ws, coef, M.d_tiles, static_cast<int>(M.tiles.size()), d_V, st);
     launch_reduce(epart, m.nleaves, d_exc2, st);
-    c.launches += 5;
+    c.launches += M.deriv == 2 ? 6 : 5;
     cuda_check(cudaGetLastError(), "kernel launch");
     return OCC_XC_OK;
   } catch (const CudaError &e) {

@@ -122,6 +122,7 @@ void launch_reduce3(const double *epart3, int n, double *out3, cudaStream_t st) 
 }
 
 void Molecule::prepare_uks() {
+  require_not_mgga(deriv, "unrestricted build");
   if (d_rho_b)
     return;
   if (!d_pts)

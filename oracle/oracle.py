@@ -27,8 +27,9 @@ _lib = None
 METHODS = {
     "lda": [1, 30], "svwn": [1, 30], "lsda": [1, 30], "svwn5": [1, 7],
     "pbe": [101, 130], "blyp": [106, 131], "bpbe": [106, 130],
-    "b3lyp": [402], "b3lyp5": [475],
+    "b3lyp": [402], "b3lyp5": [475], "tpss": [202, 231],
 }
+MGGA_IDS = (202, 231)
 
 
 def build():
@@ -70,6 +71,37 @@ def functional(fid, rho, sigma=None):
     if rc != 0:
         raise ValueError(f"unknown functional {fid}")
     return exc, vrho, vsig
+
+
+def functional_mgga(fid, rho, sigma, tau):
+    """Unpolarised meta-GGA at n points: exc (per particle), vrho, vsigma, vtau."""
+    rho, sigma, tau = (np.ascontiguousarray(x, dtype=np.float64) for x in (rho, sigma, tau))
+    n = len(rho)
+    out = [np.zeros(n) for _ in range(4)]
+    L = lib()
+    L.oracle_functional_mgga.restype = C.c_int
+    L.oracle_functional_mgga.argtypes = [C.c_int, C.c_long] + [_dp] * 7
+    rc = L.oracle_functional_mgga(int(fid), n, _p(rho), _p(sigma), _p(tau),
+                                  *[_p(x) for x in out])
+    if rc != 0:
+        raise ValueError(f"not a meta-GGA: {fid}")
+    return tuple(out)
+
+
+def functional_mgga_polarized(fid, ra, rb, saa, sab, sbb, ta, tb):
+    """Polarised meta-GGA: exc (per particle), vrho (n x 2), vsigma (n x 3),
+    vtau (n x 2)."""
+    xs = [np.ascontiguousarray(x, dtype=np.float64) for x in (ra, rb, saa, sab, sbb, ta, tb)]
+    n = len(xs[0])
+    exc, vr, vs, vt = np.zeros(n), np.zeros((n, 2)), np.zeros((n, 3)), np.zeros((n, 2))
+    L = lib()
+    L.oracle_functional_mgga_polarized.restype = C.c_int
+    L.oracle_functional_mgga_polarized.argtypes = [C.c_int, C.c_long] + [_dp] * 11
+    rc = L.oracle_functional_mgga_polarized(int(fid), n, *[_p(x) for x in xs], _p(exc), _p(vr),
+                                            _p(vs), _p(vt))
+    if rc != 0:
+        raise ValueError(f"not a meta-GGA: {fid}")
+    return exc, vr, vs, vt
 
 
 def collocation(l, pure, exps, coefs, origin, xyz, deriv=1):

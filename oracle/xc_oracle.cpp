@@ -356,11 +356,12 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
     nbf += bs.size(s);
   }
   bs.nbf = nbf;
-  int deriv = 0;
+  int deriv = 0; // OCC's density_derivative(): 0 LDA, 1 GGA, 2 meta-GGA
   for (int f = 0; f < nfunc; f++) {
-    if (oracle_functional_is_gga(func_ids[f]) < 0)
-      return -1;
-    deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
+    if (oracle_functional_is_mgga(func_ids[f]))
+      deriv = 2;
+    else
+      deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
   }
   std::vector<double> ext(nsh);
   decay_cutoff(bs, screen_threshold, ext.data());
@@ -404,7 +405,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
     std::vector<double> &K = Vloc[tid];
     K.assign(static_cast<size_t>(nbf) * nbf, 0.0);
     std::vector<double> xyz, w, phi, Dloc, Dphi, rho, sigma, exc, vrho, vsig, e1, v1, s1, Y,
-        Kb;
+        Kb, tau, vtau, t1;
     std::vector<int> sig, loc0;
 #pragma omp for schedule(dynamic, 4)
     for (long li = 0; li < nleaves; li++) {
@@ -458,7 +459,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
           int s = sig[k], nf = bs.size(s);
           tmp.assign(static_cast<size_t>(ncomp) * nf * n, 0.0);
           collocate(sh_l[s], bs.pure, sh_nprim[s], exps + sh_off[s], coefs + sh_off[s],
-                    sh_origin + 3 * s, n, xyz.data(), 3, deriv, tmp.data(), n);
+                    sh_origin + 3 * s, n, xyz.data(), 3, deriv ? 1 : 0, tmp.data(), n);
           for (int q = 0; q < ncomp; q++)
             for (int f = 0; f < nf; f++)
               std::memcpy(&phi[(static_cast<size_t>(q) * m + loc0[k] + f) * n],
@@ -491,6 +492,33 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
               rho[q * n + p] += 2.0 * g[p] * dp[p];
           }
       }
+      // meta-GGA: tau = 0.5 sum_k (d_k phi) D2 (d_k phi) (src/gto/density.cpp:
+      // 70-97); the laplacian is not formed, as no functional here reads it
+      if (deriv == 2) {
+        tau.assign(n, 0.0);
+        for (int q = 1; q < 4; q++) {
+          std::fill(Dphi.begin(), Dphi.end(), 0.0);
+          for (int j = 0; j < m; j++) {
+            double *out = &Dphi[static_cast<size_t>(j) * n];
+            for (int k = 0; k < m; k++) {
+              double d = Dloc[static_cast<size_t>(j) * m + k];
+              if (d == 0.0)
+                continue;
+              const double *g = &phi[(static_cast<size_t>(q) * m + k) * n];
+              for (long p = 0; p < n; p++)
+                out[p] += g[p] * d;
+            }
+          }
+          for (int j = 0; j < m; j++) {
+            const double *dp = &Dphi[static_cast<size_t>(j) * n];
+            const double *g = &phi[(static_cast<size_t>(q) * m + j) * n];
+            for (long p = 0; p < n; p++)
+              tau[p] += g[p] * dp[p];
+          }
+        }
+        for (long p = 0; p < n; p++)
+          tau[p] *= 0.5;
+      }
       // totals and block skip (src/dft/dft_kernels.cpp:27-40)
       double maxrho = -1e300;
       for (long p = 0; p < n; p++) {
@@ -511,15 +539,23 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
       e1.resize(n);
       v1.resize(n);
       s1.resize(n);
+      vtau.assign(n, 0.0);
+      t1.assign(n, 0.0);
       for (int f = 0; f < nfunc; f++) {
         std::fill(s1.begin(), s1.end(), 0.0);
-        oracle_functional(func_ids[f], n, rho.data(), sigma.data(), e1.data(), v1.data(),
-                          s1.data());
+        std::fill(t1.begin(), t1.end(), 0.0);
+        if (oracle_functional_is_mgga(func_ids[f]))
+          oracle_functional_mgga(func_ids[f], n, rho.data(), sigma.data(), tau.data(), e1.data(),
+                                 v1.data(), s1.data(), t1.data());
+        else
+          oracle_functional(func_ids[f], n, rho.data(), sigma.data(), e1.data(), v1.data(),
+                            s1.data());
         double c = func_coefs ? func_coefs[f] : 1.0;
         for (long p = 0; p < n; p++) {
           exc[p] += c * e1[p];
           vrho[p] += c * v1[p];
           vsig[p] += c * s1[p];
+          vtau[p] += c * t1[p];
         }
       }
       // weight_by (include/occ/dft/functional.h:460-470)
@@ -527,6 +563,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
         exc[p] *= w[p];
         vrho[p] *= w[p];
         vsig[p] *= w[p];
+        vtau[p] *= w[p];
       }
       for (long p = 0; p < n; p++)
         eloc[tid] += rho[p] * exc[p];
@@ -568,6 +605,18 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
         for (int i = 0; i < m; i++)
           Kb[static_cast<size_t>(i) * m + i] *= 2.0;
       }
+      if (deriv == 2) // V += sum_k (d_k phi)^T diag(0.5 w vtau) (d_k phi)
+        for (int q = 1; q < 4; q++)
+          for (int j = 0; j < m; j++) {
+            const double *b = &phi[(static_cast<size_t>(q) * m + j) * n];
+            for (int i = 0; i < m; i++) {
+              const double *a = &phi[(static_cast<size_t>(q) * m + i) * n];
+              double acc = 0.0;
+              for (long p = 0; p < n; p++)
+                acc += a[p] * (0.5 * vtau[p]) * b[p];
+              Kb[static_cast<size_t>(j) * m + i] += acc;
+            }
+          }
       // scatter (dft.h:361-369)
       for (size_t a = 0; a < sig.size(); a++)
         for (size_t b = 0; b < sig.size(); b++) {
@@ -624,8 +673,8 @@ extern "C" int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim,
   }
   int deriv = 0;
   for (int f = 0; f < nfunc; f++) {
-    if (oracle_functional_is_gga(func_ids[f]) < 0)
-      return -1;
+    if (oracle_functional_is_mgga(func_ids[f]))
+      return -1; // meta-GGA: restricted energy and V only
     deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
   }
   const int ncomp = deriv ? 10 : 4;
@@ -852,8 +901,8 @@ extern "C" int oracle_xc_build_unrestricted(
   bs.nbf = nbf;
   int deriv = 0;
   for (int f = 0; f < nfunc; f++) {
-    if (oracle_functional_is_gga(func_ids[f]) < 0)
-      return -1;
+    if (oracle_functional_is_mgga(func_ids[f]))
+      return -1; // meta-GGA: restricted energy and V only
     deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
   }
   std::vector<double> ext(nsh);

@@ -29,6 +29,8 @@ enum {
   ORC_GGA_C_LYP = 131,
   ORC_HYB_GGA_XC_B3LYP = 402,
   ORC_HYB_GGA_XC_B3LYP5 = 475,
+  ORC_MGGA_X_TPSS = 202,
+  ORC_MGGA_C_TPSS = 231,
 };
 
 // Evaluate one functional on n points (unpolarised).  exc is energy per
@@ -44,6 +46,19 @@ int oracle_functional_polarized(int id, long n, const double *ra, const double *
                                 const double *saa, const double *sab, const double *sbb,
                                 double *exc, double *vra, double *vrb, double *vsaa,
                                 double *vsab, double *vsbb);
+
+// Meta-GGA functionals (xc_oracle_mgga.cpp), unpolarised: rho, sigma, tau in;
+// exc (per particle), vrho, vsigma, vtau out.  Returns -1 for an id that is
+// not a meta-GGA.
+int oracle_functional_is_mgga(int id);
+int oracle_functional_mgga(int id, long n, const double *rho, const double *sigma,
+                           const double *tau, double *exc, double *vrho, double *vsigma,
+                           double *vtau);
+// The polarised form: vr[2n] (a, b), vs[3n] (aa, ab, bb), vt[2n] (a, b).
+int oracle_functional_mgga_polarized(int id, long n, const double *ra, const double *rb,
+                                     const double *saa, const double *sab, const double *sbb,
+                                     const double *ta, const double *tb, double *exc,
+                                     double *vr, double *vs, double *vt);
 
 // Collocation of one shell (values and, if deriv, gradients; deriv 2 adds the
 // second derivatives xx, xy, xz, yy, yz, zz) at n points (xyz interleaved).
@@ -66,7 +81,9 @@ long oracle_morton_leaves(long n, const double *points, long target,
                           long *leaf_off, long *leaf_cnt, double *centres,
                           double *radii);
 
-// The whole restricted XC build.  D is OCC's mo.D (nbf x nbf, column-major);
+// The whole restricted XC build (LDA, GGA and meta-GGA: for a meta-GGA the
+// density adds tau (src/gto/density.cpp:70-97) and V the tau term of
+// src/dft/xc_potential_matrix.cpp:43-56).  D is OCC's mo.D (nbf x nbf, column-major);
 // V (nbf x nbf) receives V_xc = -K of compute_JK.  func ids/coefs give the
 // components summed as in src/dft/dft_kernels.cpp:55-58 (coefficients are
 // Libxc-internal mixture weights, not OCC's never-applied scale factors).

@@ -1,0 +1,187 @@
+"""Meta-GGA (TPSS) XC build: compute_K_dft<2, Restricted> (include/occ/dft/
+dft.h:192-388) with tau in the density (src/gto/density.cpp:70-97) and the
+tau term of V_xc (src/dft/xc_potential_matrix.cpp:43-56).
+
+Libxc, which evaluates mgga_x_tpss / mgga_c_tpss in the reference, is absent,
+so the oracle's TPSS is pinned by the functional's own exact constraints:
+the uniform-gas limit (F_x = 1, correlation = PW92), the exact hydrogen-atom
+exchange energy (-0.3125 Ha, to which TPSS's constants c and e were fitted)
+and zero correlation for any one-electron density.  The oracle's V_xc is
+pinned as the derivative of its E_xc."""
+import numpy as np
+import pytest
+
+import occ_gb300 as og
+import oracle
+from helpers import host_grid
+from test_fchk_density import fchk_case
+
+K2 = (3 * np.pi ** 2) ** (2 / 3)
+
+
+def test_tpss_uniform_gas_limit():
+    rho = np.array([1e-3, 0.05, 1.0, 30.0])
+    tau = 0.3 * K2 * rho ** (5 / 3)  # tau_unif, alpha = 1
+    sig = np.full(4, 1e-40)
+    ex = oracle.functional_mgga(202, rho, sig, tau)[0]
+    assert np.allclose(ex, oracle.functional(1, rho)[0], rtol=1e-14, atol=0)
+    ec = oracle.functional_mgga(231, rho, sig, tau)[0]
+    assert np.allclose(ec, oracle.functional(130, rho, sig)[0], rtol=1e-14, atol=0)
+
+
+def _hydrogen():
+    t = np.linspace(-12.0, 4.0, 20001)
+    r = np.exp(t)
+    dv = 4 * np.pi * r ** 3 * (t[1] - t[0])  # 4 pi r^2 dr on a log grid
+    n = np.exp(-2 * r) / np.pi
+    return n, 4 * n * n, n / 2, dv  # density, |grad n|^2, tau_W, volume element
+
+
+def test_tpss_hydrogen_atom_exchange_and_correlation():
+    n, s, t, dv = _hydrogen()
+    z = np.zeros_like(n)
+    ex = oracle.functional_mgga_polarized(202, n, z, s, z, z, t, z)[0]
+    ec = oracle.functional_mgga_polarized(231, n, z, s, z, z, t, z)[0]
+    assert abs(np.sum(ex * n * dv) + 0.3125) < 1e-6
+    assert abs(np.sum(ec * n * dv)) < 1e-12
+
+
+def test_tpss_one_electron_correlation_vanishes_pointwise():
+    rng = np.random.default_rng(5)
+    n = 10 ** rng.uniform(-6, 1, 64)
+    s = 10 ** rng.uniform(-6, 2, 64)
+    t = s / (8 * n)  # a single orbital: tau = tau_W
+    z = np.zeros_like(n)
+    ec = oracle.functional_mgga_polarized(231, n, z, s, z, z, t, z)[0]
+    assert np.max(np.abs(ec)) < 1e-14
+
+
+def test_tpss_restricted_is_the_polarised_form_at_zeta_zero():
+    rng = np.random.default_rng(6)
+    rho = 10 ** rng.uniform(-4, 1, 32)
+    sig = rho ** (8 / 3) * 10 ** rng.uniform(-3, 1, 32)
+    tau = sig / (8 * rho) * (1 + 10 ** rng.uniform(-2, 1, 32))
+    for fid in (202, 231):
+        e, vr, vs, vt = oracle.functional_mgga(fid, rho, sig, tau)
+        ep, vrp, vsp, vtp = oracle.functional_mgga_polarized(
+            fid, rho / 2, rho / 2, sig / 4, sig / 4, sig / 4, tau / 2, tau / 2)
+        assert np.allclose(e, ep, rtol=1e-13, atol=0)
+        assert np.allclose(vr, 0.5 * vrp.sum(1), rtol=1e-10, atol=1e-14)
+        assert np.allclose(vs, 0.25 * vsp.sum(1), rtol=1e-10, atol=1e-14)
+        assert np.allclose(vt, 0.5 * vtp.sum(1), rtol=1e-10, atol=1e-14)
+
+
+@pytest.mark.parametrize("fid", [202, 231])
+def test_tpss_derivatives_match_finite_differences(fid):
+    rng = np.random.default_rng(7)
+    for _ in range(8):
+        r = 10 ** rng.uniform(-2, 0.5)
+        s = r ** (8 / 3) * 10 ** rng.uniform(-2, 0.5)
+        t = s / (8 * r) * (1 + 10 ** rng.uniform(-1, 1))
+        _, vr, vs, vt = oracle.functional_mgga(fid, [r], [s], [t])
+
+        def e(R, S, T):
+            return oracle.functional_mgga(fid, [R], [S], [T])[0][0] * R
+
+        for x, v, f in ((r, vr[0], lambda h: e(r + h, s, t)),
+                        (s, vs[0], lambda h: e(r, s + h, t)),
+                        (t, vt[0], lambda h: e(r, s, t + h))):
+            h = 1e-5 * x
+            fd = (f(h) - f(-h)) / (2 * h)
+            assert abs(fd - v) <= 1e-6 * max(1.0, abs(v)), (x, v, fd)
+
+
+def test_oracle_tpss_potential_is_derivative_of_energy():
+    """dE_xc/d eps along a symmetric dD is 2 tr(V dD) (D2 = 2 D), the same
+    relation the GGA build satisfies: the tau term's 0.5 w vtau is exact."""
+    b, D, _ = fchk_case()
+    P, W = host_grid(b)
+    rng = np.random.default_rng(1)
+    E = rng.standard_normal(D.shape)
+    E = E + E.T
+    E *= 1e-3 / np.linalg.norm(E)
+    _, V, _ = oracle.xc_build(b, P, W, D, "tpss")
+    h = 1e-3
+    fd = (oracle.xc_build(b, P, W, D + h * E, "tpss")[0] -
+          oracle.xc_build(b, P, W, D - h * E, "tpss")[0]) / (2 * h)
+    assert abs(fd - 2 * np.sum(V * E)) < 1e-9
+
+
+def test_oracle_tpss_screened_matches_dense():
+    b, D, _ = fchk_case()
+    P, W = host_grid(b)
+    es, Vs, _ = oracle.xc_build(b, P, W, D, "tpss", screen=1e-10)
+    ed, Vd, _ = oracle.xc_build(b, P, W, D, "tpss", screen=0.0)
+    assert abs(es - ed) < 1e-8
+    assert np.max(np.abs(Vs - Vd)) < 1e-8
+
+
+TOL_E = 1e-8   # Ha, FP64 E_xc against the oracle
+TOL_V = 1e-9   # max |dV|, FP64
+
+
+@pytest.mark.gpu
+def test_tpss_converged_water_gpu_parity():
+    b, D, _ = fchk_case()
+    dft = og.DFT("tpss", b)
+    V = dft.compute_vxc(D)
+    P, W = dft.grid()
+    e_ref, V_ref, n_ref = oracle.xc_build(b, P, W, D, "tpss")
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= TOL_E
+    assert np.max(np.abs(V - V_ref)) <= TOL_V
+    assert abs(dft.integrated_density() - n_ref) <= 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("basis_name,pure,method", [("def2-svp", True, "tpss"),
+                                                    ("6-31g(d,p)", False, "tpss"),
+                                                    ("def2-tzvp", True, "mgga_x_tpss gga_c_pbe")])
+def test_tpss_water_cluster_gpu_parity(basis_name, pure, method):
+    """Several 64-AO tiles, d and f shells, Cartesian and pure, and a method
+    that mixes a meta-GGA with a GGA component."""
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(4, box=6.0, seed=3)
+    b = wl.basis_for(mol, basis_name, pure)
+    D = wl.random_density(b.nbf(), 20, seed=4)
+    dft = og.DFT(method, b)
+    V = dft.compute_vxc(D)
+    P, W = dft.grid()
+    ids = {"tpss": [202, 231], "mgga_x_tpss gga_c_pbe": [202, 130]}[method]
+    e_ref, V_ref, _ = oracle.xc_build(b, P, W, D, method, func_ids=ids)
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= TOL_E * max(1.0, abs(e_ref))
+    assert np.max(np.abs(V - V_ref)) <= TOL_V * max(1.0, np.max(np.abs(V_ref)))
+
+
+@pytest.mark.gpu
+def test_tpss_entry_points_without_a_meta_gga_form_refuse():
+    b, D, _ = fchk_case()
+    dft = og.DFT("tpss", b)
+    with pytest.raises(og.XCError, match="meta-GGA"):
+        dft.compute_vxc(D, og.MIXED)
+    with pytest.raises(og.XCError, match="meta-GGA"):
+        dft.compute_xc_gradient(D)
+    with pytest.raises(og.XCError, match="meta-GGA"):
+        dft.compute_vxc(np.vstack([0.5 * D, 0.5 * D]))
+    # the FP64 build still works on the same molecule afterwards
+    V = dft.compute_vxc(D)
+    assert np.all(np.isfinite(V))
+
+
+@pytest.mark.gpu
+def test_tpss_noalloc_entry_point():
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    b, D, _ = fchk_case()
+    dft = og.DFT("tpss", b)
+    V = dft.compute_vxc(D)
+    dD = torch.from_numpy(np.ascontiguousarray(D.T)).cuda()
+    dV = torch.zeros_like(dD)
+    de = torch.zeros(2, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    rc = dft.ctx.lib.occ_xc_compute_vxc_noalloc(dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()),
+                                               C.c_void_p(dV.data_ptr()),
+                                               C.c_void_p(de.data_ptr()), None)
+    assert rc == 0, dft.ctx.error()
+    torch.cuda.synchronize()
+    assert np.max(np.abs(dV.cpu().numpy().T - V)) < 1e-12
+    assert abs(de[0].item() - dft.exchange_correlation_energy()) < 1e-12
