@@ -59,7 +59,7 @@ def parse():
                          "the XC nuclear gradient of the water32 molecule; grid: its molecular "
                          "grid with the Becke partition on the GPU; uks: an unrestricted FP64 "
                          "build of its cation radical; vv10: its VV10 non-local correlation; "
-                         "mgga: its meta-GGA (TPSS) FP64 build")
+                         "mgga: its meta-GGA (TPSS) build")
     ap.add_argument("--clusters", type=int, default=512)
     ap.add_argument("--requests", type=int, default=32)
     ap.add_argument("--rate", type=float, default=10.0, help="stream arrivals per second")
@@ -104,10 +104,10 @@ def run_workload(args):
         print(json.dumps(line))
         return
     if args.workload == "mgga":
-        line = {"metric": "meta-GGA (TPSS) XC builds/s, FP64",
-                "value": r["fp64"]["builds_per_s"], "unit": "builds/s", "n_gpus": 1,
+        line = {"metric": "meta-GGA (TPSS) XC builds/s (tensor-core 3xTF32, FP64 beside it)",
+                "value": r["mixed"]["builds_per_s"], "unit": "builds/s", "n_gpus": 1,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3+f64",
                 "data": "synthetic", "config": {"workload": r.pop("workload")},
                 "clocks": cs.summary()}
         line.update(r)

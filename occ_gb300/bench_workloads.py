@@ -373,9 +373,9 @@ def uks_build(torch, steps=5, warmup=2, waters=32, seed=0):
 
 
 def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
-    """The restricted meta-GGA (TPSS) build of the water cluster, FP64, D and
-    V resident; the full-size oracle build beside it (parity and the CPU
-    baseline)."""
+    """The restricted meta-GGA (TPSS) build of the water cluster, FP64 and
+    tensor-core (3xTF32) precisions, D and V resident; the full-size oracle
+    build beside them (parity and the CPU baseline)."""
     import os
     import sys
     box = 10.0 * (waters / 32.0) ** (1.0 / 3.0)
@@ -389,52 +389,57 @@ def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
     dV = torch.zeros_like(dD)
     d2 = torch.zeros(2, dtype=torch.float64, device="cuda")
     stream = torch.cuda.Stream()
-
-    def one():
-        rc = lib.occ_xc_compute_vxc_device(dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), FP64,
-                                           C.c_void_p(dV.data_ptr()), C.c_void_p(d2.data_ptr()),
-                                           C.c_void_p(stream.cuda_stream))
-        if rc != 0:
-            raise RuntimeError(dft.ctx.error())
-    for _ in range(warmup):
-        one()
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-    ev[0].record(stream)
-    for i in range(steps):
-        one()
-        ev[i + 1].record(stream)
-    torch.cuda.synchronize()
-    ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        V = dft.compute_vxc(D)
-    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
-    e = dft.exchange_correlation_energy()
-    # per-kernel device time (the library's CUDA-event profiler), two builds
     lib.occ_xc_profile_enable.argtypes = [C.c_void_p, C.c_int]
     lib.occ_xc_profile_reset.argtypes = [C.c_void_p]
     lib.occ_xc_profile_count.argtypes = [C.c_void_p]
     lib.occ_xc_profile_entry.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_char_p),
                                          C.POINTER(C.c_double), C.POINTER(C.c_long)]
-    lib.occ_xc_profile_reset(dft.ctx.h)
-    lib.occ_xc_profile_enable(dft.ctx.h, 1)
-    for _ in range(2):
-        dft.compute_vxc(D)
-    prof = {}
-    for i in range(lib.occ_xc_profile_count(dft.ctx.h)):
-        name, kms, cnt = C.c_char_p(), C.c_double(), C.c_long()
-        lib.occ_xc_profile_entry(dft.ctx.h, i, C.byref(name), C.byref(kms), C.byref(cnt))
-        prof[name.value.decode()] = kms.value / max(cnt.value, 1)
-    lib.occ_xc_profile_enable(dft.ctx.h, 0)
-    lib.occ_xc_profile_reset(dft.ctx.h)
     out = {"workload": f"water{waters}_def2svp_tpss", "nbf": nbf,
-           "npoints": int(dft.info()["npoints"]), "fp64": {"builds_per_s": 1e3 / ms,
-                                                          "ms_per_build": ms, "exc": e},
-           "e2e": {"value": 1e3 / e2e_ms, "unit": "builds/s",
-                   "h2d_bytes_per_step": int(D.size * 8),
-                   "d2h_bytes_per_step": int(D.size * 8 + 16)}}
-    out["kernels_ms_per_launch"] = prof
+           "npoints": int(dft.info()["npoints"])}
+    res = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        def one():
+            rc = lib.occ_xc_compute_vxc_device(dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()),
+                                               prec, C.c_void_p(dV.data_ptr()),
+                                               C.c_void_p(d2.data_ptr()),
+                                               C.c_void_p(stream.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(dft.ctx.error())
+        for _ in range(warmup):
+            one()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record(stream)
+        for i in range(steps):
+            one()
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            V = dft.compute_vxc(D, prec)
+        e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+        res[name] = (dft.exchange_correlation_energy(), V)
+        # per-kernel device time (the library's CUDA-event profiler), two builds
+        lib.occ_xc_profile_reset(dft.ctx.h)
+        lib.occ_xc_profile_enable(dft.ctx.h, 1)
+        for _ in range(2):
+            dft.compute_vxc(D, prec)
+        prof = {}
+        for i in range(lib.occ_xc_profile_count(dft.ctx.h)):
+            kname, kms, cnt = C.c_char_p(), C.c_double(), C.c_long()
+            lib.occ_xc_profile_entry(dft.ctx.h, i, C.byref(kname), C.byref(kms), C.byref(cnt))
+            prof[kname.value.decode()] = kms.value / 2
+        lib.occ_xc_profile_enable(dft.ctx.h, 0)
+        lib.occ_xc_profile_reset(dft.ctx.h)
+        out[name] = {"builds_per_s": 1e3 / ms, "ms_per_build": ms, "exc": res[name][0],
+                     "kernels_ms_per_build": prof,
+                     "e2e": {"value": 1e3 / e2e_ms, "unit": "builds/s",
+                             "h2d_bytes_per_step": int(D.size * 8),
+                             "d2h_bytes_per_step": int(D.size * 8 + 16)}}
+    out["abs_dE_mixed_vs_fp64"] = abs(res["mixed"][0] - res["fp64"][0])
+    out["max_abs_dV_mixed_vs_fp64"] = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1])))
+    out["e2e"] = out["mixed"]["e2e"]
     if oracle_check:
         root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
         sys.path.insert(0, os.path.join(root, "oracle"))
@@ -443,8 +448,9 @@ def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
         t0 = time.perf_counter()
         e_ref, V_ref, _ = oracle.xc_build(b, P, W, D, "tpss")
         t_cpu = time.perf_counter() - t0
-        out["abs_dE_vs_oracle"] = abs(e - e_ref)
-        out["max_abs_dV_vs_oracle"] = float(np.max(np.abs(V - V_ref)))
+        for name in ("fp64", "mixed"):
+            out[name]["abs_dE_vs_oracle"] = abs(res[name][0] - e_ref)
+            out[name]["max_abs_dV_vs_oracle"] = float(np.max(np.abs(res[name][1] - V_ref)))
         out["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "builds/s",
                                "cores": os.cpu_count(), "kind": "port",
                                "sample": "one whole build of the same molecule"}

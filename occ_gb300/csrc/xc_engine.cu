@@ -118,6 +118,7 @@ Molecule::~Molecule() {
     cudaFree(p);
   free_mixed(mixed);
   free_grad_mixed(gmixed);
+  free_meta_mixed(mmixed);
 }
 
 void *Molecule::alloc(size_t bytes) {
@@ -254,7 +255,9 @@ void Molecule::ensure_fp64_ws() {
 }
 
 void Molecule::prepare(int precision) {
-  if (precision == OCC_XC_MIXED)
+  if (precision == OCC_XC_MIXED && deriv == 2)
+    prepare_mgga_mixed();
+  else if (precision == OCC_XC_MIXED)
     ensure_mixed_ws();
   else
     ensure_fp64_ws();
@@ -493,6 +496,8 @@ void Molecule::release_device() {
   nlc.reset();
   free_grad_mixed(gmixed);
   gmixed = nullptr;
+  free_meta_mixed(mmixed);
+  mmixed = nullptr;
 }
 
 // Device bytes that materialise() allocates -- the resident state, without the

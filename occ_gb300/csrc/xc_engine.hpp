@@ -117,6 +117,8 @@ struct WsMaps {
 struct MixedState; // device state of the mixed-precision path (xc_mixed.cu)
 struct GradMixed;  // the tensor-core XC gradient's workspace and plan (xc_mixed.cu)
 void free_grad_mixed(GradMixed *g);
+struct MetaMixed;  // the tensor-core meta-GGA build's workspace and plan (xc_mixed.cu)
+void free_meta_mixed(MetaMixed *g);
 
 // Default cap of the XC gradient's workspace per leaf group (bytes).
 constexpr size_t kGradWsCapDefault = size_t(8) << 30;
@@ -189,6 +191,7 @@ struct Molecule {
   // molecule, its sorted -> grid-order map and the pair kernel's buffers
   std::unique_ptr<Molecule> nlc;
   GradMixed *gmixed = nullptr;
+  MetaMixed *mmixed = nullptr;
   int *d_nlc_perm = nullptr;
   void *d_nlc_pts = nullptr, *d_nlc_pts32 = nullptr;
   double *d_nlc_fuw = nullptr, *d_nlc_epart = nullptr;
@@ -217,6 +220,9 @@ struct Molecule {
   void build_fp64(const double *dD, double *dV, double *dout2, cudaStream_t st,
                   double *ws = nullptr, bool ws_holds_ao = false);
   void build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st);
+  // the meta-GGA build with its tau contractions on the tensor cores
+  void prepare_mgga_mixed();
+  void build_mixed_mgga(const double *dD, double *dV, double *dout2, cudaStream_t st);
   void prepare_gradient();
   void prepare_uks();
   void prepare_gradient_mixed();

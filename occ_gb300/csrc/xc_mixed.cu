@@ -717,10 +717,14 @@ __device__ __forceinline__ bool bar_all(int id, int n, bool v) {
   return r != 0;
 }
 
-template <bool DERIV>
+// TAU (meta-GGA): the same GEMM with the A slices of d_k phi (k = tk, built
+// by k_meta_ops at plane kPlaneTauA + 3 (tk - 1)), contracted with d_k phi:
+// sum_j d_k phi_j (d_k phi D2)_j into rho component 3 + tk.
+constexpr int kPlaneTauA = 11;
+template <bool DERIV, bool TAU = false>
 __global__ void __launch_bounds__(kRhoThreads, 1)
     k_rho_mixed(const MixTab *__restrict__ tabs, const MBlock *__restrict__ blocks,
-                const int *__restrict__ order, int nblocks, int *queue, int *err) {
+                const int *__restrict__ order, int nblocks, int *queue, int *err, int tk = 0) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
   RhoSmem *sm = reinterpret_cast<RhoSmem *>(smem + kRhoStages * kRhoStage);
@@ -792,8 +796,9 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
           break;
         const MBlock B = blocks[bi];
         const MixTab &T = tabs[B.mol];
+        const int aplane = TAU ? kPlaneTauA + 3 * (tk - 1) : kPlaneASlices;
         const uint8_t *as = reinterpret_cast<const uint8_t *>(
-            T.ws + B.ws_off + static_cast<size_t>(kPlaneASlices) * B.mp * kBlockPts);
+            T.ws + B.ws_off + static_cast<size_t>(aplane) * B.mp * kBlockPts);
         for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN)
           for (int k0 = 0; k0 < B.mp && ok; k0 += kExactKSeg)
             for (int c = 0; c < seg_chunks(B.mp, k0); c++, g++) {
@@ -938,8 +943,8 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
         break;
       const MBlock B = blocks[bi];
       const MixTab &T = tabs[B.mol];
-      const float *phi = T.ws + B.ws_off;
       const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+      const float *phi = T.ws + B.ws_off + (TAU ? tk * plane : 0);
       float acc[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
       for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN) {
         const int N = min(kRhoN, B.mp - n0);
@@ -964,7 +969,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
               // rho (the energy's direct input) with compensation; its
               // gradient, which enters through sigma, by plain FP32 FMAs
               dot2_step(phi[o], x, acc[0], cmp[0]);
-              if (DERIV) {
+              if (DERIV && !TAU) {
                 acc[1] = fmaf(phi[plane + o], x, acc[1]);
                 acc[2] = fmaf(phi[2 * plane + o], x, acc[2]);
                 acc[3] = fmaf(phi[3 * plane + o], x, acc[3]);
@@ -978,6 +983,10 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
       if (ok && p < B.cnt) {
         const size_t idx = static_cast<size_t>(T.m.leaves[B.leaf].off) + B.p0 + p;
         const size_t Np = static_cast<size_t>(T.m.npts);
+        if (TAU) {
+          T.rho[(3 + tk) * Np + idx] = static_cast<double>(acc[0]) + static_cast<double>(cmp[0]);
+          continue;
+        }
         T.rho[idx] = static_cast<double>(acc[0]) + static_cast<double>(cmp[0]);
         if (DERIV)
           for (int c = 1; c < 4; c++)
@@ -1528,6 +1537,9 @@ void set_smem_attributes() {
                                   kRhoSmem), "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_rho_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kRhoSmem), "cudaFuncSetAttribute");
+  cuda_check(cudaFuncSetAttribute(k_rho_mixed<true, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kRhoSmem),
+             "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_vxc_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kVxcSmem), "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_selftest_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1636,10 +1648,11 @@ template <typename T> T *plan_upload(LaunchPlan &P, const std::vector<T> &v) {
 // running at the same time come from distant parts of the Morton order (and of
 // the batch) and update different V_xc elements.
 void make_plan_lists(LaunchPlan &P, const std::vector<Molecule *> &mols,
-                     const std::vector<MixTab> &tabs) {
+                     const std::vector<MixTab> &tabs, bool meta_plan = false) {
   P.tabs = tabs;
   P.deriv = mols.empty() ? 0 : mols[0]->deriv;
-  require_not_mgga(P.deriv, "mixed precision");
+  if (!meta_plan)
+    require_not_mgga(P.deriv, "batched mixed precision");
   std::vector<VItem> items;
   for (size_t mi = 0; mi < mols.size(); mi++) {
     Molecule &M = *mols[mi];
@@ -1884,6 +1897,10 @@ void Molecule::ensure_mixed_ws() {
 }
 
 void Molecule::build_mixed(const double *dD, double *dV, double *dout2, cudaStream_t st) {
+  if (deriv == 2) {
+    build_mixed_mgga(dD, dV, dout2, st);
+    return;
+  }
   ensure_mixed_ws();
   run_plan(*mixed->single, *ctx, Override{dD, dV, dout2}, mixed->d_err, st,
            ctas > 0 ? ctas : ctx->max_ctas);
@@ -2970,6 +2987,209 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
   cuda_check(cudaGetLastError(), "kernel launch");
   if (P.ao_cacheable)
     P.ao_valid = true;
+}
+
+} // namespace occx
+
+// ---- meta-GGA build on the tensor cores -----------------------------------
+// compute_K_dft<2, Restricted> (include/occ/dft/dft.h:192-388) with
+//   tau = 0.5 sum_k (d_k phi) D2 (d_k phi)          (src/gto/density.cpp:84-96)
+//   V  += sum_k (d_k phi)^T diag(0.5 w vtau) (d_k phi)
+//                                        (src/dft/xc_potential_matrix.cpp:43-56)
+// The blocks carry, beside the build's eleven planes, the exact-split A
+// slices of d_k phi (three per k, planes 11-19: the A operand of
+// k_rho_mixed's tau mode), the hi and lo TF32 planes of d_k phi (20-25) and
+// of c_tau d_k phi with c_tau = 0.25 w vtau (26-31).  The tau term of V is the
+// V_xc kernel's K with operand pairs (d_k phi, c_tau d_k phi), accumulated
+// into the same A that k_symmetrize turns into A + A^T.  The functional is the
+// FP64 meta-GGA evaluator (the tau GEMMs, not it, bound the build).
+namespace occx {
+
+constexpr int kPlanesMeta = 32;
+constexpr int kPlaneMetaDphi = 20; // hi, lo of d_k phi: planes 20 + 2(k-1), 21 + 2(k-1)
+constexpr int kPlaneMetaY = 26;    // hi, lo of c_tau d_k phi: planes 26 + 2(k-1), 27 + 2(k-1)
+
+struct MetaMixed {
+  char *ws = nullptr;
+  size_t bytes = 0;
+  LaunchPlan plan;
+};
+
+void free_meta_mixed(MetaMixed *g) { delete g; }
+
+namespace {
+
+// Per block (one thread per point), after k_colloc_f32: for k = x, y, z the
+// hi / lo planes of d_k phi and its A slices on the exact grid of the point's
+// own power-of-two bound.
+__global__ void __launch_bounds__(kBlockPts) k_meta_ops(const MixTab *__restrict__ tabs,
+                                                        const MBlock *__restrict__ blocks) {
+  const MBlock B = blocks[blockIdx.x];
+  const MixTab &T = tabs[B.mol];
+  const int p = threadIdx.x;
+  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+  float *base = T.ws + B.ws_off;
+  for (int k = 1; k <= 3; k++) {
+    const float *g = base + k * plane;
+    float vmax = 0.f;
+    for (int f = 0; f < B.mp; f++) {
+      const size_t o = static_cast<size_t>(f) * kBlockPts + p;
+      const float v = g[o];
+      vmax = fmaxf(vmax, fabsf(v));
+      float h, l;
+      tf32_split(v, h, l);
+      base[(kPlaneMetaDphi + 2 * (k - 1)) * plane + o] = h;
+      base[(kPlaneMetaDphi + 2 * (k - 1) + 1) * plane + o] = l;
+    }
+    const float sA = pow2_bound(vmax), isA = 1.f / sA;
+    uint8_t *as = reinterpret_cast<uint8_t *>(base + (kPlaneTauA + 3 * (k - 1)) * plane);
+    for (int c = 0; c < B.mp / kKc; c++) {
+      uint8_t *tile = as + static_cast<size_t>(c) * kRhoStageA;
+#pragma unroll 2
+      for (int q = 0; q < kKc / 4; q++) {
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++)
+          v[e] = g[static_cast<size_t>(c * kKc + q * 4 + e) * kBlockPts + p];
+        store4_exact(tile, tile + 16384, tile + 32768, p, q, v, sA, isA);
+      }
+    }
+  }
+}
+
+// The meta-GGA functional per leaf (FP64), then per block the GGA operand Y
+// (ymix_block) and the tau term's operands c_tau d_k phi (hi, lo).
+__global__ void __launch_bounds__(256, 2) k_func_b_mgga(const MixTab *__restrict__ tabs,
+                                                        const MBlock *__restrict__ blocks,
+                                                        const LeafItem *__restrict__ litems) {
+  __shared__ double sh[8];
+  __shared__ float4 cf[kBlockPts];
+  __shared__ float ct[kBlockPts];
+  const LeafItem li = litems[blockIdx.x];
+  const MixTab &T = tabs[li.mol];
+  leaf_functional_mgga(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts), T.fs,
+                       T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
+  __syncthreads(); // the leaf's coefficients are written
+  const size_t N = static_cast<size_t>(T.m.npts);
+  for (int b = 0; b < li.nblk; b++) {
+    const MBlock B = blocks[li.block0 + b];
+    ymix_block<true>(T, B, cf);
+    if (threadIdx.x < kBlockPts) {
+      const int p = threadIdx.x;
+      const size_t idx = static_cast<size_t>(T.m.leaves[B.leaf].off) + B.p0 + p;
+      ct[p] = p < B.cnt ? static_cast<float>(T.coef[4 * N + idx]) : 0.f;
+    }
+    __syncthreads();
+    float *base = T.ws + B.ws_off;
+    const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+    const int n = B.mp * kBlockPts;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+      const float c = ct[q % kBlockPts];
+#pragma unroll
+      for (int k = 1; k <= 3; k++) {
+        float h, l;
+        tf32_split(base[k * plane + q] * c, h, l);
+        base[(kPlaneMetaY + 2 * (k - 1)) * plane + q] = h;
+        base[(kPlaneMetaY + 2 * (k - 1) + 1) * plane + q] = l;
+      }
+    }
+    __syncthreads(); // ct is reused by the next block
+  }
+}
+
+} // namespace
+
+void Molecule::prepare_mgga_mixed() {
+  if (mmixed)
+    return;
+  if (!mixed)
+    throw ArgError("the molecule has no device state");
+  auto g = std::make_unique<MetaMixed>();
+  const WsLayout Lw = ws_layout(*this, kPlanesMeta);
+  g->bytes = Lw.total;
+  g->ws = static_cast<char *>(alloc(g->bytes));
+  LaunchPlan &P = g->plan;
+  make_plan_lists(P, {this}, {bind_ws(*this, g->ws, g->ws, kPlanesMeta)}, true);
+  long long off = 0; // the blocks' offsets for 32 planes (same order as prepare_mixed)
+  for (MBlock &B : P.blocks) {
+    B.ws_off = off;
+    off += static_cast<long long>(kPlanesMeta) * B.mp * kBlockPts;
+  }
+  P.d_blocks = plan_upload(P, P.blocks);
+  P.d_order = plan_upload(P, P.order);
+  P.d_queue = plan_upload(P, std::vector<int>(2, 0));
+  P.d_items = plan_upload(P, P.items);
+  P.d_litems = plan_upload(P, P.litems);
+  P.d_tabs = plan_upload(P, P.tabs);
+  encode_ws_map(P.tmap, g->ws, g->bytes);
+  P.ao_cacheable = true;
+  mmixed = g.release();
+}
+
+void Molecule::build_mixed_mgga(const double *dD, double *dV, double *dout2, cudaStream_t st) {
+  prepare_mgga_mixed();
+  LaunchPlan &P = mmixed->plan;
+  Context &c = *ctx;
+  int *err = mixed->d_err;
+  const int nb = static_cast<int>(P.blocks.size());
+  const int ni = static_cast<int>(P.items.size());
+  const int nl = static_cast<int>(P.litems.size());
+  const int sms = this->ctas > 0 ? this->ctas
+                                 : (ctx->max_ctas > 0 ? ctx->max_ctas : num_sms(device));
+  Override ov{dD, dV, dout2};
+  c.launch("prep_density", st, [&] {
+    k_prep_density<<<dim3(P.maxnbf, 1), 256, 0, st>>>(P.d_tabs, ov, P.d_queue);
+  });
+  if (nb > 0) {
+    if (!P.ao_valid) {
+      c.launch("colloc_f32", st, [&] {
+        k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+      c.launch("meta_ops", st, [&] {
+        k_meta_ops<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+    }
+    const int gg = std::min(nb, sms);
+    c.launch("rho_mixed", st, [&] {
+      k_rho_mixed<true><<<gg, kRhoThreads, kRhoSmem, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
+                                                     P.d_queue, err);
+    });
+    for (int k = 1; k <= 3; k++) {
+      cuda_check(cudaMemsetAsync(P.d_queue, 0, sizeof(int), st), "cudaMemsetAsync");
+      c.launch("tau_mixed", st, [&] {
+        k_rho_mixed<true, true><<<gg, kRhoThreads, kRhoSmem, st>>>(
+            P.d_tabs, P.d_blocks, P.d_order, nb, P.d_queue, err, k);
+      });
+    }
+  }
+  if (nl > 0)
+    c.launch("func", st, [&] {
+      k_func_b_mgga<<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+    });
+  if (ni > 0) {
+    const VxcPlanes pls[3] = {
+        kVxcBuildPlanes,
+        {kPlaneMetaDphi, kPlaneMetaDphi + 1, kPlaneMetaY, kPlaneMetaY + 1, kPlaneMetaDphi + 2,
+         kPlaneMetaDphi + 3, kPlaneMetaY + 2, kPlaneMetaY + 3, 2},
+        {kPlaneMetaDphi + 4, kPlaneMetaDphi + 5, kPlaneMetaY + 4, kPlaneMetaY + 5, 0, 0, 0, 0, 1}};
+    for (int v = 0; v < 3; v++) {
+      if (v > 0)
+        cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
+      c.launch(v == 0 ? "vxc_mixed" : "vxc_tau_mixed", st, [&] {
+        k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+            P.d_tabs, P.d_blocks, P.d_items, ni, ov, P.d_queue, err, P.tmap.rows32,
+            P.tmap.rows128, pls[v]);
+      });
+    }
+  }
+  c.launch("symmetrize", st, [&] {
+    const size_t n2 = static_cast<size_t>(P.maxnbf) * P.maxnbf;
+    const int gx = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
+    k_symmetrize<<<dim3(std::max(gx, 1), 1), 256, 0, st>>>(P.d_tabs, ov);
+  });
+  c.launch("reduce", st, [&] { k_reduce_b<<<1, 256, 0, st>>>(P.d_tabs, ov); });
+  cuda_check(cudaGetLastError(), "kernel launch");
+  P.ao_valid = true;
 }
 
 } // namespace occx
