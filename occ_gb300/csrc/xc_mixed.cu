@@ -2501,8 +2501,54 @@ __global__ void k_selftest_func(FuncSet fs, int n, const double *rho, const doub
   outm[3 * i + 1] = vr;
   outm[3 * i + 2] = vs;
 }
+__global__ void k_selftest_mgga(FuncSet fs, int n, const double *rho, const double *sigma,
+                                const double *tau, double *out64) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  double e, vr, vs, vt;
+  eval_xc_mgga(fs, rho[i], sigma[i], tau[i], e, vr, vs, vt);
+  out64[4 * i] = e;
+  out64[4 * i + 1] = vr;
+  out64[4 * i + 2] = vs;
+  out64[4 * i + 3] = vt;
+}
 } // namespace
 } // namespace occx
+
+// The meta-GGA evaluator (FP64, the one both precisions' builds use) at n
+// points (host arrays; out64 receives e, vrho, vsigma, vtau per point), for
+// testing.
+extern "C" int occ_xc_selftest_functional_mgga(occ_xc_context *ctx, const char *method, int n,
+                                               const double *rho, const double *sigma,
+                                               const double *tau, double *out64) {
+  if (!ctx || !method || n <= 0 || !rho || !sigma || !tau || !out64)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return api_guard(ctx, [&] {
+    const FuncSet fs = parse_method(method);
+    cudaStream_t st = ctx->impl->stream;
+    double *d = nullptr;
+    const size_t bytes = static_cast<size_t>(n) * 7 * sizeof(double);
+    cuda_check(cudaMalloc(&d, bytes), "cudaMalloc");
+    try {
+      const double *src[3] = {rho, sigma, tau};
+      for (int k = 0; k < 3; k++)
+        cuda_check(cudaMemcpyAsync(d + k * n, src[k], n * sizeof(double), cudaMemcpyHostToDevice,
+                                   st),
+                   "H2D");
+      k_selftest_mgga<<<(n + 127) / 128, 128, 0, st>>>(fs, n, d, d + n, d + 2 * n, d + 3 * n);
+      cuda_check(cudaGetLastError(), "kernel launch");
+      cuda_check(cudaMemcpyAsync(out64, d + 3 * n, 4 * n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, st), "D2H");
+      cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    } catch (...) {
+      cudaFree(d);
+      throw;
+    }
+    cudaFree(d);
+  });
+}
 
 // The FP64 and the mixed-path functional evaluators at n points (host
 // arrays; out64 / outm receive e, vrho, vsigma per point), for testing.
@@ -3001,8 +3047,12 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
 // k_rho_mixed's tau mode), the hi and lo TF32 planes of d_k phi (20-25) and
 // of c_tau d_k phi with c_tau = 0.25 w vtau (26-31).  The tau term of V is the
 // V_xc kernel's K with operand pairs (d_k phi, c_tau d_k phi), accumulated
-// into the same A that k_symmetrize turns into A + A^T.  The functional is the
-// FP64 meta-GGA evaluator (the tau GEMMs, not it, bound the build).
+// into the same A that k_symmetrize turns into A + A^T.  The functional is
+// the FP64 meta-GGA evaluator, fused with the operand planes (two CTAs an SM:
+// one's FP64 functional overlaps the other's HBM-bound planes).  Measured
+// alternatives: a double-float (FP32-pipe) TPSS needed 255 registers a thread
+// and ran slower (5.7 against 4.7 ms for the stage), and so did the functional
+// and the planes as two kernels (2.95 + 2.17 ms).
 namespace occx {
 
 constexpr int kPlanesMeta = 32;

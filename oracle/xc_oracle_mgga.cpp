@@ -14,8 +14,9 @@
 // tau_a = tau_b = tau / 2.  Neither depends on the laplacian.
 //
 // Derivatives by the complex step (W. Squire, G. Trapp, SIAM Review 40, 110
-// (1998)): f'(x) = Im f(x + i h) / h with h = 1e-30 is exact to rounding for
-// the analytic pieces; max() and the thresholds select by the real part.
+// (1998)): f'(x) = Im f(x + i h) / h with h = 1e-25 |x| (a step relative to
+// the argument: sigma can be 1e-40) is exact to rounding for the analytic
+// pieces; max() and the thresholds select by the real part.
 // This is independent of the dual numbers the GPU functional uses.
 //
 // Thresholds (not pinned against Libxc): the point is zero below a total
@@ -144,7 +145,8 @@ cd mgga_component(int id, cd ra, cd rb, cd saa, cd sab, cd sbb, cd ta, cd tb) {
   return 0.0;
 }
 
-constexpr double kH = 1e-30;
+constexpr double kH = 1e-25; // relative complex step
+inline double step(double x) { return kH * std::fmax(std::fabs(x), 1e-280); }
 
 } // namespace
 
@@ -167,13 +169,14 @@ extern "C" int oracle_functional_mgga(int id, long n, const double *rho, const d
     auto f = [&](cd R, cd S, cd T) {
       return mgga_component(id, 0.5 * R, 0.5 * R, 0.25 * S, 0.25 * S, 0.25 * S, 0.5 * T, 0.5 * T);
     };
-    const cd fr = f(cd(r, kH), s, t);
-    const cd fs = f(r, cd(s, kH), t);
-    const cd ft = f(r, s, cd(t, kH));
+    const double hr = step(r), hs = step(s), ht = step(t);
+    const cd fr = f(cd(r, hr), s, t);
+    const cd fs = f(r, cd(s, hs), t);
+    const cd ft = f(r, s, cd(t, ht));
     exc[i] = fr.real() / r;
-    vrho[i] = fr.imag() / kH;
-    vsigma[i] = fs.imag() / kH;
-    vtau[i] = ft.imag() / kH;
+    vrho[i] = fr.imag() / hr;
+    vsigma[i] = fs.imag() / hs;
+    vtau[i] = ft.imag() / ht;
   }
   return 0;
 }
@@ -207,12 +210,13 @@ extern "C" int oracle_functional_mgga_polarized(int id, long n, const double *ra
     double d[7];
     double e = 0.0;
     for (int k = 0; k < 7; k++) {
+      const double h = step(x[k]);
       cd y[7];
       for (int j = 0; j < 7; j++)
-        y[j] = cd(x[j], j == k ? kH : 0.0);
+        y[j] = cd(x[j], j == k ? h : 0.0);
       const cd v = mgga_component(id, y[0], y[1], y[2], y[3], y[4], y[5], y[6]);
       e = v.real();
-      d[k] = v.imag() / kH;
+      d[k] = v.imag() / h;
     }
     exc[i] = e / nt;
     vr[2 * i] = d[0];
