@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include "functionals.cuh"
+#include "functionals_pol.cuh"
 
 namespace occx {
 
@@ -38,7 +39,8 @@ namespace fnm {
 struct M3 { // value and d/drho, d/dsigma, d/dtau
   double v, r, s, t;
 };
-__device__ __forceinline__ M3 cst(double v) { return {v, 0.0, 0.0, 0.0}; }
+template <class T> __device__ __forceinline__ T cst(double v);
+template <> __device__ __forceinline__ M3 cst<M3>(double v) { return {v, 0.0, 0.0, 0.0}; }
 __device__ __forceinline__ M3 operator+(M3 a, M3 b) {
   return {a.v + b.v, a.r + b.r, a.s + b.s, a.t + b.t};
 }
@@ -80,6 +82,96 @@ __device__ __forceinline__ M3 mcbrt(M3 a) { // a > 0
 }
 __device__ __forceinline__ M3 mmax(M3 a, M3 b) { return a.v >= b.v ? a : b; }
 
+// ---- the polarised form's dual: d/d rho_a, rho_b, s_aa, s_ab, s_bb, tau_a, tau_b
+constexpr int kN7 = 7;
+struct P7 {
+  double v, d[kN7];
+};
+template <> __device__ __forceinline__ P7 cst<P7>(double v) {
+  P7 r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < kN7; i++)
+    r.d[i] = 0.0;
+  return r;
+}
+__device__ __forceinline__ P7 var7(double v, int k) {
+  P7 r = cst<P7>(v);
+  r.d[k] = 1.0;
+  return r;
+}
+__device__ __forceinline__ P7 operator+(P7 a, P7 b) {
+  P7 r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < kN7; i++)
+    r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+__device__ __forceinline__ P7 operator-(P7 a, P7 b) {
+  P7 r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < kN7; i++)
+    r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+__device__ __forceinline__ P7 operator*(P7 a, P7 b) {
+  P7 r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < kN7; i++)
+    r.d[i] = fma(a.d[i], b.v, a.v * b.d[i]);
+  return r;
+}
+__device__ __forceinline__ P7 operator/(P7 a, P7 b) {
+  const double inv = 1.0 / b.v, q = a.v * inv;
+  P7 r;
+  r.v = q;
+#pragma unroll
+  for (int i = 0; i < kN7; i++)
+    r.d[i] = (a.d[i] - q * b.d[i]) * inv;
+  return r;
+}
+__device__ __forceinline__ P7 operator*(double c, P7 a) {
+  P7 r;
+  r.v = c * a.v;
+#pragma unroll
+  for (int i = 0; i < kN7; i++)
+    r.d[i] = c * a.d[i];
+  return r;
+}
+__device__ __forceinline__ P7 operator+(double c, P7 a) {
+  a.v += c;
+  return a;
+}
+__device__ __forceinline__ P7 operator-(double c, P7 a) { return cst<P7>(c) - a; }
+__device__ __forceinline__ P7 operator/(double c, P7 b) { return cst<P7>(c) / b; }
+__device__ __forceinline__ P7 chain(P7 a, double f, double df) {
+  P7 r;
+  r.v = f;
+#pragma unroll
+  for (int i = 0; i < kN7; i++)
+    r.d[i] = df * a.d[i];
+  return r;
+}
+__device__ __forceinline__ P7 mlog(P7 a) { return chain(a, log(a.v), 1.0 / a.v); }
+__device__ __forceinline__ P7 mexp(P7 a) {
+  const double e = exp(a.v);
+  return chain(a, e, e);
+}
+__device__ __forceinline__ P7 msqrt(P7 a) {
+  const double q = sqrt(a.v);
+  return chain(a, q, 0.5 / q);
+}
+__device__ __forceinline__ P7 mcbrt(P7 a) { // a > 0
+  const double c = cbrt(a.v);
+  return chain(a, c, c / (3.0 * a.v));
+}
+__device__ __forceinline__ P7 mmax(P7 a, P7 b) { return a.v >= b.v ? a : b; }
+// a, or the constant lo where a < lo (Libxc's zeta threshold)
+__device__ __forceinline__ P7 mfloor(P7 a, double lo) { return a.v >= lo ? a : cst<P7>(lo); }
+
 constexpr double kPiM = 3.14159265358979323846;
 constexpr double kK2 = 9.570780000627305;     // (3 pi^2)^(2/3)
 constexpr double kKf = 3.0936677262801355;    // (3 pi^2)^(1/3)
@@ -89,11 +181,11 @@ constexpr double kCbrt2 = 1.2599210498948732; // 2^(1/3)
 // phi(zeta = 1) with 1 - zeta held at DBL_EPSILON: (2^(2/3) + eps^(2/3)) / 2
 constexpr double kPhi1 = 0.79370052600243400;
 
-struct Pow {
-  M3 r13, r43, r53, r83;
+template <class T> struct Pow {
+  T r13, r43, r53, r83;
 };
-__device__ __forceinline__ Pow powers(M3 rho) {
-  Pow P;
+template <class T> __device__ __forceinline__ Pow<T> powers(T rho) {
+  Pow<T> P;
   P.r13 = mcbrt(rho);
   P.r43 = rho * P.r13;
   P.r53 = P.r43 * P.r13;
@@ -101,20 +193,22 @@ __device__ __forceinline__ Pow powers(M3 rho) {
   return P;
 }
 
-__device__ __forceinline__ M3 tpss_x(M3 rho, M3 sigma, M3 tau, const Pow &P) {
+template <class T>
+__device__ __forceinline__ T tpss_x(T rho, T sigma, T tau, const Pow<T> &P) {
+  using M3 = T;
   const double kappa = 0.804, b = 0.40, c = 1.59096, e = 1.537, mu = 0.21951;
   const double se = 1.2397580409095962; // sqrt(e)
   M3 p = sigma / ((4.0 * kK2) * P.r83);
   M3 tw = sigma / (8.0 * rho);
   M3 z = tw / tau;
   M3 alpha = (tau - tw) / ((0.3 * kK2) * P.r53);
-  M3 am1 = alpha - cst(1.0);
+  M3 am1 = alpha - cst<T>(1.0);
   M3 qb = 0.45 * am1 / msqrt(1.0 + b * alpha * am1) + (2.0 / 3.0) * p;
   M3 z2 = z * z;
   M3 opz2 = 1.0 + z2;
   M3 tz2 = 0.36 * z2; // (3 z / 5)^2
   M3 p2 = p * p;
-  M3 num = (cst(10.0 / 81.0) + c * z2 / (opz2 * opz2)) * p + (146.0 / 2025.0) * qb * qb -
+  M3 num = (cst<T>(10.0 / 81.0) + c * z2 / (opz2 * opz2)) * p + (146.0 / 2025.0) * qb * qb -
            (73.0 / 405.0) * qb * msqrt(0.5 * tz2 + 0.5 * p2) +
            ((1.0 / kappa) * (10.0 / 81.0) * (10.0 / 81.0)) * p2 +
            (2.0 * se * (10.0 / 81.0)) * tz2 + (e * mu) * p2 * p;
@@ -125,8 +219,10 @@ __device__ __forceinline__ M3 tpss_x(M3 rho, M3 sigma, M3 tau, const Pow &P) {
 }
 
 // PW92 G(rs) of one fit
-__device__ __forceinline__ M3 pw_g(M3 rs, double A, double a1, double b1, double b2, double b3,
-                                   double b4) {
+template <class T>
+__device__ __forceinline__ T pw_g(T rs, double A, double a1, double b1, double b2, double b3,
+                                  double b4) {
+  using M3 = T;
   M3 srs = msqrt(rs);
   M3 den = 2.0 * A * (b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs);
   return (-2.0 * A) * (1.0 + a1 * rs) * mlog(1.0 + 1.0 / den);
@@ -139,12 +235,12 @@ __device__ __forceinline__ M3 pbe_h(M3 eps, double phi, M3 kf, M3 n, M3 sig) {
   const double phi3 = phi * phi * phi;
   M3 ks2 = (4.0 / kPiM) * kf;
   M3 t2 = sig / ((4.0 * phi * phi) * ks2 * n * n);
-  M3 A = (beta / gamma) / (mexp((-1.0 / (gamma * phi3)) * eps) - cst(1.0));
+  M3 A = (beta / gamma) / (mexp((-1.0 / (gamma * phi3)) * eps) - cst<M3>(1.0));
   M3 At2 = A * t2;
   return (gamma * phi3) * mlog(1.0 + (beta / gamma) * t2 * (1.0 + At2) / (1.0 + At2 + At2 * At2));
 }
 
-__device__ __forceinline__ M3 tpss_c(M3 rho, M3 sigma, M3 tau, const Pow &P) {
+__device__ __forceinline__ M3 tpss_c(M3 rho, M3 sigma, M3 tau, const Pow<M3> &P) {
   // unpolarised PBE
   M3 rs = kRs / P.r13;
   M3 e0 = pw_g(rs, 0.0310907, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294);
@@ -160,6 +256,71 @@ __device__ __forceinline__ M3 tpss_c(M3 rho, M3 sigma, M3 tau, const Pow &P) {
   M3 z2 = z * z;
   M3 erev = epbe * (1.0 + 0.53 * z2) - 1.53 * z2 * et;
   return rho * erev * (1.0 + 2.8 * erev * z2 * z);
+}
+
+// ---- spin-polarised TPSS (the UKS build), over P7
+// PBE correlation per particle of spin densities (ra, rb) with total
+// |grad rho|^2 = sig: PW92's spin interpolation and phi(zeta)
+__device__ __forceinline__ P7 pbe_eps_pol(P7 ra, P7 rb, P7 sig) {
+  const double beta = 0.06672455060314922, gamma = 0.031090690869654897;
+  const double fpp0 = 1.7099209341613657, eps_z = 2.220446049250313e-16;
+  P7 n = ra + rb;
+  P7 z = (ra - rb) / n;
+  P7 opz = mfloor(1.0 + z, eps_z), omz = mfloor(1.0 - z, eps_z);
+  P7 n13 = mcbrt(n);
+  P7 rs = kRs / n13;
+  P7 e0 = pw_g(rs, 0.0310907, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294);
+  P7 e1 = pw_g(rs, 0.01554535, 0.20548, 14.1189, 6.1977, 3.3662, 0.62517);
+  P7 ac = cst<P7>(0.0) - pw_g(rs, 0.0168869, 0.11125, 10.357, 3.6231, 0.88026, 0.49671);
+  P7 o13 = mcbrt(opz), m13 = mcbrt(omz);
+  P7 f = (1.0 / 0.5198420997897464) * (opz * o13 + omz * m13 - cst<P7>(2.0));
+  P7 z2 = z * z, z4 = z2 * z2;
+  P7 eps = e0 + (1.0 / fpp0) * ac * f * (1.0 - z4) + (e1 - e0) * f * z4;
+  P7 phi = 0.5 * (o13 * o13 + m13 * m13);
+  P7 phi3 = phi * phi * phi;
+  P7 ks2 = (4.0 / kPiM) * (kKf * n13);
+  P7 t2 = sig / (4.0 * phi * phi * ks2 * n * n);
+  P7 A = (beta / gamma) / (mexp(cst<P7>(0.0) - eps / (gamma * phi3)) - cst<P7>(1.0));
+  P7 At2 = A * t2;
+  P7 H = gamma * phi3 * mlog(1.0 + (beta / gamma) * t2 * (1.0 + At2) / (1.0 + At2 + At2 * At2));
+  return eps + H;
+}
+
+// TPSS exchange of one spin channel: E_x[2 rho_s, 4 s_ss, 2 tau_s] / 2
+__device__ __forceinline__ P7 tpss_x_s(P7 r, P7 s, P7 t) {
+  const P7 n = 2.0 * r;
+  return 0.5 * tpss_x(n, 4.0 * s, 2.0 * t, powers(n));
+}
+
+// revPKZB / TPSS correlation (eqs. 11-14) of a polarised density
+__device__ __forceinline__ P7 tpss_c_pol(P7 ra, P7 rb, P7 saa, P7 sab, P7 sbb, P7 ta, P7 tb,
+                                         bool sa, bool sb) {
+  const double eps_z = 2.220446049250313e-16;
+  P7 n = ra + rb;
+  P7 sig = saa + 2.0 * sab + sbb;
+  P7 tau = ta + tb;
+  P7 z = sig / (8.0 * n * tau);
+  P7 zeta = (ra - rb) / n;
+  P7 opz = mfloor(1.0 + zeta, eps_z), omz = mfloor(1.0 - zeta, eps_z);
+  P7 n2 = n * n;
+  P7 gz2 = 4.0 * (rb * rb * saa - 2.0 * ra * rb * sab + ra * ra * sbb) / (n2 * n2);
+  P7 n13 = mcbrt(n);
+  P7 xi2 = gz2 / ((4.0 * kKf * kKf) * n13 * n13);
+  P7 zt2 = zeta * zeta;
+  P7 C0 = 0.53 + zt2 * (0.87 + zt2 * (0.50 + 2.26 * zt2));
+  P7 o13 = mcbrt(opz), m13 = mcbrt(omz);
+  P7 g = 1.0 + 0.5 * xi2 * (1.0 / (opz * o13) + 1.0 / (omz * m13));
+  P7 g2 = g * g;
+  P7 C = C0 / (g2 * g2);
+  P7 epbe = pbe_eps_pol(ra, rb, sig);
+  P7 sum = cst<P7>(0.0);
+  if (sa)
+    sum = sum + ra / n * mmax(pbe_eps_pol(ra, cst<P7>(0.0), saa), epbe);
+  if (sb)
+    sum = sum + rb / n * mmax(pbe_eps_pol(rb, cst<P7>(0.0), sbb), epbe);
+  P7 z2 = z * z;
+  P7 erev = epbe * (1.0 + C * z2) - (1.0 + C) * z2 * sum;
+  return n * erev * (1.0 + 2.8 * erev * z2 * z);
 }
 
 } // namespace fnm
@@ -178,7 +339,7 @@ __device__ __forceinline__ void eval_xc_mgga(const FuncSet &fs, double rho, doub
   const double tm = fmax(tau, 1e-20);
   const double sm = fmin(sg, 8.0 * rho * tm);
   fnm::M3 r{rho, 1.0, 0.0, 0.0}, s{sm, 0.0, 1.0, 0.0}, t{tm, 0.0, 0.0, 1.0};
-  const fnm::Pow P = fnm::powers(r);
+  const fnm::Pow<fnm::M3> P = fnm::powers(r);
   fn::D3 r3{rho, 1.0, 0.0}, s3{sg, 0.0, 1.0};
   fn::RhoPowers<fn::D3> P3 = fn::rho_powers(r3);
   for (int i = 0; i < fs.n; i++) {
@@ -197,6 +358,54 @@ __device__ __forceinline__ void eval_xc_mgga(const FuncSet &fs, double rho, doub
       vsigma += c * v.s;
     }
   }
+}
+
+// One point of a polarised meta-GGA method: e and vrho[2], vsigma[3],
+// vtau[2].  Meta-GGA components on the clamped arguments Libxc uses (tau_s >=
+// 1e-20, s_ss <= 8 rho_s tau_s, |s_ab| <= (s_aa + s_bb) / 2), the method's
+// LDA / GGA components through eval_xc_pol on the arguments as given.
+__device__ __forceinline__ void eval_xc_mgga_pol(const FuncSet &fs, double ra, double rb,
+                                                 double saa, double sab, double sbb, double ta,
+                                                 double tb, double &e, double *vrho,
+                                                 double *vsig, double *vtau) {
+  eval_xc_pol(fs, ra, rb, saa, sab, sbb, e, vrho, vsig); // its switch skips meta-GGA ids
+  vtau[0] = vtau[1] = 0.0;
+  ra = fmax(ra, 0.0);
+  rb = fmax(rb, 0.0);
+  if (!(ra + rb >= 1e-15))
+    return;
+  ta = fmax(ta, 1e-20);
+  tb = fmax(tb, 1e-20);
+  saa = fmin(fmax(saa, 1e-40), 8.0 * ra * ta);
+  sbb = fmin(fmax(sbb, 1e-40), 8.0 * rb * tb);
+  const double lim = 0.5 * (saa + sbb);
+  sab = fmin(fmax(sab, -lim), lim);
+  using fnm::P7;
+  const P7 Ra = fnm::var7(ra, 0), Rb = fnm::var7(rb, 1), Saa = fnm::var7(saa, 2),
+           Sab = fnm::var7(sab, 3), Sbb = fnm::var7(sbb, 4), Ta = fnm::var7(ta, 5),
+           Tb = fnm::var7(tb, 6);
+  const bool sa = ra >= 1e-15, sb = rb >= 1e-15;
+  P7 tot = fnm::cst<P7>(0.0);
+  for (int i = 0; i < fs.n; i++) {
+    if (fs.id[i] == kMggaXTpss) {
+      P7 x = fnm::cst<P7>(0.0);
+      if (sa)
+        x = x + fnm::tpss_x_s(Ra, Saa, Ta);
+      if (sb)
+        x = x + fnm::tpss_x_s(Rb, Sbb, Tb);
+      tot = tot + fs.coef[i] * x;
+    } else if (fs.id[i] == kMggaCTpss) {
+      tot = tot + fs.coef[i] * fnm::tpss_c_pol(Ra, Rb, Saa, Sab, Sbb, Ta, Tb, sa, sb);
+    }
+  }
+  e += tot.v;
+  vrho[0] += tot.d[0];
+  vrho[1] += tot.d[1];
+  vsig[0] += tot.d[2];
+  vsig[1] += tot.d[3];
+  vsig[2] += tot.d[4];
+  vtau[0] = tot.d[5];
+  vtau[1] = tot.d[6];
 }
 
 } // namespace occx

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(128) k_colloc_f64(MolDev m, double *__restrict
 // p0 + tx + 16 i, AOs j0 + ty + 16 jj.
 // TAU (meta-GGA, grid.y = 3): the same GEMM on the derivative plane
 // k = 1 + blockIdx.y, (d_k phi) D2 (d_k phi) into rho component 4 + blockIdx.y
-// (tau = half their sum, src/gto/density.cpp:84-96).
+// (tau = half their sum, src/gto/density.cpp:86-100).
 template <bool DERIV, bool TAU = false>
 __global__ void __launch_bounds__(256) k_rho_f64(MolDev m, const double *__restrict__ D,
                                                  const double *__restrict__ ws,
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(256) k_func_mgga(MolDev m, FuncSet fs, double 
 // Thread (tx, ty): K rows i0 + ty + 16 a, columns j0 + tx + 16 b.
 // META adds sum_k (d_k phi_I)^T diag(c_tau) (d_k phi_J) with c_tau =
 // 0.25 w vtau (coefficient component 4), so that K + K^T carries the
-// tau term of src/dft/xc_potential_matrix.cpp:43-56 once.
+// tau term of src/dft/xc_potential_matrix.cpp:43-58 once.
 template <bool DERIV, bool META = false>
 __global__ void __launch_bounds__(256) k_vxc_f64(MolDev m, const double *__restrict__ ws,
                                                  const double *__restrict__ coef,

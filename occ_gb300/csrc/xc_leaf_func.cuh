@@ -91,9 +91,9 @@ __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__r
 
 // The meta-GGA functional stage (FP64): rho components 0-3 as for a GGA and
 // 4-6 the three (d_k phi) D2 (d_k phi) sums, tau = half their sum
-// (src/gto/density.cpp:84-96, include/occ/dft/dft_kernels.h:49-58).
+// (src/gto/density.cpp:86-100, include/occ/dft/dft_kernels.h:49-58).
 // Coefficients 0-3 as for a GGA and coef4 = 0.25 w vtau (the V kernel's
-// K + K^T then carries src/dft/xc_potential_matrix.cpp:43-56's 0.5 w vtau).
+// K + K^T then carries src/dft/xc_potential_matrix.cpp:43-58's 0.5 w vtau).
 __device__ __forceinline__ void leaf_functional_mgga(const DevLeaf &L,
                                                      const Pt4 *__restrict__ pts, size_t N,
                                                      const FuncSet &fs, double thr,

@@ -2952,6 +2952,7 @@ __global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
 } // namespace
 
 void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cudaStream_t st) {
+  require_not_mgga(deriv, "the tensor-core unrestricted build");
   ensure_mixed_ws();
   prepare_uks();
   LaunchPlan &P = *mixed->single;
@@ -3039,9 +3040,9 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
 
 // ---- meta-GGA build on the tensor cores -----------------------------------
 // compute_K_dft<2, Restricted> (include/occ/dft/dft.h:192-388) with
-//   tau = 0.5 sum_k (d_k phi) D2 (d_k phi)          (src/gto/density.cpp:84-96)
+//   tau = 0.5 sum_k (d_k phi) D2 (d_k phi)          (src/gto/density.cpp:86-100)
 //   V  += sum_k (d_k phi)^T diag(0.5 w vtau) (d_k phi)
-//                                        (src/dft/xc_potential_matrix.cpp:43-56)
+//                                        (src/dft/xc_potential_matrix.cpp:43-58)
 // The blocks carry, beside the build's eleven planes, the exact-split A
 // slices of d_k phi (three per k, planes 11-19: the A operand of
 // k_rho_mixed's tau mode), the hi and lo TF32 planes of d_k phi (20-25) and

@@ -17,6 +17,7 @@
 // same resident AO values; only the functional stage is new (k_func_pol).
 // The tensor-core form (Molecule::build_mixed_uks, xc_mixed.cu) runs the
 // mixed density and potential kernels once per spin in the same way.
+#include "functionals_mgga.cuh"
 #include "functionals_pol.cuh"
 #include "xc_device.cuh"
 #include "xc_engine.hpp"
@@ -86,6 +87,66 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The meta-GGA form (compute_K_dft<2, Unrestricted>): rho components 4-6 of
+// each spin hold its (d_k phi) D2_s (d_k phi) sums, tau_s = half their sum
+// (src/gto/density.cpp:104-166); coef4 of each spin = 0.25 w vtau_s, so that
+// the V kernel's K + K^T carries xc_potential_matrix.cpp:110-136's 0.5 w vtau_s.
+__global__ void __launch_bounds__(256)
+    k_func_pol_mgga(MolDev m, FuncSet fs, double thr, const double *__restrict__ rho_a,
+                    const double *__restrict__ rho_b, double *__restrict__ coef_a,
+                    double *__restrict__ coef_b, double *__restrict__ epart3) {
+  __shared__ double sh[8];
+  const DevLeaf L = m.leaves[blockIdx.x];
+  const size_t N = static_cast<size_t>(m.npts);
+  double mx = -1e300;
+  for (int p = threadIdx.x; p < L.cnt; p += 256) {
+    const size_t idx = static_cast<size_t>(L.off) + p;
+    mx = fmax(mx, fmax(rho_a[idx], rho_b[idx]));
+  }
+  mx = leaf_max256(mx, sh);
+  const bool skip = mx < thr;
+  double na = 0.0, nb = 0.0, ew = 0.0;
+  for (int p = threadIdx.x; p < L.cnt; p += 256) {
+    const size_t idx = static_cast<size_t>(L.off) + p;
+    const double ra = rho_a[idx], rb = rho_b[idx];
+    const double w = m.pts[idx].w;
+    na += w * ra;
+    nb += w * rb;
+    double ga[3], gb[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      ga[c] = rho_a[(c + 1) * N + idx];
+      gb[c] = rho_b[(c + 1) * N + idx];
+    }
+    const double saa = ga[0] * ga[0] + ga[1] * ga[1] + ga[2] * ga[2];
+    const double sab = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
+    const double sbb = gb[0] * gb[0] + gb[1] * gb[1] + gb[2] * gb[2];
+    const double ta = 0.5 * (rho_a[4 * N + idx] + rho_a[5 * N + idx] + rho_a[6 * N + idx]);
+    const double tb = 0.5 * (rho_b[4 * N + idx] + rho_b[5 * N + idx] + rho_b[6 * N + idx]);
+    double e = 0.0, vr[2] = {0.0, 0.0}, vs[3] = {0.0, 0.0, 0.0}, vt[2] = {0.0, 0.0};
+    if (!skip)
+      eval_xc_mgga_pol(fs, ra, rb, saa, sab, sbb, ta, tb, e, vr, vs, vt);
+    coef_a[idx] = 0.5 * w * vr[0];
+    coef_b[idx] = 0.5 * w * vr[1];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      coef_a[(c + 1) * N + idx] = w * (2.0 * vs[0] * ga[c] + vs[1] * gb[c]);
+      coef_b[(c + 1) * N + idx] = w * (2.0 * vs[2] * gb[c] + vs[1] * ga[c]);
+    }
+    coef_a[4 * N + idx] = 0.25 * w * vt[0];
+    coef_b[4 * N + idx] = 0.25 * w * vt[1];
+    ew += w * e;
+  }
+  ew = leaf_sum256(ew, sh);
+  na = leaf_sum256(na, sh);
+  nb = leaf_sum256(nb, sh);
+  if (threadIdx.x == 0) {
+    epart3[3 * blockIdx.x] = ew;
+    epart3[3 * blockIdx.x + 1] = na;
+    epart3[3 * blockIdx.x + 2] = nb;
+  }
+}
+
 // out3 = column sums of epart3 (fixed order per thread, then the block)
 __global__ void __launch_bounds__(256) k_reduce3(const double *__restrict__ epart3, int n,
                                                  double *__restrict__ out3) {
@@ -110,7 +171,10 @@ void launch_func_pol(const MolDev &m, int deriv, const FuncSet &fs, double thr,
                      double *epart3, cudaStream_t st) {
   if (m.nleaves == 0)
     return;
-  if (deriv)
+  if (deriv == 2)
+    k_func_pol_mgga<<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b,
+                                              epart3);
+  else if (deriv)
     k_func_pol<true><<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
   else
     k_func_pol<false><<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b,
@@ -122,7 +186,6 @@ void launch_reduce3(const double *epart3, int n, double *out3, cudaStream_t st) 
 }
 
 void Molecule::prepare_uks() {
-  require_not_mgga(deriv, "unrestricted build");
   if (d_rho_b)
     return;
   if (!d_pts)
@@ -130,15 +193,15 @@ void Molecule::prepare_uks() {
   const size_t N = static_cast<size_t>(std::max<long>(plan.npts, 1));
   const size_t nl = std::max<size_t>(leaves.size(), 1);
   const size_t nbf2 = std::max<size_t>(static_cast<size_t>(basis.nbf) * basis.nbf, 1);
-  d_rho_b = static_cast<double *>(alloc(4 * N * sizeof(double)));
-  d_coef_b = static_cast<double *>(alloc(4 * N * sizeof(double)));
+  d_rho_b = static_cast<double *>(alloc(rho_components(deriv) * N * sizeof(double)));
+  d_coef_b = static_cast<double *>(alloc(coef_components(deriv) * N * sizeof(double)));
   d_epart_u = static_cast<double *>(alloc(3 * nl * sizeof(double)));
   d_Dab = static_cast<double *>(alloc(2 * nbf2 * sizeof(double)));
   d_Vab = static_cast<double *>(alloc(2 * nbf2 * sizeof(double)));
   d_Duks = static_cast<double *>(alloc(2 * nbf2 * sizeof(double)));
   d_Vuks = static_cast<double *>(alloc(2 * nbf2 * sizeof(double)));
   d_out3 = static_cast<double *>(alloc(4 * sizeof(double)));
-  cuda_check(cudaMemset(d_rho_b, 0, 4 * N * sizeof(double)), "cudaMemset");
+  cuda_check(cudaMemset(d_rho_b, 0, rho_components(deriv) * N * sizeof(double)), "cudaMemset");
 }
 
 void Molecule::build_fp64_uks(const double *dD, double *dV, double *dout3, cudaStream_t st) {
@@ -157,11 +220,17 @@ void Molecule::build_fp64_uks(const double *dD, double *dV, double *dout3, cudaS
   if (!fp64_ao_valid)
     c.launch("colloc_f64", st, [&] { launch_colloc_f64(m, deriv, d_ws, st); });
   double *rho[2] = {d_rho, d_rho_b}, *coef[2] = {d_coef, d_coef_b};
-  for (int s = 0; s < 2; s++)
+  for (int s = 0; s < 2; s++) {
     c.launch("rho_f64", st, [&] {
       launch_rho_f64(m, deriv, d_Dab + s * nbf2, d_ws, d_slabs, static_cast<int>(slabs.size()),
                      rho[s], st);
     });
+    if (deriv == 2)
+      c.launch("tau_f64", st, [&] {
+        launch_tau_f64(m, d_Dab + s * nbf2, d_ws, d_slabs, static_cast<int>(slabs.size()),
+                       rho[s], st);
+      });
+  }
   c.launch("func_pol", st, [&] {
     launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
                     d_epart_u, st);

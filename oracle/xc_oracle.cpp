@@ -493,7 +493,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
           }
       }
       // meta-GGA: tau = 0.5 sum_k (d_k phi) D2 (d_k phi) (src/gto/density.cpp:
-      // 70-97); the laplacian is not formed, as no functional here reads it
+      // 73-101); the laplacian is not formed, as no functional here reads it
       if (deriv == 2) {
         tau.assign(n, 0.0);
         for (int q = 1; q < 4; q++) {
@@ -899,11 +899,12 @@ extern "C" int oracle_xc_build_unrestricted(
     nbf += bs.size(s);
   }
   bs.nbf = nbf;
-  int deriv = 0;
+  int deriv = 0; // 0 LDA, 1 GGA, 2 meta-GGA
   for (int f = 0; f < nfunc; f++) {
     if (oracle_functional_is_mgga(func_ids[f]))
-      return -1; // meta-GGA: restricted energy and V only
-    deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
+      deriv = 2;
+    else
+      deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
   }
   std::vector<double> ext(nsh);
   decay_cutoff(bs, screen_threshold, ext.data());
@@ -930,7 +931,7 @@ extern "C" int oracle_xc_build_unrestricted(
     std::vector<double> &K = Vloc[tid];
     K.assign(ld * nbf, 0.0);
     std::vector<double> xyz, w, phi, Dloc, Dphi, rho[2], exc, e1, vr[2], v1[2], vs[3], s1[3],
-        G, Kb, kt;
+        G, Kb, kt, tau[2], vt[2], mr, ms, mt;
     std::vector<int> sig, loc0;
 #pragma omp for schedule(dynamic, 4)
     for (long li = 0; li < nleaves; li++) {
@@ -969,7 +970,7 @@ extern "C" int oracle_xc_build_unrestricted(
           int s = sig[k], nf = bs.size(s);
           tmp.assign(static_cast<size_t>(ncomp) * nf * n, 0.0);
           collocate(sh_l[s], bs.pure, sh_nprim[s], exps + sh_off[s], coefs + sh_off[s],
-                    sh_origin + 3 * s, n, xyz.data(), 3, deriv, tmp.data(), n);
+                    sh_origin + 3 * s, n, xyz.data(), 3, deriv ? 1 : 0, tmp.data(), n);
           for (int q = 0; q < ncomp; q++)
             for (int f = 0; f < nf; f++)
               std::memcpy(&phi[(static_cast<size_t>(q) * m + loc0[k] + f) * n],
@@ -1014,6 +1015,32 @@ extern "C" int oracle_xc_build_unrestricted(
           (sp == 0 ? naloc : nbloc)[tid] += rho[sp][p] * w[p];
           maxrho = std::max(maxrho, rho[sp][p]);
         }
+        // meta-GGA: tau_s = 0.5 sum_k (d_k phi) D2_s (d_k phi) (src/gto/density.cpp:
+        // 104-166)
+        if (deriv == 2) {
+          tau[sp].assign(n, 0.0);
+          for (int q = 1; q < 4; q++) {
+            std::fill(Dphi.begin(), Dphi.end(), 0.0);
+            for (int j = 0; j < m; j++)
+              for (int k = 0; k < m; k++) {
+                double d = Dloc[static_cast<size_t>(j) * m + k];
+                if (d == 0.0)
+                  continue;
+                const double *g = &phi[(static_cast<size_t>(q) * m + k) * n];
+                double *out = &Dphi[static_cast<size_t>(j) * n];
+                for (long p = 0; p < n; p++)
+                  out[p] += g[p] * d;
+              }
+            for (int j = 0; j < m; j++) {
+              const double *g = &phi[(static_cast<size_t>(q) * m + j) * n];
+              const double *dp = &Dphi[static_cast<size_t>(j) * n];
+              for (long p = 0; p < n; p++)
+                tau[sp][p] += g[p] * dp[p];
+            }
+          }
+          for (long p = 0; p < n; p++)
+            tau[sp][p] *= 0.5;
+        }
       }
       if (maxrho < density_threshold)
         continue;
@@ -1036,11 +1063,32 @@ extern "C" int oracle_xc_build_unrestricted(
         vs[k].assign(n, 0.0);
         s1[k].assign(n, 0.0);
       }
+      for (int sp = 0; sp < 2; sp++)
+        vt[sp].assign(n, 0.0);
       for (int f = 0; f < nfunc; f++) {
+        double c = func_coefs ? func_coefs[f] : 1.0;
+        if (oracle_functional_is_mgga(func_ids[f])) {
+          mr.resize(2 * n);
+          ms.resize(3 * n);
+          mt.resize(2 * n);
+          oracle_functional_mgga_polarized(func_ids[f], n, rho[0].data(), rho[1].data(),
+                                           saa.data(), sab.data(), sbb.data(), tau[0].data(),
+                                           tau[1].data(), e1.data(), mr.data(), ms.data(),
+                                           mt.data());
+          for (long p = 0; p < n; p++) {
+            exc[p] += c * e1[p];
+            for (int sp = 0; sp < 2; sp++) {
+              vr[sp][p] += c * mr[2 * p + sp];
+              vt[sp][p] += c * mt[2 * p + sp];
+            }
+            for (int k = 0; k < 3; k++)
+              vs[k][p] += c * ms[3 * p + k];
+          }
+          continue;
+        }
         oracle_functional_polarized(func_ids[f], n, rho[0].data(), rho[1].data(), saa.data(),
                                     sab.data(), sbb.data(), e1.data(), v1[0].data(),
                                     v1[1].data(), s1[0].data(), s1[1].data(), s1[2].data());
-        double c = func_coefs ? func_coefs[f] : 1.0;
         for (long p = 0; p < n; p++) {
           exc[p] += c * e1[p];
           vr[0][p] += c * v1[0][p];
@@ -1055,6 +1103,8 @@ extern "C" int oracle_xc_build_unrestricted(
         vr[1][p] *= w[p];
         for (int k = 0; k < 3; k++)
           vs[k][p] *= w[p];
+        vt[0][p] *= w[p];
+        vt[1][p] *= w[p];
         eloc[tid] += exc[p] * (rho[0][p] + rho[1][p]);
       }
       for (int sp = 0; sp < 2; sp++) {
@@ -1092,6 +1142,18 @@ extern "C" int oracle_xc_build_unrestricted(
               Kb[static_cast<size_t>(j) * m + i] +=
                   kt[static_cast<size_t>(j) * m + i] + kt[static_cast<size_t>(i) * m + j];
         }
+        if (deriv == 2) // V_s += sum_k (d_k phi)^T diag(0.5 w vtau_s) (d_k phi)
+          for (int q = 1; q < 4; q++)
+            for (int j = 0; j < m; j++) {
+              const double *b = &phi[(static_cast<size_t>(q) * m + j) * n];
+              for (int i = 0; i < m; i++) {
+                const double *a = &phi[(static_cast<size_t>(q) * m + i) * n];
+                double acc = 0.0;
+                for (long p = 0; p < n; p++)
+                  acc += a[p] * (0.5 * vt[sp][p]) * b[p];
+                Kb[static_cast<size_t>(j) * m + i] += acc;
+              }
+            }
         for (size_t a = 0; a < sig.size(); a++)
           for (size_t b = 0; b < sig.size(); b++) {
             int la = bs.size(sig[a]), lb = bs.size(sig[b]);

@@ -82,8 +82,8 @@ long oracle_morton_leaves(long n, const double *points, long target,
                           double *radii);
 
 // The whole restricted XC build (LDA, GGA and meta-GGA: for a meta-GGA the
-// density adds tau (src/gto/density.cpp:70-97) and V the tau term of
-// src/dft/xc_potential_matrix.cpp:43-56).  D is OCC's mo.D (nbf x nbf, column-major);
+// density adds tau (src/gto/density.cpp:73-101) and V the tau term of
+// src/dft/xc_potential_matrix.cpp:43-58).  D is OCC's mo.D (nbf x nbf, column-major);
 // V (nbf x nbf) receives V_xc = -K of compute_JK.  func ids/coefs give the
 // components summed as in src/dft/dft_kernels.cpp:55-58 (coefficients are
 // Libxc-internal mixture weights, not OCC's never-applied scale factors).

@@ -1,6 +1,6 @@
 """Meta-GGA (TPSS) XC build: compute_K_dft<2, Restricted> (include/occ/dft/
-dft.h:192-388) with tau in the density (src/gto/density.cpp:70-97) and the
-tau term of V_xc (src/dft/xc_potential_matrix.cpp:43-56).
+dft.h:192-388) with tau in the density (src/gto/density.cpp:73-101) and the
+tau term of V_xc (src/dft/xc_potential_matrix.cpp:43-58).
 
 Libxc, which evaluates mgga_x_tpss / mgga_c_tpss in the reference, is absent,
 so the oracle's TPSS is pinned by the functional's own exact constraints:
@@ -193,7 +193,7 @@ def test_tpss_entry_points_without_a_meta_gga_form_refuse():
     with pytest.raises(og.XCError, match="meta-GGA"):
         dft.compute_xc_gradient(D)
     with pytest.raises(og.XCError, match="meta-GGA"):
-        dft.compute_vxc(np.vstack([0.5 * D, 0.5 * D]))
+        dft.compute_vxc(np.vstack([0.5 * D, 0.5 * D]), og.MIXED)
     # the FP64 build still works on the same molecule afterwards
     V = dft.compute_vxc(D)
     assert np.all(np.isfinite(V))
@@ -217,3 +217,77 @@ def test_tpss_noalloc_entry_point():
     torch.cuda.synchronize()
     assert np.max(np.abs(dV.cpu().numpy().T - V)) < 1e-12
     assert abs(de[0].item() - dft.exchange_correlation_energy()) < 1e-12
+
+
+# ---- unrestricted meta-GGA (compute_K_dft<2, Unrestricted>) -----------------
+
+def test_oracle_tpss_closed_shell_unrestricted_equals_restricted():
+    from test_uks import _closed_shell_case
+    b, D = _closed_shell_case("tpss")
+    P, W = host_grid(b)
+    e_r, V_r, _ = oracle.xc_build(b, P, W, D, "tpss")
+    e_u, V_u, _ = oracle.xc_build_unrestricted(b, P, W, np.vstack([D / 2, D / 2]), "tpss")
+    nbf = b.nbf()
+    assert abs(e_u - e_r) < 1e-11
+    assert np.max(np.abs(V_u[:nbf] - V_r)) < 1e-11
+    assert np.max(np.abs(V_u[nbf:] - V_r)) < 1e-11
+
+
+def test_oracle_tpss_unrestricted_potential_is_derivative_of_energy():
+    from test_uks import radical_case
+    b, D = radical_case()
+    P, W = host_grid(b)
+    rng = np.random.default_rng(2)
+    nbf = b.nbf()
+    E = rng.standard_normal((2 * nbf, nbf))
+    E[:nbf] += E[:nbf].T
+    E[nbf:] += E[nbf:].T
+    E *= 1e-3 / np.linalg.norm(E)
+    _, V, _ = oracle.xc_build_unrestricted(b, P, W, D, "tpss")
+    h = 1e-3
+    fd = (oracle.xc_build_unrestricted(b, P, W, D + h * E, "tpss")[0] -
+          oracle.xc_build_unrestricted(b, P, W, D - h * E, "tpss")[0]) / (2 * h)
+    assert abs(fd - 2 * np.sum(V * E)) < 1e-9
+
+
+@pytest.mark.gpu
+def test_tpss_unrestricted_gpu_parity():
+    from test_uks import radical_case
+    b, D = radical_case()
+    dft = og.DFT("tpss", b)
+    V = dft.compute_vxc(D, og.FP64)
+    P, W = dft.grid()
+    e_ref, V_ref, n_ref = oracle.xc_build_unrestricted(b, P, W, D, "tpss")
+    assert V.shape == (2 * b.nbf(), b.nbf())
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= TOL_E
+    assert np.max(np.abs(V - V_ref)) <= TOL_V
+    na, nb = dft.integrated_spin_densities()
+    assert abs(na - n_ref[0]) < 1e-9 and abs(nb - n_ref[1]) < 1e-9
+
+
+@pytest.mark.gpu
+def test_tpss_unrestricted_gpu_water_cluster():
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(3, box=5.0, seed=4)
+    b = wl.basis_for(mol, "def2-svp")
+    D = wl.random_density_unrestricted(b.nbf(), 15, 14, seed=9)
+    dft = og.DFT("tpss", b)
+    V = dft.compute_vxc(D)
+    P, W = dft.grid()
+    e_ref, V_ref, _ = oracle.xc_build_unrestricted(b, P, W, D, "tpss")
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= TOL_E * max(1.0, abs(e_ref))
+    assert np.max(np.abs(V - V_ref)) <= TOL_V * max(1.0, np.max(np.abs(V_ref)))
+
+
+@pytest.mark.gpu
+def test_tpss_unrestricted_closed_shell_equals_restricted_gpu():
+    from test_uks import _closed_shell_case
+    b, D = _closed_shell_case("tpss")
+    dft = og.DFT("tpss", b)
+    V_r = dft.compute_vxc(D, og.FP64)
+    e_r = dft.exchange_correlation_energy()
+    V_u = dft.compute_vxc(np.vstack([D / 2, D / 2]), og.FP64)
+    nbf = b.nbf()
+    assert abs(dft.exchange_correlation_energy() - e_r) < 1e-11
+    assert np.max(np.abs(V_u[:nbf] - V_r)) < 1e-11
+    assert np.max(np.abs(V_u[nbf:] - V_r)) < 1e-11
