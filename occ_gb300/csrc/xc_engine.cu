@@ -493,6 +493,7 @@ void Molecule::release_device() {
   grad_bytes = 0.0;
   d_rho_b = d_coef_b = d_epart_u = d_Dab = d_Vab = d_Duks = d_Vuks = d_out3 = nullptr;
   d_uks_tabs = nullptr;
+  d_uks_tabs_meta = nullptr;
   nlc.reset();
   free_grad_mixed(gmixed);
   gmixed = nullptr;

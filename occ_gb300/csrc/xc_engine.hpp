@@ -239,6 +239,8 @@ struct Molecule {
   // the same with the density and potential contractions on the tensor cores
   void build_mixed_uks(const double *dD, double *dV, double *dout3, cudaStream_t st);
   void *d_uks_tabs = nullptr; // the mixed plan's table with the beta rho / coef arrays
+  void *d_uks_tabs_meta = nullptr; // the same for the meta-GGA plan
+  void build_mixed_uks_mgga(const double *dD, double *dV, double *dout3, cudaStream_t st);
   void release_gradient(); // frees the gradient's device state
   // dE_xc/dR (3 per atom, grid fixed) for mo.D = dD; dout2 = {E_xc, density}
   void xc_gradient(const double *dD, double *dgrad, double *dout2, cudaStream_t st);

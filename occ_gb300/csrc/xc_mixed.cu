@@ -2952,7 +2952,10 @@ __global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
 } // namespace
 
 void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cudaStream_t st) {
-  require_not_mgga(deriv, "the tensor-core unrestricted build");
+  if (deriv == 2) {
+    build_mixed_uks_mgga(dD, dV, dout3, st);
+    return;
+  }
   ensure_mixed_ws();
   prepare_uks();
   LaunchPlan &P = *mixed->single;
@@ -3148,6 +3151,36 @@ __global__ void __launch_bounds__(256, 2) k_func_b_mgga(const MixTab *__restrict
   }
 }
 
+// Per block, for one spin's table (the UKS build): the GGA operand Y
+// (ymix_block) and the tau term's operands c_tau d_k phi (hi, lo).
+__global__ void __launch_bounds__(256) k_ymix_mgga(const MixTab *__restrict__ tabs,
+                                                   const MBlock *__restrict__ blocks) {
+  __shared__ float4 cf[kBlockPts];
+  __shared__ float ct[kBlockPts];
+  const MBlock B = blocks[blockIdx.x];
+  const MixTab &T = tabs[B.mol];
+  const size_t N = static_cast<size_t>(T.m.npts);
+  if (threadIdx.x < kBlockPts) {
+    const int p = threadIdx.x;
+    const size_t idx = static_cast<size_t>(T.m.leaves[B.leaf].off) + B.p0 + p;
+    ct[p] = p < B.cnt ? static_cast<float>(T.coef[4 * N + idx]) : 0.f;
+  }
+  ymix_block<true>(T, B, cf); // synchronises after filling cf (and so ct)
+  float *base = T.ws + B.ws_off;
+  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+  const int n = B.mp * kBlockPts;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const float c = ct[q % kBlockPts];
+#pragma unroll
+    for (int k = 1; k <= 3; k++) {
+      float h, l;
+      tf32_split(base[k * plane + q] * c, h, l);
+      base[(kPlaneMetaY + 2 * (k - 1)) * plane + q] = h;
+      base[(kPlaneMetaY + 2 * (k - 1) + 1) * plane + q] = l;
+    }
+  }
+}
+
 } // namespace
 
 void Molecule::prepare_mgga_mixed() {
@@ -3239,6 +3272,100 @@ void Molecule::build_mixed_mgga(const double *dD, double *dV, double *dout2, cud
     k_symmetrize<<<dim3(std::max(gx, 1), 1), 256, 0, st>>>(P.d_tabs, ov);
   });
   c.launch("reduce", st, [&] { k_reduce_b<<<1, 256, 0, st>>>(P.d_tabs, ov); });
+  cuda_check(cudaGetLastError(), "kernel launch");
+  P.ao_valid = true;
+}
+
+// compute_K_dft<2, Unrestricted> on the tensor cores: the meta plan's blocks
+// per spin (a second table points rho / coef at the beta arrays), the FP64
+// polarised meta-GGA functional (k_func_pol_mgga), then per spin the operand
+// planes and the three V_xc launches of the restricted meta build.
+void Molecule::build_mixed_uks_mgga(const double *dD, double *dV, double *dout3,
+                                    cudaStream_t st) {
+  prepare_mgga_mixed();
+  prepare_uks();
+  LaunchPlan &P = mmixed->plan;
+  if (!d_uks_tabs_meta) {
+    MixTab tb = P.tabs[0];
+    tb.rho = d_rho_b;
+    tb.coef = d_coef_b;
+    d_uks_tabs_meta = alloc(sizeof(MixTab));
+    cuda_check(cudaMemcpy(d_uks_tabs_meta, &tb, sizeof(MixTab), cudaMemcpyHostToDevice),
+               "cudaMemcpy H2D");
+  }
+  const MixTab *tabs[2] = {P.d_tabs, static_cast<const MixTab *>(d_uks_tabs_meta)};
+  Context &c = *ctx;
+  int *err = mixed->d_err;
+  const size_t nbf = static_cast<size_t>(basis.nbf), nbf2 = nbf * nbf;
+  const int nb = static_cast<int>(P.blocks.size());
+  const int ni = static_cast<int>(P.items.size());
+  const int sms = this->ctas > 0 ? this->ctas
+                                 : (ctx->max_ctas > 0 ? ctx->max_ctas : num_sms(device));
+  const int gg = std::min(std::max(nb, 1), sms);
+  for (int s = 0; s < 2; s++)
+    cuda_check(cudaMemcpy2DAsync(d_Dab + s * nbf2, nbf * sizeof(double), dD + s * nbf,
+                                 2 * nbf * sizeof(double), nbf * sizeof(double), nbf,
+                                 cudaMemcpyDeviceToDevice, st),
+               "cudaMemcpy2DAsync");
+  cuda_check(cudaMemsetAsync(d_Vab, 0, 2 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
+  Override ov[2] = {{d_Dab, d_Vab, nullptr}, {d_Dab + nbf2, d_Vab + nbf2, nullptr}};
+  for (int s = 0; s < 2; s++) {
+    c.launch("prep_density", st, [&] {
+      k_prep_density<<<dim3(P.maxnbf, 1), 256, 0, st>>>(tabs[s], ov[s], P.d_queue);
+    });
+    if (nb == 0)
+      continue;
+    if (s == 0 && !P.ao_valid) {
+      c.launch("colloc_f32", st, [&] {
+        k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+      c.launch("meta_ops", st, [&] {
+        k_meta_ops<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+    }
+    c.launch("rho_mixed", st, [&] {
+      k_rho_mixed<true><<<gg, kRhoThreads, kRhoSmem, st>>>(tabs[s], P.d_blocks, P.d_order, nb,
+                                                     P.d_queue, err);
+    });
+    for (int k = 1; k <= 3; k++) {
+      cuda_check(cudaMemsetAsync(P.d_queue, 0, sizeof(int), st), "cudaMemsetAsync");
+      c.launch("tau_mixed", st, [&] {
+        k_rho_mixed<true, true><<<gg, kRhoThreads, kRhoSmem, st>>>(
+            tabs[s], P.d_blocks, P.d_order, nb, P.d_queue, err, k);
+      });
+    }
+  }
+  const MolDev m = dev();
+  c.launch("func_pol", st, [&] {
+    launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
+                    d_epart_u, st);
+  });
+  const VxcPlanes pls[3] = {
+      kVxcBuildPlanes,
+      {kPlaneMetaDphi, kPlaneMetaDphi + 1, kPlaneMetaY, kPlaneMetaY + 1, kPlaneMetaDphi + 2,
+       kPlaneMetaDphi + 3, kPlaneMetaY + 2, kPlaneMetaY + 3, 2},
+      {kPlaneMetaDphi + 4, kPlaneMetaDphi + 5, kPlaneMetaY + 4, kPlaneMetaY + 5, 0, 0, 0, 0, 1}};
+  for (int s = 0; s < 2 && nb > 0; s++) {
+    c.launch("ymix", st, [&] { k_ymix_mgga<<<nb, 256, 0, st>>>(tabs[s], P.d_blocks); });
+    for (int v = 0; v < 3 && ni > 0; v++) {
+      cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
+      c.launch(v == 0 ? "vxc_mixed" : "vxc_tau_mixed", st, [&] {
+        k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+            tabs[s], P.d_blocks, P.d_items, ni, ov[s], P.d_queue, err, P.tmap.rows32,
+            P.tmap.rows128, pls[v]);
+      });
+    }
+    c.launch("symmetrize", st, [&] {
+      const int gx = static_cast<int>(std::min<size_t>((nbf2 + 255) / 256, 1024));
+      k_symmetrize<<<dim3(std::max(gx, 1), 1), 256, 0, st>>>(tabs[s], ov[s]);
+    });
+  }
+  c.launch("reduce", st, [&] { launch_reduce3(d_epart_u, m.nleaves, dout3, st); });
+  for (int s = 0; s < 2; s++)
+    cuda_check(cudaMemcpy2DAsync(dV + s * nbf, 2 * nbf * sizeof(double), d_Vab + s * nbf2,
+                                 nbf * sizeof(double), nbf * sizeof(double), nbf,
+                                 cudaMemcpyDeviceToDevice, st),
+               "cudaMemcpy2DAsync");
   cuda_check(cudaGetLastError(), "kernel launch");
   P.ao_valid = true;
 }

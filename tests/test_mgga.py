@@ -192,8 +192,6 @@ def test_tpss_entry_points_without_a_meta_gga_form_refuse():
     dft = og.DFT("tpss", b)
     with pytest.raises(og.XCError, match="meta-GGA"):
         dft.compute_xc_gradient(D)
-    with pytest.raises(og.XCError, match="meta-GGA"):
-        dft.compute_vxc(np.vstack([0.5 * D, 0.5 * D]), og.MIXED)
     # the FP64 build still works on the same molecule afterwards
     V = dft.compute_vxc(D)
     assert np.all(np.isfinite(V))
@@ -291,3 +289,37 @@ def test_tpss_unrestricted_closed_shell_equals_restricted_gpu():
     assert abs(dft.exchange_correlation_energy() - e_r) < 1e-11
     assert np.max(np.abs(V_u[:nbf] - V_r)) < 1e-11
     assert np.max(np.abs(V_u[nbf:] - V_r)) < 1e-11
+
+
+@pytest.mark.gpu
+def test_tpss_unrestricted_mixed_against_oracle():
+    from test_uks import radical_case
+    b, D = radical_case()
+    dft = og.DFT("tpss", b)
+    V = dft.compute_vxc(D, og.MIXED)
+    P, W = dft.grid()
+    e_ref, V_ref, n_ref = oracle.xc_build_unrestricted(b, P, W, D, "tpss")
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= TOL_E_MIXED
+    assert np.max(np.abs(V - V_ref)) <= TOL_V_MIXED
+    na, nb = dft.integrated_spin_densities()
+    assert abs(na - n_ref[0]) < 1e-6 and abs(nb - n_ref[1]) < 1e-6
+    # the restricted tensor-core meta build of the same molecule after it
+    Dr = np.vstack([D[:b.nbf()], D[b.nbf():]])[:b.nbf()] * 2.0
+    Vr = dft.compute_vxc(Dr, og.MIXED)
+    e_r, V_r, _ = oracle.xc_build(b, P, W, Dr, "tpss")
+    assert abs(dft.exchange_correlation_energy() - e_r) <= TOL_E_MIXED
+    assert np.max(np.abs(Vr - V_r)) <= TOL_V_MIXED
+
+
+@pytest.mark.gpu
+def test_tpss_unrestricted_mixed_water_cluster():
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(3, box=5.0, seed=4)
+    b = wl.basis_for(mol, "def2-svp")
+    D = wl.random_density_unrestricted(b.nbf(), 15, 14, seed=9)
+    dft = og.DFT("tpss", b)
+    V64 = dft.compute_vxc(D, og.FP64)
+    e64 = dft.exchange_correlation_energy()
+    Vm = dft.compute_vxc(D, og.MIXED)
+    assert abs(dft.exchange_correlation_energy() - e64) <= TOL_E_MIXED
+    assert np.max(np.abs(Vm - V64)) <= TOL_V_MIXED
