@@ -440,6 +440,33 @@ def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
     out["abs_dE_mixed_vs_fp64"] = abs(res["mixed"][0] - res["fp64"][0])
     out["max_abs_dV_mixed_vs_fp64"] = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1])))
     out["e2e"] = out["mixed"]["e2e"]
+    # the unrestricted build of the cation radical (5n alpha, 5n - 1 beta electrons)
+    Du = wl.random_density_unrestricted(nbf, 5 * waters, 5 * waters - 1, seed=seed)
+    dDu = torch.from_numpy(np.asfortranarray(Du).ravel(order="F").copy()).cuda()
+    dVu = torch.zeros_like(dDu)
+    d3 = torch.zeros(3, dtype=torch.float64, device="cuda")
+    ures = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        def one_u():
+            rc = lib.occ_xc_compute_vxc_unrestricted_device(
+                dft.ctx.h, dft.h, C.c_void_p(dDu.data_ptr()), prec, C.c_void_p(dVu.data_ptr()),
+                C.c_void_p(d3.data_ptr()), C.c_void_p(stream.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(dft.ctx.error())
+        nrep = steps if name == "mixed" else 2
+        one_u()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(nrep + 1)]
+        ev[0].record(stream)
+        for i in range(nrep):
+            one_u()
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(nrep)]))
+        ures[name] = float(d3[0].item())
+        out.setdefault("uks", {})[name] = {"builds_per_s": 1e3 / ms, "ms_per_build": ms,
+                                           "exc": ures[name]}
+    out["uks"]["abs_dE_mixed_vs_fp64"] = abs(ures["mixed"] - ures["fp64"])
     if oracle_check:
         root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
         sys.path.insert(0, os.path.join(root, "oracle"))
