@@ -3050,8 +3050,9 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
 // slices of d_k phi (three per k, planes 11-19: the A operand of
 // k_rho_mixed's tau mode), the hi and lo TF32 planes of d_k phi (20-25) and
 // of c_tau d_k phi with c_tau = 0.25 w vtau (26-31).  The tau term of V is the
-// V_xc kernel's K with operand pairs (d_k phi, c_tau d_k phi), accumulated
-// into the same A that k_symmetrize turns into A + A^T.  The functional is
+// V_xc kernel's K with operand pairs (d_k phi, c_tau d_k phi), packed two a
+// launch with the GGA pair (phi, Y) into the same A that k_symmetrize turns
+// into A + A^T.  The functional is
 // the FP64 meta-GGA evaluator, fused with the operand planes (two CTAs an SM:
 // one's FP64 functional overlaps the other's HBM-bound planes).  Measured
 // alternatives: a double-float (FP32-pipe) TPSS needed 255 registers a thread
@@ -3062,6 +3063,15 @@ namespace occx {
 constexpr int kPlanesMeta = 32;
 constexpr int kPlaneMetaDphi = 20; // hi, lo of d_k phi: planes 20 + 2(k-1), 21 + 2(k-1)
 constexpr int kPlaneMetaY = 26;    // hi, lo of c_tau d_k phi: planes 26 + 2(k-1), 27 + 2(k-1)
+
+// The V_xc launches of a meta build: four operand pairs, two a launch (the
+// kernel's cost is partly per launch: one pair 0.91 ms, two 1.22 ms at water32)
+//   (phi, Y) + (d_x phi, c_tau d_x phi),  (d_y phi, c_tau d_y phi) + (d_z phi, c_tau d_z phi)
+constexpr VxcPlanes kMetaVxcPlanes[2] = {
+    {kPlanePhiHi, kPlanePhiLo, kPlaneYHi, kPlaneYLo, kPlaneMetaDphi, kPlaneMetaDphi + 1,
+     kPlaneMetaY, kPlaneMetaY + 1, 2},
+    {kPlaneMetaDphi + 2, kPlaneMetaDphi + 3, kPlaneMetaY + 2, kPlaneMetaY + 3,
+     kPlaneMetaDphi + 4, kPlaneMetaDphi + 5, kPlaneMetaY + 4, kPlaneMetaY + 5, 2}};
 
 struct MetaMixed {
   char *ws = nullptr;
@@ -3251,12 +3261,8 @@ void Molecule::build_mixed_mgga(const double *dD, double *dV, double *dout2, cud
       k_func_b_mgga<<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
     });
   if (ni > 0) {
-    const VxcPlanes pls[3] = {
-        kVxcBuildPlanes,
-        {kPlaneMetaDphi, kPlaneMetaDphi + 1, kPlaneMetaY, kPlaneMetaY + 1, kPlaneMetaDphi + 2,
-         kPlaneMetaDphi + 3, kPlaneMetaY + 2, kPlaneMetaY + 3, 2},
-        {kPlaneMetaDphi + 4, kPlaneMetaDphi + 5, kPlaneMetaY + 4, kPlaneMetaY + 5, 0, 0, 0, 0, 1}};
-    for (int v = 0; v < 3; v++) {
+    const VxcPlanes *pls = kMetaVxcPlanes;
+    for (int v = 0; v < 2; v++) {
       if (v > 0)
         cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
       c.launch(v == 0 ? "vxc_mixed" : "vxc_tau_mixed", st, [&] {
@@ -3340,14 +3346,10 @@ void Molecule::build_mixed_uks_mgga(const double *dD, double *dV, double *dout3,
     launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
                     d_epart_u, st);
   });
-  const VxcPlanes pls[3] = {
-      kVxcBuildPlanes,
-      {kPlaneMetaDphi, kPlaneMetaDphi + 1, kPlaneMetaY, kPlaneMetaY + 1, kPlaneMetaDphi + 2,
-       kPlaneMetaDphi + 3, kPlaneMetaY + 2, kPlaneMetaY + 3, 2},
-      {kPlaneMetaDphi + 4, kPlaneMetaDphi + 5, kPlaneMetaY + 4, kPlaneMetaY + 5, 0, 0, 0, 0, 1}};
+  const VxcPlanes *pls = kMetaVxcPlanes;
   for (int s = 0; s < 2 && nb > 0; s++) {
     c.launch("ymix", st, [&] { k_ymix_mgga<<<nb, 256, 0, st>>>(tabs[s], P.d_blocks); });
-    for (int v = 0; v < 3 && ni > 0; v++) {
+    for (int v = 0; v < 2 && ni > 0; v++) {
       cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
       c.launch(v == 0 ? "vxc_mixed" : "vxc_tau_mixed", st, [&] {
         k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
