@@ -467,6 +467,13 @@ def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
         out.setdefault("uks", {})[name] = {"builds_per_s": 1e3 / ms, "ms_per_build": ms,
                                            "exc": ures[name]}
     out["uks"]["abs_dE_mixed_vs_fp64"] = abs(ures["mixed"] - ures["fp64"])
+    # the meta-GGA XC gradient (FP64), host entry point
+    dft.compute_xc_gradient(D)
+    t0 = time.perf_counter()
+    for _ in range(2):
+        g = dft.compute_xc_gradient(D)
+    out["gradient_fp64"] = {"gradients_per_s": 2.0 / (time.perf_counter() - t0),
+                            "max_abs_g": float(np.max(np.abs(g)))}
     if oracle_check:
         root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
         sys.path.insert(0, os.path.join(root, "oracle"))

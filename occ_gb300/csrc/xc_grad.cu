@@ -25,6 +25,8 @@
 //   k_grad_f64     X, W per 64-point slab and 64-AO tile; per-AO sums over
 //                  the slab reduced over runs of AOs on one atom, then one
 //                  atomic add per atom and direction
+// and for a meta-GGA the tau density (the build's k_rho_f64 tau mode) and the
+// tau term (k_grad_f64's TAU mode, one derivative plane k per grid row).
 #include <algorithm>
 
 #include "host/gto_eval.h"
@@ -174,7 +176,12 @@ __device__ __forceinline__ int hplane(int c, int k) {
 
 // One 64-point slab of one leaf.  Thread (tx, ty): points p0 + tx + 16 i,
 // AOs mu = i0 + ty + 16 j of the current 64-AO tile.
-template <bool GGA>
+// TAU (meta-GGA, grid.y = 3, k = blockIdx.y): the tau term of
+// accumulate_gradient_contribution_R<2> (src/dft/dft_gradient_kernels.cpp:
+// 151-172), V_c(mu, nu) += sum_p d_c d_k phi_mu (0.5 w vtau) d_k phi_nu, as
+//   g_A,c -= sum_{mu on A} sum_p d_c d_k phi_mu (0.5 w vtau) T_k,mu,
+//   T_k,mu = sum_nu 4D(mu, nu) d_k phi_nu  (the same GEMM on plane 1 + k).
+template <bool GGA, bool TAU = false>
 __global__ void __launch_bounds__(256) k_grad_f64(MolDev m, const double *__restrict__ D,
                                                   const double *__restrict__ ws,
                                                   const double *__restrict__ coef,
@@ -193,6 +200,8 @@ __global__ void __launch_bounds__(256) k_grad_f64(MolDev m, const double *__rest
   const size_t N = static_cast<size_t>(m.npts);
   const int *g = m.leaf_ao + L.ao_begin;
   const size_t nbf = static_cast<size_t>(m.nbf);
+  const int kd = TAU ? static_cast<int>(blockIdx.y) : 0;
+  const double *pha = phi + (TAU ? (1 + kd) * plane : 0); // the GEMM's AO operand
 
   // functional coefficients of this thread's points (zero past the leaf)
   double c0[4], cg[GGA ? 3 : 1][4];
@@ -201,7 +210,7 @@ __global__ void __launch_bounds__(256) k_grad_f64(MolDev m, const double *__rest
     const int lp = it.p0 + tx + 16 * i;
     const bool ok = lp < L.cnt;
     const size_t gp = static_cast<size_t>(L.off) + (ok ? lp : 0);
-    c0[i] = ok ? coef[gp] : 0.0;
+    c0[i] = ok ? (TAU ? 2.0 * coef[4 * N + gp] : coef[gp]) : 0.0; // TAU: 0.5 w vtau
     if (GGA)
 #pragma unroll
       for (int k = 0; k < 3; k++)
@@ -224,7 +233,7 @@ __global__ void __launch_bounds__(256) k_grad_f64(MolDev m, const double *__rest
         const int idx = threadIdx.x + r * 256;
         const int kk = idx >> 6, pp = idx & 63;
         const size_t o = static_cast<size_t>(k0 + kk) * L.npad + it.p0 + pp;
-        const double f = phi[o];
+        const double f = pha[o];
         Ps[kk][pp] = f;
         if (GGA) {
           const int lp = it.p0 + pp;
@@ -285,7 +294,11 @@ __global__ void __launch_bounds__(256) k_grad_f64(MolDev m, const double *__rest
 #pragma unroll
         for (int c = 0; c < 3; c++)
           dphi[c] = phi[(c + 1) * plane + o];
-        if (GGA) {
+        if (TAU) {
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+            s[j][c] = fma(c0[i] * phi[hplane(c, kd) * plane + o], X[i][j], s[j][c]);
+        } else if (GGA) {
           double h[6];
 #pragma unroll
           for (int q = 0; q < 6; q++)
@@ -353,7 +366,6 @@ void upload_sph_table_grad() {
 // relative to their group), their slabs, leaf groups under the workspace cap,
 // and the AO -> atom map.  Allocated on the first gradient of a molecule.
 void Molecule::prepare_gradient() {
-  require_not_mgga(deriv, "XC gradient");
   if (d_gws)
     return;
   if (!d_pts)
@@ -449,6 +461,8 @@ void Molecule::xc_gradient(const double *dD, double *dgrad, double *dout2, cudaS
         k_colloc2_f64<4><<<G.nleaf, 128, 0, st>>>(m, d_gws);
     });
     c.launch("rho_f64", st, [&] { launch_rho_f64(m, deriv, dD, d_gws, sl, G.nslab, d_rho, st); });
+    if (deriv == 2)
+      c.launch("tau_f64", st, [&] { launch_tau_f64(m, dD, d_gws, sl, G.nslab, d_rho, st); });
     c.launch("func", st, [&] {
       launch_func(m, deriv, fs, bs.density_threshold, d_rho, d_coef, d_epart + 2 * G.leaf0, st);
     });
@@ -458,6 +472,11 @@ void Molecule::xc_gradient(const double *dD, double *dgrad, double *dout2, cudaS
       else
         k_grad_f64<false><<<G.nslab, 256, 0, st>>>(m, dD, d_gws, d_coef, sl, d_ao_atom, dgrad);
     });
+    if (deriv == 2)
+      c.launch("grad_tau_f64", st, [&] {
+        k_grad_f64<false, true><<<dim3(G.nslab, 3), 256, 0, st>>>(m, dD, d_gws, d_coef, sl,
+                                                                  d_ao_atom, dgrad);
+      });
   }
   c.launch("reduce", st, [&] {
     launch_reduce(d_epart, static_cast<int>(leaves.size()), dout2, st);

@@ -671,11 +671,12 @@ extern "C" int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim,
     bs.first_bf[s] = nbf;
     nbf += bs.size(s);
   }
-  int deriv = 0;
+  int deriv = 0; // 0 LDA, 1 GGA, 2 meta-GGA
   for (int f = 0; f < nfunc; f++) {
     if (oracle_functional_is_mgga(func_ids[f]))
-      return -1; // meta-GGA: restricted energy and V only
-    deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
+      deriv = 2;
+    else
+      deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
   }
   const int ncomp = deriv ? 10 : 4;
   std::vector<double> ext(nsh);
@@ -702,7 +703,7 @@ extern "C" int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim,
 #endif
     std::vector<double> &G = gloc[tid];
     std::vector<double> xyz, w, phi, Dloc, Dphi, rho, sigma, e1, v1, s1, vrho, vsig, aow,
-        Vx, Vy, Vz, tmp;
+        Vx, Vy, Vz, tmp, tau, vtau, t1;
     std::vector<int> sig, loc0, bf_atom;
 #pragma omp for schedule(dynamic, 4)
     for (long li = 0; li < nleaves; li++) {
@@ -775,6 +776,25 @@ extern "C" int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim,
           for (int q = 1; q < 4; q++)
             rho[q * n + p] += 2.0 * P(q, j)[p] * dp;
         }
+      if (deriv == 2) { // tau = 0.5 sum_k (d_k phi) D2 (d_k phi)
+        tau.assign(n, 0.0);
+        for (int q = 1; q < 4; q++) {
+          std::fill(Dphi.begin(), Dphi.end(), 0.0);
+          for (int j = 0; j < m; j++)
+            for (int k = 0; k < m; k++) {
+              double d = Dloc[static_cast<size_t>(j) * m + k];
+              if (d == 0.0)
+                continue;
+              for (long p = 0; p < n; p++)
+                Dphi[static_cast<size_t>(j) * n + p] += P(q, k)[p] * d;
+            }
+          for (int j = 0; j < m; j++)
+            for (long p = 0; p < n; p++)
+              tau[p] += P(q, j)[p] * Dphi[static_cast<size_t>(j) * n + p];
+        }
+        for (long p = 0; p < n; p++)
+          tau[p] *= 0.5;
+      }
       double maxrho = -1e300;
       for (long p = 0; p < n; p++)
         maxrho = std::max(maxrho, rho[p]);
@@ -789,19 +809,28 @@ extern "C" int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim,
       e1.resize(n);
       v1.resize(n);
       s1.resize(n);
+      vtau.assign(n, 0.0);
+      t1.assign(n, 0.0);
       for (int f = 0; f < nfunc; f++) {
         std::fill(s1.begin(), s1.end(), 0.0);
-        oracle_functional(func_ids[f], n, rho.data(), sigma.data(), e1.data(), v1.data(),
-                          s1.data());
+        std::fill(t1.begin(), t1.end(), 0.0);
+        if (oracle_functional_is_mgga(func_ids[f]))
+          oracle_functional_mgga(func_ids[f], n, rho.data(), sigma.data(), tau.data(), e1.data(),
+                                 v1.data(), s1.data(), t1.data());
+        else
+          oracle_functional(func_ids[f], n, rho.data(), sigma.data(), e1.data(), v1.data(),
+                            s1.data());
         double c = func_coefs ? func_coefs[f] : 1.0;
         for (long p = 0; p < n; p++) {
           vrho[p] += c * v1[p];
           vsig[p] += c * s1[p];
+          vtau[p] += c * t1[p];
         }
       }
       for (long p = 0; p < n; p++) {
         vrho[p] *= w[p];
         vsig[p] *= w[p];
+        vtau[p] *= w[p];
       }
       Vx.assign(static_cast<size_t>(m) * m, 0.0);
       Vy.assign(static_cast<size_t>(m) * m, 0.0);
@@ -855,6 +884,20 @@ extern "C" int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim,
               VV[c][static_cast<size_t>(nu) * m + mu] += acc;
             }
         }
+      }
+      // meta-GGA (accumulate_gradient_contribution_R<2>, dft_gradient_kernels.cpp:
+      // 151-172): V_c(mu, nu) += sum_k sum_p d_c d_k phi_mu (0.5 w vtau) d_k phi_nu
+      if (deriv == 2) {
+        static const int hq2[3][3] = {{4, 5, 6}, {5, 7, 8}, {6, 8, 9}};
+        for (int c = 0; c < 3; c++)
+          for (int nu = 0; nu < m; nu++)
+            for (int mu = 0; mu < m; mu++) {
+              double acc = 0.0;
+              for (int k = 0; k < 3; k++)
+                for (long p = 0; p < n; p++)
+                  acc += P(hq2[c][k], mu)[p] * (0.5 * vtau[p]) * P(1 + k, nu)[p];
+              VV[c][static_cast<size_t>(nu) * m + mu] += acc;
+            }
       }
       // distribute to atoms (dft_gradient_kernels.cpp:535-547)
       for (int mu = 0; mu < m; mu++) {

@@ -191,7 +191,7 @@ def test_tpss_entry_points_without_a_meta_gga_form_refuse():
     b, D, _ = fchk_case()
     dft = og.DFT("tpss", b)
     with pytest.raises(og.XCError, match="meta-GGA"):
-        dft.compute_xc_gradient(D)
+        dft.compute_xc_gradient(D, og.MIXED)
     # the FP64 build still works on the same molecule afterwards
     V = dft.compute_vxc(D)
     assert np.all(np.isfinite(V))
@@ -323,3 +323,49 @@ def test_tpss_unrestricted_mixed_water_cluster():
     Vm = dft.compute_vxc(D, og.MIXED)
     assert abs(dft.exchange_correlation_energy() - e64) <= TOL_E_MIXED
     assert np.max(np.abs(Vm - V64)) <= TOL_V_MIXED
+
+
+# ---- meta-GGA XC gradient (accumulate_gradient_contribution_R<2>) ----------
+
+def test_oracle_tpss_gradient_is_derivative_of_exc():
+    """The reference's tau term (bra-side second derivatives, the ket side
+    through the factor 2 of the distribution) is the derivative of E_xc."""
+    from test_xc_gradient import _shifted
+    b, D, _ = fchk_case()
+    P, W = host_grid(b)
+    g = oracle.xc_gradient(b, P, W, D, "tpss", screen=1e-14)
+    h = 1e-4
+    for atom in range(3):
+        for axis in range(3):
+            ep = oracle.xc_build(_shifted(b, atom, axis, h), P, W, D, "tpss", screen=1e-14)[0]
+            em = oracle.xc_build(_shifted(b, atom, axis, -h), P, W, D, "tpss", screen=1e-14)[0]
+            assert abs(g[atom, axis] - (ep - em) / (2 * h)) < 1e-7, (atom, axis)
+
+
+@pytest.mark.gpu
+def test_tpss_gradient_gpu_parity():
+    b, D, _ = fchk_case()
+    dft = og.DFT("tpss", b)
+    g = dft.compute_xc_gradient(D)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient(b, P, W, D, "tpss")
+    assert np.max(np.abs(g - g_ref)) <= 1e-9, np.max(np.abs(g - g_ref))
+    e_ref = oracle.xc_build(b, P, W, D, "tpss")[0]
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= 1e-8
+
+
+@pytest.mark.gpu
+def test_tpss_gradient_water_cluster_gpu_parity():
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(4, box=6.0, seed=3)
+    b = wl.basis_for(mol, "def2-svp")
+    D = wl.random_density(b.nbf(), 20, seed=4)
+    dft = og.DFT("tpss", b)
+    g = dft.compute_xc_gradient(D)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient(b, P, W, D, "tpss")
+    scale = max(1.0, np.max(np.abs(g_ref)))
+    assert np.max(np.abs(g - g_ref)) <= 1e-9 * scale, np.max(np.abs(g - g_ref))
+    # a small workspace cap: many leaf groups, the same gradient
+    dft.set_gradient_workspace_cap(2 << 20)
+    assert np.max(np.abs(dft.compute_xc_gradient(D) - g)) < 1e-11
