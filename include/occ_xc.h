@@ -206,6 +206,24 @@ int occ_xc_compute_xc_gradient_device(occ_xc_context *ctx, occ_xc_molecule *mol,
                                       const double *d_D, int precision, double *d_grad,
                                       double *d_exc2, void *stream);
 
+/* Replaces DFT::compute_xc_gradient(mo) for an unrestricted wavefunction
+ * (include/occ/dft/dft.h:599-749 with accumulate_gradient_contribution_U,
+ * src/dft/dft_gradient_kernels.cpp:175-470, 549-575): D is OCC's unrestricted
+ * mo.D (2 nbf x nbf, alpha block above beta, column-major); grad[3*natoms]
+ * and exc as occ_xc_compute_xc_gradient.  LDA, GGA and meta-GGA methods;
+ * precision OCC_XC_FP64 only (OCC_XC_MIXED fails with OCC_XC_ERR_ARG).  Host
+ * buffers; blocking. */
+int occ_xc_compute_xc_gradient_unrestricted(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                            const double *D, int precision, double *grad,
+                                            double *exc);
+
+/* Same on device buffers, asynchronous on `stream` (NULL: the context's).
+ * d_exc3 (may be NULL) receives {E_xc, integrated rho_a, integrated rho_b}. */
+int occ_xc_compute_xc_gradient_unrestricted_device(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                                   const double *d_D, int precision,
+                                                   double *d_grad, double *d_exc3,
+                                                   void *stream);
+
 /* Cap (bytes) of the gradient workspace of one leaf group; leaves are
  * processed in groups under it (0: the default, 8 GiB).  Frees the
  * molecule's gradient state, which the next gradient rebuilds. */

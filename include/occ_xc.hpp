@@ -160,11 +160,19 @@ public:
   // compute_xc_gradient(mo) (dft.h:599-749): dE_xc/dR with the grid held
   // fixed; 3 * natoms values, x, y, z per atom (the memory of OCC's
   // 3 x natoms Mat3N).  Also sets exchange_correlation_energy().
+  // As compute_vxc, the size of D decides: nbf x nbf restricted, 2 nbf x nbf
+  // (OCC's unrestricted mo.D) unrestricted (FP64).
   std::vector<double> compute_xc_gradient(const std::vector<double> &D,
                                           Precision precision = Precision::FP64) {
-    if (D.size() != nbf_ * nbf_)
-      throw Error("density matrix must be nbf x nbf", OCC_XC_ERR_ARG);
     std::vector<double> g(3 * natoms_);
+    if (D.size() == 2 * nbf_ * nbf_) {
+      check(occ_xc_compute_xc_gradient_unrestricted(ctx_, mol_.get(), D.data(),
+                                                    static_cast<int>(precision), g.data(),
+                                                    &exc_));
+      return g;
+    }
+    if (D.size() != nbf_ * nbf_)
+      throw Error("density matrix must be nbf x nbf or 2 nbf x nbf", OCC_XC_ERR_ARG);
     check(occ_xc_compute_xc_gradient(ctx_, mol_.get(), D.data(), static_cast<int>(precision),
                                      g.data(), &exc_));
     return g;

@@ -187,7 +187,8 @@ __global__ void __launch_bounds__(256) k_grad_f64(MolDev m, const double *__rest
                                                   const double *__restrict__ coef,
                                                   const SlabItem *__restrict__ slabs,
                                                   const int *__restrict__ ao_atom,
-                                                  double *__restrict__ grad) {
+                                                  double *__restrict__ grad,
+                                                  const double *__restrict__ Dot) {
   __shared__ double Ps[kKChunk][kPtTile];
   __shared__ double Ys[GGA ? kKChunk : 1][kPtTile];
   __shared__ double Ds[kKChunk][kAoTile];
@@ -249,8 +250,10 @@ __global__ void __launch_bounds__(256) k_grad_f64(MolDev m, const double *__rest
         const int nu = k0 + kb, mu = i0 + jb;
         double dv = 0.0;
         if (nu < L.nbf && mu < L.nbf) {
-          dv = 4.0 * D[static_cast<size_t>(g[nu]) * nbf + g[mu]];
-          if (fabs(dv) < kGradDensitySkip)
+          const size_t e = static_cast<size_t>(g[nu]) * nbf + g[mu];
+          dv = 4.0 * D[e];
+          // the reference's skip: |4 D| restricted, |2 (D_a + D_b)| unrestricted
+          if (fabs(Dot ? 2.0 * (D[e] + Dot[e]) : dv) < kGradDensitySkip)
             dv = 0.0;
         }
         Ds[kb][jb] = dv;
@@ -468,18 +471,85 @@ void Molecule::xc_gradient(const double *dD, double *dgrad, double *dout2, cudaS
     });
     c.launch("grad_f64", st, [&] {
       if (deriv)
-        k_grad_f64<true><<<G.nslab, 256, 0, st>>>(m, dD, d_gws, d_coef, sl, d_ao_atom, dgrad);
+        k_grad_f64<true><<<G.nslab, 256, 0, st>>>(m, dD, d_gws, d_coef, sl, d_ao_atom, dgrad,
+                                                  nullptr);
       else
-        k_grad_f64<false><<<G.nslab, 256, 0, st>>>(m, dD, d_gws, d_coef, sl, d_ao_atom, dgrad);
+        k_grad_f64<false><<<G.nslab, 256, 0, st>>>(m, dD, d_gws, d_coef, sl, d_ao_atom, dgrad,
+                                                   nullptr);
     });
     if (deriv == 2)
       c.launch("grad_tau_f64", st, [&] {
         k_grad_f64<false, true><<<dim3(G.nslab, 3), 256, 0, st>>>(m, dD, d_gws, d_coef, sl,
-                                                                  d_ao_atom, dgrad);
+                                                                  d_ao_atom, dgrad, nullptr);
       });
   }
   c.launch("reduce", st, [&] {
     launch_reduce(d_epart, static_cast<int>(leaves.size()), dout2, st);
+  });
+  cuda_check(cudaGetLastError(), "kernel launch");
+}
+
+// The unrestricted gradient (dft.h:599-749 with accumulate_gradient_
+// contribution_U, src/dft/dft_gradient_kernels.cpp:175-470, distributed as
+// :549-575, g -= 2 (V_c,a Da + V_c,b Db) with D2 = 2 mo.D): per spin the
+// restricted kernels with that spin's mo.D block and coefficients (the UKS
+// build's: 0.5 w vrho_s, w (2 vsigma_ss grad rho_s + vsigma_ab grad rho_s'),
+// 0.25 w vtau_s), so that 4 D_s V_c,s is the reference's 2 Da V_c,a; elements
+// skipped where |Da + Db| < 1e-12.  dD: OCC's 2 nbf x nbf; dout3 = {E_xc,
+// integrated rho_a, integrated rho_b}.
+void Molecule::xc_gradient_uks(const double *dD, double *dgrad, double *dout3,
+                               cudaStream_t st) {
+  prepare_gradient();
+  prepare_uks();
+  Context &c = *ctx;
+  const size_t nbf = static_cast<size_t>(basis.nbf), nbf2 = nbf * nbf;
+  for (int s = 0; s < 2; s++)
+    cuda_check(cudaMemcpy2DAsync(d_Dab + s * nbf2, nbf * sizeof(double), dD + s * nbf,
+                                 2 * nbf * sizeof(double), nbf * sizeof(double), nbf,
+                                 cudaMemcpyDeviceToDevice, st),
+               "cudaMemcpy2DAsync");
+  cuda_check(cudaMemsetAsync(dgrad, 0, 3 * Z.size() * sizeof(double), st), "cudaMemsetAsync");
+  double *rho[2] = {d_rho, d_rho_b}, *coef[2] = {d_coef, d_coef_b};
+  for (const GradGroup &G : ggroups) {
+    MolDev m = dev();
+    m.leaves = d_gleaves + G.leaf0;
+    m.nleaves = G.nleaf;
+    const SlabItem *sl = d_gslabs + G.slab0;
+    c.launch("colloc2_f64", st, [&] {
+      if (deriv)
+        k_colloc2_f64<10><<<G.nleaf, 128, 0, st>>>(m, d_gws);
+      else
+        k_colloc2_f64<4><<<G.nleaf, 128, 0, st>>>(m, d_gws);
+    });
+    for (int s = 0; s < 2; s++) {
+      const double *Ds = d_Dab + s * nbf2;
+      c.launch("rho_f64", st, [&] { launch_rho_f64(m, deriv, Ds, d_gws, sl, G.nslab, rho[s], st); });
+      if (deriv == 2)
+        c.launch("tau_f64", st, [&] { launch_tau_f64(m, Ds, d_gws, sl, G.nslab, rho[s], st); });
+    }
+    c.launch("func_pol", st, [&] {
+      launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
+                      d_epart_u + 3 * G.leaf0, st);
+    });
+    for (int s = 0; s < 2; s++) {
+      const double *Ds = d_Dab + s * nbf2, *Do = d_Dab + (1 - s) * nbf2;
+      c.launch("grad_f64", st, [&] {
+        if (deriv)
+          k_grad_f64<true><<<G.nslab, 256, 0, st>>>(m, Ds, d_gws, coef[s], sl, d_ao_atom, dgrad,
+                                                    Do);
+        else
+          k_grad_f64<false><<<G.nslab, 256, 0, st>>>(m, Ds, d_gws, coef[s], sl, d_ao_atom, dgrad,
+                                                     Do);
+      });
+      if (deriv == 2)
+        c.launch("grad_tau_f64", st, [&] {
+          k_grad_f64<false, true><<<dim3(G.nslab, 3), 256, 0, st>>>(m, Ds, d_gws, coef[s], sl,
+                                                                    d_ao_atom, dgrad, Do);
+        });
+    }
+  }
+  c.launch("reduce", st, [&] {
+    launch_reduce3(d_epart_u, static_cast<int>(leaves.size()), dout3, st);
   });
   cuda_check(cudaGetLastError(), "kernel launch");
 }
@@ -558,6 +628,51 @@ int occ_xc_compute_xc_gradient_device(occ_xc_context *ctx, occ_xc_molecule *mol,
       M.xc_gradient_mixed(d_D, d_grad, d_exc2 ? d_exc2 : M.d_out2, st);
     else
       M.xc_gradient(d_D, d_grad, d_exc2 ? d_exc2 : M.d_out2, st);
+  });
+}
+
+int occ_xc_compute_xc_gradient_unrestricted(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                            const double *D, int precision, double *grad,
+                                            double *exc) {
+  if (!ctx || !mol || !D || !grad)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return guarded(ctx, [&] {
+    if (precision != OCC_XC_FP64)
+      throw ArgError("the unrestricted XC gradient is built in FP64 (OCC_XC_FP64) only");
+    Molecule &M = *mol->impl;
+    cudaStream_t st = ctx->impl->stream;
+    M.prepare_gradient();
+    M.prepare_uks();
+    const size_t n2 = 2 * static_cast<size_t>(M.basis.nbf) * M.basis.nbf;
+    cuda_check(cudaMemcpyAsync(M.d_Duks, D, n2 * sizeof(double), cudaMemcpyHostToDevice, st),
+               "cudaMemcpyAsync H2D");
+    M.xc_gradient_uks(M.d_Duks, M.d_grad, M.d_out3, st);
+    double out3[3];
+    cuda_check(cudaMemcpyAsync(grad, M.d_grad, 3 * M.Z.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost, st),
+               "cudaMemcpyAsync D2H");
+    cuda_check(cudaMemcpyAsync(out3, M.d_out3, sizeof(out3), cudaMemcpyDeviceToHost, st),
+               "cudaMemcpyAsync D2H");
+    cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (exc)
+      *exc = out3[0];
+  });
+}
+
+int occ_xc_compute_xc_gradient_unrestricted_device(occ_xc_context *ctx, occ_xc_molecule *mol,
+                                                   const double *d_D, int precision,
+                                                   double *d_grad, double *d_exc3,
+                                                   void *stream) {
+  if (!ctx || !mol || !d_D || !d_grad)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return guarded(ctx, [&] {
+    if (precision != OCC_XC_FP64)
+      throw ArgError("the unrestricted XC gradient is built in FP64 (OCC_XC_FP64) only");
+    Molecule &M = *mol->impl;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
+    M.xc_gradient_uks(d_D, d_grad, d_exc3 ? d_exc3 : M.d_out3, st);
   });
 }
 

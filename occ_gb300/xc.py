@@ -123,6 +123,10 @@ def library():
     lib.occ_xc_compute_xc_gradient_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
                                                       C.c_int, C.c_void_p, C.c_void_p,
                                                       C.c_void_p]
+    lib.occ_xc_compute_xc_gradient_unrestricted.argtypes = [C.c_void_p, C.c_void_p, _dp,
+                                                            C.c_int, _dp, _dp]
+    lib.occ_xc_compute_xc_gradient_unrestricted_device.argtypes = [
+        C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.occ_xc_compute_vxc_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                               C.c_void_p, C.c_void_p, C.c_void_p]
     _vp = C.c_void_p
@@ -495,19 +499,25 @@ class DFT:
     def compute_xc_gradient(self, D, precision=FP64):
         """dE_xc/dR (natoms x 3, Hartree/Bohr) for mo.D = D with the grid held
         fixed (DFT::compute_xc_gradient, include/occ/dft/dft.h:599-749);
-        precision FP64 or MIXED (contractions on the tensor cores).  E_xc of
-        the same density via exchange_correlation_energy()."""
+        precision FP64 or MIXED (contractions on the tensor cores).  As OCC
+        dispatches on mo.kind, the shape of D decides: nbf x nbf restricted,
+        2 nbf x nbf (alpha block above beta) unrestricted (FP64).  E_xc of the
+        same density via exchange_correlation_energy()."""
         nbf = self.nbf()
         Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
-        if Dm.shape != (nbf, nbf):
-            raise XCError(f"density matrix must be {nbf}x{nbf}")
         natoms = len(self.basis.atoms())
         g = np.zeros((natoms, 3))
         exc = C.c_double()
-        rc = self.ctx.lib.occ_xc_compute_xc_gradient(self.ctx.h, self.h, _ptr(Dm),
-                                                     int(precision), _ptr(g), C.byref(exc))
+        if Dm.shape == (2 * nbf, nbf):
+            fn, name = (self.ctx.lib.occ_xc_compute_xc_gradient_unrestricted,
+                        "occ_xc_compute_xc_gradient_unrestricted")
+        elif Dm.shape == (nbf, nbf):
+            fn, name = self.ctx.lib.occ_xc_compute_xc_gradient, "occ_xc_compute_xc_gradient"
+        else:
+            raise XCError(f"density matrix must be {nbf}x{nbf} or {2 * nbf}x{nbf}")
+        rc = fn(self.ctx.h, self.h, _ptr(Dm), int(precision), _ptr(g), C.byref(exc))
         if rc != 0:
-            raise XCError(f"occ_xc_compute_xc_gradient failed ({rc}): {self.ctx.error()}", rc)
+            raise XCError(f"{name} failed ({rc}): {self.ctx.error()}", rc)
         self._exc = exc.value
         return g
 

@@ -194,6 +194,33 @@ def xc_gradient(basis, points, weights, D, method, screen=1e-10, density_thresho
     return g.reshape(natoms, 3)
 
 
+def xc_gradient_unrestricted(basis, points, weights, D, method, screen=1e-10,
+                             density_threshold=1e-10, leaf=(128, 32, 256), nthreads=0):
+    """dE_xc/dR (natoms x 3) for OCC's unrestricted mo.D (2 nbf x nbf), grid
+    weights fixed (include/occ/dft/dft.h:599-749, the Unrestricted branch)."""
+    l, nprim, off, exps, coefs, origin = _basis_arrays(basis)
+    atom = np.array([s.atom for s in basis.shells], dtype=np.int32)
+    natoms = len(basis.atoms())
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    Df = np.asfortranarray(D, dtype=np.float64)
+    if Df.shape != (2 * basis.nbf(), basis.nbf()):
+        raise ValueError("D must be 2 nbf x nbf")
+    ids = np.array(METHODS[method.lower()], dtype=np.int32)
+    coef = np.ones(len(ids))
+    g = np.zeros(3 * natoms)
+    L = lib()
+    L.oracle_xc_gradient_unrestricted.restype = C.c_int
+    rc = L.oracle_xc_gradient_unrestricted(
+        len(l), _p(l, _ip), _p(nprim, _ip), _p(off, _ip), _p(exps), _p(coefs), _p(origin),
+        _p(atom, _ip), natoms, int(basis.pure), len(w), _p(pts), _p(w), Df.ctypes.data_as(_dp),
+        len(ids), _p(ids, _ip), _p(coef), C.c_double(screen), C.c_double(density_threshold),
+        C.c_long(leaf[0]), C.c_long(leaf[1]), C.c_long(leaf[2]), nthreads, _p(g))
+    if rc != 0:
+        raise RuntimeError(f"oracle_xc_gradient_unrestricted failed ({rc})")
+    return g.reshape(natoms, 3)
+
+
 def functional_polarized(fid, ra, rb, saa=None, sab=None, sbb=None):
     """Polarised functional at n points: exc (per particle), vrho (n x 2),
     vsigma (n x 3; zeros for an LDA)."""

@@ -1369,3 +1369,289 @@ extern "C" int oracle_nlc_vv10(int nsh, const int *sh_l, const int *sh_nprim, co
   }
   return 0;
 }
+
+// The unrestricted XC nuclear gradient (include/occ/dft/dft.h:599-749 with
+// accumulate_gradient_contribution_U<0,1,2>, src/dft/dft_gradient_kernels.cpp:
+// 175-470, and the distribution of :549-575), screened path, grid fixed.
+// D is OCC's unrestricted mo.D (2 nbf x nbf, alpha block above beta); with
+// D2 = 2 mo.D and Da, Db its blocks, per spin s
+//   V_c,s(mu, nu) = sum_p d_c phi_mu Y_s,nu + Z_c,s,mu phi_nu
+//                   [+ sum_k d_c d_k phi_mu (0.5 w vtau_s) d_k phi_nu]
+//   Y_s = 0.5 w vrho_s phi + w (2 vsigma_ss grad rho_s + vsigma_ab grad rho_s') . grad phi
+//   Z_c,s = 0.5 w vrho_s d_c phi + w (2 vsigma_ss grad rho_s + vsigma_ab grad rho_s')
+//           . grad d_c phi
+// (for an LDA, Y_s = w vrho_s phi and Z = 0: the same sum), and
+//   g_A,c -= sum_{mu on A, nu} 2 (V_c,a Da + V_c,b Db)(mu, nu),
+// skipping |Da + Db| < 1e-12.
+extern "C" int oracle_xc_gradient_unrestricted(
+    int nsh, const int *sh_l, const int *sh_nprim, const int *sh_off, const double *exps,
+    const double *coefs, const double *sh_origin, const int *sh_atom, int natoms, int pure,
+    long npts, const double *points, const double *weights, const double *D, int nfunc,
+    const int *func_ids, const double *func_coefs, double screen_threshold,
+    double density_threshold, long leaf_target, long leaf_min, long leaf_max, int nthreads,
+    double *grad) {
+  Basis bs{nsh, sh_l, sh_nprim, sh_off, exps, coefs, sh_origin, pure != 0, {}, 0};
+  bs.first_bf.resize(nsh);
+  int nbf = 0;
+  for (int s = 0; s < nsh; s++) {
+    bs.first_bf[s] = nbf;
+    nbf += bs.size(s);
+  }
+  bs.nbf = nbf;
+  int deriv = 0;
+  for (int f = 0; f < nfunc; f++) {
+    if (oracle_functional_is_mgga(func_ids[f]))
+      deriv = 2;
+    else
+      deriv = std::max(deriv, oracle_functional_is_gga(func_ids[f]));
+  }
+  const int ncomp = deriv ? 10 : 4;
+  std::vector<double> ext(nsh);
+  decay_cutoff(bs, screen_threshold, ext.data());
+  std::vector<long> perm;
+  auto leaves = morton_leaves(npts, points, leaf_target, leaf_min, leaf_max, perm);
+  const long nleaves = static_cast<long>(leaves.size());
+  const size_t ld = 2 * static_cast<size_t>(nbf);
+#ifdef _OPENMP
+  int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  int nt = 1;
+  (void)nthreads;
+#endif
+  std::vector<std::vector<double>> gloc(nt, std::vector<double>(3 * natoms, 0.0));
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    std::vector<double> &G = gloc[tid];
+    std::vector<double> xyz, w, phi, Dloc[2], Dphi, rho[2], tau[2], tmp, e1, mr, ms, mt;
+    std::vector<double> vr[2], vs[3], vt[2], v1[2], s1[3], aow, V[2][3];
+    std::vector<int> sig, loc0, bf_atom;
+#pragma omp for schedule(dynamic, 4)
+    for (long li = 0; li < nleaves; li++) {
+      const Leaf &lf = leaves[li];
+      const long n = lf.cnt;
+      if (n == 0)
+        continue;
+      sig.clear();
+      for (int s = 0; s < nsh; s++) {
+        const double *A = sh_origin + 3 * s;
+        double dx = A[0] - lf.c[0], dy = A[1] - lf.c[1], dz = A[2] - lf.c[2];
+        if (std::sqrt(dx * dx + dy * dy + dz * dz) - ext[s] < lf.r)
+          sig.push_back(s);
+      }
+      if (sig.empty())
+        continue;
+      loc0.assign(sig.size(), 0);
+      bf_atom.clear();
+      int m = 0;
+      for (size_t k = 0; k < sig.size(); k++) {
+        loc0[k] = m;
+        for (int f = 0; f < bs.size(sig[k]); f++)
+          bf_atom.push_back(sh_atom[sig[k]]);
+        m += bs.size(sig[k]);
+      }
+      xyz.resize(3 * n);
+      w.resize(n);
+      for (long i = 0; i < n; i++) {
+        long o = perm[lf.off + i];
+        for (int d = 0; d < 3; d++)
+          xyz[3 * i + d] = points[3 * o + d];
+        w[i] = weights[o];
+      }
+      phi.assign(static_cast<size_t>(ncomp) * m * n, 0.0);
+      for (size_t k = 0; k < sig.size(); k++) {
+        int s = sig[k], nf = bs.size(s);
+        tmp.assign(static_cast<size_t>(ncomp) * nf * n, 0.0);
+        collocate(sh_l[s], bs.pure, sh_nprim[s], exps + sh_off[s], coefs + sh_off[s],
+                  sh_origin + 3 * s, n, xyz.data(), 3, deriv ? 2 : 1, tmp.data(), n);
+        for (int q = 0; q < ncomp; q++)
+          for (int f = 0; f < nf; f++)
+            std::memcpy(&phi[(static_cast<size_t>(q) * m + loc0[k] + f) * n],
+                        &tmp[(static_cast<size_t>(q) * nf + f) * n], sizeof(double) * n);
+      }
+      auto P = [&](int q, int j) { return &phi[(static_cast<size_t>(q) * m + j) * n]; };
+      // per spin: D2_s local block, rho_s, grad rho_s, tau_s
+      double maxrho = -1e300;
+      for (int sp = 0; sp < 2; sp++) {
+        Dloc[sp].assign(static_cast<size_t>(m) * m, 0.0);
+        for (size_t a = 0; a < sig.size(); a++)
+          for (size_t b = 0; b < sig.size(); b++) {
+            int la = bs.size(sig[a]), lb = bs.size(sig[b]);
+            for (int j = 0; j < lb; j++)
+              for (int i = 0; i < la; i++)
+                Dloc[sp][(loc0[b] + j) * static_cast<size_t>(m) + loc0[a] + i] =
+                    2.0 * D[(bs.first_bf[sig[b]] + j) * ld + sp * static_cast<size_t>(nbf) +
+                            bs.first_bf[sig[a]] + i];
+          }
+        rho[sp].assign(4 * n, 0.0);
+        for (int q = 0; q < (deriv == 2 ? 4 : 1); q++) {
+          Dphi.assign(static_cast<size_t>(m) * n, 0.0);
+          for (int j = 0; j < m; j++)
+            for (int k = 0; k < m; k++) {
+              double d = Dloc[sp][static_cast<size_t>(j) * m + k];
+              if (d == 0.0)
+                continue;
+              for (long p = 0; p < n; p++)
+                Dphi[static_cast<size_t>(j) * n + p] += P(q, k)[p] * d;
+            }
+          if (q == 0) {
+            for (int j = 0; j < m; j++)
+              for (long p = 0; p < n; p++) {
+                const double dp = Dphi[static_cast<size_t>(j) * n + p];
+                rho[sp][p] += P(0, j)[p] * dp;
+                for (int c = 1; c < 4; c++)
+                  rho[sp][c * n + p] += 2.0 * P(c, j)[p] * dp;
+              }
+            if (deriv == 2)
+              tau[sp].assign(n, 0.0);
+          } else {
+            for (int j = 0; j < m; j++)
+              for (long p = 0; p < n; p++)
+                tau[sp][p] += 0.5 * P(q, j)[p] * Dphi[static_cast<size_t>(j) * n + p];
+          }
+        }
+        for (long p = 0; p < n; p++)
+          maxrho = std::max(maxrho, rho[sp][p]);
+      }
+      if (maxrho < density_threshold)
+        continue;
+      std::vector<double> saa(n, 0.0), sab(n, 0.0), sbb(n, 0.0);
+      for (long p = 0; p < n; p++)
+        for (int c = 1; c < 4; c++) {
+          saa[p] += rho[0][c * n + p] * rho[0][c * n + p];
+          sab[p] += rho[0][c * n + p] * rho[1][c * n + p];
+          sbb[p] += rho[1][c * n + p] * rho[1][c * n + p];
+        }
+      e1.resize(n);
+      for (int sp = 0; sp < 2; sp++) {
+        vr[sp].assign(n, 0.0);
+        vt[sp].assign(n, 0.0);
+        v1[sp].resize(n);
+      }
+      for (int k = 0; k < 3; k++) {
+        vs[k].assign(n, 0.0);
+        s1[k].assign(n, 0.0);
+      }
+      for (int f = 0; f < nfunc; f++) {
+        const double c = func_coefs ? func_coefs[f] : 1.0;
+        if (oracle_functional_is_mgga(func_ids[f])) {
+          mr.resize(2 * n);
+          ms.resize(3 * n);
+          mt.resize(2 * n);
+          oracle_functional_mgga_polarized(func_ids[f], n, rho[0].data(), rho[1].data(),
+                                           saa.data(), sab.data(), sbb.data(), tau[0].data(),
+                                           tau[1].data(), e1.data(), mr.data(), ms.data(),
+                                           mt.data());
+          for (long p = 0; p < n; p++) {
+            for (int sp = 0; sp < 2; sp++) {
+              vr[sp][p] += c * mr[2 * p + sp];
+              vt[sp][p] += c * mt[2 * p + sp];
+            }
+            for (int k = 0; k < 3; k++)
+              vs[k][p] += c * ms[3 * p + k];
+          }
+          continue;
+        }
+        oracle_functional_polarized(func_ids[f], n, rho[0].data(), rho[1].data(), saa.data(),
+                                    sab.data(), sbb.data(), e1.data(), v1[0].data(),
+                                    v1[1].data(), s1[0].data(), s1[1].data(), s1[2].data());
+        for (long p = 0; p < n; p++) {
+          vr[0][p] += c * v1[0][p];
+          vr[1][p] += c * v1[1][p];
+          for (int k = 0; k < 3; k++)
+            vs[k][p] += c * s1[k][p];
+        }
+      }
+      for (long p = 0; p < n; p++) {
+        for (int sp = 0; sp < 2; sp++) {
+          vr[sp][p] *= w[p];
+          vt[sp][p] *= w[p];
+        }
+        for (int k = 0; k < 3; k++)
+          vs[k][p] *= w[p];
+      }
+      static const int hq[3][3] = {{4, 5, 6}, {5, 7, 8}, {6, 8, 9}};
+      for (int sp = 0; sp < 2; sp++) {
+        const int ot = 1 - sp;
+        const std::vector<double> &vss = vs[sp == 0 ? 0 : 2];
+        for (int c = 0; c < 3; c++)
+          V[sp][c].assign(static_cast<size_t>(m) * m, 0.0);
+        aow.assign(static_cast<size_t>(m) * n, 0.0);
+        // grad-rho coefficient of this spin: 2 vsigma_ss grad rho_s + vsigma_ab grad rho_s'
+        auto gc = [&](int c, long p) {
+          return 2.0 * vss[p] * rho[sp][(1 + c) * n + p] + vs[1][p] * rho[ot][(1 + c) * n + p];
+        };
+        if (!deriv) { // accumulate_gradient_contribution_U<0>
+          for (int nu = 0; nu < m; nu++)
+            for (long p = 0; p < n; p++)
+              aow[static_cast<size_t>(nu) * n + p] = P(0, nu)[p] * vr[sp][p];
+          for (int c = 0; c < 3; c++)
+            for (int nu = 0; nu < m; nu++)
+              for (int mu = 0; mu < m; mu++) {
+                double acc = 0.0;
+                for (long p = 0; p < n; p++)
+                  acc += P(1 + c, mu)[p] * aow[static_cast<size_t>(nu) * n + p];
+                V[sp][c][static_cast<size_t>(nu) * m + mu] += acc;
+              }
+        } else { // U<1>, and the GGA part of U<2>
+          for (int nu = 0; nu < m; nu++)
+            for (long p = 0; p < n; p++)
+              aow[static_cast<size_t>(nu) * n + p] =
+                  0.5 * vr[sp][p] * P(0, nu)[p] + gc(0, p) * P(1, nu)[p] +
+                  gc(1, p) * P(2, nu)[p] + gc(2, p) * P(3, nu)[p];
+          for (int c = 0; c < 3; c++)
+            for (int nu = 0; nu < m; nu++)
+              for (int mu = 0; mu < m; mu++) {
+                double acc = 0.0;
+                for (long p = 0; p < n; p++)
+                  acc += P(1 + c, mu)[p] * aow[static_cast<size_t>(nu) * n + p];
+                V[sp][c][static_cast<size_t>(nu) * m + mu] += acc;
+              }
+          for (int c = 0; c < 3; c++)
+            for (int nu = 0; nu < m; nu++)
+              for (int mu = 0; mu < m; mu++) {
+                double acc = 0.0;
+                for (long p = 0; p < n; p++) {
+                  const double z = 0.5 * vr[sp][p] * P(1 + c, mu)[p] +
+                                   gc(0, p) * P(hq[c][0], mu)[p] +
+                                   gc(1, p) * P(hq[c][1], mu)[p] + gc(2, p) * P(hq[c][2], mu)[p];
+                  acc += z * P(0, nu)[p];
+                }
+                V[sp][c][static_cast<size_t>(nu) * m + mu] += acc;
+              }
+          if (deriv == 2) // the tau terms of U<2>
+            for (int c = 0; c < 3; c++)
+              for (int nu = 0; nu < m; nu++)
+                for (int mu = 0; mu < m; mu++) {
+                  double acc = 0.0;
+                  for (int k = 0; k < 3; k++)
+                    for (long p = 0; p < n; p++)
+                      acc += P(hq[c][k], mu)[p] * (0.5 * vt[sp][p]) * P(1 + k, nu)[p];
+                  V[sp][c][static_cast<size_t>(nu) * m + mu] += acc;
+                }
+        }
+      }
+      // distribution (dft_gradient_kernels.cpp:549-575)
+      for (int mu = 0; mu < m; mu++) {
+        const int atom = bf_atom[mu];
+        for (int nu = 0; nu < m; nu++) {
+          const size_t e = static_cast<size_t>(nu) * m + mu;
+          const double da = Dloc[0][e], db = Dloc[1][e];
+          if (std::abs(da + db) < 1e-12)
+            continue;
+          for (int c = 0; c < 3; c++)
+            G[3 * atom + c] -= 2.0 * (V[0][c][e] * da + V[1][c][e] * db);
+        }
+      }
+    }
+  }
+  std::memset(grad, 0, sizeof(double) * 3 * natoms);
+  for (int t = 0; t < nt; t++)
+    for (int i = 0; i < 3 * natoms; i++)
+      grad[i] += gloc[t][i];
+  return 0;
+}

@@ -136,6 +136,19 @@ int oracle_xc_gradient(int nsh, const int *sh_l, const int *sh_nprim, const int 
                        double screen_threshold, double density_threshold, long leaf_target,
                        long leaf_min, long leaf_max, int nthreads, double *grad);
 
+// The unrestricted XC nuclear gradient (dft.h:599-749, accumulate_gradient_
+// contribution_U, src/dft/dft_gradient_kernels.cpp:175-470, 549-575): D is
+// OCC's unrestricted mo.D (2 nbf x nbf); LDA, GGA and meta-GGA.
+int oracle_xc_gradient_unrestricted(int nsh, const int *sh_l, const int *sh_nprim,
+                                    const int *sh_off, const double *exps, const double *coefs,
+                                    const double *sh_origin, const int *sh_atom, int natoms,
+                                    int pure, long npts, const double *points,
+                                    const double *weights, const double *D, int nfunc,
+                                    const int *func_ids, const double *func_coefs,
+                                    double screen_threshold, double density_threshold,
+                                    long leaf_target, long leaf_min, long leaf_max, int nthreads,
+                                    double *grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -181,3 +181,72 @@ def test_unrestricted_device_entry_point():
     Vd = dV.cpu().numpy().reshape(b.nbf(), 2 * b.nbf()).T
     assert np.max(np.abs(Vd - V)) < 1e-13
     assert abs(d3[0].item() - dft.exchange_correlation_energy()) < 1e-13
+
+
+# ---- the unrestricted XC gradient (accumulate_gradient_contribution_U) ------
+
+@pytest.mark.parametrize("method", ["svwn5", "pbe", "tpss"])
+def test_oracle_unrestricted_gradient_is_derivative_of_exc(method):
+    """Central differences of the unrestricted E_xc over shifts of one atom's
+    basis functions, grid fixed (the default lda's VWN3 spin interpolation
+    is not smooth enough at this radical's zeta ~ 1 points for a 1e-4 step)."""
+    from test_xc_gradient import _shifted
+    b, D = radical_case("6-31g")
+    P, W = host_grid(b)
+    g = oracle.xc_gradient_unrestricted(b, P, W, D, method, screen=1e-14)
+    h = 1e-4
+    for atom in range(2):
+        for axis in range(3):
+            ep = oracle.xc_build_unrestricted(_shifted(b, atom, axis, h), P, W, D, method,
+                                              screen=1e-14)[0]
+            em = oracle.xc_build_unrestricted(_shifted(b, atom, axis, -h), P, W, D, method,
+                                              screen=1e-14)[0]
+            assert abs(g[atom, axis] - (ep - em) / (2 * h)) < 1e-8, (atom, axis)
+
+
+@pytest.mark.parametrize("method", ["lda", "pbe", "tpss"])
+def test_oracle_closed_shell_unrestricted_gradient_equals_restricted(method):
+    b, D = _closed_shell_case(method)
+    P, W = host_grid(b)
+    gr = oracle.xc_gradient(b, P, W, D, method)
+    gu = oracle.xc_gradient_unrestricted(b, P, W, np.vstack([D / 2, D / 2]), method)
+    assert np.max(np.abs(gr - gu)) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["lda", "svwn5", "pbe", "blyp", "b3lyp", "tpss"])
+def test_unrestricted_gradient_gpu_parity(method):
+    b, D = radical_case()
+    dft = og.DFT(method, b)
+    g = dft.compute_xc_gradient(D)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient_unrestricted(b, P, W, D, method)
+    assert g.shape == (2, 3)
+    assert np.max(np.abs(g - g_ref)) <= 1e-9, np.max(np.abs(g - g_ref))
+    e_ref = oracle.xc_build_unrestricted(b, P, W, D, method)[0]
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= 1e-8
+
+
+@pytest.mark.gpu
+def test_unrestricted_gradient_water_cluster_and_groups():
+    mol = wl.water_cluster(3, box=5.0, seed=4)
+    b = wl.basis_for(mol, "6-31g(d,p)", pure=False)
+    D = wl.random_density_unrestricted(b.nbf(), 15, 14, seed=9)
+    dft = og.DFT("pbe", b)
+    g = dft.compute_xc_gradient(D)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient_unrestricted(b, P, W, D, "pbe")
+    assert np.max(np.abs(g - g_ref)) <= 1e-9 * max(1.0, np.max(np.abs(g_ref)))
+    dft.set_gradient_workspace_cap(2 << 20)
+    assert np.max(np.abs(dft.compute_xc_gradient(D) - g)) < 1e-11
+    with pytest.raises(og.XCError, match="FP64"):
+        dft.compute_xc_gradient(D, og.MIXED)
+
+
+@pytest.mark.gpu
+def test_unrestricted_gradient_closed_shell_equals_restricted_gpu():
+    b, D = _closed_shell_case("b3lyp")
+    dft = og.DFT("b3lyp", b)
+    gr = dft.compute_xc_gradient(D)
+    gu = dft.compute_xc_gradient(np.vstack([D / 2, D / 2]))
+    assert np.max(np.abs(gr - gu)) < 1e-12
