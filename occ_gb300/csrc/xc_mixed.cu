@@ -2061,6 +2061,7 @@ struct Batch {
   size_t ws_bytes = 0;
   double *d_ws64 = nullptr;  // FP64 workspace (molecules built one at a time), on first use
   int *d_err = nullptr;
+  bool fp64_only = false;    // holds a meta-GGA molecule: no tensor-core plans
   Context *ctx = nullptr;
   ~Batch() {
     for (double *p : dD)
@@ -2097,6 +2098,14 @@ Batch *batch_create(Context *ctx, const std::vector<Molecule *> &mols, double ws
     B->dV.push_back(v);
     cuda_check(cudaMalloc(&e, 2 * sizeof(double)), "cudaMalloc");
     B->dE.push_back(e);
+  }
+  for (Molecule *M : mols)
+    B->fp64_only = B->fp64_only || M->deriv == 2;
+  if (B->fp64_only) { // meta-GGA: FP64 builds only, no tensor-core workspace or plans
+    cuda_check(cudaMalloc(&B->d_ws, 256), "cudaMalloc");
+    cuda_check(cudaMalloc(&B->d_err, sizeof(int)), "cudaMalloc");
+    cuda_check(cudaMemset(B->d_err, 0, sizeof(int)), "cudaMemset");
+    return B.release();
   }
   // partition in order under the cap (a molecule above the cap goes alone)
   std::vector<std::vector<size_t>> parts;
@@ -2152,6 +2161,8 @@ void batch_prepare(Batch &B, int precision) {
 }
 
 void batch_build(Batch &B, int precision, cudaStream_t st) {
+  if (precision == OCC_XC_MIXED && B.fp64_only)
+    throw ArgError("a batch with a meta-GGA molecule builds in FP64 only (OCC_XC_FP64)");
   if (precision == OCC_XC_MIXED) {
     for (auto &sb : B.subs)
       for (LaunchPlan &P : sb->plan)

@@ -503,6 +503,8 @@ int occ_xc_server_open(occ_xc_server *srv, int natoms, const int *Z, const doubl
                    coefficients, pure, method, grid, build};
     auto sess = std::make_unique<Session>();
     sess->mol = molecule_host(S.ctx.get(), a); // host work on the caller's thread
+    if (S.cfg.precision == OCC_XC_MIXED)
+      require_not_mgga(sess->mol->deriv, "a tensor-core (OCC_XC_MIXED) server");
     sess->ws = S.cfg.precision == OCC_XC_MIXED ? sess->mol->mixed_workspace_bytes()
                                                : sess->mol->fp64_workspace_bytes();
     sess->ws = (sess->ws + 511) / 512 * 512;

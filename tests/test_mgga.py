@@ -369,3 +369,40 @@ def test_tpss_gradient_water_cluster_gpu_parity():
     # a small workspace cap: many leaf groups, the same gradient
     dft.set_gradient_workspace_cap(2 << 20)
     assert np.max(np.abs(dft.compute_xc_gradient(D) - g)) < 1e-11
+
+
+@pytest.mark.gpu
+def test_tpss_in_batches_and_the_server():
+    """FP64 batches and an FP64 server build meta-GGA molecules with the rest;
+    the tensor-core batch and server refuse them with a message."""
+    from occ_gb300 import workloads as wl
+    water = wl.water()
+    b1 = wl.basis_for(water, "6-31g")
+    b2 = wl.basis_for(wl.water_cluster(2, box=4.0, seed=3), "def2-svp")
+    cases = [(og.DFT("tpss", b1), wl.random_density(b1.nbf(), 5, seed=31)),
+             (og.DFT("pbe", b2), wl.random_density(b2.nbf(), 10, seed=32))]
+    direct = []
+    for dft, D in cases:
+        direct.append((dft.compute_vxc(D), dft.exchange_correlation_energy()))
+    batch = og.Batch([c[0] for c in cases])
+    Vs, exc, _ = batch.compute_vxc([c[1] for c in cases], og.FP64)
+    for i, (V, e) in enumerate(direct):
+        assert abs(exc[i] - e) <= 1e-11
+        assert np.max(np.abs(Vs[i] - V)) <= 1e-11
+    with pytest.raises(og.XCError, match="meta-GGA"):
+        batch.compute_vxc([c[1] for c in cases], og.MIXED)
+    srv = og.Server(precision=og.FP64)
+    try:
+        sid = srv.open("tpss", b1)
+        V, e, _ = srv.wait(srv.submit(sid, cases[0][1]))
+        assert abs(e - direct[0][1]) <= 1e-11
+        assert np.max(np.abs(V - direct[0][0])) <= 1e-11
+        srv.close(sid)
+    finally:
+        srv.shutdown()
+    srv = og.Server(precision=og.MIXED)
+    try:
+        with pytest.raises(og.XCError, match="meta-GGA"):
+            srv.open("tpss", b1)
+    finally:
+        srv.shutdown()
