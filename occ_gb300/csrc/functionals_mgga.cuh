@@ -172,6 +172,59 @@ __device__ __forceinline__ P7 mmax(P7 a, P7 b) { return a.v >= b.v ? a : b; }
 // a, or the constant lo where a < lo (Libxc's zeta threshold)
 __device__ __forceinline__ P7 mfloor(P7 a, double lo) { return a.v >= lo ? a : cst<P7>(lo); }
 
+// ---- the tensor-core path's dual: FP64 value, FP32 derivatives (the value
+// carries the energy; the derivatives feed V_xc, whose tolerance FP32 meets)
+struct MF3 {
+  double v;
+  float r, s, t;
+};
+template <> __device__ __forceinline__ MF3 cst<MF3>(double v) { return {v, 0.f, 0.f, 0.f}; }
+__device__ __forceinline__ MF3 operator+(MF3 a, MF3 b) {
+  return {a.v + b.v, a.r + b.r, a.s + b.s, a.t + b.t};
+}
+__device__ __forceinline__ MF3 operator-(MF3 a, MF3 b) {
+  return {a.v - b.v, a.r - b.r, a.s - b.s, a.t - b.t};
+}
+__device__ __forceinline__ MF3 operator*(MF3 a, MF3 b) {
+  const float av = static_cast<float>(a.v), bv = static_cast<float>(b.v);
+  return {a.v * b.v, fmaf(a.r, bv, av * b.r), fmaf(a.s, bv, av * b.s), fmaf(a.t, bv, av * b.t)};
+}
+__device__ __forceinline__ MF3 operator/(MF3 a, MF3 b) {
+  const double q = a.v / b.v;
+  const float iv = 1.f / static_cast<float>(b.v), qf = static_cast<float>(q);
+  return {q, (a.r - qf * b.r) * iv, (a.s - qf * b.s) * iv, (a.t - qf * b.t) * iv};
+}
+__device__ __forceinline__ MF3 operator*(double c, MF3 a) {
+  const float cf = static_cast<float>(c);
+  return {c * a.v, cf * a.r, cf * a.s, cf * a.t};
+}
+__device__ __forceinline__ MF3 operator+(double c, MF3 a) { return {c + a.v, a.r, a.s, a.t}; }
+__device__ __forceinline__ MF3 operator-(double c, MF3 a) { return {c - a.v, -a.r, -a.s, -a.t}; }
+__device__ __forceinline__ MF3 operator/(double c, MF3 b) {
+  const double q = c / b.v;
+  const float f = -static_cast<float>(q) / static_cast<float>(b.v);
+  return {q, f * b.r, f * b.s, f * b.t};
+}
+__device__ __forceinline__ MF3 chain(MF3 a, double f, float df) {
+  return {f, df * a.r, df * a.s, df * a.t};
+}
+__device__ __forceinline__ MF3 mlog(MF3 a) {
+  return chain(a, log(a.v), 1.f / static_cast<float>(a.v));
+}
+__device__ __forceinline__ MF3 mexp(MF3 a) {
+  const double e = exp(a.v);
+  return chain(a, e, static_cast<float>(e));
+}
+__device__ __forceinline__ MF3 msqrt(MF3 a) {
+  const double q = sqrt(a.v);
+  return chain(a, q, 0.5f / static_cast<float>(q));
+}
+__device__ __forceinline__ MF3 mcbrt(MF3 a) { // a > 0
+  const double c = cbrt(a.v);
+  return chain(a, c, static_cast<float>(c / (3.0 * a.v)));
+}
+__device__ __forceinline__ MF3 mmax(MF3 a, MF3 b) { return a.v >= b.v ? a : b; }
+
 constexpr double kPiM = 3.14159265358979323846;
 constexpr double kK2 = 9.570780000627305;     // (3 pi^2)^(2/3)
 constexpr double kKf = 3.0936677262801355;    // (3 pi^2)^(1/3)
@@ -230,6 +283,7 @@ __device__ __forceinline__ T pw_g(T rs, double A, double a1, double b1, double b
 
 // PBE correlation per particle given the LDA part eps, the spin factor phi
 // (phi^3 = phi3), k_F and n, and |grad n|^2
+template <class M3>
 __device__ __forceinline__ M3 pbe_h(M3 eps, double phi, M3 kf, M3 n, M3 sig) {
   const double beta = 0.06672455060314922, gamma = 0.031090690869654897;
   const double phi3 = phi * phi * phi;
@@ -240,6 +294,7 @@ __device__ __forceinline__ M3 pbe_h(M3 eps, double phi, M3 kf, M3 n, M3 sig) {
   return (gamma * phi3) * mlog(1.0 + (beta / gamma) * t2 * (1.0 + At2) / (1.0 + At2 + At2 * At2));
 }
 
+template <class M3>
 __device__ __forceinline__ M3 tpss_c(M3 rho, M3 sigma, M3 tau, const Pow<M3> &P) {
   // unpolarised PBE
   M3 rs = kRs / P.r13;
@@ -357,6 +412,72 @@ __device__ __forceinline__ void eval_xc_mgga(const FuncSet &fs, double rho, doub
       vrho += c * v.r;
       vsigma += c * v.s;
     }
+  }
+}
+
+// Out-of-line entries for the mixed evaluator's rare paths (kept out of its
+// register allocation).
+static __device__ __noinline__ void eval_xc_mgga_fp64_call(const FuncSet &fs, double rho,
+                                                           double sigma, double tau,
+                                                           double *out4) {
+  eval_xc_mgga(fs, rho, sigma, tau, out4[0], out4[1], out4[2], out4[3]);
+}
+static __device__ __noinline__ void eval_xc_mixed_call(const FuncSet &fs, double rho,
+                                                       double sigma, double *out3) {
+  eval_xc_mixed(fs, rho, sigma, out3[0], out3[1], out3[2]);
+}
+
+// The tensor-core path's evaluator: meta-GGA components with FP64 values and
+// FP32 derivatives (MF3) on the FP64 evaluator's clamped arguments, where
+// rho >= 1e-10 and p = s^2 <= 1e4 (so that the FP32 derivatives of the p^3
+// term stay inside the FP32 range), the FP64 evaluator elsewhere and for any
+// point whose result is not finite; LDA / GGA components through eval_xc_mixed.
+__device__ __forceinline__ void eval_xc_mgga_mixed(const FuncSet &fs, double rho, double sigma,
+                                                   double tau, double &e, double &vrho,
+                                                   double &vsigma, double &vtau) {
+  const double tm = fmax(tau, 1e-20);
+  const double sm = fmin(fmax(sigma, 1e-40), 8.0 * rho * tm);
+  const float rf = static_cast<float>(rho), r13 = cbrtf(rf);
+  const float pf = static_cast<float>(sm) / (38.28312000250922f * rf * rf * r13 * r13);
+  if (!(rho >= 1e-10) || !(pf <= 1e4f)) {
+    double o[4];
+    eval_xc_mgga_fp64_call(fs, rho, sigma, tau, o);
+    e = o[0], vrho = o[1], vsigma = o[2], vtau = o[3];
+    return;
+  }
+  e = vrho = vsigma = vtau = 0.0;
+  bool other = false;
+  for (int i = 0; i < fs.n; i++)
+    other = other || !func_is_mgga(fs.id[i]);
+  if (other) { // the method's LDA / GGA components, as the GGA mixed path evaluates them
+    FuncSet g = fs;
+    g.n = 0;
+    for (int i = 0; i < fs.n; i++)
+      if (!func_is_mgga(fs.id[i])) {
+        g.id[g.n] = fs.id[i];
+        g.coef[g.n++] = fs.coef[i];
+      }
+    double o[3];
+    eval_xc_mixed_call(g, rho, sigma, o);
+    e = o[0], vrho = o[1], vsigma = o[2];
+  }
+  fnm::MF3 r{rho, 1.f, 0.f, 0.f}, s{sm, 0.f, 1.f, 0.f}, t{tm, 0.f, 0.f, 1.f};
+  const fnm::Pow<fnm::MF3> P = fnm::powers(r);
+  for (int i = 0; i < fs.n; i++) {
+    const int id = fs.id[i];
+    if (id != kMggaXTpss && id != kMggaCTpss)
+      continue;
+    const fnm::MF3 v = id == kMggaXTpss ? fnm::tpss_x(r, s, t, P) : fnm::tpss_c(r, s, t, P);
+    const double c = fs.coef[i];
+    e += c * v.v;
+    vrho += c * static_cast<double>(v.r);
+    vsigma += c * static_cast<double>(v.s);
+    vtau += c * static_cast<double>(v.t);
+  }
+  if (!isfinite(e) || !isfinite(vrho) || !isfinite(vsigma) || !isfinite(vtau)) {
+    double o[4]; // an FP32 overflow
+    eval_xc_mgga_fp64_call(fs, rho, sigma, tau, o);
+    e = o[0], vrho = o[1], vsigma = o[2], vtau = o[3];
   }
 }
 

@@ -89,11 +89,12 @@ __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__r
   }
 }
 
-// The meta-GGA functional stage (FP64): rho components 0-3 as for a GGA and
+// The meta-GGA functional stage (MIXED: FP32 derivatives, eval_xc_mgga_mixed): rho components 0-3 as for a GGA and
 // 4-6 the three (d_k phi) D2 (d_k phi) sums, tau = half their sum
 // (src/gto/density.cpp:86-100, include/occ/dft/dft_kernels.h:49-58).
 // Coefficients 0-3 as for a GGA and coef4 = 0.25 w vtau (the V kernel's
 // K + K^T then carries src/dft/xc_potential_matrix.cpp:43-58's 0.5 w vtau).
+template <bool MIXED = false>
 __device__ __forceinline__ void leaf_functional_mgga(const DevLeaf &L,
                                                      const Pt4 *__restrict__ pts, size_t N,
                                                      const FuncSet &fs, double thr,
@@ -115,8 +116,12 @@ __device__ __forceinline__ void leaf_functional_mgga(const DevLeaf &L,
     const double sigma = gx * gx + gy * gy + gz * gz;
     const double tau = 0.5 * (rho[4 * N + idx] + rho[5 * N + idx] + rho[6 * N + idx]);
     double e = 0, vr = 0, vs = 0, vt = 0;
-    if (!skip)
-      eval_xc_mgga(fs, r, sigma, tau, e, vr, vs, vt);
+    if (!skip) {
+      if (MIXED)
+        eval_xc_mgga_mixed(fs, r, sigma, tau, e, vr, vs, vt);
+      else
+        eval_xc_mgga(fs, r, sigma, tau, e, vr, vs, vt);
+    }
     coef[idx] = 0.5 * w * vr;
     const double f = 2.0 * w * vs;
     coef[N + idx] = f * gx;

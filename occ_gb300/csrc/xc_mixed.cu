@@ -2513,7 +2513,7 @@ __global__ void k_selftest_func(FuncSet fs, int n, const double *rho, const doub
   outm[3 * i + 2] = vs;
 }
 __global__ void k_selftest_mgga(FuncSet fs, int n, const double *rho, const double *sigma,
-                                const double *tau, double *out64) {
+                                const double *tau, double *out64, double *outm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
     return;
@@ -2523,24 +2523,29 @@ __global__ void k_selftest_mgga(FuncSet fs, int n, const double *rho, const doub
   out64[4 * i + 1] = vr;
   out64[4 * i + 2] = vs;
   out64[4 * i + 3] = vt;
+  eval_xc_mgga_mixed(fs, rho[i], sigma[i], tau[i], e, vr, vs, vt);
+  outm[4 * i] = e;
+  outm[4 * i + 1] = vr;
+  outm[4 * i + 2] = vs;
+  outm[4 * i + 3] = vt;
 }
 } // namespace
 } // namespace occx
 
-// The meta-GGA evaluator (FP64, the one both precisions' builds use) at n
-// points (host arrays; out64 receives e, vrho, vsigma, vtau per point), for
+// The meta-GGA evaluators (FP64 and the tensor-core path's) at n points
+// (host arrays; out64 / outm receive e, vrho, vsigma, vtau per point), for
 // testing.
 extern "C" int occ_xc_selftest_functional_mgga(occ_xc_context *ctx, const char *method, int n,
                                                const double *rho, const double *sigma,
-                                               const double *tau, double *out64) {
-  if (!ctx || !method || n <= 0 || !rho || !sigma || !tau || !out64)
+                                               const double *tau, double *out64, double *outm) {
+  if (!ctx || !method || n <= 0 || !rho || !sigma || !tau || !out64 || !outm)
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   return api_guard(ctx, [&] {
     const FuncSet fs = parse_method(method);
     cudaStream_t st = ctx->impl->stream;
     double *d = nullptr;
-    const size_t bytes = static_cast<size_t>(n) * 7 * sizeof(double);
+    const size_t bytes = static_cast<size_t>(n) * 11 * sizeof(double);
     cuda_check(cudaMalloc(&d, bytes), "cudaMalloc");
     try {
       const double *src[3] = {rho, sigma, tau};
@@ -2548,10 +2553,13 @@ extern "C" int occ_xc_selftest_functional_mgga(occ_xc_context *ctx, const char *
         cuda_check(cudaMemcpyAsync(d + k * n, src[k], n * sizeof(double), cudaMemcpyHostToDevice,
                                    st),
                    "H2D");
-      k_selftest_mgga<<<(n + 127) / 128, 128, 0, st>>>(fs, n, d, d + n, d + 2 * n, d + 3 * n);
+      k_selftest_mgga<<<(n + 127) / 128, 128, 0, st>>>(fs, n, d, d + n, d + 2 * n, d + 3 * n,
+                                                       d + 7 * n);
       cuda_check(cudaGetLastError(), "kernel launch");
       cuda_check(cudaMemcpyAsync(out64, d + 3 * n, 4 * n * sizeof(double),
                                  cudaMemcpyDeviceToHost, st), "D2H");
+      cuda_check(cudaMemcpyAsync(outm, d + 7 * n, 4 * n * sizeof(double), cudaMemcpyDeviceToHost,
+                                 st), "D2H");
       cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     } catch (...) {
       cudaFree(d);
@@ -3132,7 +3140,7 @@ __global__ void __launch_bounds__(kBlockPts) k_meta_ops(const MixTab *__restrict
   }
 }
 
-// The meta-GGA functional per leaf (FP64), then per block the GGA operand Y
+// The meta-GGA functional per leaf (eval_xc_mgga_mixed), then per block the GGA operand Y
 // (ymix_block) and the tau term's operands c_tau d_k phi (hi, lo).
 __global__ void __launch_bounds__(256, 2) k_func_b_mgga(const MixTab *__restrict__ tabs,
                                                         const MBlock *__restrict__ blocks,
@@ -3142,8 +3150,8 @@ __global__ void __launch_bounds__(256, 2) k_func_b_mgga(const MixTab *__restrict
   __shared__ float ct[kBlockPts];
   const LeafItem li = litems[blockIdx.x];
   const MixTab &T = tabs[li.mol];
-  leaf_functional_mgga(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts), T.fs,
-                       T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
+  leaf_functional_mgga<true>(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts), T.fs,
+                             T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
   __syncthreads(); // the leaf's coefficients are written
   const size_t N = static_cast<size_t>(T.m.npts);
   for (int b = 0; b < li.nblk; b++) {

@@ -67,18 +67,21 @@ def _mgga_points(n, seed):
 
 @pytest.mark.parametrize("method", ["tpss", "mgga_x_tpss gga_c_pbe"])
 def test_mgga_functional_matches_oracle(method):
-    """The GPU's meta-GGA evaluator (FP64 dual numbers) against the oracle's
-    (complex-step derivatives of the spin-polarised form), point by point."""
+    """The GPU's meta-GGA evaluators against the oracle's (complex-step
+    derivatives of the spin-polarised form), point by point: the FP64 one
+    tightly, the tensor-core path's (FP64 values, FP32 derivatives) at FP32
+    accuracy for the derivatives."""
     import oracle
     ctx = _context(0)
     lib = ctx.lib
     lib.occ_xc_selftest_functional_mgga.argtypes = [C.c_void_p, C.c_char_p, C.c_int, _dp, _dp,
-                                                    _dp, _dp]
+                                                    _dp, _dp, _dp]
     n = 20000
     rho, sigma, tau = _mgga_points(n, 11)
     o64 = np.zeros(4 * n)
+    om = np.zeros(4 * n)
     rc = lib.occ_xc_selftest_functional_mgga(ctx.h, method.encode(), n, _ptr(rho), _ptr(sigma),
-                                             _ptr(tau), _ptr(o64))
+                                             _ptr(tau), _ptr(o64), _ptr(om))
     assert rc == 0, ctx.error()
     e64, vr64, vs64, vt64 = (o64[k::4] for k in range(4))
     ids = {"tpss": [202, 231], "mgga_x_tpss gga_c_pbe": [202, 130]}[method]
@@ -105,3 +108,15 @@ def test_mgga_functional_matches_oracle(method):
         err = np.where(free, np.abs(a - b) * x / scale, 0.0)
         i = int(np.argmax(err))
         assert err[i] <= 1e-10, (i, rho[i], sigma[i], tau[i], a[i], b[i])
+    # the tensor-core path's evaluator against the FP64 one
+    em, vrm, vsm, vtm = (om[k::4] for k in range(4))
+    assert np.all(np.isfinite(om))
+    # FP64 values by other roundings (a division for the reciprocal and
+    # product): the GGA evaluators' bounds, 1e-10 a point and no bias
+    rel = (em - e64) / scale
+    assert np.max(np.abs(rel)) <= 1e-10
+    assert abs(np.mean(rel)) <= 1e-13
+    for a, b, x in ((vrm, vr64, rho), (vsm, vs64, sigma), (vtm, vt64, tau)):
+        err = np.where(free, np.abs(a - b) * x / scale, 0.0)
+        i = int(np.argmax(err))
+        assert err[i] <= 1e-5, (i, rho[i], sigma[i], tau[i], a[i], b[i])
