@@ -50,9 +50,10 @@ inline int coef_components(int deriv) { return deriv == 2 ? 5 : deriv ? 4 : 1; }
 // Entry points that have no meta-GGA form throw ArgError for one.
 void require_not_mgga(int deriv, const char *what);
 // the unrestricted build's polarised functional stage and its sums (xc_uks.cu)
+// (mixed: the tensor-core build's evaluator, FP32 derivatives; LDA / GGA)
 void launch_func_pol(const MolDev &m, int deriv, const FuncSet &fs, double thr,
                      const double *rho_a, const double *rho_b, double *coef_a, double *coef_b,
-                     double *epart3, cudaStream_t st);
+                     double *epart3, cudaStream_t st, bool mixed = false);
 void launch_reduce3(const double *epart3, int n, double *out3, cudaStream_t st);
 // Becke partition weights on `device` (xc_grid.cu); fits: the kernel's
 // shared memory holds natom atoms.

@@ -2512,6 +2512,16 @@ __global__ void k_selftest_func(FuncSet fs, int n, const double *rho, const doub
   outm[3 * i + 1] = vr;
   outm[3 * i + 2] = vs;
 }
+__global__ void k_selftest_pol(FuncSet fs, int n, const double *in5, double *out64,
+                               double *outm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const double ra = in5[i], rb = in5[n + i], saa = in5[2 * n + i], sab = in5[3 * n + i],
+               sbb = in5[4 * n + i];
+  eval_xc_pol(fs, ra, rb, saa, sab, sbb, out64[6 * i], out64 + 6 * i + 1, out64 + 6 * i + 3);
+  eval_xc_pol_mixed(fs, ra, rb, saa, sab, sbb, outm[6 * i], outm + 6 * i + 1, outm + 6 * i + 3);
+}
 __global__ void k_selftest_mgga(FuncSet fs, int n, const double *rho, const double *sigma,
                                 const double *tau, double *out64, double *outm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2531,6 +2541,37 @@ __global__ void k_selftest_mgga(FuncSet fs, int n, const double *rho, const doub
 }
 } // namespace
 } // namespace occx
+
+// The polarised evaluators (FP64 and the tensor-core build's) at n points:
+// in5 = rho_a, rho_b, s_aa, s_ab, s_bb (n each); out64 / outm receive e,
+// vrho_a, vrho_b, vs_aa, vs_ab, vs_bb per point.  For testing.
+extern "C" int occ_xc_selftest_functional_pol(occ_xc_context *ctx, const char *method, int n,
+                                              const double *in5, double *out64, double *outm) {
+  if (!ctx || !method || n <= 0 || !in5 || !out64 || !outm)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return api_guard(ctx, [&] {
+    const FuncSet fs = parse_method(method);
+    cudaStream_t st = ctx->impl->stream;
+    double *d = nullptr;
+    cuda_check(cudaMalloc(&d, static_cast<size_t>(n) * 17 * sizeof(double)), "cudaMalloc");
+    try {
+      cuda_check(cudaMemcpyAsync(d, in5, 5 * static_cast<size_t>(n) * sizeof(double),
+                                 cudaMemcpyHostToDevice, st), "H2D");
+      k_selftest_pol<<<(n + 127) / 128, 128, 0, st>>>(fs, n, d, d + 5 * n, d + 11 * n);
+      cuda_check(cudaGetLastError(), "kernel launch");
+      cuda_check(cudaMemcpyAsync(out64, d + 5 * n, 6 * static_cast<size_t>(n) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, st), "D2H");
+      cuda_check(cudaMemcpyAsync(outm, d + 11 * n, 6 * static_cast<size_t>(n) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, st), "D2H");
+      cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    } catch (...) {
+      cudaFree(d);
+      throw;
+    }
+    cudaFree(d);
+  });
+}
 
 // The meta-GGA evaluators (FP64 and the tensor-core path's) at n points
 // (host arrays; out64 / outm receive e, vrho, vsigma, vtau per point), for
@@ -3025,7 +3066,7 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
   const MolDev m = dev();
   c.launch("func_pol", st, [&] {
     launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
-                    d_epart_u, st);
+                    d_epart_u, st, true);
   });
   for (int s = 0; s < 2 && nb > 0; s++) {
     c.launch("ymix", st, [&] {

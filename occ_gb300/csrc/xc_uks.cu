@@ -29,7 +29,8 @@ namespace {
 
 // One CTA of 256 threads per leaf.  epart3 receives {sum w e, sum w rho_a,
 // sum w rho_b} (the densities also for a skipped leaf, as OCC's totals).
-template <bool DERIV>
+// MIXED: the tensor-core build's evaluator (FP32 derivatives).
+template <bool DERIV, bool MIXED>
 __global__ void __launch_bounds__(256)
     k_func_pol(MolDev m, FuncSet fs, double thr, const double *__restrict__ rho_a,
                const double *__restrict__ rho_b, double *__restrict__ coef_a,
@@ -64,8 +65,12 @@ __global__ void __launch_bounds__(256)
       sbb = gb[0] * gb[0] + gb[1] * gb[1] + gb[2] * gb[2];
     }
     double e = 0.0, vr[2] = {0.0, 0.0}, vs[3] = {0.0, 0.0, 0.0};
-    if (!skip)
-      eval_xc_pol(fs, ra, rb, saa, sab, sbb, e, vr, vs);
+    if (!skip) {
+      if (MIXED)
+        eval_xc_pol_mixed(fs, ra, rb, saa, sab, sbb, e, vr, vs);
+      else
+        eval_xc_pol(fs, ra, rb, saa, sab, sbb, e, vr, vs);
+    }
     coef_a[idx] = 0.5 * w * vr[0];
     coef_b[idx] = 0.5 * w * vr[1];
     if (DERIV) {
@@ -168,17 +173,21 @@ __global__ void __launch_bounds__(256) k_reduce3(const double *__restrict__ epar
 
 void launch_func_pol(const MolDev &m, int deriv, const FuncSet &fs, double thr,
                      const double *rho_a, const double *rho_b, double *coef_a, double *coef_b,
-                     double *epart3, cudaStream_t st) {
+                     double *epart3, cudaStream_t st, bool mixed) {
   if (m.nleaves == 0)
     return;
+  const dim3 g(m.nleaves);
   if (deriv == 2)
-    k_func_pol_mgga<<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b,
-                                              epart3);
+    k_func_pol_mgga<<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
+  else if (deriv && mixed)
+    k_func_pol<true, true><<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
   else if (deriv)
-    k_func_pol<true><<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
+    k_func_pol<true, false><<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
+  else if (mixed)
+    k_func_pol<false, true><<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
   else
-    k_func_pol<false><<<m.nleaves, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b,
-                                                 epart3);
+    k_func_pol<false, false><<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b,
+                                                epart3);
 }
 
 void launch_reduce3(const double *epart3, int n, double *out3, cudaStream_t st) {
