@@ -1,4 +1,4 @@
-// Meta-GGA functionals (unpolarised), FP64 per grid point: TPSS exchange and
+// Meta-GGA functionals per grid point: TPSS exchange and
 // correlation, the Libxc 6.2.2 functionals mgga_x_tpss (id 202) and
 // mgga_c_tpss (id 231) of OCC's "tpss" method (share/methods/dft_methods.json;
 // evaluated through src/dft/functional.cpp:49-58 with rho, sigma, laplacian,
@@ -14,7 +14,9 @@
 //   where eps_PBE(rho/2, 0; sigma/4) is PBE correlation of the fully
 //   polarised density rho/2 (PW92 ferromagnetic fit, phi = phi(zeta = 1)).
 // Neither reads the laplacian.  Derivatives by forward-mode dual numbers over
-// (rho, sigma, tau).  Thresholds: as for the GGAs the point is zero below
+// (rho, sigma, tau): M3 (FP64) for the FP64 build, MF3 (FP64 value, FP32
+// derivatives) for the tensor-core build; the spin-polarised form (general
+// zeta, for the UKS builds) over seven variables in P7 (FP64).  Thresholds: as for the GGAs the point is zero below
 // rho = 1e-15; tau >= 1e-20, sigma >= 1e-40, and sigma is clamped to
 // 8 rho tau (z <= 1) before evaluation, as Libxc does for meta-GGAs.
 #pragma once

@@ -14,9 +14,13 @@
 // (and a <-> b with vs_bb), E_xc = sum w e.  Here each spin's V is the FP64
 // path's K + K^T with Y = 0.5 w vrho_s phi + c_s . grad phi, so the density
 // and potential kernels of the restricted build run once per spin on the
-// same resident AO values; only the functional stage is new (k_func_pol).
-// The tensor-core form (Molecule::build_mixed_uks, xc_mixed.cu) runs the
-// mixed density and potential kernels once per spin in the same way.
+// same resident AO values; only the functional stage is new (k_func_pol,
+// FP64 here; with FP32 derivatives in the tensor-core build).  A meta-GGA adds
+// per spin the tau densities (k_rho_f64's tau mode), the polarised TPSS
+// (k_func_pol_mgga, eval_xc_mgga_pol) and the tau segments of k_vxc_f64.
+// The tensor-core forms (Molecule::build_mixed_uks and build_mixed_uks_mgga,
+// xc_mixed.cu) run the mixed density and potential kernels once per spin in
+// the same way.
 #include "functionals_mgga.cuh"
 #include "functionals_pol.cuh"
 #include "xc_device.cuh"
