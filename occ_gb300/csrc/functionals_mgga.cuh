@@ -84,95 +84,116 @@ __device__ __forceinline__ M3 mcbrt(M3 a) { // a > 0
 }
 __device__ __forceinline__ M3 mmax(M3 a, M3 b) { return a.v >= b.v ? a : b; }
 
-// ---- the polarised form's dual: d/d rho_a, rho_b, s_aa, s_ab, s_bb, tau_a, tau_b
+// ---- the polarised form's dual: d/d rho_a, rho_b, s_aa, s_ab, s_bb, tau_a,
+// tau_b in D (double: the FP64 build; float: the tensor-core build)
 constexpr int kN7 = 7;
-struct P7 {
-  double v, d[kN7];
+template <class D> struct Q7 {
+  double v;
+  D d[kN7];
 };
-template <> __device__ __forceinline__ P7 cst<P7>(double v) {
-  P7 r;
+using P7 = Q7<double>;
+template <class D> __device__ __forceinline__ Q7<D> cst7(double v) {
+  Q7<D> r;
   r.v = v;
 #pragma unroll
   for (int i = 0; i < kN7; i++)
-    r.d[i] = 0.0;
+    r.d[i] = D(0);
   return r;
 }
-__device__ __forceinline__ P7 var7(double v, int k) {
-  P7 r = cst<P7>(v);
-  r.d[k] = 1.0;
+template <> __device__ __forceinline__ P7 cst<P7>(double v) { return cst7<double>(v); }
+template <> __device__ __forceinline__ Q7<float> cst<Q7<float>>(double v) {
+  return cst7<float>(v);
+}
+template <class D> __device__ __forceinline__ Q7<D> var7(double v, int k) {
+  Q7<D> r = cst7<D>(v);
+  r.d[k] = D(1);
   return r;
 }
-__device__ __forceinline__ P7 operator+(P7 a, P7 b) {
-  P7 r;
+template <class D> __device__ __forceinline__ Q7<D> operator+(Q7<D> a, Q7<D> b) {
+  Q7<D> r;
   r.v = a.v + b.v;
 #pragma unroll
   for (int i = 0; i < kN7; i++)
     r.d[i] = a.d[i] + b.d[i];
   return r;
 }
-__device__ __forceinline__ P7 operator-(P7 a, P7 b) {
-  P7 r;
+template <class D> __device__ __forceinline__ Q7<D> operator-(Q7<D> a, Q7<D> b) {
+  Q7<D> r;
   r.v = a.v - b.v;
 #pragma unroll
   for (int i = 0; i < kN7; i++)
     r.d[i] = a.d[i] - b.d[i];
   return r;
 }
-__device__ __forceinline__ P7 operator*(P7 a, P7 b) {
-  P7 r;
+template <class D> __device__ __forceinline__ Q7<D> operator*(Q7<D> a, Q7<D> b) {
+  Q7<D> r;
   r.v = a.v * b.v;
+  const D av = static_cast<D>(a.v), bv = static_cast<D>(b.v);
 #pragma unroll
   for (int i = 0; i < kN7; i++)
-    r.d[i] = fma(a.d[i], b.v, a.v * b.d[i]);
+    r.d[i] = fma(a.d[i], bv, av * b.d[i]);
   return r;
 }
-__device__ __forceinline__ P7 operator/(P7 a, P7 b) {
+template <class D> __device__ __forceinline__ Q7<D> operator/(Q7<D> a, Q7<D> b) {
   const double inv = 1.0 / b.v, q = a.v * inv;
-  P7 r;
+  Q7<D> r;
   r.v = q;
+  const D qd = static_cast<D>(q), ivd = static_cast<D>(inv);
 #pragma unroll
   for (int i = 0; i < kN7; i++)
-    r.d[i] = (a.d[i] - q * b.d[i]) * inv;
+    r.d[i] = (a.d[i] - qd * b.d[i]) * ivd;
   return r;
 }
-__device__ __forceinline__ P7 operator*(double c, P7 a) {
-  P7 r;
+template <class D> __device__ __forceinline__ Q7<D> operator*(double c, Q7<D> a) {
+  Q7<D> r;
   r.v = c * a.v;
+  const D cd = static_cast<D>(c);
 #pragma unroll
   for (int i = 0; i < kN7; i++)
-    r.d[i] = c * a.d[i];
+    r.d[i] = cd * a.d[i];
   return r;
 }
-__device__ __forceinline__ P7 operator+(double c, P7 a) {
+template <class D> __device__ __forceinline__ Q7<D> operator+(double c, Q7<D> a) {
   a.v += c;
   return a;
 }
-__device__ __forceinline__ P7 operator-(double c, P7 a) { return cst<P7>(c) - a; }
-__device__ __forceinline__ P7 operator/(double c, P7 b) { return cst<P7>(c) / b; }
-__device__ __forceinline__ P7 chain(P7 a, double f, double df) {
-  P7 r;
+template <class D> __device__ __forceinline__ Q7<D> operator-(double c, Q7<D> a) {
+  return cst7<D>(c) - a;
+}
+template <class D> __device__ __forceinline__ Q7<D> operator/(double c, Q7<D> b) {
+  return cst7<D>(c) / b;
+}
+template <class D> __device__ __forceinline__ Q7<D> chain(Q7<D> a, double f, double df) {
+  Q7<D> r;
   r.v = f;
+  const D dd = static_cast<D>(df);
 #pragma unroll
   for (int i = 0; i < kN7; i++)
-    r.d[i] = df * a.d[i];
+    r.d[i] = dd * a.d[i];
   return r;
 }
-__device__ __forceinline__ P7 mlog(P7 a) { return chain(a, log(a.v), 1.0 / a.v); }
-__device__ __forceinline__ P7 mexp(P7 a) {
+template <class D> __device__ __forceinline__ Q7<D> mlog(Q7<D> a) {
+  return chain(a, log(a.v), 1.0 / a.v);
+}
+template <class D> __device__ __forceinline__ Q7<D> mexp(Q7<D> a) {
   const double e = exp(a.v);
   return chain(a, e, e);
 }
-__device__ __forceinline__ P7 msqrt(P7 a) {
+template <class D> __device__ __forceinline__ Q7<D> msqrt(Q7<D> a) {
   const double q = sqrt(a.v);
   return chain(a, q, 0.5 / q);
 }
-__device__ __forceinline__ P7 mcbrt(P7 a) { // a > 0
+template <class D> __device__ __forceinline__ Q7<D> mcbrt(Q7<D> a) { // a > 0
   const double c = cbrt(a.v);
   return chain(a, c, c / (3.0 * a.v));
 }
-__device__ __forceinline__ P7 mmax(P7 a, P7 b) { return a.v >= b.v ? a : b; }
+template <class D> __device__ __forceinline__ Q7<D> mmax(Q7<D> a, Q7<D> b) {
+  return a.v >= b.v ? a : b;
+}
 // a, or the constant lo where a < lo (Libxc's zeta threshold)
-__device__ __forceinline__ P7 mfloor(P7 a, double lo) { return a.v >= lo ? a : cst<P7>(lo); }
+template <class D> __device__ __forceinline__ Q7<D> mfloor(Q7<D> a, double lo) {
+  return a.v >= lo ? a : cst7<D>(lo);
+}
 
 // ---- the tensor-core path's dual: FP64 value, FP32 derivatives (the value
 // carries the energy; the derivatives feed V_xc, whose tolerance FP32 meets)
@@ -315,10 +336,10 @@ __device__ __forceinline__ M3 tpss_c(M3 rho, M3 sigma, M3 tau, const Pow<M3> &P)
   return rho * erev * (1.0 + 2.8 * erev * z2 * z);
 }
 
-// ---- spin-polarised TPSS (the UKS build), over P7
+// ---- spin-polarised TPSS (the UKS builds), over Q7<double> or Q7<float>
 // PBE correlation per particle of spin densities (ra, rb) with total
 // |grad rho|^2 = sig: PW92's spin interpolation and phi(zeta)
-__device__ __forceinline__ P7 pbe_eps_pol(P7 ra, P7 rb, P7 sig) {
+template <class P7> __device__ __forceinline__ P7 pbe_eps_pol(P7 ra, P7 rb, P7 sig) {
   const double beta = 0.06672455060314922, gamma = 0.031090690869654897;
   const double fpp0 = 1.7099209341613657, eps_z = 2.220446049250313e-16;
   P7 n = ra + rb;
@@ -344,12 +365,13 @@ __device__ __forceinline__ P7 pbe_eps_pol(P7 ra, P7 rb, P7 sig) {
 }
 
 // TPSS exchange of one spin channel: E_x[2 rho_s, 4 s_ss, 2 tau_s] / 2
-__device__ __forceinline__ P7 tpss_x_s(P7 r, P7 s, P7 t) {
+template <class P7> __device__ __forceinline__ P7 tpss_x_s(P7 r, P7 s, P7 t) {
   const P7 n = 2.0 * r;
   return 0.5 * tpss_x(n, 4.0 * s, 2.0 * t, powers(n));
 }
 
 // revPKZB / TPSS correlation (eqs. 11-14) of a polarised density
+template <class P7>
 __device__ __forceinline__ P7 tpss_c_pol(P7 ra, P7 rb, P7 saa, P7 sab, P7 sbb, P7 ta, P7 tb,
                                          bool sa, bool sb) {
   const double eps_z = 2.220446049250313e-16;
@@ -483,35 +505,22 @@ __device__ __forceinline__ void eval_xc_mgga_mixed(const FuncSet &fs, double rho
   }
 }
 
-// One point of a polarised meta-GGA method: e and vrho[2], vsigma[3],
-// vtau[2].  Meta-GGA components on the clamped arguments Libxc uses (tau_s >=
-// 1e-20, s_ss <= 8 rho_s tau_s, |s_ab| <= (s_aa + s_bb) / 2), the method's
-// LDA / GGA components through eval_xc_pol on the arguments as given.
-__device__ __forceinline__ void eval_xc_mgga_pol(const FuncSet &fs, double ra, double rb,
-                                                 double saa, double sab, double sbb, double ta,
-                                                 double tb, double &e, double *vrho,
-                                                 double *vsig, double *vtau) {
-  eval_xc_pol(fs, ra, rb, saa, sab, sbb, e, vrho, vsig); // its switch skips meta-GGA ids
-  vtau[0] = vtau[1] = 0.0;
-  ra = fmax(ra, 0.0);
-  rb = fmax(rb, 0.0);
-  if (!(ra + rb >= 1e-15))
-    return;
-  ta = fmax(ta, 1e-20);
-  tb = fmax(tb, 1e-20);
-  saa = fmin(fmax(saa, 1e-40), 8.0 * ra * ta);
-  sbb = fmin(fmax(sbb, 1e-40), 8.0 * rb * tb);
-  const double lim = 0.5 * (saa + sbb);
-  sab = fmin(fmax(sab, -lim), lim);
-  using fnm::P7;
-  const P7 Ra = fnm::var7(ra, 0), Rb = fnm::var7(rb, 1), Saa = fnm::var7(saa, 2),
-           Sab = fnm::var7(sab, 3), Sbb = fnm::var7(sbb, 4), Ta = fnm::var7(ta, 5),
-           Tb = fnm::var7(tb, 6);
+// The meta-GGA components of a polarised method in Q7<D>, on arguments
+// already clamped as Libxc clamps them (tau_s >= 1e-20, s_ss <= 8 rho_s tau_s,
+// |s_ab| <= (s_aa + s_bb) / 2).
+template <class D>
+__device__ __forceinline__ fnm::Q7<D> mgga_pol_sum(const FuncSet &fs, double ra, double rb,
+                                                   double saa, double sab, double sbb,
+                                                   double ta, double tb) {
+  using Q = fnm::Q7<D>;
+  const Q Ra = fnm::var7<D>(ra, 0), Rb = fnm::var7<D>(rb, 1), Saa = fnm::var7<D>(saa, 2),
+          Sab = fnm::var7<D>(sab, 3), Sbb = fnm::var7<D>(sbb, 4), Ta = fnm::var7<D>(ta, 5),
+          Tb = fnm::var7<D>(tb, 6);
   const bool sa = ra >= 1e-15, sb = rb >= 1e-15;
-  P7 tot = fnm::cst<P7>(0.0);
+  Q tot = fnm::cst7<D>(0.0);
   for (int i = 0; i < fs.n; i++) {
     if (fs.id[i] == kMggaXTpss) {
-      P7 x = fnm::cst<P7>(0.0);
+      Q x = fnm::cst7<D>(0.0);
       if (sa)
         x = x + fnm::tpss_x_s(Ra, Saa, Ta);
       if (sb)
@@ -521,14 +530,89 @@ __device__ __forceinline__ void eval_xc_mgga_pol(const FuncSet &fs, double ra, d
       tot = tot + fs.coef[i] * fnm::tpss_c_pol(Ra, Rb, Saa, Sab, Sbb, Ta, Tb, sa, sb);
     }
   }
-  e += tot.v;
-  vrho[0] += tot.d[0];
-  vrho[1] += tot.d[1];
-  vsig[0] += tot.d[2];
-  vsig[1] += tot.d[3];
-  vsig[2] += tot.d[4];
-  vtau[0] = tot.d[5];
-  vtau[1] = tot.d[6];
+  return tot;
+}
+
+// Libxc's clamps of the meta-GGA arguments; false below the density threshold
+__device__ __forceinline__ bool mgga_pol_clamp(double &ra, double &rb, double &saa, double &sab,
+                                               double &sbb, double &ta, double &tb) {
+  ra = fmax(ra, 0.0);
+  rb = fmax(rb, 0.0);
+  if (!(ra + rb >= 1e-15))
+    return false;
+  ta = fmax(ta, 1e-20);
+  tb = fmax(tb, 1e-20);
+  saa = fmin(fmax(saa, 1e-40), 8.0 * ra * ta);
+  sbb = fmin(fmax(sbb, 1e-40), 8.0 * rb * tb);
+  const double lim = 0.5 * (saa + sbb);
+  sab = fmin(fmax(sab, -lim), lim);
+  return true;
+}
+
+template <class D>
+__device__ __forceinline__ void mgga_pol_add(const fnm::Q7<D> &t, double &e, double *vrho,
+                                             double *vsig, double *vtau) {
+  e += t.v;
+  vrho[0] += t.d[0];
+  vrho[1] += t.d[1];
+  vsig[0] += t.d[2];
+  vsig[1] += t.d[3];
+  vsig[2] += t.d[4];
+  vtau[0] = t.d[5];
+  vtau[1] = t.d[6];
+}
+
+// One point of a polarised meta-GGA method: e and vrho[2], vsigma[3],
+// vtau[2], FP64.  Meta-GGA components on the clamped arguments, the method's
+// LDA / GGA components through eval_xc_pol on the arguments as given.
+__device__ __forceinline__ void eval_xc_mgga_pol(const FuncSet &fs, double ra, double rb,
+                                                 double saa, double sab, double sbb, double ta,
+                                                 double tb, double &e, double *vrho,
+                                                 double *vsig, double *vtau) {
+  eval_xc_pol(fs, ra, rb, saa, sab, sbb, e, vrho, vsig); // its switch skips meta-GGA ids
+  vtau[0] = vtau[1] = 0.0;
+  if (mgga_pol_clamp(ra, rb, saa, sab, sbb, ta, tb))
+    mgga_pol_add(mgga_pol_sum<double>(fs, ra, rb, saa, sab, sbb, ta, tb), e, vrho, vsig, vtau);
+}
+
+static __device__ __noinline__ void eval_xc_mgga_pol_fp64_call(const FuncSet &fs, double ra,
+                                                               double rb, double saa,
+                                                               double sab, double sbb,
+                                                               double ta, double tb,
+                                                               double *out8) {
+  eval_xc_mgga_pol(fs, ra, rb, saa, sab, sbb, ta, tb, out8[0], out8 + 1, out8 + 3, out8 + 6);
+}
+
+// The tensor-core UKS build's evaluator: FP64 values with FP32 derivatives
+// where both spin densities are >= 1e-10 and each channel's p = s^2 <= 1e4
+// (the FP32 derivatives of TPSS exchange's p^3 term stay in range), the FP64
+// evaluator elsewhere and for any point whose result is not finite.
+__device__ __forceinline__ void eval_xc_mgga_pol_mixed(const FuncSet &fs, double ra, double rb,
+                                                       double saa, double sab, double sbb,
+                                                       double ta, double tb, double &e,
+                                                       double *vrho, double *vsig,
+                                                       double *vtau) {
+  const double ra0 = ra, rb0 = rb, saa0 = saa, sab0 = sab, sbb0 = sbb, ta0 = ta, tb0 = tb;
+  bool fast = ra >= 1e-10 && rb >= 1e-10 && mgga_pol_clamp(ra, rb, saa, sab, sbb, ta, tb);
+  if (fast) { // p of each channel (exchange of 2 rho_s, 4 s_ss)
+    const float a = static_cast<float>(2.0 * ra), b = static_cast<float>(2.0 * rb);
+    const float a13 = cbrtf(a), b13 = cbrtf(b);
+    fast = static_cast<float>(4.0 * saa) / (38.28312000250922f * a * a * a13 * a13) <= 1e4f &&
+           static_cast<float>(4.0 * sbb) / (38.28312000250922f * b * b * b13 * b13) <= 1e4f;
+  }
+  if (fast) {
+    eval_xc_pol_mixed(fs, ra0, rb0, saa0, sab0, sbb0, e, vrho, vsig);
+    vtau[0] = vtau[1] = 0.0;
+    mgga_pol_add(mgga_pol_sum<float>(fs, ra, rb, saa, sab, sbb, ta, tb), e, vrho, vsig, vtau);
+    fast = isfinite(e) && isfinite(vrho[0]) && isfinite(vrho[1]) && isfinite(vsig[0]) &&
+           isfinite(vsig[1]) && isfinite(vsig[2]) && isfinite(vtau[0]) && isfinite(vtau[1]);
+  }
+  if (!fast) {
+    double o[8];
+    eval_xc_mgga_pol_fp64_call(fs, ra0, rb0, saa0, sab0, sbb0, ta0, tb0, o);
+    e = o[0], vrho[0] = o[1], vrho[1] = o[2], vsig[0] = o[3], vsig[1] = o[4], vsig[2] = o[5];
+    vtau[0] = o[6], vtau[1] = o[7];
+  }
 }
 
 } // namespace occx

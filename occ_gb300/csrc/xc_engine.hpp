@@ -50,7 +50,7 @@ inline int coef_components(int deriv) { return deriv == 2 ? 5 : deriv ? 4 : 1; }
 // Entry points that have no meta-GGA form throw ArgError for one.
 void require_not_mgga(int deriv, const char *what);
 // the unrestricted build's polarised functional stage and its sums (xc_uks.cu)
-// (mixed: the tensor-core build's evaluator, FP32 derivatives; LDA / GGA)
+// (mixed: the tensor-core build's evaluators, FP32 derivatives)
 void launch_func_pol(const MolDev &m, int deriv, const FuncSet &fs, double thr,
                      const double *rho_a, const double *rho_b, double *coef_a, double *coef_b,
                      double *epart3, cudaStream_t st, bool mixed = false);

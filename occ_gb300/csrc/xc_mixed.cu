@@ -3404,7 +3404,7 @@ void Molecule::build_mixed_uks_mgga(const double *dD, double *dV, double *dout3,
   const MolDev m = dev();
   c.launch("func_pol", st, [&] {
     launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
-                    d_epart_u, st);
+                    d_epart_u, st, true);
   });
   const VxcPlanes *pls = kMetaVxcPlanes;
   for (int s = 0; s < 2 && nb > 0; s++) {

@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(256)
 // each spin hold its (d_k phi) D2_s (d_k phi) sums, tau_s = half their sum
 // (src/gto/density.cpp:104-166); coef4 of each spin = 0.25 w vtau_s, so that
 // the V kernel's K + K^T carries xc_potential_matrix.cpp:110-136's 0.5 w vtau_s.
+template <bool MIXED>
 __global__ void __launch_bounds__(256)
     k_func_pol_mgga(MolDev m, FuncSet fs, double thr, const double *__restrict__ rho_a,
                     const double *__restrict__ rho_b, double *__restrict__ coef_a,
@@ -133,8 +134,12 @@ __global__ void __launch_bounds__(256)
     const double ta = 0.5 * (rho_a[4 * N + idx] + rho_a[5 * N + idx] + rho_a[6 * N + idx]);
     const double tb = 0.5 * (rho_b[4 * N + idx] + rho_b[5 * N + idx] + rho_b[6 * N + idx]);
     double e = 0.0, vr[2] = {0.0, 0.0}, vs[3] = {0.0, 0.0, 0.0}, vt[2] = {0.0, 0.0};
-    if (!skip)
-      eval_xc_mgga_pol(fs, ra, rb, saa, sab, sbb, ta, tb, e, vr, vs, vt);
+    if (!skip) {
+      if (MIXED)
+        eval_xc_mgga_pol_mixed(fs, ra, rb, saa, sab, sbb, ta, tb, e, vr, vs, vt);
+      else
+        eval_xc_mgga_pol(fs, ra, rb, saa, sab, sbb, ta, tb, e, vr, vs, vt);
+    }
     coef_a[idx] = 0.5 * w * vr[0];
     coef_b[idx] = 0.5 * w * vr[1];
 #pragma unroll
@@ -181,8 +186,10 @@ void launch_func_pol(const MolDev &m, int deriv, const FuncSet &fs, double thr,
   if (m.nleaves == 0)
     return;
   const dim3 g(m.nleaves);
-  if (deriv == 2)
-    k_func_pol_mgga<<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
+  if (deriv == 2 && mixed)
+    k_func_pol_mgga<true><<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
+  else if (deriv == 2)
+    k_func_pol_mgga<false><<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
   else if (deriv && mixed)
     k_func_pol<true, true><<<g, 256, 0, st>>>(m, fs, thr, rho_a, rho_b, coef_a, coef_b, epart3);
   else if (deriv)
