@@ -161,7 +161,7 @@ public:
   // fixed; 3 * natoms values, x, y, z per atom (the memory of OCC's
   // 3 x natoms Mat3N).  Also sets exchange_correlation_energy().
   // As compute_vxc, the size of D decides: nbf x nbf restricted, 2 nbf x nbf
-  // (OCC's unrestricted mo.D) unrestricted (FP64).
+  // (OCC's unrestricted mo.D) unrestricted.
   std::vector<double> compute_xc_gradient(const std::vector<double> &D,
                                           Precision precision = Precision::FP64) {
     std::vector<double> g(3 * natoms_);

@@ -369,6 +369,17 @@ def uks_build(torch, steps=5, warmup=2, waters=32, seed=0):
     out["abs_dE_mixed_vs_fp64"] = abs(res["mixed"][0] - res["fp64"][0])
     out["max_abs_dV_mixed_vs_fp64"] = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1])))
     out["e2e"] = out["mixed"]["e2e"]
+    # the unrestricted XC gradient (host entry point), both precisions
+    grads = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        dft.compute_xc_gradient(D, prec)
+        t0 = time.perf_counter()
+        for _ in range(2):
+            grads[name] = dft.compute_xc_gradient(D, prec)
+        out.setdefault("gradient", {})[name] = {
+            "gradients_per_s": 2.0 / (time.perf_counter() - t0)}
+    out["gradient"]["max_abs_dg_mixed_vs_fp64"] = float(
+        np.max(np.abs(grads["mixed"] - grads["fp64"])))
     return out
 
 

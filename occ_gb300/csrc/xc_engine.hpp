@@ -247,6 +247,8 @@ struct Molecule {
   void xc_gradient(const double *dD, double *dgrad, double *dout2, cudaStream_t st);
   // the same for OCC's unrestricted mo.D (2 nbf x nbf); dout3 = {E_xc, rho_a, rho_b}
   void xc_gradient_uks(const double *dD, double *dgrad, double *dout3, cudaStream_t st);
+  // ... with the contractions on the tensor cores (LDA / GGA)
+  void xc_gradient_uks_mixed(const double *dD, double *dgrad, double *dout3, cudaStream_t st);
 };
 
 // Host part of a molecule: basis, molecular grid, Morton leaves and screening

@@ -638,16 +638,26 @@ int occ_xc_compute_xc_gradient_unrestricted(occ_xc_context *ctx, occ_xc_molecule
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   return guarded(ctx, [&] {
-    if (precision != OCC_XC_FP64)
-      throw ArgError("the unrestricted XC gradient is built in FP64 (OCC_XC_FP64) only");
+    if (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED)
+      throw ArgError("precision must be OCC_XC_FP64 or OCC_XC_MIXED");
     Molecule &M = *mol->impl;
     cudaStream_t st = ctx->impl->stream;
-    M.prepare_gradient();
+    if (precision == OCC_XC_MIXED) {
+      M.prepare_gradient_mixed();
+      if (!M.d_grad)
+        M.d_grad = static_cast<double *>(M.alloc(std::max<size_t>(3 * M.Z.size(), 1) *
+                                                 sizeof(double)));
+    } else {
+      M.prepare_gradient();
+    }
     M.prepare_uks();
     const size_t n2 = 2 * static_cast<size_t>(M.basis.nbf) * M.basis.nbf;
     cuda_check(cudaMemcpyAsync(M.d_Duks, D, n2 * sizeof(double), cudaMemcpyHostToDevice, st),
                "cudaMemcpyAsync H2D");
-    M.xc_gradient_uks(M.d_Duks, M.d_grad, M.d_out3, st);
+    if (precision == OCC_XC_MIXED)
+      M.xc_gradient_uks_mixed(M.d_Duks, M.d_grad, M.d_out3, st);
+    else
+      M.xc_gradient_uks(M.d_Duks, M.d_grad, M.d_out3, st);
     double out3[3];
     cuda_check(cudaMemcpyAsync(grad, M.d_grad, 3 * M.Z.size() * sizeof(double),
                                cudaMemcpyDeviceToHost, st),
@@ -655,6 +665,8 @@ int occ_xc_compute_xc_gradient_unrestricted(occ_xc_context *ctx, occ_xc_molecule
     cuda_check(cudaMemcpyAsync(out3, M.d_out3, sizeof(out3), cudaMemcpyDeviceToHost, st),
                "cudaMemcpyAsync D2H");
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (precision == OCC_XC_MIXED && mixed_error_flag(M, st))
+      throw TimeoutError("a bounded wait of the tensor-core pipeline gave up");
     if (exc)
       *exc = out3[0];
   });
@@ -668,11 +680,14 @@ int occ_xc_compute_xc_gradient_unrestricted_device(occ_xc_context *ctx, occ_xc_m
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   return guarded(ctx, [&] {
-    if (precision != OCC_XC_FP64)
-      throw ArgError("the unrestricted XC gradient is built in FP64 (OCC_XC_FP64) only");
+    if (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED)
+      throw ArgError("precision must be OCC_XC_FP64 or OCC_XC_MIXED");
     Molecule &M = *mol->impl;
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
-    M.xc_gradient_uks(d_D, d_grad, d_exc3 ? d_exc3 : M.d_out3, st);
+    if (precision == OCC_XC_MIXED)
+      M.xc_gradient_uks_mixed(d_D, d_grad, d_exc3 ? d_exc3 : M.d_out3, st);
+    else
+      M.xc_gradient_uks(d_D, d_grad, d_exc3 ? d_exc3 : M.d_out3, st);
   });
 }
 

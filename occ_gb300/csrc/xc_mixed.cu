@@ -2854,7 +2854,8 @@ __global__ void __launch_bounds__(128) k_grad_ops(const MixTab *__restrict__ tab
 __global__ void __launch_bounds__(256) k_grad_contract(const double *__restrict__ D,
                                                        const double *__restrict__ G, int nbf,
                                                        const int *__restrict__ ao_atom,
-                                                       double *__restrict__ grad) {
+                                                       double *__restrict__ grad,
+                                                       const double *__restrict__ Dot) {
   __shared__ double sh[8];
   const int mu = blockIdx.x;
   const size_t n2 = static_cast<size_t>(nbf) * nbf;
@@ -2862,7 +2863,8 @@ __global__ void __launch_bounds__(256) k_grad_contract(const double *__restrict_
   for (int nu = threadIdx.x; nu < nbf; nu += 256) {
     const size_t o = static_cast<size_t>(nu) * nbf + mu;
     const double d4 = 4.0 * D[o];
-    if (fabs(d4) < 1e-12)
+    // the reference's skip: |4 D| restricted, |2 (D_a + D_b)| unrestricted
+    if (fabs(Dot ? 2.0 * (D[o] + Dot[o]) : d4) < 1e-12)
       continue;
 #pragma unroll
     for (int c = 0; c < 3; c++)
@@ -2884,6 +2886,7 @@ struct GradMixed {
   LaunchPlan plan;
   double *G = nullptr;
   int *ao_atom = nullptr;
+  void *d_tab_b = nullptr; // the plan's table with the beta rho / coef arrays (UKS)
 };
 
 void free_grad_mixed(GradMixed *g) { delete g; }
@@ -2985,7 +2988,7 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
   cuda_check(cudaMemsetAsync(dgrad, 0, 3 * Z.size() * sizeof(double), st), "cudaMemsetAsync");
   c.launch("grad_contract", st, [&] {
     if (basis.nbf > 0)
-      k_grad_contract<<<basis.nbf, 256, 0, st>>>(dD, g.G, basis.nbf, g.ao_atom, dgrad);
+      k_grad_contract<<<basis.nbf, 256, 0, st>>>(dD, g.G, basis.nbf, g.ao_atom, dgrad, nullptr);
   });
   c.launch("reduce", st, [&] { k_reduce_b<<<1, 256, 0, st>>>(P.d_tabs, ov); });
   cuda_check(cudaGetLastError(), "kernel launch");
@@ -3428,6 +3431,104 @@ void Molecule::build_mixed_uks_mgga(const double *dD, double *dV, double *dout3,
                                  nbf * sizeof(double), nbf * sizeof(double), nbf,
                                  cudaMemcpyDeviceToDevice, st),
                "cudaMemcpy2DAsync");
+  cuda_check(cudaGetLastError(), "kernel launch");
+  P.ao_valid = true;
+}
+
+} // namespace occx
+
+// The unrestricted XC gradient on the tensor cores: the gradient plan per spin
+// (a second table points rho / coef at the beta arrays), the polarised
+// functional with FP32 derivatives, then per spin the operand planes (k_ymix,
+// k_grad_ops with that spin's coefficients), the three G_c launches and the
+// contraction with that spin's mo.D block, g -= 4 D_s G_c,s (the reference's
+// 2 Da V_c,a with D2 = 2 mo.D), skipping |Da + Db| < 1e-12.  dout3 = {E_xc,
+// integrated rho_a, integrated rho_b}.
+namespace occx {
+
+void Molecule::xc_gradient_uks_mixed(const double *dD, double *dgrad, double *dout3,
+                                     cudaStream_t st) {
+  prepare_gradient_mixed();
+  prepare_uks();
+  GradMixed &g = *gmixed;
+  LaunchPlan &P = g.plan;
+  if (!g.d_tab_b) {
+    MixTab tb = P.tabs[0];
+    tb.rho = d_rho_b;
+    tb.coef = d_coef_b;
+    g.d_tab_b = alloc(sizeof(MixTab));
+    cuda_check(cudaMemcpy(g.d_tab_b, &tb, sizeof(MixTab), cudaMemcpyHostToDevice),
+               "cudaMemcpy H2D");
+  }
+  const MixTab *tabs[2] = {P.d_tabs, static_cast<const MixTab *>(g.d_tab_b)};
+  Context &c = *ctx;
+  int *err = mixed->d_err;
+  const size_t nbf = static_cast<size_t>(basis.nbf), nbf2 = nbf * nbf;
+  const int nb = static_cast<int>(P.blocks.size());
+  const int ni = static_cast<int>(P.items.size());
+  const int sms = this->ctas > 0 ? this->ctas
+                                 : (ctx->max_ctas > 0 ? ctx->max_ctas : num_sms(device));
+  for (int s = 0; s < 2; s++)
+    cuda_check(cudaMemcpy2DAsync(d_Dab + s * nbf2, nbf * sizeof(double), dD + s * nbf,
+                                 2 * nbf * sizeof(double), nbf * sizeof(double), nbf,
+                                 cudaMemcpyDeviceToDevice, st),
+               "cudaMemcpy2DAsync");
+  cuda_check(cudaMemsetAsync(dgrad, 0, 3 * Z.size() * sizeof(double), st), "cudaMemsetAsync");
+  for (int s = 0; s < 2; s++) {
+    const Override ov{d_Dab + s * nbf2, nullptr, nullptr};
+    c.launch("prep_density", st, [&] {
+      k_prep_density<<<dim3(P.maxnbf, 1), 256, 0, st>>>(tabs[s], ov, P.d_queue);
+    });
+    if (nb == 0)
+      continue;
+    if (s == 0 && !P.ao_valid)
+      c.launch("colloc_f32", st, [&] {
+        k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+    c.launch("rho_mixed", st, [&] {
+      const int gg = std::min(nb, sms);
+      if (P.deriv)
+        k_rho_mixed<true><<<gg, kRhoThreads, kRhoSmem, st>>>(tabs[s], P.d_blocks, P.d_order, nb,
+                                                       P.d_queue, err);
+      else
+        k_rho_mixed<false><<<gg, kRhoThreads, kRhoSmem, st>>>(tabs[s], P.d_blocks, P.d_order,
+                                                        nb, P.d_queue, err);
+    });
+  }
+  const MolDev m = dev();
+  c.launch("func_pol", st, [&] {
+    launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
+                    d_epart_u, st, true);
+  });
+  for (int s = 0; s < 2 && nb > 0; s++) {
+    const double *Ds = d_Dab + s * nbf2, *Do = d_Dab + (1 - s) * nbf2;
+    c.launch("ymix", st, [&] {
+      if (P.deriv)
+        k_ymix<true><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
+      else
+        k_ymix<false><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
+    });
+    c.launch("grad_ops", st, [&] {
+      k_grad_ops<<<nb, kBlockPts, 0, st>>>(tabs[s], P.d_blocks, P.deriv);
+    });
+    cuda_check(cudaMemsetAsync(g.G, 0, 3 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
+    for (int cc = 0; cc < 3 && ni > 0; cc++) {
+      cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
+      const VxcPlanes pl{kPlaneDphi + 2 * cc, kPlaneDphi + 2 * cc + 1, kPlaneYHi, kPlaneYLo,
+                         kPlaneZ + 2 * cc,    kPlaneZ + 2 * cc + 1,    kPlanePhiHi, kPlanePhiLo,
+                         2};
+      const Override ovc{Ds, g.G + cc * nbf2, nullptr};
+      c.launch("grad_vxc", st, [&] {
+        k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+            tabs[s], P.d_blocks, P.d_items, ni, ovc, P.d_queue, err, P.tmap.rows32,
+            P.tmap.rows128, pl);
+      });
+    }
+    c.launch("grad_contract", st, [&] {
+      k_grad_contract<<<basis.nbf, 256, 0, st>>>(Ds, g.G, basis.nbf, g.ao_atom, dgrad, Do);
+    });
+  }
+  c.launch("reduce", st, [&] { launch_reduce3(d_epart_u, m.nleaves, dout3, st); });
   cuda_check(cudaGetLastError(), "kernel launch");
   P.ao_valid = true;
 }

@@ -501,7 +501,7 @@ class DFT:
         fixed (DFT::compute_xc_gradient, include/occ/dft/dft.h:599-749);
         precision FP64 or MIXED (contractions on the tensor cores).  As OCC
         dispatches on mo.kind, the shape of D decides: nbf x nbf restricted,
-        2 nbf x nbf (alpha block above beta) unrestricted (FP64).  E_xc of the
+        2 nbf x nbf (alpha block above beta) unrestricted.  E_xc of the
         same density via exchange_correlation_energy()."""
         nbf = self.nbf()
         Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))

@@ -239,8 +239,26 @@ def test_unrestricted_gradient_water_cluster_and_groups():
     assert np.max(np.abs(g - g_ref)) <= 1e-9 * max(1.0, np.max(np.abs(g_ref)))
     dft.set_gradient_workspace_cap(2 << 20)
     assert np.max(np.abs(dft.compute_xc_gradient(D) - g)) < 1e-11
-    with pytest.raises(og.XCError, match="FP64"):
-        dft.compute_xc_gradient(D, og.MIXED)
+    # the tensor-core form (3xTF32 contractions) at the restricted one's bar
+    gm = dft.compute_xc_gradient(D, og.MIXED)
+    assert np.max(np.abs(gm - g)) <= 3e-5, np.max(np.abs(gm - g))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["lda", "pbe", "b3lyp"])
+def test_unrestricted_gradient_mixed_against_oracle(method):
+    b, D = radical_case()
+    dft = og.DFT(method, b)
+    g = dft.compute_xc_gradient(D, og.MIXED)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient_unrestricted(b, P, W, D, method)
+    assert np.max(np.abs(g - g_ref)) <= 3e-5, np.max(np.abs(g - g_ref))
+    e_ref = oracle.xc_build_unrestricted(b, P, W, D, method)[0]
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= 1e-6
+    # the restricted tensor-core gradient of the same molecule after it
+    Dr = 2.0 * D[:b.nbf()]
+    gr = dft.compute_xc_gradient(Dr, og.MIXED)
+    assert np.max(np.abs(gr - oracle.xc_gradient(b, P, W, Dr, method))) <= 3e-5
 
 
 @pytest.mark.gpu
