@@ -19,11 +19,13 @@
 // pieces; max() and the thresholds select by the real part.
 // This is independent of the dual numbers the GPU functional uses.
 //
-// Thresholds (not pinned against Libxc): the point is zero below a total
-// density of 1e-15 (a spin channel's exchange below 1e-15); tau >= 1e-20;
-// sigma >= 1e-40; as Libxc does for meta-GGAs, sigma is clamped to 8 rho tau
-// (per spin channel when polarised) before evaluation, which keeps
-// z = tau_W / tau <= 1; 1 +- zeta is kept >= DBL_EPSILON.
+// Pinned against the reference's Libxc known answers (tests/dft_tests.cpp:
+// 138-193; met to 4.3e-9), whose four points all sit on the sigma = 8 rho tau
+// clamp below.  Other thresholds (not pinned against Libxc): the point is zero
+// below a total density of 1e-15 (a spin channel's exchange below 1e-15);
+// tau >= 1e-20; sigma >= 1e-40; as Libxc does for meta-GGAs, sigma is clamped
+// to 8 rho tau (per spin channel when polarised) before evaluation, which
+// keeps z = tau_W / tau <= 1; 1 +- zeta is kept >= DBL_EPSILON.
 #include "xc_oracle.h"
 
 #include <cmath>

@@ -161,3 +161,27 @@ def test_polarised_mixed_functional_matches_fp64(method):
         err = np.abs(om[k::6] - o64[k::6]) * x / scale
         i = int(np.argmax(err))
         assert err[i] <= 5e-5, (k, i, ra[i], rb[i], om[6 * i + k], o64[6 * i + k])
+
+
+def test_mgga_functional_matches_reference_known_answers():
+    """Both GPU meta-GGA evaluators at the reference's TPSS known answers
+    (tests/dft_tests.cpp:138-193, asserted there at 1e-6)."""
+    from test_mgga import (TPSS_EXC_C, TPSS_EXC_X, TPSS_VRHO_C, TPSS_VSIGMA_C, TPSS_VTAU_C,
+                           _tpss_inputs)
+    ctx = _context(0)
+    lib = ctx.lib
+    lib.occ_xc_selftest_functional_mgga.argtypes = [C.c_void_p, C.c_char_p, C.c_int, _dp, _dp,
+                                                    _dp, _dp, _dp]
+    rho, sig, tau = _tpss_inputs()
+    n = len(rho)
+    for method, checks in (("mgga_x_tpss", ((0, TPSS_EXC_X * rho),)),
+                           ("mgga_c_tpss", ((0, TPSS_EXC_C * rho), (1, TPSS_VRHO_C),
+                                            (2, TPSS_VSIGMA_C), (3, TPSS_VTAU_C)))):
+        o64 = np.zeros(4 * n)
+        om = np.zeros(4 * n)
+        rc = lib.occ_xc_selftest_functional_mgga(ctx.h, method.encode(), n, _ptr(rho),
+                                                 _ptr(sig), _ptr(tau), _ptr(o64), _ptr(om))
+        assert rc == 0, ctx.error()
+        for k, want in checks:
+            assert np.max(np.abs(o64[k::4] - want)) < 1e-8, (method, k)
+            assert np.max(np.abs(om[k::4] - want)) < 1e-6, (method, k)

@@ -3,11 +3,13 @@ dft.h:192-388) with tau in the density (src/gto/density.cpp:73-101) and the
 tau term of V_xc (src/dft/xc_potential_matrix.cpp:43-58).
 
 Libxc, which evaluates mgga_x_tpss / mgga_c_tpss in the reference, is absent,
-so the oracle's TPSS is pinned by the functional's own exact constraints:
-the uniform-gas limit (F_x = 1, correlation = PW92), the exact hydrogen-atom
-exchange energy (-0.3125 Ha, to which TPSS's constants c and e were fitted)
-and zero correlation for any one-electron density.  The oracle's V_xc is
-pinned as the derivative of its E_xc."""
+the oracle's TPSS is pinned against the reference's own Libxc known answers
+(tests/dft_tests.cpp:138-193: exchange and correlation energies, correlation
+vrho, vsigma, vtau) and by the functional's exact constraints: the uniform-gas
+limit (F_x = 1, correlation = PW92), the exact hydrogen-atom exchange energy
+(-0.3125 Ha, to which TPSS's constants c and e were fitted) and zero
+correlation for any one-electron density.  The oracle's V_xc is pinned as the
+derivative of its E_xc."""
 import numpy as np
 import pytest
 
@@ -17,6 +19,43 @@ from helpers import host_grid
 from test_fchk_density import fchk_case
 
 K2 = (3 * np.pi ** 2) ** (2 / 3)
+
+# The reference's TPSS known answers (tests/dft_tests.cpp:138-193, Libxc's
+# mgga_x_tpss / mgga_c_tpss through DensityFunctional::evaluate, asserted
+# there at 1e-6): rows rho, d_x rho, d_y rho, d_z rho, laplacian, tau.
+TPSS_POINTS = np.array([
+    [0.06019401627252133, -0.12747174847145987, -0.0, 0.03731311973522952,
+     0.09472176570942804, 0.036634279981580156],
+    [0.06019401627252133, -0.0, -0.12747174847145987, 0.03731311973522952,
+     0.09472176570942804, 0.036634279981580156],
+    [0.30171849914696935, -0.0, -0.0, 0.26070301592021455, -2.594981941107205,
+     0.02815789498408782],
+    [0.3550246251878335, -0.0, -0.0, 0.15685208520532756, -6.307746108179051,
+     0.008662278222335566]])
+TPSS_EXC_X = np.array([-0.33175882, -0.33175882, -0.56154382, -0.59257418])
+TPSS_EXC_C = np.array([-0.02276044, -0.02276044, -0.04168478, -0.04268936])
+TPSS_VRHO_C = np.array([-5.57565777e-02, -5.57565777e-02, -8.00593613e-02, -8.53775165e-02])
+TPSS_VSIGMA_C = np.array([3.91761083e-02, 3.91761083e-02, 1.47458233e-01, 5.51608074e-01])
+TPSS_VTAU_C = np.array([1.10283011e-03, 1.10283011e-03, -3.50002323e-01, -1.56487879e+00])
+
+
+def _tpss_inputs():
+    """rho, sigma, tau of the known-answer points (contiguous arrays)."""
+    rho = np.ascontiguousarray(TPSS_POINTS[:, 0])
+    tau = np.ascontiguousarray(TPSS_POINTS[:, 5])
+    return rho, (TPSS_POINTS[:, 1:4] ** 2).sum(1), tau
+
+
+def test_oracle_tpss_matches_reference_known_answers():
+    """The oracle's TPSS against the reference's Libxc values (1e-6 there;
+    the values are printed to 8 digits, and the oracle meets them to 1e-8).
+    All four points have tau = tau_W after Libxc's sigma <= 8 rho tau clamp."""
+    rho, sig, tau = _tpss_inputs()
+    ex = oracle.functional_mgga(202, rho, sig, tau)[0]
+    ec, vr, vs, vt = oracle.functional_mgga(231, rho, sig, tau)
+    for got, want in ((ex, TPSS_EXC_X), (ec, TPSS_EXC_C), (vr, TPSS_VRHO_C),
+                      (vs, TPSS_VSIGMA_C), (vt, TPSS_VTAU_C)):
+        assert np.max(np.abs(got - want)) < 1e-8, (got, want)
 
 
 def test_tpss_uniform_gas_limit():
