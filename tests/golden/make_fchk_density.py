@@ -1,7 +1,15 @@
-"""Generate water_rhf_631gdp.npz: a converged RHF density of water in a pure
-6-31G(d,p) basis (24 AOs) from the Gaussian formatted checkpoint embedded in
-the reference's tests (tests/wavefunction_io_tests.cpp, `pure_fchk_contents`,
-read as text), in OCC's conventions:
+"""Generate two density fixtures from the Gaussian formatted checkpoints
+embedded in the reference's tests (tests/wavefunction_io_tests.cpp, read as
+text):
+
+* water_rhf_631gdp.npz: a converged RHF density of water in a pure
+  6-31G(d,p) basis (24 AOs), `pure_fchk_contents`;
+* water_uhf_321g_fchk.npz: the converged water 3-21G UHF with 5 alpha = 5
+  beta electrons, `unrestricted_fchk_contents` (a closed shell, so its alpha
+  density is the RHF density; SCF energy -75.585325704292 Ha, RMS density
+  change 6e-10), which pins tests/golden/make_hf_density.py at its geometry;
+
+both in OCC's conventions:
 
 * shells as OCC's FchkReader::basis_set builds them (src/qm/io/fchkreader.cpp
   :327-395): SP shells split into an s and a p shell on the same exponents,
@@ -16,6 +24,8 @@ read as text), in OCC's conventions:
   cross-check of the conversion.
 
 usage: python tests/golden/make_fchk_density.py [path of wavefunction_io_tests.cpp]
+(default: $OCC_REFERENCE/tests/wavefunction_io_tests.cpp, OCC_REFERENCE being
+the reference checkout)
 """
 import os
 import re
@@ -24,14 +34,15 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = "/root/reference/tests/wavefunction_io_tests.cpp"
+SRC = os.path.join(os.environ.get("OCC_REFERENCE", "/root/reference"),
+                   "tests", "wavefunction_io_tests.cpp")
 
 
-def fchk_text(src):
+def fchk_text(src, name="pure_fchk_contents"):
     s = open(src).read()
-    m = re.search(r'pure_fchk_contents\s*=\s*R"\((.*?)\)"', s, re.S)
+    m = re.search(name + r'\s*=\s*R"\((.*?)\)"', s, re.S)
     if not m:
-        raise SystemExit("pure_fchk_contents not found")
+        raise SystemExit(name + " not found")
     return m.group(1)
 
 
@@ -66,8 +77,9 @@ def gaussian_to_occ(l, pure=True):
     return out
 
 
-def main(src):
-    t = fchk_text(src)
+def convert(t):
+    """Basis, OCC-ordered alpha density mo.D = C_occ C_occ^T and the file's
+    Total SCF Density (reordered) of one formatted checkpoint."""
     Z = field(t, "Atomic numbers")
     xyz = field(t, "Current cartesian coordinates").reshape(-1, 3)  # Bohr
     types = field(t, "Shell types")
@@ -107,9 +119,7 @@ def main(src):
     C_occ = C[perm, :nalpha]
     D = C_occ @ C_occ.T
     P_occ = P[np.ix_(perm, perm)]
-    assert np.max(np.abs(2 * D - P_occ)) < 1e-6, np.max(np.abs(2 * D - P_occ))
-    np.savez_compressed(
-        os.path.join(HERE, "water_rhf_631gdp.npz"),
+    return dict(
         Z=Z, xyz_bohr=xyz, shell_l=np.array([s[0] for s in shells]),
         shell_atom=np.array([s[1] for s in shells]),
         shell_nprim=np.array([len(s[2]) for s in shells]),
@@ -117,7 +127,22 @@ def main(src):
         coefficients=np.concatenate([s[3] for s in shells]),
         D=D, total_scf_density=P_occ, nelec=np.array(2 * nalpha),
         scf_energy=np.array(field(t, "SCF Energy")))
-    print("wrote water_rhf_631gdp.npz: nbf", nbf, "max|2D - P|", np.max(np.abs(2 * D - P_occ)))
+
+
+def main(src):
+    # pure 6-31G(d,p) RHF
+    d = convert(fchk_text(src, "pure_fchk_contents"))
+    err = np.max(np.abs(2 * d["D"] - d["total_scf_density"]))
+    assert err < 1e-6, err
+    np.savez_compressed(os.path.join(HERE, "water_rhf_631gdp.npz"), **d)
+    print("wrote water_rhf_631gdp.npz: nbf", d["D"].shape[0], "max|2D - P|", err)
+    # 3-21G UHF with 5 alpha = 5 beta electrons (a closed shell): its alpha
+    # density pins the small RHF of make_hf_density.py at this geometry
+    d = convert(fchk_text(src, "unrestricted_fchk_contents"))
+    err = np.max(np.abs(2 * d["D"] - d["total_scf_density"]))
+    assert err < 1e-6, err
+    np.savez_compressed(os.path.join(HERE, "water_uhf_321g_fchk.npz"), **d)
+    print("wrote water_uhf_321g_fchk.npz: nbf", d["D"].shape[0], "max|2D - P|", err)
 
 
 if __name__ == "__main__":
