@@ -338,10 +338,12 @@ def measured_traffic(kernel):
     return None
 
 
-def cpu_baseline(basis, P, W, D, target_s=15.0):
+def cpu_baseline(basis, P, W, D, target_s=15.0, method="pbe"):
     """Oracle (CPU restatement of the reference algorithm) on every host core,
-    on a strided sample of leaves; scaled to builds/s by the sampled share of
-    the contraction FLOPs."""
+    on a strided sample of leaves scaled by the sampled share of the
+    contraction FLOPs, or on whole builds when one build is shorter than
+    the target.  Returns (baseline dict, (E_xc, V_xc) of a whole oracle
+    build of this input, for the parity check)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     cores = os.cpu_count() or 1
@@ -350,33 +352,40 @@ def cpu_baseline(basis, P, W, D, target_s=15.0):
     L.oracle_total_flops.restype = C.c_double
     stride = 64
     t0 = time.perf_counter()
-    oracle.xc_build(basis, P, W, D, "pbe", nthreads=cores, leaf_stride=stride)
+    oracle.xc_build(basis, P, W, D, method, nthreads=cores, leaf_stride=stride)
     dt = time.perf_counter() - t0
     f_sample = L.oracle_last_flops()
     f_all = L.oracle_total_flops()
+    whole = None
     # grow the sample to about target_s of work
     stride2 = max(1, int(stride * dt / target_s)) if dt > 0 else stride
     if stride2 < stride:
         t0 = time.perf_counter()
-        oracle.xc_build(basis, P, W, D, "pbe", nthreads=cores, leaf_stride=stride2)
+        r = oracle.xc_build(basis, P, W, D, method, nthreads=cores, leaf_stride=stride2)
         dt = time.perf_counter() - t0
         f_sample = L.oracle_last_flops()
         stride = stride2
+        if stride == 1:
+            whole = r
     reps = 1
     if stride == 1 and dt < target_s:
         # the whole build is shorter than the target: repeat it
         reps = max(1, int(np.ceil(target_s / max(dt, 1e-3))))
         t0 = time.perf_counter()
         for _ in range(reps):
-            oracle.xc_build(basis, P, W, D, "pbe", nthreads=cores)
+            whole = oracle.xc_build(basis, P, W, D, method, nthreads=cores)
         dt = (time.perf_counter() - t0) / reps
         f_sample = f_all
     builds_per_s = (f_sample / f_all) / dt
     what = (f"{reps} whole builds, {dt:.2f} s each" if stride == 1 else
             f"every {stride}th Morton leaf ({100 * f_sample / f_all:.1f}% of the contraction "
             f"FLOPs) of the same build, {dt:.1f} s, scaled by the FLOP share")
-    return {"value": builds_per_s, "unit": "builds/s", "cores": cores, "kind": "port",
-            "sample": f"{what}; {cores} OpenMP threads"}
+    if whole is None:
+        whole = oracle.xc_build(basis, P, W, D, method, nthreads=cores)
+    return ({"value": builds_per_s, "unit": "builds/s", "cores": cores, "kind": "port",
+             "sample": f"{what}; {cores} OpenMP threads",
+             "contraction_gflops": f_sample / dt / 1e9},
+            (whole[0], whole[1]))
 
 
 def run_reference(args):
@@ -392,7 +401,7 @@ def run_reference(args):
         cpu_baseline(basis, P, W, D, target_s=5.0)
     cb = None
     for _ in range(args.steps if args.steps <= 3 else 3):
-        cb = cpu_baseline(basis, P, W, D, target_s=10.0)
+        cb, _ = cpu_baseline(basis, P, W, D, target_s=10.0)
         vals.append(cb["value"])
     v = statistics.median(vals)
     cb["value"] = v
@@ -436,6 +445,8 @@ def main():
     lib.occ_xc_launch_count.restype = C.c_long
     lib.occ_xc_launch_count.argtypes = [C.c_void_p]
 
+    nbf_ = basis.nbf()
+    V_fp64 = V_mixed = None
     have_mixed = True
     try:
         dft.compute_vxc(D, og.MIXED)
@@ -452,7 +463,12 @@ def main():
         torch.cuda.synchronize()
         l0 = lib.occ_xc_launch_count(dft.ctx.h)
         with ClockSampler(local) as cs:
-            total_ms, per, exc, _ = device_timing(dft, D, prec, args.steps, args.warmup, torch)
+            total_ms, per, exc, dV = device_timing(dft, D, prec, args.steps, args.warmup, torch)
+        Vres = dV.cpu().numpy().reshape(nbf_, nbf_, order="F").copy()
+        if prec == og.FP64:
+            V_fp64 = Vres
+        else:
+            V_mixed = Vres
         launches = lib.occ_xc_launch_count(dft.ctx.h) - l0
         rate, secs, _ = aggregate_rate(args.steps, total_ms / 1e3, dist if world > 1 else None)
         results[prec] = dict(total_ms=secs * 1e3, rate=rate, per=per, exc=exc,
@@ -495,7 +511,9 @@ def main():
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": measured_traffic(dom_name),
                 "kernel": dom_name, "algorithmic_bytes": nbytes,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                "peak_source": ("MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
+                                else "6.8 TB/s copy bandwidth measured earlier on a GB300 "
+                                     "(of fallback)"),
                 # the contraction it carries, for reference (not the bound)
                 "useful_tflops": (flops_half / (dom_avg_ms / 1e3) / 1e12
                                   if dom_name in ("rho_mixed", "vxc_mixed") else None)}
@@ -535,7 +553,20 @@ def main():
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         P, W = dft.grid()
-        out["cpu_baseline"] = cpu_baseline(basis, P, W, D)
+        out["cpu_baseline"], (e_or, V_or) = cpu_baseline(basis, P, W, D)
+        # parity at this size: the GPU builds against a whole oracle build of
+        # the same input (bars: FP64 1e-8 Ha and 1e-9, mixed 1e-6 Ha and 1e-5)
+        par = {"exc_oracle": e_or,
+               "fp64": {"dE_xc": results[og.FP64]["exc"] - e_or,
+                        "max_dV": float(np.max(np.abs(V_fp64 - V_or))),
+                        "bars": [1e-8, 1e-9]}}
+        if og.MIXED in results:
+            par["mixed"] = {"dE_xc": results[og.MIXED]["exc"] - e_or,
+                            "max_dV": float(np.max(np.abs(V_mixed - V_or))),
+                            "bars": [1e-6, 1e-5]}
+        par["within_bars"] = all(abs(v["dE_xc"]) <= v["bars"][0] and v["max_dV"] <= v["bars"][1]
+                                 for k, v in par.items() if k in ("fp64", "mixed"))
+        out["parity_vs_oracle"] = par
     print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()

@@ -256,7 +256,9 @@ def becke_cell_weights(P, R, radii, treutler_ahlrichs=True):
     """calculate_atomic_grid_weights_impl (grid_utils.cpp:149-200) with the
     Becke partition: (npts, natom) unnormalised cell functions."""
     natom = len(R)
-    d = np.sqrt(((P[:, None, :] - R[None, :, :]) ** 2).sum(axis=2))
+    d = np.empty((len(P), natom))
+    for a in range(natom):
+        d[:, a] = np.sqrt(((P - R[a]) ** 2).sum(axis=1))
     W = np.ones((len(P), natom))
     for i in range(natom):
         for j in range(i):
@@ -290,7 +292,7 @@ def exponent_ranges(shells, natom):
     return lmax, amax, amin
 
 
-def molecular_grid(Z, R, shells, s=None, product_theta=0, chunk=200000):
+def molecular_grid(Z, R, shells, s=None, product_theta=0, chunk=50000):
     """Points (n, 3) and weights (n,) in the reference's order (atom blocks,
     radial shells, angular points), Bohr.  Z: atomic numbers, R: (natom, 3)
     Bohr, shells: (l, atom, exponents) per shell."""
@@ -332,7 +334,7 @@ def becke_radial(n, rm):
     return r, wx * 2.0 * rm / (1.0 - x) ** 2 * r * r
 
 
-def refined_grid(Z, R, nrad, ntheta, chunk=200000):
+def refined_grid(Z, R, nrad, ntheta, chunk=50000):
     """A grid for converging integrals far beyond the default one: per atom
     Becke's radial rule with nrad points (rm = the Bragg radius, half of it
     for H) times product_rule(ntheta) on every shell, partitioned like the

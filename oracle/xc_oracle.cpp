@@ -1,5 +1,6 @@
 // CPU oracle for the restricted Kohn-Sham XC build -- TEST INFRASTRUCTURE
 // ONLY (see xc_oracle.h).  Every step cites the reference code it restates.
+#include "gemm.h"
 #include "xc_oracle.h"
 
 #include <algorithm>
@@ -468,17 +469,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
       }
       // density (src/gto/density.cpp:33-43): Dphi = phi * D, rho = rowsum(phi o Dphi)
       Dphi.assign(static_cast<size_t>(m) * n, 0.0);
-      for (int j = 0; j < m; j++) {
-        double *out = &Dphi[static_cast<size_t>(j) * n];
-        for (int k = 0; k < m; k++) {
-          double d = Dloc[static_cast<size_t>(j) * m + k];
-          if (d == 0.0)
-            continue;
-          const double *ph = &phi[static_cast<size_t>(k) * n];
-          for (long p = 0; p < n; p++)
-            out[p] += ph[p] * d;
-        }
-      }
+      oracle_gemm::gemm_nn(n, m, m, phi.data(), n, Dloc.data(), m, Dphi.data(), n);
       rho.assign(4 * n, 0.0);
       for (int j = 0; j < m; j++) {
         const double *dp = &Dphi[static_cast<size_t>(j) * n];
@@ -498,17 +489,8 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
         tau.assign(n, 0.0);
         for (int q = 1; q < 4; q++) {
           std::fill(Dphi.begin(), Dphi.end(), 0.0);
-          for (int j = 0; j < m; j++) {
-            double *out = &Dphi[static_cast<size_t>(j) * n];
-            for (int k = 0; k < m; k++) {
-              double d = Dloc[static_cast<size_t>(j) * m + k];
-              if (d == 0.0)
-                continue;
-              const double *g = &phi[(static_cast<size_t>(q) * m + k) * n];
-              for (long p = 0; p < n; p++)
-                out[p] += g[p] * d;
-            }
-          }
+          oracle_gemm::gemm_nn(n, m, m, &phi[static_cast<size_t>(q) * m * n], n, Dloc.data(), m,
+                               Dphi.data(), n);
           for (int j = 0; j < m; j++) {
             const double *dp = &Dphi[static_cast<size_t>(j) * n];
             const double *g = &phi[(static_cast<size_t>(q) * m + j) * n];
@@ -586,15 +568,7 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
         }
       }
       Kb.assign(static_cast<size_t>(m) * m, 0.0);
-      for (int j = 0; j < m; j++)
-        for (int i = 0; i < m; i++) {
-          const double *a = &phi[static_cast<size_t>(i) * n];
-          const double *b = &Y[static_cast<size_t>(j) * n];
-          double acc = 0.0;
-          for (long p = 0; p < n; p++)
-            acc += a[p] * b[p];
-          Kb[static_cast<size_t>(j) * m + i] = acc;
-        }
+      oracle_gemm::gemm_tn(m, m, n, phi.data(), n, Y.data(), n, Kb.data(), m);
       if (deriv) { // V = K + K^T
         for (int j = 0; j < m; j++)
           for (int i = 0; i < j; i++) {
@@ -606,17 +580,13 @@ extern "C" int oracle_xc_build(int nsh, const int *sh_l, const int *sh_nprim,
           Kb[static_cast<size_t>(i) * m + i] *= 2.0;
       }
       if (deriv == 2) // V += sum_k (d_k phi)^T diag(0.5 w vtau) (d_k phi)
-        for (int q = 1; q < 4; q++)
-          for (int j = 0; j < m; j++) {
-            const double *b = &phi[(static_cast<size_t>(q) * m + j) * n];
-            for (int i = 0; i < m; i++) {
-              const double *a = &phi[(static_cast<size_t>(q) * m + i) * n];
-              double acc = 0.0;
-              for (long p = 0; p < n; p++)
-                acc += a[p] * (0.5 * vtau[p]) * b[p];
-              Kb[static_cast<size_t>(j) * m + i] += acc;
-            }
-          }
+        for (int q = 1; q < 4; q++) {
+          const double *g = &phi[static_cast<size_t>(q) * m * n];
+          for (int j = 0; j < m; j++)
+            for (long p = 0; p < n; p++)
+              Y[static_cast<size_t>(j) * n + p] = (0.5 * vtau[p]) * g[static_cast<size_t>(j) * n + p];
+          oracle_gemm::gemm_tn(m, m, n, g, n, Y.data(), n, Kb.data(), m);
+        }
       // scatter (dft.h:361-369)
       for (size_t a = 0; a < sig.size(); a++)
         for (size_t b = 0; b < sig.size(); b++) {

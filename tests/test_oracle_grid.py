@@ -42,12 +42,14 @@ def _cases():
         "water_def2svp": (wl.basis_for(water, "def2-svp"), True),
         "water_def2tzvp": (wl.basis_for(water, "def2-tzvp"), True),
         "waters4_def2svp": (wl.basis_for(wl.water_cluster(4, box=5.0, seed=1), "def2-svp"), True),
+        # the benchmark cluster's density: 8 waters in a 6.3 Angstrom cube
+        "waters8_def2svp": (wl.basis_for(wl.water_cluster(8, box=6.3, seed=0), "def2-svp"), True),
         "ethane_631gdp_cart": (wl.basis_for(wl.alkane(2), "6-31g(d,p)", False), False),
     }
 
 
 NAMES = ["water_321g", "water_631g", "water_def2svp", "water_def2tzvp", "waters4_def2svp",
-         "ethane_631gdp_cart"]
+         "waters8_def2svp", "ethane_631gdp_cart"]
 
 
 @pytest.mark.parametrize("name", NAMES)
