@@ -4,7 +4,7 @@
  * A drop-in for the XC part of OCC's Kohn-Sham method: the molecule, its
  * AOBasis and a density matrix go in; E_xc and the V_xc matrix come out.
  * Plain C types only (no C++ or CUDA types), so any host language can bind
- * it (see INTEGRATION.md for the C++ and Python bindings).
+ * it; include/occ_xc.hpp is a C++ interface shaped like occ::dft::DFT over it.
  *
  * Conventions (those of OCC):
  *   - coordinates in Bohr;
@@ -392,6 +392,15 @@ int occ_xc_molecule_apply_tuning(occ_xc_context *ctx, occ_xc_molecule *mol,
  * fewer leave SMs free for concurrent builds on other streams. */
 int occ_xc_set_persistent_ctas(occ_xc_context *ctx, int ctas);
 
+/* Bound, in polls, of every pipeline wait of the persistent tensor-core
+ * kernels on this context's device (default 16777216 = 2^24).  A wait that
+ * runs out sets the build's error flag; the kernel waits for its own bulk
+ * copies and MMAs in flight (under the default bound), frees its tensor
+ * memory and returns, and the call reports OCC_XC_ERR_TIMEOUT once; the next
+ * build starts clean.  No counterpart in the reference (it has no GPU
+ * pipeline); tests lower the bound, to 0 even, to make a wait run out. */
+int occ_xc_set_wait_limit(occ_xc_context *ctx, unsigned int polls);
+
 /* The FP64 build of occ_xc_compute_vxc_device for callers that cannot
  * allocate device memory -- code inside a host application that owns all of
  * the GPU's memory through its own pool, or code that must never block in the
@@ -400,11 +409,16 @@ int occ_xc_set_persistent_ctas(occ_xc_context *ctx, int ctas);
  * its scratch is one static device array of 64 MiB that every GPU loading
  * the library holds until the process exits.  A molecule whose scratch would
  * exceed 64 MiB (roughly a water molecule in a split-valence basis with a GGA)
- * is rejected with OCC_XC_ERR_ARG and a message.  The first call on a device
- * looks up the array's device address (make it before any stream capture).
- * All calls share the array: calls that overlap on the GPU race on it, so
- * serialise them.  d_D, d_V and d_exc2 are as for occ_xc_compute_vxc_device;
- * the molecule is created beforehand with occ_xc_molecule_create. */
+ * is rejected with OCC_XC_ERR_ARG and a message, as is a molecule created on
+ * another context.  The first call on a device looks up the array's device
+ * address; under CUDA's lazy module loading that is also when the 64 MiB are
+ * taken on that device, so make the first call at set-up, before the
+ * caller's pool takes the GPU's memory and before any stream capture.  The
+ * call makes the context's device current and restores the caller's current
+ * device before it returns.  All calls share the array: calls that overlap
+ * on the GPU race on it, so serialise them.  d_D, d_V and d_exc2 are as for
+ * occ_xc_compute_vxc_device; the molecule is created beforehand with
+ * occ_xc_molecule_create. */
 int occ_xc_compute_vxc_noalloc(occ_xc_context *ctx, occ_xc_molecule *mol, const double *d_D,
                                double *d_V, double *d_exc2, void *stream);
 

@@ -1,8 +1,9 @@
 // tcgen05 (5th-generation tensor core) helpers for sm_103a, in inline PTX.
 //
 // Used by the mixed-precision contractions: one elected thread issues
-// tcgen05.mma.kind::tf32 with both operands in shared memory (K-major,
-// 128-byte swizzle) and the FP32 accumulator in tensor memory (TMEM);
+// tcgen05.mma.kind::tf32 or kind::f16 (BF16 operands) with both operands in
+// shared memory (K-major, 128-byte swizzle) and the FP32 accumulator in
+// tensor memory (TMEM);
 // completion is tracked with mbarriers through tcgen05.commit; the epilogue
 // reads TMEM with tcgen05.ld.  Every wait is bounded: on expiry the caller
 // records an error and leaves the loop instead of spinning forever.
@@ -138,6 +139,27 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
          | (2u << 10)                                // B format TF32
          | (static_cast<uint32_t>(N >> 3) << 17)     // N / 8
          | (static_cast<uint32_t>(M >> 4) << 24);    // M / 16
+}
+
+// Instruction descriptor: kind::f16 with BF16 A and B (K-major), FP32
+// accumulate, shape M x N.  One MMA covers K = 16 (32 bytes of a row), the
+// same bytes per step as a TF32 MMA's K = 8, so the 128-byte-swizzled tile
+// layout and its descriptors are shared with the TF32 path.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4)                                   // D format F32
+         | (1u << 7)                                 // A format BF16
+         | (1u << 10)                                // B format BF16
+         | (static_cast<uint32_t>(N >> 3) << 17)     // N / 8
+         | (static_cast<uint32_t>(M >> 4) << 24);    // M / 16
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile("{\n\t.reg .pred p;\n\t"
+               "setp.ne.b32 p, %4, 0;\n\t"
+               "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+               "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+               : "memory");
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,

@@ -66,6 +66,7 @@ void free_mixed(MixedState *S);
 struct Molecule;
 // 1 if a bounded wait in the mixed-precision kernels gave up (synchronises st)
 int mixed_error_flag(Molecule &M, cudaStream_t st);
+void set_wait_limit(int device, uint32_t polls);
 
 // Per-kernel device timing with CUDA events on the launching stream, the
 // device analogue of OCC's timing categories (include/occ/core/timings.h).

@@ -28,6 +28,7 @@
 #include <type_traits>
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include "../../include/occ_xc.h"
@@ -100,6 +101,11 @@ constexpr uint32_t kOffAhi = 0, kOffAlo = 16 * 1024, kOffBhi = 32 * 1024, kOffBl
 constexpr uint32_t kOffA1 = 0, kOffA2 = 16 * 1024, kOffA3 = 32 * 1024;
 constexpr uint32_t kOffB1 = 48 * 1024, kOffB2 = 64 * 1024, kOffB3 = 80 * 1024;
 constexpr uint32_t kWaitIter = 1u << 24; // bounded mbarrier waits
+// The bound of the persistent kernels' pipeline waits (polls), read once per
+// CTA.  occ_xc_set_wait_limit lowers it so that a test can make a wait run
+// out; the final drains (bulk copies and MMAs in flight, before a CTA frees
+// its TMEM and leaves) keep kWaitIter.
+__device__ uint32_t g_wait_limit = kWaitIter;
 constexpr uint32_t kRhoStageA = 3 * 16384; // exact-grid A slices of one K chunk (128 x 32 each)
 constexpr int kErrTimeout = 1;
 // AO planes of a block, [plane][mp][128] FP32 each: phi, d/dx, d/dy, d/dz
@@ -345,6 +351,48 @@ __device__ __forceinline__ void store4_exact(uint8_t *t1, uint8_t *t2, uint8_t *
   *reinterpret_cast<uint4 *>(t3 + off) = make_uint4(a3[0], a3[1], a3[2], a3[3]);
 }
 
+// The density GEMM's operands: the same three slices in BF16.  a1 and a2 hold
+// at most 8 significant bits and are exact in BF16; the tail a3 is rounded to
+// the nearest BF16 (|error| <= 2^-25 s).  A K chunk of the density GEMM is 64
+// AOs: one 128-byte row of BF16, the same bytes as 32 TF32 values, so the
+// tiles keep the TF32 path's 128-byte-swizzled layout and descriptors.
+constexpr int kKcR = 64;
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi); // .x (low half) = lo
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+__device__ __forceinline__ void slice3f(float x, float s, float inv_s, float &a1, float &a2,
+                                        float &a3, float tail) {
+  const float q = x * inv_s;
+  const float i1 = rintf(q * 128.f);
+  const float r1 = q - i1 * (1.f / 128.f);
+  const float i2 = rintf(r1 * 32768.f);
+  const float r2 = r1 - i2 * (1.f / 32768.f);
+  a1 = i1 * (1.f / 128.f) * s;
+  a2 = i2 * (1.f / 32768.f) * s;
+  a3 = fmaf(r2, s, tail);
+}
+// Eight consecutive K values of row r (16-byte chunk c) of the three BF16
+// slice tiles.
+__device__ __forceinline__ void store8_exact_bf16(uint8_t *t1, uint8_t *t2, uint8_t *t3, int r,
+                                                  int c, const float (&v)[8], float s,
+                                                  float inv_s, const float (&tail)[8]) {
+  float a1[8], a2[8], a3[8];
+#pragma unroll
+  for (int e = 0; e < 8; e++)
+    slice3f(v[e], s, inv_s, a1[e], a2[e], a3[e], tail[e]);
+  const uint32_t off = umma::sw128_offset(r, c);
+  *reinterpret_cast<uint4 *>(t1 + off) =
+      make_uint4(bf16x2_bits(a1[0], a1[1]), bf16x2_bits(a1[2], a1[3]), bf16x2_bits(a1[4], a1[5]),
+                 bf16x2_bits(a1[6], a1[7]));
+  *reinterpret_cast<uint4 *>(t2 + off) =
+      make_uint4(bf16x2_bits(a2[0], a2[1]), bf16x2_bits(a2[2], a2[3]), bf16x2_bits(a2[4], a2[5]),
+                 bf16x2_bits(a2[6], a2[7]));
+  *reinterpret_cast<uint4 *>(t3 + off) =
+      make_uint4(bf16x2_bits(a3[0], a3[1]), bf16x2_bits(a3[2], a3[3]), bf16x2_bits(a3[4], a3[5]),
+                 bf16x2_bits(a3[6], a3[7]));
+}
+
 // Power of two >= |v| (1 for zero rows).
 __device__ __forceinline__ float pow2_bound(float v) {
   if (!(v > 0.f))
@@ -423,6 +471,28 @@ __device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
   umma::split_tf32(x, h, l);
   hi = __uint_as_float(h);
   lo = __uint_as_float(l);
+}
+
+// The exact-grid BF16 slices of one point's row of an AO plane (phi or a
+// derivative, [mp][128]) as the density GEMM's A operand: per K chunk of 64
+// AOs one 48 KB image of the three swizzled 128 x 64 tiles, AOs at and beyond
+// mp zero.  ceil(mp / 64) images take at most the three planes' room.
+__device__ __forceinline__ void write_a_slices(uint8_t *as, const float *plane0, int mp, int p,
+                                               float sA, float isA) {
+  const float zero8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int c = 0; c < (mp + kKcR - 1) / kKcR; c++) {
+    uint8_t *tile = as + static_cast<size_t>(c) * kRhoStageA;
+#pragma unroll 2
+    for (int q = 0; q < kKcR / 8; q++) {
+      float v[8];
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const int f = c * kKcR + q * 8 + e;
+        v[e] = f < mp ? plane0[static_cast<size_t>(f) * kBlockPts + p] : 0.f;
+      }
+      store8_exact_bf16(tile, tile + 16384, tile + 32768, p, q, v, sA, isA, zero8);
+    }
+  }
 }
 
 template <int L>
@@ -568,19 +638,10 @@ __global__ void __launch_bounds__(128, 3) k_colloc_f32(const MixTab *__restrict_
   const float sA = pow2_bound(vmax), isA = 1.f / sA;
   T.rowscale[static_cast<size_t>(B.lblock) * kBlockPts + p] = sA;
   // the A operand of k_rho_mixed: this point's row of phi on the exact grid
-  // (scale sA), chunk by chunk, at its swizzled place in the three tiles
-  uint8_t *as = reinterpret_cast<uint8_t *>(base + kPlaneASlices * plane);
-  for (int c = 0; c < B.mp / kKc; c++) {
-    uint8_t *tile = as + static_cast<size_t>(c) * kRhoStageA;
-#pragma unroll 2
-    for (int q = 0; q < kKc / 4; q++) {
-      float v[4];
-#pragma unroll
-      for (int e = 0; e < 4; e++)
-        v[e] = base[static_cast<size_t>(c * kKc + q * 4 + e) * kBlockPts + p];
-      store4_exact(tile, tile + 16384, tile + 32768, p, q, v, sA, isA);
-    }
-  }
+  // (scale sA) in BF16, chunk by chunk of 64 AOs (the last one zero-padded),
+  // at its swizzled place in the three tiles
+  write_a_slices(reinterpret_cast<uint8_t *>(base + kPlaneASlices * plane), base, B.mp, p, sA,
+                 isA);
 }
 
 constexpr uint32_t kSmemMain = 2 * kStageBytes;
@@ -690,7 +751,8 @@ constexpr int kRhoEpi = 128;   // epilogue threads (warps 0-3)
 constexpr int kRhoMap = 1024;  // AO maps up to this size are staged in shared memory
 
 struct alignas(16) RhoSmem {
-  uint64_t full[kRhoStages], empty[kRhoStages]; // per stage: A and B landed, MMAs done
+  uint64_t full[kRhoStages], empty[kRhoStages]; // per stage: B written, MMAs done
+  uint64_t afull[kRhoStages];                     // per stage: the A bulk copy landed
   uint64_t tfull[2], tempty[2];
   uint64_t ifull[kRing], iempty[kRing];
   uint64_t done;
@@ -731,7 +793,8 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   if (t == 0) {
     for (int s = 0; s < kRhoStages; s++) {
-      umma::mbar_init(&sm->full[s], 1 + kRhoProd);
+      umma::mbar_init(&sm->full[s], kRhoProd);
+      umma::mbar_init(&sm->afull[s], 1);
       umma::mbar_init(&sm->empty[s], 1);
     }
     for (int b = 0; b < 2; b++) {
@@ -752,8 +815,9 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
   umma::fence_after_sync();
   const uint32_t tmem = sm->tmem_slot;
   bool ok = true;
+  const uint32_t wait_limit = g_wait_limit;
   auto wait = [&](uint64_t *bar, uint32_t parity) {
-    if (ok && !umma::mbar_wait(bar, parity, kWaitIter)) {
+    if (ok && !umma::mbar_wait(bar, parity, wait_limit)) {
       ok = false;
       atomicExch(err, kErrTimeout);
     }
@@ -778,7 +842,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     return bi;
   };
   auto segs = [](int mp) { return (mp + kExactKSeg - 1) / kExactKSeg; };
-  auto seg_chunks = [](int mp, int k0) { return min(kExactKSeg, mp - k0) / kKc; };
+  auto seg_chunks = [](int mp, int k0) { return (min(kExactKSeg, mp - k0) + kKcR - 1) / kKcR; };
 
   if (warp == 12) {
     // ---- block fetch and A slices (lane 0) ----
@@ -806,16 +870,16 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
               const uint32_t use = g / kRhoStages;
               if (use > 0 && !wait(&sm->empty[s], (use - 1) & 1))
                 break;
-              umma::mbar_arrive_expect_tx(&sm->full[s], kRhoStageA);
+              umma::mbar_arrive_expect_tx(&sm->afull[s], kRhoStageA);
               umma::bulk_load(smem + s * kRhoStage,
-                              as + static_cast<size_t>(k0 / kKc + c) * kRhoStageA, kRhoStageA,
-                              &sm->full[s]);
+                              as + static_cast<size_t>(k0 / kKcR + c) * kRhoStageA, kRhoStageA,
+                              &sm->afull[s]);
             }
         if (!ok)
           break;
       }
       for (uint32_t q = (g >= kRhoStages ? g - kRhoStages : 0); q < g; q++)
-        umma::mbar_wait(&sm->full[q % kRhoStages], (q / kRhoStages) & 1, kWaitIter);
+        umma::mbar_wait(&sm->afull[q % kRhoStages], (q / kRhoStages) & 1, kWaitIter);
     }
   } else if (prod) {
     // ---- B producers ----
@@ -853,21 +917,25 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
             if (use > 0 && !wait(&sm->empty[s], (use - 1) & 1))
               break;
             uint8_t *st = smem + s * kRhoStage + kRhoStageA;
-            float2 d[2][4];
+            float2 d[2][8];
 #pragma unroll
             for (int r = 0; r < 2; r++)
 #pragma unroll
-              for (int e = 0; e < 4; e++) {
-                const int lk = k0 + c * kKc + (qb + 4 * r) * 4 + e;
+              for (int e = 0; e < 8; e++) {
+                const int lk = k0 + c * kKcR + (qb + 4 * r) * 8 + e;
                 d[r][e] = (jv && lk < L.nbf) ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
                                              : make_float2(0.f, 0.f);
               }
 #pragma unroll
             for (int r = 0; r < 2; r++) {
-              const float v[4] = {d[r][0].x, d[r][1].x, d[r][2].x, d[r][3].x};
-              const float lo[4] = {d[r][0].y, d[r][1].y, d[r][2].y, d[r][3].y};
-              store4_exact(st, st + kRhoN * 128, st + 2 * kRhoN * 128, jr, qb + 4 * r, v, sB,
-                           isB, lo);
+              float v[8], lo[8];
+#pragma unroll
+              for (int e = 0; e < 8; e++) {
+                v[e] = d[r][e].x;
+                lo[e] = d[r][e].y;
+              }
+              store8_exact_bf16(st, st + kRhoN * 128, st + 2 * kRhoN * 128, jr, qb + 4 * r, v,
+                                sB, isB, lo);
             }
             umma::fence_proxy_async();
             umma::mbar_arrive(&sm->full[s]);
@@ -886,7 +954,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
         const int mp = blocks[bi].mp;
         for (int n0 = 0; n0 < mp && ok; n0 += kRhoN) {
           const int N = min(kRhoN, mp - n0);
-          const uint32_t idesc = umma::idesc_tf32(128, N);
+          const uint32_t idesc = umma::idesc_bf16(128, N);
           for (int k0 = 0; k0 < mp && ok; k0 += kExactKSeg, sc++) {
             const uint32_t buf = sc & 1, ub = sc >> 1;
             if (ub > 0 && !wait(&sm->tempty[buf], (ub - 1) & 1))
@@ -896,12 +964,13 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
             const int nch = seg_chunks(mp, k0);
             for (int c = 0; c < nch && ok; c++, g++) {
               const int s = g % kRhoStages;
-              if (!wait(&sm->full[s], (g / kRhoStages) & 1))
+              if (!wait(&sm->afull[s], (g / kRhoStages) & 1) ||
+                  !wait(&sm->full[s], (g / kRhoStages) & 1))
                 break;
               umma::fence_after_sync();
               const uint32_t base = umma::smem_u32(smem + s * kRhoStage);
 #pragma unroll
-              for (int kk = 0; kk < kKc / 8; kk++) {
+              for (int kk = 0; kk < 4; kk++) { // K = 16 AOs (32 bytes of a row) per MMA
                 const uint32_t o = kk * 32;
                 const uint64_t a1 = umma::desc_kmajor_sw128(base + o);
                 const uint64_t a2 = umma::desc_kmajor_sw128(base + 16384 + o);
@@ -911,14 +980,14 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
                 const uint64_t b3 =
                     umma::desc_kmajor_sw128(base + kRhoStageA + 2 * kRhoN * 128 + o);
                 const uint32_t acc = (c == 0 && kk == 0) ? 0u : 1u;
-                umma::mma_tf32(d0, a1, b1, idesc, acc);
-                umma::mma_tf32(d1, a1, b2, idesc, acc);
-                umma::mma_tf32(d1, a2, b1, idesc, 1u);
-                umma::mma_tf32(d2, a2, b3, idesc, acc);
-                umma::mma_tf32(d2, a3, b2, idesc, 1u);
-                umma::mma_tf32(d2, a2, b2, idesc, 1u);
-                umma::mma_tf32(d2, a1, b3, idesc, 1u);
-                umma::mma_tf32(d2, a3, b1, idesc, 1u);
+                umma::mma_bf16(d0, a1, b1, idesc, acc);
+                umma::mma_bf16(d1, a1, b2, idesc, acc);
+                umma::mma_bf16(d1, a2, b1, idesc, 1u);
+                umma::mma_bf16(d2, a2, b3, idesc, acc);
+                umma::mma_bf16(d2, a3, b2, idesc, 1u);
+                umma::mma_bf16(d2, a2, b2, idesc, 1u);
+                umma::mma_bf16(d2, a1, b3, idesc, 1u);
+                umma::mma_bf16(d2, a3, b1, idesc, 1u);
               }
               umma::commit(&sm->empty[s]);
               issued = true;
@@ -1126,8 +1195,9 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
   umma::fence_after_sync();
   const uint32_t tmem = sm->tmem_slot;
   bool ok = true;
+  const uint32_t wait_limit = g_wait_limit;
   auto wait = [&](uint64_t *bar, uint32_t parity) {
-    if (ok && !umma::mbar_wait(bar, parity, kWaitIter)) {
+    if (ok && !umma::mbar_wait(bar, parity, wait_limit)) {
       ok = false;
       atomicExch(err, kErrTimeout);
     }
@@ -1913,7 +1983,18 @@ int mixed_error_flag(Molecule &M, cudaStream_t st) {
   cuda_check(cudaMemcpyAsync(&h, M.mixed->d_err, sizeof(int), cudaMemcpyDeviceToHost, st),
              "cudaMemcpyAsync D2H");
   cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  if (h) // reported once; the next build starts clean
+    cuda_check(cudaMemsetAsync(M.mixed->d_err, 0, sizeof(int), st), "cudaMemsetAsync");
   return h;
+}
+
+void set_wait_limit(int device, uint32_t polls) {
+  int prev = 0;
+  cuda_check(cudaGetDevice(&prev), "cudaGetDevice");
+  cuda_check(cudaSetDevice(device), "cudaSetDevice");
+  const cudaError_t e = cudaMemcpyToSymbol(g_wait_limit, &polls, sizeof(polls));
+  cudaSetDevice(prev);
+  cuda_check(e, "cudaMemcpyToSymbol");
 }
 
 void free_mixed(MixedState *S) { delete S; }
@@ -2186,6 +2267,8 @@ int batch_error_flag(Batch &B, cudaStream_t st) {
   int h = 0;
   cuda_check(cudaMemcpyAsync(&h, B.d_err, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
   cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  if (h) // reported once; the next build starts clean
+    cuda_check(cudaMemsetAsync(B.d_err, 0, sizeof(int), st), "cudaMemsetAsync");
   return h;
 }
 
@@ -2423,6 +2506,19 @@ int occ_xc_set_persistent_ctas(occ_xc_context *ctx, int ctas) {
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   ctx->impl->max_ctas = ctas;
+  return OCC_XC_OK;
+}
+
+int occ_xc_set_wait_limit(occ_xc_context *ctx, unsigned int polls) {
+  if (!ctx)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  try {
+    set_wait_limit(ctx->impl->device, polls);
+  } catch (const std::exception &e) {
+    ctx->err = e.what();
+    return OCC_XC_ERR_CUDA;
+  }
   return OCC_XC_OK;
 }
 
@@ -3169,18 +3265,8 @@ __global__ void __launch_bounds__(kBlockPts) k_meta_ops(const MixTab *__restrict
       base[(kPlaneMetaDphi + 2 * (k - 1) + 1) * plane + o] = l;
     }
     const float sA = pow2_bound(vmax), isA = 1.f / sA;
-    uint8_t *as = reinterpret_cast<uint8_t *>(base + (kPlaneTauA + 3 * (k - 1)) * plane);
-    for (int c = 0; c < B.mp / kKc; c++) {
-      uint8_t *tile = as + static_cast<size_t>(c) * kRhoStageA;
-#pragma unroll 2
-      for (int q = 0; q < kKc / 4; q++) {
-        float v[4];
-#pragma unroll
-        for (int e = 0; e < 4; e++)
-          v[e] = g[static_cast<size_t>(c * kKc + q * 4 + e) * kBlockPts + p];
-        store4_exact(tile, tile + 16384, tile + 32768, p, q, v, sA, isA);
-      }
-    }
+    write_a_slices(reinterpret_cast<uint8_t *>(base + (kPlaneTauA + 3 * (k - 1)) * plane), g,
+                   B.mp, p, sA, isA);
   }
 }
 

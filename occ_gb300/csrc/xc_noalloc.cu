@@ -13,12 +13,17 @@
 // scratch (AO values, densities, functional coefficients, per-leaf energy
 // partials) lives in one file-scope __device__ array of kNoAllocScratchBytes
 // instead of the molecule's own workspace:
-//  - every GPU that loads the library holds that array until the process
-//    exits;
+//  - every GPU on which the entry point has run holds that array until the
+//    process exits.  Under CUDA's lazy module loading (the default) the
+//    module that holds the array loads, and its 64 MiB are taken, on the
+//    first call on a device, when the host looks up the array's address: a
+//    caller whose pool takes the GPU's memory makes that first call at
+//    set-up, before the pool grows;
 //  - the host obtains the array's device address with cudaGetSymbolAddress,
-//    once per device, with that device current, the first time the entry
-//    point runs on that device; make that first call before any stream
-//    capture;
+//    once per device, with that device current (the call makes the
+//    context's device current and restores the caller's device before it
+//    returns), the first time the entry point runs on that device; make that
+//    first call before any stream capture;
 //  - every call shares the array: calls whose work overlaps on the GPU race
 //    on it and give wrong results, so a caller serialises them (one stream,
 //    or events between streams);
@@ -57,6 +62,22 @@ double *noalloc_scratch(int device) {
 
 size_t align_elems(size_t n) { return (n + 31) / 32 * 32; } // 256-byte boundaries
 
+// Makes `device` current for the lifetime of the guard and puts the caller's
+// current device back on every exit path.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int device) {
+    cuda_check(cudaGetDevice(&prev), "cudaGetDevice");
+    if (prev != device)
+      cuda_check(cudaSetDevice(device), "cudaSetDevice");
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
+      cudaSetDevice(prev);
+  }
+};
+
 } // namespace
 } // namespace occx
 
@@ -69,6 +90,10 @@ extern "C" int occ_xc_compute_vxc_noalloc(occ_xc_context *ctx, occ_xc_molecule *
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   try {
+    if (mol->ctx != ctx) {
+      ctx->err = "occ_xc_compute_vxc_noalloc: the molecule was created on another context";
+      return OCC_XC_ERR_ARG;
+    }
     Context &c = *ctx->impl;
     Molecule &M = *mol->impl;
     const size_t N = static_cast<size_t>(M.plan.npts);
@@ -83,7 +108,7 @@ extern "C" int occ_xc_compute_vxc_noalloc(occ_xc_context *ctx, occ_xc_molecule *
                  std::to_string(kNoAllocScratchBytes) + " bytes; use occ_xc_compute_vxc_device";
       return OCC_XC_ERR_ARG;
     }
-    cuda_check(cudaSetDevice(c.device), "cudaSetDevice");
+    DeviceGuard on_device(c.device);
     double *ws = noalloc_scratch(c.device);
     double *rho = ws + align_elems(M.ws_elems);
     double *coef = rho + align_elems(nrho);
@@ -92,14 +117,19 @@ extern "C" int occ_xc_compute_vxc_noalloc(occ_xc_context *ctx, occ_xc_molecule *
     const MolDev m = M.dev();
     const size_t nbf2 = static_cast<size_t>(M.basis.nbf) * M.basis.nbf;
     cuda_check(cudaMemsetAsync(d_V, 0, nbf2 * sizeof(double), st), "cudaMemsetAsync");
-    launch_colloc_f64(m, M.deriv, ws, st);
-    launch_rho_f64(m, M.deriv, d_D, ws, M.d_slabs, static_cast<int>(M.slabs.size()), rho, st);
+    // the launches of Molecule::build_fp64, counted and profiled the same way
+    const int nslabs = static_cast<int>(M.slabs.size()), ntiles = static_cast<int>(M.tiles.size());
+    c.launch("colloc_f64", st, [&] { launch_colloc_f64(m, M.deriv, ws, st); });
+    c.launch("rho_f64", st,
+             [&] { launch_rho_f64(m, M.deriv, d_D, ws, M.d_slabs, nslabs, rho, st); });
     if (M.deriv == 2)
-      launch_tau_f64(m, d_D, ws, M.d_slabs, static_cast<int>(M.slabs.size()), rho, st);
-    launch_func(m, M.deriv, M.fs, M.bs.density_threshold, rho, coef, epart, st);
-    launch_vxc_f64(m, M.deriv, ws, coef, M.d_tiles, static_cast<int>(M.tiles.size()), d_V, st);
-    launch_reduce(epart, m.nleaves, d_exc2, st);
-    c.launches += M.deriv == 2 ? 6 : 5;
+      c.launch("tau_f64", st, [&] { launch_tau_f64(m, d_D, ws, M.d_slabs, nslabs, rho, st); });
+    c.launch("func", st, [&] {
+      launch_func(m, M.deriv, M.fs, M.bs.density_threshold, rho, coef, epart, st);
+    });
+    c.launch("vxc_f64", st,
+             [&] { launch_vxc_f64(m, M.deriv, ws, coef, M.d_tiles, ntiles, d_V, st); });
+    c.launch("reduce", st, [&] { launch_reduce(epart, m.nleaves, d_exc2, st); });
     cuda_check(cudaGetLastError(), "kernel launch");
     return OCC_XC_OK;
   } catch (const CudaError &e) {

@@ -143,6 +143,7 @@ def library():
     lib.occ_xc_graph_launch.argtypes = [_vp, _vp]
     lib.occ_xc_graph_destroy.argtypes = [_vp]
     lib.occ_xc_set_persistent_ctas.argtypes = [_vp, C.c_int]
+    lib.occ_xc_set_wait_limit.argtypes = [_vp, C.c_uint]
     _u64 = C.c_uint64
     lib.occ_xc_default_server_settings.argtypes = [C.POINTER(_ServerSettings)]
     lib.occ_xc_server_last_error.restype = C.c_char_p
