@@ -51,9 +51,10 @@ def parse():
     ap.add_argument("--ctas", type=int, default=0,
                     help="CTAs of the persistent tensor-core kernels (0: one per SM)")
     ap.add_argument("--workload", default="water32",
-                    choices=["water32", "alkane", "clusters", "stream", "gradient", "grid", "uks",
-                             "vv10", "mgga"],
-                    help="water32: the headline build (default); alkane: C30H62 def2-TZVP "
+                    choices=["water32", "water", "alkane", "clusters", "stream", "gradient", "grid",
+                             "uks", "vv10", "mgga"],
+                    help="water32: the headline build (default); water: one water molecule, "
+                         "6-31G, LDA (latency-bound); alkane: C30H62 def2-TZVP "
                          "B3LYP, 15 iterations as one CUDA graph; clusters: 512 clusters "
                          "as one batch; stream: served Poisson request stream; gradient: "
                          "the XC nuclear gradient of the water32 molecule; grid: its molecular "
@@ -87,6 +88,8 @@ def run_workload(args):
             r = bw.vv10(steps=args.steps, warmup=args.warmup, waters=args.waters)
         elif args.workload == "mgga":
             r = bw.mgga_build(torch, steps=args.steps, warmup=args.warmup, waters=args.waters)
+        elif args.workload == "water":
+            r = bw.water_latency(torch, steps=max(args.steps, 100), warmup=max(args.warmup, 10))
         else:
             r = bw.stream(nreq=args.requests, rate=args.rate)
     if args.workload in ("uks", "vv10"):

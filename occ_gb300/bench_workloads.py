@@ -154,8 +154,15 @@ def clusters_batch(torch, steps=2, warmup=1, nclusters=512, seed=0, autotune=Tru
 
 
 def serve_stream(precision, nreq=32, rate=10.0, seed=0, budget=150e9, sessions=None):
-    """One pass of the seeded request stream through a server.  `sessions`
-    (basis, D0, iterations) may be passed in to reuse the host inputs."""
+    """One pass of the seeded request stream through a server.  Each request
+    opens its session when it arrives (grid, screening and admission inside
+    the timed stream, on a pool of opener threads so that the polling loop
+    keeps running), then submits its SCF iterations one after another.
+    Latencies: per build (submit -> result, the server's own statistics),
+    per session open, and per request to its first result (arrival -> first
+    V_xc, open included).  `sessions` (basis, D0, iterations) may be passed in
+    to reuse the host inputs."""
+    from concurrent.futures import ThreadPoolExecutor
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, nreq)
     arrivals = np.cumsum(gaps) - gaps[0]
@@ -168,36 +175,51 @@ def serve_stream(precision, nreq=32, rate=10.0, seed=0, budget=150e9, sessions=N
             sessions.append((b, wl.random_density(b.nbf(), 5 * n, seed=seed + 300 + i),
                              int(rng.integers(8, 21))))
     srv = Server(precision=precision, hbm_budget_bytes=budget)
+    pool = ThreadPoolExecutor(max_workers=8)
     try:
-        t0 = time.perf_counter()
-        sids = [srv.open("pbe", b) for b, _, _ in sessions]
-        open_s = time.perf_counter() - t0
-        state = {}  # request -> [iteration, ticket, D]
+        def opener(r):
+            t = time.perf_counter()
+            sid = srv.open("pbe", sessions[r][0])
+            return sid, time.perf_counter() - t
+        opening = {}  # request -> future of (session id, open seconds)
+        state = {}    # request -> [iteration, ticket, D, session id]
+        open_s, first_ms = [], []
         done_req, nxt, builds = 0, 0, 0
         h2d = d2h = 0
         t0 = time.perf_counter()
         while done_req < nreq:
             now = time.perf_counter() - t0
             while nxt < nreq and arrivals[nxt] <= now:
-                b, D0, _ = sessions[nxt]
-                state[nxt] = [0, srv.submit(sids[nxt], D0), D0]
-                h2d += D0.size * 8
+                opening[nxt] = pool.submit(opener, nxt)
                 nxt += 1
             progressed = False
+            for r in list(opening):
+                f = opening[r]
+                if not f.done():
+                    continue
+                sid, dt = f.result()
+                open_s.append(dt)
+                D0 = sessions[r][1]
+                state[r] = [0, srv.submit(sid, D0), D0, sid]
+                h2d += D0.size * 8
+                del opening[r]
+                progressed = True
             for r in list(state):
-                it, ticket, D = state[r]
+                it, ticket, D, sid = state[r]
                 res = srv.poll(ticket)
                 if res is None:
                     continue
                 progressed = True
                 builds += 1
                 d2h += res[0].size * 8 + 16
+                if it == 0:
+                    first_ms.append((time.perf_counter() - t0 - arrivals[r]) * 1e3)
                 if it + 1 < sessions[r][2]:
                     Dn = wl.perturbed(D, 1e-3, seed + 10000 * r + it + 1)
-                    state[r] = [it + 1, srv.submit(sids[r], Dn), Dn]
+                    state[r] = [it + 1, srv.submit(sid, Dn), Dn, sid]
                     h2d += Dn.size * 8
                 else:
-                    srv.close(sids[r])
+                    srv.close(sid)
                     del state[r]
                     done_req += 1
             if not progressed:
@@ -205,22 +227,104 @@ def serve_stream(precision, nreq=32, rate=10.0, seed=0, budget=150e9, sessions=N
         wall = time.perf_counter() - t0
         st = srv.stats()
     finally:
+        pool.shutdown()
         srv.shutdown()
     return {"builds": builds, "wall_s": wall, "builds_per_s": builds / wall,
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+            "open_p50_ms": float(np.percentile(open_s, 50) * 1e3),
+            "open_p99_ms": float(np.percentile(open_s, 99) * 1e3),
+            "first_result_p50_ms": float(np.percentile(first_ms, 50)),
+            "first_result_p99_ms": float(np.percentile(first_ms, 99)),
             "mean_batch": st["mean_batch"], "ticks": st["ticks"], "failed": st["failed"],
-            "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9, "host_open_s": open_s,
+            "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9,
             "h2d_bytes_per_build": h2d / max(builds, 1),
             "d2h_bytes_per_build": d2h / max(builds, 1)}, sessions
 
 
 def stream(nreq=32, rate=10.0, seed=0):
     out = {"workload": f"stream{nreq}_poisson{rate:g}_n2to48_def2svp_pbe", "requests": nreq,
-           "rate_per_s": rate, "budget_gb": 150}
+           "rate_per_s": rate, "budget_gb": 150,
+           "note": "sessions open at arrival inside the timed stream (open and first-result "
+                   "latencies reported beside the per-build ones)"}
     m, sessions = serve_stream(MIXED, nreq, rate, seed)
     out["mixed"] = m
     f, _ = serve_stream(FP64, nreq, rate, seed, sessions=sessions)
     out["fp64"] = f
+    return out
+
+
+def water_latency(torch, steps=200, warmup=20, method="lda", seed=0):
+    """The smallest configuration: water (O at the origin, H at (+-0.757,
+    0.586, 0) Angstrom), 6-31G (13 AOs), OCC's "lda" (Slater + VWN3) on the
+    default grid, D from 5 occupied columns of a seeded orthonormal matrix.
+    Launch- and latency-bound: per-build latency p50 / p99 with D, V on the
+    device, through the host entry point, and the oracle's time beside it."""
+    import os
+    import sys
+    mol = wl.water()
+    b = wl.basis_for(mol, "6-31g")
+    D = wl.random_density(b.nbf(), 5, seed=seed)
+    dft = DFT(method, b)
+    info = dft.info()
+    lib = dft.ctx.lib
+    nbf = b.nbf()
+    dD = torch.tensor(np.asfortranarray(D).ravel(order="F"), device="cuda", dtype=torch.float64)
+    dV = torch.zeros(nbf * nbf, device="cuda", dtype=torch.float64)
+    dE = torch.zeros(2, device="cuda", dtype=torch.float64)
+    stream = torch.cuda.Stream()
+    out = {"workload": f"water_631g_{method}", "nbf": nbf, "npoints": info["npoints"]}
+    excs = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        def one():
+            rc = lib.occ_xc_compute_vxc_device(dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()), prec,
+                                               C.c_void_p(dV.data_ptr()),
+                                               C.c_void_p(dE.data_ptr()),
+                                               C.c_void_p(stream.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(dft.ctx.error())
+        for _ in range(warmup):
+            one()
+        torch.cuda.synchronize()
+        per = []
+        for _ in range(steps):
+            a = torch.cuda.Event(enable_timing=True)
+            z = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            one()
+            z.record(stream)
+            z.synchronize()
+            per.append(a.elapsed_time(z))
+        excs[name] = float(dE[0].item())
+        # through the host entry point: D in, V and E_xc out, synchronous
+        for _ in range(warmup):
+            dft.compute_vxc(D, prec)
+        lat = []
+        for _ in range(steps):
+            t = time.perf_counter()
+            dft.compute_vxc(D, prec)
+            lat.append((time.perf_counter() - t) * 1e3)
+        out[name] = {"builds_per_s": 1e3 / float(np.mean(per)),
+                     "p50_ms": float(np.percentile(per, 50)),
+                     "p99_ms": float(np.percentile(per, 99)),
+                     "e2e": {"value": 1e3 / float(np.mean(lat)), "unit": "builds/s",
+                             "p50_ms": float(np.percentile(lat, 50)),
+                             "p99_ms": float(np.percentile(lat, 99)),
+                             "h2d_bytes_per_step": nbf * nbf * 8,
+                             "d2h_bytes_per_step": nbf * nbf * 8 + 16}}
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, os.path.join(root, "oracle"))
+    import oracle
+    P, W = dft.grid()
+    t = time.perf_counter()
+    reps = 20
+    for _ in range(reps):
+        e_ref, _, _ = oracle.xc_build(b, P, W, D, method)
+    cpu_s = (time.perf_counter() - t) / reps
+    out["dE_xc_fp64_vs_oracle"] = excs["fp64"] - e_ref
+    out["dE_xc_mixed_vs_oracle"] = excs["mixed"] - e_ref
+    out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "builds/s", "cores": os.cpu_count(),
+                           "kind": "port", "sample": f"{reps} whole builds"}
+    out["e2e"] = out["fp64"]["e2e"]
     return out
 
 

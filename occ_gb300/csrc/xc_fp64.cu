@@ -174,7 +174,10 @@ __global__ void __launch_bounds__(256) k_rho_f64(MolDev m, const double *__restr
 #pragma unroll
       for (int j = 0; j < 4; j++)
         acc[i][j] = 0.0;
-    for (int k0 = 0; k0 < L.mpad; k0 += kKChunk) {
+    // AOs at and beyond nbf contribute zeros: the reduction stops at the
+    // first chunk boundary past them
+    const int kend = (L.nbf + kKChunk - 1) / kKChunk * kKChunk;
+    for (int k0 = 0; k0 < kend; k0 += kKChunk) {
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         int idx = threadIdx.x + r * 256;
@@ -304,7 +307,7 @@ __global__ void __launch_bounds__(256) k_vxc_f64(MolDev m, const double *__restr
       acc[a][b] = 0.0;
   constexpr int NSEG = META ? 4 : 1;
   for (int seg = 0; seg < NSEG; seg++)
-  for (int p0 = 0; p0 < L.npad; p0 += kKChunk) {
+  for (int p0 = 0; p0 < (L.cnt + kKChunk - 1) / kKChunk * kKChunk; p0 += kKChunk) {
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const int idx = threadIdx.x + r * 256;

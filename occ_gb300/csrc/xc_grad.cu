@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256) k_grad_f64(MolDev m, const double *__rest
         if (GGA)
           W[i][j] = 0.0;
       }
-    for (int k0 = 0; k0 < L.mpad; k0 += kKChunk) {
+    for (int k0 = 0; k0 < (L.nbf + kKChunk - 1) / kKChunk * kKChunk; k0 += kKChunk) {
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         const int idx = threadIdx.x + r * 256;
