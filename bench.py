@@ -308,8 +308,10 @@ def leaf_stats(dft):
 def algorithmic_bytes(kernel, cnt, m, npts, nbf, deriv):
     """Bytes a mixed-path kernel must move once per build in this layout
     (each AO plane is FP32 [block][mp][128]):
-      rho_mixed  phi (+ gradient) planes and the three exact-grid A-slice
-                 planes read once, rho (+ gradient) written, D2 read once
+      rho_mixed  phi (+ gradient) planes read once, the BF16 exact-grid
+                 A-slice images read once (three 128 x 64 BF16 tiles per K
+                 chunk of 64 AOs, the last chunk zero-padded), rho (+
+                 gradient) written, D2 read once
       func       rho and the grid read, Y hi / lo written from the phi
                  (+ gradient) planes, coefficients written
       vxc_mixed  phi hi / lo and Y hi / lo read once, V written once"""
@@ -318,7 +320,8 @@ def algorithmic_bytes(kernel, cnt, m, npts, nbf, deriv):
     pairs = float(np.sum(blocks * 128 * mp))  # point-AO entries of one plane
     ncomp = 4 if deriv else 1
     if kernel == "rho_mixed":
-        return (ncomp + 3) * 4 * pairs + 8 * ncomp * npts + 8.0 * nbf * nbf
+        a_images = float(np.sum(blocks * np.ceil(mp / 64.0))) * 3 * 128 * 64 * 2
+        return ncomp * 4 * pairs + a_images + 8 * ncomp * npts + 8.0 * nbf * nbf
     if kernel == "func":
         return (ncomp + 2) * 4 * pairs + (32 + 8 * ncomp + 8 * ncomp) * npts
     if kernel == "vxc_mixed":

@@ -27,6 +27,7 @@
 // The FP64 products of step 3 are taken in a different order than OCC's
 // sequential loop (rounding differences of ~1e-16 relative).
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "host/xc_host.hpp"
@@ -171,6 +172,8 @@ struct DevBuf {
 
 } // namespace
 
+constexpr int kMaxBeckeDevices = 64;
+
 size_t becke_smem_bytes(int natom) {
   // atom coordinates + per warp d (FP64) and two FP32 / int arrays
   return static_cast<size_t>(natom) * (3 * sizeof(double) + kBeckeWarps * 2 * sizeof(double));
@@ -239,9 +242,26 @@ void device_partition(int device, const PartitionInput &in, double *w_out) {
   up(off_own, in.owner, n * 4);
   up(off_wra, in.wra, n * 8);
   const size_t smem = becke_smem_bytes(in.natom);
-  cuda_check(cudaFuncSetAttribute(k_becke, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(smem)),
-             "cudaFuncSetAttribute");
+  {
+    // the kernel's shared-memory ceiling is a property of the function on
+    // this device, shared by every thread that builds a grid: raise it once,
+    // to the device's opt-in maximum, so that concurrent callers with smaller
+    // molecules never lower it under a larger one's launch
+    static std::mutex mu;
+    static bool raised[kMaxBeckeDevices] = {};
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 0 || device >= kMaxBeckeDevices)
+      throw ArgError("device ordinal out of range for the grid kernel");
+    if (!raised[device]) {
+      int optin = 0;
+      cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device),
+                 "cudaDeviceGetAttribute");
+      cuda_check(cudaFuncSetAttribute(k_becke, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      optin),
+                 "cudaFuncSetAttribute");
+      raised[device] = true;
+    }
+  }
   int sms = 0;
   cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device),
              "cudaDeviceGetAttribute");

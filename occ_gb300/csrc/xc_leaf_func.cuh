@@ -1,7 +1,7 @@
 // The functional stage of one Morton leaf, shared by the FP64 and the mixed
 // paths: include/occ/dft/dft.h:339-352 with src/dft/dft_kernels.cpp:27-70.
-// One CTA of 256 threads per leaf; a leaf may hold any number of points
-// (threads stride over them).  The leaf is skipped when max rho < thr
+// One CTA per leaf (256 threads, or NT); a leaf may hold any number of
+// points (threads stride over them).  The leaf is skipped when max rho < thr
 // (dft_kernels.cpp:37-40); coefficients are those of the V_xc contraction
 // (src/dft/xc_potential_matrix.cpp:19-41): coef0 = 0.5 w vrho and, for a GGA,
 // coef1..3 = 2 w vsigma grad rho.  epart2 receives {sum w e_xc rho, sum w rho}.
@@ -12,7 +12,8 @@
 
 namespace occx {
 
-__device__ __forceinline__ double leaf_sum256(double v, double *sh) {
+// Sum / maximum over the NT threads of the CTA (sh: NT / 32 doubles).
+template <int NT = 256> __device__ __forceinline__ double leaf_sum256(double v, double *sh) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
     v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -20,13 +21,13 @@ __device__ __forceinline__ double leaf_sum256(double v, double *sh) {
     sh[threadIdx.x >> 5] = v;
   __syncthreads();
   double s = 0.0;
-  for (int i = 0; i < 8; i++)
+  for (int i = 0; i < NT / 32; i++)
     s += sh[i];
   __syncthreads();
   return s;
 }
 
-__device__ __forceinline__ double leaf_max256(double v, double *sh) {
+template <int NT = 256> __device__ __forceinline__ double leaf_max256(double v, double *sh) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
     v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -34,26 +35,27 @@ __device__ __forceinline__ double leaf_max256(double v, double *sh) {
     sh[threadIdx.x >> 5] = v;
   __syncthreads();
   double s = sh[0];
-  for (int i = 1; i < 8; i++)
+  for (int i = 1; i < NT / 32; i++)
     s = fmax(s, sh[i]);
   __syncthreads();
   return s;
 }
 
 // MIXED: the mixed path's evaluator (double-float values, FP32 derivatives).
-template <bool DERIV, bool MIXED = false>
+// NT: threads of the CTA (they stride over the leaf's points).
+template <bool DERIV, bool MIXED = false, int NT = 256>
 __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__restrict__ pts,
                                                 size_t N, const FuncSet &fs, double thr,
                                                 const double *__restrict__ rho,
                                                 double *__restrict__ coef, double *epart2,
                                                 double *sh) {
   double mx = -1e300;
-  for (int p = threadIdx.x; p < L.cnt; p += 256)
+  for (int p = threadIdx.x; p < L.cnt; p += NT)
     mx = fmax(mx, rho[static_cast<size_t>(L.off) + p]);
-  mx = leaf_max256(mx, sh);
+  mx = leaf_max256<NT>(mx, sh);
   const bool skip = mx < thr;
   double nel = 0.0, ew = 0.0;
-  for (int p = threadIdx.x; p < L.cnt; p += 256) {
+  for (int p = threadIdx.x; p < L.cnt; p += NT) {
     const size_t idx = static_cast<size_t>(L.off) + p;
     const double r = rho[idx];
     const double w = pts[idx].w;
@@ -81,8 +83,8 @@ __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__r
     }
     ew += w * e;
   }
-  nel = leaf_sum256(nel, sh);
-  ew = leaf_sum256(ew, sh);
+  nel = leaf_sum256<NT>(nel, sh);
+  ew = leaf_sum256<NT>(ew, sh);
   if (threadIdx.x == 0) {
     epart2[0] = ew;
     epart2[1] = nel;

@@ -730,29 +730,41 @@ __global__ void __launch_bounds__(256) k_symmetrize(const MixTab *__restrict__ t
 // 512 AOs, acc2 collects the tail products (at most 2^-15 of the result).
 // One CTA per SM, persistent over blocks (most AOs first) from a global
 // queue, with a ring of block indices in shared memory and these roles:
-//   warp 12      block fetch, and per K chunk of 32 AOs one bulk copy of the
-//                block's precomputed A slices (k_colloc_f32)
+//   warp 12      block fetch, and per K chunk of 64 AOs one bulk copy of the
+//                block's precomputed BF16 A slices (k_colloc_f32)
 //   warps 4-11   B producers: D2 (hi, lo) gathered through the block's AO map
-//                for 64 columns j x 32 AOs k, sliced with t_j, into the stage
-//   warp 13      MMA issuer: eight TF32 MMAs per K step into acc0..acc2 of one
-//                of two TMEM buffers (3 x 64 columns each)
+//                for 64 columns j x 64 AOs k, sliced with t_j, into the stage
+//   warp 13      MMA issuer: eight BF16 MMAs per K step of 16 into acc0..acc2
+//                of one of two TMEM buffers (3 x 64 columns each)
+//   warp 14      epilogue loader: per 16 columns of a pass, bulk copies of
+//                phi (and grad phi) of those AOs into a ring of two slots
 //   warps 0-3    epilogue, one point per thread: X = acc0 + acc1 + acc2 and
-//                compensated FP32 dot products with phi and grad phi; rho
-//                and grad rho (FP64) when the block is done
+//                compensated FP32 dot products with phi and grad phi read
+//                from shared memory; rho and grad rho (FP64) when the block
+//                is done
+// The epilogue once read phi straight from global memory after each TMEM
+// load, with only four warps to hide that latency; staging it through the
+// loader takes the loads off its path.
 // Every wait is bounded; on expiry the error flag is set and all roles leave.
 constexpr int kRing = 4;                                   // depth of the work-item rings
 constexpr int kRhoN = 64;                                  // columns j per pass
-constexpr uint32_t kRhoStageB = 3 * (kRhoN * 128);        // B slices (64 x 32 each)
+constexpr uint32_t kRhoStageB = 3 * (kRhoN * 128);        // B slices (64 x 64 BF16 each)
 constexpr uint32_t kRhoStage = kRhoStageA + kRhoStageB;   // 72 KB
-constexpr int kRhoStages = 3;
-constexpr int kRhoThreads = 448;
+constexpr int kRhoStages = 2;
+constexpr int kRhoThreads = 480;
 constexpr int kRhoProd = 256;  // B producer threads (warps 4-11)
 constexpr int kRhoEpi = 128;   // epilogue threads (warps 0-3)
 constexpr int kRhoMap = 1024;  // AO maps up to this size are staged in shared memory
+constexpr int kEpiCols = 16;   // columns per epilogue slot
+constexpr int kEpiSlots = 2;
+constexpr uint32_t kEpiPlaneBytes = kEpiCols * kBlockPts * 4;      // 8 KB
+constexpr uint32_t kEpiSlotBytes = 4 * kEpiPlaneBytes;             // phi and grad phi
+constexpr uint32_t kEpiBytes = kEpiSlots * kEpiSlotBytes;          // 64 KB
 
 struct alignas(16) RhoSmem {
   uint64_t full[kRhoStages], empty[kRhoStages]; // per stage: B written, MMAs done
   uint64_t afull[kRhoStages];                     // per stage: the A bulk copy landed
+  uint64_t efull[kEpiSlots], eempty[kEpiSlots];   // per epilogue slot: landed, read
   uint64_t tfull[2], tempty[2];
   uint64_t ifull[kRing], iempty[kRing];
   uint64_t done;
@@ -760,7 +772,7 @@ struct alignas(16) RhoSmem {
   int ring[kRing];
   int gmap[kRhoMap]; // the producers' current AO map
 };
-constexpr uint32_t kRhoSmem = kRhoStages * kRhoStage + sizeof(RhoSmem) + 1024;
+constexpr uint32_t kRhoSmem = kRhoStages * kRhoStage + kEpiBytes + sizeof(RhoSmem) + 1024;
 static_assert(kRhoSmem <= 232448, "density kernel exceeds the shared memory of a CTA");
 
 __device__ __forceinline__ void bar_named(int id, int n) {
@@ -789,13 +801,20 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
                 const int *__restrict__ order, int nblocks, int *queue, int *err, int tk = 0) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
-  RhoSmem *sm = reinterpret_cast<RhoSmem *>(smem + kRhoStages * kRhoStage);
+  uint8_t *ebuf = smem + kRhoStages * kRhoStage; // epilogue slots
+  RhoSmem *sm = reinterpret_cast<RhoSmem *>(ebuf + kEpiBytes);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  // AO planes the epilogue reads: phi (and its gradient), or d_k phi (TAU)
+  constexpr int kEpiPlanes = (DERIV && !TAU) ? 4 : 1;
   if (t == 0) {
     for (int s = 0; s < kRhoStages; s++) {
       umma::mbar_init(&sm->full[s], kRhoProd);
       umma::mbar_init(&sm->afull[s], 1);
       umma::mbar_init(&sm->empty[s], 1);
+    }
+    for (int e = 0; e < kEpiSlots; e++) {
+      umma::mbar_init(&sm->efull[e], 1);
+      umma::mbar_init(&sm->eempty[e], kRhoEpi);
     }
     for (int b = 0; b < 2; b++) {
       umma::mbar_init(&sm->tfull[b], 1);
@@ -803,7 +822,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     }
     for (int r = 0; r < kRing; r++) {
       umma::mbar_init(&sm->ifull[r], 1);
-      umma::mbar_init(&sm->iempty[r], 1 + kRhoProd + kRhoEpi);
+      umma::mbar_init(&sm->iempty[r], 2 + kRhoProd + kRhoEpi);
     }
     umma::mbar_init(&sm->done, 1);
     umma::fence_proxy_async();
@@ -1001,19 +1020,50 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
         umma::mbar_wait(&sm->done, 0, kWaitIter);
       }
     }
+  } else if (warp == 14) {
+    // ---- epilogue loader (lane 0): the AO values of each 16 columns of a
+    // pass into a slot, in the order the epilogue consumes them ----
+    if (lane == 0) {
+      uint32_t e = 0; // slots filled
+      for (int k = 0; ok; k++) {
+        const int bi = next_block(k);
+        if (bi < 0)
+          break;
+        const MBlock B = blocks[bi];
+        const MixTab &T = tabs[B.mol];
+        const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
+        const float *src = T.ws + B.ws_off + (TAU ? tk * plane : 0);
+        for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN) {
+          const int N = min(kRhoN, B.mp - n0);
+          for (int k0 = 0; k0 < B.mp && ok; k0 += kExactKSeg)
+            for (int c0 = 0; c0 < N && ok; c0 += kEpiCols, e++) {
+              const int slot = e % kEpiSlots;
+              const uint32_t use = e / kEpiSlots;
+              if (use > 0 && !wait(&sm->eempty[slot], (use - 1) & 1))
+                break;
+              umma::mbar_arrive_expect_tx(&sm->efull[slot], kEpiPlanes * kEpiPlaneBytes);
+              for (int c = 0; c < kEpiPlanes; c++)
+                umma::bulk_load(ebuf + slot * kEpiSlotBytes + c * kEpiPlaneBytes,
+                                src + c * plane + static_cast<size_t>(n0 + c0) * kBlockPts,
+                                kEpiPlaneBytes, &sm->efull[slot]);
+            }
+        }
+      }
+      // copies still in flight land before the CTA leaves
+      for (uint32_t q = (e >= kEpiSlots ? e - kEpiSlots : 0); q < e; q++)
+        umma::mbar_wait(&sm->efull[q % kEpiSlots], (q / kEpiSlots) & 1, kWaitIter);
+    }
   } else if (epi) {
     // ---- epilogue: thread t holds point t of the block ----
     const int quad = warp;
     const int p = t;
-    uint32_t sc = 0;
+    uint32_t sc = 0, e = 0; // segments, epilogue slots consumed
     for (int k = 0; ok; k++) {
       const int bi = next_block(k);
       if (bi < 0)
         break;
       const MBlock B = blocks[bi];
       const MixTab &T = tabs[B.mol];
-      const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
-      const float *phi = T.ws + B.ws_off + (TAU ? tk * plane : 0);
       float acc[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
       for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN) {
         const int N = min(kRhoN, B.mp - n0);
@@ -1024,26 +1074,33 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
             break;
           umma::fence_after_sync();
           const uint32_t lanebase = tmem + (static_cast<uint32_t>(quad * 32) << 16) + buf * 256;
-          for (int c0 = 0; c0 < N; c0 += 16) {
+          for (int c0 = 0; c0 < N; c0 += kEpiCols, e++) {
+            const int slot = e % kEpiSlots;
+            wait(&sm->efull[slot], (e / kEpiSlots) & 1);
+            if (!agree())
+              break;
+            const float *eph =
+                reinterpret_cast<const float *>(ebuf + slot * kEpiSlotBytes) + p;
             uint32_t r0[16], r1[16], r2[16];
             umma::tmem_ld16(lanebase + c0, r0);
             umma::tmem_ld16(lanebase + kRhoN + c0, r1);
             umma::tmem_ld16(lanebase + 2 * kRhoN + c0, r2);
             umma::tmem_wait_ld();
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
+            for (int i = 0; i < kEpiCols; i++) {
               const float x = __fadd_rn(__uint_as_float(r0[i]),
                                         __fadd_rn(__uint_as_float(r1[i]), __uint_as_float(r2[i])));
-              const size_t o = static_cast<size_t>(n0 + c0 + i) * kBlockPts + p;
+              const int o = i * kBlockPts;
               // rho (the energy's direct input) with compensation; its
               // gradient, which enters through sigma, by plain FP32 FMAs
-              dot2_step(phi[o], x, acc[0], cmp[0]);
+              dot2_step(eph[o], x, acc[0], cmp[0]);
               if (DERIV && !TAU) {
-                acc[1] = fmaf(phi[plane + o], x, acc[1]);
-                acc[2] = fmaf(phi[2 * plane + o], x, acc[2]);
-                acc[3] = fmaf(phi[3 * plane + o], x, acc[3]);
+                acc[1] = fmaf(eph[kEpiCols * kBlockPts + o], x, acc[1]);
+                acc[2] = fmaf(eph[2 * kEpiCols * kBlockPts + o], x, acc[2]);
+                acc[3] = fmaf(eph[3 * kEpiCols * kBlockPts + o], x, acc[3]);
               }
             }
+            umma::mbar_arrive(&sm->eempty[slot]);
           }
           umma::fence_before_sync();
           umma::mbar_arrive(&sm->tempty[buf]);
@@ -1476,18 +1533,22 @@ __device__ __forceinline__ double bsum256(double v, double *sh) {
 }
 
 // ... followed by the V_xc operand Y of each of the leaf's blocks (ymix_block):
-// the FP64-bound functional of one CTA overlaps the HBM-bound Y streaming of
-// the other CTA on the SM.
+// the latency-bound functional of some CTAs overlaps the HBM-bound Y
+// streaming of the others on the SM.  128 threads, one per point of a full
+// block (a CTA of 256 left half of its threads idle in the functional, with
+// eight active warps an SM).
+constexpr int kFuncThreads = 128;
 template <bool DERIV>
-__global__ void __launch_bounds__(256, 2) k_func_b(const MixTab *__restrict__ tabs,
-                                                const MBlock *__restrict__ blocks,
-                                                const LeafItem *__restrict__ litems) {
-  __shared__ double sh[8];
+__global__ void __launch_bounds__(kFuncThreads, 4) k_func_b(const MixTab *__restrict__ tabs,
+                                                         const MBlock *__restrict__ blocks,
+                                                         const LeafItem *__restrict__ litems) {
+  __shared__ double sh[kFuncThreads / 32];
   __shared__ float4 cf[kBlockPts];
   const LeafItem li = litems[blockIdx.x];
   const MixTab &T = tabs[li.mol];
-  leaf_functional<DERIV, true>(T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts),
-                               T.fs, T.dens_thr, T.rho, T.coef, T.epart + 2 * li.leaf, sh);
+  leaf_functional<DERIV, true, kFuncThreads>(T.m.leaves[li.leaf], T.m.pts,
+                                             static_cast<size_t>(T.m.npts), T.fs, T.dens_thr,
+                                             T.rho, T.coef, T.epart + 2 * li.leaf, sh);
   __syncthreads(); // the leaf's coefficients are written
   for (int b = 0; b < li.nblk; b++)
     ymix_block<DERIV>(T, blocks[li.block0 + b], cf);
@@ -1824,9 +1885,9 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
   if (nl > 0)
     c.launch("func", st, [&] {
       if (P.deriv)
-        k_func_b<true><<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_b<true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
       else
-        k_func_b<false><<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_b<false><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
     });
   if (ni > 0)
     c.launch("vxc_mixed", st, [&] {
@@ -3060,9 +3121,9 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
   if (nl > 0)
     c.launch("func", st, [&] {
       if (P.deriv)
-        k_func_b<true><<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_b<true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
       else
-        k_func_b<false><<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_b<false><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
     });
   if (nb > 0)
     c.launch("grad_ops", st, [&] {
