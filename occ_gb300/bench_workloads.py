@@ -167,13 +167,20 @@ def serve_stream(precision, nreq=32, rate=10.0, seed=0, budget=150e9, sessions=N
     gaps = rng.exponential(1.0 / rate, nreq)
     arrivals = np.cumsum(gaps) - gaps[0]
     if sessions is None:
+        # inputs made before the clock starts: each request's basis and its
+        # sequence of densities (the first a seeded guess, then perturbed by
+        # seeded symmetric noise per iteration), so that the client submits
+        # as fast as results come back
         sessions = []
         for i in range(nreq):
             n = int(rng.integers(2, 49))
             mol = wl.water_cluster(n, box=10.0 * (n / 32.0) ** (1.0 / 3.0), seed=seed + 100 + i)
             b = wl.basis_for(mol, "def2-svp")
-            sessions.append((b, wl.random_density(b.nbf(), 5 * n, seed=seed + 300 + i),
-                             int(rng.integers(8, 21))))
+            iters = int(rng.integers(8, 21))
+            Ds = [wl.random_density(b.nbf(), 5 * n, seed=seed + 300 + i)]
+            for it in range(1, iters):
+                Ds.append(wl.perturbed(Ds[-1], 1e-3, seed + 10000 * i + it))
+            sessions.append((b, Ds, iters))
     srv = Server(precision=precision, hbm_budget_bytes=budget)
     pool = ThreadPoolExecutor(max_workers=8)
     try:
@@ -199,7 +206,7 @@ def serve_stream(precision, nreq=32, rate=10.0, seed=0, budget=150e9, sessions=N
                     continue
                 sid, dt = f.result()
                 open_s.append(dt)
-                D0 = sessions[r][1]
+                D0 = sessions[r][1][0]
                 state[r] = [0, srv.submit(sid, D0), D0, sid]
                 h2d += D0.size * 8
                 del opening[r]
@@ -215,7 +222,7 @@ def serve_stream(precision, nreq=32, rate=10.0, seed=0, budget=150e9, sessions=N
                 if it == 0:
                     first_ms.append((time.perf_counter() - t0 - arrivals[r]) * 1e3)
                 if it + 1 < sessions[r][2]:
-                    Dn = wl.perturbed(D, 1e-3, seed + 10000 * r + it + 1)
+                    Dn = sessions[r][1][it + 1]
                     state[r] = [it + 1, srv.submit(sid, Dn), Dn, sid]
                     h2d += Dn.size * 8
                 else:

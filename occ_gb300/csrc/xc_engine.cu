@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -132,8 +133,15 @@ void *Molecule::alloc(size_t bytes) {
 static size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
 void Molecule::build_plan() {
-  morton_leaves(grid, bs, plan);
-  screen_leaves(basis, bs, plan);
+  // on the molecule's GPU; OCC_XC_PLAN=host selects the host restatement
+  // (host/plan.cpp), which gives the same plan (tests compare the two)
+  const char *sel = std::getenv("OCC_XC_PLAN");
+  if (sel && std::strcmp(sel, "host") == 0) {
+    morton_leaves(grid, bs, plan);
+    screen_leaves(basis, bs, plan);
+  } else {
+    device_plan(device, grid, basis, bs, plan);
+  }
   const int ncomp = deriv ? 4 : 1;
   leaves.clear();
   leaf_sh.clear();

@@ -59,6 +59,10 @@ void launch_reduce3(const double *epart3, int n, double *out3, cudaStream_t st);
 // shared memory holds natom atoms.
 bool device_partition_fits(int device, int natom);
 void device_partition(int device, const PartitionInput &in, double *w);
+// The build plan (Morton order, leaves, screening) on the GPU (xc_plan.cu);
+// the same plan as host/plan.cpp's morton_leaves + screen_leaves.
+void device_plan(int device, const MolecularGrid &grid, const Basis &basis,
+                 const BuildSettings &bs, Plan &plan);
 FuncSet parse_method(const std::string &method);
 void upload_sph_table_mixed();
 struct MixedState;

@@ -929,36 +929,50 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
         const bool jv = lj < L.nbf;
         const size_t gj = jv ? static_cast<size_t>(gm[lj]) : 0;
         const float sB = jv ? T.colb[gj] : 1.f, isB = 1.f / sB;
-        for (int k0 = 0; k0 < B.mp && ok; k0 += kExactKSeg)
-          for (int c = 0; c < seg_chunks(B.mp, k0); c++, g++) {
-            const int s = g % kRhoStages;
-            const uint32_t use = g / kRhoStages;
-            if (use > 0 && !wait(&sm->empty[s], (use - 1) & 1))
-              break;
-            uint8_t *st = smem + s * kRhoStage + kRhoStageA;
-            float2 d[2][8];
+        // the pass's K chunks of 64 AOs in the order of the segments and
+        // chunks the loader and the MMA issuer walk; each chunk's gathers
+        // are issued one chunk ahead, so that their latency overlaps the
+        // wait for the stage and the slicing of the previous chunk
+        const int nq = (B.mp + kKcR - 1) / kKcR;
+        auto fetch = [&](int q, float2(&d)[2][8]) {
 #pragma unroll
-            for (int r = 0; r < 2; r++)
+          for (int r = 0; r < 2; r++)
 #pragma unroll
-              for (int e = 0; e < 8; e++) {
-                const int lk = k0 + c * kKcR + (qb + 4 * r) * 8 + e;
-                d[r][e] = (jv && lk < L.nbf) ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
-                                             : make_float2(0.f, 0.f);
-              }
-#pragma unroll
-            for (int r = 0; r < 2; r++) {
-              float v[8], lo[8];
-#pragma unroll
-              for (int e = 0; e < 8; e++) {
-                v[e] = d[r][e].x;
-                lo[e] = d[r][e].y;
-              }
-              store8_exact_bf16(st, st + kRhoN * 128, st + 2 * kRhoN * 128, jr, qb + 4 * r, v,
-                                sB, isB, lo);
+            for (int e = 0; e < 8; e++) {
+              const int lk = q * kKcR + (qb + 4 * r) * 8 + e;
+              d[r][e] = (jv && lk < L.nbf) ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
+                                           : make_float2(0.f, 0.f);
             }
-            umma::fence_proxy_async();
-            umma::mbar_arrive(&sm->full[s]);
+        };
+        float2 cur[2][8], nxt[2][8];
+        fetch(0, cur);
+        for (int q = 0; q < nq && ok; q++, g++) {
+          if (q + 1 < nq)
+            fetch(q + 1, nxt);
+          const int s = g % kRhoStages;
+          const uint32_t use = g / kRhoStages;
+          if (use > 0 && !wait(&sm->empty[s], (use - 1) & 1))
+            break;
+          uint8_t *st = smem + s * kRhoStage + kRhoStageA;
+#pragma unroll
+          for (int r = 0; r < 2; r++) {
+            float v[8], lo[8];
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+              v[e] = cur[r][e].x;
+              lo[e] = cur[r][e].y;
+            }
+            store8_exact_bf16(st, st + kRhoN * 128, st + 2 * kRhoN * 128, jr, qb + 4 * r, v,
+                              sB, isB, lo);
           }
+          umma::fence_proxy_async();
+          umma::mbar_arrive(&sm->full[s]);
+#pragma unroll
+          for (int r = 0; r < 2; r++)
+#pragma unroll
+            for (int e = 0; e < 8; e++)
+              cur[r][e] = nxt[r][e];
+        }
       }
     }
   } else if (warp == 13) {

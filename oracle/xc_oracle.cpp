@@ -110,8 +110,18 @@ void collocate(int l, bool pure, int nprim, const double *exps, const double *co
   if (pure)
     T = spherical_transform(l);
   const double fac = common_fac(l, pure);
+  // the shell's Cartesian components in CCA order, hoisted out of the point loop
+  struct Comp {
+    int a, b, c, i;
+  };
+  std::vector<Comp> comps;
+  for (int a = l; a >= 0; a--)
+    for (int b = l - a; b >= 0; b--)
+      comps.push_back({a, b, l - a - b, cart_index(l, a, b)});
   std::vector<double> cart(10 * nc);
   static const int hi[6] = {0, 0, 0, 1, 1, 2}, hj[6] = {0, 1, 2, 1, 2, 2};
+  const int ncomp = deriv > 1 ? 10 : (deriv ? 4 : 1);
+  double xp[8], yp[8], zp[8]; // powers 0..l (l <= 6), built by repeated products
   for (long p = 0; p < n; p++) {
     double x = xyz[3 * p] - A[0], y = xyz[3 * p + 1] - A[1], z = xyz[3 * p + 2] - A[2];
     double r2 = x * x + y * y + z * z;
@@ -119,39 +129,45 @@ void collocate(int l, bool pure, int nprim, const double *exps, const double *co
     for (int k = 0; k < nprim; k++) {
       double e = coefs[k] * std::exp(-exps[k] * r2);
       R += e;
-      dR += -2.0 * exps[k] * e;
-      d2R += 4.0 * exps[k] * exps[k] * e;
+      if (deriv) {
+        dR += -2.0 * exps[k] * e;
+        if (deriv > 1)
+          d2R += 4.0 * exps[k] * exps[k] * e;
+      }
+    }
+    xp[0] = yp[0] = zp[0] = 1.0;
+    for (int k = 1; k <= l; k++) {
+      xp[k] = xp[k - 1] * x;
+      yp[k] = yp[k - 1] * y;
+      zp[k] = zp[k - 1] * z;
     }
     const double r[3] = {x, y, z};
-    for (int a = l; a >= 0; a--)
-      for (int b = l - a; b >= 0; b--) {
-        int c = l - a - b;
-        int i = cart_index(l, a, b);
-        double mono = ipow(x, a) * ipow(y, b) * ipow(z, c);
-        cart[i] = mono * R;
-        if (deriv) {
-          double gx = (a > 0 ? a * ipow(x, a - 1) * ipow(y, b) * ipow(z, c) : 0.0);
-          double gy = (b > 0 ? b * ipow(x, a) * ipow(y, b - 1) * ipow(z, c) : 0.0);
-          double gz = (c > 0 ? c * ipow(x, a) * ipow(y, b) * ipow(z, c - 1) : 0.0);
-          cart[nc + i] = gx * R + mono * x * dR;
-          cart[2 * nc + i] = gy * R + mono * y * dR;
-          cart[3 * nc + i] = gz * R + mono * z * dR;
-          if (deriv > 1) {
-            const double M1[3] = {gx, gy, gz};
-            const int pw[3] = {a, b, c};
-            for (int q = 0; q < 6; q++) {
-              const int u = hi[q], v = hj[q];
-              int k[3] = {0, 0, 0};
-              k[u]++;
-              k[v]++;
-              const double Mij = dpow(x, pw[0], k[0]) * dpow(y, pw[1], k[1]) * dpow(z, pw[2], k[2]);
-              cart[(4 + q) * nc + i] = Mij * R + (M1[u] * r[v] + M1[v] * r[u]) * dR +
-                                       mono * (r[u] * r[v] * d2R + (u == v ? dR : 0.0));
-            }
+    for (const Comp &cp : comps) {
+      const int a = cp.a, b = cp.b, c = cp.c, i = cp.i;
+      double mono = xp[a] * yp[b] * zp[c];
+      cart[i] = mono * R;
+      if (deriv) {
+        double gx = (a > 0 ? a * xp[a - 1] * yp[b] * zp[c] : 0.0);
+        double gy = (b > 0 ? b * xp[a] * yp[b - 1] * zp[c] : 0.0);
+        double gz = (c > 0 ? c * xp[a] * yp[b] * zp[c - 1] : 0.0);
+        cart[nc + i] = gx * R + mono * x * dR;
+        cart[2 * nc + i] = gy * R + mono * y * dR;
+        cart[3 * nc + i] = gz * R + mono * z * dR;
+        if (deriv > 1) {
+          const double M1[3] = {gx, gy, gz};
+          const int pw[3] = {a, b, c};
+          for (int q = 0; q < 6; q++) {
+            const int u = hi[q], v = hj[q];
+            int k[3] = {0, 0, 0};
+            k[u]++;
+            k[v]++;
+            const double Mij = dpow(x, pw[0], k[0]) * dpow(y, pw[1], k[1]) * dpow(z, pw[2], k[2]);
+            cart[(4 + q) * nc + i] = Mij * R + (M1[u] * r[v] + M1[v] * r[u]) * dR +
+                                     mono * (r[u] * r[v] * d2R + (u == v ? dR : 0.0));
           }
         }
       }
-    int ncomp = deriv > 1 ? 10 : (deriv ? 4 : 1);
+    }
     for (int q = 0; q < ncomp; q++)
       for (int f = 0; f < nf; f++) {
         double v;
