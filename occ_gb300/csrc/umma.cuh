@@ -103,8 +103,12 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
 }
 
 // 32 lanes x 32 bits, 16 consecutive columns starting at taddr.  The warp
-// reads its own 32-lane quarter of TMEM (lane field of taddr).
+// reads its own 32-lane quarter of TMEM (lane field of taddr).  The load is
+// warp-collective (.sync.aligned): every lane must execute it together, so
+// the warp is reconverged first (its lanes may leave a preceding mbarrier
+// poll in different iterations).
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  __syncwarp();
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
                "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
@@ -113,6 +117,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
                : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_wait_ld() {
+  __syncwarp();
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 

@@ -1114,6 +1114,10 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
                 acc[3] = fmaf(eph[3 * kEpiCols * kBlockPts + o], x, acc[3]);
               }
             }
+            // the slot's next fill is a bulk copy (async proxy): order this
+            // thread's generic-proxy reads of it before that write (without
+            // the fence a build now and then read a refilled slot)
+            umma::fence_proxy_async();
             umma::mbar_arrive(&sm->eempty[slot]);
           }
           umma::fence_before_sync();
