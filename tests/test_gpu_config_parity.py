@@ -60,3 +60,17 @@ def test_alkane_c30_def2tzvp_b3lyp_against_oracle():
     assert basis.nbf() == 1302
     D = wl.random_density(basis.nbf(), 121, seed=0)
     _both("b3lyp", basis, D)
+
+
+def test_water32_mixed_builds_repeat_exactly():
+    """Twenty tensor-core builds of the same input give the same E_xc and
+    V_xc: every stage's shared-memory hand-offs are ordered (a missing proxy
+    fence once let one build in three read a refilled buffer)."""
+    basis, D = water32()
+    dft = og.DFT("pbe", basis)
+    V0 = dft.compute_vxc(D, og.MIXED)
+    e0 = dft.exchange_correlation_energy()
+    for _ in range(20):
+        V = dft.compute_vxc(D, og.MIXED)
+        assert abs(dft.exchange_correlation_energy() - e0) <= 1e-12
+        assert np.max(np.abs(V - V0)) <= 1e-12
