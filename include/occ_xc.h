@@ -187,6 +187,27 @@ int occ_xc_nlc_vv10(occ_xc_context *ctx, occ_xc_molecule *mol, const double *D, 
 int occ_xc_nlc_grid_points(const occ_xc_molecule *mol, long *npoints);
 int occ_xc_nlc_grid(const occ_xc_molecule *mol, double *points, double *weights);
 
+/* Seminumerical (COSX) exchange, the ESP form of OCC's
+ * SemiNumericalExchange (include/occ/qm/seminumerical_exchange.h:104-118,
+ * src/qm/seminumerical_exchange.cpp:233-250 set-up, :516-529 restricted K,
+ * :714-855 the grid sweep), replacing its constructor and compute_K(mo) for
+ * a restricted wavefunction.  occ_xc_cosx_create builds, on `mol`'s device
+ * and over its basis, the grid of `grid` (NULL: GridSettings::for_sgx(50),
+ * src/numint/grid_settings.cpp:59-68), its AO values, the numerical overlap
+ * S_num and the overlap projector Q = S_num^-1 S; shells up to d
+ * (OCC_XC_ERR_ARG above).  Every operation is FP64. */
+typedef struct occ_xc_cosx occ_xc_cosx;
+int occ_xc_cosx_create(occ_xc_context *ctx, occ_xc_molecule *mol,
+                       const occ_xc_grid_settings *grid, occ_xc_cosx **out);
+void occ_xc_cosx_destroy(occ_xc_cosx *cx);
+/* Points of the exchange grid. */
+int occ_xc_cosx_grid_points(const occ_xc_cosx *cx, long *npoints);
+/* K (nbf x nbf, symmetric) of mo.D = D (nbf x nbf); host buffers, blocking. */
+int occ_xc_cosx_exchange(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D, double *K);
+/* The same on device buffers, asynchronous on `stream` (NULL: the context's). */
+int occ_xc_cosx_exchange_device(occ_xc_context *ctx, occ_xc_cosx *cx, const double *d_D,
+                                double *d_K, void *stream);
+
 /* Replaces DFT::compute_xc_gradient(mo) for a restricted wavefunction
  * (include/occ/dft/dft.h:599-749, src/dft/dft_gradient_kernels.cpp:472-595):
  * dE_xc/dR with the grid held fixed.  grad[3*natoms] receives x, y, z per

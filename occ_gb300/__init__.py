@@ -16,6 +16,7 @@ from .xc import (  # noqa: F401
     Graph,
     GridSettings,
     Molecule,
+    SemiNumericalExchange,
     Server,
     Shell,
     XCError,

@@ -18,7 +18,7 @@ LIB = os.path.join(OUT_DIR, "libocc_xc.so")
 
 CU_SOURCES = ["xc_fp64.cu", "xc_mixed.cu", "xc_engine.cu", "xc_noalloc.cu", "xc_server.cu",
               "xc_tune.cu", "xc_grad.cu", "xc_grid.cu", "xc_uks.cu",
-              "xc_vv10.cu", "xc_plan.cu"]
+              "xc_vv10.cu", "xc_plan.cu", "xc_cosx.cu"]
 CXX_SOURCES = ["host/basis.cpp", "host/grid.cpp", "host/plan.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1,0 +1,739 @@
+// Seminumerical exchange (COSX, the ESP form) on the GPU: OCC's
+// SemiNumericalExchange with set_use_esp(true)
+// (src/qm/seminumerical_exchange.cpp:233-250 set-up, :517-529 restricted
+// build, :714-855 the grid sweep), on the grid of GridSettings::for_sgx(n)
+// (src/numint/grid_settings.cpp:59-68).
+//
+// Set-up (once per molecule and angular order): a second molecule over the
+// same basis on the SGX grid (n angular points on every shell, LMG radial
+// precision 1e-5, no pruning, no reduced H / He grid), its AO values, the
+// numerical overlap S_num = sum_g w_g phi phi^T (the FP64 V_xc kernel with
+// coefficient w / 2), the analytic overlap S (McMurchie-Davidson, host) and
+// the overlap projector Q = S_num^-1 S (Cholesky solve, host); the shell
+// pairs' primitive-pair tables (exponent sum, centre, prefactor, Hermite
+// expansion coefficients E^{ij}_t per axis).
+//
+// Per call, for mo.D:
+//   k_cosx_d2q    D2q = Q (2 D), row-major
+//   k_cosx_mask   shell pair (p, q) kept when max |D2q| over its two blocks
+//                 reaches 1e-6 (the reference's density screen)
+//   per group of leaves (a workspace cap bounds the point-major F and G):
+//   k_cosx_f      F[g, lambda] = w_g sum_sigma phi_sigma(g) D2q[sigma, lambda]
+//   k_cosx_g      G[g, nu] -= sum_mu F[g, mu] V_g(mu, nu) (and the transposed
+//                 block for p != q), V_g(mu, nu) = int phi_mu phi_nu / |r - g|
+//                 by McMurchie-Davidson over the Boys function, one thread
+//                 per grid point, every kept pair
+//   k_cosx_k      K'[mu, lambda] -= sum_g phi_mu(g) G[g, lambda]
+//   k_cosx_sym    K = (K' + K'^T) / 4
+// All in FP64.  The reference's per-batch geometric screen of shell pairs is
+// not applied (every kept pair reaches every point).  Shells up to d.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "../../include/occ_xc.h"
+#include "host/xc_host.hpp"
+#include "xc_device.cuh"
+#include "xc_engine.hpp"
+
+namespace occx {
+namespace {
+
+constexpr int kCosxLmax = 2;                   // shells up to d
+constexpr int kCosxNc = 6;                     // Cartesian components of a d shell
+constexpr int kCosxR = 35;                     // R_tuv with t + u + v <= 4
+constexpr double kCosxDensityThreshold = 1e-6; // seminumerical_exchange.cpp:789
+constexpr double kPi = 3.14159265358979323846;
+
+// Cartesian powers of the components of a shell (CCA order), packed a | b<<4 | c<<8.
+__constant__ int c_cx_comp[3][kCosxNc];
+// Real solid-harmonic transforms (m = -l..l) of l = 0..2, T[f][i], and the
+// identity for Cartesian shells.
+__constant__ double c_cx_T[3][5][kCosxNc];
+
+struct CxPair {
+  int bf_p, bf_q, np, nq;   // first AO and AO count of each shell
+  int la, lb, prim0, nprim; // angular momenta, primitive-pair range
+};
+struct CxPrim {
+  double pexp, P[3], pref; // a + b, centre, c_a c_b 2 pi / p fac_a fac_b
+  int e_off;               // E tables: 3 axes x (la+1)(lb+1)(la+lb+1)
+  int pad;
+};
+
+// Index of R_tuv (t + u + v <= 4) in a packed array: by shell of degree s,
+// then t descending, then u descending.
+__host__ __device__ constexpr int r_index(int t, int u, int v) {
+  return (t + u + v) * (t + u + v + 1) * (t + u + v + 2) / 6 +
+         ((u + v) * (u + v + 1)) / 2 + v;
+}
+
+// F_n(T), n = 0..nmax (nmax <= 8): for T < 36 the series
+// F_n(T) = e^-T sum_k (2T)^k / ((2n+1)(2n+3)...(2n+2k+1)) for n = nmax and
+// downward recursion F_{n-1} = (2T F_n + e^-T) / (2n - 1); beyond, the
+// asymptotic F_0 = (pi / T)^{1/2} / 2 (erf(sqrt T) = 1 to 1e-17) and upward
+// recursion F_{n+1} = ((2n+1) F_n - e^-T) / (2T).
+__device__ __forceinline__ void boys(int nmax, double T, double *F) {
+  const double et = exp(-T);
+  if (T < 36.0) {
+    double term = 1.0 / (2 * nmax + 1), sum = term;
+    for (int k = 1; k < 256; k++) {
+      term *= 2.0 * T / (2 * nmax + 2 * k + 1);
+      sum += term;
+      if (term < 1e-17 * sum)
+        break;
+    }
+    F[nmax] = et * sum;
+    for (int n = nmax; n > 0; n--)
+      F[n - 1] = (2.0 * T * F[n] + et) / (2 * n - 1);
+  } else {
+    F[0] = 0.5 * sqrt(kPi / T);
+    for (int n = 0; n < nmax; n++)
+      F[n + 1] = ((2 * n + 1) * F[n] - et) / (2.0 * T);
+  }
+}
+
+// R_tuv^(0), t + u + v <= L, for exponent p and PC = P - C (McMurchie-
+// Davidson recursion from R^(n)_000 = (-2p)^n F_n, level by level).
+__device__ __forceinline__ void hermite_r(int L, double p, double X, double Y, double Z,
+                                          double *R) {
+  double F[kCosxLmax * 2 + 1];
+  boys(L, p * (X * X + Y * Y + Z * Z), F);
+  double up[kCosxR], cur[kCosxR];
+  double m2p = 1.0;
+  for (int n = 0; n < L; n++)
+    m2p *= -2.0 * p;
+  for (int n = L; n >= 0; n--) { // level n holds t + u + v <= L - n
+    const int smax = L - n;
+    for (int s = 0; s <= smax; s++)
+      for (int t = s; t >= 0; t--)
+        for (int u = s - t; u >= 0; u--) {
+          const int v = s - t - u;
+          double val;
+          if (s == 0)
+            val = m2p * F[n];
+          else if (t > 0)
+            val = (t > 1 ? (t - 1) * up[r_index(t - 2, u, v)] : 0.0) + X * up[r_index(t - 1, u, v)];
+          else if (u > 0)
+            val = (u > 1 ? (u - 1) * up[r_index(t, u - 2, v)] : 0.0) + Y * up[r_index(t, u - 1, v)];
+          else
+            val = (v > 1 ? (v - 1) * up[r_index(t, u, v - 2)] : 0.0) + Z * up[r_index(t, u, v - 1)];
+          cur[r_index(t, u, v)] = val;
+        }
+    for (int i = 0; i < (smax + 1) * (smax + 2) * (smax + 3) / 6; i++)
+      up[i] = cur[i];
+    if (n > 0)
+      m2p /= -2.0 * p;
+  }
+  for (int i = 0; i < (L + 1) * (L + 2) * (L + 3) / 6; i++)
+    R[i] = up[i];
+}
+
+// D2q = Q (2 D): Q, D column-major nbf x nbf; out row-major.  16 x 16 tiles.
+__global__ void k_cosx_d2q(int nbf, const double *__restrict__ Q, const double *__restrict__ D,
+                           double *__restrict__ D2q) {
+  __shared__ double Qs[16][17], Ds[16][17];
+  const int lam = blockIdx.x * 16 + threadIdx.x, sig = blockIdx.y * 16 + threadIdx.y;
+  double acc = 0.0;
+  for (int k0 = 0; k0 < nbf; k0 += 16) {
+    const int kq = k0 + threadIdx.x, kd = k0 + threadIdx.y;
+    Qs[threadIdx.y][threadIdx.x] = (sig < nbf && kq < nbf) ? Q[static_cast<size_t>(kq) * nbf + sig] : 0.0;
+    Ds[threadIdx.y][threadIdx.x] = (kd < nbf && lam < nbf) ? D[static_cast<size_t>(lam) * nbf + kd] : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+      acc = fma(Qs[threadIdx.y][k], Ds[k][threadIdx.x], acc);
+    __syncthreads();
+  }
+  if (sig < nbf && lam < nbf)
+    D2q[static_cast<size_t>(sig) * nbf + lam] = 2.0 * acc;
+}
+
+__global__ void k_cosx_mask(int npairs, int nbf, const CxPair *__restrict__ pairs,
+                            const double *__restrict__ D2q, int *__restrict__ mask) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= npairs)
+    return;
+  const CxPair P = pairs[k];
+  double mx = 0.0;
+  for (int i = 0; i < P.np; i++)
+    for (int j = 0; j < P.nq; j++) {
+      mx = fmax(mx, fabs(D2q[static_cast<size_t>(P.bf_p + i) * nbf + P.bf_q + j]));
+      mx = fmax(mx, fabs(D2q[static_cast<size_t>(P.bf_q + j) * nbf + P.bf_p + i]));
+    }
+  mask[k] = mx >= kCosxDensityThreshold ? 1 : 0;
+}
+
+// F[g, lambda] for the points of leaves l0 .. l0 + gridDim.x - 1 (g counted
+// from the group's first point off0); thread lambda.
+__global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restrict__ ws, int l0,
+                                                int off0, const double *__restrict__ D2q,
+                                                double *__restrict__ F) {
+  const DevLeaf L = m.leaves[l0 + blockIdx.x];
+  const int lam = blockIdx.y * blockDim.x + threadIdx.x;
+  if (lam >= m.nbf)
+    return;
+  const double *phi = ws + L.ws_off;
+  const int *g = m.leaf_ao + L.ao_begin;
+  const size_t nbf = static_cast<size_t>(m.nbf);
+  for (int p = 0; p < L.cnt; p++) {
+    double acc = 0.0;
+    for (int s = 0; s < L.nbf; s++)
+      acc = fma(phi[static_cast<size_t>(s) * L.npad + p], D2q[static_cast<size_t>(g[s]) * nbf + lam],
+                acc);
+    F[static_cast<size_t>(L.off - off0 + p) * nbf + lam] = m.pts[L.off + p].w * acc;
+  }
+}
+
+// G[g, :] of one point g: every kept shell pair's ESP block V_g and its
+// two updates.
+__device__ __noinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int p, int off0,
+                                          int npairs, const CxPair *__restrict__ pairs,
+                                          const CxPrim *__restrict__ prims,
+                                          const double *__restrict__ etab,
+                                          const int *__restrict__ mask, int pure,
+                                          const double *__restrict__ F, double *__restrict__ G) {
+  const Pt4 C = m.pts[L.off + p];
+  const size_t nbf = static_cast<size_t>(m.nbf);
+  const double *Fg = F + static_cast<size_t>(L.off - off0 + p) * nbf;
+  double *Gg = G + static_cast<size_t>(L.off - off0 + p) * nbf;
+  for (int k = 0; k < npairs; k++) {
+    if (!mask[k])
+      continue;
+    const CxPair P = pairs[k];
+    const int ncp = (P.la + 1) * (P.la + 2) / 2, ncq = (P.lb + 1) * (P.lb + 2) / 2;
+    const int L2 = P.la + P.lb;
+    double V[kCosxNc][kCosxNc];
+    for (int i = 0; i < ncp; i++)
+      for (int j = 0; j < ncq; j++)
+        V[i][j] = 0.0;
+    for (int r = 0; r < P.nprim; r++) {
+      const CxPrim Q = prims[P.prim0 + r];
+      double R[kCosxR];
+      hermite_r(L2, Q.pexp, Q.P[0] - C.x, Q.P[1] - C.y, Q.P[2] - C.z, R);
+      const int na = P.la + 1, nb = P.lb + 1, nt = L2 + 1;
+      const double *Ex = etab + Q.e_off, *Ey = Ex + na * nb * nt, *Ez = Ey + na * nb * nt;
+      for (int i = 0; i < ncp; i++) {
+        const int ci = c_cx_comp[P.la][i];
+        const int ax = ci & 15, ay = (ci >> 4) & 15, az = ci >> 8;
+        for (int j = 0; j < ncq; j++) {
+          const int cj = c_cx_comp[P.lb][j];
+          const int bx = cj & 15, by = (cj >> 4) & 15, bz = cj >> 8;
+          const double *ex = Ex + (ax * nb + bx) * nt, *ey = Ey + (ay * nb + by) * nt,
+                       *ez = Ez + (az * nb + bz) * nt;
+          double acc = 0.0;
+          for (int t = 0; t <= ax + bx; t++)
+            for (int u = 0; u <= ay + by; u++) {
+              const double exy = ex[t] * ey[u];
+              for (int v = 0; v <= az + bz; v++)
+                acc = fma(exy * ez[v], R[r_index(t, u, v)], acc);
+            }
+          V[i][j] = fma(Q.pref, acc, V[i][j]);
+        }
+      }
+    }
+    // G[:, q] -= F[:, p] V (and G[:, p] -= F[:, q] V^T), through the shells'
+    // transforms when pure
+    double Fc[kCosxNc], Gc[kCosxNc];
+    const int tp = pure ? P.la : kCosxLmax + 1, tq = pure ? P.lb : kCosxLmax + 1;
+    for (int i = 0; i < ncp; i++) {
+      double s = 0.0;
+      for (int f = 0; f < P.np; f++)
+        s += Fg[P.bf_p + f] * (tp <= kCosxLmax ? c_cx_T[tp][f][i] : (f == i ? 1.0 : 0.0));
+      Fc[i] = s;
+    }
+    for (int j = 0; j < ncq; j++) {
+      double s = 0.0;
+      for (int i = 0; i < ncp; i++)
+        s = fma(Fc[i], V[i][j], s);
+      Gc[j] = s;
+    }
+    for (int h = 0; h < P.nq; h++) {
+      double s = 0.0;
+      for (int j = 0; j < ncq; j++)
+        s += (tq <= kCosxLmax ? c_cx_T[tq][h][j] : (h == j ? 1.0 : 0.0)) * Gc[j];
+      Gg[P.bf_q + h] -= s;
+    }
+    if (P.bf_p != P.bf_q) {
+      for (int j = 0; j < ncq; j++) {
+        double s = 0.0;
+        for (int h = 0; h < P.nq; h++)
+          s += Fg[P.bf_q + h] * (tq <= kCosxLmax ? c_cx_T[tq][h][j] : (h == j ? 1.0 : 0.0));
+        Fc[j] = s;
+      }
+      for (int i = 0; i < ncp; i++) {
+        double s = 0.0;
+        for (int j = 0; j < ncq; j++)
+          s = fma(V[i][j], Fc[j], s);
+        Gc[i] = s;
+      }
+      for (int f = 0; f < P.np; f++) {
+        double s = 0.0;
+        for (int i = 0; i < ncp; i++)
+          s += (tp <= kCosxLmax ? c_cx_T[tp][f][i] : (f == i ? 1.0 : 0.0)) * Gc[i];
+        Gg[P.bf_p + f] -= s;
+      }
+    }
+  }
+}
+
+// G for one leaf's points, a thread per point, every kept shell pair.
+__global__ void __launch_bounds__(256) k_cosx_g(MolDev m, int l0, int off0, int npairs,
+                                                const CxPair *__restrict__ pairs,
+                                                const CxPrim *__restrict__ prims,
+                                                const double *__restrict__ etab,
+                                                const int *__restrict__ mask, int pure,
+                                                const double *__restrict__ F,
+                                                double *__restrict__ G) {
+  const DevLeaf L = m.leaves[l0 + blockIdx.x];
+  for (int p = threadIdx.x; p < L.cnt; p += blockDim.x)
+    cosx_g_point(m, L, p, off0, npairs, pairs, prims, etab, mask, pure, F, G);
+}
+
+// K'[mu, lambda] -= sum_g phi_mu(g) G[g, lambda], mu over the leaf's AOs.
+__global__ void __launch_bounds__(128) k_cosx_k(MolDev m, const double *__restrict__ ws, int l0,
+                                                int off0, const double *__restrict__ G,
+                                                double *__restrict__ Kp) {
+  const DevLeaf L = m.leaves[l0 + blockIdx.x];
+  const int lam = blockIdx.y * blockDim.x + threadIdx.x;
+  if (lam >= m.nbf)
+    return;
+  const double *phi = ws + L.ws_off;
+  const int *g = m.leaf_ao + L.ao_begin;
+  const size_t nbf = static_cast<size_t>(m.nbf);
+  for (int s = 0; s < L.nbf; s++) {
+    double acc = 0.0;
+    for (int p = 0; p < L.cnt; p++)
+      acc = fma(phi[static_cast<size_t>(s) * L.npad + p],
+                G[static_cast<size_t>(L.off - off0 + p) * nbf + lam], acc);
+    atomicAdd(&Kp[static_cast<size_t>(g[s]) * nbf + lam], -acc);
+  }
+}
+
+__global__ void k_cosx_sym(int nbf, const double *__restrict__ Kp, double *__restrict__ K) {
+  const size_t n2 = static_cast<size_t>(nbf) * nbf;
+  for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n2;
+       e += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t i = e / nbf, j = e % nbf;
+    K[e] = 0.25 * (Kp[e] + Kp[j * nbf + i]);
+  }
+}
+
+__global__ void k_cosx_halfw(long n, const Pt4 *__restrict__ pts, double *__restrict__ coef) {
+  const long i = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n)
+    coef[i] = 0.5 * pts[i].w;
+}
+
+// Hermite expansion coefficients E^{ij}_t (t = 0..i+j) of x^i e^{-a x^2}
+// times x^j e^{-b x^2}, centres Qx = A - B apart (Helgaker et al., ch. 9).
+void hermite_table(int la, int lb, double a, double b, double Qx, std::vector<double> &out) {
+  const double p = a + b, q = a * b / p;
+  const int nt = la + lb + 1;
+  // E[i][j][t]
+  std::vector<double> E(static_cast<size_t>(la + 1) * (lb + 1) * (nt + 1), 0.0);
+  auto at = [&](int i, int j, int t) -> double & {
+    return E[(static_cast<size_t>(i) * (lb + 1) + j) * (nt + 1) + t];
+  };
+  auto get = [&](int i, int j, int t) {
+    if (t < 0 || t > i + j)
+      return 0.0;
+    return at(i, j, t);
+  };
+  for (int i = 0; i <= la; i++)
+    for (int j = 0; j <= lb; j++)
+      for (int t = 0; t <= i + j; t++) {
+        double v;
+        if (i == 0 && j == 0)
+          v = std::exp(-q * Qx * Qx);
+        else if (j == 0)
+          v = get(i - 1, j, t - 1) / (2 * p) - q * Qx / a * get(i - 1, j, t) +
+              (t + 1) * get(i - 1, j, t + 1);
+        else
+          v = get(i, j - 1, t - 1) / (2 * p) + q * Qx / b * get(i, j - 1, t) +
+              (t + 1) * get(i, j - 1, t + 1);
+        at(i, j, t) = v;
+      }
+  for (int i = 0; i <= la; i++)
+    for (int j = 0; j <= lb; j++)
+      for (int t = 0; t < nt; t++)
+        out.push_back(get(i, j, t));
+}
+
+std::vector<int> cart_powers(int l) {
+  std::vector<int> c;
+  for (int a = l; a >= 0; a--)
+    for (int b = l - a; b >= 0; b--)
+      c.push_back(a | (b << 4) | ((l - a - b) << 8));
+  return c;
+}
+
+// The analytic overlap of the basis' functions (host, McMurchie-Davidson).
+std::vector<double> overlap_matrix(const Basis &B) {
+  const int n = B.nbf;
+  std::vector<double> S(static_cast<size_t>(n) * n, 0.0);
+  std::vector<double> et;
+  for (size_t s1 = 0; s1 < B.shells.size(); s1++)
+    for (size_t s2 = 0; s2 < B.shells.size(); s2++) {
+      const Shell &A = B.shells[s1], &Bs = B.shells[s2];
+      const auto ca = cart_powers(A.l), cb = cart_powers(Bs.l);
+      std::vector<double> Sc(ca.size() * cb.size(), 0.0);
+      for (size_t x = 0; x < A.exps.size(); x++)
+        for (size_t y = 0; y < Bs.exps.size(); y++) {
+          const double a = A.exps[x], b = Bs.exps[y], p = a + b;
+          std::vector<double> E[3];
+          for (int d = 0; d < 3; d++)
+            hermite_table(A.l, Bs.l, a, b, A.origin[d] - Bs.origin[d], E[d]);
+          const int nb = Bs.l + 1, nt = A.l + Bs.l + 1;
+          const double pref = A.coefs[x] * Bs.coefs[y] * std::pow(kPi / p, 1.5);
+          for (size_t i = 0; i < ca.size(); i++)
+            for (size_t j = 0; j < cb.size(); j++) {
+              const int pa[3] = {ca[i] & 15, (ca[i] >> 4) & 15, ca[i] >> 8};
+              const int pb[3] = {cb[j] & 15, (cb[j] >> 4) & 15, cb[j] >> 8};
+              double e = pref;
+              for (int d = 0; d < 3; d++)
+                e *= E[d][(pa[d] * nb + pb[d]) * nt];
+              Sc[i * cb.size() + j] += e;
+            }
+        }
+      const double fac = common_fac(A.l, B.pure) * common_fac(Bs.l, B.pure);
+      const int na = B.shell_size(static_cast<int>(s1)), nbb = B.shell_size(static_cast<int>(s2));
+      const std::vector<double> *Ta = B.pure ? &spherical_transform(A.l) : nullptr;
+      const std::vector<double> *Tb = B.pure ? &spherical_transform(Bs.l) : nullptr;
+      for (int f = 0; f < na; f++)
+        for (int h = 0; h < nbb; h++) {
+          double v = 0.0;
+          for (size_t i = 0; i < ca.size(); i++)
+            for (size_t j = 0; j < cb.size(); j++) {
+              const double ta = Ta ? (*Ta)[f * ca.size() + i] : (static_cast<size_t>(f) == i);
+              const double tb = Tb ? (*Tb)[h * cb.size() + j] : (static_cast<size_t>(h) == j);
+              v += ta * Sc[i * cb.size() + j] * tb;
+            }
+          const size_t r = B.first_bf[s1] + f, c = B.first_bf[s2] + h;
+          S[c * n + r] = fac * v; // column-major
+        }
+    }
+  return S;
+}
+
+// X = A^-1 B for symmetric positive definite A (column-major n x n): Cholesky.
+std::vector<double> spd_solve(std::vector<double> A, const std::vector<double> &B, int n) {
+  auto a = [&](int i, int j) -> double & { return A[static_cast<size_t>(j) * n + i]; };
+  for (int j = 0; j < n; j++) {
+    double d = a(j, j);
+    for (int k = 0; k < j; k++)
+      d -= a(j, k) * a(j, k);
+    if (!(d > 0.0))
+      throw ArgError("COSX: the numerical overlap matrix is not positive definite");
+    a(j, j) = std::sqrt(d);
+    for (int i = j + 1; i < n; i++) {
+      double s = a(i, j);
+      for (int k = 0; k < j; k++)
+        s -= a(i, k) * a(j, k);
+      a(i, j) = s / a(j, j);
+    }
+  }
+  std::vector<double> X = B;
+  for (int c = 0; c < n; c++) {
+    double *x = &X[static_cast<size_t>(c) * n];
+    for (int i = 0; i < n; i++) {
+      double s = x[i];
+      for (int k = 0; k < i; k++)
+        s -= a(i, k) * x[k];
+      x[i] = s / a(i, i);
+    }
+    for (int i = n - 1; i >= 0; i--) {
+      double s = x[i];
+      for (int k = i + 1; k < n; k++)
+        s -= a(k, i) * x[k];
+      x[i] = s / a(i, i);
+    }
+  }
+  return X;
+}
+
+} // namespace
+
+struct CosxState {
+  std::unique_ptr<Molecule> N;
+  int nbf = 0, npairs = 0;
+  std::vector<int> group_leaf0, group_nleaf, group_off0, group_npts;
+  size_t group_pts_max = 0;
+  double *d_Q = nullptr, *d_D = nullptr, *d_D2q = nullptr, *d_Kp = nullptr, *d_K = nullptr;
+  double *d_F = nullptr, *d_G = nullptr, *d_etab = nullptr;
+  CxPair *d_pairs = nullptr;
+  CxPrim *d_prims = nullptr;
+  int *d_mask = nullptr;
+  std::vector<void *> allocations;
+  ~CosxState() {
+    for (void *p : allocations)
+      cudaFree(p);
+  }
+  template <typename T> T *alloc(size_t n) {
+    void *p = nullptr;
+    cuda_check(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc");
+    allocations.push_back(p);
+    return static_cast<T *>(p);
+  }
+};
+
+namespace {
+
+// GridSettings::for_sgx(n) (src/numint/grid_settings.cpp:59-68)
+GridSettings sgx_grid_settings(int angular) {
+  GridSettings g;
+  g.max_angular_points = angular;
+  g.min_angular_points = angular;
+  g.radial_precision = 1e-5;
+  g.pruning_scheme = 0;
+  g.reduced_first_row_element_grid = false;
+  return g;
+}
+
+void upload_cosx_tables() {
+  int comp[3][kCosxNc] = {};
+  double T[3][5][kCosxNc] = {};
+  for (int l = 0; l <= kCosxLmax; l++) {
+    const auto c = cart_powers(l);
+    for (size_t i = 0; i < c.size(); i++)
+      comp[l][i] = c[i];
+    const auto &t = spherical_transform(l);
+    const int nc = static_cast<int>(c.size());
+    for (int f = 0; f < 2 * l + 1; f++)
+      for (int i = 0; i < nc; i++)
+        T[l][f][i] = t[f * nc + i];
+  }
+  cuda_check(cudaMemcpyToSymbol(c_cx_comp, comp, sizeof(comp)), "cudaMemcpyToSymbol");
+  cuda_check(cudaMemcpyToSymbol(c_cx_T, T, sizeof(T)), "cudaMemcpyToSymbol");
+}
+
+} // namespace
+
+std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size_t ws_cap_bytes) {
+  for (const Shell &s : M.basis.shells)
+    if (s.l > kCosxLmax)
+      throw ArgError("COSX: shells up to d are supported");
+  DeviceGuard on_device(M.device);
+  upload_cosx_tables();
+  auto S = std::make_unique<CosxState>();
+  S->nbf = M.basis.nbf;
+  const int nbf = S->nbf;
+  // the molecule on the SGX grid, AO values only
+  auto N = std::make_unique<Molecule>();
+  N->ctx = M.ctx;
+  N->device = M.device;
+  N->Z = M.Z;
+  N->xyz = M.xyz;
+  N->basis = M.basis;
+  N->fs = M.fs;
+  N->deriv = 0;
+  N->gs = gs;
+  N->bs = M.bs;
+  N->bs.xc_screening_threshold = 1e-14;
+  PartitionFn part;
+  if (device_partition_fits(M.device, static_cast<int>(M.Z.size())))
+    part = [dev = M.device](const PartitionInput &in, double *w) { device_partition(dev, in, w); };
+  N->grid = build_molecular_grid(N->Z, N->xyz, N->basis, N->gs, 0, part ? &part : nullptr);
+  N->build_plan();
+  N->upload();
+  N->ensure_fp64_ws();
+  cudaStream_t st = M.ctx->stream;
+  const MolDev m = N->dev();
+  launch_colloc_f64(m, 0, N->d_ws, st);
+  N->fp64_ao_valid = true;
+  // S_num = phi^T diag(w) phi: the V_xc kernel with coefficient w / 2
+  const long npts = N->plan.npts;
+  k_cosx_halfw<<<static_cast<int>((npts + 255) / 256), 256, 0, st>>>(npts, N->d_pts, N->d_coef);
+  double *d_Sn = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
+  cuda_check(cudaMemsetAsync(d_Sn, 0, static_cast<size_t>(nbf) * nbf * sizeof(double), st),
+             "cudaMemsetAsync");
+  launch_vxc_f64(m, 0, N->d_ws, N->d_coef, N->d_tiles, static_cast<int>(N->tiles.size()), d_Sn,
+                 st);
+  cuda_check(cudaGetLastError(), "kernel launch");
+  std::vector<double> Sn(static_cast<size_t>(nbf) * nbf);
+  cuda_check(cudaMemcpyAsync(Sn.data(), d_Sn, Sn.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                             st),
+             "cudaMemcpyAsync D2H");
+  cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  // Q = S_num^-1 S
+  const std::vector<double> Q = spd_solve(Sn, overlap_matrix(M.basis), nbf);
+  S->d_Q = S->alloc<double>(Q.size());
+  cuda_check(cudaMemcpy(S->d_Q, Q.data(), Q.size() * sizeof(double), cudaMemcpyHostToDevice),
+             "cudaMemcpy H2D");
+  // shell pairs p >= q and their primitive pairs
+  std::vector<CxPair> pairs;
+  std::vector<CxPrim> prims;
+  std::vector<double> et;
+  const Basis &B = M.basis;
+  for (size_t p = 0; p < B.shells.size(); p++)
+    for (size_t q = 0; q <= p; q++) {
+      const Shell &A = B.shells[p], &Bq = B.shells[q];
+      CxPair P{};
+      P.bf_p = B.first_bf[p];
+      P.bf_q = B.first_bf[q];
+      P.np = B.shell_size(static_cast<int>(p));
+      P.nq = B.shell_size(static_cast<int>(q));
+      P.la = A.l;
+      P.lb = Bq.l;
+      P.prim0 = static_cast<int>(prims.size());
+      const double fac = common_fac(A.l, B.pure) * common_fac(Bq.l, B.pure);
+      for (size_t x = 0; x < A.exps.size(); x++)
+        for (size_t y = 0; y < Bq.exps.size(); y++) {
+          CxPrim r{};
+          const double a = A.exps[x], b = Bq.exps[y];
+          r.pexp = a + b;
+          for (int d = 0; d < 3; d++)
+            r.P[d] = (a * A.origin[d] + b * Bq.origin[d]) / r.pexp;
+          r.pref = A.coefs[x] * Bq.coefs[y] * 2.0 * kPi / r.pexp * fac;
+          r.e_off = static_cast<int>(et.size());
+          for (int d = 0; d < 3; d++)
+            hermite_table(A.l, Bq.l, a, b, A.origin[d] - Bq.origin[d], et);
+          prims.push_back(r);
+        }
+      P.nprim = static_cast<int>(prims.size()) - P.prim0;
+      pairs.push_back(P);
+    }
+  S->npairs = static_cast<int>(pairs.size());
+  size_t bytes = 0;
+  S->d_pairs = dev_upload(pairs, bytes);
+  S->allocations.push_back(S->d_pairs);
+  S->d_prims = dev_upload(prims, bytes);
+  S->allocations.push_back(S->d_prims);
+  S->d_etab = dev_upload(et, bytes);
+  S->allocations.push_back(S->d_etab);
+  S->d_mask = S->alloc<int>(pairs.size());
+  S->d_D = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
+  S->d_D2q = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
+  S->d_Kp = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
+  S->d_K = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
+  // leaf groups whose point-major F and G fit the cap
+  const size_t per_pt = 2 * static_cast<size_t>(nbf) * sizeof(double);
+  const size_t cap_pts = std::max<size_t>(ws_cap_bytes / std::max<size_t>(per_pt, 1), 256);
+  const auto &Ls = N->leaves;
+  size_t i = 0;
+  while (i < Ls.size()) {
+    const size_t l0 = i;
+    const int off0 = Ls[i].off;
+    size_t pts = 0;
+    while (i < Ls.size() && (pts + Ls[i].cnt <= cap_pts || i == l0)) {
+      pts = static_cast<size_t>(Ls[i].off + Ls[i].cnt - off0);
+      i++;
+    }
+    S->group_leaf0.push_back(static_cast<int>(l0));
+    S->group_nleaf.push_back(static_cast<int>(i - l0));
+    S->group_off0.push_back(off0);
+    S->group_npts.push_back(static_cast<int>(pts));
+    S->group_pts_max = std::max(S->group_pts_max, pts);
+  }
+  S->d_F = S->alloc<double>(S->group_pts_max * nbf);
+  S->d_G = S->alloc<double>(S->group_pts_max * nbf);
+  S->N = std::move(N);
+  return S;
+}
+
+void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaStream_t st) {
+  const int nbf = S.nbf;
+  const size_t n2 = static_cast<size_t>(nbf) * nbf;
+  Molecule &N = *S.N;
+  const MolDev m = N.dev();
+  c.launch("cosx_d2q", st, [&] {
+    k_cosx_d2q<<<dim3((nbf + 15) / 16, (nbf + 15) / 16), dim3(16, 16), 0, st>>>(nbf, S.d_Q, dD,
+                                                                              S.d_D2q);
+  });
+  c.launch("cosx_mask", st, [&] {
+    k_cosx_mask<<<(S.npairs + 127) / 128, 128, 0, st>>>(S.npairs, nbf, S.d_pairs, S.d_D2q,
+                                                        S.d_mask);
+  });
+  cuda_check(cudaMemsetAsync(S.d_Kp, 0, n2 * sizeof(double), st), "cudaMemsetAsync");
+  for (size_t gi = 0; gi < S.group_leaf0.size(); gi++) {
+    const int l0 = S.group_leaf0[gi], nl = S.group_nleaf[gi], off0 = S.group_off0[gi];
+    const dim3 gf(nl, (nbf + 127) / 128);
+    cuda_check(cudaMemsetAsync(S.d_G, 0, static_cast<size_t>(S.group_npts[gi]) * nbf *
+                                             sizeof(double), st),
+               "cudaMemsetAsync");
+    c.launch("cosx_f", st,
+             [&] { k_cosx_f<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_D2q, S.d_F); });
+    c.launch("cosx_g", st, [&] {
+      k_cosx_g<<<nl, 256, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims, S.d_etab,
+                                   S.d_mask, N.basis.pure ? 1 : 0, S.d_F, S.d_G);
+    });
+    c.launch("cosx_k", st,
+             [&] { k_cosx_k<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_G, S.d_Kp); });
+  }
+  c.launch("cosx_sym", st, [&] {
+    const int g = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
+    k_cosx_sym<<<g, 256, 0, st>>>(nbf, S.d_Kp, dK);
+  });
+  cuda_check(cudaGetLastError(), "kernel launch");
+}
+
+} // namespace occx
+
+using namespace occx;
+
+struct occ_xc_cosx {
+  std::unique_ptr<CosxState> impl;
+  occ_xc_context *ctx;
+};
+
+extern "C" {
+
+int occ_xc_cosx_create(occ_xc_context *ctx, occ_xc_molecule *mol,
+                       const occ_xc_grid_settings *grid, occ_xc_cosx **out) {
+  if (!ctx || !mol || !out || mol->ctx != ctx)
+    return OCC_XC_ERR_ARG;
+  if (grid && (grid->max_angular_points <= 0 || grid->min_angular_points <= 0 ||
+               !(grid->radial_precision > 0.0)))
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return guarded(ctx, [&] {
+    auto cx = std::make_unique<occ_xc_cosx>();
+    cx->ctx = ctx;
+    cx->impl = cosx_create(*mol->impl, grid ? grid_settings_from(grid) : sgx_grid_settings(50),
+                           size_t(2) << 30);
+    *out = cx.release();
+  });
+}
+
+void occ_xc_cosx_destroy(occ_xc_cosx *cx) { delete cx; }
+
+int occ_xc_cosx_grid_points(const occ_xc_cosx *cx, long *npoints) {
+  if (!cx || !npoints)
+    return OCC_XC_ERR_ARG;
+  *npoints = cx->impl->N->plan.npts;
+  return OCC_XC_OK;
+}
+
+int occ_xc_cosx_exchange(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D, double *K) {
+  if (!ctx || !cx || !D || !K || cx->ctx != ctx)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return guarded(ctx, [&] {
+    DeviceGuard on_device(ctx->impl->device);
+    CosxState &S = *cx->impl;
+    cudaStream_t st = ctx->impl->stream;
+    const size_t n2 = static_cast<size_t>(S.nbf) * S.nbf;
+    cuda_check(cudaMemcpyAsync(S.d_D, D, n2 * sizeof(double), cudaMemcpyHostToDevice, st),
+               "cudaMemcpyAsync H2D");
+    cosx_exchange(*ctx->impl, S, S.d_D, S.d_K, st);
+    cuda_check(cudaMemcpyAsync(K, S.d_K, n2 * sizeof(double), cudaMemcpyDeviceToHost, st),
+               "cudaMemcpyAsync D2H");
+    cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  });
+}
+
+int occ_xc_cosx_exchange_device(occ_xc_context *ctx, occ_xc_cosx *cx, const double *d_D,
+                                double *d_K, void *stream) {
+  if (!ctx || !cx || !d_D || !d_K || cx->ctx != ctx)
+    return OCC_XC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return guarded(ctx, [&] {
+    DeviceGuard on_device(ctx->impl->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
+    cosx_exchange(*ctx->impl, *cx->impl, d_D, d_K, st);
+  });
+}
+
+} // extern "C"

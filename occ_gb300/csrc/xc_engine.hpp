@@ -30,6 +30,22 @@ struct TimeoutError : std::runtime_error {
 
 void cuda_check(cudaError_t e, const char *what);
 
+// Makes `device` current for the lifetime of the guard and puts the caller's
+// current device back on every exit path.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int device) {
+    cuda_check(cudaGetDevice(&prev), "cudaGetDevice");
+    if (prev != device)
+      cuda_check(cudaSetDevice(device), "cudaSetDevice");
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
+      cudaSetDevice(prev);
+  }
+};
+
 // cudaMalloc of max(size, 1) elements and a copy of h; adds the bytes to `bytes`.
 template <typename T> T *dev_upload(const std::vector<T> &h, size_t &bytes) {
   T *d = nullptr;
@@ -64,6 +80,8 @@ void device_partition(int device, const PartitionInput &in, double *w);
 void device_plan(int device, const MolecularGrid &grid, const Basis &basis,
                  const BuildSettings &bs, Plan &plan);
 FuncSet parse_method(const std::string &method);
+// occ_xc_grid_settings -> GridSettings (defaults for NULL)
+GridSettings grid_settings_from(const occ_xc_grid_settings *grid);
 void upload_sph_table_mixed();
 struct MixedState;
 void free_mixed(MixedState *S);

@@ -62,22 +62,6 @@ double *noalloc_scratch(int device) {
 
 size_t align_elems(size_t n) { return (n + 31) / 32 * 32; } // 256-byte boundaries
 
-// Makes `device` current for the lifetime of the guard and puts the caller's
-// current device back on every exit path.
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int device) {
-    cuda_check(cudaGetDevice(&prev), "cudaGetDevice");
-    if (prev != device)
-      cuda_check(cudaSetDevice(device), "cudaSetDevice");
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
-      cudaSetDevice(prev);
-  }
-};
-
 } // namespace
 } // namespace occx
 

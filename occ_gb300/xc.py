@@ -113,6 +113,13 @@ def library():
                                     C.c_int, _dp, _dp]
     lib.occ_xc_nlc_grid_points.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
     lib.occ_xc_nlc_grid.argtypes = [C.c_void_p, _dp, _dp]
+    lib.occ_xc_cosx_create.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(_GridSettings),
+                                       C.POINTER(C.c_void_p)]
+    lib.occ_xc_cosx_destroy.argtypes = [C.c_void_p]
+    lib.occ_xc_cosx_grid_points.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
+    lib.occ_xc_cosx_exchange.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp]
+    lib.occ_xc_cosx_exchange_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p]
     lib.occ_xc_compute_vxc_unrestricted.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp,
                                                     _dp, _dp]
     lib.occ_xc_compute_vxc_unrestricted_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
@@ -286,6 +293,15 @@ class GridSettings:
     reduced_first_row_element_grid: bool = True
     treutler_alrichs_adjustment: bool = True
     pruning_scheme: int = 1
+
+    @staticmethod
+    def for_sgx(angular_points=50):
+        """GridSettings::for_sgx (src/numint/grid_settings.cpp:59-68): the
+        same angular order on every shell, LMG radial precision 1e-5, no
+        pruning, no reduced H / He grid."""
+        return GridSettings(max_angular_points=angular_points, min_angular_points=angular_points,
+                            radial_precision=1e-5, reduced_first_row_element_grid=False,
+                            pruning_scheme=0)
 
     def _c(self):
         return _GridSettings(self.max_angular_points, self.min_angular_points, self.radial_points,
@@ -565,6 +581,54 @@ class DFT:
 
     def integrated_density(self):
         return self._nelec
+
+
+class SemiNumericalExchange:
+    """occ::qm::cosx::SemiNumericalExchange with set_use_esp(true)
+    (include/occ/qm/seminumerical_exchange.h:104-118): the seminumerical
+    exchange matrix of a restricted density on its own grid
+    (GridSettings.for_sgx(50) unless given), FP64 on the GPU.  `dft` gives
+    the basis and the device (its XC grid is not used)."""
+
+    def __init__(self, dft, grid_settings=None):
+        self.dft = dft
+        self.ctx = dft.ctx
+        gs = (grid_settings or GridSettings.for_sgx(50))._c()
+        h = C.c_void_p()
+        rc = self.ctx.lib.occ_xc_cosx_create(self.ctx.h, dft.h, C.byref(gs), C.byref(h))
+        if rc != 0:
+            raise XCError(f"occ_xc_cosx_create failed ({rc}): {self.ctx.error()}", rc)
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.occ_xc_cosx_destroy(self.h)
+            self.h = None
+
+    def grid_points(self):
+        n = C.c_long(-1)
+        self.ctx.lib.occ_xc_cosx_grid_points(self.h, C.byref(n))
+        return n.value
+
+    def compute_K(self, D):
+        """K (nbf x nbf) of mo.D = D (compute_K(mo) of a restricted mo)."""
+        nbf = self.dft.nbf()
+        Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
+        if Dm.shape != (nbf, nbf):
+            raise XCError(f"density matrix must be {nbf}x{nbf}")
+        K = np.zeros((nbf, nbf), order="F")
+        rc = self.ctx.lib.occ_xc_cosx_exchange(self.ctx.h, self.h, _ptr(Dm), _ptr(K))
+        if rc != 0:
+            raise XCError(f"occ_xc_cosx_exchange failed ({rc}): {self.ctx.error()}", rc)
+        return K
+
+    def compute_K_device(self, d_D, d_K, stream=None):
+        """The same on device buffers (addresses), asynchronous on `stream`."""
+        rc = self.ctx.lib.occ_xc_cosx_exchange_device(self.ctx.h, self.h, C.c_void_p(d_D),
+                                                      C.c_void_p(d_K),
+                                                      C.c_void_p(stream) if stream else None)
+        if rc != 0:
+            raise XCError(f"occ_xc_cosx_exchange_device failed ({rc}): {self.ctx.error()}", rc)
 
 
 class Batch:

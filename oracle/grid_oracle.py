@@ -292,10 +292,11 @@ def exponent_ranges(shells, natom):
     return lmax, amax, amin
 
 
-def molecular_grid(Z, R, shells, s=None, product_theta=0, chunk=50000):
+def molecular_grid(Z, R, shells, s=None, product_theta=0, chunk=50000, atom_counts=False):
     """Points (n, 3) and weights (n,) in the reference's order (atom blocks,
     radial shells, angular points), Bohr.  Z: atomic numbers, R: (natom, 3)
-    Bohr, shells: (l, atom, exponents) per shell."""
+    Bohr, shells: (l, atom, exponents) per shell.  atom_counts: also return
+    the number of points of each atom's block."""
     s = s or Settings()
     # ensure_settings (molecular_grid.cpp:142-181)
     if s.max_angular < s.min_angular:
@@ -321,6 +322,8 @@ def molecular_grid(Z, R, shells, s=None, product_theta=0, chunk=50000):
             w[c0:c0 + chunk] = w0[c0:c0 + chunk] * cw[:, a] / cw.sum(axis=1)
         Ps.append(P)
         Ws.append(w)
+    if atom_counts:
+        return np.concatenate(Ps), np.concatenate(Ws), [len(w) for w in Ws]
     return np.concatenate(Ps), np.concatenate(Ws)
 
 

@@ -1,0 +1,158 @@
+"""Seminumerical (COSX) exchange, the ESP form of OCC's SemiNumericalExchange
+(src/qm/seminumerical_exchange.cpp:233-250, :516-529, :714-855).
+
+CPU: the oracle (oracle/cosx_oracle.py) is pinned against the exact
+exchange matrix of the same density from four-centre integrals
+(tests/golden/make_hf_density.py), on the reference's own test system
+(tests/dft_tests.cpp:322-347, 371-418: water, 6-31G Cartesian, RHF density,
+GridSettings::for_sgx(50) and (110)); its analytic overlap against that
+file's overlap, its AO values against the collocation oracle, and its grid
+against the library's host grid.
+GPU: the library's K against the oracle's at 1e-9 (FP64 throughout)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import occ_gb300 as og
+import oracle
+import cosx_oracle as cx
+import grid_oracle as go
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import make_hf_density as hf  # noqa: E402
+
+WATER = [(8, -1.32695761, -0.10593856, 0.01878821),
+         (1, -1.93166418, 1.60017351, -0.02171049),
+         (1, 0.48664409, 0.07959806, 0.00986248)]
+TOL_GPU = 1e-9
+
+
+def _water(basis="6-31g", pure=False, shift=(0.0, 0.0, 0.0)):
+    atoms = [og.Atom(z, x + shift[0], y + shift[1], w + shift[2]) for z, x, y, w in WATER]
+    b = og.AOBasis.load(atoms, basis)
+    b.set_pure(pure)
+    return atoms, b
+
+
+_CACHE = {}
+
+
+def _rhf_water_631g():
+    """RHF density and exact K of water / 6-31G (Cartesian), as the
+    reference's test computes them (SCF, then HartreeFock::compute_JK)."""
+    if "rhf" not in _CACHE:
+        atoms, b = _water()
+        Z = np.array([a.atomic_number for a in atoms], dtype=float)
+        xyz = np.array([[a.x, a.y, a.z] for a in atoms])
+        enuc = sum(Z[i] * Z[j] / np.linalg.norm(xyz[i] - xyz[j])
+                   for i in range(3) for j in range(i))
+        aos = hf.ao_list(b)
+        S, T, V = hf.one_electron(aos, Z, xyz)
+        G = hf.eri(aos)
+        _, D, _ = hf.rhf(S, T + V, G, 5, enuc)
+        K = np.einsum("ls,mlns->mn", D, G)
+        _CACHE["rhf"] = (b, D, K, S)
+    return _CACHE["rhf"]
+
+
+def test_oracle_overlap_and_ao_values_match_independent_forms():
+    b, _, _, S = _rhf_water_631g()
+    shells = cx.shells_of(b)
+    assert np.abs(cx.overlap(shells) - S).max() < 1e-13
+    P = np.random.default_rng(0).normal(size=(50, 3))
+    col = [oracle.collocation(s.l, b.pure, s.exponents, s.coefficients, s.origin, P,
+                              deriv=0)[0].T for s in b.shells]
+    assert np.abs(np.concatenate(col, axis=1) - cx.ao_values(shells, P)).max() < 1e-14
+    # pure d shells through the solid-harmonic transform
+    _, bp = _water("def2-svp", pure=True)
+    col = [oracle.collocation(s.l, bp.pure, s.exponents, s.coefficients, s.origin, P,
+                              deriv=0)[0].T for s in bp.shells]
+    assert np.abs(np.concatenate(col, axis=1) - cx.ao_values(cx.shells_of(bp), P)).max() < 1e-14
+
+
+def test_oracle_boys_function_limits():
+    T = np.array([0.0, 1e-12, 0.5, 7.0, 30.0, 60.0])
+    F = cx.boys(4, T)
+    assert np.allclose(F[:, 0], 1.0 / (2 * np.arange(5) + 1), rtol=0, atol=1e-15)
+    assert abs(F[0, -1] - 0.5 * np.sqrt(np.pi / 60.0)) < 1e-15
+    # downward recursion F_{n-1} = (2T F_n + e^-T) / (2n - 1)
+    for n in range(1, 5):
+        assert np.allclose(F[n - 1], (2 * T * F[n] + np.exp(-T)) / (2 * n - 1), rtol=1e-13)
+
+
+@pytest.mark.parametrize("angular,bar", [(50, 5e-4), (110, 5e-5)])
+def test_oracle_exchange_approaches_exact_exchange(angular, bar):
+    """max |K_COSX - K_exact| on water / 6-31G: 3.0e-4 at 50 angular points,
+    2.0e-5 at 110 (max |K| 4.9); the reference test prints the same
+    difference (tests/dft_tests.cpp:346-347)."""
+    b, D, K, _ = _rhf_water_631g()
+    Kc = cx.cosx_exchange(b, D, angular=angular)
+    assert np.abs(Kc - Kc.T).max() < 1e-14
+    err = np.abs(Kc - K).max()
+    assert err < bar, err
+
+
+def test_oracle_sgx_grid_is_the_library_host_grid():
+    _, b = _water()
+    P, W, counts = cx.sgx_grid(b, 50)
+    gs = og.GridSettings.for_sgx(50)
+    Pl, Wl = og.molecular_grid(b, gs)
+    assert len(W) == len(Wl) == sum(counts)
+    assert np.abs(P - Pl).max() < 1e-12
+    assert np.abs(W - Wl).max() < 1e-12 * np.abs(W).max()
+
+
+def _gpu_case(b, D, grid):
+    dft = og.DFT("lda", b)
+    sgx = og.SemiNumericalExchange(dft, grid)
+    assert sgx.grid_points() == len(og.molecular_grid(b, grid)[1])
+    return dft, sgx, sgx.compute_K(D)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("angular", [50, 110])
+def test_gpu_cosx_matches_oracle_water_631g(angular):
+    b, D, K, _ = _rhf_water_631g()
+    _, _, Kg = _gpu_case(b, D, og.GridSettings.for_sgx(angular))
+    Ko = cx.cosx_exchange(b, D, angular=angular)
+    assert np.abs(Kg - Kg.T).max() < 1e-14
+    assert np.abs(Kg - Ko).max() < TOL_GPU, np.abs(Kg - Ko).max()
+
+
+@pytest.mark.gpu
+def test_gpu_cosx_pure_d_two_waters():
+    """def2-SVP (pure d shells) on two waters, a random symmetric density."""
+    atoms1, _ = _water()
+    atoms2, _ = _water(shift=(0.0, 0.0, 5.5))
+    b = og.AOBasis.load(atoms1 + atoms2, "def2-svp")
+    b.set_pure(True)
+    n = b.nbf()
+    rng = np.random.default_rng(7)
+    C = rng.normal(size=(n, 10)) * 0.3
+    D = C @ C.T
+    _, sgx, Kg = _gpu_case(b, D, og.GridSettings.for_sgx(50))
+    Ko = cx.cosx_exchange(b, D, angular=50)
+    assert np.abs(Kg - Ko).max() < TOL_GPU * max(1.0, np.abs(Ko).max())
+    # the device entry point writes the same K
+    import torch
+    dD = torch.tensor(np.asfortranarray(D).ravel(order="F"), device="cuda", dtype=torch.float64)
+    dK = torch.empty(n * n, device="cuda", dtype=torch.float64)
+    sgx.compute_K_device(dD.data_ptr(), dK.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    Kd = dK.cpu().numpy().reshape(n, n, order="F")
+    assert np.abs(Kd - Kg).max() < 1e-13
+
+
+@pytest.mark.gpu
+def test_gpu_cosx_refuses_f_shells_and_bad_grid():
+    _, b = _water("def2-tzvp", pure=True)
+    dft = og.DFT("lda", b)
+    with pytest.raises(og.XCError) as e:
+        og.SemiNumericalExchange(dft)
+    assert e.value.code == -1
+    _, b = _water()
+    dft = og.DFT("lda", b)
+    with pytest.raises(og.XCError):
+        og.SemiNumericalExchange(dft, og.GridSettings(max_angular_points=0))
