@@ -123,6 +123,45 @@ void morton_leaves(const MolecularGrid &grid, const BuildSettings &bs, Plan &pla
   }
 }
 
+void atom_batch_leaves(const MolecularGrid &grid, long batch, Plan &plan) {
+  const long n = grid.npts();
+  plan.npts = n;
+  plan.perm.resize(n);
+  plan.pts4.assign(4 * n, 0.0);
+  plan.leaf_off.clear();
+  plan.leaf_cnt.clear();
+  plan.leaf_centre.clear();
+  plan.leaf_radius.clear();
+  for (long i = 0; i < n; i++) {
+    plan.perm[i] = i;
+    for (int d = 0; d < 3; d++)
+      plan.pts4[4 * i + d] = grid.xyz[3 * i + d];
+    plan.pts4[4 * i + 3] = grid.w[i];
+  }
+  for (size_t a = 0; a < grid.atom_offset.size(); a++) {
+    const long a0 = grid.atom_offset[a], na = grid.atom_count[a];
+    for (long b0 = 0; b0 < na; b0 += batch) {
+      const long off = a0 + b0, cnt = std::min(batch, na - b0);
+      double c[3] = {0, 0, 0};
+      for (long i = off; i < off + cnt; i++)
+        for (int d = 0; d < 3; d++)
+          c[d] += grid.xyz[3 * i + d];
+      for (int d = 0; d < 3; d++)
+        c[d] /= static_cast<double>(cnt);
+      double r = 0.0;
+      for (long i = off; i < off + cnt; i++) {
+        const double dx = grid.xyz[3 * i] - c[0], dy = grid.xyz[3 * i + 1] - c[1],
+                     dz = grid.xyz[3 * i + 2] - c[2];
+        r = std::max(r, std::sqrt(dx * dx + dy * dy + dz * dz));
+      }
+      plan.leaf_off.push_back(off);
+      plan.leaf_cnt.push_back(cnt);
+      plan.leaf_centre.insert(plan.leaf_centre.end(), c, c + 3);
+      plan.leaf_radius.push_back(r);
+    }
+  }
+}
+
 void screen_leaves(const Basis &basis, const BuildSettings &bs, Plan &plan) {
   const long nl = plan.nleaves();
   const int nsh = static_cast<int>(basis.shells.size());

@@ -114,6 +114,11 @@ struct Plan {
 std::vector<double> decay_cutoff(const Basis &basis, double threshold);
 void morton_leaves(const MolecularGrid &grid, const BuildSettings &bs, Plan &plan);
 void screen_leaves(const Basis &basis, const BuildSettings &bs, Plan &plan);
+// Batches of `batch` consecutive points of each atom block, in the grid's
+// own order (the seminumerical exchange's batching,
+// src/qm/seminumerical_exchange.cpp:726-752), with their centroids and
+// bounding radii; perm is the identity.
+void atom_batch_leaves(const MolecularGrid &grid, long batch, Plan &plan);
 
 // Host evaluation of one shell (values only) at n points; out[f*n + p].
 void eval_shell_values(const Shell &sh, bool pure, long n, const double *xyz, double *out);

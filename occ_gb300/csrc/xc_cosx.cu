@@ -4,29 +4,33 @@
 // build, :714-855 the grid sweep), on the grid of GridSettings::for_sgx(n)
 // (src/numint/grid_settings.cpp:59-68).
 //
-// Set-up (once per molecule and angular order): a second molecule over the
-// same basis on the SGX grid (n angular points on every shell, LMG radial
-// precision 1e-5, no pruning, no reduced H / He grid), its AO values, the
-// numerical overlap S_num = sum_g w_g phi phi^T (the FP64 V_xc kernel with
-// coefficient w / 2), the analytic overlap S (McMurchie-Davidson, host) and
-// the overlap projector Q = S_num^-1 S (Cholesky solve, host); the shell
-// pairs' primitive-pair tables (exponent sum, centre, prefactor, Hermite
-// expansion coefficients E^{ij}_t per axis).
+// Set-up (once per molecule and grid): a second molecule over the same basis
+// on the exchange grid (for_sgx(n): n angular points on every shell, LMG
+// radial precision 1e-5, no pruning, no reduced H / He grid), cut into the
+// reference's batches (128 consecutive points of each atom block, in grid
+// order), its AO values, the numerical overlap S_num = sum_g w_g phi phi^T
+// (the FP64 V_xc kernel with coefficient w / 2), the analytic overlap S
+// (McMurchie-Davidson, host) and the overlap projector Q = S_num^-1 S
+// (Cholesky solve, host); the significant shell pairs p >= q (a shared
+// origin or an overlap block of norm >= 1e-12) with their primitive-pair
+// tables (exponent sum, centre, prefactor, Hermite expansion coefficients
+// E^{ij}_t per axis) and the centre and extent of their most diffuse
+// primitive pair.
 //
 // Per call, for mo.D:
 //   k_cosx_d2q    D2q = Q (2 D), row-major
 //   k_cosx_mask   shell pair (p, q) kept when max |D2q| over its two blocks
 //                 reaches 1e-6 (the reference's density screen)
-//   per group of leaves (a workspace cap bounds the point-major F and G):
+//   per group of batches (a workspace cap bounds the point-major F and G):
 //   k_cosx_f      F[g, lambda] = w_g sum_sigma phi_sigma(g) D2q[sigma, lambda]
 //   k_cosx_g      G[g, nu] -= sum_mu F[g, mu] V_g(mu, nu) (and the transposed
 //                 block for p != q), V_g(mu, nu) = int phi_mu phi_nu / |r - g|
 //                 by McMurchie-Davidson over the Boys function, one thread
-//                 per grid point, every kept pair
+//                 per grid point, every kept pair that passes the batch's
+//                 geometric screen (|P - c| - extent < radius + 1 Bohr)
 //   k_cosx_k      K'[mu, lambda] -= sum_g phi_mu(g) G[g, lambda]
 //   k_cosx_sym    K = (K' + K'^T) / 4
-// All in FP64.  The reference's per-batch geometric screen of shell pairs is
-// not applied (every kept pair reaches every point).  Shells up to d.
+// All in FP64.  Shells up to d.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -45,6 +49,9 @@ constexpr int kCosxLmax = 2;                   // shells up to d
 constexpr int kCosxNc = 6;                     // Cartesian components of a d shell
 constexpr int kCosxR = 35;                     // R_tuv with t + u + v <= 4
 constexpr double kCosxDensityThreshold = 1e-6; // seminumerical_exchange.cpp:789
+constexpr double kCosxMargin = 1.0;            // cosx::Settings::margin (Bohr)
+constexpr double kCosxLogThreshold = 27.631021115928547; // -ln(1e-12): pair extents
+constexpr double kCosxPairOverlap = 1e-12;     // IntegralEngine::compute_shellpairs
 constexpr double kPi = 3.14159265358979323846;
 
 // Cartesian powers of the components of a shell (CCA order), packed a | b<<4 | c<<8.
@@ -54,6 +61,7 @@ __constant__ int c_cx_comp[3][kCosxNc];
 __constant__ double c_cx_T[3][5][kCosxNc];
 
 struct CxPair {
+  double Pc[3], ext;        // centre and extent of the most diffuse primitive pair
   int bf_p, bf_q, np, nq;   // first AO and AO count of each shell
   int la, lb, prim0, nprim; // angular momenta, primitive-pair range
 };
@@ -193,7 +201,7 @@ __device__ __noinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int
                                           int npairs, const CxPair *__restrict__ pairs,
                                           const CxPrim *__restrict__ prims,
                                           const double *__restrict__ etab,
-                                          const int *__restrict__ mask, int pure,
+                                          const int *__restrict__ mask, double4 geo, int pure,
                                           const double *__restrict__ F, double *__restrict__ G) {
   const Pt4 C = m.pts[L.off + p];
   const size_t nbf = static_cast<size_t>(m.nbf);
@@ -203,6 +211,12 @@ __device__ __noinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int
     if (!mask[k])
       continue;
     const CxPair P = pairs[k];
+    // the batch's geometric screen (seminumerical_exchange.cpp:793-799)
+    {
+      const double dx = P.Pc[0] - geo.x, dy = P.Pc[1] - geo.y, dz = P.Pc[2] - geo.z;
+      if (sqrt(dx * dx + dy * dy + dz * dz) - P.ext >= geo.w + kCosxMargin)
+        continue;
+    }
     const int ncp = (P.la + 1) * (P.la + 2) / 2, ncq = (P.lb + 1) * (P.lb + 2) / 2;
     const int L2 = P.la + P.lb;
     double V[kCosxNc][kCosxNc];
@@ -284,12 +298,14 @@ __global__ void __launch_bounds__(256) k_cosx_g(MolDev m, int l0, int off0, int 
                                                 const CxPair *__restrict__ pairs,
                                                 const CxPrim *__restrict__ prims,
                                                 const double *__restrict__ etab,
-                                                const int *__restrict__ mask, int pure,
+                                                const int *__restrict__ mask,
+                                                const double4 *__restrict__ lgeo, int pure,
                                                 const double *__restrict__ F,
                                                 double *__restrict__ G) {
   const DevLeaf L = m.leaves[l0 + blockIdx.x];
+  const double4 geo = lgeo[l0 + blockIdx.x];
   for (int p = threadIdx.x; p < L.cnt; p += blockDim.x)
-    cosx_g_point(m, L, p, off0, npairs, pairs, prims, etab, mask, pure, F, G);
+    cosx_g_point(m, L, p, off0, npairs, pairs, prims, etab, mask, geo, pure, F, G);
 }
 
 // K'[mu, lambda] -= sum_g phi_mu(g) G[g, lambda], mu over the leaf's AOs.
@@ -466,6 +482,7 @@ struct CosxState {
   CxPair *d_pairs = nullptr;
   CxPrim *d_prims = nullptr;
   int *d_mask = nullptr;
+  double4 *d_lgeo = nullptr;
   std::vector<void *> allocations;
   ~CosxState() {
     for (void *p : allocations)
@@ -532,6 +549,7 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
   N->gs = gs;
   N->bs = M.bs;
   N->bs.xc_screening_threshold = 1e-14;
+  N->atom_batch = 128; // the reference's batches (seminumerical_exchange.cpp:726-752)
   PartitionFn part;
   if (device_partition_fits(M.device, static_cast<int>(M.Z.size())))
     part = [dev = M.device](const PartitionInput &in, double *w) { device_partition(dev, in, w); };
@@ -558,7 +576,8 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
              "cudaMemcpyAsync D2H");
   cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   // Q = S_num^-1 S
-  const std::vector<double> Q = spd_solve(Sn, overlap_matrix(M.basis), nbf);
+  const std::vector<double> Sa = overlap_matrix(M.basis);
+  const std::vector<double> Q = spd_solve(Sn, Sa, nbf);
   S->d_Q = S->alloc<double>(Q.size());
   cuda_check(cudaMemcpy(S->d_Q, Q.data(), Q.size() * sizeof(double), cudaMemcpyHostToDevice),
              "cudaMemcpy H2D");
@@ -570,7 +589,22 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
   for (size_t p = 0; p < B.shells.size(); p++)
     for (size_t q = 0; q <= p; q++) {
       const Shell &A = B.shells[p], &Bq = B.shells[q];
+      // the engine's significant pairs: a shared origin, or an overlap block
+      // of Frobenius norm >= 1e-12
+      const bool same = A.origin[0] == Bq.origin[0] && A.origin[1] == Bq.origin[1] &&
+                        A.origin[2] == Bq.origin[2];
+      if (!same) {
+        double f2 = 0.0;
+        for (int i = 0; i < B.shell_size(static_cast<int>(p)); i++)
+          for (int j = 0; j < B.shell_size(static_cast<int>(q)); j++) {
+            const double v = Sa[static_cast<size_t>(B.first_bf[q] + j) * nbf + B.first_bf[p] + i];
+            f2 += v * v;
+          }
+        if (!(std::sqrt(f2) >= kCosxPairOverlap))
+          continue;
+      }
       CxPair P{};
+      double pmin = 1e300;
       P.bf_p = B.first_bf[p];
       P.bf_q = B.first_bf[q];
       P.np = B.shell_size(static_cast<int>(p));
@@ -586,6 +620,11 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
           r.pexp = a + b;
           for (int d = 0; d < 3; d++)
             r.P[d] = (a * A.origin[d] + b * Bq.origin[d]) / r.pexp;
+          if (r.pexp < pmin) { // the first most diffuse pair (esp.cpp:84-96)
+            pmin = r.pexp;
+            for (int d = 0; d < 3; d++)
+              P.Pc[d] = r.P[d];
+          }
           r.pref = A.coefs[x] * Bq.coefs[y] * 2.0 * kPi / r.pexp * fac;
           r.e_off = static_cast<int>(et.size());
           for (int d = 0; d < 3; d++)
@@ -593,6 +632,7 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
           prims.push_back(r);
         }
       P.nprim = static_cast<int>(prims.size()) - P.prim0;
+      P.ext = std::sqrt(kCosxLogThreshold / pmin);
       pairs.push_back(P);
     }
   S->npairs = static_cast<int>(pairs.size());
@@ -604,6 +644,16 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
   S->d_etab = dev_upload(et, bytes);
   S->allocations.push_back(S->d_etab);
   S->d_mask = S->alloc<int>(pairs.size());
+  // bounding spheres of the leaves kept by the plan (those with AOs)
+  std::vector<double4> lgeo;
+  for (long b = 0; b < N->plan.nleaves(); b++)
+    if (N->plan.leaf_nbf[b] > 0)
+      lgeo.push_back(make_double4(N->plan.leaf_centre[3 * b], N->plan.leaf_centre[3 * b + 1],
+                                  N->plan.leaf_centre[3 * b + 2], N->plan.leaf_radius[b]));
+  if (lgeo.size() != N->leaves.size())
+    throw std::runtime_error("COSX: leaf geometry does not match the plan");
+  S->d_lgeo = dev_upload(lgeo, bytes);
+  S->allocations.push_back(S->d_lgeo);
   S->d_D = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
   S->d_D2q = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
   S->d_Kp = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
@@ -657,7 +707,7 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
              [&] { k_cosx_f<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_D2q, S.d_F); });
     c.launch("cosx_g", st, [&] {
       k_cosx_g<<<nl, 256, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims, S.d_etab,
-                                   S.d_mask, N.basis.pure ? 1 : 0, S.d_F, S.d_G);
+                                   S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0, S.d_F, S.d_G);
     });
     c.launch("cosx_k", st,
              [&] { k_cosx_k<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_G, S.d_Kp); });

@@ -136,7 +136,10 @@ void Molecule::build_plan() {
   // on the molecule's GPU; OCC_XC_PLAN=host selects the host restatement
   // (host/plan.cpp), which gives the same plan (tests compare the two)
   const char *sel = std::getenv("OCC_XC_PLAN");
-  if (sel && std::strcmp(sel, "host") == 0) {
+  if (atom_batch > 0) {
+    atom_batch_leaves(grid, atom_batch, plan);
+    screen_leaves(basis, bs, plan);
+  } else if (sel && std::strcmp(sel, "host") == 0) {
     morton_leaves(grid, bs, plan);
     screen_leaves(basis, bs, plan);
   } else {

@@ -174,6 +174,8 @@ struct Molecule {
   int deriv = 0; // OCC's density_derivative(): 0 LDA, 1 GGA, 2 meta-GGA
   int vxc_n = 256; // tuning: N of the mixed path's V_xc tile
   int ctas = 0;    // tuning: CTAs of its persistent kernels (0: the context's setting)
+  long atom_batch = 0; // > 0: leaves are batches of this many points per atom block in
+                       // grid order (atom_batch_leaves), not Morton leaves
   MolecularGrid grid;
   Plan plan;
   // device plan

@@ -15,10 +15,14 @@ Restates SemiNumericalExchange's ESP path (src/qm/seminumerical_exchange.cpp):
               p != q, G[:, mu] -= F[:, nu] V^T; K' -= phi^T G
 with the grid of GridSettings::for_sgx (src/numint/grid_settings.cpp:59-68):
 n angular points on every shell, LMG radial precision 1e-5, no pruning, no
-reduced H / He grid.  The reference's per-batch geometric screen (pair
-centre and extent against the batch's bounding sphere plus a 1 Bohr margin)
-is left out: it drops only pairs whose overlap density is negligible at the
-batch, and the GPU form skips it the same way.
+reduced H / He grid.  The two screens of the sweep are restated: the shell
+pairs are the integral engine's significant ones (a shared origin, or an
+overlap block of Frobenius norm >= 1e-12; include/occ/qm/integral_engine.h:
+250-275, seminumerical_exchange.cpp:279-318), and a pair is skipped for a
+batch when |P - c| - extent >= r + 1 Bohr, with c, r the batch's centroid
+and bounding radius and P, extent = sqrt(-ln(1e-12) / p) from the pair's
+first most diffuse primitive pair (src/ints/esp.cpp:84-96,
+seminumerical_exchange.cpp:771-799).
 
 The ESP integrals are McMurchie-Davidson (Hermite expansion of the Gaussian
 product, Hermite Coulomb integrals R_tuv over the Boys function; Helgaker,
@@ -234,11 +238,37 @@ def sgx_grid(basis, angular=110):
     return go.molecular_grid(Z, R, go.basis_shells(basis), s, atom_counts=True)
 
 
+def pair_geometry(s1, s2):
+    """Centre and extent of a shell pair: its first primitive pair (s1's
+    primitives outer, s2's inner) of smallest exponent sum p, and
+    sqrt(-ln(1e-12) / p)."""
+    pmin, P = None, None
+    for a in s1.exps:
+        for b in s2.exps:
+            p = a + b
+            if pmin is None or p < pmin:
+                pmin, P = p, (a * s1.A + b * s2.A) / p
+    return P, math.sqrt(27.631021115928547 / pmin)
+
+
+def significant_pairs(shells, S, threshold=1e-12):
+    """(p, q), p >= q, of a shared origin or overlap block norm >= threshold."""
+    first = np.cumsum([0] + [s.size() for s in shells])
+    out = []
+    for p in range(len(shells)):
+        for q in range(p + 1):
+            if np.array_equal(shells[p].A, shells[q].A) or \
+                    np.linalg.norm(S[first[p]:first[p + 1], first[q]:first[q + 1]]) >= threshold:
+                out.append((p, q))
+    return out
+
+
 def cosx_exchange(basis, D, angular=110, precision=np.finfo(np.float64).eps,
-                  density_threshold=1e-6, block=128):
-    """K (nbf x nbf) of mo.D = D, restricted, ESP path."""
+                  density_threshold=1e-6, block=128, margin=1.0, grid=None):
+    """K (nbf x nbf) of mo.D = D, restricted, ESP path.  grid: (points,
+    weights, atom block sizes) instead of for_sgx(angular)."""
     shells = shells_of(basis)
-    P, W, counts = sgx_grid(basis, angular)
+    P, W, counts = grid if grid is not None else sgx_grid(basis, angular)
     phi = ao_values(shells, P)
     Snum = phi.T @ (phi * W[:, None])
     S = overlap(shells)
@@ -246,29 +276,35 @@ def cosx_exchange(basis, D, angular=110, precision=np.finfo(np.float64).eps,
     D2q = Q @ (2.0 * np.asarray(D))
     first = np.cumsum([0] + [s.size() for s in shells])
     nbf = first[-1]
+    pairs = significant_pairs(shells, S)
+    geo = {pq: pair_geometry(shells[pq[0]], shells[pq[1]]) for pq in pairs}
     K = np.zeros((nbf, nbf))
     off = 0
     for cnt in counts:
         for b0 in range(0, cnt, block):
             idx = slice(off + b0, off + min(cnt, b0 + block))
             ph, w, pts = phi[idx], W[idx], P[idx]
+            centre = pts.mean(axis=0)
+            radius = np.sqrt(((pts - centre) ** 2).sum(axis=1)).max()
             if ph.max() < precision:
                 continue
             F = (ph * w[:, None]) @ D2q
             G = np.zeros_like(F)
-            for p in range(len(shells)):
-                for q in range(p + 1):
-                    bp = slice(first[p], first[p + 1])
-                    bq = slice(first[q], first[q + 1])
-                    mD = np.abs(D2q[bp, bq]).max()
-                    if p != q:
-                        mD = max(mD, np.abs(D2q[bq, bp]).max())
-                    if mD < density_threshold:
-                        continue
-                    V = esp_pair(shells[p], shells[q], pts)
-                    G[:, bq] -= np.einsum("gi,gij->gj", F[:, bp], V)
-                    if p != q:
-                        G[:, bp] -= np.einsum("gj,gij->gi", F[:, bq], V)
+            for p, q in pairs:
+                Pc, ext = geo[(p, q)]
+                if np.linalg.norm(Pc - centre) - ext >= radius + margin:
+                    continue
+                bp = slice(first[p], first[p + 1])
+                bq = slice(first[q], first[q + 1])
+                mD = np.abs(D2q[bp, bq]).max()
+                if p != q:
+                    mD = max(mD, np.abs(D2q[bq, bp]).max())
+                if mD < density_threshold:
+                    continue
+                V = esp_pair(shells[p], shells[q], pts)
+                G[:, bq] -= np.einsum("gi,gij->gj", F[:, bp], V)
+                if p != q:
+                    G[:, bp] -= np.einsum("gj,gij->gi", F[:, bq], V)
             K -= ph.T @ G
         off += cnt
     return 0.25 * (K + K.T)

@@ -94,6 +94,39 @@ def test_oracle_exchange_approaches_exact_exchange(angular, bar):
     assert err < bar, err
 
 
+def test_oracle_screens_act_on_separated_waters():
+    """Two waters 7 Angstrom apart with a density that does not couple them
+    (the screen relies on the decay of D): the geometric screen skips far
+    pairs in far batches, and what it drops is small."""
+    atoms1, _ = _water()
+    atoms2, _ = _water(shift=(0.0, 0.0, 7.0))
+    b = og.AOBasis.load(atoms1 + atoms2, "sto-3g")
+    b.set_pure(False)
+    n = b.nbf()
+    C = np.random.default_rng(3).normal(size=(n // 2, 5)) * 0.3
+    D = np.zeros((n, n))
+    D[:n // 2, :n // 2] = C @ C.T
+    D[n // 2:, n // 2:] = C @ C.T
+    shells = cx.shells_of(b)
+    P, W, counts = cx.sgx_grid(b, 26)
+    skipped = 0
+    pairs = cx.significant_pairs(shells, cx.overlap(shells))
+    off = 0
+    for cnt in counts:
+        for b0 in range(0, cnt, 128):
+            pts = P[off + b0:off + min(cnt, b0 + 128)]
+            c = pts.mean(axis=0)
+            r = np.sqrt(((pts - c) ** 2).sum(axis=1)).max()
+            for pq in pairs:
+                Pc, ext = cx.pair_geometry(shells[pq[0]], shells[pq[1]])
+                skipped += np.linalg.norm(Pc - c) - ext >= r + 1.0
+        off += cnt
+    assert skipped > 0
+    K = cx.cosx_exchange(b, D, grid=(P, W, counts))
+    K_all = cx.cosx_exchange(b, D, grid=(P, W, counts), margin=np.inf)
+    assert 0.0 < np.abs(K - K_all).max() < 2e-4
+
+
 def test_oracle_sgx_grid_is_the_library_host_grid():
     _, b = _water()
     P, W, counts = cx.sgx_grid(b, 50)
