@@ -106,6 +106,25 @@ __device__ __forceinline__ F2 quick_two_sum(float a, float b) { // |a| >= |b|
   const float s = __fadd_rn(a, b);
   return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
+// x as a double-float by integer operations, off the FP64 pipe: the sign,
+// exponent and top 23 mantissa bits as h, the remaining 29 bits (an exact
+// integer times a power of two) rounded to FP32 as l, then renormalised.
+// For |x| below FP32's largest value; l underflows to zero when x is below
+// about 1e-21 (x then keeps FP32 precision), and values below FP32's normal
+// range give zero.
+__device__ __forceinline__ F2 f2_bits(double x) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+  const int e = static_cast<int>((u >> 52) & 0x7ff);
+  if (e - 1023 + 127 < 1) // below FP32's normal range (and zero)
+    return {0.f, 0.f};
+  const unsigned sgn = static_cast<unsigned>(u >> 32) & 0x80000000u;
+  const float h = __uint_as_float(sgn | (static_cast<unsigned>(e - 1023 + 127) << 23) |
+                                  static_cast<unsigned>((u >> 29) & 0x7fffffu));
+  const int el = e - 1023 - 52 + 127; // biased exponent of the lowest mantissa bit
+  const float scale = el >= 1 ? __uint_as_float(static_cast<unsigned>(el) << 23) : 0.f;
+  const float l = __uint2float_rn(static_cast<unsigned>(u & 0x1fffffffu)) * scale;
+  return quick_two_sum(h, sgn ? -l : l);
+}
 __device__ __forceinline__ F2 two_sum_f(float a, float b) {
   const float s = __fadd_rn(a, b);
   const float bb = __fsub_rn(s, a);
@@ -452,6 +471,34 @@ __device__ __forceinline__ void eval_xc_mixed(const FuncSet &fs, double rho, dou
     e += fs.coef[i] * fn::to_d(c.v);
     vrho += fs.coef[i] * static_cast<double>(c.r);
     vsigma += fs.coef[i] * static_cast<double>(c.s);
+  }
+}
+
+// The same with double-float inputs and outputs: no FP64 operation where
+// rho >= 1e-10 and, for a GGA (gga), sigma >= 1e-30 (the mixture
+// coefficients are split by integer operations).
+__device__ __forceinline__ void eval_xc_mixed_f2(const FuncSet &fs, bool gga, fn::F2 rho,
+                                                 fn::F2 sigma, fn::F2 &e, float &vrho,
+                                                 float &vsigma) {
+  if (!(rho.h >= 1e-10f) || (gga && !(sigma.h >= 1e-30f))) {
+    double ed, vr, vs;
+    eval_xc(fs, fn::to_d(rho), fn::to_d(sigma), ed, vr, vs);
+    e = fn::f2(ed);
+    vrho = static_cast<float>(vr);
+    vsigma = static_cast<float>(vs);
+    return;
+  }
+  fn::G r{rho, 1.f, 0.f};
+  fn::G s{sigma, 0.f, 1.f};
+  fn::RhoPowers<fn::G> P = fn::rho_powers(r);
+  e = {0.f, 0.f};
+  vrho = vsigma = 0.f;
+  for (int i = 0; i < fs.n; i++) {
+    const fn::F2 ci = fn::f2_bits(fs.coef[i]);
+    fn::G c = fn::component(fs.id[i], r, s, P);
+    e = fn::f2_add(e, fn::f2_mul(ci, c.v));
+    vrho = fmaf(ci.h, c.r, vrho);
+    vsigma = fmaf(ci.h, c.s, vsigma);
   }
 }
 

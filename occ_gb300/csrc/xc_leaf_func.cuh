@@ -12,38 +12,50 @@
 
 namespace occx {
 
-// Sum / maximum over the NT threads of the CTA (sh: NT / 32 doubles).
-template <int NT = 256> __device__ __forceinline__ double leaf_sum256(double v, double *sh) {
+// The barrier of the NT threads that run a leaf's functional: the whole CTA
+// (BAR = 0), or named barrier BAR shared by threads 0 .. NT - 1 only.
+template <int NT, int BAR> __device__ __forceinline__ void leaf_bar() {
+  if constexpr (BAR == 0)
+    __syncthreads();
+  else
+    asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(NT) : "memory");
+}
+
+// Sum / maximum over the NT threads 0 .. NT - 1 (sh: NT / 32 doubles).
+template <int NT = 256, int BAR = 0>
+__device__ __forceinline__ double leaf_sum256(double v, double *sh) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
     v += __shfl_xor_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0)
     sh[threadIdx.x >> 5] = v;
-  __syncthreads();
+  leaf_bar<NT, BAR>();
   double s = 0.0;
   for (int i = 0; i < NT / 32; i++)
     s += sh[i];
-  __syncthreads();
+  leaf_bar<NT, BAR>();
   return s;
 }
 
-template <int NT = 256> __device__ __forceinline__ double leaf_max256(double v, double *sh) {
+template <int NT = 256, int BAR = 0>
+__device__ __forceinline__ double leaf_max256(double v, double *sh) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
     v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   if ((threadIdx.x & 31) == 0)
     sh[threadIdx.x >> 5] = v;
-  __syncthreads();
+  leaf_bar<NT, BAR>();
   double s = sh[0];
   for (int i = 1; i < NT / 32; i++)
     s = fmax(s, sh[i]);
-  __syncthreads();
+  leaf_bar<NT, BAR>();
   return s;
 }
 
 // MIXED: the mixed path's evaluator (double-float values, FP32 derivatives).
-// NT: threads of the CTA (they stride over the leaf's points).
-template <bool DERIV, bool MIXED = false, int NT = 256>
+// NT: threads 0 .. NT - 1 stride over the leaf's points; BAR: their barrier
+// (leaf_bar).
+template <bool DERIV, bool MIXED = false, int NT = 256, int BAR = 0>
 __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__restrict__ pts,
                                                 size_t N, const FuncSet &fs, double thr,
                                                 const double *__restrict__ rho,
@@ -52,7 +64,7 @@ __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__r
   double mx = -1e300;
   for (int p = threadIdx.x; p < L.cnt; p += NT)
     mx = fmax(mx, rho[static_cast<size_t>(L.off) + p]);
-  mx = leaf_max256<NT>(mx, sh);
+  mx = leaf_max256<NT, BAR>(mx, sh);
   const bool skip = mx < thr;
   double nel = 0.0, ew = 0.0;
   for (int p = threadIdx.x; p < L.cnt; p += NT) {
@@ -83,11 +95,104 @@ __device__ __forceinline__ void leaf_functional(const DevLeaf &L, const Pt4 *__r
     }
     ew += w * e;
   }
-  nel = leaf_sum256<NT>(nel, sh);
-  ew = leaf_sum256<NT>(ew, sh);
+  nel = leaf_sum256<NT, BAR>(nel, sh);
+  ew = leaf_sum256<NT, BAR>(ew, sh);
   if (threadIdx.x == 0) {
     epart2[0] = ew;
     epart2[1] = nel;
+  }
+}
+
+// Sum over threads 0 .. NT - 1 of a double-float (sh: NT / 32 float2).
+template <int NT, int BAR>
+__device__ __forceinline__ fn::F2 leaf_sum_f2(fn::F2 v, float2 *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const fn::F2 w{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+    v = fn::f2_add(v, w);
+  }
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = make_float2(v.h, v.l);
+  leaf_bar<NT, BAR>();
+  fn::F2 s{0.f, 0.f};
+  for (int i = 0; i < NT / 32; i++)
+    s = fn::f2_add(s, fn::F2{sh[i].x, sh[i].y});
+  leaf_bar<NT, BAR>();
+  return s;
+}
+
+// Maximum over threads 0 .. NT - 1 of FP64 bit patterns as signed integers:
+// the maximum of the values when any is non-negative, and a negative value
+// when all are (sh: NT / 32 long longs).
+template <int NT, int BAR>
+__device__ __forceinline__ long long leaf_max_bits(long long v, long long *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = v;
+  leaf_bar<NT, BAR>();
+  long long s = sh[0];
+  for (int i = 1; i < NT / 32; i++)
+    s = max(s, sh[i]);
+  leaf_bar<NT, BAR>();
+  return s;
+}
+
+// The tensor-core build's functional stage in double-float arithmetic, with
+// no FP64 operation per point (the FP64 inputs are split by integer
+// operations, fn::f2_bits; eval_xc_mixed_f2): the skip, weights and
+// coefficients of leaf_functional<.., MIXED>, the coefficients as FP32 into
+// cf[p] for p < npad (zero past the leaf's points; no FP64 coefficient
+// array), E and the electron count summed in double-float and written as
+// FP64 partials.  sh: NT / 32 eight-byte words.
+template <bool DERIV, int NT, int BAR>
+__device__ __forceinline__ void leaf_functional_f2(const DevLeaf &L, const Pt4 *__restrict__ pts,
+                                                   size_t N, const FuncSet &fs, double thr,
+                                                   const double *__restrict__ rho, float4 *cf,
+                                                   int npad, double *epart2, double *sh) {
+  long long mb = -0x7fffffffffffffffLL - 1;
+  for (int p = threadIdx.x; p < L.cnt; p += NT)
+    mb = max(mb, __double_as_longlong(rho[static_cast<size_t>(L.off) + p]));
+  mb = leaf_max_bits<NT, BAR>(mb, reinterpret_cast<long long *>(sh));
+  const bool skip = __longlong_as_double(mb) < thr;
+  fn::F2 nel{0.f, 0.f}, ew{0.f, 0.f};
+  for (int p = threadIdx.x; p < npad; p += NT) {
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (p < L.cnt) {
+      const size_t idx = static_cast<size_t>(L.off) + p;
+      const fn::F2 r = fn::f2_bits(rho[idx]);
+      const fn::F2 w = fn::f2_bits(pts[idx].w);
+      nel = fn::f2_add(nel, fn::f2_mul(w, r));
+      fn::F2 gx{0.f, 0.f}, gy{0.f, 0.f}, gz{0.f, 0.f}, sigma{0.f, 0.f};
+      if (DERIV) {
+        gx = fn::f2_bits(rho[N + idx]);
+        gy = fn::f2_bits(rho[2 * N + idx]);
+        gz = fn::f2_bits(rho[3 * N + idx]);
+        sigma = fn::f2_add(fn::f2_add(fn::f2_mul(gx, gx), fn::f2_mul(gy, gy)), fn::f2_mul(gz, gz));
+      }
+      if (!skip) {
+        fn::F2 e;
+        float vr, vs;
+        eval_xc_mixed_f2(fs, DERIV, r, sigma, e, vr, vs);
+        c.x = 0.5f * w.h * vr;
+        if (DERIV) {
+          const float f = 2.f * w.h * vs;
+          c.y = f * gx.h;
+          c.z = f * gy.h;
+          c.w = f * gz.h;
+        }
+        ew = fn::f2_add(ew, fn::f2_mul(w, e));
+      }
+    }
+    cf[p] = c;
+  }
+  float2 *shf = reinterpret_cast<float2 *>(sh);
+  nel = leaf_sum_f2<NT, BAR>(nel, shf);
+  ew = leaf_sum_f2<NT, BAR>(ew, shf);
+  if (threadIdx.x == 0) {
+    epart2[0] = fn::to_d(ew);
+    epart2[1] = fn::to_d(nel);
   }
 }
 

@@ -1572,6 +1572,66 @@ __global__ void __launch_bounds__(kFuncThreads, 4) k_func_b(const MixTab *__rest
     ymix_block<DERIV>(T, blocks[li.block0 + b], cf);
 }
 
+constexpr int kLeafMaxPts = 1024; // leaf_max's bound (check_build_settings)
+
+// Y hi / lo of one block from the coefficients cf[0 .. 127] (FP32), by the
+// NS threads tid = 0 .. NS - 1.
+template <bool DERIV, int NS>
+__device__ __forceinline__ void ymix_stream(const MixTab &T, const MBlock &B,
+                                            const float4 *__restrict__ cf, int tid) {
+  float4 *__restrict__ base = reinterpret_cast<float4 *>(T.ws + B.ws_off);
+  const size_t plane = static_cast<size_t>(B.mp) * (kBlockPts / 4); // in float4
+  const int n4 = B.mp * (kBlockPts / 4);
+#pragma unroll 4
+  for (int q = tid; q < n4; q += NS) {
+    const int p = (q % (kBlockPts / 4)) * 4;
+    const float4 a = base[q];
+    const float4 c0 = cf[p], c1 = cf[p + 1], c2 = cf[p + 2], c3 = cf[p + 3];
+    float4 y;
+    y.x = a.x * c0.x;
+    y.y = a.y * c1.x;
+    y.z = a.z * c2.x;
+    y.w = a.w * c3.x;
+    if (DERIV) {
+      const float4 gx = base[plane + q], gy = base[2 * plane + q], gz = base[3 * plane + q];
+      y.x = fmaf(gz.x, c0.w, fmaf(gy.x, c0.z, fmaf(gx.x, c0.y, y.x)));
+      y.y = fmaf(gz.y, c1.w, fmaf(gy.y, c1.z, fmaf(gx.y, c1.y, y.y)));
+      y.z = fmaf(gz.z, c2.w, fmaf(gy.z, c2.z, fmaf(gx.z, c2.y, y.z)));
+      y.w = fmaf(gz.w, c3.w, fmaf(gy.w, c3.z, fmaf(gx.w, c3.y, y.w)));
+    }
+    float4 yh, yl;
+    tf32_split(y.x, yh.x, yl.x);
+    tf32_split(y.y, yh.y, yl.y);
+    tf32_split(y.z, yh.z, yl.z);
+    tf32_split(y.w, yh.w, yl.w);
+    base[kPlaneYHi * plane + q] = yh;
+    base[kPlaneYLo * plane + q] = yl;
+  }
+}
+
+// The build's functional stage (one CTA per leaf item, four per SM): the
+// functional in double-float arithmetic (leaf_functional_f2, no FP64
+// operation per point) with the coefficients as FP32 into shared memory, then
+// the V_xc operand Y of each of the leaf's blocks from them (ymix_stream).
+// The FP64 coefficient array is not written.
+template <bool DERIV>
+__global__ void __launch_bounds__(kFuncThreads, 4) k_func_f2(const MixTab *__restrict__ tabs,
+                                                          const MBlock *__restrict__ blocks,
+                                                          const LeafItem *__restrict__ litems) {
+  __shared__ double red[kFuncThreads / 32];
+  __shared__ float4 cf[kLeafMaxPts];
+  const LeafItem li = litems[blockIdx.x];
+  const MixTab &T = tabs[li.mol];
+  const int nblk = min(li.nblk, kLeafMaxPts / kBlockPts);
+  leaf_functional_f2<DERIV, kFuncThreads, 0>(T.m.leaves[li.leaf], T.m.pts,
+                                             static_cast<size_t>(T.m.npts), T.fs, T.dens_thr,
+                                             T.rho, cf, nblk * kBlockPts, T.epart + 2 * li.leaf,
+                                             red);
+  __syncthreads(); // cf is complete
+  for (int q = 0; q < nblk; q++)
+    ymix_stream<DERIV, kFuncThreads>(T, blocks[li.block0 + q], &cf[q * kBlockPts], threadIdx.x);
+}
+
 // Fixed-order FP64 sums of the per-leaf partials, one CTA per molecule.
 __global__ void __launch_bounds__(256) k_reduce_b(const MixTab *__restrict__ tabs, Override ov) {
   __shared__ double sh[8];
@@ -1903,9 +1963,9 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
   if (nl > 0)
     c.launch("func", st, [&] {
       if (P.deriv)
-        k_func_b<true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_f2<true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
       else
-        k_func_b<false><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_f2<false><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
     });
   if (ni > 0)
     c.launch("vxc_mixed", st, [&] {
@@ -2672,8 +2732,10 @@ extern "C" int occ_xc_batch_get_result(occ_xc_context *ctx, occ_xc_batch *b, int
 
 namespace occx {
 namespace {
+// f2: the build's evaluator (eval_xc_mixed_f2 on inputs split by
+// fn::f2_bits) instead of eval_xc_mixed.
 __global__ void k_selftest_func(FuncSet fs, int n, const double *rho, const double *sigma,
-                                double *out64, double *outm) {
+                                double *out64, double *outm, int f2) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
     return;
@@ -2682,7 +2744,19 @@ __global__ void k_selftest_func(FuncSet fs, int n, const double *rho, const doub
   out64[3 * i] = e;
   out64[3 * i + 1] = vr;
   out64[3 * i + 2] = vs;
-  eval_xc_mixed(fs, rho[i], sigma[i], e, vr, vs);
+  if (f2) {
+    bool gga = false;
+    for (int k = 0; k < fs.n; k++)
+      gga = gga || func_is_gga(fs.id[k]);
+    fn::F2 ef;
+    float vrf, vsf;
+    eval_xc_mixed_f2(fs, gga, fn::f2_bits(rho[i]), fn::f2_bits(sigma[i]), ef, vrf, vsf);
+    e = fn::to_d(ef);
+    vr = vrf;
+    vs = vsf;
+  } else {
+    eval_xc_mixed(fs, rho[i], sigma[i], e, vr, vs);
+  }
   outm[3 * i] = e;
   outm[3 * i + 1] = vr;
   outm[3 * i + 2] = vs;
@@ -2785,11 +2859,29 @@ extern "C" int occ_xc_selftest_functional_mgga(occ_xc_context *ctx, const char *
   });
 }
 
+namespace {
+int selftest_functional(occ_xc_context *ctx, const char *method, int n, const double *rho,
+                        const double *sigma, double *out64, double *outm, int f2);
+}
+
 // The FP64 and the mixed-path functional evaluators at n points (host
-// arrays; out64 / outm receive e, vrho, vsigma per point), for testing.
+// arrays; out64 / outm receive e, vrho, vsigma per point), for testing:
+// eval_xc_mixed (the gradient's and the unrestricted builds' functional
+// stage) and, with _f2, eval_xc_mixed_f2 (the restricted build's).
 extern "C" int occ_xc_selftest_functional(occ_xc_context *ctx, const char *method, int n,
                                           const double *rho, const double *sigma,
                                           double *out64, double *outm) {
+  return selftest_functional(ctx, method, n, rho, sigma, out64, outm, 0);
+}
+extern "C" int occ_xc_selftest_functional_f2(occ_xc_context *ctx, const char *method, int n,
+                                             const double *rho, const double *sigma,
+                                             double *out64, double *outm) {
+  return selftest_functional(ctx, method, n, rho, sigma, out64, outm, 1);
+}
+
+namespace {
+int selftest_functional(occ_xc_context *ctx, const char *method, int n, const double *rho,
+                        const double *sigma, double *out64, double *outm, int f2) {
   if (!ctx || !method || n <= 0 || !rho || !sigma || !out64 || !outm)
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
@@ -2803,7 +2895,8 @@ extern "C" int occ_xc_selftest_functional(occ_xc_context *ctx, const char *metho
       cuda_check(cudaMemcpyAsync(d, rho, n * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
       cuda_check(cudaMemcpyAsync(d + n, sigma, n * sizeof(double), cudaMemcpyHostToDevice, st),
                  "H2D");
-      k_selftest_func<<<(n + 127) / 128, 128, 0, st>>>(fs, n, d, d + n, d + 2 * n, d + 5 * n);
+      k_selftest_func<<<(n + 127) / 128, 128, 0, st>>>(fs, n, d, d + n, d + 2 * n, d + 5 * n,
+                                                       f2);
       cuda_check(cudaGetLastError(), "kernel launch");
       cuda_check(cudaMemcpyAsync(out64, d + 2 * n, 3 * n * sizeof(double),
                                  cudaMemcpyDeviceToHost, st), "D2H");
@@ -2817,6 +2910,7 @@ extern "C" int occ_xc_selftest_functional(occ_xc_context *ctx, const char *metho
     cudaFree(d);
   });
 }
+} // namespace
 
 // ---- XC nuclear gradient on the tensor cores ------------------------------
 // DFT::compute_xc_gradient (include/occ/dft/dft.h:599-749) as

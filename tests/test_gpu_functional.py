@@ -25,18 +25,20 @@ def _points(n, seed):
     return rho, sigma
 
 
+@pytest.mark.parametrize("entry", ["occ_xc_selftest_functional", "occ_xc_selftest_functional_f2"])
 @pytest.mark.parametrize("method", METHODS)
-def test_mixed_functional_matches_fp64(method):
+def test_mixed_functional_matches_fp64(method, entry):
+    """eval_xc_mixed (gradient, unrestricted builds) and eval_xc_mixed_f2
+    (the restricted build's stage, inputs split by integer operations)."""
     ctx = _context(0)
     lib = ctx.lib
-    lib.occ_xc_selftest_functional.argtypes = [C.c_void_p, C.c_char_p, C.c_int, _dp, _dp, _dp,
-                                               _dp]
+    fn = getattr(lib, entry)
+    fn.argtypes = [C.c_void_p, C.c_char_p, C.c_int, _dp, _dp, _dp, _dp]
     n = 20000
     rho, sigma = _points(n, 7)
     o64 = np.zeros(3 * n)
     om = np.zeros(3 * n)
-    rc = lib.occ_xc_selftest_functional(ctx.h, method.encode(), n, _ptr(rho), _ptr(sigma),
-                                        _ptr(o64), _ptr(om))
+    rc = fn(ctx.h, method.encode(), n, _ptr(rho), _ptr(sigma), _ptr(o64), _ptr(om))
     assert rc == 0, ctx.error()
     e64, vr64, vs64 = o64[0::3], o64[1::3], o64[2::3]
     em, vrm, vsm = om[0::3], om[1::3], om[2::3]
