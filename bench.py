@@ -52,7 +52,7 @@ def parse():
                     help="CTAs of the persistent tensor-core kernels (0: one per SM)")
     ap.add_argument("--workload", default="water32",
                     choices=["water32", "water", "alkane", "clusters", "stream", "gradient", "grid",
-                             "uks", "vv10", "mgga"],
+                             "uks", "vv10", "mgga", "cosx"],
                     help="water32: the headline build (default); water: one water molecule, "
                          "6-31G, LDA (latency-bound); alkane: C30H62 def2-TZVP "
                          "B3LYP, 15 iterations as one CUDA graph; clusters: 512 clusters "
@@ -60,7 +60,8 @@ def parse():
                          "the XC nuclear gradient of the water32 molecule; grid: its molecular "
                          "grid with the Becke partition on the GPU; uks: an unrestricted FP64 "
                          "build of its cation radical; vv10: its VV10 non-local correlation; "
-                         "mgga: its meta-GGA (TPSS) build")
+                         "mgga: its meta-GGA (TPSS) build; cosx: seminumerical exchange of "
+                         "an 8-water cluster (--waters) on the for_sgx(50) grid, FP64")
     ap.add_argument("--clusters", type=int, default=512)
     ap.add_argument("--requests", type=int, default=32)
     ap.add_argument("--rate", type=float, default=10.0, help="stream arrivals per second")
@@ -74,8 +75,10 @@ def run_workload(args):
     torch.cuda.set_device(0)
     with ClockSampler(0) as cs:
         if args.workload == "alkane":
+            args.steps = min(args.steps, 3)  # graphs of 15 builds; FP64 takes seconds
             r = bw.alkane_graph(torch, steps=args.steps, warmup=args.warmup)
         elif args.workload == "clusters":
+            args.steps, args.warmup = min(args.steps, 2), min(args.warmup, 1)  # FP64: ~20 s a batch
             r = bw.clusters_batch(torch, steps=args.steps, warmup=args.warmup,
                                   nclusters=args.clusters)
         elif args.workload == "gradient":
@@ -88,6 +91,9 @@ def run_workload(args):
             r = bw.vv10(steps=args.steps, warmup=args.warmup, waters=args.waters)
         elif args.workload == "mgga":
             r = bw.mgga_build(torch, steps=args.steps, warmup=args.warmup, waters=args.waters)
+        elif args.workload == "cosx":
+            r = bw.cosx(torch, steps=max(1, min(args.steps, 5)), warmup=1,
+                        waters=8 if args.waters == 32 else args.waters)
         elif args.workload == "water":
             r = bw.water_latency(torch, steps=max(args.steps, 100), warmup=max(args.warmup, 10))
         else:
@@ -111,6 +117,16 @@ def run_workload(args):
                 "value": r["mixed"]["builds_per_s"], "unit": "builds/s", "n_gpus": 1,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3+f64",
+                "data": "synthetic", "config": {"workload": r.pop("workload")},
+                "clocks": cs.summary()}
+        line.update(r)
+        print(json.dumps(line))
+        return
+    if args.workload == "cosx":
+        line = {"metric": "seminumerical (COSX) exchange matrices/s (FP64)",
+                "value": r.pop("calls_per_s"), "unit": "calls/s", "n_gpus": 1,
+                "steps": max(1, min(args.steps, 5)), "warmup": 1, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": {"workload": r.pop("workload")},
                 "clocks": cs.summary()}
         line.update(r)

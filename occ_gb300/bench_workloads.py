@@ -7,8 +7,9 @@ alkane_graph    n-C30H62, def2-TZVP, B3LYP (local part), 15 SCF-iteration
 clusters        512 water clusters, n uniform in {1..24}, box 3.1 n^(1/3)
                 Angstrom, def2-SVP, PBE, built as one batch (one launch
                 sequence per sub-batch); leaf size and tile from the
-                autotuner, tuned on one molecule per size and applied to the
-                rest; builds/s and grid points/s, mixed against FP64.
+                autotuner, tuned on one molecule of each of seven sizes and
+                applied to the molecules nearest in size; builds/s and grid
+                points/s, mixed against FP64 (at most 2 timed batches).
 stream          Poisson arrivals (seeded rate) of requests of 8-20 SCF
                 iterations for water clusters with n uniform in {2..48},
                 def2-SVP, PBE, each iteration's density the previous one plus
@@ -31,6 +32,9 @@ uks             unrestricted (UKS) build of a 32-water cation radical (def2-SVP,
                 host one, and the mixed result against FP64.
 vv10            VV10 non-local correlation of 32 waters (def2-SVP, 254,976
                 NLC points): FP64 and FP32-pair-sum calls, their difference.
+cosx            seminumerical (COSX) exchange matrix of an 8-water cluster
+                (def2-SVP) on the for_sgx(50) grid, FP64, device and host
+                entry points, set-up apart.
 
 Every input is seeded synthetic data with the shapes of these workloads.
 Each function returns a dict for one JSON line.
@@ -93,6 +97,12 @@ def alkane_graph(torch, steps=3, warmup=3, iterations=15, seed=0, ncarbon=30):
     return out
 
 
+def _progress(msg):
+    import sys
+    sys.stderr.write(f"[{time.strftime('%H:%M:%S')}] {msg}\n")
+    sys.stderr.flush()
+
+
 def clusters_batch(torch, steps=2, warmup=1, nclusters=512, seed=0, autotune=True):
     rng = np.random.default_rng(seed)
     sizes = rng.integers(1, 25, nclusters)
@@ -105,16 +115,22 @@ def clusters_batch(torch, steps=2, warmup=1, nclusters=512, seed=0, autotune=Tru
         dfts.append(DFT("pbe", b))
         Ds.append(wl.random_density(b.nbf(), 5 * int(n), seed=seed + 5000 + i))
     setup_s = time.perf_counter() - t0
+    _progress(f"clusters: {nclusters} molecules set up in {setup_s:.1f} s")
+    # the tuner runs on one molecule of each of seven sizes; every molecule
+    # takes the choice of the nearest tuned size
     tuned = {}
     t0 = time.perf_counter()
     if autotune:
+        reps = (1, 4, 8, 12, 16, 20, 24)
         for i, n in enumerate(sizes):
             n = int(n)
-            if n not in tuned:
+            if n in reps and n not in tuned:
                 tuned[n] = dfts[i].autotune(Ds[i], MIXED, tol_exc=1e-7)
-            else:
-                dfts[i].apply_tuning(tuned[n])
+        for i, n in enumerate(sizes):
+            near = min(tuned, key=lambda r: abs(r - int(n)))
+            dfts[i].apply_tuning(tuned[near])
     tune_s = time.perf_counter() - t0
+    _progress(f"clusters: tuned in {tune_s:.1f} s")
     npts = sum(d.info()["npoints"] for d in dfts)
     out = {"workload": f"clusters{nclusters}_n1to24_def2svp_pbe_batch", "nclusters": nclusters,
            "total_points": int(npts), "total_atoms": int(3 * sizes.sum()),
@@ -135,6 +151,7 @@ def clusters_batch(torch, steps=2, warmup=1, nclusters=512, seed=0, autotune=Tru
         for _ in range(warmup):
             one()
         torch.cuda.synchronize()
+        _progress(f"clusters: {name} warm-up done")
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
         ev[0].record(stream)
         for i in range(steps):
@@ -142,6 +159,7 @@ def clusters_batch(torch, steps=2, warmup=1, nclusters=512, seed=0, autotune=Tru
             ev[i + 1].record(stream)
         torch.cuda.synchronize()
         batch.check(C.c_void_p(stream.cuda_stream))
+        _progress(f"clusters: {name} timed")
         per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
         ms = float(np.median(per))
         res[name] = np.array([batch.result(i)[1] for i in range(nclusters)])
@@ -637,3 +655,45 @@ def vv10(steps=3, warmup=1, waters=32, seed=0):
     out["abs_dE_mixed_vs_fp64"] = abs(res["mixed"][0] - res["fp64"][0])
     out["max_abs_dV_mixed_vs_fp64"] = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1])))
     return out
+
+
+def cosx(torch, steps=3, warmup=1, waters=8, seed=0, angular=50):
+    """Seminumerical (COSX) exchange of a water cluster (def2-SVP, pure d
+    shells) on the grid of GridSettings.for_sgx(angular), FP64: calls/s
+    through the device entry point (CUDA events, D and K resident) and
+    through the host one (D in, K out), with the set-up (grid, AO values,
+    overlap projector) timed apart."""
+    from .xc import GridSettings, SemiNumericalExchange
+    box = 10.0 * (waters / 32.0) ** (1.0 / 3.0)
+    mol = wl.water_cluster(waters, box=box, seed=seed)
+    b = wl.basis_for(mol, "def2-svp")
+    nbf = b.nbf()
+    D = wl.random_density(nbf, 5 * waters, seed=seed)
+    dft = DFT("lda", b)
+    t0 = time.perf_counter()
+    sgx = SemiNumericalExchange(dft, GridSettings.for_sgx(angular))
+    setup_s = time.perf_counter() - t0
+    dD = torch.from_numpy(np.asfortranarray(D).ravel(order="F").copy()).cuda()
+    dK = torch.zeros_like(dD)
+    stream = torch.cuda.Stream()
+    for _ in range(warmup):
+        sgx.compute_K_device(dD.data_ptr(), dK.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for i in range(steps):
+        sgx.compute_K_device(dD.data_ptr(), dK.data_ptr(), stream.cuda_stream)
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        K = sgx.compute_K(D)
+    e2e_s = (time.perf_counter() - t0) / steps
+    Kd = dK.cpu().numpy().reshape(nbf, nbf, order="F")
+    return {"workload": f"water{waters}_def2svp_cosx{angular}", "nbf": nbf,
+            "npoints": int(sgx.grid_points()), "calls_per_s": 1e3 / ms, "ms_per_call": ms,
+            "e2e": {"value": 1.0 / e2e_s, "unit": "calls/s",
+                    "h2d_bytes_per_step": int(D.nbytes), "d2h_bytes_per_step": int(K.nbytes)},
+            "setup_s": setup_s, "max_abs_K": float(np.abs(K).max()),
+            "host_vs_device_max_dK": float(np.abs(K - Kd).max())}

@@ -25,6 +25,9 @@ enum FuncId : int {
   kGgaCPbe = 130,
   kGgaCLyp = 131,
   kHybB3lyp = 402,
+  kHybPbeh = 406,      // 0.75 PBE exchange + PBE correlation (PBE0's local part)
+  kHybBhandh = 435,    // 0.5 Slater + LYP
+  kHybBhandhlyp = 436, // 0.5 B88 + LYP
   kHybB3lyp5 = 475,
 };
 
@@ -37,7 +40,8 @@ struct FuncSet {
 
 __host__ __device__ inline bool func_is_gga(int id) {
   return id == kGgaXPbe || id == kGgaXB88 || id == kGgaCPbe || id == kGgaCLyp ||
-         id == kHybB3lyp || id == kHybB3lyp5;
+         id == kHybB3lyp || id == kHybB3lyp5 || id == kHybPbeh || id == kHybBhandh ||
+         id == kHybBhandhlyp;
 }
 __host__ __device__ inline bool func_known(int id) {
   return id == kLdaX || id == kLdaCVwn || id == kLdaCVwnRpa || id == kLdaCVwn3 ||
@@ -107,11 +111,12 @@ __device__ __forceinline__ F2 quick_two_sum(float a, float b) { // |a| >= |b|
   return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 // x as a double-float by integer operations, off the FP64 pipe: the sign,
-// exponent and top 23 mantissa bits as h, the remaining 29 bits (an exact
-// integer times a power of two) rounded to FP32 as l, then renormalised.
-// For |x| below FP32's largest value; l underflows to zero when x is below
-// about 1e-21 (x then keeps FP32 precision), and values below FP32's normal
-// range give zero.
+// exponent and top 23 mantissa bits as h, the remaining 29 bits as l =
+// (m29 2^-29) 2^(E-23), E the exponent of x: m29 rounded to FP32 and scaled
+// by two powers of two, both exact while 2^(E-23) is an FP32 normal number
+// (|x| above about 1e-31), then renormalised.  For |x| below FP32's largest
+// value; below about 1e-31 l is dropped (x keeps FP32 precision), and values
+// below FP32's normal range give zero.
 __device__ __forceinline__ F2 f2_bits(double x) {
   const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
   const int e = static_cast<int>((u >> 52) & 0x7ff);
@@ -120,9 +125,9 @@ __device__ __forceinline__ F2 f2_bits(double x) {
   const unsigned sgn = static_cast<unsigned>(u >> 32) & 0x80000000u;
   const float h = __uint_as_float(sgn | (static_cast<unsigned>(e - 1023 + 127) << 23) |
                                   static_cast<unsigned>((u >> 29) & 0x7fffffu));
-  const int el = e - 1023 - 52 + 127; // biased exponent of the lowest mantissa bit
-  const float scale = el >= 1 ? __uint_as_float(static_cast<unsigned>(el) << 23) : 0.f;
-  const float l = __uint2float_rn(static_cast<unsigned>(u & 0x1fffffffu)) * scale;
+  const int es = e - 1023 - 23 + 127; // biased exponent of 2^(E-23)
+  const float scale = es >= 1 ? __uint_as_float(static_cast<unsigned>(es) << 23) : 0.f;
+  const float l = (__uint2float_rn(static_cast<unsigned>(u & 0x1fffffffu)) * 0x1p-29f) * scale;
   return quick_two_sum(h, sgn ? -l : l);
 }
 __device__ __forceinline__ F2 two_sum_f(float a, float b) {
@@ -427,6 +432,12 @@ __device__ __forceinline__ T component(int id, T rho, T sigma, const RhoPowers<T
   case kHybB3lyp5:
     return 0.08 * slater(P) + 0.72 * b88(rho, sigma, P) + 0.19 * vwn5(rho, P) +
            0.81 * lyp(rho, sigma, P);
+  case kHybPbeh:
+    return 0.75 * pbe_x(rho, sigma, P) + pbe_c(rho, sigma, P);
+  case kHybBhandh:
+    return 0.5 * slater(P) + lyp(rho, sigma, P);
+  case kHybBhandhlyp:
+    return 0.5 * b88(rho, sigma, P) + lyp(rho, sigma, P);
   }
   return Num<T>::c(0.0);
 }
@@ -474,20 +485,16 @@ __device__ __forceinline__ void eval_xc_mixed(const FuncSet &fs, double rho, dou
   }
 }
 
-// The same with double-float inputs and outputs: no FP64 operation where
-// rho >= 1e-10 and, for a GGA (gga), sigma >= 1e-30 (the mixture
-// coefficients are split by integer operations).
-__device__ __forceinline__ void eval_xc_mixed_f2(const FuncSet &fs, bool gga, fn::F2 rho,
+// The same with double-float inputs and outputs and no FP64 operation
+// (the mixture coefficients are split by integer operations), where
+// rho >= 1e-10 and, for a GGA (gga), sigma >= 1e-30.  Elsewhere it returns
+// false without a result, and the caller evaluates the point with eval_xc on
+// its FP64 inputs (a double-float sigma below FP32's range would be zero).
+__device__ __forceinline__ bool eval_xc_mixed_f2(const FuncSet &fs, bool gga, fn::F2 rho,
                                                  fn::F2 sigma, fn::F2 &e, float &vrho,
                                                  float &vsigma) {
-  if (!(rho.h >= 1e-10f) || (gga && !(sigma.h >= 1e-30f))) {
-    double ed, vr, vs;
-    eval_xc(fs, fn::to_d(rho), fn::to_d(sigma), ed, vr, vs);
-    e = fn::f2(ed);
-    vrho = static_cast<float>(vr);
-    vsigma = static_cast<float>(vs);
-    return;
-  }
+  if (!(rho.h >= 1e-10f) || (gga && !(sigma.h >= 1e-30f)))
+    return false;
   fn::G r{rho, 1.f, 0.f};
   fn::G s{sigma, 0.f, 1.f};
   fn::RhoPowers<fn::G> P = fn::rho_powers(r);
@@ -500,6 +507,7 @@ __device__ __forceinline__ void eval_xc_mixed_f2(const FuncSet &fs, bool gga, fn
     vrho = fmaf(ci.h, c.r, vrho);
     vsigma = fmaf(ci.h, c.s, vsigma);
   }
+  return true;
 }
 
 } // namespace occx

@@ -364,6 +364,17 @@ __device__ __forceinline__ fnp::PD<D> eval_pol_sum(const FuncSet &fs, double ra,
     case kHybB3lyp5:
       c = 0.08 * slater() + 0.72 * b88() + 0.19 * vwn(0) + 0.81 * lyp_pol(S);
       break;
+    case kHybPbeh: {
+      PD<D> x = cst<D>(0.0);
+      if (sa)
+        x = x + pbe_x_s(S.ra, S.saa);
+      if (sb)
+        x = x + pbe_x_s(S.rb, S.sbb);
+      c = 0.75 * x + pbe_c_pol(S);
+      break;
+    }
+    case kHybBhandh: c = 0.5 * slater() + lyp_pol(S); break;
+    case kHybBhandhlyp: c = 0.5 * b88() + lyp_pol(S); break;
     default: break; // meta-GGA components: eval_xc_mgga_pol
     }
     tot = tot + fs.coef[i] * c;

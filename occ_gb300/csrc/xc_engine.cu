@@ -76,6 +76,14 @@ FuncSet parse_method(const std::string &method_in) {
       add(kHybB3lyp);
     } else if (tok == "b3lyp5") {
       add(kHybB3lyp5);
+    } else if (tok == "pbeh" || tok == "hyb_gga_xc_pbeh") {
+      add(kHybPbeh);
+    } else if (tok == "bhandh" || tok == "hyb_gga_xc_bhandh") {
+      add(kHybBhandh);
+    } else if (tok == "bhandhlyp" || tok == "hyb_gga_xc_bhandhlyp") {
+      add(kHybBhandhlyp);
+    } else if (tok == "vwn5") {
+      add(kLdaCVwn);
     } else if (tok == "tpss") {
       add(kMggaXTpss);
       add(kMggaCTpss);

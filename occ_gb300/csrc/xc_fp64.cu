@@ -139,13 +139,51 @@ __global__ void __launch_bounds__(128) k_colloc_f64(MolDev m, double *__restrict
   }
 }
 
+// acc[i][j] += sum_kk A[kk][ta + 16 i] B[kk][tb + 16 j] over one staged
+// chunk, i < NI and j < NJ: a tile's last 32 rows or columns that lie past
+// the leaf's points or AOs are not computed (NI or NJ = 2), which keeps the
+// executed FLOPs near the useful ones for leaves whose sizes are not
+// multiples of 64.
+template <int NI, int NJ, int LDA, int LDB>
+__device__ __forceinline__ void mac_chunk(const double (*As)[LDA], const double (*Bs)[LDB],
+                                          double (&acc)[4][4], int ta, int tb) {
+#pragma unroll
+  for (int kk = 0; kk < kKChunk; kk++) {
+    double a[NI], b[NJ];
+#pragma unroll
+    for (int i = 0; i < NI; i++)
+      a[i] = As[kk][ta + 16 * i];
+#pragma unroll
+    for (int j = 0; j < NJ; j++)
+      b[j] = Bs[kk][tb + 16 * j];
+#pragma unroll
+    for (int i = 0; i < NI; i++)
+#pragma unroll
+      for (int j = 0; j < NJ; j++)
+        acc[i][j] = fma(a[i], b[j], acc[i][j]);
+  }
+}
+template <int LDA, int LDB>
+__device__ __forceinline__ void mac_chunk_n(const double (*As)[LDA], const double (*Bs)[LDB],
+                                            double (&acc)[4][4], int ta, int tb, bool full_i,
+                                            bool full_j) {
+  if (full_i && full_j)
+    mac_chunk<4, 4>(As, Bs, acc, ta, tb);
+  else if (full_i)
+    mac_chunk<4, 2>(As, Bs, acc, ta, tb);
+  else if (full_j)
+    mac_chunk<2, 4>(As, Bs, acc, ta, tb);
+  else
+    mac_chunk<2, 2>(As, Bs, acc, ta, tb);
+}
+
 // rho for one 64-point slab of one leaf.  Thread (tx, ty): points
 // p0 + tx + 16 i, AOs j0 + ty + 16 jj.
 // TAU (meta-GGA, grid.y = 3): the same GEMM on the derivative plane
 // k = 1 + blockIdx.y, (d_k phi) D2 (d_k phi) into rho component 4 + blockIdx.y
 // (tau = half their sum, src/gto/density.cpp:86-100).
 template <bool DERIV, bool TAU = false>
-__global__ void __launch_bounds__(256) k_rho_f64(MolDev m, const double *__restrict__ D,
+__global__ void __launch_bounds__(256, 2) k_rho_f64(MolDev m, const double *__restrict__ D,
                                                  const double *__restrict__ ws,
                                                  const SlabItem *__restrict__ slabs,
                                                  double *__restrict__ rho) {
@@ -167,7 +205,11 @@ __global__ void __launch_bounds__(256) k_rho_f64(MolDev m, const double *__restr
     for (int i = 0; i < 4; i++)
       part[c][i] = 0.0;
 
+  // a slab with at most 32 points, a last AO tile with at most 32 AOs:
+  // their upper halves are not computed
+  const bool full_i = L.cnt - it.p0 > 32;
   for (int j0 = 0; j0 < L.mpad; j0 += kAoTile) {
+    const bool full_j = L.nbf - j0 > 32;
     double acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; i++)
@@ -191,21 +233,7 @@ __global__ void __launch_bounds__(256) k_rho_f64(MolDev m, const double *__restr
         Bs[kb][jb] = dv;
       }
       __syncthreads();
-#pragma unroll
-      for (int kk = 0; kk < kKChunk; kk++) {
-        double a[4], b[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-          a[i] = As[kk][tx + 16 * i];
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-          b[j] = Bs[kk][ty + 16 * j];
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-#pragma unroll
-          for (int j = 0; j < 4; j++)
-            acc[i][j] = fma(a[i], b[j], acc[i][j]);
-      }
+      mac_chunk_n<kPtTile, kAoTile>(As, Bs, acc, tx, ty, full_i, full_j);
       __syncthreads();
     }
 #pragma unroll
@@ -306,6 +334,9 @@ __global__ void __launch_bounds__(256) k_vxc_f64(MolDev m, const double *__restr
     for (int b = 0; b < 4; b++)
       acc[a][b] = 0.0;
   constexpr int NSEG = META ? 4 : 1;
+  // a last AO tile with at most 32 rows or columns: its upper half is not
+  // computed
+  const bool full_i = L.nbf - it.i0 > 32, full_j = L.nbf - it.j0 > 32;
   for (int seg = 0; seg < NSEG; seg++)
   for (int p0 = 0; p0 < (L.cnt + kKChunk - 1) / kKChunk * kKChunk; p0 += kKChunk) {
 #pragma unroll
@@ -331,21 +362,7 @@ __global__ void __launch_bounds__(256) k_vxc_f64(MolDev m, const double *__restr
       Bs[pp][aa] = y;
     }
     __syncthreads();
-#pragma unroll
-    for (int pp = 0; pp < kKChunk; pp++) {
-      double a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-        a[i] = As[pp][ty + 16 * i];
-#pragma unroll
-      for (int j = 0; j < 4; j++)
-        b[j] = Bs[pp][tx + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-          acc[i][j] = fma(a[i], b[j], acc[i][j]);
-    }
+    mac_chunk_n<kAoTile + 1, kAoTile + 1>(As, Bs, acc, ty, tx, full_i, full_j);
     __syncthreads();
   }
   const int *g = m.leaf_ao + L.ao_begin;

@@ -140,8 +140,9 @@ __device__ __forceinline__ long long leaf_max_bits(long long v, long long *sh) {
 }
 
 // The tensor-core build's functional stage in double-float arithmetic, with
-// no FP64 operation per point (the FP64 inputs are split by integer
-// operations, fn::f2_bits; eval_xc_mixed_f2): the skip, weights and
+// no FP64 operation per point where rho >= 1e-10 and sigma >= 1e-30 (the
+// FP64 inputs are split by integer operations, fn::f2_bits;
+// eval_xc_mixed_f2; the FP64 evaluator elsewhere): the skip, weights and
 // coefficients of leaf_functional<.., MIXED>, the coefficients as FP32 into
 // cf[p] for p < npad (zero past the leaf's points; no FP64 coefficient
 // array), E and the electron count summed in double-float and written as
@@ -174,7 +175,18 @@ __device__ __forceinline__ void leaf_functional_f2(const DevLeaf &L, const Pt4 *
       if (!skip) {
         fn::F2 e;
         float vr, vs;
-        eval_xc_mixed_f2(fs, DERIV, r, sigma, e, vr, vs);
+        if (!eval_xc_mixed_f2(fs, DERIV, r, sigma, e, vr, vs)) {
+          // low density or gradient: FP64 on the FP64 inputs
+          double sd = 0.0, ed, vrd, vsd;
+          if (DERIV) {
+            const double dx = rho[N + idx], dy = rho[2 * N + idx], dz = rho[3 * N + idx];
+            sd = dx * dx + dy * dy + dz * dz;
+          }
+          eval_xc(fs, rho[idx], sd, ed, vrd, vsd);
+          e = fn::f2(ed);
+          vr = static_cast<float>(vrd);
+          vs = static_cast<float>(vsd);
+        }
         c.x = 0.5f * w.h * vr;
         if (DERIV) {
           const float f = 2.f * w.h * vs;

@@ -1157,6 +1157,12 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 //                it from 1.02 to 0.90 ms at 32 waters)
 //   warp 9       MMA issuer: hi*hi + hi*lo + lo*hi ("3xTF32") into one of two
 //                TMEM accumulators of 256 columns
+//   warps 10-13  (split mode) the TF32 split: the producer copies each
+//                operand once, as its FP32 plane, into the hi slot; these
+//                warps split every word in place into hi and the lo slot
+//                (elementwise, so the swizzle does not matter) and release
+//                the stage to the MMA issuer.  Half the operand bytes of
+//                pre-split hi / lo planes.
 //   warps 0-7    epilogue (two warps per TMEM lane quarter, each half of the
 //                columns): TMEM -> FP64 atomics, coalesced along the rows,
 //                into A with V_xc = A + A^T.  (Forming K^T beside K to add
@@ -1168,11 +1174,13 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 // the error flag is set and all roles leave.
 constexpr int kItemBlocks = 2;   // blocks of a leaf accumulated in one V item
 constexpr int kVxcEpi = 256;     // epilogue threads (warps 0-7)
-constexpr int kVxcThreads = 320; // + producer warp + MMA warp
+constexpr int kVxcConv = 128;    // split threads (warps 10-13)
+constexpr int kVxcThreads = 448; // + producer warp + MMA warp + split warps
 constexpr int kVxcMap = 2048;    // AO maps up to this size are staged in shared memory
 
 struct alignas(16) VxcSmem {
   uint64_t full[2], empty[2];   // per stage: TMA landed, MMAs done
+  uint64_t conv[2];             // per stage: split done (split mode)
   uint64_t tfull[2], tempty[2]; // per accumulator: ready, drained
   uint64_t ifull[kRing], iempty[kRing];
   uint64_t done;                // the MMA thread's final commit
@@ -1183,16 +1191,20 @@ struct alignas(16) VxcSmem {
 constexpr uint32_t kVxcSmem = 2 * kStageBytes + sizeof(VxcSmem) + 1024;
 
 // Operand planes of k_vxc_tma: K = sum over npairs of (A pair)^T (B pair),
-// each operand as its (hi, lo) TF32 planes.  The build: one pair (phi, Y);
-// the XC gradient: two pairs (d_c phi, Y) and (Z_c, phi).  Scalar fields,
-// selected without indexing, so that the parameters stay in the constant
-// bank.
+// each operand as its (hi, lo) TF32 planes, or (split != 0) as one FP32
+// plane (the *_hi fields; the *_lo fields unused) split in shared memory.
+// The restricted build: one pair (phi, Y), split; the unrestricted build
+// one pre-split pair per spin; the XC gradient: two pairs (d_c phi, Y) and
+// (Z_c, phi).  Scalar fields, selected without indexing, so that the
+// parameters stay in the constant bank.
 struct VxcPlanes {
   int a_hi0, a_lo0, b_hi0, b_lo0, a_hi1, a_lo1, b_hi1, b_lo1;
-  int npairs;
+  int npairs, split;
 };
 constexpr VxcPlanes kVxcBuildPlanes{kPlanePhiHi, kPlanePhiLo, kPlaneYHi, kPlaneYLo, 0, 0, 0, 0,
-                                    1};
+                                    1, 0};
+// phi (FP32, plane 0) and Y (FP32 in the Y hi plane, written by k_func_f2)
+constexpr VxcPlanes kVxcSplitPlanes{0, 0, kPlaneYHi, 0, 0, 0, 0, 0, 1, 1};
 
 struct VxcWork { // what every role derives from an item
   int mp, rows_a, nblk, i0, nbf_leaf;
@@ -1224,6 +1236,35 @@ __device__ __forceinline__ bool epi_all(bool v) {
                : "memory");
   return r != 0;
 }
+// The same over the split threads (named barrier 2).
+__device__ __forceinline__ bool conv_all(bool v) {
+  uint32_t r;
+  asm volatile("{\n\t.reg .pred p, q;\n\t"
+               "setp.ne.u32 p, %1, 0;\n\t"
+               "barrier.red.and.pred q, 2, %2, p;\n\t"
+               "selp.u32 %0, 1, 0, q;\n\t}"
+               : "=r"(r)
+               : "r"(static_cast<uint32_t>(v)), "n"(kVxcConv)
+               : "memory");
+  return r != 0;
+}
+// Split n16 16-byte words at hi in place into TF32 hi and their remainders
+// (TF32) at lo, by the split threads (ct = 0 .. kVxcConv - 1).
+__device__ __forceinline__ void split_words(uint8_t *hi, uint8_t *lo, int n16, int ct) {
+  float4 *h4 = reinterpret_cast<float4 *>(hi);
+  float4 *l4 = reinterpret_cast<float4 *>(lo);
+#pragma unroll 4
+  for (int q = ct; q < n16; q += kVxcConv) {
+    const float4 v = h4[q];
+    float4 h, l;
+    tf32_split(v.x, h.x, l.x);
+    tf32_split(v.y, h.y, l.y);
+    tf32_split(v.z, h.z, l.z);
+    tf32_split(v.w, h.w, l.w);
+    h4[q] = h;
+    l4[q] = l;
+  }
+}
 
 // The FP64 value of FP32 bits by integer operations (rebias the exponent,
 // widen the mantissa), off the FP64 pipe, which GB300 has little of and
@@ -1251,12 +1292,13 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     for (int s = 0; s < 2; s++) {
       umma::mbar_init(&sm->full[s], 1);
       umma::mbar_init(&sm->empty[s], 1);
+      umma::mbar_init(&sm->conv[s], kVxcConv);
       umma::mbar_init(&sm->tfull[s], 1);
       umma::mbar_init(&sm->tempty[s], kVxcEpi);
     }
     for (int r = 0; r < kRing; r++) {
       umma::mbar_init(&sm->ifull[r], 1);
-      umma::mbar_init(&sm->iempty[r], 1 + kVxcEpi);
+      umma::mbar_init(&sm->iempty[r], 1 + kVxcEpi + (pl.split ? kVxcConv : 0));
     }
     umma::mbar_init(&sm->done, 1);
     umma::fence_proxy_async();
@@ -1278,12 +1320,15 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     }
     return ok;
   };
-  // the epilogue warps issue warp-collective TMEM loads and share barriers:
-  // all of their threads take every decision to stop together
-  const bool epi = warp < 8;
+  // the epilogue warps issue warp-collective TMEM loads and share barriers,
+  // the split warps share a barrier: all threads of either group take every
+  // decision to stop together
+  const bool epi = warp < 8, cv = warp >= 10;
   auto agree = [&] {
     if (epi)
       ok = epi_all(ok);
+    else if (cv)
+      ok = conv_all(ok);
     return ok;
   };
   // consumer side of the item ring: next item index or -1
@@ -1327,8 +1372,8 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
               const int s = g & 1;
               if (g >= 2 && !wait(&sm->empty[s], ((g >> 1) - 1) & 1))
                 break;
-              umma::mbar_arrive_expect_tx(&sm->full[s],
-                                          static_cast<uint32_t>(W.rows_a + N) * 256u);
+              umma::mbar_arrive_expect_tx(&sm->full[s], static_cast<uint32_t>(W.rows_a + N) *
+                                                            (pl.split ? 128u : 256u));
               uint8_t *st = stage[s];
               const int ah = pr ? pl.a_hi1 : pl.a_hi0, al = pr ? pl.a_lo1 : pl.a_lo0;
               const int bh = pr ? pl.b_hi1 : pl.b_hi0, bl = pr ? pl.b_lo1 : pl.b_lo0;
@@ -1338,8 +1383,9 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
                 const CUtensorMap *mp_ = big ? &tmap128 : &tmap;
                 umma::tma_load_2d(st + kOffAhi + r * 128, mp_, c * kKc,
                                   r0 + ah * mp + W.i0 + r, &sm->full[s]);
-                umma::tma_load_2d(st + kOffAlo + r * 128, mp_, c * kKc,
-                                  r0 + al * mp + W.i0 + r, &sm->full[s]);
+                if (!pl.split)
+                  umma::tma_load_2d(st + kOffAlo + r * 128, mp_, c * kKc,
+                                    r0 + al * mp + W.i0 + r, &sm->full[s]);
                 r += big ? 128 : 32;
               }
               for (int r = 0; r < N;) {
@@ -1347,8 +1393,9 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
                 const CUtensorMap *mp_ = big ? &tmap128 : &tmap;
                 umma::tma_load_2d(st + kOffBhi + r * 128, mp_, c * kKc,
                                   r0 + bh * mp + n0 + r, &sm->full[s]);
-                umma::tma_load_2d(st + kOffBlo + r * 128, mp_, c * kKc,
-                                  r0 + bl * mp + n0 + r, &sm->full[s]);
+                if (!pl.split)
+                  umma::tma_load_2d(st + kOffBlo + r * 128, mp_, c * kKc,
+                                    r0 + bl * mp + n0 + r, &sm->full[s]);
                 r += big ? 128 : 32;
               }
             }
@@ -1385,7 +1432,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
           const int nch = pl.npairs * W.nblk * (kBlockPts / kKc);
           for (int c = 0; c < nch && ok; c++, g++) {
             const int s = g & 1;
-            if (!wait(&sm->full[s], (g >> 1) & 1))
+            if (!wait(pl.split ? &sm->conv[s] : &sm->full[s], (g >> 1) & 1))
               break;
             umma::fence_after_sync();
             const uint32_t base = umma::smem_u32(stage[s]);
@@ -1410,6 +1457,35 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       if (issued) { // every MMA done before TMEM is released
         umma::commit(&sm->done);
         umma::mbar_wait(&sm->done, 0, kWaitIter);
+      }
+    }
+  } else if (cv) {
+    // ---- TF32 split (warps 10-13), split mode only ----
+    if (pl.split) {
+      const int ct = t - 10 * 32;
+      uint32_t g = 0; // chunks split
+      for (int k = 0; ok; k++) {
+        const int it = next_item(k);
+        if (it < 0)
+          break;
+        const VItem I = items[it];
+        const VxcWork W = vxc_work(tabs, blocks, I);
+        const int NT = tabs[blocks[I.block0].mol].vxc_n;
+        for (int n0 = 0; n0 < W.mp && ok; n0 += NT) {
+          const int N = min(NT, W.mp - n0);
+          const int nch = pl.npairs * W.nblk * (kBlockPts / kKc);
+          for (int c = 0; c < nch; c++, g++) {
+            const int s = g & 1;
+            wait(&sm->full[s], (g >> 1) & 1);
+            if (!agree())
+              break;
+            uint8_t *st = stage[s];
+            split_words(st + kOffAhi, st + kOffAlo, W.rows_a * 8, ct);
+            split_words(st + kOffBhi, st + kOffBlo, N * 8, ct);
+            umma::fence_proxy_async(); // generic-proxy writes, read by the MMAs
+            umma::mbar_arrive(&sm->conv[s]);
+          }
+        }
       }
     }
   } else {
@@ -1481,8 +1557,9 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
 
 // The B operand of k_vxc_tma for one block, pre-split for 3xTF32 (tf32_split):
 // Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi (FP32) into the Y hi / lo
-// planes; streams 4 planes in, 2 out.  Run by a whole CTA; cf holds 128 float4.
-template <bool DERIV>
+// planes; streams 4 planes in, 2 out.  RAW: Y as FP32 into the Y hi plane
+// only, for k_vxc_tma's split mode.  Run by a whole CTA; cf holds 128 float4.
+template <bool DERIV, bool RAW = false>
 __device__ __forceinline__ void ymix_block(const MixTab &T, const MBlock &B, float4 *cf) {
   if (threadIdx.x < kBlockPts) {
     const int p = threadIdx.x;
@@ -1525,10 +1602,14 @@ __device__ __forceinline__ void ymix_block(const MixTab &T, const MBlock &B, flo
       y.z = fmaf(gz.z, cf[p + 2].w, fmaf(gy.z, cf[p + 2].z, fmaf(gx.z, cf[p + 2].y, y.z)));
       y.w = fmaf(gz.w, cf[p + 3].w, fmaf(gy.w, cf[p + 3].z, fmaf(gx.w, cf[p + 3].y, y.w)));
     }
-    float4 yh, yl;
-    split4(y, yh, yl);
-    base[kPlaneYHi * plane + q] = yh;
-    base[kPlaneYLo * plane + q] = yl;
+    if (RAW) {
+      base[kPlaneYHi * plane + q] = y;
+    } else {
+      float4 yh, yl;
+      split4(y, yh, yl);
+      base[kPlaneYHi * plane + q] = yh;
+      base[kPlaneYLo * plane + q] = yl;
+    }
   }
   __syncthreads(); // cf is reused by the next block
 }
@@ -1556,7 +1637,7 @@ __device__ __forceinline__ double bsum256(double v, double *sh) {
 // block (a CTA of 256 left half of its threads idle in the functional, with
 // eight active warps an SM).
 constexpr int kFuncThreads = 128;
-template <bool DERIV>
+template <bool DERIV, bool RAW = false>
 __global__ void __launch_bounds__(kFuncThreads, 4) k_func_b(const MixTab *__restrict__ tabs,
                                                          const MBlock *__restrict__ blocks,
                                                          const LeafItem *__restrict__ litems) {
@@ -1569,13 +1650,14 @@ __global__ void __launch_bounds__(kFuncThreads, 4) k_func_b(const MixTab *__rest
                                              T.rho, T.coef, T.epart + 2 * li.leaf, sh);
   __syncthreads(); // the leaf's coefficients are written
   for (int b = 0; b < li.nblk; b++)
-    ymix_block<DERIV>(T, blocks[li.block0 + b], cf);
+    ymix_block<DERIV, RAW>(T, blocks[li.block0 + b], cf);
 }
 
 constexpr int kLeafMaxPts = 1024; // leaf_max's bound (check_build_settings)
 
-// Y hi / lo of one block from the coefficients cf[0 .. 127] (FP32), by the
-// NS threads tid = 0 .. NS - 1.
+// Y of one block from the coefficients cf[0 .. 127] (FP32) into the Y hi
+// plane as FP32 (k_vxc_tma splits it in shared memory), by the NS threads
+// tid = 0 .. NS - 1.
 template <bool DERIV, int NS>
 __device__ __forceinline__ void ymix_stream(const MixTab &T, const MBlock &B,
                                             const float4 *__restrict__ cf, int tid) {
@@ -1599,21 +1681,16 @@ __device__ __forceinline__ void ymix_stream(const MixTab &T, const MBlock &B,
       y.z = fmaf(gz.z, c2.w, fmaf(gy.z, c2.z, fmaf(gx.z, c2.y, y.z)));
       y.w = fmaf(gz.w, c3.w, fmaf(gy.w, c3.z, fmaf(gx.w, c3.y, y.w)));
     }
-    float4 yh, yl;
-    tf32_split(y.x, yh.x, yl.x);
-    tf32_split(y.y, yh.y, yl.y);
-    tf32_split(y.z, yh.z, yl.z);
-    tf32_split(y.w, yh.w, yl.w);
-    base[kPlaneYHi * plane + q] = yh;
-    base[kPlaneYLo * plane + q] = yl;
+    base[kPlaneYHi * plane + q] = y;
   }
 }
 
 // The build's functional stage (one CTA per leaf item, four per SM): the
 // functional in double-float arithmetic (leaf_functional_f2, no FP64
 // operation per point) with the coefficients as FP32 into shared memory, then
-// the V_xc operand Y of each of the leaf's blocks from them (ymix_stream).
-// The FP64 coefficient array is not written.
+// the V_xc operand Y of each of the leaf's blocks from them (ymix_stream, one
+// FP32 plane: k_vxc_tma's split mode forms hi and lo).  The FP64 coefficient
+// array is not written.
 template <bool DERIV>
 __global__ void __launch_bounds__(kFuncThreads, 4) k_func_f2(const MixTab *__restrict__ tabs,
                                                           const MBlock *__restrict__ blocks,
@@ -1971,7 +2048,7 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
     c.launch("vxc_mixed", st, [&] {
       const int g = std::min(ni, ctas);
       k_vxc_tma<<<g, kVxcThreads, kVxcSmem, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov, P.d_queue, err,
-                                          P.tmap.rows32, P.tmap.rows128, kVxcBuildPlanes);
+                                          P.tmap.rows32, P.tmap.rows128, kVxcSplitPlanes);
     });
   c.launch("symmetrize", st, [&] {
     const size_t n2 = static_cast<size_t>(P.maxnbf) * P.maxnbf;
@@ -2750,10 +2827,11 @@ __global__ void k_selftest_func(FuncSet fs, int n, const double *rho, const doub
       gga = gga || func_is_gga(fs.id[k]);
     fn::F2 ef;
     float vrf, vsf;
-    eval_xc_mixed_f2(fs, gga, fn::f2_bits(rho[i]), fn::f2_bits(sigma[i]), ef, vrf, vsf);
-    e = fn::to_d(ef);
-    vr = vrf;
-    vs = vsf;
+    if (eval_xc_mixed_f2(fs, gga, fn::f2_bits(rho[i]), fn::f2_bits(sigma[i]), ef, vrf, vsf)) {
+      e = fn::to_d(ef);
+      vr = vrf;
+      vs = vsf;
+    } // else: FP64 on the FP64 inputs, e, vr, vs as above
   } else {
     eval_xc_mixed(fs, rho[i], sigma[i], e, vr, vs);
   }
@@ -2919,14 +2997,16 @@ int selftest_functional(occ_xc_context *ctx, const char *method, int n, const do
 // (src/dft/dft_gradient_kernels.cpp:472-595): the three G_c are the V_xc
 // kernel's K with two operand pairs each, accumulated over the leaves into
 // nbf x nbf FP64 matrices, then contracted with D.  The blocks carry, beside
-// the build's eleven planes, the hi and lo TF32 planes of d_c phi and of
+// the build's eleven planes, the FP32 planes of
 //   Z_c = 0.5 w vrho d_c phi + 2 w vsigma grad rho . grad d_c phi
-// (k_grad_ops, with the AO second derivatives in FP32).
+// (k_grad_ops, with the AO second derivatives in FP32); the pairs
+// (d_c phi, Y) and (Z_c, phi) are read as FP32 planes (d_c phi and phi the
+// collocation's, Y written unsplit by the functional stage) and split into
+// TF32 hi / lo by the V_xc kernel's split mode.
 namespace occx {
 
-constexpr int kPlanesGrad = 23;
-constexpr int kPlaneDphi = 11; // hi, lo of d_c phi: planes 11 + 2c, 12 + 2c
-constexpr int kPlaneZ = 17;    // hi, lo of Z_c: planes 17 + 2c, 18 + 2c
+constexpr int kPlanesGrad = 14;
+constexpr int kPlaneZ = 11; // Z_c as FP32: planes 11 + c (d_c phi: the collocation's 1 + c)
 
 namespace {
 
@@ -3028,13 +3108,7 @@ __device__ __forceinline__ void grad_ops_shell(bool pure, float x, float y, floa
     for (int cc = 0; cc < 3; cc++) {
       const float dphi = out[(1 + cc) * plane + o];
       const float zc = fmaf(c0, dphi, zh[cc]);
-      float h, l;
-      tf32_split(valid ? dphi : 0.f, h, l);
-      out[(kPlaneDphi + 2 * cc) * plane + o] = h;
-      out[(kPlaneDphi + 2 * cc + 1) * plane + o] = l;
-      tf32_split(valid ? zc : 0.f, h, l);
-      out[(kPlaneZ + 2 * cc) * plane + o] = h;
-      out[(kPlaneZ + 2 * cc + 1) * plane + o] = l;
+      out[(kPlaneZ + cc) * plane + o] = valid ? zc : 0.f;
     }
   }
 }
@@ -3113,7 +3187,7 @@ __global__ void __launch_bounds__(128) k_grad_ops(const MixTab *__restrict__ tab
   for (int f = loc; f < B.mp; f++) {
     const size_t o = static_cast<size_t>(f) * kBlockPts + p;
 #pragma unroll
-    for (int q = kPlaneDphi; q < kPlanesGrad; q++)
+    for (int q = kPlaneZ; q < kPlanesGrad; q++)
       base[q * plane + o] = 0.f;
   }
 }
@@ -3233,9 +3307,9 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
   if (nl > 0)
     c.launch("func", st, [&] {
       if (P.deriv)
-        k_func_b<true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_b<true, true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
       else
-        k_func_b<false><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_b<false, true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
     });
   if (nb > 0)
     c.launch("grad_ops", st, [&] {
@@ -3244,9 +3318,8 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
   cuda_check(cudaMemsetAsync(g.G, 0, 3 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
   for (int cc = 0; cc < 3 && ni > 0; cc++) {
     cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
-    const VxcPlanes pl{kPlaneDphi + 2 * cc, kPlaneDphi + 2 * cc + 1, kPlaneYHi, kPlaneYLo,
-                       kPlaneZ + 2 * cc,    kPlaneZ + 2 * cc + 1,    kPlanePhiHi, kPlanePhiLo,
-                       2};
+    // (d_c phi, Y) and (Z_c, phi), FP32 planes split by the kernel
+    const VxcPlanes pl{1 + cc, 0, kPlaneYHi, 0, kPlaneZ + cc, 0, 0, 0, 2, 1};
     Override ovc{dD, g.G + cc * nbf2, dout2};
     c.launch("grad_vxc", st, [&] {
       k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
@@ -3274,12 +3347,12 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
 // are the restricted build's, in the molecule's private workspace.
 namespace occx {
 namespace {
-template <bool DERIV>
+template <bool DERIV, bool RAW = false>
 __global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
                                              const MBlock *__restrict__ blocks) {
   __shared__ float4 cf[kBlockPts];
   const MBlock B = blocks[blockIdx.x];
-  ymix_block<DERIV>(tabs[B.mol], B, cf);
+  ymix_block<DERIV, RAW>(tabs[B.mol], B, cf);
 }
 } // namespace
 
@@ -3401,9 +3474,9 @@ constexpr int kPlaneMetaY = 26;    // hi, lo of c_tau d_k phi: planes 26 + 2(k-1
 //   (phi, Y) + (d_x phi, c_tau d_x phi),  (d_y phi, c_tau d_y phi) + (d_z phi, c_tau d_z phi)
 constexpr VxcPlanes kMetaVxcPlanes[2] = {
     {kPlanePhiHi, kPlanePhiLo, kPlaneYHi, kPlaneYLo, kPlaneMetaDphi, kPlaneMetaDphi + 1,
-     kPlaneMetaY, kPlaneMetaY + 1, 2},
+     kPlaneMetaY, kPlaneMetaY + 1, 2, 0},
     {kPlaneMetaDphi + 2, kPlaneMetaDphi + 3, kPlaneMetaY + 2, kPlaneMetaY + 3,
-     kPlaneMetaDphi + 4, kPlaneMetaDphi + 5, kPlaneMetaY + 4, kPlaneMetaY + 5, 2}};
+     kPlaneMetaDphi + 4, kPlaneMetaDphi + 5, kPlaneMetaY + 4, kPlaneMetaY + 5, 2, 0}};
 
 struct MetaMixed {
   char *ws = nullptr;
@@ -3763,9 +3836,9 @@ void Molecule::xc_gradient_uks_mixed(const double *dD, double *dgrad, double *do
     const double *Ds = d_Dab + s * nbf2, *Do = d_Dab + (1 - s) * nbf2;
     c.launch("ymix", st, [&] {
       if (P.deriv)
-        k_ymix<true><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
+        k_ymix<true, true><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
       else
-        k_ymix<false><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
+        k_ymix<false, true><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
     });
     c.launch("grad_ops", st, [&] {
       k_grad_ops<<<nb, kBlockPts, 0, st>>>(tabs[s], P.d_blocks, P.deriv);
@@ -3773,9 +3846,7 @@ void Molecule::xc_gradient_uks_mixed(const double *dD, double *dgrad, double *do
     cuda_check(cudaMemsetAsync(g.G, 0, 3 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
     for (int cc = 0; cc < 3 && ni > 0; cc++) {
       cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
-      const VxcPlanes pl{kPlaneDphi + 2 * cc, kPlaneDphi + 2 * cc + 1, kPlaneYHi, kPlaneYLo,
-                         kPlaneZ + 2 * cc,    kPlaneZ + 2 * cc + 1,    kPlanePhiHi, kPlanePhiLo,
-                         2};
+      const VxcPlanes pl{1 + cc, 0, kPlaneYHi, 0, kPlaneZ + cc, 0, 0, 0, 2, 1};
       const Override ovc{Ds, g.G + cc * nbf2, nullptr};
       c.launch("grad_vxc", st, [&] {
         k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(

@@ -27,7 +27,8 @@ _lib = None
 METHODS = {
     "lda": [1, 30], "svwn": [1, 30], "lsda": [1, 30], "svwn5": [1, 7],
     "pbe": [101, 130], "blyp": [106, 131], "bpbe": [106, 130],
-    "b3lyp": [402], "b3lyp5": [475], "tpss": [202, 231],
+    "b3lyp": [402], "b3lyp5": [475], "tpss": [202, 231], "vwn5": [7],
+    "pbeh": [406], "bhandh": [435], "bhandhlyp": [436],
 }
 MGGA_IDS = (202, 231)
 

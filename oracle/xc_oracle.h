@@ -29,6 +29,9 @@ enum {
   ORC_GGA_C_LYP = 131,
   ORC_HYB_GGA_XC_B3LYP = 402,
   ORC_HYB_GGA_XC_B3LYP5 = 475,
+  ORC_HYB_GGA_XC_PBEH = 406,
+  ORC_HYB_GGA_XC_BHANDH = 435,
+  ORC_HYB_GGA_XC_BHANDHLYP = 436,
   ORC_MGGA_X_TPSS = 202,
   ORC_MGGA_C_TPSS = 231,
 };

@@ -157,6 +157,9 @@ bool is_gga(int id) {
   case ORC_GGA_C_LYP:
   case ORC_HYB_GGA_XC_B3LYP:
   case ORC_HYB_GGA_XC_B3LYP5:
+  case ORC_HYB_GGA_XC_PBEH:
+  case ORC_HYB_GGA_XC_BHANDH:
+  case ORC_HYB_GGA_XC_BHANDHLYP:
     return true;
   default:
     return false;
@@ -198,6 +201,14 @@ Dual energy_density(int id, Dual rho, Dual sigma) {
   case ORC_HYB_GGA_XC_B3LYP5: // same mixture with the VWN5 fit
     return 0.08 * slater(rho) + 0.72 * b88(rho, sigma) + 0.19 * vwn5(rho) +
            0.81 * lyp(rho, sigma);
+  // Libxc's hybrid mixtures of OCC's pbeh, bhandh and bhandhlyp (their
+  // Hartree-Fock share is outside the XC build)
+  case ORC_HYB_GGA_XC_PBEH: // 0.75 PBE exchange + PBE correlation
+    return 0.75 * pbe_x(rho, sigma) + pbe_c(rho, sigma);
+  case ORC_HYB_GGA_XC_BHANDH: // 0.5 Slater + LYP
+    return 0.5 * slater(rho) + lyp(rho, sigma);
+  case ORC_HYB_GGA_XC_BHANDHLYP: // 0.5 B88 + LYP
+    return 0.5 * b88(rho, sigma) + lyp(rho, sigma);
   }
   return Dual(0.0);
 }
@@ -389,6 +400,12 @@ Cx pol_energy(int id, const PolPoint &P) {
     return 0.08 * slater() + 0.72 * X(b88_c) + 0.19 * vwn(1) + 0.81 * lyp();
   case ORC_HYB_GGA_XC_B3LYP5:
     return 0.08 * slater() + 0.72 * X(b88_c) + 0.19 * vwn(0) + 0.81 * lyp();
+  case ORC_HYB_GGA_XC_PBEH:
+    return 0.75 * X(pbe_x_c) + pbe_c();
+  case ORC_HYB_GGA_XC_BHANDH:
+    return 0.5 * slater() + lyp();
+  case ORC_HYB_GGA_XC_BHANDHLYP:
+    return 0.5 * X(b88_c) + lyp();
   }
   return 0.0;
 }

@@ -12,7 +12,8 @@ from occ_gb300.xc import _context, _dp, _ptr
 
 pytestmark = pytest.mark.gpu
 
-METHODS = ["lda", "svwn5", "pbe", "blyp", "bpbe", "b3lyp", "b3lyp5"]
+METHODS = ["lda", "svwn5", "pbe", "blyp", "bpbe", "b3lyp", "b3lyp5", "pbeh", "bhandh",
+           "bhandhlyp"]
 
 
 def _points(n, seed):

@@ -24,7 +24,8 @@ def _run(method, basis, D, precision=og.FP64, build=None):
     return dft, V, V_ref, e_ref, n_ref
 
 
-@pytest.mark.parametrize("method", ["lda", "svwn5", "pbe", "blyp", "b3lyp", "b3lyp5", "bpbe"])
+@pytest.mark.parametrize("method", ["lda", "svwn5", "pbe", "blyp", "b3lyp", "b3lyp5", "bpbe",
+                                    "pbeh", "bhandh", "bhandhlyp", "vwn5"])
 @pytest.mark.parametrize("basis_name", ["6-31g", "3-21g"])
 def test_water_fp64(method, basis_name):
     mol, b, D = water_case(basis_name)

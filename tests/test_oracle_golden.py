@@ -157,3 +157,23 @@ def test_oracle_second_derivatives_vs_gau2grid(pure, l):
                              g[key + "_xyz"], deriv=2)
     ref = g[key + "_vals"]
     assert np.max(np.abs(out - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref)))
+
+
+@pytest.mark.parametrize("mid,parts", [(406, [(101, 0.75), (130, 1.0)]),
+                                       (435, [(1, 0.5), (131, 1.0)]),
+                                       (436, [(106, 0.5), (131, 1.0)])])
+def test_oracle_hybrid_mixtures(mid, parts):
+    """Libxc's local parts of the hybrids OCC names pbeh, bhandh and bhandhlyp
+    (hyb_gga_xc_pbeh, _bhandh, _bhandhlyp) are the weighted sums of their
+    components."""
+    rng = np.random.default_rng(5)
+    n = 64
+    rho = 10.0 ** rng.uniform(-6, 2, n)
+    sigma = 10.0 ** rng.uniform(-8, 1, n) * rho ** (8.0 / 3.0)
+    e, vr, vs = oracle.functional(mid, rho, sigma)
+    es = sum(c * oracle.functional(i, rho, sigma)[0] for i, c in parts)
+    vrs = sum(c * oracle.functional(i, rho, sigma)[1] for i, c in parts)
+    vss = sum(c * oracle.functional(i, rho, sigma)[2] for i, c in parts)
+    assert np.allclose(e, es, rtol=1e-14, atol=0)
+    assert np.allclose(vr, vrs, rtol=1e-13, atol=0)
+    assert np.allclose(vs, vss, rtol=1e-13, atol=0)
