@@ -103,6 +103,98 @@ __device__ __forceinline__ void boys(int nmax, double T, double *F) {
   }
 }
 
+// 1 / (2 i + 1), i = 0 .. kBoysTable - 1: the Boys series and recursions
+// multiply by these instead of dividing (GB300's FP64 divisions are slow).
+constexpr int kBoysTable = 272;
+__constant__ double c_inv_odd[kBoysTable];
+
+// boys() with compile-time nmax and the reciprocal table: for T < 36 the
+// series at nmax and downward recursion; beyond, the asymptotic F_0 and
+// upward recursion.  Equal to boys() to rounding.
+template <int NMAX> __device__ __forceinline__ void boys_t(double T, double (&F)[NMAX + 1]) {
+  const double et = exp(-T);
+  const double t2 = 2.0 * T;
+  if (T < 36.0) {
+    double term = c_inv_odd[NMAX], sum = term;
+    for (int k = 1; k < kBoysTable - NMAX; k++) {
+      term *= t2 * c_inv_odd[NMAX + k];
+      sum += term;
+      if (term < 1e-17 * sum)
+        break;
+    }
+    F[NMAX] = et * sum;
+#pragma unroll
+    for (int n = NMAX; n > 0; n--)
+      F[n - 1] = fma(t2, F[n], et) * c_inv_odd[n - 1];
+  } else {
+    F[0] = 0.5 * sqrt(kPi / T);
+    const double it2 = 1.0 / t2;
+#pragma unroll
+    for (int n = 0; n < NMAX; n++)
+      F[n + 1] = ((2 * n + 1) * F[n] - et) * it2;
+  }
+}
+
+// Index of R_tuv in a level array of degree <= S: as r_index.
+// R_tuv^(0), t + u + v <= L (compile time), all in registers: the same
+// recursion as hermite_r.
+template <int L>
+__device__ __forceinline__ void hermite_r_t(double p, double X, double Y, double Z,
+                                            double (&R)[(L + 1) * (L + 2) * (L + 3) / 6]) {
+  constexpr int NR = (L + 1) * (L + 2) * (L + 3) / 6;
+  double F[L + 1];
+  boys_t<L>(p * (X * X + Y * Y + Z * Z), F);
+  double up[NR], cur[NR];
+  double m2p[L + 1];
+  m2p[0] = 1.0;
+#pragma unroll
+  for (int n = 1; n <= L; n++)
+    m2p[n] = m2p[n - 1] * (-2.0 * p);
+#pragma unroll
+  for (int n = L; n >= 0; n--) {
+#pragma unroll
+    for (int sdeg = 0; sdeg <= L - n; sdeg++)
+#pragma unroll
+      for (int t = sdeg; t >= 0; t--)
+#pragma unroll
+        for (int u = sdeg - t; u >= 0; u--) {
+          const int v = sdeg - t - u;
+          double val;
+          if (sdeg == 0)
+            val = m2p[n] * F[n];
+          else if (t > 0)
+            val = (t > 1 ? (t - 1) * up[r_index(t > 1 ? t - 2 : 0, u, v)] : 0.0) +
+                  X * up[r_index(t - 1, u, v)];
+          else if (u > 0)
+            val = (u > 1 ? (u - 1) * up[r_index(t, u > 1 ? u - 2 : 0, v)] : 0.0) +
+                  Y * up[r_index(t, u - 1, v)];
+          else
+            val = (v > 1 ? (v - 1) * up[r_index(t, u, v > 1 ? v - 2 : 0)] : 0.0) +
+                  Z * up[r_index(t, u, v - 1)];
+          cur[r_index(t, u, v)] = val;
+        }
+#pragma unroll
+    for (int i = 0; i < NR; i++)
+      up[i] = cur[i];
+  }
+#pragma unroll
+  for (int i = 0; i < NR; i++)
+    R[i] = up[i];
+}
+
+// Cartesian power of component i (CCA order) of a shell of angular momentum
+// l along axis (0 x, 1 y, 2 z).
+__host__ __device__ constexpr int cca_pow(int l, int i, int axis) {
+  int k = 0;
+  for (int a = l; a >= 0; a--)
+    for (int b = l - a; b >= 0; b--) {
+      if (k == i)
+        return axis == 0 ? a : (axis == 1 ? b : l - a - b);
+      k++;
+    }
+  return 0;
+}
+
 // R_tuv^(0), t + u + v <= L, for exponent p and PC = P - C (McMurchie-
 // Davidson recursion from R^(n)_000 = (-2p)^n F_n, level by level).
 __device__ __forceinline__ void hermite_r(int L, double p, double X, double Y, double Z,
@@ -195,9 +287,122 @@ __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restri
   }
 }
 
+// One kept shell pair (angular momenta LA, LB at compile time, so that the
+// Hermite integrals, the ESP block and the transforms stay in registers) at
+// one point C: V_g(mu, nu) = sum over primitive pairs of pref sum_tuv
+// E^x_t E^y_u E^z_v R_tuv, then G[:, q] -= F[:, p] V and, for p != q,
+// G[:, p] -= F[:, q] V^T, through the shells' solid-harmonic transforms
+// when pure.
+template <int LA, int LB>
+__device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restrict__ prims,
+                                          const double *__restrict__ etab, const Pt4 &C, bool pure,
+                                          const double *__restrict__ Fg, double *__restrict__ Gg) {
+  constexpr int NCA = (LA + 1) * (LA + 2) / 2, NCB = (LB + 1) * (LB + 2) / 2;
+  constexpr int L2 = LA + LB, NA = LA + 1, NB = LB + 1, NT = L2 + 1;
+  constexpr int NR = (L2 + 1) * (L2 + 2) * (L2 + 3) / 6;
+  double V[NCA][NCB];
+#pragma unroll
+  for (int i = 0; i < NCA; i++)
+#pragma unroll
+    for (int j = 0; j < NCB; j++)
+      V[i][j] = 0.0;
+  for (int r = 0; r < P.nprim; r++) {
+    const CxPrim Q = prims[P.prim0 + r];
+    double R[NR];
+    hermite_r_t<L2>(Q.pexp, Q.P[0] - C.x, Q.P[1] - C.y, Q.P[2] - C.z, R);
+    const double *Ex = etab + Q.e_off, *Ey = Ex + NA * NB * NT, *Ez = Ey + NA * NB * NT;
+#pragma unroll
+    for (int i = 0; i < NCA; i++) {
+      const int ax = cca_pow(LA, i, 0), ay = cca_pow(LA, i, 1), az = cca_pow(LA, i, 2);
+#pragma unroll
+      for (int j = 0; j < NCB; j++) {
+        const int bx = cca_pow(LB, j, 0), by = cca_pow(LB, j, 1), bz = cca_pow(LB, j, 2);
+        const double *ex = Ex + (ax * NB + bx) * NT, *ey = Ey + (ay * NB + by) * NT,
+                     *ez = Ez + (az * NB + bz) * NT;
+        double acc = 0.0;
+        // compile-time trip counts (L2) with the exponent bounds as guards,
+        // so that every R index is a constant and R stays in registers
+#pragma unroll
+        for (int t = 0; t <= L2; t++)
+#pragma unroll
+          for (int u = 0; u <= L2 - t; u++) {
+            if (t > ax + bx || u > ay + by)
+              continue;
+            const double exy = ex[t] * ey[u];
+#pragma unroll
+            for (int v = 0; v <= L2 - t - u; v++)
+              if (v <= az + bz)
+                acc = fma(exy * ez[v], R[r_index(t, u, v)], acc);
+          }
+        V[i][j] = fma(Q.pref, acc, V[i][j]);
+      }
+    }
+  }
+  // the shells' functions: NFA / NFB of them, pure (2l + 1) or Cartesian
+  const int nfa = pure ? 2 * LA + 1 : NCA, nfb = pure ? 2 * LB + 1 : NCB;
+  auto ta = [&](int f, int i) { return pure ? c_cx_T[LA][f < 5 ? f : 4][i] : (f == i ? 1.0 : 0.0); };
+  auto tb = [&](int h, int j) { return pure ? c_cx_T[LB][h < 5 ? h : 4][j] : (h == j ? 1.0 : 0.0); };
+  double Fc[NCA], Gc[NCB];
+#pragma unroll
+  for (int i = 0; i < NCA; i++) {
+    double s = 0.0;
+#pragma unroll
+    for (int f = 0; f < NCA; f++)
+      if (f < nfa)
+        s = fma(Fg[P.bf_p + f], ta(f, i), s);
+    Fc[i] = s;
+  }
+#pragma unroll
+  for (int j = 0; j < NCB; j++) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < NCA; i++)
+      s = fma(Fc[i], V[i][j], s);
+    Gc[j] = s;
+  }
+#pragma unroll
+  for (int h = 0; h < NCB; h++)
+    if (h < nfb) {
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < NCB; j++)
+        s = fma(tb(h, j), Gc[j], s);
+      Gg[P.bf_q + h] -= s;
+    }
+  if (P.bf_p != P.bf_q) {
+    double Fq[NCB], Gp[NCA];
+#pragma unroll
+    for (int j = 0; j < NCB; j++) {
+      double s = 0.0;
+#pragma unroll
+      for (int h = 0; h < NCB; h++)
+        if (h < nfb)
+          s = fma(Fg[P.bf_q + h], tb(h, j), s);
+      Fq[j] = s;
+    }
+#pragma unroll
+    for (int i = 0; i < NCA; i++) {
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < NCB; j++)
+        s = fma(V[i][j], Fq[j], s);
+      Gp[i] = s;
+    }
+#pragma unroll
+    for (int f = 0; f < NCA; f++)
+      if (f < nfa) {
+        double s = 0.0;
+#pragma unroll
+        for (int i = 0; i < NCA; i++)
+          s = fma(ta(f, i), Gp[i], s);
+        Gg[P.bf_p + f] -= s;
+      }
+  }
+}
+
 // G[g, :] of one point g: every kept shell pair's ESP block V_g and its
 // two updates.
-__device__ __noinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int p, int off0,
+__device__ __forceinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int p, int off0,
                                           int npairs, const CxPair *__restrict__ pairs,
                                           const CxPrim *__restrict__ prims,
                                           const double *__restrict__ etab,
@@ -217,84 +422,22 @@ __device__ __noinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int
       if (sqrt(dx * dx + dy * dy + dz * dz) - P.ext >= geo.w + kCosxMargin)
         continue;
     }
-    const int ncp = (P.la + 1) * (P.la + 2) / 2, ncq = (P.lb + 1) * (P.lb + 2) / 2;
-    const int L2 = P.la + P.lb;
-    double V[kCosxNc][kCosxNc];
-    for (int i = 0; i < ncp; i++)
-      for (int j = 0; j < ncq; j++)
-        V[i][j] = 0.0;
-    for (int r = 0; r < P.nprim; r++) {
-      const CxPrim Q = prims[P.prim0 + r];
-      double R[kCosxR];
-      hermite_r(L2, Q.pexp, Q.P[0] - C.x, Q.P[1] - C.y, Q.P[2] - C.z, R);
-      const int na = P.la + 1, nb = P.lb + 1, nt = L2 + 1;
-      const double *Ex = etab + Q.e_off, *Ey = Ex + na * nb * nt, *Ez = Ey + na * nb * nt;
-      for (int i = 0; i < ncp; i++) {
-        const int ci = c_cx_comp[P.la][i];
-        const int ax = ci & 15, ay = (ci >> 4) & 15, az = ci >> 8;
-        for (int j = 0; j < ncq; j++) {
-          const int cj = c_cx_comp[P.lb][j];
-          const int bx = cj & 15, by = (cj >> 4) & 15, bz = cj >> 8;
-          const double *ex = Ex + (ax * nb + bx) * nt, *ey = Ey + (ay * nb + by) * nt,
-                       *ez = Ez + (az * nb + bz) * nt;
-          double acc = 0.0;
-          for (int t = 0; t <= ax + bx; t++)
-            for (int u = 0; u <= ay + by; u++) {
-              const double exy = ex[t] * ey[u];
-              for (int v = 0; v <= az + bz; v++)
-                acc = fma(exy * ez[v], R[r_index(t, u, v)], acc);
-            }
-          V[i][j] = fma(Q.pref, acc, V[i][j]);
-        }
-      }
-    }
-    // G[:, q] -= F[:, p] V (and G[:, p] -= F[:, q] V^T), through the shells'
-    // transforms when pure
-    double Fc[kCosxNc], Gc[kCosxNc];
-    const int tp = pure ? P.la : kCosxLmax + 1, tq = pure ? P.lb : kCosxLmax + 1;
-    for (int i = 0; i < ncp; i++) {
-      double s = 0.0;
-      for (int f = 0; f < P.np; f++)
-        s += Fg[P.bf_p + f] * (tp <= kCosxLmax ? c_cx_T[tp][f][i] : (f == i ? 1.0 : 0.0));
-      Fc[i] = s;
-    }
-    for (int j = 0; j < ncq; j++) {
-      double s = 0.0;
-      for (int i = 0; i < ncp; i++)
-        s = fma(Fc[i], V[i][j], s);
-      Gc[j] = s;
-    }
-    for (int h = 0; h < P.nq; h++) {
-      double s = 0.0;
-      for (int j = 0; j < ncq; j++)
-        s += (tq <= kCosxLmax ? c_cx_T[tq][h][j] : (h == j ? 1.0 : 0.0)) * Gc[j];
-      Gg[P.bf_q + h] -= s;
-    }
-    if (P.bf_p != P.bf_q) {
-      for (int j = 0; j < ncq; j++) {
-        double s = 0.0;
-        for (int h = 0; h < P.nq; h++)
-          s += Fg[P.bf_q + h] * (tq <= kCosxLmax ? c_cx_T[tq][h][j] : (h == j ? 1.0 : 0.0));
-        Fc[j] = s;
-      }
-      for (int i = 0; i < ncp; i++) {
-        double s = 0.0;
-        for (int j = 0; j < ncq; j++)
-          s = fma(V[i][j], Fc[j], s);
-        Gc[i] = s;
-      }
-      for (int f = 0; f < P.np; f++) {
-        double s = 0.0;
-        for (int i = 0; i < ncp; i++)
-          s += (tp <= kCosxLmax ? c_cx_T[tp][f][i] : (f == i ? 1.0 : 0.0)) * Gc[i];
-        Gg[P.bf_p + f] -= s;
-      }
+    switch (P.la * 3 + P.lb) { // shells up to d (kCosxLmax)
+    case 0: cosx_pair<0, 0>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 1: cosx_pair<0, 1>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 2: cosx_pair<0, 2>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 3: cosx_pair<1, 0>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 4: cosx_pair<1, 1>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 5: cosx_pair<1, 2>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 6: cosx_pair<2, 0>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 7: cosx_pair<2, 1>(P, prims, etab, C, pure, Fg, Gg); break;
+    default: cosx_pair<2, 2>(P, prims, etab, C, pure, Fg, Gg); break;
     }
   }
 }
 
 // G for one leaf's points, a thread per point, every kept shell pair.
-__global__ void __launch_bounds__(256) k_cosx_g(MolDev m, int l0, int off0, int npairs,
+__global__ void __launch_bounds__(128, 1) k_cosx_g(MolDev m, int l0, int off0, int npairs,
                                                 const CxPair *__restrict__ pairs,
                                                 const CxPrim *__restrict__ prims,
                                                 const double *__restrict__ etab,
@@ -524,6 +667,10 @@ void upload_cosx_tables() {
   }
   cuda_check(cudaMemcpyToSymbol(c_cx_comp, comp, sizeof(comp)), "cudaMemcpyToSymbol");
   cuda_check(cudaMemcpyToSymbol(c_cx_T, T, sizeof(T)), "cudaMemcpyToSymbol");
+  double inv[kBoysTable];
+  for (int i = 0; i < kBoysTable; i++)
+    inv[i] = 1.0 / (2 * i + 1);
+  cuda_check(cudaMemcpyToSymbol(c_inv_odd, inv, sizeof(inv)), "cudaMemcpyToSymbol");
 }
 
 } // namespace
@@ -706,7 +853,7 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
     c.launch("cosx_f", st,
              [&] { k_cosx_f<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_D2q, S.d_F); });
     c.launch("cosx_g", st, [&] {
-      k_cosx_g<<<nl, 256, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims, S.d_etab,
+      k_cosx_g<<<nl, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims, S.d_etab,
                                    S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0, S.d_F, S.d_G);
     });
     c.launch("cosx_k", st,

@@ -140,9 +140,10 @@ __global__ void __launch_bounds__(128) k_colloc_f64(MolDev m, double *__restrict
 }
 
 // acc[i][j] += sum_kk A[kk][ta + 16 i] B[kk][tb + 16 j] over one staged
-// chunk, i < NI and j < NJ: a tile's last 32 rows or columns that lie past
-// the leaf's points or AOs are not computed (NI or NJ = 2), which keeps the
-// executed FLOPs near the useful ones for leaves whose sizes are not
+// chunk, i < NI and j < NJ: the 16-row groups of a tile that lie wholly past
+// the leaf's points or AOs are not computed, which keeps the executed FLOPs
+// near the useful ones (0.91 of them for the 32-water cluster, against 0.80
+// and 0.69 for whole 64 x 64 tiles) for leaves whose sizes are not
 // multiples of 64.
 template <int NI, int NJ, int LDA, int LDB>
 __device__ __forceinline__ void mac_chunk(const double (*As)[LDA], const double (*Bs)[LDB],
@@ -163,18 +164,27 @@ __device__ __forceinline__ void mac_chunk(const double (*As)[LDA], const double 
         acc[i][j] = fma(a[i], b[j], acc[i][j]);
   }
 }
+// ni, nj: 16-row groups to compute (1..4), uniform over the CTA
 template <int LDA, int LDB>
 __device__ __forceinline__ void mac_chunk_n(const double (*As)[LDA], const double (*Bs)[LDB],
-                                            double (&acc)[4][4], int ta, int tb, bool full_i,
-                                            bool full_j) {
-  if (full_i && full_j)
+                                            double (&acc)[4][4], int ta, int tb, int ni, int nj) {
+#define OCCX_MAC_CASE(I, J)                                                                        \
+  case (I - 1) * 4 + (J - 1):                                                                      \
+    mac_chunk<I, J>(As, Bs, acc, ta, tb);                                                          \
+    break;
+  switch ((ni - 1) * 4 + (nj - 1)) {
+    OCCX_MAC_CASE(1, 1) OCCX_MAC_CASE(1, 2) OCCX_MAC_CASE(1, 3) OCCX_MAC_CASE(1, 4)
+    OCCX_MAC_CASE(2, 1) OCCX_MAC_CASE(2, 2) OCCX_MAC_CASE(2, 3) OCCX_MAC_CASE(2, 4)
+    OCCX_MAC_CASE(3, 1) OCCX_MAC_CASE(3, 2) OCCX_MAC_CASE(3, 3) OCCX_MAC_CASE(3, 4)
+    OCCX_MAC_CASE(4, 1) OCCX_MAC_CASE(4, 2) OCCX_MAC_CASE(4, 3)
+  default:
     mac_chunk<4, 4>(As, Bs, acc, ta, tb);
-  else if (full_i)
-    mac_chunk<4, 2>(As, Bs, acc, ta, tb);
-  else if (full_j)
-    mac_chunk<2, 4>(As, Bs, acc, ta, tb);
-  else
-    mac_chunk<2, 2>(As, Bs, acc, ta, tb);
+  }
+#undef OCCX_MAC_CASE
+}
+// 16-row groups of a 64-wide tile starting at t0 that hold any of n rows
+__device__ __forceinline__ int groups16(int n, int t0) {
+  return max(1, min(4, (n - t0 + 15) / 16));
 }
 
 // rho for one 64-point slab of one leaf.  Thread (tx, ty): points
@@ -205,11 +215,11 @@ __global__ void __launch_bounds__(256, 2) k_rho_f64(MolDev m, const double *__re
     for (int i = 0; i < 4; i++)
       part[c][i] = 0.0;
 
-  // a slab with at most 32 points, a last AO tile with at most 32 AOs:
-  // their upper halves are not computed
-  const bool full_i = L.cnt - it.p0 > 32;
+  // the 16-point groups of the slab and 16-AO groups of the tile past the
+  // leaf's points and AOs are not computed
+  const int gi = groups16(L.cnt, it.p0);
   for (int j0 = 0; j0 < L.mpad; j0 += kAoTile) {
-    const bool full_j = L.nbf - j0 > 32;
+    const int gj = groups16(L.nbf, j0);
     double acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; i++)
@@ -233,7 +243,7 @@ __global__ void __launch_bounds__(256, 2) k_rho_f64(MolDev m, const double *__re
         Bs[kb][jb] = dv;
       }
       __syncthreads();
-      mac_chunk_n<kPtTile, kAoTile>(As, Bs, acc, tx, ty, full_i, full_j);
+      mac_chunk_n<kPtTile, kAoTile>(As, Bs, acc, tx, ty, gi, gj);
       __syncthreads();
     }
 #pragma unroll
@@ -334,9 +344,8 @@ __global__ void __launch_bounds__(256) k_vxc_f64(MolDev m, const double *__restr
     for (int b = 0; b < 4; b++)
       acc[a][b] = 0.0;
   constexpr int NSEG = META ? 4 : 1;
-  // a last AO tile with at most 32 rows or columns: its upper half is not
-  // computed
-  const bool full_i = L.nbf - it.i0 > 32, full_j = L.nbf - it.j0 > 32;
+  // the 16-AO groups of the tile past the leaf's AOs are not computed
+  const int gi = groups16(L.nbf, it.i0), gj = groups16(L.nbf, it.j0);
   for (int seg = 0; seg < NSEG; seg++)
   for (int p0 = 0; p0 < (L.cnt + kKChunk - 1) / kKChunk * kKChunk; p0 += kKChunk) {
 #pragma unroll
@@ -362,7 +371,7 @@ __global__ void __launch_bounds__(256) k_vxc_f64(MolDev m, const double *__restr
       Bs[pp][aa] = y;
     }
     __syncthreads();
-    mac_chunk_n<kAoTile + 1, kAoTile + 1>(As, Bs, acc, ty, tx, full_i, full_j);
+    mac_chunk_n<kAoTile + 1, kAoTile + 1>(As, Bs, acc, ty, tx, gi, gj);
     __syncthreads();
   }
   const int *g = m.leaf_ao + L.ao_begin;

@@ -1146,8 +1146,10 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 
 // ---- V_xc: K = phi^T Y on tcgen05, operands staged by TMA ------------------
 // One CTA per SM, persistent over V items (AO rows i0 .. i0 + 127 of the
-// blocks of one leaf; K = their points) fetched from a global queue and
-// handed to the roles through a ring in shared memory:
+// blocks of one leaf; K = their points) fetched from a global queue by a
+// scheduler warp (14), which resolves each item (sizes, workspace rows, AO
+// map, output) and hands it to the roles through a ring in shared memory,
+// up to four items ahead:
 //   warp 8       TMA producer: per K chunk of 32 points, hi and lo of the A
 //                rows (phi, split by k_colloc_f32) and of the B rows (Y,
 //                split by ymix_block), with the 128-byte swizzle: one
@@ -1175,20 +1177,42 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 constexpr int kItemBlocks = 2;   // blocks of a leaf accumulated in one V item
 constexpr int kVxcEpi = 256;     // epilogue threads (warps 0-7)
 constexpr int kVxcConv = 128;    // split threads (warps 10-13)
-constexpr int kVxcThreads = 448; // + producer warp + MMA warp + split warps
+constexpr int kVxcThreads = 480; // + TMA warp 8, MMA warp 9, split warps, scheduler warp 14
 constexpr int kVxcMap = 2048;    // AO maps up to this size are staged in shared memory
+// The stages share 192 KB: two of 96 KB for tiles of up to 256 columns
+// (k_vxc_tma<2>), or three of 64 KB for tiles of up to 128 columns
+// (k_vxc_tma<3>), which keeps one more chunk in flight.
+constexpr uint32_t kVxcStageArea = 2 * kStageBytes;
+template <int NS> struct VxcStage {
+  static constexpr uint32_t bytes = kVxcStageArea / NS;
+  static constexpr int max_n = NS == 2 ? 256 : 128;
+  static constexpr uint32_t off_blo = kOffBhi + static_cast<uint32_t>(max_n) * 128u;
+};
+static_assert(VxcStage<3>::off_blo + 128 * 128 <= VxcStage<3>::bytes, "three-stage layout");
+static_assert(VxcStage<2>::off_blo + 256 * 128 <= VxcStage<2>::bytes, "two-stage layout");
+
+// What every role needs of a V item, resolved once by the scheduler warp
+// (the chain of dependent global loads would otherwise stall each role at
+// every item).
+struct VxcInfo {
+  int it; // item index; -1: the queue is exhausted
+  int mp, rows_a, nblk, i0, nbf_leaf, vxc_n, nbf;
+  int r0[kItemBlocks]; // first row of each block in the tensor map
+  const int *amap;     // the leaf's AO map
+  double *V;           // accumulation target (A with V_xc = A + A^T)
+};
 
 struct alignas(16) VxcSmem {
-  uint64_t full[2], empty[2];   // per stage: TMA landed, MMAs done
-  uint64_t conv[2];             // per stage: split done (split mode)
+  uint64_t full[3], empty[3];   // per stage: TMA landed, MMAs done
+  uint64_t conv[3];             // per stage: split done (split mode)
   uint64_t tfull[2], tempty[2]; // per accumulator: ready, drained
   uint64_t ifull[kRing], iempty[kRing];
   uint64_t done;                // the MMA thread's final commit
   uint32_t tmem_slot;
-  int ring[kRing];
+  VxcInfo info[kRing];
   int gmap[kVxcMap];            // the epilogue's current AO map
 };
-constexpr uint32_t kVxcSmem = 2 * kStageBytes + sizeof(VxcSmem) + 1024;
+constexpr uint32_t kVxcSmem = kVxcStageArea + sizeof(VxcSmem) + 1024;
 
 // Operand planes of k_vxc_tma: K = sum over npairs of (A pair)^T (B pair),
 // each operand as its (hi, lo) TF32 planes, or (split != 0) as one FP32
@@ -1205,21 +1229,6 @@ constexpr VxcPlanes kVxcBuildPlanes{kPlanePhiHi, kPlanePhiLo, kPlaneYHi, kPlaneY
                                     1, 0};
 // phi (FP32, plane 0) and Y (FP32 in the Y hi plane, written by k_func_f2)
 constexpr VxcPlanes kVxcSplitPlanes{0, 0, kPlaneYHi, 0, 0, 0, 0, 0, 1, 1};
-
-struct VxcWork { // what every role derives from an item
-  int mp, rows_a, nblk, i0, nbf_leaf;
-};
-__device__ __forceinline__ VxcWork vxc_work(const MixTab *tabs, const MBlock *blocks,
-                                            const VItem &it) {
-  const MBlock B = blocks[it.block0];
-  VxcWork w;
-  w.mp = B.mp;
-  w.nblk = it.nblk;
-  w.i0 = it.i0;
-  w.rows_a = min(128, B.mp - it.i0); // a multiple of 32
-  w.nbf_leaf = tabs[B.mol].m.leaves[B.leaf].nbf;
-  return w;
-}
 
 __device__ __forceinline__ void epi_bar() { // the epilogue threads
   asm volatile("bar.sync 1, %0;" ::"n"(kVxcEpi) : "memory");
@@ -1278,6 +1287,7 @@ __device__ __forceinline__ double f32_bits_to_f64(uint32_t u) {
   return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
 }
 
+template <int NS>
 __global__ void __launch_bounds__(kVxcThreads, 1)
     k_vxc_tma(const MixTab *__restrict__ tabs, const MBlock *__restrict__ blocks,
               const VItem *__restrict__ items, int nitems, Override ov, int *queue, int *err,
@@ -1285,20 +1295,24 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
               VxcPlanes pl) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = aligned_smem(smem_raw);
-  VxcSmem *sm = reinterpret_cast<VxcSmem *>(smem + 2 * kStageBytes);
-  uint8_t *stage[2] = {smem, smem + kStageBytes};
+  using SG = VxcStage<NS>;
+  VxcSmem *sm = reinterpret_cast<VxcSmem *>(smem + kVxcStageArea);
+  auto stage = [&](int s) { return smem + static_cast<uint32_t>(s) * SG::bytes; };
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   if (t == 0) {
-    for (int s = 0; s < 2; s++) {
+    for (int s = 0; s < NS; s++) {
       umma::mbar_init(&sm->full[s], 1);
       umma::mbar_init(&sm->empty[s], 1);
       umma::mbar_init(&sm->conv[s], kVxcConv);
+    }
+    for (int s = 0; s < 2; s++) {
       umma::mbar_init(&sm->tfull[s], 1);
       umma::mbar_init(&sm->tempty[s], kVxcEpi);
     }
     for (int r = 0; r < kRing; r++) {
       umma::mbar_init(&sm->ifull[r], 1);
-      umma::mbar_init(&sm->iempty[r], 1 + kVxcEpi + (pl.split ? kVxcConv : 0));
+      // consumers: the TMA thread, the MMA thread, the epilogue, the split
+      umma::mbar_init(&sm->iempty[r], 2 + kVxcEpi + (pl.split ? kVxcConv : 0));
     }
     umma::mbar_init(&sm->done, 1);
     umma::fence_proxy_async();
@@ -1323,7 +1337,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
   // the epilogue warps issue warp-collective TMEM loads and share barriers,
   // the split warps share a barrier: all threads of either group take every
   // decision to stop together
-  const bool epi = warp < 8, cv = warp >= 10;
+  const bool epi = warp < 8, cv = warp >= 10 && warp < 14;
   auto agree = [&] {
     if (epi)
       ok = epi_all(ok);
@@ -1331,50 +1345,75 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       ok = conv_all(ok);
     return ok;
   };
-  // consumer side of the item ring: next item index or -1
-  auto next_item = [&](int k) {
+  // consumer side of the item ring: the next item's resolved description
+  // (false at the end of the queue or on a timed-out wait)
+  auto next_item = [&](int k, VxcInfo &w) {
     const int slot = k % kRing;
     wait(&sm->ifull[slot], (k / kRing) & 1);
     if (!agree())
-      return -1;
-    const int it = sm->ring[slot];
+      return false;
+    w = sm->info[slot];
     umma::mbar_arrive(&sm->iempty[slot]);
-    return it;
+    return w.it >= 0;
   };
 
-  if (warp == 8) {
-    // ---- TMA producer (lane 0) ----
+  if (warp == 14) {
+    // ---- scheduler (lane 0): items from the global queue, resolved into the
+    // ring up to kRing ahead of the slowest role ----
     if (lane == 0) {
-      uint32_t g = 0; // chunks issued
       for (int k = 0;; k++) {
         const int slot = k % kRing;
         if (k >= kRing && !wait(&sm->iempty[slot], ((k / kRing) - 1) & 1))
           break;
-        int it = atomicAdd(&queue[1], 1);
-        if (it >= nitems)
-          it = -1;
-        sm->ring[slot] = it;
+        const int it = atomicAdd(&queue[1], 1);
+        VxcInfo w;
+        w.it = it < nitems ? it : -1;
+        if (w.it >= 0) {
+          const VItem I = items[it];
+          const MBlock B0 = blocks[I.block0];
+          const MixTab &T = tabs[B0.mol];
+          const DevLeaf L = T.m.leaves[B0.leaf];
+          w.mp = B0.mp;
+          w.nblk = I.nblk;
+          w.i0 = I.i0;
+          w.rows_a = min(128, B0.mp - I.i0); // a multiple of 32
+          w.nbf_leaf = L.nbf;
+          w.vxc_n = T.vxc_n;
+          w.nbf = T.m.nbf;
+          w.r0[0] = static_cast<int>(T.ws_row0 + B0.ws_off / kBlockPts);
+          w.r0[1] = I.nblk > 1
+                        ? static_cast<int>(T.ws_row0 + blocks[I.block0 + 1].ws_off / kBlockPts)
+                        : 0;
+          w.amap = T.m.leaf_ao + L.ao_begin;
+          w.V = t_V(T, ov);
+        }
+        sm->info[slot] = w;
         umma::mbar_arrive(&sm->ifull[slot]);
-        if (it < 0)
+        if (w.it < 0)
           break;
-        const VItem I = items[it];
-        const VxcWork W = vxc_work(tabs, blocks, I);
-        const MixTab &T = tabs[blocks[I.block0].mol];
-        const int NT = T.vxc_n;
-        for (int n0 = 0; n0 < W.mp && ok; n0 += NT) {
-          const int N = min(NT, W.mp - n0);
+      }
+    }
+  } else if (warp == 8) {
+    // ---- TMA producer (lane 0) ----
+    if (lane == 0) {
+      uint32_t g = 0; // chunks issued
+      VxcInfo W;
+      for (int k = 0; ok; k++) {
+        if (!next_item(k, W))
+          break;
+        const int NT = W.vxc_n, mp = W.mp;
+        for (int n0 = 0; n0 < mp && ok; n0 += NT) {
+          const int N = min(NT, mp - n0);
           for (int pr = 0; pr < pl.npairs && ok; pr++)
           for (int b = 0; b < W.nblk && ok; b++) {
-            const MBlock Bb = blocks[I.block0 + b];
-            const int r0 = static_cast<int>(T.ws_row0 + Bb.ws_off / kBlockPts);
-            const int mp = W.mp;
+            const int r0 = b ? W.r0[1] : W.r0[0];
             for (int c = 0; c < kBlockPts / kKc; c++, g++) {
-              const int s = g & 1;
-              if (g >= 2 && !wait(&sm->empty[s], ((g >> 1) - 1) & 1))
+              const int s = static_cast<int>(g % NS);
+              if (g >= NS && !wait(&sm->empty[s], ((g / NS) - 1) & 1))
                 break;
               umma::mbar_arrive_expect_tx(&sm->full[s], static_cast<uint32_t>(W.rows_a + N) *
                                                             (pl.split ? 128u : 256u));
-              uint8_t *st = stage[s];
+              uint8_t *st = stage(s);
               const int ah = pr ? pl.a_hi1 : pl.a_hi0, al = pr ? pl.a_lo1 : pl.a_lo0;
               const int bh = pr ? pl.b_hi1 : pl.b_hi0, bl = pr ? pl.b_lo1 : pl.b_lo0;
               // whole 128-row tiles in one copy each, the rest 32 rows at a time
@@ -1394,33 +1433,28 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
                 umma::tma_load_2d(st + kOffBhi + r * 128, mp_, c * kKc,
                                   r0 + bh * mp + n0 + r, &sm->full[s]);
                 if (!pl.split)
-                  umma::tma_load_2d(st + kOffBlo + r * 128, mp_, c * kKc,
+                  umma::tma_load_2d(st + SG::off_blo + r * 128, mp_, c * kKc,
                                     r0 + bl * mp + n0 + r, &sm->full[s]);
                 r += big ? 128 : 32;
               }
             }
           }
         }
-        if (!ok)
-          break;
       }
       // loads still in flight land before the CTA leaves
-      for (uint32_t q = (g >= 2 ? g - 2 : 0); q < g; q++)
-        umma::mbar_wait(&sm->full[q & 1], (q >> 1) & 1, kWaitIter);
+      for (uint32_t q = (g >= NS ? g - NS : 0); q < g; q++)
+        umma::mbar_wait(&sm->full[q % NS], (q / NS) & 1, kWaitIter);
     }
   } else if (warp == 9) {
     // ---- MMA issuer (lane 0) ----
     if (lane == 0) {
       uint32_t g = 0, pc = 0; // chunks consumed, passes
       bool issued = false;
+      VxcInfo W;
       for (int k = 0; ok; k++) {
-        const int it = next_item(k);
-        if (it < 0)
+        if (!next_item(k, W))
           break;
-        const VItem I = items[it];
-        const VxcWork W = vxc_work(tabs, blocks, I);
-        const MixTab &T = tabs[blocks[I.block0].mol];
-        const int NT = T.vxc_n;
+        const int NT = W.vxc_n;
         for (int n0 = 0; n0 < W.mp && ok; n0 += NT, pc++) {
           const int N = min(NT, W.mp - n0);
           const uint32_t buf = pc & 1, ub = pc >> 1;
@@ -1431,18 +1465,18 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
           const uint32_t idesc = umma::idesc_tf32(128, N);
           const int nch = pl.npairs * W.nblk * (kBlockPts / kKc);
           for (int c = 0; c < nch && ok; c++, g++) {
-            const int s = g & 1;
-            if (!wait(pl.split ? &sm->conv[s] : &sm->full[s], (g >> 1) & 1))
+            const int s = static_cast<int>(g % NS);
+            if (!wait(pl.split ? &sm->conv[s] : &sm->full[s], (g / NS) & 1))
               break;
             umma::fence_after_sync();
-            const uint32_t base = umma::smem_u32(stage[s]);
+            const uint32_t base = umma::smem_u32(stage(s));
 #pragma unroll
             for (int kk = 0; kk < kKc / 8; kk++) {
               const uint32_t o = kk * 32;
               const uint64_t ahi = umma::desc_kmajor_sw128(base + kOffAhi + o);
               const uint64_t alo = umma::desc_kmajor_sw128(base + kOffAlo + o);
               const uint64_t bhi = umma::desc_kmajor_sw128(base + kOffBhi + o);
-              const uint64_t blo = umma::desc_kmajor_sw128(base + kOffBlo + o);
+              const uint64_t blo = umma::desc_kmajor_sw128(base + SG::off_blo + o);
               const uint32_t acc = (c == 0 && kk == 0) ? 0u : 1u;
               umma::mma_tf32(d, alo, bhi, idesc, acc);
               umma::mma_tf32(d, ahi, blo, idesc, 1u);
@@ -1464,56 +1498,48 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     if (pl.split) {
       const int ct = t - 10 * 32;
       uint32_t g = 0; // chunks split
+      VxcInfo W;
       for (int k = 0; ok; k++) {
-        const int it = next_item(k);
-        if (it < 0)
+        if (!next_item(k, W))
           break;
-        const VItem I = items[it];
-        const VxcWork W = vxc_work(tabs, blocks, I);
-        const int NT = tabs[blocks[I.block0].mol].vxc_n;
+        const int NT = W.vxc_n;
         for (int n0 = 0; n0 < W.mp && ok; n0 += NT) {
           const int N = min(NT, W.mp - n0);
           const int nch = pl.npairs * W.nblk * (kBlockPts / kKc);
           for (int c = 0; c < nch; c++, g++) {
-            const int s = g & 1;
-            wait(&sm->full[s], (g >> 1) & 1);
+            const int s = static_cast<int>(g % NS);
+            wait(&sm->full[s], (g / NS) & 1);
             if (!agree())
               break;
-            uint8_t *st = stage[s];
+            uint8_t *st = stage(s);
             split_words(st + kOffAhi, st + kOffAlo, W.rows_a * 8, ct);
-            split_words(st + kOffBhi, st + kOffBlo, N * 8, ct);
+            split_words(st + kOffBhi, st + SG::off_blo, N * 8, ct);
             umma::fence_proxy_async(); // generic-proxy writes, read by the MMAs
             umma::mbar_arrive(&sm->conv[s]);
           }
         }
       }
     }
-  } else {
+  } else if (epi) {
     // ---- epilogue (warps 0-7) ----
     const int quad = warp & 3, half = warp >> 2;
     const int i = quad * 32 + lane; // row of the tile
     uint32_t pc = 0;
+    VxcInfo W;
     for (int k = 0; ok; k++) {
-      const int it = next_item(k);
-      if (it < 0)
+      if (!next_item(k, W))
         break;
-      const VItem I = items[it];
-      const VxcWork W = vxc_work(tabs, blocks, I);
-      const MBlock B0 = blocks[I.block0];
-      const MixTab &T = tabs[B0.mol];
-      const DevLeaf L = T.m.leaves[B0.leaf];
-      const int *gsrc = T.m.leaf_ao + L.ao_begin;
       const bool gsh = W.nbf_leaf <= kVxcMap;
       if (gsh) {
         epi_bar(); // the previous item's map is no longer read
         for (int q = t; q < W.nbf_leaf; q += kVxcEpi)
-          sm->gmap[q] = gsrc[q];
+          sm->gmap[q] = W.amap[q];
         epi_bar();
       }
-      const int *g = gsh ? sm->gmap : gsrc;
-      double *__restrict__ V = t_V(T, ov);
-      const size_t nbf = static_cast<size_t>(T.m.nbf);
-      const int NT = T.vxc_n;
+      const int *g = gsh ? sm->gmap : W.amap;
+      double *__restrict__ V = W.V;
+      const size_t nbf = static_cast<size_t>(W.nbf);
+      const int NT = W.vxc_n;
       const int li = W.i0 + i;
       const bool iv = li < W.nbf_leaf;
       const size_t gi = iv ? static_cast<size_t>(g[li]) : 0;
@@ -1826,7 +1852,9 @@ void set_smem_attributes() {
   cuda_check(cudaFuncSetAttribute(k_rho_mixed<true, true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kRhoSmem),
              "cudaFuncSetAttribute");
-  cuda_check(cudaFuncSetAttribute(k_vxc_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cuda_check(cudaFuncSetAttribute(k_vxc_tma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kVxcSmem), "cudaFuncSetAttribute");
+  cuda_check(cudaFuncSetAttribute(k_vxc_tma<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kVxcSmem), "cudaFuncSetAttribute");
   cuda_check(cudaFuncSetAttribute(k_selftest_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kSmemTotal), "cudaFuncSetAttribute");
@@ -1860,6 +1888,21 @@ struct LaunchPlan {
       cudaFree(p);
   }
 };
+
+// k_vxc_tma with the stage count that the widest V tile of the launch
+// allows: three stages when every molecule's tile N is at most 128.
+int plan_max_n(const LaunchPlan &P) {
+  int m = 0;
+  for (const MixTab &t : P.tabs)
+    m = std::max(m, t.vxc_n);
+  return m;
+}
+template <class... A> void launch_vxc(const LaunchPlan &P, int grid, cudaStream_t st, A... args) {
+  if (plan_max_n(P) <= VxcStage<3>::max_n)
+    k_vxc_tma<3><<<grid, kVxcThreads, kVxcSmem, st>>>(args...);
+  else
+    k_vxc_tma<2><<<grid, kVxcThreads, kVxcSmem, st>>>(args...);
+}
 
 // Per-molecule resident state of the mixed path.  The per-build workspace
 // (AO planes, row scales, D2 hi/lo, column bounds) is bound separately: a
@@ -2047,8 +2090,8 @@ void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st,
   if (ni > 0)
     c.launch("vxc_mixed", st, [&] {
       const int g = std::min(ni, ctas);
-      k_vxc_tma<<<g, kVxcThreads, kVxcSmem, st>>>(P.d_tabs, P.d_blocks, P.d_items, ni, ov, P.d_queue, err,
-                                          P.tmap.rows32, P.tmap.rows128, kVxcSplitPlanes);
+      launch_vxc(P, g, st, P.d_tabs, P.d_blocks, P.d_items, ni, ov, P.d_queue, err, P.tmap.rows32,
+                 P.tmap.rows128, kVxcSplitPlanes);
     });
   c.launch("symmetrize", st, [&] {
     const size_t n2 = static_cast<size_t>(P.maxnbf) * P.maxnbf;
@@ -3322,7 +3365,7 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
     const VxcPlanes pl{1 + cc, 0, kPlaneYHi, 0, kPlaneZ + cc, 0, 0, 0, 2, 1};
     Override ovc{dD, g.G + cc * nbf2, dout2};
     c.launch("grad_vxc", st, [&] {
-      k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+      launch_vxc(P, std::min(ni, sms), st,
           P.d_tabs, P.d_blocks, P.d_items, ni, ovc, P.d_queue, err, P.tmap.rows32, P.tmap.rows128,
           pl);
     });
@@ -3423,7 +3466,7 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
     if (ni > 0) {
       cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
       c.launch("vxc_mixed", st, [&] {
-        k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+        launch_vxc(P, std::min(ni, sms), st,
             tabs[s], P.d_blocks, P.d_items, ni, ov[s], P.d_queue, err, P.tmap.rows32,
             P.tmap.rows128, kVxcBuildPlanes);
       });
@@ -3661,7 +3704,7 @@ void Molecule::build_mixed_mgga(const double *dD, double *dV, double *dout2, cud
       if (v > 0)
         cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
       c.launch(v == 0 ? "vxc_mixed" : "vxc_tau_mixed", st, [&] {
-        k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+        launch_vxc(P, std::min(ni, sms), st,
             P.d_tabs, P.d_blocks, P.d_items, ni, ov, P.d_queue, err, P.tmap.rows32,
             P.tmap.rows128, pls[v]);
       });
@@ -3747,7 +3790,7 @@ void Molecule::build_mixed_uks_mgga(const double *dD, double *dV, double *dout3,
     for (int v = 0; v < 2 && ni > 0; v++) {
       cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
       c.launch(v == 0 ? "vxc_mixed" : "vxc_tau_mixed", st, [&] {
-        k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+        launch_vxc(P, std::min(ni, sms), st,
             tabs[s], P.d_blocks, P.d_items, ni, ov[s], P.d_queue, err, P.tmap.rows32,
             P.tmap.rows128, pls[v]);
       });
@@ -3849,7 +3892,7 @@ void Molecule::xc_gradient_uks_mixed(const double *dD, double *dgrad, double *do
       const VxcPlanes pl{1 + cc, 0, kPlaneYHi, 0, kPlaneZ + cc, 0, 0, 0, 2, 1};
       const Override ovc{Ds, g.G + cc * nbf2, nullptr};
       c.launch("grad_vxc", st, [&] {
-        k_vxc_tma<<<std::min(ni, sms), kVxcThreads, kVxcSmem, st>>>(
+        launch_vxc(P, std::min(ni, sms), st,
             tabs[s], P.d_blocks, P.d_items, ni, ovc, P.d_queue, err, P.tmap.rows32,
             P.tmap.rows128, pl);
       });
