@@ -123,10 +123,11 @@ def run_workload(args):
         print(json.dumps(line))
         return
     if args.workload == "cosx":
-        line = {"metric": "seminumerical (COSX) exchange matrices/s (FP64)",
+        line = {"metric": "seminumerical (COSX) exchange matrices/s (ESP integrals in FP32, "
+                          "FP64 beside it)",
                 "value": r.pop("calls_per_s"), "unit": "calls/s", "n_gpus": 1,
                 "steps": max(1, min(args.steps, 5)), "warmup": 1, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
                 "data": "synthetic", "config": {"workload": r.pop("workload")},
                 "clocks": cs.summary()}
         line.update(r)
@@ -328,9 +329,10 @@ def algorithmic_bytes(kernel, cnt, m, npts, nbf, deriv):
                  A-slice images read once (three 128 x 64 BF16 tiles per K
                  chunk of 64 AOs, the last chunk zero-padded), rho (+
                  gradient) written, D2 read once
-      func       rho and the grid read, Y hi / lo written from the phi
-                 (+ gradient) planes, coefficients written
-      vxc_mixed  phi hi / lo and Y hi / lo read once, V written once"""
+      func       rho and the grid read, Y written (one FP32 plane) from the
+                 phi (+ gradient) planes
+      vxc_mixed  phi and Y (FP32 planes, split into TF32 hi / lo in shared
+                 memory) read once, V written once"""
     blocks = np.ceil(cnt / 128.0)
     mp = np.ceil(m / 32.0) * 32
     pairs = float(np.sum(blocks * 128 * mp))  # point-AO entries of one plane
@@ -339,9 +341,9 @@ def algorithmic_bytes(kernel, cnt, m, npts, nbf, deriv):
         a_images = float(np.sum(blocks * np.ceil(mp / 64.0))) * 3 * 128 * 64 * 2
         return ncomp * 4 * pairs + a_images + 8 * ncomp * npts + 8.0 * nbf * nbf
     if kernel == "func":
-        return (ncomp + 2) * 4 * pairs + (32 + 8 * ncomp + 8 * ncomp) * npts
+        return (ncomp + 1) * 4 * pairs + (32 + 8 * ncomp) * npts
     if kernel == "vxc_mixed":
-        return 4 * 4 * pairs + 8.0 * nbf * nbf
+        return 2 * 4 * pairs + 8.0 * nbf * nbf
     return float("nan")
 
 
@@ -539,6 +541,21 @@ def main():
                 # the contraction it carries, for reference (not the bound)
                 "useful_tflops": (flops_half / (dom_avg_ms / 1e3) / 1e12
                                   if dom_name in ("rho_mixed", "vxc_mixed") else None)}
+        if dom_name in ("rho_mixed", "vxc_mixed"):
+            # the same kernel against the tensor roof: the split products
+            # executed per useful product (3xTF32: 3 on the TF32 rate, half
+            # the measured BF16 one; the exact-grid density: 8 BF16 MMAs per
+            # K step), padding of the tiles not counted
+            tf32 = dom_name == "vxc_mixed"
+            bf16 = peaks.get("bf16_tflops", 1900.0)
+            tpeak = bf16 / 2 if tf32 else bf16
+            executed = roof["useful_tflops"] * (3 if tf32 else 8)
+            roof["tensor"] = {"executed_tflops": executed, "peak": tpeak, "unit": "TFLOP/s",
+                              "frac": executed / tpeak,
+                              "peak_source": ("half of MEASURED_PEAKS.json bf16_tflops (TF32 rate)"
+                                              if tf32 else "MEASURED_PEAKS.json bf16_tflops")
+                                             + (" (of measured)" if "bf16_tflops" in peaks
+                                                else " (of fallback)")}
     roof["kernel_share"] = dom_ms / tot if tot else None
     roof["kernels_ms_per_build"] = {k: v[0] / v[1] for k, v in prof.items()}
 

@@ -195,11 +195,17 @@ int occ_xc_nlc_grid(const occ_xc_molecule *mol, double *points, double *weights)
  * and over its basis, the grid of `grid` (NULL: GridSettings::for_sgx(50),
  * src/numint/grid_settings.cpp:59-68), its AO values, the numerical overlap
  * S_num and the overlap projector Q = S_num^-1 S; shells up to d
- * (OCC_XC_ERR_ARG above).  Every operation is FP64. */
+ * (OCC_XC_ERR_ARG above).  Every operation is FP64 unless
+ * occ_xc_cosx_set_precision selects OCC_XC_MIXED. */
 typedef struct occ_xc_cosx occ_xc_cosx;
 int occ_xc_cosx_create(occ_xc_context *ctx, occ_xc_molecule *mol,
                        const occ_xc_grid_settings *grid, occ_xc_cosx **out);
 void occ_xc_cosx_destroy(occ_xc_cosx *cx);
+/* OCC_XC_FP64 (the default) or OCC_XC_MIXED: the ESP integrals of every
+ * shell pair at every grid point (Boys function, Hermite integrals and their
+ * contraction) in FP32, the rest (F, G, K', the projector) in FP64.  No
+ * counterpart in OCC, whose ESP integrals are FP64. */
+int occ_xc_cosx_set_precision(occ_xc_cosx *cx, int precision);
 /* Points of the exchange grid. */
 int occ_xc_cosx_grid_points(const occ_xc_cosx *cx, long *npoints);
 /* K (nbf x nbf, symmetric) of mo.D = D (nbf x nbf); host buffers, blocking. */

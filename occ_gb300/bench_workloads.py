@@ -33,8 +33,8 @@ uks             unrestricted (UKS) build of a 32-water cation radical (def2-SVP,
 vv10            VV10 non-local correlation of 32 waters (def2-SVP, 254,976
                 NLC points): FP64 and FP32-pair-sum calls, their difference.
 cosx            seminumerical (COSX) exchange matrix of an 8-water cluster
-                (def2-SVP) on the for_sgx(50) grid, FP64, device and host
-                entry points, set-up apart.
+                (def2-SVP) on the for_sgx(50) grid, FP64 and with the ESP
+                integrals in FP32, device and host entry points, set-up apart.
 
 Every input is seeded synthetic data with the shapes of these workloads.
 Each function returns a dict for one JSON line.
@@ -614,6 +614,31 @@ def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
         g = dft.compute_xc_gradient(D)
     out["gradient_fp64"] = {"gradients_per_s": 2.0 / (time.perf_counter() - t0),
                             "max_abs_g": float(np.max(np.abs(g)))}
+    # the tensor-core meta-GGA gradient, device entry point (CUDA events)
+    dG = torch.zeros(3 * len(mol), dtype=torch.float64, device="cuda")
+    lib.occ_xc_compute_xc_gradient_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
+                                                      C.c_int, C.c_void_p, C.c_void_p,
+                                                      C.c_void_p]
+
+    def one_g():
+        rc = lib.occ_xc_compute_xc_gradient_device(dft.ctx.h, dft.h, C.c_void_p(dD.data_ptr()),
+                                                   MIXED, C.c_void_p(dG.data_ptr()),
+                                                   C.c_void_p(d2.data_ptr()),
+                                                   C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(dft.ctx.error())
+    one_g()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for i in range(steps):
+        one_g()
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
+    gm = dG.cpu().numpy().reshape(-1, 3)
+    out["gradient_mixed"] = {"gradients_per_s": 1e3 / ms, "ms_per_gradient": ms,
+                             "max_abs_dg_vs_fp64": float(np.max(np.abs(gm - g)))}
     if oracle_check:
         root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
         sys.path.insert(0, os.path.join(root, "oracle"))
@@ -676,24 +701,34 @@ def cosx(torch, steps=3, warmup=1, waters=8, seed=0, angular=50):
     dD = torch.from_numpy(np.asfortranarray(D).ravel(order="F").copy()).cuda()
     dK = torch.zeros_like(dD)
     stream = torch.cuda.Stream()
-    for _ in range(warmup):
-        sgx.compute_K_device(dD.data_ptr(), dK.data_ptr(), stream.cuda_stream)
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-    ev[0].record(stream)
-    for i in range(steps):
-        sgx.compute_K_device(dD.data_ptr(), dK.data_ptr(), stream.cuda_stream)
-        ev[i + 1].record(stream)
-    torch.cuda.synchronize()
-    ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        K = sgx.compute_K(D)
-    e2e_s = (time.perf_counter() - t0) / steps
-    Kd = dK.cpu().numpy().reshape(nbf, nbf, order="F")
-    return {"workload": f"water{waters}_def2svp_cosx{angular}", "nbf": nbf,
-            "npoints": int(sgx.grid_points()), "calls_per_s": 1e3 / ms, "ms_per_call": ms,
-            "e2e": {"value": 1.0 / e2e_s, "unit": "calls/s",
-                    "h2d_bytes_per_step": int(D.nbytes), "d2h_bytes_per_step": int(K.nbytes)},
-            "setup_s": setup_s, "max_abs_K": float(np.abs(K).max()),
-            "host_vs_device_max_dK": float(np.abs(K - Kd).max())}
+    out = {"workload": f"water{waters}_def2svp_cosx{angular}", "nbf": nbf,
+           "npoints": int(sgx.grid_points()), "setup_s": setup_s}
+    Ks = {}
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        sgx.set_precision(prec)
+        for _ in range(warmup):
+            sgx.compute_K_device(dD.data_ptr(), dK.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record(stream)
+        for i in range(steps):
+            sgx.compute_K_device(dD.data_ptr(), dK.data_ptr(), stream.cuda_stream)
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            K = sgx.compute_K(D)
+        e2e_s = (time.perf_counter() - t0) / steps
+        Kd = dK.cpu().numpy().reshape(nbf, nbf, order="F")
+        Ks[name] = K
+        out[name] = {"calls_per_s": 1e3 / ms, "ms_per_call": ms,
+                     "e2e": {"value": 1.0 / e2e_s, "unit": "calls/s",
+                             "h2d_bytes_per_step": int(D.nbytes),
+                             "d2h_bytes_per_step": int(K.nbytes)},
+                     "host_vs_device_max_dK": float(np.abs(K - Kd).max())}
+    out["max_abs_K"] = float(np.abs(Ks["fp64"]).max())
+    out["max_abs_dK_mixed_vs_fp64"] = float(np.abs(Ks["mixed"] - Ks["fp64"]).max())
+    out["calls_per_s"] = out["mixed"]["calls_per_s"]
+    out["e2e"] = out["mixed"]["e2e"]
+    return out

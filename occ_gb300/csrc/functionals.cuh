@@ -485,8 +485,9 @@ __device__ __forceinline__ void eval_xc_mixed(const FuncSet &fs, double rho, dou
   }
 }
 
-// The same with double-float inputs and outputs and no FP64 operation
-// (the mixture coefficients are split by integer operations), where
+// The same with double-float inputs and outputs and no FP64 operation but
+// VWN's atan and B88's asinh (the mixture coefficients are split by integer
+// operations), where
 // rho >= 1e-10 and, for a GGA (gga), sigma >= 1e-30.  Elsewhere it returns
 // false without a result, and the caller evaluates the point with eval_xc on
 // its FP64 inputs (a double-float sigma below FP32's range would be zero).

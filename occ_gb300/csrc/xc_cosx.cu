@@ -78,78 +78,67 @@ __host__ __device__ constexpr int r_index(int t, int u, int v) {
          ((u + v) * (u + v + 1)) / 2 + v;
 }
 
-// F_n(T), n = 0..nmax (nmax <= 8): for T < 36 the series
-// F_n(T) = e^-T sum_k (2T)^k / ((2n+1)(2n+3)...(2n+2k+1)) for n = nmax and
-// downward recursion F_{n-1} = (2T F_n + e^-T) / (2n - 1); beyond, the
-// asymptotic F_0 = (pi / T)^{1/2} / 2 (erf(sqrt T) = 1 to 1e-17) and upward
-// recursion F_{n+1} = ((2n+1) F_n - e^-T) / (2T).
-__device__ __forceinline__ void boys(int nmax, double T, double *F) {
-  const double et = exp(-T);
-  if (T < 36.0) {
-    double term = 1.0 / (2 * nmax + 1), sum = term;
-    for (int k = 1; k < 256; k++) {
-      term *= 2.0 * T / (2 * nmax + 2 * k + 1);
-      sum += term;
-      if (term < 1e-17 * sum)
-        break;
-    }
-    F[nmax] = et * sum;
-    for (int n = nmax; n > 0; n--)
-      F[n - 1] = (2.0 * T * F[n] + et) / (2 * n - 1);
-  } else {
-    F[0] = 0.5 * sqrt(kPi / T);
-    for (int n = 0; n < nmax; n++)
-      F[n + 1] = ((2 * n + 1) * F[n] - et) / (2.0 * T);
-  }
-}
-
 // 1 / (2 i + 1), i = 0 .. kBoysTable - 1: the Boys series and recursions
 // multiply by these instead of dividing (GB300's FP64 divisions are slow).
 constexpr int kBoysTable = 272;
 __constant__ double c_inv_odd[kBoysTable];
+__constant__ float c_inv_odd_f[kBoysTable];
+template <typename R> __device__ __forceinline__ R inv_odd(int i);
+template <> __device__ __forceinline__ double inv_odd<double>(int i) { return c_inv_odd[i]; }
+template <> __device__ __forceinline__ float inv_odd<float>(int i) { return c_inv_odd_f[i]; }
+__device__ __forceinline__ double r_exp(double x) { return exp(x); }
+__device__ __forceinline__ float r_exp(float x) { return expf(x); }
+__device__ __forceinline__ double r_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float r_sqrt(float x) { return sqrtf(x); }
 
-// boys() with compile-time nmax and the reciprocal table: for T < 36 the
-// series at nmax and downward recursion; beyond, the asymptotic F_0 and
-// upward recursion.  Equal to boys() to rounding.
-template <int NMAX> __device__ __forceinline__ void boys_t(double T, double (&F)[NMAX + 1]) {
-  const double et = exp(-T);
-  const double t2 = 2.0 * T;
-  if (T < 36.0) {
-    double term = c_inv_odd[NMAX], sum = term;
+// F_n(T), n = 0..NMAX: for T < 36 the series
+// F_n(T) = e^-T sum_k (2T)^k / ((2n+1)(2n+3)...(2n+2k+1)) at n = NMAX and
+// downward recursion F_{n-1} = (2T F_n + e^-T) / (2n - 1); beyond, the
+// asymptotic F_0 = (pi / T)^{1/2} / 2 (erf(sqrt T) = 1 to 1e-17) and upward
+// recursion F_{n+1} = ((2n+1) F_n - e^-T) / (2T); divisions by odd numbers
+// through the reciprocal table.
+// R: double (the FP64 path) or float (the mixed path; the series stops at
+// 1e-8 of the sum).
+template <typename R, int NMAX> __device__ __forceinline__ void boys_t(R T, R (&F)[NMAX + 1]) {
+  const R et = r_exp(-T);
+  const R t2 = R(2) * T;
+  if (T < R(36)) {
+    R term = inv_odd<R>(NMAX), sum = term;
+    const R stop = sizeof(R) == 8 ? R(1e-17) : R(1e-8);
     for (int k = 1; k < kBoysTable - NMAX; k++) {
-      term *= t2 * c_inv_odd[NMAX + k];
+      term *= t2 * inv_odd<R>(NMAX + k);
       sum += term;
-      if (term < 1e-17 * sum)
+      if (term < stop * sum)
         break;
     }
     F[NMAX] = et * sum;
 #pragma unroll
     for (int n = NMAX; n > 0; n--)
-      F[n - 1] = fma(t2, F[n], et) * c_inv_odd[n - 1];
+      F[n - 1] = (t2 * F[n] + et) * inv_odd<R>(n - 1);
   } else {
-    F[0] = 0.5 * sqrt(kPi / T);
-    const double it2 = 1.0 / t2;
+    F[0] = R(0.5) * r_sqrt(R(kPi) / T);
+    const R it2 = R(1) / t2;
 #pragma unroll
     for (int n = 0; n < NMAX; n++)
-      F[n + 1] = ((2 * n + 1) * F[n] - et) * it2;
+      F[n + 1] = (R(2 * n + 1) * F[n] - et) * it2;
   }
 }
 
-// Index of R_tuv in a level array of degree <= S: as r_index.
-// R_tuv^(0), t + u + v <= L (compile time), all in registers: the same
-// recursion as hermite_r.
-template <int L>
-__device__ __forceinline__ void hermite_r_t(double p, double X, double Y, double Z,
-                                            double (&R)[(L + 1) * (L + 2) * (L + 3) / 6]) {
+// R_tuv^(0), t + u + v <= L (compile time, all in registers), for exponent p
+// and PC = P - C (McMurchie-Davidson recursion from R^(n)_000 = (-2p)^n F_n,
+// level by level).
+template <typename Rt, int L>
+__device__ __forceinline__ void hermite_r_t(Rt p, Rt X, Rt Y, Rt Z,
+                                            Rt (&R)[(L + 1) * (L + 2) * (L + 3) / 6]) {
   constexpr int NR = (L + 1) * (L + 2) * (L + 3) / 6;
-  double F[L + 1];
-  boys_t<L>(p * (X * X + Y * Y + Z * Z), F);
-  double up[NR], cur[NR];
-  double m2p[L + 1];
-  m2p[0] = 1.0;
+  Rt F[L + 1];
+  boys_t<Rt, L>(p * (X * X + Y * Y + Z * Z), F);
+  Rt up[NR], cur[NR];
+  Rt m2p[L + 1];
+  m2p[0] = Rt(1);
 #pragma unroll
   for (int n = 1; n <= L; n++)
-    m2p[n] = m2p[n - 1] * (-2.0 * p);
+    m2p[n] = m2p[n - 1] * (Rt(-2) * p);
 #pragma unroll
   for (int n = L; n >= 0; n--) {
 #pragma unroll
@@ -159,17 +148,17 @@ __device__ __forceinline__ void hermite_r_t(double p, double X, double Y, double
 #pragma unroll
         for (int u = sdeg - t; u >= 0; u--) {
           const int v = sdeg - t - u;
-          double val;
+          Rt val;
           if (sdeg == 0)
             val = m2p[n] * F[n];
           else if (t > 0)
-            val = (t > 1 ? (t - 1) * up[r_index(t > 1 ? t - 2 : 0, u, v)] : 0.0) +
+            val = (t > 1 ? Rt(t - 1) * up[r_index(t > 1 ? t - 2 : 0, u, v)] : Rt(0)) +
                   X * up[r_index(t - 1, u, v)];
           else if (u > 0)
-            val = (u > 1 ? (u - 1) * up[r_index(t, u > 1 ? u - 2 : 0, v)] : 0.0) +
+            val = (u > 1 ? Rt(u - 1) * up[r_index(t, u > 1 ? u - 2 : 0, v)] : Rt(0)) +
                   Y * up[r_index(t, u - 1, v)];
           else
-            val = (v > 1 ? (v - 1) * up[r_index(t, u, v > 1 ? v - 2 : 0)] : 0.0) +
+            val = (v > 1 ? Rt(v - 1) * up[r_index(t, u, v > 1 ? v - 2 : 0)] : Rt(0)) +
                   Z * up[r_index(t, u, v - 1)];
           cur[r_index(t, u, v)] = val;
         }
@@ -193,42 +182,6 @@ __host__ __device__ constexpr int cca_pow(int l, int i, int axis) {
       k++;
     }
   return 0;
-}
-
-// R_tuv^(0), t + u + v <= L, for exponent p and PC = P - C (McMurchie-
-// Davidson recursion from R^(n)_000 = (-2p)^n F_n, level by level).
-__device__ __forceinline__ void hermite_r(int L, double p, double X, double Y, double Z,
-                                          double *R) {
-  double F[kCosxLmax * 2 + 1];
-  boys(L, p * (X * X + Y * Y + Z * Z), F);
-  double up[kCosxR], cur[kCosxR];
-  double m2p = 1.0;
-  for (int n = 0; n < L; n++)
-    m2p *= -2.0 * p;
-  for (int n = L; n >= 0; n--) { // level n holds t + u + v <= L - n
-    const int smax = L - n;
-    for (int s = 0; s <= smax; s++)
-      for (int t = s; t >= 0; t--)
-        for (int u = s - t; u >= 0; u--) {
-          const int v = s - t - u;
-          double val;
-          if (s == 0)
-            val = m2p * F[n];
-          else if (t > 0)
-            val = (t > 1 ? (t - 1) * up[r_index(t - 2, u, v)] : 0.0) + X * up[r_index(t - 1, u, v)];
-          else if (u > 0)
-            val = (u > 1 ? (u - 1) * up[r_index(t, u - 2, v)] : 0.0) + Y * up[r_index(t, u - 1, v)];
-          else
-            val = (v > 1 ? (v - 1) * up[r_index(t, u, v - 2)] : 0.0) + Z * up[r_index(t, u, v - 1)];
-          cur[r_index(t, u, v)] = val;
-        }
-    for (int i = 0; i < (smax + 1) * (smax + 2) * (smax + 3) / 6; i++)
-      up[i] = cur[i];
-    if (n > 0)
-      m2p /= -2.0 * p;
-  }
-  for (int i = 0; i < (L + 1) * (L + 2) * (L + 3) / 6; i++)
-    R[i] = up[i];
 }
 
 // D2q = Q (2 D): Q, D column-major nbf x nbf; out row-major.  16 x 16 tiles.
@@ -293,23 +246,24 @@ __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restri
 // E^x_t E^y_u E^z_v R_tuv, then G[:, q] -= F[:, p] V and, for p != q,
 // G[:, p] -= F[:, q] V^T, through the shells' solid-harmonic transforms
 // when pure.
-template <int LA, int LB>
+template <typename Rt, int LA, int LB>
 __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restrict__ prims,
                                           const double *__restrict__ etab, const Pt4 &C, bool pure,
                                           const double *__restrict__ Fg, double *__restrict__ Gg) {
   constexpr int NCA = (LA + 1) * (LA + 2) / 2, NCB = (LB + 1) * (LB + 2) / 2;
   constexpr int L2 = LA + LB, NA = LA + 1, NB = LB + 1, NT = L2 + 1;
   constexpr int NR = (L2 + 1) * (L2 + 2) * (L2 + 3) / 6;
-  double V[NCA][NCB];
+  Rt V[NCA][NCB];
 #pragma unroll
   for (int i = 0; i < NCA; i++)
 #pragma unroll
     for (int j = 0; j < NCB; j++)
-      V[i][j] = 0.0;
+      V[i][j] = Rt(0);
   for (int r = 0; r < P.nprim; r++) {
     const CxPrim Q = prims[P.prim0 + r];
-    double R[NR];
-    hermite_r_t<L2>(Q.pexp, Q.P[0] - C.x, Q.P[1] - C.y, Q.P[2] - C.z, R);
+    Rt R[NR];
+    hermite_r_t<Rt, L2>(static_cast<Rt>(Q.pexp), static_cast<Rt>(Q.P[0] - C.x),
+                        static_cast<Rt>(Q.P[1] - C.y), static_cast<Rt>(Q.P[2] - C.z), R);
     const double *Ex = etab + Q.e_off, *Ey = Ex + NA * NB * NT, *Ez = Ey + NA * NB * NT;
 #pragma unroll
     for (int i = 0; i < NCA; i++) {
@@ -319,7 +273,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
         const int bx = cca_pow(LB, j, 0), by = cca_pow(LB, j, 1), bz = cca_pow(LB, j, 2);
         const double *ex = Ex + (ax * NB + bx) * NT, *ey = Ey + (ay * NB + by) * NT,
                      *ez = Ez + (az * NB + bz) * NT;
-        double acc = 0.0;
+        Rt acc = Rt(0);
         // compile-time trip counts (L2) with the exponent bounds as guards,
         // so that every R index is a constant and R stays in registers
 #pragma unroll
@@ -328,13 +282,13 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
           for (int u = 0; u <= L2 - t; u++) {
             if (t > ax + bx || u > ay + by)
               continue;
-            const double exy = ex[t] * ey[u];
+            const Rt exy = static_cast<Rt>(ex[t]) * static_cast<Rt>(ey[u]);
 #pragma unroll
             for (int v = 0; v <= L2 - t - u; v++)
               if (v <= az + bz)
-                acc = fma(exy * ez[v], R[r_index(t, u, v)], acc);
+                acc = fma(exy * static_cast<Rt>(ez[v]), R[r_index(t, u, v)], acc);
           }
-        V[i][j] = fma(Q.pref, acc, V[i][j]);
+        V[i][j] = fma(static_cast<Rt>(Q.pref), acc, V[i][j]);
       }
     }
   }
@@ -357,7 +311,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
     double s = 0.0;
 #pragma unroll
     for (int i = 0; i < NCA; i++)
-      s = fma(Fc[i], V[i][j], s);
+      s = fma(Fc[i], static_cast<double>(V[i][j]), s);
     Gc[j] = s;
   }
 #pragma unroll
@@ -385,7 +339,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
       double s = 0.0;
 #pragma unroll
       for (int j = 0; j < NCB; j++)
-        s = fma(V[i][j], Fq[j], s);
+        s = fma(static_cast<double>(V[i][j]), Fq[j], s);
       Gp[i] = s;
     }
 #pragma unroll
@@ -402,6 +356,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 
 // G[g, :] of one point g: every kept shell pair's ESP block V_g and its
 // two updates.
+template <typename Rt>
 __device__ __forceinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int p, int off0,
                                           int npairs, const CxPair *__restrict__ pairs,
                                           const CxPrim *__restrict__ prims,
@@ -423,20 +378,21 @@ __device__ __forceinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, 
         continue;
     }
     switch (P.la * 3 + P.lb) { // shells up to d (kCosxLmax)
-    case 0: cosx_pair<0, 0>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 1: cosx_pair<0, 1>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 2: cosx_pair<0, 2>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 3: cosx_pair<1, 0>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 4: cosx_pair<1, 1>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 5: cosx_pair<1, 2>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 6: cosx_pair<2, 0>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 7: cosx_pair<2, 1>(P, prims, etab, C, pure, Fg, Gg); break;
-    default: cosx_pair<2, 2>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 0: cosx_pair<Rt, 0, 0>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 1: cosx_pair<Rt, 0, 1>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 2: cosx_pair<Rt, 0, 2>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 3: cosx_pair<Rt, 1, 0>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 4: cosx_pair<Rt, 1, 1>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 5: cosx_pair<Rt, 1, 2>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 6: cosx_pair<Rt, 2, 0>(P, prims, etab, C, pure, Fg, Gg); break;
+    case 7: cosx_pair<Rt, 2, 1>(P, prims, etab, C, pure, Fg, Gg); break;
+    default: cosx_pair<Rt, 2, 2>(P, prims, etab, C, pure, Fg, Gg); break;
     }
   }
 }
 
 // G for one leaf's points, a thread per point, every kept shell pair.
+template <typename Rt>
 __global__ void __launch_bounds__(128, 1) k_cosx_g(MolDev m, int l0, int off0, int npairs,
                                                 const CxPair *__restrict__ pairs,
                                                 const CxPrim *__restrict__ prims,
@@ -448,7 +404,7 @@ __global__ void __launch_bounds__(128, 1) k_cosx_g(MolDev m, int l0, int off0, i
   const DevLeaf L = m.leaves[l0 + blockIdx.x];
   const double4 geo = lgeo[l0 + blockIdx.x];
   for (int p = threadIdx.x; p < L.cnt; p += blockDim.x)
-    cosx_g_point(m, L, p, off0, npairs, pairs, prims, etab, mask, geo, pure, F, G);
+    cosx_g_point<Rt>(m, L, p, off0, npairs, pairs, prims, etab, mask, geo, pure, F, G);
 }
 
 // K'[mu, lambda] -= sum_g phi_mu(g) G[g, lambda], mu over the leaf's AOs.
@@ -618,6 +574,7 @@ std::vector<double> spd_solve(std::vector<double> A, const std::vector<double> &
 struct CosxState {
   std::unique_ptr<Molecule> N;
   int nbf = 0, npairs = 0;
+  int precision = OCC_XC_FP64; // OCC_XC_MIXED: the ESP integrals in FP32
   std::vector<int> group_leaf0, group_nleaf, group_off0, group_npts;
   size_t group_pts_max = 0;
   double *d_Q = nullptr, *d_D = nullptr, *d_D2q = nullptr, *d_Kp = nullptr, *d_K = nullptr;
@@ -671,6 +628,10 @@ void upload_cosx_tables() {
   for (int i = 0; i < kBoysTable; i++)
     inv[i] = 1.0 / (2 * i + 1);
   cuda_check(cudaMemcpyToSymbol(c_inv_odd, inv, sizeof(inv)), "cudaMemcpyToSymbol");
+  float invf[kBoysTable];
+  for (int i = 0; i < kBoysTable; i++)
+    invf[i] = static_cast<float>(inv[i]);
+  cuda_check(cudaMemcpyToSymbol(c_inv_odd_f, invf, sizeof(invf)), "cudaMemcpyToSymbol");
 }
 
 } // namespace
@@ -853,8 +814,14 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
     c.launch("cosx_f", st,
              [&] { k_cosx_f<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_D2q, S.d_F); });
     c.launch("cosx_g", st, [&] {
-      k_cosx_g<<<nl, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims, S.d_etab,
-                                   S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0, S.d_F, S.d_G);
+      if (S.precision == OCC_XC_MIXED)
+        k_cosx_g<float><<<nl, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
+                                            S.d_etab, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
+                                            S.d_F, S.d_G);
+      else
+        k_cosx_g<double><<<nl, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
+                                             S.d_etab, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
+                                             S.d_F, S.d_G);
     });
     c.launch("cosx_k", st,
              [&] { k_cosx_k<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_G, S.d_Kp); });
@@ -895,6 +862,13 @@ int occ_xc_cosx_create(occ_xc_context *ctx, occ_xc_molecule *mol,
 }
 
 void occ_xc_cosx_destroy(occ_xc_cosx *cx) { delete cx; }
+
+int occ_xc_cosx_set_precision(occ_xc_cosx *cx, int precision) {
+  if (!cx || (precision != OCC_XC_FP64 && precision != OCC_XC_MIXED))
+    return OCC_XC_ERR_ARG;
+  cx->impl->precision = precision;
+  return OCC_XC_OK;
+}
 
 int occ_xc_cosx_grid_points(const occ_xc_cosx *cx, long *npoints) {
   if (!cx || !npoints)

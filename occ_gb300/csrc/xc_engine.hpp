@@ -254,6 +254,8 @@ struct Molecule {
   void prepare_gradient_mixed();
   // the same gradient with the contractions on the tensor cores (3xTF32)
   void xc_gradient_mixed(const double *dD, double *dgrad, double *dout2, cudaStream_t st);
+  void xc_gradient_mixed_mgga(const double *dD, double *dgrad, double *dout2, cudaStream_t st);
+  void grad_tables(GradMixed &g);
   void prepare_nlc();
   // VV10 energy (dE, one double) and, if dV, its V (nbf x nbf) for mo.D = dD;
   // precision OCC_XC_FP64 or OCC_XC_MIXED (FP32 pair sums)

@@ -140,7 +140,8 @@ __device__ __forceinline__ long long leaf_max_bits(long long v, long long *sh) {
 }
 
 // The tensor-core build's functional stage in double-float arithmetic, with
-// no FP64 operation per point where rho >= 1e-10 and sigma >= 1e-30 (the
+// no FP64 operation per point but VWN's atan and B88's asinh where
+// rho >= 1e-10 and sigma >= 1e-30 (the
 // FP64 inputs are split by integer operations, fn::f2_bits;
 // eval_xc_mixed_f2; the FP64 evaluator elsewhere): the skip, weights and
 // coefficients of leaf_functional<.., MIXED>, the coefficients as FP32 into

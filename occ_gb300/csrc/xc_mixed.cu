@@ -109,15 +109,15 @@ __device__ uint32_t g_wait_limit = kWaitIter;
 constexpr uint32_t kRhoStageA = 3 * 16384; // exact-grid A slices of one K chunk (128 x 32 each)
 constexpr int kErrTimeout = 1;
 // AO planes of a block, [plane][mp][128] FP32 each: phi, d/dx, d/dy, d/dz
-// (k_colloc_f32), hi and lo of Y (ymix_block, per build) and of phi (k_colloc_f32),
-// then three planes' worth of the exact-grid slices of phi as the density
-// GEMM's A operand: per K chunk of 32 AOs, three 128 x 32 K-major tiles in
-// the 128-byte-swizzled layout of shared memory (k_colloc_f32), so that
-// k_rho_mixed stages them with one bulk copy.  Everything but Y depends only
-// on the grid and the basis and stays valid across builds of a molecule whose
-// workspace is its own.
-constexpr int kPlanes = 11;
-constexpr int kPlaneYHi = 4, kPlaneYLo = 5, kPlanePhiHi = 6, kPlanePhiLo = 7, kPlaneASlices = 8;
+// (k_colloc_f32), Y (the V_xc operand, per build), then three planes' worth
+// of the exact-grid slices of phi as the density GEMM's A operand: per K
+// chunk of 64 AOs, three 128 x 64 BF16 K-major tiles in the 128-byte-swizzled
+// layout of shared memory (k_colloc_f32), so that k_rho_mixed stages them
+// with one bulk copy.  Everything but Y depends only on the grid and the
+// basis and stays valid across builds of a molecule whose workspace is its
+// own.
+constexpr int kPlanes = 8;
+constexpr int kPlaneYHi = 4, kPlaneASlices = 5;
 
 struct MBlock {
   int mol;          // molecule (row of the MixTab table)
@@ -546,10 +546,6 @@ __device__ __forceinline__ float colloc_shell_f32(const DevShell &sh, bool pure,
       out[plane + o] = valid ? gx[f] : 0.f;
       out[2 * plane + o] = valid ? gy[f] : 0.f;
       out[3 * plane + o] = valid ? gz[f] : 0.f;
-      float h, l;
-      tf32_split(val, h, l);
-      out[kPlanePhiHi * plane + o] = h;
-      out[kPlanePhiLo * plane + o] = l;
     }
   }
   return vmax;
@@ -632,8 +628,6 @@ __global__ void __launch_bounds__(128, 3) k_colloc_f32(const MixTab *__restrict_
     base[plane + o] = 0.f;
     base[2 * plane + o] = 0.f;
     base[3 * plane + o] = 0.f;
-    base[kPlanePhiHi * plane + o] = 0.f;
-    base[kPlanePhiLo * plane + o] = 0.f;
   }
   const float sA = pow2_bound(vmax), isA = 1.f / sA;
   T.rowscale[static_cast<size_t>(B.lblock) * kBlockPts + p] = sA;
@@ -794,7 +788,7 @@ __device__ __forceinline__ bool bar_all(int id, int n, bool v) {
 // TAU (meta-GGA): the same GEMM with the A slices of d_k phi (k = tk, built
 // by k_meta_ops at plane kPlaneTauA + 3 (tk - 1)), contracted with d_k phi:
 // sum_j d_k phi_j (d_k phi D2)_j into rho component 3 + tk.
-constexpr int kPlaneTauA = 11;
+constexpr int kPlaneTauA = kPlanes; // planes 8-16
 template <bool DERIV, bool TAU = false>
 __global__ void __launch_bounds__(kRhoThreads, 1)
     k_rho_mixed(const MixTab *__restrict__ tabs, const MBlock *__restrict__ blocks,
@@ -1150,21 +1144,19 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 // scheduler warp (14), which resolves each item (sizes, workspace rows, AO
 // map, output) and hands it to the roles through a ring in shared memory,
 // up to four items ahead:
-//   warp 8       TMA producer: per K chunk of 32 points, hi and lo of the A
-//                rows (phi, split by k_colloc_f32) and of the B rows (Y,
-//                split by ymix_block), with the 128-byte swizzle: one
+//   warp 8       TMA producer: per K chunk of 32 points the FP32 A rows
+//                (phi, or the pair's A plane) and B rows (Y, or the pair's B
+//                plane) into the hi slots, with the 128-byte swizzle: one
 //                32 x 128 box per whole 128-row tile, 32 x 32 boxes for the
 //                rest (the copies issued by the one producer thread bound
-//                this kernel more than its atomics: the 128-row boxes took
-//                it from 1.02 to 0.90 ms at 32 waters)
+//                this kernel: the 128-row boxes took it from 1.02 to 0.90 ms
+//                at 32 waters)
+//   warps 10-13  the TF32 split: every word split in place into hi and,
+//                beside it, lo (elementwise, so the swizzle does not
+//                matter); then the stage goes to the MMA issuer.  Half the
+//                operand bytes of pre-split hi / lo planes.
 //   warp 9       MMA issuer: hi*hi + hi*lo + lo*hi ("3xTF32") into one of two
 //                TMEM accumulators of 256 columns
-//   warps 10-13  (split mode) the TF32 split: the producer copies each
-//                operand once, as its FP32 plane, into the hi slot; these
-//                warps split every word in place into hi and the lo slot
-//                (elementwise, so the swizzle does not matter) and release
-//                the stage to the MMA issuer.  Half the operand bytes of
-//                pre-split hi / lo planes.
 //   warps 0-7    epilogue (two warps per TMEM lane quarter, each half of the
 //                columns): TMEM -> FP64 atomics, coalesced along the rows,
 //                into A with V_xc = A + A^T.  (Forming K^T beside K to add
@@ -1178,7 +1170,6 @@ constexpr int kItemBlocks = 2;   // blocks of a leaf accumulated in one V item
 constexpr int kVxcEpi = 256;     // epilogue threads (warps 0-7)
 constexpr int kVxcConv = 128;    // split threads (warps 10-13)
 constexpr int kVxcThreads = 480; // + TMA warp 8, MMA warp 9, split warps, scheduler warp 14
-constexpr int kVxcMap = 2048;    // AO maps up to this size are staged in shared memory
 // The stages share 192 KB: two of 96 KB for tiles of up to 256 columns
 // (k_vxc_tma<2>), or three of 64 KB for tiles of up to 128 columns
 // (k_vxc_tma<3>), which keeps one more chunk in flight.
@@ -1204,59 +1195,29 @@ struct VxcInfo {
 
 struct alignas(16) VxcSmem {
   uint64_t full[3], empty[3];   // per stage: TMA landed, MMAs done
-  uint64_t conv[3];             // per stage: split done (split mode)
+  uint64_t conv[3];             // per stage: TF32 split done
   uint64_t tfull[2], tempty[2]; // per accumulator: ready, drained
   uint64_t ifull[kRing], iempty[kRing];
   uint64_t done;                // the MMA thread's final commit
   uint32_t tmem_slot;
   VxcInfo info[kRing];
-  int gmap[kVxcMap];            // the epilogue's current AO map
 };
 constexpr uint32_t kVxcSmem = kVxcStageArea + sizeof(VxcSmem) + 1024;
 
-// Operand planes of k_vxc_tma: K = sum over npairs of (A pair)^T (B pair),
-// each operand as its (hi, lo) TF32 planes, or (split != 0) as one FP32
-// plane (the *_hi fields; the *_lo fields unused) split in shared memory.
-// The restricted build: one pair (phi, Y), split; the unrestricted build
-// one pre-split pair per spin; the XC gradient: two pairs (d_c phi, Y) and
-// (Z_c, phi).  Scalar fields, selected without indexing, so that the
-// parameters stay in the constant bank.
+// Operand planes of k_vxc_tma: K = sum over npairs (1..3) of (A pair)^T
+// (B pair), each operand an FP32 plane of the blocks, split into TF32 hi / lo
+// in shared memory.  The builds: one pair (phi, Y) (the meta-GGA build adds
+// (d_k phi, t_k)); the XC gradient: two pairs (d_c phi, Y) and (Z_c, phi);
+// the meta-GGA gradient's tau term three pairs (2 d_c d_k phi, t_k).  Scalar
+// fields, selected without indexing, so that the parameters stay in the
+// constant bank.
 struct VxcPlanes {
-  int a_hi0, a_lo0, b_hi0, b_lo0, a_hi1, a_lo1, b_hi1, b_lo1;
-  int npairs, split;
+  int a0, b0, a1, b1, a2, b2;
+  int npairs;
 };
-constexpr VxcPlanes kVxcBuildPlanes{kPlanePhiHi, kPlanePhiLo, kPlaneYHi, kPlaneYLo, 0, 0, 0, 0,
-                                    1, 0};
-// phi (FP32, plane 0) and Y (FP32 in the Y hi plane, written by k_func_f2)
-constexpr VxcPlanes kVxcSplitPlanes{0, 0, kPlaneYHi, 0, 0, 0, 0, 0, 1, 1};
+// phi (plane 0) and Y (written by the functional stage)
+constexpr VxcPlanes kVxcSplitPlanes{0, kPlaneYHi, 0, 0, 0, 0, 1};
 
-__device__ __forceinline__ void epi_bar() { // the epilogue threads
-  asm volatile("bar.sync 1, %0;" ::"n"(kVxcEpi) : "memory");
-}
-// AND of v over the epilogue threads (a barrier among them as well).
-__device__ __forceinline__ bool epi_all(bool v) {
-  uint32_t r;
-  asm volatile("{\n\t.reg .pred p, q;\n\t"
-               "setp.ne.u32 p, %1, 0;\n\t"
-               "barrier.red.and.pred q, 1, %2, p;\n\t"
-               "selp.u32 %0, 1, 0, q;\n\t}"
-               : "=r"(r)
-               : "r"(static_cast<uint32_t>(v)), "n"(kVxcEpi)
-               : "memory");
-  return r != 0;
-}
-// The same over the split threads (named barrier 2).
-__device__ __forceinline__ bool conv_all(bool v) {
-  uint32_t r;
-  asm volatile("{\n\t.reg .pred p, q;\n\t"
-               "setp.ne.u32 p, %1, 0;\n\t"
-               "barrier.red.and.pred q, 2, %2, p;\n\t"
-               "selp.u32 %0, 1, 0, q;\n\t}"
-               : "=r"(r)
-               : "r"(static_cast<uint32_t>(v)), "n"(kVxcConv)
-               : "memory");
-  return r != 0;
-}
 // Split n16 16-byte words at hi in place into TF32 hi and their remainders
 // (TF32) at lo, by the split threads (ct = 0 .. kVxcConv - 1).
 __device__ __forceinline__ void split_words(uint8_t *hi, uint8_t *lo, int n16, int ct) {
@@ -1312,7 +1273,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     for (int r = 0; r < kRing; r++) {
       umma::mbar_init(&sm->ifull[r], 1);
       // consumers: the TMA thread, the MMA thread, the epilogue, the split
-      umma::mbar_init(&sm->iempty[r], 2 + kVxcEpi + (pl.split ? kVxcConv : 0));
+      umma::mbar_init(&sm->iempty[r], 2 + kVxcEpi + kVxcConv);
     }
     umma::mbar_init(&sm->done, 1);
     umma::fence_proxy_async();
@@ -1334,15 +1295,14 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     }
     return ok;
   };
-  // the epilogue warps issue warp-collective TMEM loads and share barriers,
-  // the split warps share a barrier: all threads of either group take every
-  // decision to stop together
+  // the epilogue and split warps work warp by warp, with no barrier between
+  // warps (the epilogue reads the AO map through L1, the split warps each
+  // release their share of a stage): the threads of a warp, which issue
+  // warp-collective TMEM loads, take every decision to stop together
   const bool epi = warp < 8, cv = warp >= 10 && warp < 14;
   auto agree = [&] {
-    if (epi)
-      ok = epi_all(ok);
-    else if (cv)
-      ok = conv_all(ok);
+    if (epi || cv)
+      ok = __all_sync(0xffffffffu, ok);
     return ok;
   };
   // consumer side of the item ring: the next item's resolved description
@@ -1411,30 +1371,22 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
               const int s = static_cast<int>(g % NS);
               if (g >= NS && !wait(&sm->empty[s], ((g / NS) - 1) & 1))
                 break;
-              umma::mbar_arrive_expect_tx(&sm->full[s], static_cast<uint32_t>(W.rows_a + N) *
-                                                            (pl.split ? 128u : 256u));
+              umma::mbar_arrive_expect_tx(&sm->full[s],
+                                          static_cast<uint32_t>(W.rows_a + N) * 128u);
               uint8_t *st = stage(s);
-              const int ah = pr ? pl.a_hi1 : pl.a_hi0, al = pr ? pl.a_lo1 : pl.a_lo0;
-              const int bh = pr ? pl.b_hi1 : pl.b_hi0, bl = pr ? pl.b_lo1 : pl.b_lo0;
+              const int ah = pr == 0 ? pl.a0 : (pr == 1 ? pl.a1 : pl.a2);
+              const int bh = pr == 0 ? pl.b0 : (pr == 1 ? pl.b1 : pl.b2);
               // whole 128-row tiles in one copy each, the rest 32 rows at a time
               for (int r = 0; r < W.rows_a;) {
                 const bool big = W.rows_a - r >= 128;
-                const CUtensorMap *mp_ = big ? &tmap128 : &tmap;
-                umma::tma_load_2d(st + kOffAhi + r * 128, mp_, c * kKc,
+                umma::tma_load_2d(st + kOffAhi + r * 128, big ? &tmap128 : &tmap, c * kKc,
                                   r0 + ah * mp + W.i0 + r, &sm->full[s]);
-                if (!pl.split)
-                  umma::tma_load_2d(st + kOffAlo + r * 128, mp_, c * kKc,
-                                    r0 + al * mp + W.i0 + r, &sm->full[s]);
                 r += big ? 128 : 32;
               }
               for (int r = 0; r < N;) {
                 const bool big = N - r >= 128;
-                const CUtensorMap *mp_ = big ? &tmap128 : &tmap;
-                umma::tma_load_2d(st + kOffBhi + r * 128, mp_, c * kKc,
+                umma::tma_load_2d(st + kOffBhi + r * 128, big ? &tmap128 : &tmap, c * kKc,
                                   r0 + bh * mp + n0 + r, &sm->full[s]);
-                if (!pl.split)
-                  umma::tma_load_2d(st + SG::off_blo + r * 128, mp_, c * kKc,
-                                    r0 + bl * mp + n0 + r, &sm->full[s]);
                 r += big ? 128 : 32;
               }
             }
@@ -1466,7 +1418,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
           const int nch = pl.npairs * W.nblk * (kBlockPts / kKc);
           for (int c = 0; c < nch && ok; c++, g++) {
             const int s = static_cast<int>(g % NS);
-            if (!wait(pl.split ? &sm->conv[s] : &sm->full[s], (g / NS) & 1))
+            if (!wait(&sm->conv[s], (g / NS) & 1))
               break;
             umma::fence_after_sync();
             const uint32_t base = umma::smem_u32(stage(s));
@@ -1494,8 +1446,8 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       }
     }
   } else if (cv) {
-    // ---- TF32 split (warps 10-13), split mode only ----
-    if (pl.split) {
+    // ---- TF32 split (warps 10-13) ----
+    {
       const int ct = t - 10 * 32;
       uint32_t g = 0; // chunks split
       VxcInfo W;
@@ -1529,14 +1481,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     for (int k = 0; ok; k++) {
       if (!next_item(k, W))
         break;
-      const bool gsh = W.nbf_leaf <= kVxcMap;
-      if (gsh) {
-        epi_bar(); // the previous item's map is no longer read
-        for (int q = t; q < W.nbf_leaf; q += kVxcEpi)
-          sm->gmap[q] = W.amap[q];
-        epi_bar();
-      }
-      const int *g = gsh ? sm->gmap : W.amap;
+      const int *__restrict__ g = W.amap;
       double *__restrict__ V = W.V;
       const size_t nbf = static_cast<size_t>(W.nbf);
       const int NT = W.vxc_n;
@@ -1555,19 +1500,19 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
         for (int c0 = half * cols; c0 < (half + 1) * cols; c0 += 16) {
           uint32_t r[16];
           umma::tmem_ld16(lanebase + c0, r);
+          // the chunk's 16 column AOs, one load per lane, shared by shuffles
+          const int ljl = n0 + c0 + (lane & 15);
+          const int gl = ljl < W.nbf_leaf ? g[ljl] : 0;
           umma::tmem_wait_ld();
-          if (!iv)
-            continue;
 #pragma unroll
           for (int e = 0; e < 16; e++) {
             const int lj = n0 + c0 + e;
-            if (lj >= W.nbf_leaf)
-              continue;
+            const size_t gj = static_cast<size_t>(__shfl_sync(0xffffffffu, gl, e));
             // V accumulates A with V_xc = A + A^T (k_symmetrize): K[i][j]
             // goes to A[gi][gj], so a warp's lanes (consecutive rows i)
             // update consecutive addresses of one column
-            const size_t gj = static_cast<size_t>(g[lj]);
-            atomicAdd(&V[gj * nbf + gi], f32_bits_to_f64(r[e]));
+            if (iv && lj < W.nbf_leaf)
+              atomicAdd(&V[gj * nbf + gi], f32_bits_to_f64(r[e]));
           }
         }
         umma::fence_before_sync();
@@ -1581,11 +1526,11 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     umma::tmem_dealloc(tmem, 512);
 }
 
-// The B operand of k_vxc_tma for one block, pre-split for 3xTF32 (tf32_split):
-// Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi (FP32) into the Y hi / lo
-// planes; streams 4 planes in, 2 out.  RAW: Y as FP32 into the Y hi plane
-// only, for k_vxc_tma's split mode.  Run by a whole CTA; cf holds 128 float4.
-template <bool DERIV, bool RAW = false>
+// The B operand of k_vxc_tma for one block:
+// Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi (FP32) into the Y plane
+// (split into TF32 hi / lo by k_vxc_tma); streams 4 planes in, 1 out.  Run by
+// a whole CTA; cf holds 128 float4.
+template <bool DERIV>
 __device__ __forceinline__ void ymix_block(const MixTab &T, const MBlock &B, float4 *cf) {
   if (threadIdx.x < kBlockPts) {
     const int p = threadIdx.x;
@@ -1606,12 +1551,6 @@ __device__ __forceinline__ void ymix_block(const MixTab &T, const MBlock &B, flo
   float4 *__restrict__ base = reinterpret_cast<float4 *>(T.ws + B.ws_off);
   const size_t plane = static_cast<size_t>(B.mp) * (kBlockPts / 4); // in float4
   const int n4 = B.mp * (kBlockPts / 4);
-  auto split4 = [](float4 v, float4 &h, float4 &l) {
-    tf32_split(v.x, h.x, l.x);
-    tf32_split(v.y, h.y, l.y);
-    tf32_split(v.z, h.z, l.z);
-    tf32_split(v.w, h.w, l.w);
-  };
 #pragma unroll 2
   for (int q = threadIdx.x; q < n4; q += blockDim.x) {
     const int p = (q % (kBlockPts / 4)) * 4;
@@ -1628,14 +1567,7 @@ __device__ __forceinline__ void ymix_block(const MixTab &T, const MBlock &B, flo
       y.z = fmaf(gz.z, cf[p + 2].w, fmaf(gy.z, cf[p + 2].z, fmaf(gx.z, cf[p + 2].y, y.z)));
       y.w = fmaf(gz.w, cf[p + 3].w, fmaf(gy.w, cf[p + 3].z, fmaf(gx.w, cf[p + 3].y, y.w)));
     }
-    if (RAW) {
-      base[kPlaneYHi * plane + q] = y;
-    } else {
-      float4 yh, yl;
-      split4(y, yh, yl);
-      base[kPlaneYHi * plane + q] = yh;
-      base[kPlaneYLo * plane + q] = yl;
-    }
+    base[kPlaneYHi * plane + q] = y;
   }
   __syncthreads(); // cf is reused by the next block
 }
@@ -1663,7 +1595,7 @@ __device__ __forceinline__ double bsum256(double v, double *sh) {
 // block (a CTA of 256 left half of its threads idle in the functional, with
 // eight active warps an SM).
 constexpr int kFuncThreads = 128;
-template <bool DERIV, bool RAW = false>
+template <bool DERIV>
 __global__ void __launch_bounds__(kFuncThreads, 4) k_func_b(const MixTab *__restrict__ tabs,
                                                          const MBlock *__restrict__ blocks,
                                                          const LeafItem *__restrict__ litems) {
@@ -1676,7 +1608,7 @@ __global__ void __launch_bounds__(kFuncThreads, 4) k_func_b(const MixTab *__rest
                                              T.rho, T.coef, T.epart + 2 * li.leaf, sh);
   __syncthreads(); // the leaf's coefficients are written
   for (int b = 0; b < li.nblk; b++)
-    ymix_block<DERIV, RAW>(T, blocks[li.block0 + b], cf);
+    ymix_block<DERIV>(T, blocks[li.block0 + b], cf);
 }
 
 constexpr int kLeafMaxPts = 1024; // leaf_max's bound (check_build_settings)
@@ -1715,7 +1647,7 @@ __device__ __forceinline__ void ymix_stream(const MixTab &T, const MBlock &B,
 // functional in double-float arithmetic (leaf_functional_f2, no FP64
 // operation per point) with the coefficients as FP32 into shared memory, then
 // the V_xc operand Y of each of the leaf's blocks from them (ymix_stream, one
-// FP32 plane: k_vxc_tma's split mode forms hi and lo).  The FP64 coefficient
+// FP32 plane: k_vxc_tma forms hi and lo).  The FP64 coefficient
 // array is not written.
 template <bool DERIV>
 __global__ void __launch_bounds__(kFuncThreads, 4) k_func_f2(const MixTab *__restrict__ tabs,
@@ -3040,16 +2972,26 @@ int selftest_functional(occ_xc_context *ctx, const char *method, int n, const do
 // (src/dft/dft_gradient_kernels.cpp:472-595): the three G_c are the V_xc
 // kernel's K with two operand pairs each, accumulated over the leaves into
 // nbf x nbf FP64 matrices, then contracted with D.  The blocks carry, beside
-// the build's eleven planes, the FP32 planes of
+// the build's eight planes, the FP32 planes of
 //   Z_c = 0.5 w vrho d_c phi + 2 w vsigma grad rho . grad d_c phi
 // (k_grad_ops, with the AO second derivatives in FP32); the pairs
 // (d_c phi, Y) and (Z_c, phi) are read as FP32 planes (d_c phi and phi the
 // collocation's, Y written unsplit by the functional stage) and split into
-// TF32 hi / lo by the V_xc kernel's split mode.
+// TF32 hi / lo by the V_xc kernel.
 namespace occx {
 
-constexpr int kPlanesGrad = 14;
-constexpr int kPlaneZ = 11; // Z_c as FP32: planes 11 + c (d_c phi: the collocation's 1 + c)
+constexpr int kPlaneZ = kPlanes; // Z_c as FP32: planes 8 + c (d_c phi: the collocation's 1 + c)
+constexpr int kPlanesGrad = kPlaneZ + 3;
+// the meta-GGA plan's planes (its build and gradient share one workspace):
+// after the tau density's A slices (kPlaneTauA, 9 planes)
+constexpr int kPlaneMetaT = kPlaneTauA + 9; // t_k = c_tau d_k phi (FP32): planes 17 + (k-1)
+constexpr int kPlaneMetaZ = kPlaneMetaT + 3; // Z_c (FP32, the gradient): planes 20 + c
+constexpr int kPlaneMetaH = kPlaneMetaZ + 3; // 2 d_c d_k phi (FP32): xx, xy, xz, yy, yz, zz
+constexpr int kPlanesMeta = kPlaneMetaH + 6;
+// index of d_c d_k among xx, xy, xz, yy, yz, zz
+__host__ __device__ constexpr int hess_index(int c, int k) {
+  return c <= k ? (c == 0 ? k : (c == 1 ? 2 + k : 5)) : hess_index(k, c);
+}
 
 namespace {
 
@@ -3116,6 +3058,110 @@ __device__ __forceinline__ void cart_hess_dot_f32(float x, float y, float z, flo
   }
 }
 
+// The six second derivatives (xx, xy, xz, yy, yz, zz) of the Cartesian
+// functions of one shell (CCA order), by the same formula as
+// cart_hess_dot_f32.
+template <int L>
+__device__ __forceinline__ void cart_hess6_f32(float x, float y, float z, float R, float dR,
+                                               float d2R, float (*h6)[6]) {
+  float px[L + 1], py[L + 1], pz[L + 1];
+  px[0] = py[0] = pz[0] = 1.f;
+#pragma unroll
+  for (int i = 1; i <= L; i++) {
+    px[i] = px[i - 1] * x;
+    py[i] = py[i - 1] * y;
+    pz[i] = pz[i - 1] * z;
+  }
+  const float r[3] = {x, y, z};
+  int k = 0;
+#pragma unroll
+  for (int a = L; a >= 0; a--) {
+#pragma unroll
+    for (int b = L - a; b >= 0; b--) {
+      const int c = L - a - b;
+      const int e[3] = {a, b, c};
+      const float *pp[3] = {px, py, pz};
+      const float M = px[a] * py[b] * pz[c];
+      float Mi[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const int o1 = (i + 1) % 3, o2 = (i + 2) % 3;
+        Mi[i] = e[i] > 0 ? e[i] * pp[i][e[i] > 0 ? e[i] - 1 : 0] * pp[o1][e[o1]] * pp[o2][e[o2]]
+                         : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+#pragma unroll
+        for (int j = i; j < 3; j++) {
+          float Mij;
+          if (i == j) {
+            const int o1 = (i + 1) % 3, o2 = (i + 2) % 3;
+            Mij = e[i] > 1 ? e[i] * (e[i] - 1) * pp[i][e[i] > 1 ? e[i] - 2 : 0] * pp[o1][e[o1]] *
+                                 pp[o2][e[o2]]
+                           : 0.f;
+          } else {
+            const int l3 = 3 - i - j;
+            Mij = (e[i] > 0 && e[j] > 0)
+                      ? e[i] * e[j] * pp[i][e[i] > 0 ? e[i] - 1 : 0] *
+                            pp[j][e[j] > 0 ? e[j] - 1 : 0] * pp[l3][e[l3]]
+                      : 0.f;
+          }
+          h6[k][hess_index(i, j)] = Mij * R + (Mi[i] * r[j] + Mi[j] * r[i]) * dR +
+                                    M * ((i == j ? dR : 0.f) + r[i] * r[j] * d2R);
+        }
+      }
+      k++;
+    }
+  }
+}
+
+// The meta-GGA gradient's operand planes of one shell: Z_c (as grad_ops_shell
+// forms it) into kPlaneMetaZ + c and twice the AO Hessian into kPlaneMetaH.
+template <int L>
+__device__ __forceinline__ void grad_ops_shell_meta(bool pure, float x, float y, float z,
+                                                    float R, float dR, float d2R, bool valid,
+                                                    float c0, const float *cg, float *out,
+                                                    size_t plane) {
+  constexpr int NC = ncart_of(L);
+  constexpr int NF = 2 * L + 1 > NC ? 2 * L + 1 : NC;
+  float h6[NC][6];
+  cart_hess6_f32<L>(x, y, z, R, dR, d2R, h6);
+  const int nf = pure ? 2 * L + 1 : NC;
+#pragma unroll
+  for (int f = 0; f < NF; f++) {
+    if (f >= nf)
+      continue;
+    float hf[6];
+    if (!pure || L == 0) {
+#pragma unroll
+      for (int q = 0; q < 6; q++)
+        hf[q] = h6[f < NC ? f : 0][q];
+    } else {
+      const float *Tm = c_spht + sph_offset(L) + f * NC;
+      const float2 n = c_sphn[L * L + f];
+#pragma unroll
+      for (int q = 0; q < 6; q++) {
+        float a = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < NC; kk++)
+          a = fmaf(Tm[kk], h6[kk][q], a);
+        hf[q] = fmaf(n.x, a, n.y * a);
+      }
+    }
+    const size_t o = static_cast<size_t>(f) * kBlockPts;
+#pragma unroll
+    for (int cc = 0; cc < 3; cc++) {
+      const float dphi = out[(1 + cc) * plane + o];
+      const float zh = fmaf(cg[0], hf[hess_index(cc, 0)],
+                            fmaf(cg[1], hf[hess_index(cc, 1)], cg[2] * hf[hess_index(cc, 2)]));
+      out[(kPlaneMetaZ + cc) * plane + o] = valid ? fmaf(c0, dphi, zh) : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 6; q++)
+      out[(kPlaneMetaH + q) * plane + o] = valid ? 2.f * hf[q] : 0.f;
+  }
+}
+
 template <int L>
 __device__ __forceinline__ void grad_ops_shell(bool pure, float x, float y, float z, float R,
                                                float dR, float d2R, bool valid, float c0,
@@ -3159,6 +3205,7 @@ __device__ __forceinline__ void grad_ops_shell(bool pure, float x, float y, floa
 // One CTA of 128 threads (one point each) per block, after the functional
 // stage: the gradient operand planes from the collocation's d_c phi, the
 // functional's coefficients and the AO second derivatives.
+template <bool META = false>
 __global__ void __launch_bounds__(128) k_grad_ops(const MixTab *__restrict__ tabs,
                                                  const MBlock *__restrict__ blocks, int deriv) {
   const MBlock B = blocks[blockIdx.x];
@@ -3218,20 +3265,36 @@ __global__ void __launch_bounds__(128) k_grad_ops(const MixTab *__restrict__ tab
       d2R = fmaf(4.f * a * a, e, d2R);
     }
     float *out = base + static_cast<size_t>(loc) * kBlockPts + p;
-    switch (sh.l) {
-    case 0: grad_ops_shell<0>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
-    case 1: grad_ops_shell<1>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
-    case 2: grad_ops_shell<2>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
-    case 3: grad_ops_shell<3>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
-    default: grad_ops_shell<4>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+    if (META) {
+      switch (sh.l) {
+      case 0: grad_ops_shell_meta<0>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      case 1: grad_ops_shell_meta<1>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      case 2: grad_ops_shell_meta<2>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      case 3: grad_ops_shell_meta<3>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      default: grad_ops_shell_meta<4>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      }
+    } else {
+      switch (sh.l) {
+      case 0: grad_ops_shell<0>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      case 1: grad_ops_shell<1>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      case 2: grad_ops_shell<2>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      case 3: grad_ops_shell<3>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      default: grad_ops_shell<4>(m.pure, x, y, z, R, dR, d2R, valid, c0, cg, out, plane); break;
+      }
     }
     loc += sh.nfunc;
   }
   for (int f = loc; f < B.mp; f++) {
     const size_t o = static_cast<size_t>(f) * kBlockPts + p;
+    if (META) {
 #pragma unroll
-    for (int q = kPlaneZ; q < kPlanesGrad; q++)
-      base[q * plane + o] = 0.f;
+      for (int q = kPlaneMetaZ; q < kPlanesMeta; q++)
+        base[q * plane + o] = 0.f;
+    } else {
+#pragma unroll
+      for (int q = kPlaneZ; q < kPlanesGrad; q++)
+        base[q * plane + o] = 0.f;
+    }
   }
 }
 
@@ -3278,18 +3341,24 @@ struct GradMixed {
 void free_grad_mixed(GradMixed *g) { delete g; }
 
 void Molecule::prepare_gradient_mixed() {
-  require_not_mgga(deriv, "XC gradient");
   if (gmixed)
     return;
   if (!mixed)
     throw ArgError("the molecule has no device state");
   auto g = std::make_unique<GradMixed>();
+  if (deriv == 2) {
+    // the meta-GGA plan's workspace carries the gradient's planes too
+    prepare_mgga_mixed();
+    grad_tables(*g);
+    gmixed = g.release();
+    return;
+  }
   const WsLayout Lw = ws_layout(*this, kPlanesGrad);
   g->bytes = Lw.total;
   g->ws = static_cast<char *>(alloc(g->bytes));
   LaunchPlan &P = g->plan;
   make_plan_lists(P, {this}, {bind_ws(*this, g->ws, g->ws, kPlanesGrad)});
-  long long off = 0; // the blocks' offsets for 23 planes (same order as prepare_mixed)
+  long long off = 0; // the blocks' offsets for kPlanesGrad planes (same order as prepare_mixed)
   for (MBlock &B : P.blocks) {
     B.ws_off = off;
     off += static_cast<long long>(kPlanesGrad) * B.mp * kBlockPts;
@@ -3302,22 +3371,31 @@ void Molecule::prepare_gradient_mixed() {
   P.d_tabs = plan_upload(P, P.tabs);
   encode_ws_map(P.tmap, g->ws, g->bytes);
   P.ao_cacheable = true;
+  grad_tables(*g);
+  gmixed = g.release();
+}
+
+// The three G_c matrices and the AO -> atom map of a tensor-core gradient.
+void Molecule::grad_tables(GradMixed &g) {
   const size_t nbf2 = std::max<size_t>(static_cast<size_t>(basis.nbf) * basis.nbf, 1);
-  g->G = static_cast<double *>(alloc(3 * nbf2 * sizeof(double)));
+  g.G = static_cast<double *>(alloc(3 * nbf2 * sizeof(double)));
   std::vector<int> ao_atom(std::max(basis.nbf, 1));
   for (size_t s = 0; s < basis.shells.size(); s++)
     for (int f = 0; f < basis.shell_size(static_cast<int>(s)); f++)
       ao_atom[basis.first_bf[s] + f] = basis.shells[s].atom;
-  g->ao_atom = static_cast<int *>(alloc(ao_atom.size() * sizeof(int)));
-  cuda_check(cudaMemcpy(g->ao_atom, ao_atom.data(), ao_atom.size() * sizeof(int),
+  g.ao_atom = static_cast<int *>(alloc(ao_atom.size() * sizeof(int)));
+  cuda_check(cudaMemcpy(g.ao_atom, ao_atom.data(), ao_atom.size() * sizeof(int),
                         cudaMemcpyHostToDevice),
              "cudaMemcpy H2D");
-  gmixed = g.release();
 }
 
 void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
                                  cudaStream_t st) {
   prepare_gradient_mixed();
+  if (deriv == 2) {
+    xc_gradient_mixed_mgga(dD, dgrad, dout2, st);
+    return;
+  }
   GradMixed &g = *gmixed;
   LaunchPlan &P = g.plan;
   Context &c = *ctx;
@@ -3350,9 +3428,9 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
   if (nl > 0)
     c.launch("func", st, [&] {
       if (P.deriv)
-        k_func_b<true, true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_b<true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
       else
-        k_func_b<false, true><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+        k_func_b<false><<<nl, kFuncThreads, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
     });
   if (nb > 0)
     c.launch("grad_ops", st, [&] {
@@ -3362,7 +3440,7 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
   for (int cc = 0; cc < 3 && ni > 0; cc++) {
     cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
     // (d_c phi, Y) and (Z_c, phi), FP32 planes split by the kernel
-    const VxcPlanes pl{1 + cc, 0, kPlaneYHi, 0, kPlaneZ + cc, 0, 0, 0, 2, 1};
+    const VxcPlanes pl{1 + cc, kPlaneYHi, kPlaneZ + cc, 0, 0, 0, 2};
     Override ovc{dD, g.G + cc * nbf2, dout2};
     c.launch("grad_vxc", st, [&] {
       launch_vxc(P, std::min(ni, sms), st,
@@ -3390,12 +3468,12 @@ void Molecule::xc_gradient_mixed(const double *dD, double *dgrad, double *dout2,
 // are the restricted build's, in the molecule's private workspace.
 namespace occx {
 namespace {
-template <bool DERIV, bool RAW = false>
+template <bool DERIV>
 __global__ void __launch_bounds__(256) k_ymix(const MixTab *__restrict__ tabs,
                                              const MBlock *__restrict__ blocks) {
   __shared__ float4 cf[kBlockPts];
   const MBlock B = blocks[blockIdx.x];
-  ymix_block<DERIV, RAW>(tabs[B.mol], B, cf);
+  ymix_block<DERIV>(tabs[B.mol], B, cf);
 }
 } // namespace
 
@@ -3468,7 +3546,7 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
       c.launch("vxc_mixed", st, [&] {
         launch_vxc(P, std::min(ni, sms), st,
             tabs[s], P.d_blocks, P.d_items, ni, ov[s], P.d_queue, err, P.tmap.rows32,
-            P.tmap.rows128, kVxcBuildPlanes);
+            P.tmap.rows128, kVxcSplitPlanes);
       });
     }
     c.launch("symmetrize", st, [&] {
@@ -3494,13 +3572,15 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
 //   tau = 0.5 sum_k (d_k phi) D2 (d_k phi)          (src/gto/density.cpp:86-100)
 //   V  += sum_k (d_k phi)^T diag(0.5 w vtau) (d_k phi)
 //                                        (src/dft/xc_potential_matrix.cpp:43-58)
-// The blocks carry, beside the build's eleven planes, the exact-split A
-// slices of d_k phi (three per k, planes 11-19: the A operand of
-// k_rho_mixed's tau mode), the hi and lo TF32 planes of d_k phi (20-25) and
-// of c_tau d_k phi with c_tau = 0.25 w vtau (26-31).  The tau term of V is the
-// V_xc kernel's K with operand pairs (d_k phi, c_tau d_k phi), packed two a
-// launch with the GGA pair (phi, Y) into the same A that k_symmetrize turns
-// into A + A^T.  The functional is
+// The blocks carry, beside the build's eight planes, the exact-split A
+// slices of d_k phi (three per k, planes 8-16: the A operand of
+// k_rho_mixed's tau mode) and, as FP32 planes, t_k = c_tau d_k phi with
+// c_tau = 0.25 w vtau (17-19); the XC gradient adds Z_c (20-22) and twice the
+// AO Hessian (23-28: xx, xy, xz, yy, yz, zz).  The tau term of V is the V_xc
+// kernel's K with operand pairs (d_k phi, t_k), packed two a launch with the
+// GGA pair (phi, Y) into the same A that k_symmetrize turns into A + A^T, all
+// read as FP32 planes and split into TF32 hi / lo by the kernel.  The
+// functional is
 // the FP64 meta-GGA evaluator, fused with the operand planes (two CTAs an SM:
 // one's FP64 functional overlaps the other's HBM-bound planes).  Measured
 // alternatives: a double-float (FP32-pipe) TPSS needed 255 registers a thread
@@ -3508,18 +3588,11 @@ void Molecule::build_mixed_uks(const double *dD, double *dV, double *dout3, cuda
 // and the planes as two kernels (2.95 + 2.17 ms).
 namespace occx {
 
-constexpr int kPlanesMeta = 32;
-constexpr int kPlaneMetaDphi = 20; // hi, lo of d_k phi: planes 20 + 2(k-1), 21 + 2(k-1)
-constexpr int kPlaneMetaY = 26;    // hi, lo of c_tau d_k phi: planes 26 + 2(k-1), 27 + 2(k-1)
-
 // The V_xc launches of a meta build: four operand pairs, two a launch (the
-// kernel's cost is partly per launch: one pair 0.91 ms, two 1.22 ms at water32)
-//   (phi, Y) + (d_x phi, c_tau d_x phi),  (d_y phi, c_tau d_y phi) + (d_z phi, c_tau d_z phi)
-constexpr VxcPlanes kMetaVxcPlanes[2] = {
-    {kPlanePhiHi, kPlanePhiLo, kPlaneYHi, kPlaneYLo, kPlaneMetaDphi, kPlaneMetaDphi + 1,
-     kPlaneMetaY, kPlaneMetaY + 1, 2, 0},
-    {kPlaneMetaDphi + 2, kPlaneMetaDphi + 3, kPlaneMetaY + 2, kPlaneMetaY + 3,
-     kPlaneMetaDphi + 4, kPlaneMetaDphi + 5, kPlaneMetaY + 4, kPlaneMetaY + 5, 2, 0}};
+// kernel's cost is partly per launch), FP32 planes split by the kernel:
+//   (phi, Y) + (d_x phi, t_x),  (d_y phi, t_y) + (d_z phi, t_z)
+constexpr VxcPlanes kMetaVxcPlanes[2] = {{0, kPlaneYHi, 1, kPlaneMetaT, 0, 0, 2},
+                                         {2, kPlaneMetaT + 1, 3, kPlaneMetaT + 2, 0, 0, 2}};
 
 struct MetaMixed {
   char *ws = nullptr;
@@ -3532,8 +3605,8 @@ void free_meta_mixed(MetaMixed *g) { delete g; }
 namespace {
 
 // Per block (one thread per point), after k_colloc_f32: for k = x, y, z the
-// hi / lo planes of d_k phi and its A slices on the exact grid of the point's
-// own power-of-two bound.
+// A slices of d_k phi on the exact grid of the point's own power-of-two
+// bound.
 __global__ void __launch_bounds__(kBlockPts) k_meta_ops(const MixTab *__restrict__ tabs,
                                                         const MBlock *__restrict__ blocks) {
   const MBlock B = blocks[blockIdx.x];
@@ -3544,15 +3617,8 @@ __global__ void __launch_bounds__(kBlockPts) k_meta_ops(const MixTab *__restrict
   for (int k = 1; k <= 3; k++) {
     const float *g = base + k * plane;
     float vmax = 0.f;
-    for (int f = 0; f < B.mp; f++) {
-      const size_t o = static_cast<size_t>(f) * kBlockPts + p;
-      const float v = g[o];
-      vmax = fmaxf(vmax, fabsf(v));
-      float h, l;
-      tf32_split(v, h, l);
-      base[(kPlaneMetaDphi + 2 * (k - 1)) * plane + o] = h;
-      base[(kPlaneMetaDphi + 2 * (k - 1) + 1) * plane + o] = l;
-    }
+    for (int f = 0; f < B.mp; f++)
+      vmax = fmaxf(vmax, fabsf(g[static_cast<size_t>(f) * kBlockPts + p]));
     const float sA = pow2_bound(vmax), isA = 1.f / sA;
     write_a_slices(reinterpret_cast<uint8_t *>(base + (kPlaneTauA + 3 * (k - 1)) * plane), g,
                    B.mp, p, sA, isA);
@@ -3560,7 +3626,7 @@ __global__ void __launch_bounds__(kBlockPts) k_meta_ops(const MixTab *__restrict
 }
 
 // The meta-GGA functional per leaf (eval_xc_mgga_mixed), then per block the GGA operand Y
-// (ymix_block) and the tau term's operands c_tau d_k phi (hi, lo).
+// (ymix_block) and the tau term's operands t_k = c_tau d_k phi, as FP32 planes.
 __global__ void __launch_bounds__(256, 2) k_func_b_mgga(const MixTab *__restrict__ tabs,
                                                         const MBlock *__restrict__ blocks,
                                                         const LeafItem *__restrict__ litems) {
@@ -3588,19 +3654,15 @@ __global__ void __launch_bounds__(256, 2) k_func_b_mgga(const MixTab *__restrict
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
       const float c = ct[q % kBlockPts];
 #pragma unroll
-      for (int k = 1; k <= 3; k++) {
-        float h, l;
-        tf32_split(base[k * plane + q] * c, h, l);
-        base[(kPlaneMetaY + 2 * (k - 1)) * plane + q] = h;
-        base[(kPlaneMetaY + 2 * (k - 1) + 1) * plane + q] = l;
-      }
+      for (int k = 1; k <= 3; k++)
+        base[(kPlaneMetaT + k - 1) * plane + q] = base[k * plane + q] * c;
     }
     __syncthreads(); // ct is reused by the next block
   }
 }
 
 // Per block, for one spin's table (the UKS build): the GGA operand Y
-// (ymix_block) and the tau term's operands c_tau d_k phi (hi, lo).
+// (ymix_block) and the tau term's operands t_k = c_tau d_k phi, as FP32 planes.
 __global__ void __launch_bounds__(256) k_ymix_mgga(const MixTab *__restrict__ tabs,
                                                    const MBlock *__restrict__ blocks) {
   __shared__ float4 cf[kBlockPts];
@@ -3620,12 +3682,8 @@ __global__ void __launch_bounds__(256) k_ymix_mgga(const MixTab *__restrict__ ta
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
     const float c = ct[q % kBlockPts];
 #pragma unroll
-    for (int k = 1; k <= 3; k++) {
-      float h, l;
-      tf32_split(base[k * plane + q] * c, h, l);
-      base[(kPlaneMetaY + 2 * (k - 1)) * plane + q] = h;
-      base[(kPlaneMetaY + 2 * (k - 1) + 1) * plane + q] = l;
-    }
+    for (int k = 1; k <= 3; k++)
+      base[(kPlaneMetaT + k - 1) * plane + q] = base[k * plane + q] * c;
   }
 }
 
@@ -3642,7 +3700,7 @@ void Molecule::prepare_mgga_mixed() {
   g->ws = static_cast<char *>(alloc(g->bytes));
   LaunchPlan &P = g->plan;
   make_plan_lists(P, {this}, {bind_ws(*this, g->ws, g->ws, kPlanesMeta)}, true);
-  long long off = 0; // the blocks' offsets for 32 planes (same order as prepare_mixed)
+  long long off = 0; // the blocks' offsets for kPlanesMeta planes (same order as prepare_mixed)
   for (MBlock &B : P.blocks) {
     B.ws_off = off;
     off += static_cast<long long>(kPlanesMeta) * B.mp * kBlockPts;
@@ -3714,6 +3772,84 @@ void Molecule::build_mixed_mgga(const double *dD, double *dV, double *dout2, cud
     const size_t n2 = static_cast<size_t>(P.maxnbf) * P.maxnbf;
     const int gx = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
     k_symmetrize<<<dim3(std::max(gx, 1), 1), 256, 0, st>>>(P.d_tabs, ov);
+  });
+  c.launch("reduce", st, [&] { k_reduce_b<<<1, 256, 0, st>>>(P.d_tabs, ov); });
+  cuda_check(cudaGetLastError(), "kernel launch");
+  P.ao_valid = true;
+}
+
+// The meta-GGA XC gradient on the tensor cores (accumulate_gradient_contribution_R<2>,
+// src/dft/dft_gradient_kernels.cpp:124-172, 472-595): the meta build's density,
+// tau and functional stages on the meta plan, the operand planes Z_c and 2 d_c d_k phi
+// (k_grad_ops<true>), then per direction two V_xc-kernel launches into G_c,
+//   (d_c phi, Y) + (Z_c, phi)   and   sum_k (2 d_c d_k phi, t_k),  t_k = 0.25 w vtau d_k phi,
+// the second the reference's tau term sum_p d_c d_k phi_mu (0.5 w vtau) d_k phi_nu; then
+// g_A,c = - sum_{mu on A} sum_nu 4 D(mu, nu) G_c(mu, nu) (k_grad_contract).
+void Molecule::xc_gradient_mixed_mgga(const double *dD, double *dgrad, double *dout2,
+                                      cudaStream_t st) {
+  GradMixed &g = *gmixed;
+  LaunchPlan &P = mmixed->plan;
+  Context &c = *ctx;
+  int *err = mixed->d_err;
+  const int nb = static_cast<int>(P.blocks.size());
+  const int ni = static_cast<int>(P.items.size());
+  const int nl = static_cast<int>(P.litems.size());
+  const int sms = this->ctas > 0 ? this->ctas
+                                 : (ctx->max_ctas > 0 ? ctx->max_ctas : num_sms(device));
+  const size_t nbf2 = static_cast<size_t>(basis.nbf) * basis.nbf;
+  Override ov{dD, nullptr, dout2};
+  c.launch("prep_density", st, [&] {
+    k_prep_density<<<dim3(P.maxnbf, 1), 256, 0, st>>>(P.d_tabs, ov, P.d_queue);
+  });
+  if (nb > 0) {
+    if (!P.ao_valid) {
+      c.launch("colloc_f32", st, [&] {
+        k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+      c.launch("meta_ops", st, [&] {
+        k_meta_ops<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+    }
+    const int gg = std::min(nb, sms);
+    c.launch("rho_mixed", st, [&] {
+      k_rho_mixed<true><<<gg, kRhoThreads, kRhoSmem, st>>>(P.d_tabs, P.d_blocks, P.d_order, nb,
+                                                     P.d_queue, err);
+    });
+    for (int k = 1; k <= 3; k++) {
+      cuda_check(cudaMemsetAsync(P.d_queue, 0, sizeof(int), st), "cudaMemsetAsync");
+      c.launch("tau_mixed", st, [&] {
+        k_rho_mixed<true, true><<<gg, kRhoThreads, kRhoSmem, st>>>(
+            P.d_tabs, P.d_blocks, P.d_order, nb, P.d_queue, err, k);
+      });
+    }
+  }
+  if (nl > 0)
+    c.launch("func", st, [&] {
+      k_func_b_mgga<<<nl, 256, 0, st>>>(P.d_tabs, P.d_blocks, P.d_litems);
+    });
+  if (nb > 0)
+    c.launch("grad_ops", st, [&] {
+      k_grad_ops<true><<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks, 1);
+    });
+  cuda_check(cudaMemsetAsync(g.G, 0, 3 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
+  for (int cc = 0; cc < 3 && ni > 0; cc++) {
+    const Override ovc{dD, g.G + cc * nbf2, dout2};
+    const VxcPlanes pls[2] = {
+        {1 + cc, kPlaneYHi, kPlaneMetaZ + cc, 0, 0, 0, 2},
+        {kPlaneMetaH + hess_index(cc, 0), kPlaneMetaT, kPlaneMetaH + hess_index(cc, 1),
+         kPlaneMetaT + 1, kPlaneMetaH + hess_index(cc, 2), kPlaneMetaT + 2, 3}};
+    for (int v = 0; v < 2; v++) {
+      cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
+      c.launch(v == 0 ? "grad_vxc" : "grad_vxc_tau", st, [&] {
+        launch_vxc(P, std::min(ni, sms), st, P.d_tabs, P.d_blocks, P.d_items, ni, ovc, P.d_queue,
+                   err, P.tmap.rows32, P.tmap.rows128, pls[v]);
+      });
+    }
+  }
+  cuda_check(cudaMemsetAsync(dgrad, 0, 3 * Z.size() * sizeof(double), st), "cudaMemsetAsync");
+  c.launch("grad_contract", st, [&] {
+    if (basis.nbf > 0)
+      k_grad_contract<<<basis.nbf, 256, 0, st>>>(dD, g.G, basis.nbf, g.ao_atom, dgrad, nullptr);
   });
   c.launch("reduce", st, [&] { k_reduce_b<<<1, 256, 0, st>>>(P.d_tabs, ov); });
   cuda_check(cudaGetLastError(), "kernel launch");
@@ -3823,6 +3959,7 @@ namespace occx {
 
 void Molecule::xc_gradient_uks_mixed(const double *dD, double *dgrad, double *dout3,
                                      cudaStream_t st) {
+  require_not_mgga(deriv, "the unrestricted tensor-core XC gradient");
   prepare_gradient_mixed();
   prepare_uks();
   GradMixed &g = *gmixed;
@@ -3879,9 +4016,9 @@ void Molecule::xc_gradient_uks_mixed(const double *dD, double *dgrad, double *do
     const double *Ds = d_Dab + s * nbf2, *Do = d_Dab + (1 - s) * nbf2;
     c.launch("ymix", st, [&] {
       if (P.deriv)
-        k_ymix<true, true><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
+        k_ymix<true><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
       else
-        k_ymix<false, true><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
+        k_ymix<false><<<nb, 256, 0, st>>>(tabs[s], P.d_blocks);
     });
     c.launch("grad_ops", st, [&] {
       k_grad_ops<<<nb, kBlockPts, 0, st>>>(tabs[s], P.d_blocks, P.deriv);
@@ -3889,7 +4026,7 @@ void Molecule::xc_gradient_uks_mixed(const double *dD, double *dgrad, double *do
     cuda_check(cudaMemsetAsync(g.G, 0, 3 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
     for (int cc = 0; cc < 3 && ni > 0; cc++) {
       cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
-      const VxcPlanes pl{1 + cc, 0, kPlaneYHi, 0, kPlaneZ + cc, 0, 0, 0, 2, 1};
+      const VxcPlanes pl{1 + cc, kPlaneYHi, kPlaneZ + cc, 0, 0, 0, 2};
       const Override ovc{Ds, g.G + cc * nbf2, nullptr};
       c.launch("grad_vxc", st, [&] {
         launch_vxc(P, std::min(ni, sms), st,

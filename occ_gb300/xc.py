@@ -116,6 +116,7 @@ def library():
     lib.occ_xc_cosx_create.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(_GridSettings),
                                        C.POINTER(C.c_void_p)]
     lib.occ_xc_cosx_destroy.argtypes = [C.c_void_p]
+    lib.occ_xc_cosx_set_precision.argtypes = [C.c_void_p, C.c_int]
     lib.occ_xc_cosx_grid_points.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
     lib.occ_xc_cosx_exchange.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp]
     lib.occ_xc_cosx_exchange_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -587,10 +588,11 @@ class SemiNumericalExchange:
     """occ::qm::cosx::SemiNumericalExchange with set_use_esp(true)
     (include/occ/qm/seminumerical_exchange.h:104-118): the seminumerical
     exchange matrix of a restricted density on its own grid
-    (GridSettings.for_sgx(50) unless given), FP64 on the GPU.  `dft` gives
+    (GridSettings.for_sgx(50) unless given), on the GPU in FP64 or with the
+    ESP integrals in FP32 (precision=MIXED).  `dft` gives
     the basis and the device (its XC grid is not used)."""
 
-    def __init__(self, dft, grid_settings=None):
+    def __init__(self, dft, grid_settings=None, precision=FP64):
         self.dft = dft
         self.ctx = dft.ctx
         gs = (grid_settings or GridSettings.for_sgx(50))._c()
@@ -599,6 +601,13 @@ class SemiNumericalExchange:
         if rc != 0:
             raise XCError(f"occ_xc_cosx_create failed ({rc}): {self.ctx.error()}", rc)
         self.h = h
+        self.set_precision(precision)
+
+    def set_precision(self, precision):
+        """FP64, or MIXED: the ESP integrals in FP32 (F, G, K in FP64)."""
+        rc = self.ctx.lib.occ_xc_cosx_set_precision(self.h, int(precision))
+        if rc != 0:
+            raise XCError(f"occ_xc_cosx_set_precision failed ({rc})", rc)
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -8,7 +8,8 @@ exchange matrix of the same density from four-centre integrals
 GridSettings::for_sgx(50) and (110)); its analytic overlap against that
 file's overlap, its AO values against the collocation oracle, and its grid
 against the library's host grid.
-GPU: the library's K against the oracle's at 1e-9 (FP64 throughout)."""
+GPU: the library's K against the oracle's at 1e-9 (FP64 throughout); the
+mixed precision (ESP integrals in FP32) against FP64."""
 import os
 import sys
 
@@ -189,3 +190,33 @@ def test_gpu_cosx_refuses_f_shells_and_bad_grid():
     dft = og.DFT("lda", b)
     with pytest.raises(og.XCError):
         og.SemiNumericalExchange(dft, og.GridSettings(max_angular_points=0))
+
+
+TOL_K_MIXED = 1e-6  # relative to max |K|: FP32 ESP integrals against FP64 (3e-8 measured)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["water_631g", "two_waters_svp"])
+def test_gpu_cosx_mixed_precision(case):
+    """The ESP integrals in FP32 (F, G, K' and the projector in FP64): K
+    against the FP64 build, far inside COSX's own error against exact
+    exchange (3e-4 of max |K| on water / 6-31G at for_sgx(50))."""
+    if case == "water_631g":
+        b, D, _, _ = _rhf_water_631g()
+    else:
+        atoms1, _ = _water()
+        atoms2, _ = _water(shift=(0.0, 0.0, 5.5))
+        b = og.AOBasis.load(atoms1 + atoms2, "def2-svp")
+        b.set_pure(True)
+        C = np.random.default_rng(7).normal(size=(b.nbf(), 10)) * 0.3
+        D = C @ C.T
+    dft = og.DFT("lda", b)
+    sgx = og.SemiNumericalExchange(dft, og.GridSettings.for_sgx(50))
+    K64 = sgx.compute_K(D)
+    sgx.set_precision(og.MIXED)
+    Km = sgx.compute_K(D)
+    assert np.abs(Km - Km.T).max() < 1e-14
+    rel = np.abs(Km - K64).max() / np.abs(K64).max()
+    assert rel <= TOL_K_MIXED, rel
+    sgx.set_precision(og.FP64)
+    assert np.abs(sgx.compute_K(D) - K64).max() < 1e-13

@@ -227,13 +227,52 @@ def test_tpss_mixed_water_cluster(basis_name, pure):
 
 @pytest.mark.gpu
 def test_tpss_entry_points_without_a_meta_gga_form_refuse():
+    """The unrestricted tensor-core XC gradient has no meta-GGA form."""
     b, D, _ = fchk_case()
     dft = og.DFT("tpss", b)
+    Dab = np.vstack([0.5 * D, 0.5 * D])
     with pytest.raises(og.XCError, match="meta-GGA"):
-        dft.compute_xc_gradient(D, og.MIXED)
+        dft.compute_xc_gradient(Dab, og.MIXED)
     # the FP64 build still works on the same molecule afterwards
     V = dft.compute_vxc(D)
     assert np.all(np.isfinite(V))
+
+
+TOL_G_MIXED = 3e-5  # Ha/Bohr, tensor-core XC gradient (as tests/test_xc_gradient.py)
+
+
+@pytest.mark.gpu
+def test_tpss_mixed_gradient_converged_water():
+    """The tensor-core meta-GGA gradient (tau term as three operand pairs of
+    the V_xc kernel per direction) against the oracle."""
+    b, D, _ = fchk_case()
+    dft = og.DFT("tpss", b)
+    g = dft.compute_xc_gradient(D, og.MIXED)
+    P, W = dft.grid()
+    g_ref = oracle.xc_gradient(b, P, W, D, "tpss")
+    assert np.max(np.abs(g - g_ref)) <= TOL_G_MIXED, np.max(np.abs(g - g_ref))
+    e_ref = oracle.xc_build(b, P, W, D, "tpss")[0]
+    assert abs(dft.exchange_correlation_energy() - e_ref) <= TOL_E_MIXED
+    # the meta build on the same molecule (its planes share the workspace)
+    Vm = dft.compute_vxc(D, og.MIXED)
+    _, V_ref, _ = oracle.xc_build(b, P, W, D, "tpss")
+    assert np.max(np.abs(Vm - V_ref)) <= TOL_V_MIXED
+    g2 = dft.compute_xc_gradient(D, og.MIXED)
+    assert np.max(np.abs(g2 - g)) < 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("basis_name,pure", [("def2-svp", True), ("6-31g(d,p)", False)])
+def test_tpss_mixed_gradient_water_cluster(basis_name, pure):
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(4, box=6.0, seed=3)
+    b = wl.basis_for(mol, basis_name, pure)
+    D = wl.random_density(b.nbf(), 20, seed=4)
+    dft = og.DFT("tpss", b)
+    g64 = dft.compute_xc_gradient(D, og.FP64)
+    gm = dft.compute_xc_gradient(D, og.MIXED)
+    scale = max(1.0, np.max(np.abs(g64)))
+    assert np.max(np.abs(gm - g64)) <= TOL_G_MIXED * scale, np.max(np.abs(gm - g64))
 
 
 @pytest.mark.gpu
