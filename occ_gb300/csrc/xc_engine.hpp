@@ -255,6 +255,7 @@ struct Molecule {
   // the same gradient with the contractions on the tensor cores (3xTF32)
   void xc_gradient_mixed(const double *dD, double *dgrad, double *dout2, cudaStream_t st);
   void xc_gradient_mixed_mgga(const double *dD, double *dgrad, double *dout2, cudaStream_t st);
+  void xc_gradient_uks_mixed_mgga(const double *dD, double *dgrad, double *dout3, cudaStream_t st);
   void grad_tables(GradMixed &g);
   void prepare_nlc();
   // VV10 energy (dE, one double) and, if dV, its V (nbf x nbf) for mo.D = dD;

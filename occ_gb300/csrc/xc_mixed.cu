@@ -3946,6 +3946,104 @@ void Molecule::build_mixed_uks_mgga(const double *dD, double *dV, double *dout3,
   P.ao_valid = true;
 }
 
+// The unrestricted meta-GGA XC gradient on the tensor cores
+// (accumulate_gradient_contribution_U<2>, src/dft/dft_gradient_kernels.cpp:
+// 175-470): per spin the meta plan's density and tau, the polarised functional
+// once, then per spin the operand planes (Y_s and t_k,s by k_ymix_mgga, Z_c,s
+// and the AO Hessian by k_grad_ops<true>), the two G_c launches per direction
+// of the restricted meta gradient and the contraction with that spin's block
+// and the reference's |D_a + D_b| skip rule.
+void Molecule::xc_gradient_uks_mixed_mgga(const double *dD, double *dgrad, double *dout3,
+                                          cudaStream_t st) {
+  prepare_gradient_mixed();
+  prepare_uks();
+  LaunchPlan &P = mmixed->plan;
+  GradMixed &g = *gmixed;
+  if (!d_uks_tabs_meta) {
+    MixTab tb = P.tabs[0];
+    tb.rho = d_rho_b;
+    tb.coef = d_coef_b;
+    d_uks_tabs_meta = alloc(sizeof(MixTab));
+    cuda_check(cudaMemcpy(d_uks_tabs_meta, &tb, sizeof(MixTab), cudaMemcpyHostToDevice),
+               "cudaMemcpy H2D");
+  }
+  const MixTab *tabs[2] = {P.d_tabs, static_cast<const MixTab *>(d_uks_tabs_meta)};
+  Context &c = *ctx;
+  int *err = mixed->d_err;
+  const size_t nbf = static_cast<size_t>(basis.nbf), nbf2 = nbf * nbf;
+  const int nb = static_cast<int>(P.blocks.size());
+  const int ni = static_cast<int>(P.items.size());
+  const int sms = this->ctas > 0 ? this->ctas
+                                 : (ctx->max_ctas > 0 ? ctx->max_ctas : num_sms(device));
+  const int gg = std::min(std::max(nb, 1), sms);
+  for (int s = 0; s < 2; s++)
+    cuda_check(cudaMemcpy2DAsync(d_Dab + s * nbf2, nbf * sizeof(double), dD + s * nbf,
+                                 2 * nbf * sizeof(double), nbf * sizeof(double), nbf,
+                                 cudaMemcpyDeviceToDevice, st),
+               "cudaMemcpy2DAsync");
+  cuda_check(cudaMemsetAsync(dgrad, 0, 3 * Z.size() * sizeof(double), st), "cudaMemsetAsync");
+  for (int s = 0; s < 2; s++) {
+    const Override ov{d_Dab + s * nbf2, nullptr, nullptr};
+    c.launch("prep_density", st, [&] {
+      k_prep_density<<<dim3(P.maxnbf, 1), 256, 0, st>>>(tabs[s], ov, P.d_queue);
+    });
+    if (nb == 0)
+      continue;
+    if (s == 0 && !P.ao_valid) {
+      c.launch("colloc_f32", st, [&] {
+        k_colloc_f32<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+      c.launch("meta_ops", st, [&] {
+        k_meta_ops<<<nb, kBlockPts, 0, st>>>(P.d_tabs, P.d_blocks);
+      });
+    }
+    c.launch("rho_mixed", st, [&] {
+      k_rho_mixed<true><<<gg, kRhoThreads, kRhoSmem, st>>>(tabs[s], P.d_blocks, P.d_order, nb,
+                                                     P.d_queue, err);
+    });
+    for (int k = 1; k <= 3; k++) {
+      cuda_check(cudaMemsetAsync(P.d_queue, 0, sizeof(int), st), "cudaMemsetAsync");
+      c.launch("tau_mixed", st, [&] {
+        k_rho_mixed<true, true><<<gg, kRhoThreads, kRhoSmem, st>>>(
+            tabs[s], P.d_blocks, P.d_order, nb, P.d_queue, err, k);
+      });
+    }
+  }
+  const MolDev m = dev();
+  c.launch("func_pol", st, [&] {
+    launch_func_pol(m, deriv, fs, bs.density_threshold, d_rho, d_rho_b, d_coef, d_coef_b,
+                    d_epart_u, st, true);
+  });
+  for (int s = 0; s < 2 && nb > 0; s++) {
+    const double *Ds = d_Dab + s * nbf2, *Do = d_Dab + (1 - s) * nbf2;
+    c.launch("ymix", st, [&] { k_ymix_mgga<<<nb, 256, 0, st>>>(tabs[s], P.d_blocks); });
+    c.launch("grad_ops", st, [&] {
+      k_grad_ops<true><<<nb, kBlockPts, 0, st>>>(tabs[s], P.d_blocks, 1);
+    });
+    cuda_check(cudaMemsetAsync(g.G, 0, 3 * nbf2 * sizeof(double), st), "cudaMemsetAsync");
+    for (int cc = 0; cc < 3 && ni > 0; cc++) {
+      const Override ovc{Ds, g.G + cc * nbf2, nullptr};
+      const VxcPlanes pls[2] = {
+          {1 + cc, kPlaneYHi, kPlaneMetaZ + cc, 0, 0, 0, 2},
+          {kPlaneMetaH + hess_index(cc, 0), kPlaneMetaT, kPlaneMetaH + hess_index(cc, 1),
+           kPlaneMetaT + 1, kPlaneMetaH + hess_index(cc, 2), kPlaneMetaT + 2, 3}};
+      for (int v = 0; v < 2; v++) {
+        cuda_check(cudaMemsetAsync(P.d_queue + 1, 0, sizeof(int), st), "cudaMemsetAsync");
+        c.launch(v == 0 ? "grad_vxc" : "grad_vxc_tau", st, [&] {
+          launch_vxc(P, std::min(ni, sms), st, tabs[s], P.d_blocks, P.d_items, ni, ovc,
+                     P.d_queue, err, P.tmap.rows32, P.tmap.rows128, pls[v]);
+        });
+      }
+    }
+    c.launch("grad_contract", st, [&] {
+      k_grad_contract<<<basis.nbf, 256, 0, st>>>(Ds, g.G, basis.nbf, g.ao_atom, dgrad, Do);
+    });
+  }
+  c.launch("reduce", st, [&] { launch_reduce3(d_epart_u, m.nleaves, dout3, st); });
+  cuda_check(cudaGetLastError(), "kernel launch");
+  P.ao_valid = true;
+}
+
 } // namespace occx
 
 // The unrestricted XC gradient on the tensor cores: the gradient plan per spin
@@ -3959,7 +4057,10 @@ namespace occx {
 
 void Molecule::xc_gradient_uks_mixed(const double *dD, double *dgrad, double *dout3,
                                      cudaStream_t st) {
-  require_not_mgga(deriv, "the unrestricted tensor-core XC gradient");
+  if (deriv == 2) {
+    xc_gradient_uks_mixed_mgga(dD, dgrad, dout3, st);
+    return;
+  }
   prepare_gradient_mixed();
   prepare_uks();
   GradMixed &g = *gmixed;

@@ -225,20 +225,27 @@ def test_tpss_mixed_water_cluster(basis_name, pure):
     assert np.max(np.abs(Vm - V64)) <= TOL_V_MIXED
 
 
-@pytest.mark.gpu
-def test_tpss_entry_points_without_a_meta_gga_form_refuse():
-    """The unrestricted tensor-core XC gradient has no meta-GGA form."""
-    b, D, _ = fchk_case()
-    dft = og.DFT("tpss", b)
-    Dab = np.vstack([0.5 * D, 0.5 * D])
-    with pytest.raises(og.XCError, match="meta-GGA"):
-        dft.compute_xc_gradient(Dab, og.MIXED)
-    # the FP64 build still works on the same molecule afterwards
-    V = dft.compute_vxc(D)
-    assert np.all(np.isfinite(V))
-
-
 TOL_G_MIXED = 3e-5  # Ha/Bohr, tensor-core XC gradient (as tests/test_xc_gradient.py)
+
+
+@pytest.mark.gpu
+def test_tpss_unrestricted_mixed_gradient():
+    """The unrestricted tensor-core meta-GGA gradient (per spin the restricted
+    meta gradient's operand pairs) against the FP64 one, an open shell and a
+    closed shell written as alpha = beta (equal to the restricted gradient)."""
+    from occ_gb300 import workloads as wl
+    mol = wl.water_cluster(3, box=5.0, seed=4)
+    b = wl.basis_for(mol, "def2-svp")
+    D = wl.random_density_unrestricted(b.nbf(), 15, 14, seed=9)
+    dft = og.DFT("tpss", b)
+    g64 = dft.compute_xc_gradient(D, og.FP64)
+    gm = dft.compute_xc_gradient(D, og.MIXED)
+    scale = max(1.0, np.max(np.abs(g64)))
+    assert np.max(np.abs(gm - g64)) <= TOL_G_MIXED * scale, np.max(np.abs(gm - g64))
+    Dr = wl.random_density(b.nbf(), 15, seed=9)
+    gr = dft.compute_xc_gradient(Dr, og.MIXED)
+    gu = dft.compute_xc_gradient(np.vstack([0.5 * Dr, 0.5 * Dr]), og.MIXED)
+    assert np.max(np.abs(gu - gr)) <= TOL_G_MIXED * max(1.0, np.max(np.abs(gr)))
 
 
 @pytest.mark.gpu
