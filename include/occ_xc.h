@@ -237,10 +237,9 @@ int occ_xc_compute_xc_gradient_device(occ_xc_context *ctx, occ_xc_molecule *mol,
  * (include/occ/dft/dft.h:599-749 with accumulate_gradient_contribution_U,
  * src/dft/dft_gradient_kernels.cpp:175-470, 549-575): D is OCC's unrestricted
  * mo.D (2 nbf x nbf, alpha block above beta, column-major); grad[3*natoms]
- * and exc as occ_xc_compute_xc_gradient.  precision OCC_XC_FP64 (LDA, GGA
- * and meta-GGA methods) or OCC_XC_MIXED (LDA and GGA: the contractions on the
- * tensor cores in 3xTF32; a meta-GGA method fails with OCC_XC_ERR_ARG).  Host
- * buffers; blocking. */
+ * and exc as occ_xc_compute_xc_gradient.  precision OCC_XC_FP64 or
+ * OCC_XC_MIXED (the contractions on the tensor cores in 3xTF32), for LDA, GGA
+ * and meta-GGA methods.  Host buffers; blocking. */
 int occ_xc_compute_xc_gradient_unrestricted(occ_xc_context *ctx, occ_xc_molecule *mol,
                                             const double *D, int precision, double *grad,
                                             double *exc);
