@@ -745,7 +745,7 @@ constexpr int kRhoN = 64;                                  // columns j per pass
 constexpr uint32_t kRhoStageB = 3 * (kRhoN * 128);        // B slices (64 x 64 BF16 each)
 constexpr uint32_t kRhoStage = kRhoStageA + kRhoStageB;   // 72 KB
 constexpr int kRhoStages = 2;
-constexpr int kRhoThreads = 480;
+constexpr int kRhoThreads = 512; // + the scheduler warp (15)
 constexpr int kRhoProd = 256;  // B producer threads (warps 4-11)
 constexpr int kRhoEpi = 128;   // epilogue threads (warps 0-3)
 constexpr int kRhoMap = 1024;  // AO maps up to this size are staged in shared memory
@@ -755,6 +755,19 @@ constexpr uint32_t kEpiPlaneBytes = kEpiCols * kBlockPts * 4;      // 8 KB
 constexpr uint32_t kEpiSlotBytes = 4 * kEpiPlaneBytes;             // phi and grad phi
 constexpr uint32_t kEpiBytes = kEpiSlots * kEpiSlotBytes;          // 64 KB
 
+// What every role needs of a block, resolved once by the scheduler warp.
+struct RhoInfo {
+  int bi; // block index; -1: the queue is exhausted
+  int mp, cnt, nbf_leaf, nbf;
+  const float *ws;   // the block's AO planes
+  const int *amap;   // the leaf's AO map
+  const float2 *dhl; // D2 as (hi, lo)
+  const float *colb; // D2's column bounds
+  double *rho;       // the density components
+  long long idx0;    // the block's first point in the molecule's grid
+  long long np;      // the molecule's points
+};
+
 struct alignas(16) RhoSmem {
   uint64_t full[kRhoStages], empty[kRhoStages]; // per stage: B written, MMAs done
   uint64_t afull[kRhoStages];                     // per stage: the A bulk copy landed
@@ -763,7 +776,7 @@ struct alignas(16) RhoSmem {
   uint64_t ifull[kRing], iempty[kRing];
   uint64_t done;
   uint32_t tmem_slot;
-  int ring[kRing];
+  RhoInfo info[kRing];
   int gmap[kRhoMap]; // the producers' current AO map
 };
 constexpr uint32_t kRhoSmem = kRhoStages * kRhoStage + kEpiBytes + sizeof(RhoSmem) + 1024;
@@ -816,7 +829,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     }
     for (int r = 0; r < kRing; r++) {
       umma::mbar_init(&sm->ifull[r], 1);
-      umma::mbar_init(&sm->iempty[r], 2 + kRhoProd + kRhoEpi);
+      umma::mbar_init(&sm->iempty[r], 3 + kRhoProd + kRhoEpi);
     }
     umma::mbar_init(&sm->done, 1);
     umma::fence_proxy_async();
@@ -845,37 +858,64 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
       ok = bar_all(2, kRhoProd, ok);
     return ok;
   };
-  auto next_block = [&](int k) {
+  // consumer side of the block ring: the next block's resolved description
+  // (false at the end of the queue or on a timed-out wait)
+  auto next_block = [&](int k, RhoInfo &w) {
     const int slot = k % kRing;
     wait(&sm->ifull[slot], (k / kRing) & 1);
     if (!agree())
-      return -1;
-    const int bi = sm->ring[slot];
+      return false;
+    w = sm->info[slot];
     umma::mbar_arrive(&sm->iempty[slot]);
-    return bi;
+    return w.bi >= 0;
   };
   auto segs = [](int mp) { return (mp + kExactKSeg - 1) / kExactKSeg; };
   auto seg_chunks = [](int mp, int k0) { return (min(kExactKSeg, mp - k0) + kKcR - 1) / kKcR; };
 
-  if (warp == 12) {
-    // ---- block fetch and A slices (lane 0) ----
+  if (warp == 15) {
+    // ---- scheduler (lane 0): blocks from the global queue, resolved into the
+    // ring up to kRing ahead of the slowest role ----
     if (lane == 0) {
-      uint32_t g = 0;
       for (int k = 0;; k++) {
         const int slot = k % kRing;
         if (k >= kRing && !wait(&sm->iempty[slot], ((k / kRing) - 1) & 1))
           break;
         const int qi = atomicAdd(&queue[0], 1);
-        const int bi = qi < nblocks ? order[qi] : -1;
-        sm->ring[slot] = bi;
+        RhoInfo w;
+        w.bi = qi < nblocks ? order[qi] : -1;
+        if (w.bi >= 0) {
+          const MBlock B = blocks[w.bi];
+          const MixTab &T = tabs[B.mol];
+          const DevLeaf L = T.m.leaves[B.leaf];
+          w.mp = B.mp;
+          w.cnt = B.cnt;
+          w.nbf_leaf = L.nbf;
+          w.nbf = T.m.nbf;
+          w.ws = T.ws + B.ws_off;
+          w.amap = T.m.leaf_ao + L.ao_begin;
+          w.dhl = T.dhl;
+          w.colb = T.colb;
+          w.rho = T.rho;
+          w.idx0 = static_cast<long long>(L.off) + B.p0;
+          w.np = T.m.npts;
+        }
+        sm->info[slot] = w;
         umma::mbar_arrive(&sm->ifull[slot]);
-        if (bi < 0)
+        if (w.bi < 0)
           break;
-        const MBlock B = blocks[bi];
-        const MixTab &T = tabs[B.mol];
+      }
+    }
+  } else if (warp == 12) {
+    // ---- A slices (lane 0) ----
+    if (lane == 0) {
+      uint32_t g = 0;
+      RhoInfo B;
+      for (int k = 0; ok; k++) {
+        if (!next_block(k, B))
+          break;
         const int aplane = TAU ? kPlaneTauA + 3 * (tk - 1) : kPlaneASlices;
         const uint8_t *as = reinterpret_cast<const uint8_t *>(
-            T.ws + B.ws_off + static_cast<size_t>(aplane) * B.mp * kBlockPts);
+            B.ws + static_cast<size_t>(aplane) * B.mp * kBlockPts);
         for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN)
           for (int k0 = 0; k0 < B.mp && ok; k0 += kExactKSeg)
             for (int c = 0; c < seg_chunks(B.mp, k0); c++, g++) {
@@ -900,29 +940,27 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     const int jr = pt & 63;        // row j of the B tile this thread fills
     const int qb = pt >> 6;        // first 16-byte chunk (0..3); then qb + 4
     uint32_t g = 0;
+    RhoInfo B;
     for (int k = 0; ok; k++) {
-      const int bi = next_block(k);
-      if (bi < 0)
+      if (!next_block(k, B))
         break;
-      const MBlock B = blocks[bi];
-      const MixTab &T = tabs[B.mol];
-      const DevLeaf L = T.m.leaves[B.leaf];
-      const int *gsrc = T.m.leaf_ao + L.ao_begin;
-      const bool gsh = L.nbf <= kRhoMap;
+      const int *gsrc = B.amap;
+      const int lnbf = B.nbf_leaf;
+      const bool gsh = lnbf <= kRhoMap;
       if (gsh) {
         bar_named(2, kRhoProd);
-        for (int q = pt; q < L.nbf; q += kRhoProd)
+        for (int q = pt; q < lnbf; q += kRhoProd)
           sm->gmap[q] = gsrc[q];
         bar_named(2, kRhoProd);
       }
       const int *gm = gsh ? sm->gmap : gsrc;
-      const float2 *__restrict__ dhl = T.dhl;
-      const size_t nbf = static_cast<size_t>(T.m.nbf);
+      const float2 *__restrict__ dhl = B.dhl;
+      const size_t nbf = static_cast<size_t>(B.nbf);
       for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN) {
         const int lj = n0 + jr;
-        const bool jv = lj < L.nbf;
+        const bool jv = lj < lnbf;
         const size_t gj = jv ? static_cast<size_t>(gm[lj]) : 0;
-        const float sB = jv ? T.colb[gj] : 1.f, isB = 1.f / sB;
+        const float sB = jv ? B.colb[gj] : 1.f, isB = 1.f / sB;
         // the pass's K chunks of 64 AOs in the order of the segments and
         // chunks the loader and the MMA issuer walk; each chunk's gathers
         // are issued one chunk ahead, so that their latency overlaps the
@@ -934,8 +972,8 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 #pragma unroll
             for (int e = 0; e < 8; e++) {
               const int lk = q * kKcR + (qb + 4 * r) * 8 + e;
-              d[r][e] = (jv && lk < L.nbf) ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
-                                           : make_float2(0.f, 0.f);
+              d[r][e] = (jv && lk < lnbf) ? dhl[static_cast<size_t>(gm[lk]) * nbf + gj]
+                                          : make_float2(0.f, 0.f);
             }
         };
         float2 cur[2][8], nxt[2][8];
@@ -974,11 +1012,11 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     if (lane == 0) {
       uint32_t g = 0, sc = 0; // chunks, segments
       bool issued = false;
+      RhoInfo B;
       for (int k = 0; ok; k++) {
-        const int bi = next_block(k);
-        if (bi < 0)
+        if (!next_block(k, B))
           break;
-        const int mp = blocks[bi].mp;
+        const int mp = B.mp;
         for (int n0 = 0; n0 < mp && ok; n0 += kRhoN) {
           const int N = min(kRhoN, mp - n0);
           const uint32_t idesc = umma::idesc_bf16(128, N);
@@ -1033,14 +1071,12 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     // pass into a slot, in the order the epilogue consumes them ----
     if (lane == 0) {
       uint32_t e = 0; // slots filled
+      RhoInfo B;
       for (int k = 0; ok; k++) {
-        const int bi = next_block(k);
-        if (bi < 0)
+        if (!next_block(k, B))
           break;
-        const MBlock B = blocks[bi];
-        const MixTab &T = tabs[B.mol];
         const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
-        const float *src = T.ws + B.ws_off + (TAU ? tk * plane : 0);
+        const float *src = B.ws + (TAU ? tk * plane : 0);
         for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN) {
           const int N = min(kRhoN, B.mp - n0);
           for (int k0 = 0; k0 < B.mp && ok; k0 += kExactKSeg)
@@ -1066,12 +1102,10 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
     const int quad = warp;
     const int p = t;
     uint32_t sc = 0, e = 0; // segments, epilogue slots consumed
+    RhoInfo B;
     for (int k = 0; ok; k++) {
-      const int bi = next_block(k);
-      if (bi < 0)
+      if (!next_block(k, B))
         break;
-      const MBlock B = blocks[bi];
-      const MixTab &T = tabs[B.mol];
       float acc[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
       for (int n0 = 0; n0 < B.mp && ok; n0 += kRhoN) {
         const int N = min(kRhoN, B.mp - n0);
@@ -1119,16 +1153,16 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
         }
       }
       if (ok && p < B.cnt) {
-        const size_t idx = static_cast<size_t>(T.m.leaves[B.leaf].off) + B.p0 + p;
-        const size_t Np = static_cast<size_t>(T.m.npts);
+        const size_t idx = static_cast<size_t>(B.idx0) + p;
+        const size_t Np = static_cast<size_t>(B.np);
         if (TAU) {
-          T.rho[(3 + tk) * Np + idx] = static_cast<double>(acc[0]) + static_cast<double>(cmp[0]);
+          B.rho[(3 + tk) * Np + idx] = static_cast<double>(acc[0]) + static_cast<double>(cmp[0]);
           continue;
         }
-        T.rho[idx] = static_cast<double>(acc[0]) + static_cast<double>(cmp[0]);
+        B.rho[idx] = static_cast<double>(acc[0]) + static_cast<double>(cmp[0]);
         if (DERIV)
           for (int c = 1; c < 4; c++)
-            T.rho[c * Np + idx] = 2.0 * (static_cast<double>(acc[c]) + static_cast<double>(cmp[c]));
+            B.rho[c * Np + idx] = 2.0 * (static_cast<double>(acc[c]) + static_cast<double>(cmp[c]));
       }
     }
   }
