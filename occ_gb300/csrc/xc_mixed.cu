@@ -1175,7 +1175,7 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 // ---- V_xc: K = phi^T Y on tcgen05, operands staged by TMA ------------------
 // One CTA per SM, persistent over V items (AO rows i0 .. i0 + 127 of the
 // blocks of one leaf; K = their points) fetched from a global queue by a
-// scheduler warp (14), which resolves each item (sizes, workspace rows, AO
+// scheduler warp (kVxcSchedWarp), which resolves each item (sizes, workspace rows, AO
 // map, output) and hands it to the roles through a ring in shared memory,
 // up to four items ahead:
 //   warp 8       TMA producer: per K chunk of 32 points the FP32 A rows
@@ -1202,8 +1202,10 @@ __global__ void __launch_bounds__(kRhoThreads, 1)
 // the error flag is set and all roles leave.
 constexpr int kItemBlocks = 2;   // blocks of a leaf accumulated in one V item
 constexpr int kVxcEpi = 256;     // epilogue threads (warps 0-7)
-constexpr int kVxcConv = 128;    // split threads (warps 10-13)
-constexpr int kVxcThreads = 480; // + TMA warp 8, MMA warp 9, split warps, scheduler warp 14
+constexpr int kVxcConvWarps = 4;                 // split warps (10 .. 10 + kVxcConvWarps - 1)
+constexpr int kVxcConv = 32 * kVxcConvWarps;      // split threads
+constexpr int kVxcSchedWarp = 10 + kVxcConvWarps; // the scheduler warp
+constexpr int kVxcThreads = 32 * (kVxcSchedWarp + 1); // + TMA warp 8, MMA warp 9
 // The stages share 192 KB: two of 96 KB for tiles of up to 256 columns
 // (k_vxc_tma<2>), or three of 64 KB for tiles of up to 128 columns
 // (k_vxc_tma<3>), which keeps one more chunk in flight.
@@ -1330,10 +1332,10 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     return ok;
   };
   // the epilogue and split warps work warp by warp, with no barrier between
-  // warps (the epilogue reads the AO map through L1, the split warps each
-  // release their share of a stage): the threads of a warp, which issue
+  // warps (the epilogue shares each step's column AOs by shuffles, the split
+  // warps each release their share of a stage): the threads of a warp, which issue
   // warp-collective TMEM loads, take every decision to stop together
-  const bool epi = warp < 8, cv = warp >= 10 && warp < 14;
+  const bool epi = warp < 8, cv = warp >= 10 && warp < kVxcSchedWarp;
   auto agree = [&] {
     if (epi || cv)
       ok = __all_sync(0xffffffffu, ok);
@@ -1351,7 +1353,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     return w.it >= 0;
   };
 
-  if (warp == 14) {
+  if (warp == kVxcSchedWarp) {
     // ---- scheduler (lane 0): items from the global queue, resolved into the
     // ring up to kRing ahead of the slowest role ----
     if (lane == 0) {
@@ -1480,7 +1482,7 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
       }
     }
   } else if (cv) {
-    // ---- TF32 split (warps 10-13) ----
+    // ---- TF32 split (warps 10 .. kVxcSchedWarp - 1) ----
     {
       const int ct = t - 10 * 32;
       uint32_t g = 0; // chunks split
