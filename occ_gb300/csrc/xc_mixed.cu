@@ -1681,7 +1681,8 @@ __device__ __forceinline__ void ymix_stream(const MixTab &T, const MBlock &B,
 
 // The build's functional stage (one CTA per leaf item, four per SM): the
 // functional in double-float arithmetic (leaf_functional_f2, no FP64
-// operation per point) with the coefficients as FP32 into shared memory, then
+// operation per point but VWN's atan and B88's asinh) with the coefficients
+// as FP32 into shared memory, then
 // the V_xc operand Y of each of the leaf's blocks from them (ymix_stream, one
 // FP32 plane: k_vxc_tma forms hi and lo).  The FP64 coefficient
 // array is not written.
