@@ -59,6 +59,14 @@ __constant__ int c_cx_comp[3][kCosxNc];
 // Real solid-harmonic transforms (m = -l..l) of l = 0..2, T[f][i], and the
 // identity for Cartesian shells.
 __constant__ double c_cx_T[3][5][kCosxNc];
+__constant__ float c_cx_Tf[3][5][kCosxNc]; // the same in FP32 (the mixed precision)
+template <typename R> __device__ __forceinline__ R sph_t(int l, int f, int i);
+template <> __device__ __forceinline__ double sph_t<double>(int l, int f, int i) {
+  return c_cx_T[l][f][i];
+}
+template <> __device__ __forceinline__ float sph_t<float>(int l, int f, int i) {
+  return c_cx_Tf[l][f][i];
+}
 
 struct CxPair {
   double Pc[3], ext;        // centre and extent of the most diffuse primitive pair
@@ -248,7 +256,7 @@ __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restri
 // when pure.
 template <typename Rt, int LA, int LB>
 __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restrict__ prims,
-                                          const double *__restrict__ etab, const Pt4 &C, bool pure,
+                                          const Rt *__restrict__ etab, const Pt4 &C, bool pure,
                                           const double *__restrict__ Fg, double *__restrict__ Gg) {
   constexpr int NCA = (LA + 1) * (LA + 2) / 2, NCB = (LB + 1) * (LB + 2) / 2;
   constexpr int L2 = LA + LB, NA = LA + 1, NB = LB + 1, NT = L2 + 1;
@@ -264,15 +272,15 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
     Rt R[NR];
     hermite_r_t<Rt, L2>(static_cast<Rt>(Q.pexp), static_cast<Rt>(Q.P[0] - C.x),
                         static_cast<Rt>(Q.P[1] - C.y), static_cast<Rt>(Q.P[2] - C.z), R);
-    const double *Ex = etab + Q.e_off, *Ey = Ex + NA * NB * NT, *Ez = Ey + NA * NB * NT;
+    const Rt *Ex = etab + Q.e_off, *Ey = Ex + NA * NB * NT, *Ez = Ey + NA * NB * NT;
 #pragma unroll
     for (int i = 0; i < NCA; i++) {
       const int ax = cca_pow(LA, i, 0), ay = cca_pow(LA, i, 1), az = cca_pow(LA, i, 2);
 #pragma unroll
       for (int j = 0; j < NCB; j++) {
         const int bx = cca_pow(LB, j, 0), by = cca_pow(LB, j, 1), bz = cca_pow(LB, j, 2);
-        const double *ex = Ex + (ax * NB + bx) * NT, *ey = Ey + (ay * NB + by) * NT,
-                     *ez = Ez + (az * NB + bz) * NT;
+        const Rt *ex = Ex + (ax * NB + bx) * NT, *ey = Ey + (ay * NB + by) * NT,
+                 *ez = Ez + (az * NB + bz) * NT;
         Rt acc = Rt(0);
         // compile-time trip counts (L2) with the exponent bounds as guards,
         // so that every R index is a constant and R stays in registers
@@ -282,74 +290,80 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
           for (int u = 0; u <= L2 - t; u++) {
             if (t > ax + bx || u > ay + by)
               continue;
-            const Rt exy = static_cast<Rt>(ex[t]) * static_cast<Rt>(ey[u]);
+            const Rt exy = ex[t] * ey[u];
 #pragma unroll
             for (int v = 0; v <= L2 - t - u; v++)
               if (v <= az + bz)
-                acc = fma(exy * static_cast<Rt>(ez[v]), R[r_index(t, u, v)], acc);
+                acc = fma(exy * ez[v], R[r_index(t, u, v)], acc);
           }
         V[i][j] = fma(static_cast<Rt>(Q.pref), acc, V[i][j]);
       }
     }
   }
-  // the shells' functions: NFA / NFB of them, pure (2l + 1) or Cartesian
+  // the shells' functions: NFA / NFB of them, pure (2l + 1) or Cartesian;
+  // the contraction with F in the ESP integrals' precision, G accumulated
+  // in FP64
   const int nfa = pure ? 2 * LA + 1 : NCA, nfb = pure ? 2 * LB + 1 : NCB;
-  auto ta = [&](int f, int i) { return pure ? c_cx_T[LA][f < 5 ? f : 4][i] : (f == i ? 1.0 : 0.0); };
-  auto tb = [&](int h, int j) { return pure ? c_cx_T[LB][h < 5 ? h : 4][j] : (h == j ? 1.0 : 0.0); };
-  double Fc[NCA], Gc[NCB];
+  auto ta = [&](int f, int i) {
+    return pure ? sph_t<Rt>(LA, f < 5 ? f : 4, i) : (f == i ? Rt(1) : Rt(0));
+  };
+  auto tb = [&](int h, int j) {
+    return pure ? sph_t<Rt>(LB, h < 5 ? h : 4, j) : (h == j ? Rt(1) : Rt(0));
+  };
+  Rt Fc[NCA], Gc[NCB];
 #pragma unroll
   for (int i = 0; i < NCA; i++) {
-    double s = 0.0;
+    Rt s = Rt(0);
 #pragma unroll
     for (int f = 0; f < NCA; f++)
       if (f < nfa)
-        s = fma(Fg[P.bf_p + f], ta(f, i), s);
+        s = fma(static_cast<Rt>(Fg[P.bf_p + f]), ta(f, i), s);
     Fc[i] = s;
   }
 #pragma unroll
   for (int j = 0; j < NCB; j++) {
-    double s = 0.0;
+    Rt s = Rt(0);
 #pragma unroll
     for (int i = 0; i < NCA; i++)
-      s = fma(Fc[i], static_cast<double>(V[i][j]), s);
+      s = fma(Fc[i], V[i][j], s);
     Gc[j] = s;
   }
 #pragma unroll
   for (int h = 0; h < NCB; h++)
     if (h < nfb) {
-      double s = 0.0;
+      Rt s = Rt(0);
 #pragma unroll
       for (int j = 0; j < NCB; j++)
         s = fma(tb(h, j), Gc[j], s);
-      Gg[P.bf_q + h] -= s;
+      Gg[P.bf_q + h] -= static_cast<double>(s);
     }
   if (P.bf_p != P.bf_q) {
-    double Fq[NCB], Gp[NCA];
+    Rt Fq[NCB], Gp[NCA];
 #pragma unroll
     for (int j = 0; j < NCB; j++) {
-      double s = 0.0;
+      Rt s = Rt(0);
 #pragma unroll
       for (int h = 0; h < NCB; h++)
         if (h < nfb)
-          s = fma(Fg[P.bf_q + h], tb(h, j), s);
+          s = fma(static_cast<Rt>(Fg[P.bf_q + h]), tb(h, j), s);
       Fq[j] = s;
     }
 #pragma unroll
     for (int i = 0; i < NCA; i++) {
-      double s = 0.0;
+      Rt s = Rt(0);
 #pragma unroll
       for (int j = 0; j < NCB; j++)
-        s = fma(static_cast<double>(V[i][j]), Fq[j], s);
+        s = fma(V[i][j], Fq[j], s);
       Gp[i] = s;
     }
 #pragma unroll
     for (int f = 0; f < NCA; f++)
       if (f < nfa) {
-        double s = 0.0;
+        Rt s = Rt(0);
 #pragma unroll
         for (int i = 0; i < NCA; i++)
           s = fma(ta(f, i), Gp[i], s);
-        Gg[P.bf_p + f] -= s;
+        Gg[P.bf_p + f] -= static_cast<double>(s);
       }
   }
 }
@@ -360,7 +374,7 @@ template <typename Rt>
 __device__ __forceinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int p, int off0,
                                           int npairs, const CxPair *__restrict__ pairs,
                                           const CxPrim *__restrict__ prims,
-                                          const double *__restrict__ etab,
+                                          const Rt *__restrict__ etab,
                                           const int *__restrict__ mask, double4 geo, int pure,
                                           const double *__restrict__ F, double *__restrict__ G) {
   const Pt4 C = m.pts[L.off + p];
@@ -396,7 +410,7 @@ template <typename Rt>
 __global__ void __launch_bounds__(128, 1) k_cosx_g(MolDev m, int l0, int off0, int npairs,
                                                 const CxPair *__restrict__ pairs,
                                                 const CxPrim *__restrict__ prims,
-                                                const double *__restrict__ etab,
+                                                const Rt *__restrict__ etab,
                                                 const int *__restrict__ mask,
                                                 const double4 *__restrict__ lgeo, int pure,
                                                 const double *__restrict__ F,
@@ -579,6 +593,7 @@ struct CosxState {
   size_t group_pts_max = 0;
   double *d_Q = nullptr, *d_D = nullptr, *d_D2q = nullptr, *d_Kp = nullptr, *d_K = nullptr;
   double *d_F = nullptr, *d_G = nullptr, *d_etab = nullptr;
+  float *d_etab_f = nullptr; // the E coefficients in FP32 (the mixed precision)
   CxPair *d_pairs = nullptr;
   CxPrim *d_prims = nullptr;
   int *d_mask = nullptr;
@@ -624,6 +639,12 @@ void upload_cosx_tables() {
   }
   cuda_check(cudaMemcpyToSymbol(c_cx_comp, comp, sizeof(comp)), "cudaMemcpyToSymbol");
   cuda_check(cudaMemcpyToSymbol(c_cx_T, T, sizeof(T)), "cudaMemcpyToSymbol");
+  float Tf[3][5][kCosxNc];
+  for (int l = 0; l < 3; l++)
+    for (int f = 0; f < 5; f++)
+      for (int i = 0; i < kCosxNc; i++)
+        Tf[l][f][i] = static_cast<float>(T[l][f][i]);
+  cuda_check(cudaMemcpyToSymbol(c_cx_Tf, Tf, sizeof(Tf)), "cudaMemcpyToSymbol");
   double inv[kBoysTable];
   for (int i = 0; i < kBoysTable; i++)
     inv[i] = 1.0 / (2 * i + 1);
@@ -751,6 +772,9 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
   S->allocations.push_back(S->d_prims);
   S->d_etab = dev_upload(et, bytes);
   S->allocations.push_back(S->d_etab);
+  const std::vector<float> etf(et.begin(), et.end());
+  S->d_etab_f = dev_upload(etf, bytes);
+  S->allocations.push_back(S->d_etab_f);
   S->d_mask = S->alloc<int>(pairs.size());
   // bounding spheres of the leaves kept by the plan (those with AOs)
   std::vector<double4> lgeo;
@@ -816,7 +840,7 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
     c.launch("cosx_g", st, [&] {
       if (S.precision == OCC_XC_MIXED)
         k_cosx_g<float><<<nl, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
-                                            S.d_etab, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
+                                            S.d_etab_f, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
                                             S.d_F, S.d_G);
       else
         k_cosx_g<double><<<nl, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
