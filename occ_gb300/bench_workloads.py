@@ -529,11 +529,6 @@ def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
     dV = torch.zeros_like(dD)
     d2 = torch.zeros(2, dtype=torch.float64, device="cuda")
     stream = torch.cuda.Stream()
-    lib.occ_xc_profile_enable.argtypes = [C.c_void_p, C.c_int]
-    lib.occ_xc_profile_reset.argtypes = [C.c_void_p]
-    lib.occ_xc_profile_count.argtypes = [C.c_void_p]
-    lib.occ_xc_profile_entry.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_char_p),
-                                         C.POINTER(C.c_double), C.POINTER(C.c_long)]
     out = {"workload": f"water{waters}_def2svp_tpss", "nbf": nbf,
            "npoints": int(dft.info()["npoints"])}
     res = {}
@@ -561,17 +556,7 @@ def mgga_build(torch, steps=5, warmup=2, waters=32, seed=0, oracle_check=True):
         e2e_ms = (time.perf_counter() - t0) / steps * 1e3
         res[name] = (dft.exchange_correlation_energy(), V)
         # per-kernel device time (the library's CUDA-event profiler), two builds
-        lib.occ_xc_profile_reset(dft.ctx.h)
-        lib.occ_xc_profile_enable(dft.ctx.h, 1)
-        for _ in range(2):
-            dft.compute_vxc(D, prec)
-        prof = {}
-        for i in range(lib.occ_xc_profile_count(dft.ctx.h)):
-            kname, kms, cnt = C.c_char_p(), C.c_double(), C.c_long()
-            lib.occ_xc_profile_entry(dft.ctx.h, i, C.byref(kname), C.byref(kms), C.byref(cnt))
-            prof[kname.value.decode()] = kms.value / 2
-        lib.occ_xc_profile_enable(dft.ctx.h, 0)
-        lib.occ_xc_profile_reset(dft.ctx.h)
+        prof = _kernel_profile(dft.ctx, lambda: dft.compute_vxc(D, prec))
         out[name] = {"builds_per_s": 1e3 / ms, "ms_per_build": ms, "exc": res[name][0],
                      "kernels_ms_per_build": prof,
                      "e2e": {"value": 1e3 / e2e_ms, "unit": "builds/s",
@@ -682,6 +667,29 @@ def vv10(steps=3, warmup=1, waters=32, seed=0):
     return out
 
 
+def _kernel_profile(ctx, call, n=2):
+    """Per-kernel device time (ms per call) of n calls, from the library's
+    CUDA-event profiler."""
+    lib = ctx.lib
+    lib.occ_xc_profile_enable.argtypes = [C.c_void_p, C.c_int]
+    lib.occ_xc_profile_reset.argtypes = [C.c_void_p]
+    lib.occ_xc_profile_count.argtypes = [C.c_void_p]
+    lib.occ_xc_profile_entry.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_char_p),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_long)]
+    lib.occ_xc_profile_reset(ctx.h)
+    lib.occ_xc_profile_enable(ctx.h, 1)
+    for _ in range(n):
+        call()
+    prof = {}
+    for i in range(lib.occ_xc_profile_count(ctx.h)):
+        kname, kms, cnt = C.c_char_p(), C.c_double(), C.c_long()
+        lib.occ_xc_profile_entry(ctx.h, i, C.byref(kname), C.byref(kms), C.byref(cnt))
+        prof[kname.value.decode()] = kms.value / n
+    lib.occ_xc_profile_enable(ctx.h, 0)
+    lib.occ_xc_profile_reset(ctx.h)
+    return prof
+
+
 def cosx(torch, steps=3, warmup=1, waters=8, seed=0, angular=50):
     """Seminumerical (COSX) exchange of a water cluster (def2-SVP, pure d
     shells) on the grid of GridSettings.for_sgx(angular), FP64: calls/s
@@ -722,7 +730,8 @@ def cosx(torch, steps=3, warmup=1, waters=8, seed=0, angular=50):
         e2e_s = (time.perf_counter() - t0) / steps
         Kd = dK.cpu().numpy().reshape(nbf, nbf, order="F")
         Ks[name] = K
-        out[name] = {"calls_per_s": 1e3 / ms, "ms_per_call": ms,
+        prof = _kernel_profile(dft.ctx, lambda: sgx.compute_K(D))
+        out[name] = {"calls_per_s": 1e3 / ms, "ms_per_call": ms, "kernels_ms_per_call": prof,
                      "e2e": {"value": 1.0 / e2e_s, "unit": "calls/s",
                              "h2d_bytes_per_step": int(D.nbytes),
                              "d2h_bytes_per_step": int(K.nbytes)},

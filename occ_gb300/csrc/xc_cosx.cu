@@ -21,16 +21,20 @@
 //   k_cosx_d2q    D2q = Q (2 D), row-major
 //   k_cosx_mask   shell pair (p, q) kept when max |D2q| over its two blocks
 //                 reaches 1e-6 (the reference's density screen)
-//   per group of batches (a workspace cap bounds the point-major F and G):
-//   k_cosx_f      F[g, lambda] = w_g sum_sigma phi_sigma(g) D2q[sigma, lambda]
-//   k_cosx_g      G[g, nu] -= sum_mu F[g, mu] V_g(mu, nu) (and the transposed
+//   per group of batches (a workspace cap bounds F and G, both AO-major:
+//   row lambda, one column per point of the group):
+//   k_cosx_f      F[lambda, g] = w_g sum_sigma phi_sigma(g) D2q[sigma, lambda]
+//   k_cosx_g      G[nu, g] -= sum_mu F[mu, g] V_g(mu, nu) (and the transposed
 //                 block for p != q), V_g(mu, nu) = int phi_mu phi_nu / |r - g|
 //                 by McMurchie-Davidson over the Boys function, one thread
-//                 per grid point, every kept pair that passes the batch's
-//                 geometric screen (|P - c| - extent < radius + 1 Bohr)
-//   k_cosx_k      K'[mu, lambda] -= sum_g phi_mu(g) G[g, lambda]
+//                 per grid point, the kept pairs that pass the batch's
+//                 geometric screen (|P - c| - extent < radius + 1 Bohr) split
+//                 into slices over the blocks of a batch
+//   k_cosx_k      K'[mu, lambda] -= sum_g phi_mu(g) G[lambda, g]
 //   k_cosx_sym    K = (K' + K'^T) / 4
-// All in FP64.  Shells up to d.
+// All in FP64, except under OCC_XC_MIXED the ESP integrals (E coefficients,
+// Boys function, R_tuv) and their contraction with F, in FP32; G is summed in
+// FP64 either way.  Shells up to d.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -50,6 +54,9 @@ constexpr int kCosxNc = 6;                     // Cartesian components of a d sh
 constexpr int kCosxR = 35;                     // R_tuv with t + u + v <= 4
 constexpr double kCosxDensityThreshold = 1e-6; // seminumerical_exchange.cpp:789
 constexpr double kCosxMargin = 1.0;            // cosx::Settings::margin (Bohr)
+constexpr int kCosxAoTile = 16;                // AOs lambda per block of the F and K kernels
+constexpr int kCosxTargetBlocks = 152 * 8;     // G kernel: blocks to aim for (8 per SM)
+constexpr int kCosxMaxSlices = 32;             // G kernel: most pair slices per leaf
 constexpr double kCosxLogThreshold = 27.631021115928547; // -ln(1e-12): pair extents
 constexpr double kCosxPairOverlap = 1e-12;     // IntegralEngine::compute_shellpairs
 constexpr double kPi = 3.14159265358979323846;
@@ -227,24 +234,39 @@ __global__ void k_cosx_mask(int npairs, int nbf, const CxPair *__restrict__ pair
   mask[k] = mx >= kCosxDensityThreshold ? 1 : 0;
 }
 
-// F[g, lambda] for the points of leaves l0 .. l0 + gridDim.x - 1 (g counted
-// from the group's first point off0); thread lambda.
+// F[lambda, g] = w_g sum_sigma phi_sigma(g) D2q[sigma, lambda] for the
+// points of leaf l0 + blockIdx.x (g counted from the group's first point off0,
+// row stride ld) and the kCosxAoTile AOs lambda of blockIdx.y; a thread per
+// point.
 __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restrict__ ws, int l0,
-                                                int off0, const double *__restrict__ D2q,
+                                                int off0, size_t ld,
+                                                const double *__restrict__ D2q,
                                                 double *__restrict__ F) {
   const DevLeaf L = m.leaves[l0 + blockIdx.x];
-  const int lam = blockIdx.y * blockDim.x + threadIdx.x;
-  if (lam >= m.nbf)
-    return;
+  const int lam0 = blockIdx.y * kCosxAoTile;
+  const int nl = min(kCosxAoTile, m.nbf - lam0);
   const double *phi = ws + L.ws_off;
   const int *g = m.leaf_ao + L.ao_begin;
   const size_t nbf = static_cast<size_t>(m.nbf);
-  for (int p = 0; p < L.cnt; p++) {
-    double acc = 0.0;
-    for (int s = 0; s < L.nbf; s++)
-      acc = fma(phi[static_cast<size_t>(s) * L.npad + p], D2q[static_cast<size_t>(g[s]) * nbf + lam],
-                acc);
-    F[static_cast<size_t>(L.off - off0 + p) * nbf + lam] = m.pts[L.off + p].w * acc;
+  for (int p = threadIdx.x; p < L.cnt; p += blockDim.x) {
+    double acc[kCosxAoTile];
+#pragma unroll
+    for (int j = 0; j < kCosxAoTile; j++)
+      acc[j] = 0.0;
+    for (int s = 0; s < L.nbf; s++) {
+      const double ph = phi[static_cast<size_t>(s) * L.npad + p];
+      const double *d = D2q + static_cast<size_t>(g[s]) * nbf + lam0;
+#pragma unroll
+      for (int j = 0; j < kCosxAoTile; j++)
+        if (j < nl)
+          acc[j] = fma(ph, d[j], acc[j]);
+    }
+    const double w = m.pts[L.off + p].w;
+    const size_t col = static_cast<size_t>(L.off - off0 + p);
+#pragma unroll
+    for (int j = 0; j < kCosxAoTile; j++)
+      if (j < nl)
+        F[(lam0 + j) * ld + col] = w * acc[j];
   }
 }
 
@@ -257,7 +279,8 @@ __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restri
 template <typename Rt, int LA, int LB>
 __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restrict__ prims,
                                           const Rt *__restrict__ etab, const Pt4 &C, bool pure,
-                                          const double *__restrict__ Fg, double *__restrict__ Gg) {
+                                          const double *__restrict__ Fg, double *__restrict__ Gg,
+                                          size_t ld) {
   constexpr int NCA = (LA + 1) * (LA + 2) / 2, NCB = (LB + 1) * (LB + 2) / 2;
   constexpr int L2 = LA + LB, NA = LA + 1, NB = LB + 1, NT = L2 + 1;
   constexpr int NR = (L2 + 1) * (L2 + 2) * (L2 + 3) / 6;
@@ -317,7 +340,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 #pragma unroll
     for (int f = 0; f < NCA; f++)
       if (f < nfa)
-        s = fma(static_cast<Rt>(Fg[P.bf_p + f]), ta(f, i), s);
+        s = fma(static_cast<Rt>(Fg[(P.bf_p + f) * ld]), ta(f, i), s);
     Fc[i] = s;
   }
 #pragma unroll
@@ -335,7 +358,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 #pragma unroll
       for (int j = 0; j < NCB; j++)
         s = fma(tb(h, j), Gc[j], s);
-      Gg[P.bf_q + h] -= static_cast<double>(s);
+      atomicAdd(Gg + (P.bf_q + h) * ld, -static_cast<double>(s));
     }
   if (P.bf_p != P.bf_q) {
     Rt Fq[NCB], Gp[NCA];
@@ -345,7 +368,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 #pragma unroll
       for (int h = 0; h < NCB; h++)
         if (h < nfb)
-          s = fma(static_cast<Rt>(Fg[P.bf_q + h]), tb(h, j), s);
+          s = fma(static_cast<Rt>(Fg[(P.bf_q + h) * ld]), tb(h, j), s);
       Fq[j] = s;
     }
 #pragma unroll
@@ -363,81 +386,113 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 #pragma unroll
         for (int i = 0; i < NCA; i++)
           s = fma(ta(f, i), Gp[i], s);
-        Gg[P.bf_p + f] -= static_cast<double>(s);
+        atomicAdd(Gg + (P.bf_p + f) * ld, -static_cast<double>(s));
       }
   }
 }
 
-// G[g, :] of one point g: every kept shell pair's ESP block V_g and its
-// two updates.
+// G for one leaf's points and one slice of the shell pairs (pairs k with
+// k = blockIdx.y mod gridDim.y), a thread per point.  The block screens 128
+// candidate pairs at a time, once for all its points (the density mask and
+// the batch's geometric screen, seminumerical_exchange.cpp:789-799), and
+// compacts the survivors into shared memory in pair order; every thread then
+// runs them at its point.  F and G are AO-major (row lambda, column the
+// group's point, row stride ld); the slices of a leaf add into G by atomics.
+// In FP32 the bounds give 168 registers and three blocks per SM without
+// spills; the FP64 form needs the full register file.
 template <typename Rt>
-__device__ __forceinline__ void cosx_g_point(const MolDev &m, const DevLeaf &L, int p, int off0,
-                                          int npairs, const CxPair *__restrict__ pairs,
-                                          const CxPrim *__restrict__ prims,
-                                          const Rt *__restrict__ etab,
-                                          const int *__restrict__ mask, double4 geo, int pure,
-                                          const double *__restrict__ F, double *__restrict__ G) {
-  const Pt4 C = m.pts[L.off + p];
-  const size_t nbf = static_cast<size_t>(m.nbf);
-  const double *Fg = F + static_cast<size_t>(L.off - off0 + p) * nbf;
-  double *Gg = G + static_cast<size_t>(L.off - off0 + p) * nbf;
-  for (int k = 0; k < npairs; k++) {
-    if (!mask[k])
-      continue;
-    const CxPair P = pairs[k];
-    // the batch's geometric screen (seminumerical_exchange.cpp:793-799)
-    {
-      const double dx = P.Pc[0] - geo.x, dy = P.Pc[1] - geo.y, dz = P.Pc[2] - geo.z;
-      if (sqrt(dx * dx + dy * dy + dz * dz) - P.ext >= geo.w + kCosxMargin)
-        continue;
-    }
-    switch (P.la * 3 + P.lb) { // shells up to d (kCosxLmax)
-    case 0: cosx_pair<Rt, 0, 0>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 1: cosx_pair<Rt, 0, 1>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 2: cosx_pair<Rt, 0, 2>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 3: cosx_pair<Rt, 1, 0>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 4: cosx_pair<Rt, 1, 1>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 5: cosx_pair<Rt, 1, 2>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 6: cosx_pair<Rt, 2, 0>(P, prims, etab, C, pure, Fg, Gg); break;
-    case 7: cosx_pair<Rt, 2, 1>(P, prims, etab, C, pure, Fg, Gg); break;
-    default: cosx_pair<Rt, 2, 2>(P, prims, etab, C, pure, Fg, Gg); break;
-    }
-  }
-}
-
-// G for one leaf's points, a thread per point, every kept shell pair.
-template <typename Rt>
-__global__ void __launch_bounds__(128, 1) k_cosx_g(MolDev m, int l0, int off0, int npairs,
+__global__ void __launch_bounds__(128, sizeof(Rt) == 4 ? 3 : 1) k_cosx_g(MolDev m, int l0, int off0, int npairs,
                                                 const CxPair *__restrict__ pairs,
                                                 const CxPrim *__restrict__ prims,
                                                 const Rt *__restrict__ etab,
                                                 const int *__restrict__ mask,
                                                 const double4 *__restrict__ lgeo, int pure,
-                                                const double *__restrict__ F,
+                                                size_t ld, const double *__restrict__ F,
                                                 double *__restrict__ G) {
+  __shared__ CxPair list[128];
+  __shared__ int wcount[4];
   const DevLeaf L = m.leaves[l0 + blockIdx.x];
   const double4 geo = lgeo[l0 + blockIdx.x];
-  for (int p = threadIdx.x; p < L.cnt; p += blockDim.x)
-    cosx_g_point<Rt>(m, L, p, off0, npairs, pairs, prims, etab, mask, geo, pure, F, G);
+  const int nslice = gridDim.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c0 = blockIdx.y; c0 < npairs; c0 += 128 * nslice) {
+    const int k = c0 + threadIdx.x * nslice;
+    bool keep = false;
+    CxPair P;
+    if (k < npairs && mask[k]) {
+      P = pairs[k];
+      const double dx = P.Pc[0] - geo.x, dy = P.Pc[1] - geo.y, dz = P.Pc[2] - geo.z;
+      keep = sqrt(dx * dx + dy * dy + dz * dz) - P.ext < geo.w + kCosxMargin;
+    }
+    const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0)
+      wcount[warp] = __popc(ballot);
+    __syncthreads();
+    int base = 0, n = 0;
+#pragma unroll
+    for (int w = 0; w < 4; w++) {
+      base += w < warp ? wcount[w] : 0;
+      n += wcount[w];
+    }
+    if (keep)
+      list[base + __popc(ballot & ((1u << lane) - 1u))] = P;
+    __syncthreads();
+    for (int p = threadIdx.x; p < L.cnt; p += blockDim.x) {
+      const Pt4 C = m.pts[L.off + p];
+      const size_t g = static_cast<size_t>(L.off - off0 + p);
+      const double *Fg = F + g;
+      double *Gg = G + g;
+      for (int e = 0; e < n; e++) {
+        const CxPair &Q = list[e];
+        switch (Q.la * 3 + Q.lb) { // shells up to d (kCosxLmax)
+        case 0: cosx_pair<Rt, 0, 0>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        case 1: cosx_pair<Rt, 0, 1>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        case 2: cosx_pair<Rt, 0, 2>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        case 3: cosx_pair<Rt, 1, 0>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        case 4: cosx_pair<Rt, 1, 1>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        case 5: cosx_pair<Rt, 1, 2>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        case 6: cosx_pair<Rt, 2, 0>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        case 7: cosx_pair<Rt, 2, 1>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        default: cosx_pair<Rt, 2, 2>(Q, prims, etab, C, pure, Fg, Gg, ld); break;
+        }
+      }
+    }
+    __syncthreads();
+  }
 }
 
-// K'[mu, lambda] -= sum_g phi_mu(g) G[g, lambda], mu over the leaf's AOs.
+// K'[mu, lambda] -= sum_g phi_mu(g) G[lambda, g], mu over the leaf's AOs and
+// the kCosxAoTile AOs lambda of blockIdx.y: the leaf's G columns staged in
+// shared memory, 128 points at a time; thread (mu group, lambda).
 __global__ void __launch_bounds__(128) k_cosx_k(MolDev m, const double *__restrict__ ws, int l0,
-                                                int off0, const double *__restrict__ G,
+                                                int off0, size_t ld,
+                                                const double *__restrict__ G,
                                                 double *__restrict__ Kp) {
+  __shared__ double Gs[kCosxAoTile][129]; // padded: the 16 rows in distinct banks
   const DevLeaf L = m.leaves[l0 + blockIdx.x];
-  const int lam = blockIdx.y * blockDim.x + threadIdx.x;
-  if (lam >= m.nbf)
-    return;
+  const int lam0 = blockIdx.y * kCosxAoTile;
+  const int nl = min(kCosxAoTile, m.nbf - lam0);
   const double *phi = ws + L.ws_off;
   const int *g = m.leaf_ao + L.ao_begin;
   const size_t nbf = static_cast<size_t>(m.nbf);
-  for (int s = 0; s < L.nbf; s++) {
-    double acc = 0.0;
-    for (int p = 0; p < L.cnt; p++)
-      acc = fma(phi[static_cast<size_t>(s) * L.npad + p],
-                G[static_cast<size_t>(L.off - off0 + p) * nbf + lam], acc);
-    atomicAdd(&Kp[static_cast<size_t>(g[s]) * nbf + lam], -acc);
+  const size_t col0 = static_cast<size_t>(L.off - off0);
+  constexpr int kGroups = 128 / kCosxAoTile;
+  const int j = threadIdx.x % kCosxAoTile, sg = threadIdx.x / kCosxAoTile;
+  for (int pc = 0; pc < L.cnt; pc += 128) {
+    const int np = min(128, L.cnt - pc);
+    for (int e = threadIdx.x; e < kCosxAoTile * 128; e += blockDim.x) {
+      const int r = e / 128, p = e % 128;
+      Gs[r][p] = r < nl && p < np ? G[(lam0 + r) * ld + col0 + pc + p] : 0.0;
+    }
+    __syncthreads();
+    for (int s = sg; s < L.nbf; s += kGroups) {
+      const double *ph = phi + static_cast<size_t>(s) * L.npad + pc;
+      double acc = 0.0;
+      for (int p = 0; p < np; p++)
+        acc = fma(ph[p], Gs[j][p], acc);
+      if (j < nl)
+        atomicAdd(&Kp[static_cast<size_t>(g[s]) * nbf + lam0 + j], -acc);
+    }
+    __syncthreads();
   }
 }
 
@@ -831,24 +886,26 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
   cuda_check(cudaMemsetAsync(S.d_Kp, 0, n2 * sizeof(double), st), "cudaMemsetAsync");
   for (size_t gi = 0; gi < S.group_leaf0.size(); gi++) {
     const int l0 = S.group_leaf0[gi], nl = S.group_nleaf[gi], off0 = S.group_off0[gi];
-    const dim3 gf(nl, (nbf + 127) / 128);
-    cuda_check(cudaMemsetAsync(S.d_G, 0, static_cast<size_t>(S.group_npts[gi]) * nbf *
-                                             sizeof(double), st),
-               "cudaMemsetAsync");
+    const size_t ld = static_cast<size_t>(S.group_npts[gi]);
+    const dim3 gf(nl, (nbf + kCosxAoTile - 1) / kCosxAoTile);
+    // pair slices: enough blocks to fill the SMs a few times over
+    const int nslice = std::max(1, std::min(kCosxMaxSlices, (kCosxTargetBlocks + nl - 1) / nl));
+    const dim3 gg(nl, nslice);
+    cuda_check(cudaMemsetAsync(S.d_G, 0, ld * nbf * sizeof(double), st), "cudaMemsetAsync");
     c.launch("cosx_f", st,
-             [&] { k_cosx_f<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_D2q, S.d_F); });
+             [&] { k_cosx_f<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_D2q, S.d_F); });
     c.launch("cosx_g", st, [&] {
       if (S.precision == OCC_XC_MIXED)
-        k_cosx_g<float><<<nl, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
+        k_cosx_g<float><<<gg, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
                                             S.d_etab_f, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
-                                            S.d_F, S.d_G);
+                                            ld, S.d_F, S.d_G);
       else
-        k_cosx_g<double><<<nl, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
+        k_cosx_g<double><<<gg, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
                                              S.d_etab, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
-                                             S.d_F, S.d_G);
+                                             ld, S.d_F, S.d_G);
     });
     c.launch("cosx_k", st,
-             [&] { k_cosx_k<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, S.d_G, S.d_Kp); });
+             [&] { k_cosx_k<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_G, S.d_Kp); });
   }
   c.launch("cosx_sym", st, [&] {
     const int g = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
