@@ -33,7 +33,7 @@
 //   k_cosx_k      K'[mu, lambda] -= sum_g phi_mu(g) G[lambda, g]
 //   k_cosx_sym    K = (K' + K'^T) / 4
 // All in FP64, except under OCC_XC_MIXED the ESP integrals (E coefficients,
-// Boys function, R_tuv) and their contraction with F, in FP32; G is summed in
+// Boys function, R_tuv), F and their contraction, in FP32; G is summed in
 // FP64 either way.  Shells up to d.
 #include <algorithm>
 #include <cmath>
@@ -51,7 +51,6 @@ namespace {
 
 constexpr int kCosxLmax = 2;                   // shells up to d
 constexpr int kCosxNc = 6;                     // Cartesian components of a d shell
-constexpr int kCosxR = 35;                     // R_tuv with t + u + v <= 4
 constexpr double kCosxDensityThreshold = 1e-6; // seminumerical_exchange.cpp:789
 constexpr double kCosxMargin = 1.0;            // cosx::Settings::margin (Bohr)
 constexpr int kCosxAoTile = 16;                // AOs lambda per block of the F and K kernels
@@ -85,6 +84,54 @@ struct CxPrim {
   int e_off;               // E tables: 3 axes x (la+1)(lb+1)(la+lb+1)
   int pad;
 };
+// The same in FP32 for the mixed precision: the centre as an unevaluated sum
+// hi + lo of two floats, so that P - C keeps the FP32 relative precision of
+// the difference, not of the coordinates (GB300 runs FP64 at 1/64 of the FP32
+// rate: the FP32 path does no FP64 arithmetic per primitive pair).
+struct CxPrimF {
+  float pexp, pref, Ph[3], Pl[3];
+  int e_off, pad;
+};
+struct CxPtF {
+  float h[3], l[3];
+};
+
+__device__ __forceinline__ void pc_diff(const CxPrim &Q, const Pt4 &C, double &x, double &y,
+                                        double &z) {
+  x = Q.P[0] - C.x;
+  y = Q.P[1] - C.y;
+  z = Q.P[2] - C.z;
+}
+__device__ __forceinline__ void pc_diff(const CxPrimF &Q, const CxPtF &C, float &x, float &y,
+                                        float &z) {
+  x = (Q.Ph[0] - C.h[0]) + (Q.Pl[0] - C.l[0]);
+  y = (Q.Ph[1] - C.h[1]) + (Q.Pl[1] - C.l[1]);
+  z = (Q.Ph[2] - C.h[2]) + (Q.Pl[2] - C.l[2]);
+}
+__device__ __forceinline__ Pt4 cx_point(const Pt4 &C, double) { return C; }
+__device__ __forceinline__ CxPtF cx_point(const Pt4 &C, float) {
+  CxPtF r;
+  const double c[3] = {C.x, C.y, C.z};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    r.h[d] = static_cast<float>(c[d]);
+    r.l[d] = static_cast<float>(c[d] - static_cast<double>(r.h[d]));
+  }
+  return r;
+}
+// FP32 to FP64 by integer operations (exact for normal numbers; zero and
+// FP32 subnormals, below 1.2e-38, give a signed zero), off the FP64 pipe.
+__device__ __forceinline__ double to_f64(double x) { return x; }
+__device__ __forceinline__ double to_f64(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned hi = e == 0 ? (u & 0x80000000u)
+                             : (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  const unsigned lo = e == 0 ? 0u : u << 29;
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+template <typename Rt> struct CxPrimOf { using type = CxPrim; };
+template <> struct CxPrimOf<float> { using type = CxPrimF; };
 
 // Index of R_tuv (t + u + v <= 4) in a packed array: by shell of degree s,
 // then t descending, then u descending.
@@ -95,7 +142,7 @@ __host__ __device__ constexpr int r_index(int t, int u, int v) {
 
 // 1 / (2 i + 1), i = 0 .. kBoysTable - 1: the Boys series and recursions
 // multiply by these instead of dividing (GB300's FP64 divisions are slow).
-constexpr int kBoysTable = 272;
+constexpr int kBoysTable = 64; // the series runs below T = 5: under 40 terms
 __constant__ double c_inv_odd[kBoysTable];
 __constant__ float c_inv_odd_f[kBoysTable];
 template <typename R> __device__ __forceinline__ R inv_odd(int i);
@@ -105,19 +152,24 @@ __device__ __forceinline__ double r_exp(double x) { return exp(x); }
 __device__ __forceinline__ float r_exp(float x) { return expf(x); }
 __device__ __forceinline__ double r_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float r_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double r_erf(double x) { return erf(x); }
+__device__ __forceinline__ float r_erf(float x) { return erff(x); }
 
-// F_n(T), n = 0..NMAX: for T < 36 the series
+// F_n(T), n = 0..NMAX: for T < 5 the series
 // F_n(T) = e^-T sum_k (2T)^k / ((2n+1)(2n+3)...(2n+2k+1)) at n = NMAX and
-// downward recursion F_{n-1} = (2T F_n + e^-T) / (2n - 1); beyond, the
-// asymptotic F_0 = (pi / T)^{1/2} / 2 (erf(sqrt T) = 1 to 1e-17) and upward
-// recursion F_{n+1} = ((2n+1) F_n - e^-T) / (2T); divisions by odd numbers
-// through the reciprocal table.
+// downward recursion F_{n-1} = (2T F_n + e^-T) / (2n - 1); from there
+// F_0 = (pi / T)^{1/2} erf(sqrt T) / 2 (erf(sqrt T) taken as 1 beyond T = 36
+// in FP64 and T = 18 in FP32, where it is 1 to the working precision) and
+// upward recursion F_{n+1} = ((2n+1) F_n - e^-T) / (2T), whose cancellation
+// at T >= 5 up to F_4 stays within a few ulps; divisions by odd numbers through
+// the reciprocal table.
 // R: double (the FP64 path) or float (the mixed path; the series stops at
 // 1e-8 of the sum).
 template <typename R, int NMAX> __device__ __forceinline__ void boys_t(R T, R (&F)[NMAX + 1]) {
+  static_assert(NMAX <= 4, "upward recursion from T = 5 is checked for n <= 4 (shells up to d)");
   const R et = r_exp(-T);
   const R t2 = R(2) * T;
-  if (T < R(36)) {
+  if (T < R(5)) {
     R term = inv_odd<R>(NMAX), sum = term;
     const R stop = sizeof(R) == 8 ? R(1e-17) : R(1e-8);
     for (int k = 1; k < kBoysTable - NMAX; k++) {
@@ -132,6 +184,8 @@ template <typename R, int NMAX> __device__ __forceinline__ void boys_t(R T, R (&
       F[n - 1] = (t2 * F[n] + et) * inv_odd<R>(n - 1);
   } else {
     F[0] = R(0.5) * r_sqrt(R(kPi) / T);
+    if (T < (sizeof(R) == 8 ? R(36) : R(18)))
+      F[0] *= r_erf(r_sqrt(T));
     const R it2 = R(1) / t2;
 #pragma unroll
     for (int n = 0; n < NMAX; n++)
@@ -237,11 +291,12 @@ __global__ void k_cosx_mask(int npairs, int nbf, const CxPair *__restrict__ pair
 // F[lambda, g] = w_g sum_sigma phi_sigma(g) D2q[sigma, lambda] for the
 // points of leaf l0 + blockIdx.x (g counted from the group's first point off0,
 // row stride ld) and the kCosxAoTile AOs lambda of blockIdx.y; a thread per
-// point.
+// point.  F is stored in the ESP integrals' precision To.
+template <typename To>
 __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restrict__ ws, int l0,
                                                 int off0, size_t ld,
                                                 const double *__restrict__ D2q,
-                                                double *__restrict__ F) {
+                                                To *__restrict__ F) {
   const DevLeaf L = m.leaves[l0 + blockIdx.x];
   const int lam0 = blockIdx.y * kCosxAoTile;
   const int nl = min(kCosxAoTile, m.nbf - lam0);
@@ -266,7 +321,7 @@ __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restri
 #pragma unroll
     for (int j = 0; j < kCosxAoTile; j++)
       if (j < nl)
-        F[(lam0 + j) * ld + col] = w * acc[j];
+        F[(lam0 + j) * ld + col] = static_cast<To>(w * acc[j]);
   }
 }
 
@@ -276,10 +331,10 @@ __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restri
 // E^x_t E^y_u E^z_v R_tuv, then G[:, q] -= F[:, p] V and, for p != q,
 // G[:, p] -= F[:, q] V^T, through the shells' solid-harmonic transforms
 // when pure.
-template <typename Rt, int LA, int LB>
-__device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restrict__ prims,
-                                          const Rt *__restrict__ etab, const Pt4 &C, bool pure,
-                                          const double *__restrict__ Fg, double *__restrict__ Gg,
+template <typename Rt, int LA, int LB, typename Prim, typename Pt>
+__device__ __forceinline__ void cosx_pair(const CxPair &P, const Prim *__restrict__ prims,
+                                          const Rt *__restrict__ etab, const Pt &C, bool pure,
+                                          const Rt *__restrict__ Fg, double *__restrict__ Gg,
                                           size_t ld) {
   constexpr int NCA = (LA + 1) * (LA + 2) / 2, NCB = (LB + 1) * (LB + 2) / 2;
   constexpr int L2 = LA + LB, NA = LA + 1, NB = LB + 1, NT = L2 + 1;
@@ -291,10 +346,10 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
     for (int j = 0; j < NCB; j++)
       V[i][j] = Rt(0);
   for (int r = 0; r < P.nprim; r++) {
-    const CxPrim Q = prims[P.prim0 + r];
-    Rt R[NR];
-    hermite_r_t<Rt, L2>(static_cast<Rt>(Q.pexp), static_cast<Rt>(Q.P[0] - C.x),
-                        static_cast<Rt>(Q.P[1] - C.y), static_cast<Rt>(Q.P[2] - C.z), R);
+    const Prim Q = prims[P.prim0 + r];
+    Rt R[NR], X, Y, Z;
+    pc_diff(Q, C, X, Y, Z);
+    hermite_r_t<Rt, L2>(Q.pexp, X, Y, Z, R);
     const Rt *Ex = etab + Q.e_off, *Ey = Ex + NA * NB * NT, *Ez = Ey + NA * NB * NT;
 #pragma unroll
     for (int i = 0; i < NCA; i++) {
@@ -319,13 +374,13 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
               if (v <= az + bz)
                 acc = fma(exy * ez[v], R[r_index(t, u, v)], acc);
           }
-        V[i][j] = fma(static_cast<Rt>(Q.pref), acc, V[i][j]);
+        V[i][j] = fma(Q.pref, acc, V[i][j]);
       }
     }
   }
   // the shells' functions: NFA / NFB of them, pure (2l + 1) or Cartesian;
-  // the contraction with F in the ESP integrals' precision, G accumulated
-  // in FP64
+  // the contraction with F in the ESP integrals' precision (F is stored in
+  // it), G accumulated in FP64
   const int nfa = pure ? 2 * LA + 1 : NCA, nfb = pure ? 2 * LB + 1 : NCB;
   auto ta = [&](int f, int i) {
     return pure ? sph_t<Rt>(LA, f < 5 ? f : 4, i) : (f == i ? Rt(1) : Rt(0));
@@ -340,7 +395,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 #pragma unroll
     for (int f = 0; f < NCA; f++)
       if (f < nfa)
-        s = fma(static_cast<Rt>(Fg[(P.bf_p + f) * ld]), ta(f, i), s);
+        s = fma(Fg[(P.bf_p + f) * ld], ta(f, i), s);
     Fc[i] = s;
   }
 #pragma unroll
@@ -358,7 +413,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 #pragma unroll
       for (int j = 0; j < NCB; j++)
         s = fma(tb(h, j), Gc[j], s);
-      atomicAdd(Gg + (P.bf_q + h) * ld, -static_cast<double>(s));
+      atomicAdd(Gg + (P.bf_q + h) * ld, to_f64(-s));
     }
   if (P.bf_p != P.bf_q) {
     Rt Fq[NCB], Gp[NCA];
@@ -368,7 +423,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 #pragma unroll
       for (int h = 0; h < NCB; h++)
         if (h < nfb)
-          s = fma(static_cast<Rt>(Fg[(P.bf_q + h) * ld]), tb(h, j), s);
+          s = fma(Fg[(P.bf_q + h) * ld], tb(h, j), s);
       Fq[j] = s;
     }
 #pragma unroll
@@ -386,7 +441,7 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 #pragma unroll
         for (int i = 0; i < NCA; i++)
           s = fma(ta(f, i), Gp[i], s);
-        atomicAdd(Gg + (P.bf_p + f) * ld, -static_cast<double>(s));
+        atomicAdd(Gg + (P.bf_p + f) * ld, to_f64(-s));
       }
   }
 }
@@ -403,11 +458,11 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const CxPrim *__restr
 template <typename Rt>
 __global__ void __launch_bounds__(128, sizeof(Rt) == 4 ? 3 : 1) k_cosx_g(MolDev m, int l0, int off0, int npairs,
                                                 const CxPair *__restrict__ pairs,
-                                                const CxPrim *__restrict__ prims,
+                                                const typename CxPrimOf<Rt>::type *__restrict__ prims,
                                                 const Rt *__restrict__ etab,
                                                 const int *__restrict__ mask,
                                                 const double4 *__restrict__ lgeo, int pure,
-                                                size_t ld, const double *__restrict__ F,
+                                                size_t ld, const Rt *__restrict__ F,
                                                 double *__restrict__ G) {
   __shared__ CxPair list[128];
   __shared__ int wcount[4];
@@ -437,9 +492,9 @@ __global__ void __launch_bounds__(128, sizeof(Rt) == 4 ? 3 : 1) k_cosx_g(MolDev 
       list[base + __popc(ballot & ((1u << lane) - 1u))] = P;
     __syncthreads();
     for (int p = threadIdx.x; p < L.cnt; p += blockDim.x) {
-      const Pt4 C = m.pts[L.off + p];
+      const auto C = cx_point(m.pts[L.off + p], Rt(0));
       const size_t g = static_cast<size_t>(L.off - off0 + p);
-      const double *Fg = F + g;
+      const Rt *Fg = F + g;
       double *Gg = G + g;
       for (int e = 0; e < n; e++) {
         const CxPair &Q = list[e];
@@ -651,6 +706,7 @@ struct CosxState {
   float *d_etab_f = nullptr; // the E coefficients in FP32 (the mixed precision)
   CxPair *d_pairs = nullptr;
   CxPrim *d_prims = nullptr;
+  CxPrimF *d_prims_f = nullptr;
   int *d_mask = nullptr;
   double4 *d_lgeo = nullptr;
   std::vector<void *> allocations;
@@ -825,6 +881,20 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
   S->allocations.push_back(S->d_pairs);
   S->d_prims = dev_upload(prims, bytes);
   S->allocations.push_back(S->d_prims);
+  std::vector<CxPrimF> primsf(prims.size());
+  for (size_t i = 0; i < prims.size(); i++) {
+    CxPrimF &f = primsf[i];
+    f.pexp = static_cast<float>(prims[i].pexp);
+    f.pref = static_cast<float>(prims[i].pref);
+    for (int d = 0; d < 3; d++) {
+      f.Ph[d] = static_cast<float>(prims[i].P[d]);
+      f.Pl[d] = static_cast<float>(prims[i].P[d] - static_cast<double>(f.Ph[d]));
+    }
+    f.e_off = prims[i].e_off;
+    f.pad = 0;
+  }
+  S->d_prims_f = dev_upload(primsf, bytes);
+  S->allocations.push_back(S->d_prims_f);
   S->d_etab = dev_upload(et, bytes);
   S->allocations.push_back(S->d_etab);
   const std::vector<float> etf(et.begin(), et.end());
@@ -892,13 +962,19 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
     const int nslice = std::max(1, std::min(kCosxMaxSlices, (kCosxTargetBlocks + nl - 1) / nl));
     const dim3 gg(nl, nslice);
     cuda_check(cudaMemsetAsync(S.d_G, 0, ld * nbf * sizeof(double), st), "cudaMemsetAsync");
-    c.launch("cosx_f", st,
-             [&] { k_cosx_f<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_D2q, S.d_F); });
+    const bool mixed = S.precision == OCC_XC_MIXED;
+    float *Ff = reinterpret_cast<float *>(S.d_F); // the mixed precision's F (half the buffer)
+    c.launch("cosx_f", st, [&] {
+      if (mixed)
+        k_cosx_f<float><<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_D2q, Ff);
+      else
+        k_cosx_f<double><<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_D2q, S.d_F);
+    });
     c.launch("cosx_g", st, [&] {
-      if (S.precision == OCC_XC_MIXED)
-        k_cosx_g<float><<<gg, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
+      if (mixed)
+        k_cosx_g<float><<<gg, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims_f,
                                             S.d_etab_f, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
-                                            ld, S.d_F, S.d_G);
+                                            ld, Ff, S.d_G);
       else
         k_cosx_g<double><<<gg, 128, 0, st>>>(m, l0, off0, S.npairs, S.d_pairs, S.d_prims,
                                              S.d_etab, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
