@@ -291,12 +291,11 @@ __global__ void k_cosx_mask(int npairs, int nbf, const CxPair *__restrict__ pair
 // F[lambda, g] = w_g sum_sigma phi_sigma(g) D2q[sigma, lambda] for the
 // points of leaf l0 + blockIdx.x (g counted from the group's first point off0,
 // row stride ld) and the kCosxAoTile AOs lambda of blockIdx.y; a thread per
-// point.  F is stored in the ESP integrals' precision To.
-template <typename To>
+// point.
 __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restrict__ ws, int l0,
                                                 int off0, size_t ld,
                                                 const double *__restrict__ D2q,
-                                                To *__restrict__ F) {
+                                                double *__restrict__ F) {
   const DevLeaf L = m.leaves[l0 + blockIdx.x];
   const int lam0 = blockIdx.y * kCosxAoTile;
   const int nl = min(kCosxAoTile, m.nbf - lam0);
@@ -321,7 +320,67 @@ __global__ void __launch_bounds__(128) k_cosx_f(MolDev m, const double *__restri
 #pragma unroll
     for (int j = 0; j < kCosxAoTile; j++)
       if (j < nl)
-        F[(lam0 + j) * ld + col] = static_cast<To>(w * acc[j]);
+        F[(lam0 + j) * ld + col] = w * acc[j];
+  }
+}
+
+// Double-float operands of the mixed precision's F and K: x = hi + lo, hi the
+// FP32 rounding of x and lo that of the rest (about 48 significant bits).
+__device__ __forceinline__ float2 split_hl(double x) {
+  const float h = static_cast<float>(x);
+  return make_float2(h, static_cast<float>(x - static_cast<double>(h)));
+}
+__global__ void k_cosx_split(size_t n, const double *__restrict__ x, float2 *__restrict__ y) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    y[i] = split_hl(x[i]);
+}
+// sh + sl += a b for double-float a and b in FP32 arithmetic (GB300's FP32
+// rate is 64 times its FP64 rate): the product's rounding error (an FMA) and
+// its cross terms, and the sum's rounding error (Knuth's TwoSum, rounded
+// intrinsics so that nothing is contracted), go to sl.  Relative to the sum
+// of |a b| the result holds about 1e-14.
+__device__ __forceinline__ void df_fma(float2 a, float2 b, float &sh, float &sl) {
+  const float p = __fmul_rn(a.x, b.x);
+  const float e = fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.x, b.x, -p)));
+  const float t = __fadd_rn(sh, p);
+  const float v = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, v)), __fsub_rn(p, v));
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+  sh = t;
+}
+
+// k_cosx_f in the mixed precision: double-float phi (the workspace split into
+// phi_hl) and D2q (D2q_hl), F stored in FP32.
+__global__ void __launch_bounds__(128) k_cosx_f_df(MolDev m, const float2 *__restrict__ phi_hl,
+                                                   int l0, int off0, size_t ld,
+                                                   const float2 *__restrict__ D2q_hl,
+                                                   float *__restrict__ F) {
+  const DevLeaf L = m.leaves[l0 + blockIdx.x];
+  const int lam0 = blockIdx.y * kCosxAoTile;
+  const int nl = min(kCosxAoTile, m.nbf - lam0);
+  const float2 *phi = phi_hl + L.ws_off;
+  const int *g = m.leaf_ao + L.ao_begin;
+  const size_t nbf = static_cast<size_t>(m.nbf);
+  for (int p = threadIdx.x; p < L.cnt; p += blockDim.x) {
+    float sh[kCosxAoTile], sl[kCosxAoTile];
+#pragma unroll
+    for (int j = 0; j < kCosxAoTile; j++)
+      sh[j] = sl[j] = 0.f;
+    for (int s = 0; s < L.nbf; s++) {
+      const float2 a = phi[static_cast<size_t>(s) * L.npad + p];
+      const float2 *d = D2q_hl + static_cast<size_t>(g[s]) * nbf + lam0;
+#pragma unroll
+      for (int j = 0; j < kCosxAoTile; j++)
+        if (j < nl)
+          df_fma(a, d[j], sh[j], sl[j]);
+    }
+    const float w = static_cast<float>(m.pts[L.off + p].w);
+    const size_t col = static_cast<size_t>(L.off - off0 + p);
+#pragma unroll
+    for (int j = 0; j < kCosxAoTile; j++)
+      if (j < nl)
+        F[(lam0 + j) * ld + col] = w * (sh[j] + sl[j]);
   }
 }
 
@@ -551,6 +610,42 @@ __global__ void __launch_bounds__(128) k_cosx_k(MolDev m, const double *__restri
   }
 }
 
+// k_cosx_k in the mixed precision: double-float phi and G (G split as it is
+// staged), K' summed in FP64.
+__global__ void __launch_bounds__(128) k_cosx_k_df(MolDev m, const float2 *__restrict__ phi_hl,
+                                                   int l0, int off0, size_t ld,
+                                                   const double *__restrict__ G,
+                                                   double *__restrict__ Kp) {
+  __shared__ float2 Gs[kCosxAoTile][129]; // padded: the 16 rows in distinct banks
+  const DevLeaf L = m.leaves[l0 + blockIdx.x];
+  const int lam0 = blockIdx.y * kCosxAoTile;
+  const int nl = min(kCosxAoTile, m.nbf - lam0);
+  const float2 *phi = phi_hl + L.ws_off;
+  const int *g = m.leaf_ao + L.ao_begin;
+  const size_t nbf = static_cast<size_t>(m.nbf);
+  const size_t col0 = static_cast<size_t>(L.off - off0);
+  constexpr int kGroups = 128 / kCosxAoTile;
+  const int j = threadIdx.x % kCosxAoTile, sg = threadIdx.x / kCosxAoTile;
+  for (int pc = 0; pc < L.cnt; pc += 128) {
+    const int np = min(128, L.cnt - pc);
+    for (int e = threadIdx.x; e < kCosxAoTile * 128; e += blockDim.x) {
+      const int r = e / 128, p = e % 128;
+      Gs[r][p] = r < nl && p < np ? split_hl(G[(lam0 + r) * ld + col0 + pc + p])
+                                  : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int s = sg; s < L.nbf; s += kGroups) {
+      const float2 *ph = phi + static_cast<size_t>(s) * L.npad + pc;
+      float sh = 0.f, sl = 0.f;
+      for (int p = 0; p < np; p++)
+        df_fma(ph[p], Gs[j][p], sh, sl);
+      if (j < nl)
+        atomicAdd(&Kp[static_cast<size_t>(g[s]) * nbf + lam0 + j], -(to_f64(sh) + to_f64(sl)));
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_cosx_sym(int nbf, const double *__restrict__ Kp, double *__restrict__ K) {
   const size_t n2 = static_cast<size_t>(nbf) * nbf;
   for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n2;
@@ -704,6 +799,7 @@ struct CosxState {
   double *d_Q = nullptr, *d_D = nullptr, *d_D2q = nullptr, *d_Kp = nullptr, *d_K = nullptr;
   double *d_F = nullptr, *d_G = nullptr, *d_etab = nullptr;
   float *d_etab_f = nullptr; // the E coefficients in FP32 (the mixed precision)
+  float2 *d_phi_hl = nullptr, *d_D2q_hl = nullptr; // double-float phi and D2q (mixed)
   CxPair *d_pairs = nullptr;
   CxPrim *d_prims = nullptr;
   CxPrimF *d_prims_f = nullptr;
@@ -801,6 +897,8 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
   const MolDev m = N->dev();
   launch_colloc_f64(m, 0, N->d_ws, st);
   N->fp64_ao_valid = true;
+  S->d_phi_hl = S->alloc<float2>(N->ws_elems);
+  k_cosx_split<<<1024, 256, 0, st>>>(N->ws_elems, N->d_ws, S->d_phi_hl);
   // S_num = phi^T diag(w) phi: the V_xc kernel with coefficient w / 2
   const long npts = N->plan.npts;
   k_cosx_halfw<<<static_cast<int>((npts + 255) / 256), 256, 0, st>>>(npts, N->d_pts, N->d_coef);
@@ -913,6 +1011,7 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
   S->allocations.push_back(S->d_lgeo);
   S->d_D = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
   S->d_D2q = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
+  S->d_D2q_hl = S->alloc<float2>(static_cast<size_t>(nbf) * nbf);
   S->d_Kp = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
   S->d_K = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
   // leaf groups whose point-major F and G fit the cap
@@ -949,6 +1048,12 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
     k_cosx_d2q<<<dim3((nbf + 15) / 16, (nbf + 15) / 16), dim3(16, 16), 0, st>>>(nbf, S.d_Q, dD,
                                                                               S.d_D2q);
   });
+  const bool mixed = S.precision == OCC_XC_MIXED;
+  if (mixed)
+    c.launch("cosx_split", st, [&] {
+      const int g = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
+      k_cosx_split<<<g, 256, 0, st>>>(n2, S.d_D2q, S.d_D2q_hl);
+    });
   c.launch("cosx_mask", st, [&] {
     k_cosx_mask<<<(S.npairs + 127) / 128, 128, 0, st>>>(S.npairs, nbf, S.d_pairs, S.d_D2q,
                                                         S.d_mask);
@@ -962,13 +1067,12 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
     const int nslice = std::max(1, std::min(kCosxMaxSlices, (kCosxTargetBlocks + nl - 1) / nl));
     const dim3 gg(nl, nslice);
     cuda_check(cudaMemsetAsync(S.d_G, 0, ld * nbf * sizeof(double), st), "cudaMemsetAsync");
-    const bool mixed = S.precision == OCC_XC_MIXED;
     float *Ff = reinterpret_cast<float *>(S.d_F); // the mixed precision's F (half the buffer)
     c.launch("cosx_f", st, [&] {
       if (mixed)
-        k_cosx_f<float><<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_D2q, Ff);
+        k_cosx_f_df<<<gf, 128, 0, st>>>(m, S.d_phi_hl, l0, off0, ld, S.d_D2q_hl, Ff);
       else
-        k_cosx_f<double><<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_D2q, S.d_F);
+        k_cosx_f<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_D2q, S.d_F);
     });
     c.launch("cosx_g", st, [&] {
       if (mixed)
@@ -980,8 +1084,12 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
                                              S.d_etab, S.d_mask, S.d_lgeo, N.basis.pure ? 1 : 0,
                                              ld, S.d_F, S.d_G);
     });
-    c.launch("cosx_k", st,
-             [&] { k_cosx_k<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_G, S.d_Kp); });
+    c.launch("cosx_k", st, [&] {
+      if (mixed)
+        k_cosx_k_df<<<gf, 128, 0, st>>>(m, S.d_phi_hl, l0, off0, ld, S.d_G, S.d_Kp);
+      else
+        k_cosx_k<<<gf, 128, 0, st>>>(m, N.d_ws, l0, off0, ld, S.d_G, S.d_Kp);
+    });
   }
   c.launch("cosx_sym", st, [&] {
     const int g = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
