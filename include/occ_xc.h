@@ -191,7 +191,8 @@ int occ_xc_nlc_grid(const occ_xc_molecule *mol, double *points, double *weights)
  * SemiNumericalExchange (include/occ/qm/seminumerical_exchange.h:104-118,
  * src/qm/seminumerical_exchange.cpp:233-250 set-up, :516-529 restricted K,
  * :714-855 the grid sweep), replacing its constructor and compute_K(mo) for
- * a restricted wavefunction.  occ_xc_cosx_create builds, on `mol`'s device
+ * restricted and unrestricted wavefunctions (:616-648).  occ_xc_cosx_create
+ * builds, on `mol`'s device
  * and over its basis, the grid of `grid` (NULL: GridSettings::for_sgx(50),
  * src/numint/grid_settings.cpp:59-68), its AO values, the numerical overlap
  * S_num and the overlap projector Q = S_num^-1 S; shells up to d
@@ -213,6 +214,15 @@ int occ_xc_cosx_exchange(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D, 
 /* The same on device buffers, asynchronous on `stream` (NULL: the context's). */
 int occ_xc_cosx_exchange_device(occ_xc_context *ctx, occ_xc_cosx *cx, const double *d_D,
                                 double *d_K, void *stream);
+/* Unrestricted: D and K are 2 nbf x nbf, column-major, the alpha block above
+ * the beta one (OCC's unrestricted mo.D, each block 0.5 C_s C_s^T); per spin
+ * K_s = 1/2 (K'_s + K'_s^T) of Q (2 D_s), as compute_K_unrestricted
+ * (src/qm/seminumerical_exchange.cpp:616-648).  Host buffers, blocking. */
+int occ_xc_cosx_exchange_unrestricted(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D,
+                                      double *K);
+/* The same on device buffers, asynchronous on `stream` (NULL: the context's). */
+int occ_xc_cosx_exchange_unrestricted_device(occ_xc_context *ctx, occ_xc_cosx *cx,
+                                             const double *d_D, double *d_K, void *stream);
 
 /* Replaces DFT::compute_xc_gradient(mo) for a restricted wavefunction
  * (include/occ/dft/dft.h:599-749, src/dft/dft_gradient_kernels.cpp:472-595):

@@ -54,7 +54,7 @@ constexpr int kCosxNc = 6;                     // Cartesian components of a d sh
 constexpr double kCosxDensityThreshold = 1e-6; // seminumerical_exchange.cpp:789
 constexpr double kCosxMargin = 1.0;            // cosx::Settings::margin (Bohr)
 constexpr int kCosxAoTile = 16;                // AOs lambda per block of the F and K kernels
-constexpr int kCosxTargetBlocks = 152 * 8;     // G kernel: blocks to aim for (8 per SM)
+constexpr int kCosxTargetBlocks = 152 * 16;    // G kernel: blocks to aim for (16 per SM)
 constexpr int kCosxMaxSlices = 32;             // G kernel: most pair slices per leaf
 constexpr double kCosxLogThreshold = 27.631021115928547; // -ln(1e-12): pair extents
 constexpr double kCosxPairOverlap = 1e-12;     // IntegralEngine::compute_shellpairs
@@ -255,14 +255,14 @@ __host__ __device__ constexpr int cca_pow(int l, int i, int axis) {
 
 // D2q = Q (2 D): Q, D column-major nbf x nbf; out row-major.  16 x 16 tiles.
 __global__ void k_cosx_d2q(int nbf, const double *__restrict__ Q, const double *__restrict__ D,
-                           double *__restrict__ D2q) {
+                           size_t ldd, double *__restrict__ D2q) {
   __shared__ double Qs[16][17], Ds[16][17];
   const int lam = blockIdx.x * 16 + threadIdx.x, sig = blockIdx.y * 16 + threadIdx.y;
   double acc = 0.0;
   for (int k0 = 0; k0 < nbf; k0 += 16) {
     const int kq = k0 + threadIdx.x, kd = k0 + threadIdx.y;
     Qs[threadIdx.y][threadIdx.x] = (sig < nbf && kq < nbf) ? Q[static_cast<size_t>(kq) * nbf + sig] : 0.0;
-    Ds[threadIdx.y][threadIdx.x] = (kd < nbf && lam < nbf) ? D[static_cast<size_t>(lam) * nbf + kd] : 0.0;
+    Ds[threadIdx.y][threadIdx.x] = (kd < nbf && lam < nbf) ? D[lam * ldd + kd] : 0.0;
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < 16; k++)
@@ -512,17 +512,16 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const Prim *__restric
 // compacts the survivors into shared memory in pair order; every thread then
 // runs them at its point.  F and G are AO-major (row lambda, column the
 // group's point, row stride ld); the slices of a leaf add into G by atomics.
-// In FP32 the bounds give 168 registers and three blocks per SM without
-// spills; the FP64 form needs the full register file.
+// In FP32 the bounds give 128 registers and four blocks per SM (a 144-byte
+// spill; faster than 168 registers and three blocks: 3.35 -> 2.72 ms a call
+// at 8 waters with 16 target blocks per SM, against 8); the FP64 form needs
+// the full register file.
 template <typename Rt>
-__global__ void __launch_bounds__(128, sizeof(Rt) == 4 ? 3 : 1) k_cosx_g(MolDev m, int l0, int off0, int npairs,
-                                                const CxPair *__restrict__ pairs,
-                                                const typename CxPrimOf<Rt>::type *__restrict__ prims,
-                                                const Rt *__restrict__ etab,
-                                                const int *__restrict__ mask,
-                                                const double4 *__restrict__ lgeo, int pure,
-                                                size_t ld, const Rt *__restrict__ F,
-                                                double *__restrict__ G) {
+__global__ void __launch_bounds__(128, sizeof(Rt) == 4 ? 4 : 1)
+    k_cosx_g(MolDev m, int l0, int off0, int npairs, const CxPair *__restrict__ pairs,
+             const typename CxPrimOf<Rt>::type *__restrict__ prims, const Rt *__restrict__ etab,
+             const int *__restrict__ mask, const double4 *__restrict__ lgeo, int pure, size_t ld,
+             const Rt *__restrict__ F, double *__restrict__ G) {
   __shared__ CxPair list[128];
   __shared__ int wcount[4];
   const DevLeaf L = m.leaves[l0 + blockIdx.x];
@@ -646,12 +645,14 @@ __global__ void __launch_bounds__(128) k_cosx_k_df(MolDev m, const float2 *__res
   }
 }
 
-__global__ void k_cosx_sym(int nbf, const double *__restrict__ Kp, double *__restrict__ K) {
+// K = scale (K' + K'^T) into column-major K with leading dimension ldk.
+__global__ void k_cosx_sym(int nbf, const double *__restrict__ Kp, double *__restrict__ K,
+                           size_t ldk, double scale) {
   const size_t n2 = static_cast<size_t>(nbf) * nbf;
   for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n2;
        e += static_cast<size_t>(gridDim.x) * blockDim.x) {
     const size_t i = e / nbf, j = e % nbf;
-    K[e] = 0.25 * (Kp[e] + Kp[j * nbf + i]);
+    K[i * ldk + j] = scale * (Kp[e] + Kp[j * nbf + i]);
   }
 }
 
@@ -1009,11 +1010,11 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
     throw std::runtime_error("COSX: leaf geometry does not match the plan");
   S->d_lgeo = dev_upload(lgeo, bytes);
   S->allocations.push_back(S->d_lgeo);
-  S->d_D = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
+  S->d_D = S->alloc<double>(2 * static_cast<size_t>(nbf) * nbf); // room for a UHF D
   S->d_D2q = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
   S->d_D2q_hl = S->alloc<float2>(static_cast<size_t>(nbf) * nbf);
   S->d_Kp = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
-  S->d_K = S->alloc<double>(static_cast<size_t>(nbf) * nbf);
+  S->d_K = S->alloc<double>(2 * static_cast<size_t>(nbf) * nbf);
   // leaf groups whose point-major F and G fit the cap
   const size_t per_pt = 2 * static_cast<size_t>(nbf) * sizeof(double);
   const size_t cap_pts = std::max<size_t>(ws_cap_bytes / std::max<size_t>(per_pt, 1), 256);
@@ -1039,13 +1040,17 @@ std::unique_ptr<CosxState> cosx_create(Molecule &M, const GridSettings &gs, size
   return S;
 }
 
-void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaStream_t st) {
+// K of one density block: dD column-major with leading dimension ldd (nbf for
+// a restricted D, 2 nbf for a spin block of an unrestricted one), K = scale
+// (K' + K'^T) into dK with leading dimension ldk.
+void cosx_exchange(Context &c, CosxState &S, const double *dD, size_t ldd, double *dK, size_t ldk,
+                   double scale, cudaStream_t st) {
   const int nbf = S.nbf;
   const size_t n2 = static_cast<size_t>(nbf) * nbf;
   Molecule &N = *S.N;
   const MolDev m = N.dev();
   c.launch("cosx_d2q", st, [&] {
-    k_cosx_d2q<<<dim3((nbf + 15) / 16, (nbf + 15) / 16), dim3(16, 16), 0, st>>>(nbf, S.d_Q, dD,
+    k_cosx_d2q<<<dim3((nbf + 15) / 16, (nbf + 15) / 16), dim3(16, 16), 0, st>>>(nbf, S.d_Q, dD, ldd,
                                                                               S.d_D2q);
   });
   const bool mixed = S.precision == OCC_XC_MIXED;
@@ -1093,7 +1098,7 @@ void cosx_exchange(Context &c, CosxState &S, const double *dD, double *dK, cudaS
   }
   c.launch("cosx_sym", st, [&] {
     const int g = static_cast<int>(std::min<size_t>((n2 + 255) / 256, 1024));
-    k_cosx_sym<<<g, 256, 0, st>>>(nbf, S.d_Kp, dK);
+    k_cosx_sym<<<g, 256, 0, st>>>(nbf, S.d_Kp, dK, ldk, scale);
   });
   cuda_check(cudaGetLastError(), "kernel launch");
 }
@@ -1142,7 +1147,21 @@ int occ_xc_cosx_grid_points(const occ_xc_cosx *cx, long *npoints) {
   return OCC_XC_OK;
 }
 
-int occ_xc_cosx_exchange(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D, double *K) {
+// Restricted: K = 1/4 (K' + K'^T) of D2q = Q (2 D) (seminumerical_exchange.cpp:
+// 517-529).  Unrestricted (D and K 2 nbf x nbf, the alpha block above the
+// beta one): per spin K_s = 1/2 (K'_s + K'_s^T) of Q (2 D_s) (:616-648).
+static void cosx_any(Context &c, CosxState &S, const double *dD, double *dK, bool uhf,
+                     cudaStream_t st) {
+  const size_t n = static_cast<size_t>(S.nbf);
+  if (!uhf) {
+    cosx_exchange(c, S, dD, n, dK, n, 0.25, st);
+    return;
+  }
+  cosx_exchange(c, S, dD, 2 * n, dK, 2 * n, 0.5, st);
+  cosx_exchange(c, S, dD + n, 2 * n, dK + n, 2 * n, 0.5, st);
+}
+
+static int cosx_host(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D, double *K, bool uhf) {
   if (!ctx || !cx || !D || !K || cx->ctx != ctx)
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
@@ -1150,26 +1169,45 @@ int occ_xc_cosx_exchange(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D, 
     DeviceGuard on_device(ctx->impl->device);
     CosxState &S = *cx->impl;
     cudaStream_t st = ctx->impl->stream;
-    const size_t n2 = static_cast<size_t>(S.nbf) * S.nbf;
+    const size_t n2 = static_cast<size_t>(S.nbf) * S.nbf * (uhf ? 2 : 1);
     cuda_check(cudaMemcpyAsync(S.d_D, D, n2 * sizeof(double), cudaMemcpyHostToDevice, st),
                "cudaMemcpyAsync H2D");
-    cosx_exchange(*ctx->impl, S, S.d_D, S.d_K, st);
+    cosx_any(*ctx->impl, S, S.d_D, S.d_K, uhf, st);
     cuda_check(cudaMemcpyAsync(K, S.d_K, n2 * sizeof(double), cudaMemcpyDeviceToHost, st),
                "cudaMemcpyAsync D2H");
     cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   });
 }
 
-int occ_xc_cosx_exchange_device(occ_xc_context *ctx, occ_xc_cosx *cx, const double *d_D,
-                                double *d_K, void *stream) {
+static int cosx_device(occ_xc_context *ctx, occ_xc_cosx *cx, const double *d_D, double *d_K,
+                       void *stream, bool uhf) {
   if (!ctx || !cx || !d_D || !d_K || cx->ctx != ctx)
     return OCC_XC_ERR_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   return guarded(ctx, [&] {
     DeviceGuard on_device(ctx->impl->device);
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->impl->stream;
-    cosx_exchange(*ctx->impl, *cx->impl, d_D, d_K, st);
+    cosx_any(*ctx->impl, *cx->impl, d_D, d_K, uhf, st);
   });
+}
+
+int occ_xc_cosx_exchange(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D, double *K) {
+  return cosx_host(ctx, cx, D, K, false);
+}
+
+int occ_xc_cosx_exchange_device(occ_xc_context *ctx, occ_xc_cosx *cx, const double *d_D,
+                                double *d_K, void *stream) {
+  return cosx_device(ctx, cx, d_D, d_K, stream, false);
+}
+
+int occ_xc_cosx_exchange_unrestricted(occ_xc_context *ctx, occ_xc_cosx *cx, const double *D,
+                                      double *K) {
+  return cosx_host(ctx, cx, D, K, true);
+}
+
+int occ_xc_cosx_exchange_unrestricted_device(occ_xc_context *ctx, occ_xc_cosx *cx,
+                                             const double *d_D, double *d_K, void *stream) {
+  return cosx_device(ctx, cx, d_D, d_K, stream, true);
 }
 
 } // extern "C"

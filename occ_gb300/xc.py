@@ -119,6 +119,9 @@ def library():
     lib.occ_xc_cosx_set_precision.argtypes = [C.c_void_p, C.c_int]
     lib.occ_xc_cosx_grid_points.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
     lib.occ_xc_cosx_exchange.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp]
+    lib.occ_xc_cosx_exchange_unrestricted.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp]
+    lib.occ_xc_cosx_exchange_unrestricted_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
+                                                             C.c_void_p, C.c_void_p]
     lib.occ_xc_cosx_exchange_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p]
     lib.occ_xc_compute_vxc_unrestricted.argtypes = [C.c_void_p, C.c_void_p, _dp, C.c_int, _dp,
@@ -620,24 +623,36 @@ class SemiNumericalExchange:
         return n.value
 
     def compute_K(self, D):
-        """K (nbf x nbf) of mo.D = D (compute_K(mo) of a restricted mo)."""
+        """K of mo.D = D, as compute_K(mo): nbf x nbf for a restricted mo,
+        2 nbf x nbf (alpha block above beta, each 0.5 C_s C_s^T) for an
+        unrestricted one, K in the same shape."""
         nbf = self.dft.nbf()
         Dm = np.asfortranarray(np.asarray(D, dtype=np.float64))
-        if Dm.shape != (nbf, nbf):
-            raise XCError(f"density matrix must be {nbf}x{nbf}")
-        K = np.zeros((nbf, nbf), order="F")
-        rc = self.ctx.lib.occ_xc_cosx_exchange(self.ctx.h, self.h, _ptr(Dm), _ptr(K))
+        if Dm.shape == (nbf, nbf):
+            fn, name = self.ctx.lib.occ_xc_cosx_exchange, "occ_xc_cosx_exchange"
+        elif Dm.shape == (2 * nbf, nbf):
+            fn = self.ctx.lib.occ_xc_cosx_exchange_unrestricted
+            name = "occ_xc_cosx_exchange_unrestricted"
+        else:
+            raise XCError(f"density matrix must be {nbf}x{nbf} or {2 * nbf}x{nbf}")
+        K = np.zeros(Dm.shape, order="F")
+        rc = fn(self.ctx.h, self.h, _ptr(Dm), _ptr(K))
         if rc != 0:
-            raise XCError(f"occ_xc_cosx_exchange failed ({rc}): {self.ctx.error()}", rc)
+            raise XCError(f"{name} failed ({rc}): {self.ctx.error()}", rc)
         return K
 
-    def compute_K_device(self, d_D, d_K, stream=None):
-        """The same on device buffers (addresses), asynchronous on `stream`."""
-        rc = self.ctx.lib.occ_xc_cosx_exchange_device(self.ctx.h, self.h, C.c_void_p(d_D),
-                                                      C.c_void_p(d_K),
-                                                      C.c_void_p(stream) if stream else None)
+    def compute_K_device(self, d_D, d_K, stream=None, unrestricted=False):
+        """The same on device buffers (addresses, column-major), asynchronous
+        on `stream`."""
+        if unrestricted:
+            fn = self.ctx.lib.occ_xc_cosx_exchange_unrestricted_device
+            name = "occ_xc_cosx_exchange_unrestricted_device"
+        else:
+            fn, name = self.ctx.lib.occ_xc_cosx_exchange_device, "occ_xc_cosx_exchange_device"
+        rc = fn(self.ctx.h, self.h, C.c_void_p(d_D), C.c_void_p(d_K),
+                C.c_void_p(stream) if stream else None)
         if rc != 0:
-            raise XCError(f"occ_xc_cosx_exchange_device failed ({rc}): {self.ctx.error()}", rc)
+            raise XCError(f"{name} failed ({rc}): {self.ctx.error()}", rc)
 
 
 class Batch:

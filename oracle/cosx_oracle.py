@@ -7,6 +7,8 @@ Restates SemiNumericalExchange's ESP path (src/qm/seminumerical_exchange.cpp):
               projector Q = S_num^-1 S (an LDL^T solve there, a dense solve
               here)
   :517-529    restricted: D2q = Q (2 mo.D), K = 0.25 (K' + K'^T)
+  :616-648    unrestricted (mo.D 2 nbf x nbf, alpha block above beta): per
+              spin D2q_s = Q (2 D_s), K_s = 0.5 (K'_s + K'_s^T)
   :714-855    the sweep: per atom grid, batches of 128 consecutive points;
               a batch is skipped when max phi < precision; F = (w phi) D2q;
               for every shell pair p >= q whose D2q blocks reach 1e-6,
@@ -308,3 +310,13 @@ def cosx_exchange(basis, D, angular=110, precision=np.finfo(np.float64).eps,
             K -= ph.T @ G
         off += cnt
     return 0.25 * (K + K.T)
+
+
+def cosx_exchange_unrestricted(basis, D, **kw):
+    """K (2 nbf x nbf) of an unrestricted mo.D (alpha block above beta):
+    per spin 0.5 (K'_s + K'_s^T) of Q (2 D_s), twice the restricted
+    expression's 0.25 for the same block (seminumerical_exchange.cpp:616-648)."""
+    D = np.asarray(D)
+    nbf = D.shape[1]
+    return np.vstack([2.0 * cosx_exchange(basis, D[:nbf], **kw),
+                      2.0 * cosx_exchange(basis, D[nbf:], **kw)])

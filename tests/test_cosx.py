@@ -198,9 +198,10 @@ TOL_K_MIXED = 1e-6  # relative to max |K|: FP32 ESP integrals against FP64 (3e-8
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["water_631g", "two_waters_svp"])
 def test_gpu_cosx_mixed_precision(case):
-    """The ESP integrals in FP32 (F, G, K' and the projector in FP64): K
-    against the FP64 build, far inside COSX's own error against exact
-    exchange (3e-4 of max |K| on water / 6-31G at for_sgx(50))."""
+    """The ESP integrals and F in FP32, F and K' formed in double-float FP32
+    arithmetic, G and K' summed in FP64: K against the FP64 build, far inside
+    COSX's own error against exact exchange (3e-4 of max |K| on water /
+    6-31G at for_sgx(50))."""
     if case == "water_631g":
         b, D, _, _ = _rhf_water_631g()
     else:
@@ -220,3 +221,60 @@ def test_gpu_cosx_mixed_precision(case):
     assert rel <= TOL_K_MIXED, rel
     sgx.set_precision(og.FP64)
     assert np.abs(sgx.compute_K(D) - K64).max() < 1e-13
+
+
+def _open_shell_density(n, na, nb, seed):
+    """An unrestricted mo.D (alpha block above beta, each 0.5 C_s C_s^T) of
+    random orbitals, na alpha and nb beta."""
+    rng = np.random.default_rng(seed)
+    Ca = rng.normal(size=(n, na)) * 0.3
+    Cb = rng.normal(size=(n, nb)) * 0.3
+    return np.vstack([0.5 * Ca @ Ca.T, 0.5 * Cb @ Cb.T])
+
+
+@pytest.mark.gpu
+def test_gpu_cosx_unrestricted_matches_oracle():
+    """compute_K of an unrestricted mo (seminumerical_exchange.cpp:616-648) on
+    water / 6-31G: each spin block against the oracle, the host and device
+    entry points equal, and a closed shell (D_a = D_b = D / 2) giving the
+    restricted K of D in both blocks."""
+    _, b = _water()
+    n = b.nbf()
+    Du = _open_shell_density(n, 5, 4, seed=11)
+    dft = og.DFT("lda", b)
+    sgx = og.SemiNumericalExchange(dft, og.GridSettings.for_sgx(50))
+    Ku = sgx.compute_K(Du)
+    assert Ku.shape == (2 * n, n)
+    Ko = cx.cosx_exchange_unrestricted(b, Du, angular=50)
+    assert np.abs(Ku - Ko).max() < TOL_GPU * max(1.0, np.abs(Ko).max()), np.abs(Ku - Ko).max()
+    for s in (slice(0, n), slice(n, 2 * n)):
+        assert np.abs(Ku[s] - Ku[s].T).max() < 1e-14
+    import torch
+    dD = torch.tensor(np.asfortranarray(Du).ravel(order="F"), device="cuda", dtype=torch.float64)
+    dK = torch.empty(2 * n * n, device="cuda", dtype=torch.float64)
+    sgx.compute_K_device(dD.data_ptr(), dK.data_ptr(), torch.cuda.current_stream().cuda_stream,
+                         unrestricted=True)
+    torch.cuda.synchronize()
+    assert np.abs(dK.cpu().numpy().reshape(2 * n, n, order="F") - Ku).max() < 1e-13
+    D = 2.0 * Du[:n]
+    Kr = sgx.compute_K(D)
+    Kc = sgx.compute_K(np.vstack([0.5 * D, 0.5 * D]))
+    assert np.abs(Kc[:n] - Kr).max() < 1e-13 and np.abs(Kc[n:] - Kr).max() < 1e-13
+
+
+@pytest.mark.gpu
+def test_gpu_cosx_unrestricted_mixed_precision():
+    """The mixed precision on an unrestricted mo: both blocks within
+    TOL_K_MIXED of max |K| of the FP64 build."""
+    atoms1, _ = _water()
+    atoms2, _ = _water(shift=(0.0, 0.0, 5.5))
+    b = og.AOBasis.load(atoms1 + atoms2, "def2-svp")
+    b.set_pure(True)
+    Du = _open_shell_density(b.nbf(), 10, 9, seed=5)
+    dft = og.DFT("lda", b)
+    sgx = og.SemiNumericalExchange(dft, og.GridSettings.for_sgx(50))
+    K64 = sgx.compute_K(Du)
+    sgx.set_precision(og.MIXED)
+    Km = sgx.compute_K(Du)
+    rel = np.abs(Km - K64).max() / np.abs(K64).max()
+    assert rel <= TOL_K_MIXED, rel
