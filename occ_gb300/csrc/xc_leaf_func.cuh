@@ -144,14 +144,14 @@ __device__ __forceinline__ long long leaf_max_bits(long long v, long long *sh) {
 // rho >= 1e-10 and sigma >= 1e-30 (the
 // FP64 inputs are split by integer operations, fn::f2_bits;
 // eval_xc_mixed_f2; the FP64 evaluator elsewhere): the skip, weights and
-// coefficients of leaf_functional<.., MIXED>, the coefficients as FP32 into
-// cf[p] for p < npad (zero past the leaf's points; no FP64 coefficient
-// array), E and the electron count summed in double-float and written as
-// FP64 partials.  sh: NT / 32 eight-byte words.
-template <bool DERIV, int NT, int BAR>
+// coefficients of leaf_functional<.., MIXED>, the coefficients as FP32
+// handed to store(p, c) for p < npad (zero past the leaf's points), E and
+// the electron count summed in double-float and written as FP64 partials.
+// sh: NT / 32 eight-byte words.
+template <bool DERIV, int NT, int BAR, class Store>
 __device__ __forceinline__ void leaf_functional_f2(const DevLeaf &L, const Pt4 *__restrict__ pts,
                                                    size_t N, const FuncSet &fs, double thr,
-                                                   const double *__restrict__ rho, float4 *cf,
+                                                   const double *__restrict__ rho, Store store,
                                                    int npad, double *epart2, double *sh) {
   long long mb = -0x7fffffffffffffffLL - 1;
   for (int p = threadIdx.x; p < L.cnt; p += NT)
@@ -198,7 +198,7 @@ __device__ __forceinline__ void leaf_functional_f2(const DevLeaf &L, const Pt4 *
         ew = fn::f2_add(ew, fn::f2_mul(w, e));
       }
     }
-    cf[p] = c;
+    store(p, c);
   }
   float2 *shf = reinterpret_cast<float2 *>(sh);
   nel = leaf_sum_f2<NT, BAR>(nel, shf);

@@ -1648,6 +1648,7 @@ __global__ void __launch_bounds__(kFuncThreads, 4) k_func_b(const MixTab *__rest
 }
 
 constexpr int kLeafMaxPts = 1024; // leaf_max's bound (check_build_settings)
+constexpr int kYmixBatch = 4;     // ymix_stream: iterations whose loads are issued together
 
 // Y of one block from the coefficients cf[0 .. 127] (FP32) into the Y hi
 // plane as FP32 (k_vxc_tma splits it in shared memory), by the NS threads
@@ -1655,27 +1656,45 @@ constexpr int kLeafMaxPts = 1024; // leaf_max's bound (check_build_settings)
 template <bool DERIV, int NS>
 __device__ __forceinline__ void ymix_stream(const MixTab &T, const MBlock &B,
                                             const float4 *__restrict__ cf, int tid) {
-  float4 *__restrict__ base = reinterpret_cast<float4 *>(T.ws + B.ws_off);
+  // Every load of kYmixBatch iterations is issued before the first store:
+  // Y shares its base with the planes it is formed from, so the compiler
+  // would otherwise keep one iteration's loads in flight per thread, too few
+  // with the four CTAs an SM of the functional stage.
+  constexpr int U = kYmixBatch, NC = DERIV ? 4 : 1;
   const size_t plane = static_cast<size_t>(B.mp) * (kBlockPts / 4); // in float4
   const int n4 = B.mp * (kBlockPts / 4);
-#pragma unroll 4
-  for (int q = tid; q < n4; q += NS) {
-    const int p = (q % (kBlockPts / 4)) * 4;
-    const float4 a = base[q];
-    const float4 c0 = cf[p], c1 = cf[p + 1], c2 = cf[p + 2], c3 = cf[p + 3];
-    float4 y;
-    y.x = a.x * c0.x;
-    y.y = a.y * c1.x;
-    y.z = a.z * c2.x;
-    y.w = a.w * c3.x;
-    if (DERIV) {
-      const float4 gx = base[plane + q], gy = base[2 * plane + q], gz = base[3 * plane + q];
-      y.x = fmaf(gz.x, c0.w, fmaf(gy.x, c0.z, fmaf(gx.x, c0.y, y.x)));
-      y.y = fmaf(gz.y, c1.w, fmaf(gy.y, c1.z, fmaf(gx.y, c1.y, y.y)));
-      y.z = fmaf(gz.z, c2.w, fmaf(gy.z, c2.z, fmaf(gx.z, c2.y, y.z)));
-      y.w = fmaf(gz.w, c3.w, fmaf(gy.w, c3.z, fmaf(gx.w, c3.y, y.w)));
+  const float4 *__restrict__ src = reinterpret_cast<const float4 *>(T.ws + B.ws_off);
+  float4 *__restrict__ dst = reinterpret_cast<float4 *>(T.ws + B.ws_off) + kPlaneYHi * plane;
+  for (int q0 = tid; q0 < n4; q0 += NS * U) {
+    float4 v[U][NC];
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (q0 + u * NS < n4)
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+          v[u][c] = src[c * plane + q0 + u * NS];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * NS;
+      if (q >= n4)
+        break;
+      const int p = (q % (kBlockPts / 4)) * 4;
+      const float4 c0 = cf[p], c1 = cf[p + 1], c2 = cf[p + 2], c3 = cf[p + 3];
+      const float4 a = v[u][0];
+      float4 y;
+      y.x = a.x * c0.x;
+      y.y = a.y * c1.x;
+      y.z = a.z * c2.x;
+      y.w = a.w * c3.x;
+      if (DERIV) {
+        const float4 gx = v[u][DERIV ? 1 : 0], gy = v[u][DERIV ? 2 : 0], gz = v[u][DERIV ? 3 : 0];
+        y.x = fmaf(gz.x, c0.w, fmaf(gy.x, c0.z, fmaf(gx.x, c0.y, y.x)));
+        y.y = fmaf(gz.y, c1.w, fmaf(gy.y, c1.z, fmaf(gx.y, c1.y, y.y)));
+        y.z = fmaf(gz.z, c2.w, fmaf(gy.z, c2.z, fmaf(gx.z, c2.y, y.z)));
+        y.w = fmaf(gz.w, c3.w, fmaf(gy.w, c3.z, fmaf(gx.w, c3.y, y.w)));
+      }
+      dst[q] = y;
     }
-    base[kPlaneYHi * plane + q] = y;
   }
 }
 
@@ -1695,10 +1714,9 @@ __global__ void __launch_bounds__(kFuncThreads, 4) k_func_f2(const MixTab *__res
   const LeafItem li = litems[blockIdx.x];
   const MixTab &T = tabs[li.mol];
   const int nblk = min(li.nblk, kLeafMaxPts / kBlockPts);
-  leaf_functional_f2<DERIV, kFuncThreads, 0>(T.m.leaves[li.leaf], T.m.pts,
-                                             static_cast<size_t>(T.m.npts), T.fs, T.dens_thr,
-                                             T.rho, cf, nblk * kBlockPts, T.epart + 2 * li.leaf,
-                                             red);
+  leaf_functional_f2<DERIV, kFuncThreads, 0>(
+      T.m.leaves[li.leaf], T.m.pts, static_cast<size_t>(T.m.npts), T.fs, T.dens_thr, T.rho,
+      [&](int p, float4 c) { cf[p] = c; }, nblk * kBlockPts, T.epart + 2 * li.leaf, red);
   __syncthreads(); // cf is complete
   for (int q = 0; q < nblk; q++)
     ymix_stream<DERIV, kFuncThreads>(T, blocks[li.block0 + q], &cf[q * kBlockPts], threadIdx.x);
@@ -2022,7 +2040,8 @@ int num_sms(int device) {
   return n;
 }
 
-// The mixed launch sequence of a plan (7 kernels whatever the molecule count).
+// The mixed launch sequence of a plan (seven kernels whatever the molecule count,
+// and the collocation on a workspace's first build).
 void run_plan(LaunchPlan &P, Context &c, Override ov, int *err, cudaStream_t st, int max_ctas) {
   const int nmol = static_cast<int>(P.tabs.size());
   const int nb = static_cast<int>(P.blocks.size());
