@@ -1562,6 +1562,56 @@ __global__ void __launch_bounds__(kVxcThreads, 1)
     umma::tmem_dealloc(tmem, 512);
 }
 
+constexpr int kYmixBatch = 4; // ymix_stream: iterations whose loads are issued together
+
+// Y of one block from the coefficients cf[0 .. 127] (FP32) into the Y hi
+// plane as FP32 (k_vxc_tma splits it in shared memory), by the NS threads
+// tid = 0 .. NS - 1.
+template <bool DERIV>
+__device__ __forceinline__ void ymix_stream(const MixTab &T, const MBlock &B,
+                                            const float4 *__restrict__ cf, int tid, int NS) {
+  // Every load of kYmixBatch iterations is issued before the first store:
+  // Y shares its base with the planes it is formed from, so the compiler
+  // would otherwise keep one iteration's loads in flight per thread, too few
+  // with the four CTAs an SM of the functional stage.
+  constexpr int U = kYmixBatch, NC = DERIV ? 4 : 1;
+  const size_t plane = static_cast<size_t>(B.mp) * (kBlockPts / 4); // in float4
+  const int n4 = B.mp * (kBlockPts / 4);
+  const float4 *__restrict__ src = reinterpret_cast<const float4 *>(T.ws + B.ws_off);
+  float4 *__restrict__ dst = reinterpret_cast<float4 *>(T.ws + B.ws_off) + kPlaneYHi * plane;
+  for (int q0 = tid; q0 < n4; q0 += NS * U) {
+    float4 v[U][NC];
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (q0 + u * NS < n4)
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+          v[u][c] = src[c * plane + q0 + u * NS];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * NS;
+      if (q >= n4)
+        break;
+      const int p = (q % (kBlockPts / 4)) * 4;
+      const float4 c0 = cf[p], c1 = cf[p + 1], c2 = cf[p + 2], c3 = cf[p + 3];
+      const float4 a = v[u][0];
+      float4 y;
+      y.x = a.x * c0.x;
+      y.y = a.y * c1.x;
+      y.z = a.z * c2.x;
+      y.w = a.w * c3.x;
+      if (DERIV) {
+        const float4 gx = v[u][DERIV ? 1 : 0], gy = v[u][DERIV ? 2 : 0], gz = v[u][DERIV ? 3 : 0];
+        y.x = fmaf(gz.x, c0.w, fmaf(gy.x, c0.z, fmaf(gx.x, c0.y, y.x)));
+        y.y = fmaf(gz.y, c1.w, fmaf(gy.y, c1.z, fmaf(gx.y, c1.y, y.y)));
+        y.z = fmaf(gz.z, c2.w, fmaf(gy.z, c2.z, fmaf(gx.z, c2.y, y.z)));
+        y.w = fmaf(gz.w, c3.w, fmaf(gy.w, c3.z, fmaf(gx.w, c3.y, y.w)));
+      }
+      dst[q] = y;
+    }
+  }
+}
+
 // The B operand of k_vxc_tma for one block:
 // Y = 0.5 w vrho phi + 2 w vsigma grad rho . grad phi (FP32) into the Y plane
 // (split into TF32 hi / lo by k_vxc_tma); streams 4 planes in, 1 out.  Run by
@@ -1584,27 +1634,7 @@ __device__ __forceinline__ void ymix_block(const MixTab &T, const MBlock &B, flo
     cf[p] = c;
   }
   __syncthreads();
-  float4 *__restrict__ base = reinterpret_cast<float4 *>(T.ws + B.ws_off);
-  const size_t plane = static_cast<size_t>(B.mp) * (kBlockPts / 4); // in float4
-  const int n4 = B.mp * (kBlockPts / 4);
-#pragma unroll 2
-  for (int q = threadIdx.x; q < n4; q += blockDim.x) {
-    const int p = (q % (kBlockPts / 4)) * 4;
-    const float4 a = base[q];
-    float4 y;
-    y.x = a.x * cf[p].x;
-    y.y = a.y * cf[p + 1].x;
-    y.z = a.z * cf[p + 2].x;
-    y.w = a.w * cf[p + 3].x;
-    if (DERIV) {
-      const float4 gx = base[plane + q], gy = base[2 * plane + q], gz = base[3 * plane + q];
-      y.x = fmaf(gz.x, cf[p].w, fmaf(gy.x, cf[p].z, fmaf(gx.x, cf[p].y, y.x)));
-      y.y = fmaf(gz.y, cf[p + 1].w, fmaf(gy.y, cf[p + 1].z, fmaf(gx.y, cf[p + 1].y, y.y)));
-      y.z = fmaf(gz.z, cf[p + 2].w, fmaf(gy.z, cf[p + 2].z, fmaf(gx.z, cf[p + 2].y, y.z)));
-      y.w = fmaf(gz.w, cf[p + 3].w, fmaf(gy.w, cf[p + 3].z, fmaf(gx.w, cf[p + 3].y, y.w)));
-    }
-    base[kPlaneYHi * plane + q] = y;
-  }
+  ymix_stream<DERIV>(T, B, cf, threadIdx.x, blockDim.x);
   __syncthreads(); // cf is reused by the next block
 }
 
@@ -1648,55 +1678,6 @@ __global__ void __launch_bounds__(kFuncThreads, 4) k_func_b(const MixTab *__rest
 }
 
 constexpr int kLeafMaxPts = 1024; // leaf_max's bound (check_build_settings)
-constexpr int kYmixBatch = 4;     // ymix_stream: iterations whose loads are issued together
-
-// Y of one block from the coefficients cf[0 .. 127] (FP32) into the Y hi
-// plane as FP32 (k_vxc_tma splits it in shared memory), by the NS threads
-// tid = 0 .. NS - 1.
-template <bool DERIV, int NS>
-__device__ __forceinline__ void ymix_stream(const MixTab &T, const MBlock &B,
-                                            const float4 *__restrict__ cf, int tid) {
-  // Every load of kYmixBatch iterations is issued before the first store:
-  // Y shares its base with the planes it is formed from, so the compiler
-  // would otherwise keep one iteration's loads in flight per thread, too few
-  // with the four CTAs an SM of the functional stage.
-  constexpr int U = kYmixBatch, NC = DERIV ? 4 : 1;
-  const size_t plane = static_cast<size_t>(B.mp) * (kBlockPts / 4); // in float4
-  const int n4 = B.mp * (kBlockPts / 4);
-  const float4 *__restrict__ src = reinterpret_cast<const float4 *>(T.ws + B.ws_off);
-  float4 *__restrict__ dst = reinterpret_cast<float4 *>(T.ws + B.ws_off) + kPlaneYHi * plane;
-  for (int q0 = tid; q0 < n4; q0 += NS * U) {
-    float4 v[U][NC];
-#pragma unroll
-    for (int u = 0; u < U; u++)
-      if (q0 + u * NS < n4)
-#pragma unroll
-        for (int c = 0; c < NC; c++)
-          v[u][c] = src[c * plane + q0 + u * NS];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int q = q0 + u * NS;
-      if (q >= n4)
-        break;
-      const int p = (q % (kBlockPts / 4)) * 4;
-      const float4 c0 = cf[p], c1 = cf[p + 1], c2 = cf[p + 2], c3 = cf[p + 3];
-      const float4 a = v[u][0];
-      float4 y;
-      y.x = a.x * c0.x;
-      y.y = a.y * c1.x;
-      y.z = a.z * c2.x;
-      y.w = a.w * c3.x;
-      if (DERIV) {
-        const float4 gx = v[u][DERIV ? 1 : 0], gy = v[u][DERIV ? 2 : 0], gz = v[u][DERIV ? 3 : 0];
-        y.x = fmaf(gz.x, c0.w, fmaf(gy.x, c0.z, fmaf(gx.x, c0.y, y.x)));
-        y.y = fmaf(gz.y, c1.w, fmaf(gy.y, c1.z, fmaf(gx.y, c1.y, y.y)));
-        y.z = fmaf(gz.z, c2.w, fmaf(gy.z, c2.z, fmaf(gx.z, c2.y, y.z)));
-        y.w = fmaf(gz.w, c3.w, fmaf(gy.w, c3.z, fmaf(gx.w, c3.y, y.w)));
-      }
-      dst[q] = y;
-    }
-  }
-}
 
 // The build's functional stage (one CTA per leaf item, four per SM): the
 // functional in double-float arithmetic (leaf_functional_f2, no FP64
@@ -1719,7 +1700,8 @@ __global__ void __launch_bounds__(kFuncThreads, 4) k_func_f2(const MixTab *__res
       [&](int p, float4 c) { cf[p] = c; }, nblk * kBlockPts, T.epart + 2 * li.leaf, red);
   __syncthreads(); // cf is complete
   for (int q = 0; q < nblk; q++)
-    ymix_stream<DERIV, kFuncThreads>(T, blocks[li.block0 + q], &cf[q * kBlockPts], threadIdx.x);
+    ymix_stream<DERIV>(T, blocks[li.block0 + q], &cf[q * kBlockPts], threadIdx.x,
+                       kFuncThreads);
 }
 
 // Fixed-order FP64 sums of the per-leaf partials, one CTA per molecule.
@@ -3681,6 +3663,39 @@ __global__ void __launch_bounds__(kBlockPts) k_meta_ops(const MixTab *__restrict
   }
 }
 
+// The tau term's operands t_k = c_tau d_k phi (k = x, y, z) of one block into
+// the planes from kPlaneMetaT on, by the NS threads tid = 0 .. NS - 1; as in
+// ymix_stream the loads of kYmixBatch iterations go out before their stores.
+__device__ __forceinline__ void tau_stream(const MixTab &T, const MBlock &B,
+                                           const float *__restrict__ ct, int tid, int NS) {
+  constexpr int U = kYmixBatch;
+  const size_t plane = static_cast<size_t>(B.mp) * (kBlockPts / 4); // in float4
+  const int n4 = B.mp * (kBlockPts / 4);
+  const float4 *__restrict__ src = reinterpret_cast<const float4 *>(T.ws + B.ws_off);
+  float4 *__restrict__ dst = reinterpret_cast<float4 *>(T.ws + B.ws_off) + kPlaneMetaT * plane;
+  for (int q0 = tid; q0 < n4; q0 += NS * U) {
+    float4 v[U][3];
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (q0 + u * NS < n4)
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          v[u][k] = src[(k + 1) * plane + q0 + u * NS];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * NS;
+      if (q >= n4)
+        break;
+      const int p = (q % (kBlockPts / 4)) * 4;
+      const float c0 = ct[p], c1 = ct[p + 1], c2 = ct[p + 2], c3 = ct[p + 3];
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+        dst[k * plane + q] = make_float4(v[u][k].x * c0, v[u][k].y * c1, v[u][k].z * c2,
+                                         v[u][k].w * c3);
+    }
+  }
+}
+
 // The meta-GGA functional per leaf (eval_xc_mgga_mixed), then per block the GGA operand Y
 // (ymix_block) and the tau term's operands t_k = c_tau d_k phi, as FP32 planes.
 __global__ void __launch_bounds__(256, 2) k_func_b_mgga(const MixTab *__restrict__ tabs,
@@ -3704,15 +3719,7 @@ __global__ void __launch_bounds__(256, 2) k_func_b_mgga(const MixTab *__restrict
       ct[p] = p < B.cnt ? static_cast<float>(T.coef[4 * N + idx]) : 0.f;
     }
     __syncthreads();
-    float *base = T.ws + B.ws_off;
-    const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
-    const int n = B.mp * kBlockPts;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-      const float c = ct[q % kBlockPts];
-#pragma unroll
-      for (int k = 1; k <= 3; k++)
-        base[(kPlaneMetaT + k - 1) * plane + q] = base[k * plane + q] * c;
-    }
+    tau_stream(T, B, ct, threadIdx.x, blockDim.x);
     __syncthreads(); // ct is reused by the next block
   }
 }
@@ -3732,15 +3739,7 @@ __global__ void __launch_bounds__(256) k_ymix_mgga(const MixTab *__restrict__ ta
     ct[p] = p < B.cnt ? static_cast<float>(T.coef[4 * N + idx]) : 0.f;
   }
   ymix_block<true>(T, B, cf); // synchronises after filling cf (and so ct)
-  float *base = T.ws + B.ws_off;
-  const size_t plane = static_cast<size_t>(B.mp) * kBlockPts;
-  const int n = B.mp * kBlockPts;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const float c = ct[q % kBlockPts];
-#pragma unroll
-    for (int k = 1; k <= 3; k++)
-      base[(kPlaneMetaT + k - 1) * plane + q] = base[k * plane + q] * c;
-  }
+  tau_stream(T, B, ct, threadIdx.x, blockDim.x);
 }
 
 } // namespace
