@@ -95,6 +95,31 @@ def test_oracle_exchange_approaches_exact_exchange(angular, bar):
     assert err < bar, err
 
 
+def test_oracle_unrestricted_approaches_exact_exchange():
+    """The unrestricted oracle (seminumerical_exchange.cpp:616-648: per spin
+    0.5 (K' + K'^T) of Q (2 D_s), D_s = 0.5 C_s C_s^T as OCC stores it)
+    against each spin's exact exchange K_s = (ml|ns) (C_s C_s^T)_ls on water /
+    6-31G at for_sgx(50): 1.6e-4 of max |K_s| measured with these random
+    orbitals (the restricted RHF test: 6e-5), where a wrong spin factor would
+    be off by max |K_s| itself; and a closed shell (D_a = D_b = D / 2) giving
+    the restricted K in both blocks."""
+    b, D, _, _ = _rhf_water_631g()
+    n = b.nbf()
+    G = hf.eri(hf.ao_list(b))
+    rng = np.random.default_rng(3)
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+    Ca, Cb = Q[:, :5], Q[:, 1:5]
+    Du = np.vstack([0.5 * Ca @ Ca.T, 0.5 * Cb @ Cb.T])
+    Ku = cx.cosx_exchange_unrestricted(b, Du, angular=50)
+    for Cs, blk in ((Ca, Ku[:n]), (Cb, Ku[n:])):
+        Kx = np.einsum("ls,mlns->mn", Cs @ Cs.T, G)
+        rel = np.abs(blk - Kx).max() / np.abs(Kx).max()
+        assert rel < 2.5e-4, rel
+    Kc = cx.cosx_exchange_unrestricted(b, np.vstack([0.5 * D, 0.5 * D]), angular=50)
+    Kr = cx.cosx_exchange(b, D, angular=50)
+    assert np.abs(Kc[:n] - Kr).max() < 1e-13 and np.abs(Kc[n:] - Kr).max() < 1e-13
+
+
 def test_oracle_screens_act_on_separated_waters():
     """Two waters 7 Angstrom apart with a density that does not couple them
     (the screen relies on the decay of D): the geometric screen skips far
