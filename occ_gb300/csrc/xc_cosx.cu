@@ -54,8 +54,8 @@ constexpr int kCosxNc = 6;                     // Cartesian components of a d sh
 constexpr double kCosxDensityThreshold = 1e-6; // seminumerical_exchange.cpp:789
 constexpr double kCosxMargin = 1.0;            // cosx::Settings::margin (Bohr)
 constexpr int kCosxAoTile = 16;                // AOs lambda per block of the F and K kernels
-constexpr int kCosxTargetBlocks = 152 * 16;    // G kernel: blocks to aim for (16 per SM)
-constexpr int kCosxMaxSlices = 32;             // G kernel: most pair slices per leaf
+constexpr int kCosxTargetBlocks = 152 * 32;    // G kernel: blocks to aim for (32 per SM)
+constexpr int kCosxMaxSlices = 64;             // G kernel: most pair slices per leaf
 constexpr double kCosxLogThreshold = 27.631021115928547; // -ln(1e-12): pair extents
 constexpr double kCosxPairOverlap = 1e-12;     // IntegralEngine::compute_shellpairs
 constexpr double kPi = 3.14159265358979323846;
@@ -514,8 +514,8 @@ __device__ __forceinline__ void cosx_pair(const CxPair &P, const Prim *__restric
 // group's point, row stride ld); the slices of a leaf add into G by atomics.
 // In FP32 the bounds give 128 registers and four blocks per SM (a 144-byte
 // spill; faster than 168 registers and three blocks: 3.35 -> 2.72 ms a call
-// at 8 waters with 16 target blocks per SM, against 8); the FP64 form needs
-// the full register file.
+// at 8 waters with 16 target blocks per SM, against 8, and 2.53 ms with 32);
+// the FP64 form needs the full register file.
 template <typename Rt>
 __global__ void __launch_bounds__(128, sizeof(Rt) == 4 ? 4 : 1)
     k_cosx_g(MolDev m, int l0, int off0, int npairs, const CxPair *__restrict__ pairs,
