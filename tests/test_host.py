@@ -11,6 +11,7 @@ import pytest
 import occ_gb300 as og
 import oracle
 from occ_gb300 import workloads as wl
+from occ_gb300.xc import ERR_ARG
 from helpers import host_grid, water_case
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -24,6 +25,22 @@ def test_library_exports_every_declared_symbol():
     lib = og.library()
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_cosx_entry_points_refuse_null_arguments():
+    """The COSX entry points (restricted and unrestricted, host and device
+    buffers) return OCC_XC_ERR_ARG for missing handles or buffers before any
+    device work."""
+    lib = og.library()
+    four = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    for name in ("occ_xc_cosx_exchange", "occ_xc_cosx_exchange_unrestricted"):
+        fn = getattr(lib, name)
+        fn.argtypes = four
+        assert fn(None, None, None, None) == ERR_ARG
+    for name in ("occ_xc_cosx_exchange_device", "occ_xc_cosx_exchange_unrestricted_device"):
+        fn = getattr(lib, name)
+        fn.argtypes = four + [C.c_void_p]
+        assert fn(None, None, None, None, None) == ERR_ARG
 
 
 def test_normalised_shell_has_unit_self_overlap():
